@@ -1,0 +1,157 @@
+/*
+ * sesp.h - C ABI of the GB300 engine for the per-timestep force-and-integrate
+ * path of jhalverson/surfactant_enhanced_spreading (water / trisiloxane
+ * surfactant nanodroplets on graphite).
+ *
+ * The reference is a Fortran 90 + MPI program whose driver (src/mybox.f90)
+ * calls, every step, the velocity-Verlet first halves, the force section and
+ * the second halves.  Its subroutines take one integer (the rank) and move
+ * all data through COMMON blocks (src/mybox.cmns:207-259), so there is no
+ * binary interface to keep; this header is the boundary a Fortran driver
+ * binds through ISO_C_BINDING (include/sesp_mod.f90) and that the Python
+ * host layer binds through ctypes.  Each entry point names the reference
+ * call sequence it replaces.
+ *
+ * Conventions: every function returns 0 on success or a positive SESP_E*
+ * code; sesp_last_error() returns the message of the last failure of the
+ * calling thread.  State arrays are host-owned (n_sites, 3) row-major
+ * doubles in the reference's order (waters O,H,H first, then 29-site
+ * surfactants, src/read_config.f90:16-38) and reduced units (sigma = 3.166 A,
+ * epsilon = 650.2 J/mol, mass of O; velocities are displacements per step).
+ * The engine copies them to its own device state, which persists between
+ * calls.  Calls are synchronous unless named *_async.  One context is bound
+ * to one GPU; contexts are independent and may be used from different
+ * threads, one thread per context at a time.
+ */
+#ifndef SESP_H
+#define SESP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SESP_ABI_VERSION 1
+
+/* error codes */
+#define SESP_OK 0
+#define SESP_EINVAL 1      /* bad argument                                   */
+#define SESP_ECUDA 2       /* CUDA runtime failure                           */
+#define SESP_ENOMEM 3      /* device allocation failed                       */
+#define SESP_ESTATE 4      /* call out of order (e.g. step before upload)    */
+#define SESP_ECAPACITY 5   /* a cell or list exceeded its capacity           */
+#define SESP_ESHAKE 6      /* SHAKE/RATTLE did not converge (state is kept)  */
+#define SESP_EBUDGET 7     /* request exceeds the memory budget (serving)    */
+
+/* precision of the force path */
+#define SESP_PLAIN_FP64 0  /* every force term in FP64                       */
+#define SESP_MIXED 1       /* FP32 pair and local-expansion arithmetic with
+                              compensated per-site accumulation; FP64 for the
+                              constraints, thermostat, positions and sums     */
+
+/* force terms (bit mask for sesp_force_terms) */
+#define SESP_T_NEAR 1        /* short-range LJ + Coulomb, src/eval[wS]*.f90   */
+#define SESP_T_FAR 2         /* FMA local expansion, src/evalLjk4.f90         */
+#define SESP_T_VALENCE 4     /* src/eval_valence.f90                          */
+#define SESP_T_DIHEDRAL 8    /* src/eval_dihedral.f90                         */
+#define SESP_T_BERENDSEN 16  /* src/eval_dihedral_berendsen.f90               */
+#define SESP_T_INTERNAL 32   /* src/eval_surfactant_internal.f90              */
+#define SESP_T_SUBTRACT 64   /* src/eval_subtract_fma.f90                     */
+#define SESP_T_WALL 128      /* src/eval_wall.f90                             */
+#define SESP_T_GRAPHITE 256  /* src/eval_graphite.f90                         */
+#define SESP_T_ALL 511
+
+typedef struct sesp_ctx sesp_ctx;
+
+typedef struct {
+    int n_cells[3];        /* L4 cells per axis, multiples of 4; the reference
+                              uses 12 x 12 x 12 (3 x 3 x 3 ranks of 4^3 cells,
+                              src/mybox.cmns:55-57, src/init_box_dimensions.f90) */
+    int precision;         /* SESP_PLAIN_FP64 or SESP_MIXED                   */
+    int rebuild_interval;  /* steps between list / far-field rebuilds; ifar = 10
+                              (src/mybox.f90:24)                               */
+    int graphite_on;       /* apply src/eval_graphite.f90                     */
+    double tr;             /* thermostat target temperature, 3.81087
+                              (src/mybox.f90:48)                               */
+    double tau_steps;      /* thermostat relaxation time in steps, 7.5
+                              (src/mybox.f90:49)                               */
+    double shake_tol;      /* 1e-4 (src/move_w1_a.f90:19)                     */
+    int shake_maxit;       /* 100 (src/move_w1_a.f90:20)                      */
+    int device;            /* CUDA device ordinal                             */
+    int max_cell_sites;    /* capacity of one cell, 0 = default (1024)        */
+} sesp_params;
+
+/* library and error handling */
+int sesp_abi_version(void);
+int sesp_last_error(char *buf, size_t len);
+int sesp_default_params(sesp_params *p);
+
+/* lifecycle.  sesp_create allocates nothing that depends on the system size;
+ * sesp_upload_state sizes the device state for the system.
+ * Replaces: src/mybox.f90:19-60 (init_box_dimensions, init_arrays,
+ * read_config, read_graphite; velocities as given, init_temp is host side). */
+int sesp_create(const sesp_params *p, sesp_ctx **out);
+int sesp_destroy(sesp_ctx *ctx);
+int sesp_upload_state(sesp_ctx *ctx, int n_water, int n_surf, const double *pos, const double *vel,
+                      int n_carbon, const double *carbons);
+/* any of pos / vel / acc may be NULL */
+int sesp_download_state(sesp_ctx *ctx, double *pos, double *vel, double *acc);
+/* velocities and accelerations in, e.g. to resume a saved state */
+int sesp_set_state(sesp_ctx *ctx, const double *pos, const double *vel, const double *acc, double eta);
+
+/* the force section.  rebuild = 1 replaces src/mybox.f90:142-152 (molecule
+ * re-keying), :163-175 (list builders, multipoles and translations) and
+ * :183-223 (all force kernels); rebuild = 0 replaces src/mybox.f90:179-223
+ * (up_downSR_isr's intra-cell kernels, evalLjk4 and the 33 neighbour
+ * kernels) with the lists and local expansions frozen at the last rebuild. */
+int sesp_force(sesp_ctx *ctx, int rebuild);
+/* the same with only the terms in `terms` (SESP_T_* mask); for tests */
+int sesp_force_terms(sesp_ctx *ctx, int rebuild, int terms);
+int sesp_download_forces(sesp_ctx *ctx, double *f);
+
+/* src/init_accel.f90: a = F dt^2 / (2 m) after the first force call */
+int sesp_init_accel(sesp_ctx *ctx);
+/* move_surfactant_a, move_w1_a, move_w2_a (src/move_*_a.f90): Nose-Hoover
+ * scaled predictor, SHAKE, kinetic sums and the eta update of
+ * src/move_w2_a.f90:145-157 */
+int sesp_move_a(sesp_ctx *ctx);
+/* move_surfactant_b, move_w1_b, move_w2_b (src/move_*_b.f90): RATTLE */
+int sesp_move_b(sesp_ctx *ctx);
+
+/* one pass of the step loop body src/mybox.f90:136-227 for step number kb
+ * (rebuild when kb mod rebuild_interval == 0) */
+int sesp_step(sesp_ctx *ctx, int kb);
+/* nsteps passes starting at kb0, launched as captured CUDA graphs of
+ * rebuild_interval steps where possible */
+int sesp_run(sesp_ctx *ctx, int kb0, int nsteps);
+/* the same without waiting for completion; sesp_sync waits */
+int sesp_run_async(sesp_ctx *ctx, int kb0, int nsteps);
+int sesp_sync(sesp_ctx *ctx);
+
+/* diagnostics */
+int sesp_temperature(sesp_ctx *ctx, double *t);   /* src/compute_temperature.f90:240-242 */
+int sesp_get_eta(sesp_ctx *ctx, double *eta);
+int sesp_set_eta(sesp_ctx *ctx, double eta);
+/* energies (the reference computes none; these integrate its force laws):
+ * [0] near Coulomb, [1] near LJ, [2] far field incl. the intramolecular
+ * correction, [3] intramolecular pairs, [4] angles + dihedrals, [5] walls,
+ * [6] graphite, [7] kinetic */
+int sesp_energies(sesp_ctx *ctx, double out[8]);
+/* counts: [0] SHAKE/RATTLE non-convergences since upload, [1] capacity
+ * overflows, [2] sites in no cell, [3] steps done, [4] max sites in a cell,
+ * [5] near-field ordered pairs of the last rebuild, [6] LJ-eligible pairs */
+int sesp_counters(sesp_ctx *ctx, int64_t out[8]);
+/* average device time in ms per launch of each kernel family since the last
+ * reset, measured with CUDA events on the engine's stream:
+ * [0] near field, [1] local-expansion force, [2] move_a, [3] move_b,
+ * [4] intramolecular + external, [5] rebuild (sort + lists), [6] far-field build */
+int sesp_kernel_times(sesp_ctx *ctx, double out[8], int reset);
+int sesp_enable_timing(sesp_ctx *ctx, int on);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

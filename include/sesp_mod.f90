@@ -1,0 +1,150 @@
+! sesp_mod.f90 - ISO_C_BINDING interface to the GB300 engine (include/sesp.h)
+! for the reference's Fortran driver src/mybox.f90.  A driver that keeps
+! program mybox as the host replaces the force section and the move_*_a /
+! move_*_b calls with the bindings below (see the integration notes shipped
+! with the engine).  All arrays are (3, n_sites) real(c_double) in the
+! reference's site order and reduced units.
+module sesp_mod
+  use iso_c_binding
+  implicit none
+
+  integer(c_int), parameter :: SESP_PLAIN_FP64 = 0, SESP_MIXED = 1
+  integer(c_int), parameter :: SESP_T_ALL = 511
+
+  type, bind(C) :: sesp_params
+    integer(c_int) :: n_cells(3)
+    integer(c_int) :: precision
+    integer(c_int) :: rebuild_interval
+    integer(c_int) :: graphite_on
+    real(c_double) :: tr
+    real(c_double) :: tau_steps
+    real(c_double) :: shake_tol
+    integer(c_int) :: shake_maxit
+    integer(c_int) :: device
+    integer(c_int) :: max_cell_sites
+  end type sesp_params
+
+  interface
+    integer(c_int) function sesp_abi_version() bind(C, name="sesp_abi_version")
+      import :: c_int
+    end function
+    integer(c_int) function sesp_last_error(buf, len) bind(C, name="sesp_last_error")
+      import :: c_int, c_char, c_size_t
+      character(kind=c_char), intent(out) :: buf(*)
+      integer(c_size_t), value :: len
+    end function
+    integer(c_int) function sesp_default_params(p) bind(C, name="sesp_default_params")
+      import :: c_int, sesp_params
+      type(sesp_params), intent(out) :: p
+    end function
+    integer(c_int) function sesp_create(p, ctx) bind(C, name="sesp_create")
+      import :: c_int, c_ptr, sesp_params
+      type(sesp_params), intent(in) :: p
+      type(c_ptr), intent(out) :: ctx
+    end function
+    integer(c_int) function sesp_destroy(ctx) bind(C, name="sesp_destroy")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function sesp_upload_state(ctx, n_water, n_surf, pos, vel, n_carbon, carbons) &
+        bind(C, name="sesp_upload_state")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: n_water, n_surf, n_carbon
+      real(c_double), intent(in) :: pos(*), vel(*), carbons(*)
+    end function
+    integer(c_int) function sesp_download_state(ctx, pos, vel, acc) bind(C, name="sesp_download_state")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: pos(*), vel(*), acc(*)
+    end function
+    integer(c_int) function sesp_set_state(ctx, pos, vel, acc, eta) bind(C, name="sesp_set_state")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: pos(*), vel(*), acc(*)
+      real(c_double), value :: eta
+    end function
+    integer(c_int) function sesp_force(ctx, rebuild) bind(C, name="sesp_force")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: rebuild
+    end function
+    integer(c_int) function sesp_force_terms(ctx, rebuild, terms) bind(C, name="sesp_force_terms")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: rebuild, terms
+    end function
+    integer(c_int) function sesp_download_forces(ctx, f) bind(C, name="sesp_download_forces")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: f(*)
+    end function
+    integer(c_int) function sesp_init_accel(ctx) bind(C, name="sesp_init_accel")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function sesp_move_a(ctx) bind(C, name="sesp_move_a")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function sesp_move_b(ctx) bind(C, name="sesp_move_b")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function sesp_step(ctx, kb) bind(C, name="sesp_step")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: kb
+    end function
+    integer(c_int) function sesp_run(ctx, kb0, nsteps) bind(C, name="sesp_run")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: kb0, nsteps
+    end function
+    integer(c_int) function sesp_run_async(ctx, kb0, nsteps) bind(C, name="sesp_run_async")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: kb0, nsteps
+    end function
+    integer(c_int) function sesp_sync(ctx) bind(C, name="sesp_sync")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function sesp_temperature(ctx, t) bind(C, name="sesp_temperature")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: t
+    end function
+    integer(c_int) function sesp_get_eta(ctx, eta) bind(C, name="sesp_get_eta")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: eta
+    end function
+    integer(c_int) function sesp_set_eta(ctx, eta) bind(C, name="sesp_set_eta")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), value :: eta
+    end function
+    integer(c_int) function sesp_energies(ctx, e) bind(C, name="sesp_energies")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: e(8)
+    end function
+    integer(c_int) function sesp_counters(ctx, c) bind(C, name="sesp_counters")
+      import :: c_int, c_ptr, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int64_t), intent(out) :: c(8)
+    end function
+    integer(c_int) function sesp_kernel_times(ctx, t, reset) bind(C, name="sesp_kernel_times")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: t(8)
+      integer(c_int), value :: reset
+    end function
+    integer(c_int) function sesp_enable_timing(ctx, on) bind(C, name="sesp_enable_timing")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: on
+    end function
+  end interface
+end module sesp_mod

@@ -1,0 +1,317 @@
+// Kernels whose FP64 arithmetic must round exactly like the reference's:
+// cell assignment (the discrete ibox2 / ibox64 / isCentral decisions), the
+// intramolecular-correction lists, and the SHAKE / RATTLE velocity-Verlet
+// halves with the Nose-Hoover friction.  This translation unit is compiled
+// with -fmad=false so no multiply-add is contracted, as in the reference.
+#include "k_launch.cuh"
+
+namespace sesp {
+
+static __constant__ Tables cT;
+
+void upload_tables_exact(const Tables &t, cudaStream_t st) {
+    cudaMemcpyToSymbolAsync(cT, &t, sizeof(Tables), 0, cudaMemcpyHostToDevice, st);
+}
+
+// ibox2 - 1 along one axis, src/ibox.f90:300-312
+__device__ inline int rank_axis(const Rep &r, int a, double v) {
+    int k = (int)((v + r.rhs[a]) * r.nr[a] / r.rsd[a]);
+    return k < 0 ? 0 : (k >= r.nr[a] ? r.nr[a] - 1 : k);
+}
+// rcen2xtmp, src/init_box_dimensions.f90:40-42
+__device__ inline double rcen2_axis(const Rep &r, int a, int rk) {
+    double b = (double)r.nr[a];
+    return r.rsd[a] * (rk + 1) / b - r.rhs[a] - r.rsd[a] / b / 2.0;
+}
+// ibox64 along one axis relative to a rank centre, src/ibox.f90:345-359
+__device__ inline int local_axis(double v, double c2) {
+    int k = (int)((v - c2 + 2.0 * RS) / RS);
+    return k < 0 ? 0 : (k > 3 ? 3 : k);
+}
+// global key-cell coordinate along one axis (rank by ibox2, cell by ibox64)
+__device__ inline int key_axis(const Rep &r, int a, double v, int *rk) {
+    *rk = rank_axis(r, a, v);
+    return 4 * (*rk) + local_axis(v, rcen2_axis(r, a, *rk));
+}
+// isCentral along one axis (src/ibox.f90:274-297): the cell whose
+// [centre - rs/2, centre + rs/2) holds v, -1 if none
+__device__ inline int central_axis(const double *cen, int n, double v, double rhs) {
+    int k0 = (int)floor((v + rhs) / RS);
+    const double rs2 = RS / 2.0;
+    for (int k = k0 - 1; k <= k0 + 1; k++) {
+        if (k < 0 || k >= n) continue;
+        double c = cen[k];
+        if (v < c + rs2 && v >= c - rs2) return k;
+    }
+    return -1;
+}
+
+// Re-key molecules (src/read_config.f90:44-175 and the delete/add pairs
+// src/delete_w1.f90:54-195, src/delete_s.f90:33-43; key site O for water,
+// 14 for surfactants) and locate every site in the cell it is Central in.
+// A w1 water (all three sites in one rank and one ibox64 cell) has its
+// sites located in its key cell, as the reference stores it there.
+__global__ void k_locate(Dev d, int nmol) {
+    int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmol) return;
+    const Rep r = d.rep[d.mrep[m]];
+    int g0 = d.mfirst[m];
+    int kind = d.mkind[m];
+    int ks = kind == 0 ? g0 : g0 + 13;
+    double p[3] = {d.x[ks], d.y[ks], d.z[ks]};
+    int rk[3], kc[3];
+    for (int a = 0; a < 3; a++) kc[a] = key_axis(r, a, p[a], &rk[a]);
+    int key = cell_index(r, kc[0], kc[1], kc[2]);
+    d.mkey[m] = key;
+    int w1 = 0;
+    if (kind == 0) {
+        w1 = 1;
+        for (int t = 1; t < 3; t++) {
+            double q[3] = {d.x[g0 + t], d.y[g0 + t], d.z[g0 + t]};
+            for (int a = 0; a < 3; a++) {
+                if (rank_axis(r, a, q[a]) != rk[a]) w1 = 0;
+                else if (4 * rk[a] + local_axis(q[a], rcen2_axis(r, a, rk[a])) != kc[a]) w1 = 0;
+            }
+        }
+    }
+    d.mw1[m] = w1;
+    int ns = kind == 0 ? 3 : NSURF;
+    const double *cx = d.axis + r.axis0;
+    const double *cy = cx + r.nc[0];
+    const double *cz = cy + r.nc[1];
+    for (int t = 0; t < ns; t++) {
+        int g = g0 + t;
+        int loc;
+        if (w1) {
+            loc = key;
+        } else {
+            int ix = central_axis(cx, r.nc[0], d.x[g], r.rhs[0]);
+            int iy = central_axis(cy, r.nc[1], d.y[g], r.rhs[1]);
+            int iz = central_axis(cz, r.nc[2], d.z[g], r.rhs[2]);
+            loc = (ix < 0 || iy < 0 || iz < 0) ? -1 : cell_index(r, ix, iy, iz);
+        }
+        d.sloc[g] = loc;
+        if (loc >= 0) atomicAdd(&d.ccount[loc], 1);
+        else atomicAdd(&d.counters[2], 1ull);
+    }
+}
+
+// Sites of each surfactant that lie outside the 27-cell block of a site's
+// own cell (src/buildinternal.f90:71-121); cells on the 10^3 grid of the
+// key rank (ibox1000, rcen1000: src/ibox.f90:379-393,
+// src/init_box_dimensions.f90:155-170).  One thread per surfactant site.
+__global__ void k_isub(Dev d, int nsurf_sites, const int *surf_mol_of) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsurf_sites) return;
+    int m = surf_mol_of[t / NSURF];
+    int j = t % NSURF;
+    const Rep r = d.rep[d.mrep[m]];
+    int g0 = d.mfirst[m];
+    int key = d.mkey[m] - r.cell0;
+    int kc[3] = {key % r.nc[0], (key / r.nc[0]) % r.nc[1], key / (r.nc[0] * r.nc[1])};
+    double pm[3] = {d.x[g0 + j], d.y[g0 + j], d.z[g0 + j]};
+    double cen[3];
+    for (int a = 0; a < 3; a++) {
+        double c2 = rcen2_axis(r, a, kc[a] / 4);
+        int li = (int)((pm[a] - c2 + 5.0 * RS) / RS) + 1;
+        cen[a] = 10.0 * RS * li / 10.0 - 10.0 * RS / 2.0 - 10.0 * RS / 20.0 + c2;
+    }
+    const double r15 = 1.5 * RS;
+    uint32_t mask = 0;
+    for (int k = 0; k < NSURF; k++) {
+        if (k == j) continue;
+        double pk[3] = {d.x[g0 + k], d.y[g0 + k], d.z[g0 + k]};
+        bool near = true;
+        for (int a = 0; a < 3; a++) near = near && (pk[a] < cen[a] + r15 && pk[a] >= cen[a] - r15);
+        if (!near) mask |= (1u << k);
+    }
+    d.isub[t] = mask;
+}
+
+// ---------------------------------------------------------------- integrator
+
+template <int NSITE>
+struct MolTopo;
+
+template <>
+struct MolTopo<3> {
+    static constexpr int NB = 3;
+    __device__ static int bi(int b) { return b; }
+    __device__ static int bj(int b) { return b == 2 ? 0 : b + 1; }
+    __device__ static double dsq(int b) { return cT.dsqw[b]; }
+    __device__ static double mass(int i) { return cT.mass[i == 0 ? 0 : 1]; }
+};
+template <>
+struct MolTopo<NSURF> {
+    static constexpr int NB = NBOND;
+    __device__ static int bi(int b) { return cT.bi[b]; }
+    __device__ static int bj(int b) { return cT.bj[b]; }
+    __device__ static double dsq(int b) { return cT.dsqs[b]; }
+    __device__ static double mass(int i) { return cT.mass[2 + i]; }
+};
+
+// move_*_a for one molecule: Nose-Hoover scaled predictor, SHAKE
+// (src/move_w1_a.f90:36-134, src/move_surfactant_a.f90:36-134), and the
+// kinetic sums before and after (src/nh_water1.f90, src/nh_surfactant.f90)
+template <int NSITE>
+__global__ void k_move_a(Dev d, const int *mols, int nm, double tol, int maxit) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nm) return;
+    int m = mols[t];
+    int rep = d.mrep[m];
+    int g0 = d.mfirst[m];
+    double escale = 1.0 - d.eta[rep] * DT / 2.0;
+    double rx[NSITE], ry[NSITE], rz[NSITE], px[NSITE], py[NSITE], pz[NSITE], vx[NSITE], vy[NSITE], vz[NSITE];
+    double ke0 = 0.0;
+    for (int i = 0; i < NSITE; i++) {
+        int g = g0 + i;
+        double vxg = d.vx[g], vyg = d.vy[g], vzg = d.vz[g];
+        ke0 += MolTopo<NSITE>::mass(i) * (vxg * vxg + vyg * vyg + vzg * vzg);
+        rx[i] = d.x[g]; ry[i] = d.y[g]; rz[i] = d.z[g];
+        px[i] = d.x[g] + vxg * escale + d.ax[g];
+        py[i] = d.y[g] + vyg * escale + d.ay[g];
+        pz[i] = d.z[g] + vzg * escale + d.az[g];
+        vx[i] = vxg * escale + d.ax[g];
+        vy[i] = vyg * escale + d.ay[g];
+        vz[i] = vzg * escale + d.az[g];
+    }
+    const double tol2 = 2.0 * tol;
+    int it = 0;
+    bool ldone = false;
+    while (!ldone && it <= maxit) {
+        ldone = true;
+        for (int b = 0; b < MolTopo<NSITE>::NB; b++) {
+            int i = MolTopo<NSITE>::bi(b), j = MolTopo<NSITE>::bj(b);
+            double pxab = px[i] - px[j], pyab = py[i] - py[j], pzab = pz[i] - pz[j];
+            double pabsq = pxab * pxab + pyab * pyab + pzab * pzab;
+            double rabsq = MolTopo<NSITE>::dsq(b);
+            double diffsq = rabsq - pabsq;
+            if (fabs(diffsq) > rabsq * tol2) {
+                double rxab = rx[i] - rx[j], ryab = ry[i] - ry[j], rzab = rz[i] - rz[j];
+                double rpab = rxab * pxab + ryab * pyab + rzab * pzab;
+                double rma = 1.0 / MolTopo<NSITE>::mass(i), rmb = 1.0 / MolTopo<NSITE>::mass(j);
+                double gab = diffsq / (2.0 * (rma + rmb) * rpab);
+                double dx = rxab * gab, dy = ryab * gab, dz = rzab * gab;
+                px[i] = px[i] + rma * dx; py[i] = py[i] + rma * dy; pz[i] = pz[i] + rma * dz;
+                px[j] = px[j] - rmb * dx; py[j] = py[j] - rmb * dy; pz[j] = pz[j] - rmb * dz;
+                vx[i] = vx[i] + rma * dx; vy[i] = vy[i] + rma * dy; vz[i] = vz[i] + rma * dz;
+                vx[j] = vx[j] - rmb * dx; vy[j] = vy[j] - rmb * dy; vz[j] = vz[j] - rmb * dz;
+                ldone = false;
+            }
+        }
+        it++;
+    }
+    double ke1 = 0.0;
+    for (int i = 0; i < NSITE; i++) {
+        int g = g0 + i;
+        d.x[g] = px[i]; d.y[g] = py[i]; d.z[g] = pz[i];
+        d.vx[g] = vx[i]; d.vy[g] = vy[i]; d.vz[g] = vz[i];
+        ke1 += MolTopo<NSITE>::mass(i) * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+    }
+    d.ke[2 * m] = ke0;
+    d.ke[2 * m + 1] = ke1;
+    if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+}
+
+// eta update of src/move_w2_a.f90:145-157, one block per replica, fixed
+// summation order (thread-strided partial sums, then a tree)
+__global__ void k_eta(Dev d) {
+    const Rep r = d.rep[blockIdx.x];
+    __shared__ double s0[256], s1[256];
+    double a = 0.0, b = 0.0;
+    for (int m = r.mol0 + threadIdx.x; m < r.mol0 + r.nmol; m += blockDim.x) { a += d.ke[2 * m]; b += d.ke[2 * m + 1]; }
+    s0[threadIdx.x] = a; s1[threadIdx.x] = b;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) { s0[threadIdx.x] += s0[threadIdx.x + w]; s1[threadIdx.x] += s1[threadIdx.x + w]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double sum1 = s0[0] / (DT * DT), sum2 = s1[0] / (DT * DT);
+        d.eta[blockIdx.x] = d.eta[blockIdx.x] + r.pnh1 * (sum1 + r.pnh2 + sum2);
+    }
+}
+
+// move_*_b for one molecule: acceleration from force, friction, RATTLE
+// (src/move_w1_b.f90:30-119, src/move_surfactant_b.f90:30-118)
+template <int NSITE>
+__global__ void k_move_b(Dev d, const int *mols, int nm, double tol, int maxit) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nm) return;
+    int m = mols[t];
+    int rep = d.mrep[m];
+    int g0 = d.mfirst[m];
+    double escale = 2.0 / (2.0 + d.eta[rep] * DT);
+    double rx[NSITE], ry[NSITE], rz[NSITE], vx[NSITE], vy[NSITE], vz[NSITE];
+    for (int i = 0; i < NSITE; i++) {
+        int g = g0 + i;
+        double mi = MolTopo<NSITE>::mass(i);
+        rx[i] = d.x[g]; ry[i] = d.y[g]; rz[i] = d.z[g];
+        double axg = d.fx[g] * DTSQ2 / mi, ayg = d.fy[g] * DTSQ2 / mi, azg = d.fz[g] * DTSQ2 / mi;
+        d.ax[g] = axg; d.ay[g] = ayg; d.az[g] = azg;
+        vx[i] = escale * (d.vx[g] + axg);
+        vy[i] = escale * (d.vy[g] + ayg);
+        vz[i] = escale * (d.vz[g] + azg);
+    }
+    int it = 0;
+    bool ldone = false;
+    while (!ldone && it <= maxit) {
+        ldone = true;
+        for (int b = 0; b < MolTopo<NSITE>::NB; b++) {
+            int i = MolTopo<NSITE>::bi(b), j = MolTopo<NSITE>::bj(b);
+            double vxab = vx[i] - vx[j], vyab = vy[i] - vy[j], vzab = vz[i] - vz[j];
+            double rxab = rx[i] - rx[j], ryab = ry[i] - ry[j], rzab = rz[i] - rz[j];
+            double rvab = rxab * vxab + ryab * vyab + rzab * vzab;
+            rvab = rvab / DT;
+            double rma = 1.0 / MolTopo<NSITE>::mass(i), rmb = 1.0 / MolTopo<NSITE>::mass(j);
+            double gab = -rvab / ((rma + rmb) * MolTopo<NSITE>::dsq(b));
+            if (fabs(gab) > tol) {
+                double dx = rxab * gab, dy = ryab * gab, dz = rzab * gab;
+                vx[i] = vx[i] + rma * dx * DT; vy[i] = vy[i] + rma * dy * DT; vz[i] = vz[i] + rma * dz * DT;
+                vx[j] = vx[j] - rmb * dx * DT; vy[j] = vy[j] - rmb * dy * DT; vz[j] = vz[j] - rmb * dz * DT;
+                ldone = false;
+            }
+        }
+        it++;
+    }
+    for (int i = 0; i < NSITE; i++) {
+        int g = g0 + i;
+        d.vx[g] = vx[i]; d.vy[g] = vy[i]; d.vz[g] = vz[i];
+    }
+    if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+}
+
+// src/init_accel.f90:10-46
+__global__ void k_init_accel(Dev d, int nsite) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nsite) return;
+    double m = cT.mass[d.ptype[g]];
+    d.ax[g] = d.fx[g] * DTSQ2 / m;
+    d.ay[g] = d.fy[g] * DTSQ2 / m;
+    d.az[g] = d.fz[g] * DTSQ2 / m;
+}
+
+// ---------------------------------------------------------------- launchers
+
+void launch_locate(const Dev &d, int nmol, cudaStream_t st) {
+    k_locate<<<(nmol + 127) / 128, 128, 0, st>>>(d, nmol);
+}
+void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st) {
+    if (nsurf_sites) k_isub<<<(nsurf_sites + 127) / 128, 128, 0, st>>>(d, nsurf_sites, surf_mols);
+}
+void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
+                   cudaStream_t st) {
+    if (ns) k_move_a<NSURF><<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, tol, maxit);
+    if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+    k_eta<<<nrep, 256, 0, st>>>(d);
+}
+void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit,
+                   cudaStream_t st) {
+    if (ns) k_move_b<NSURF><<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, tol, maxit);
+    if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+}
+void launch_init_accel(const Dev &d, int nsite, cudaStream_t st) {
+    k_init_accel<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite);
+}
+
+}  // namespace sesp

@@ -1,0 +1,879 @@
+// Force kernels of the GB300 engine: cell sort, the full-shell short-range
+// pair kernel (FP64, or FP32 with compensated accumulation) with the local
+// expansion force fused into its epilogue, the order-4 multipole passes,
+// walls, graphite and the surfactant intramolecular terms.
+//
+// The reference splits its short-range work into 39 list kernels
+// (src/eval[wS]*.f90) over "Central" and "26" lists built every 10 steps
+// (src/build*.f90).  Together they give every site the Coulomb force of all
+// sites of other molecules that sit in the 27 cells around its own cell, plus
+// the LJ force within rc for the site kinds that carry LJ.  Here that rule is
+// one kernel: one CTA per cell, the 27 neighbour cells staged through shared
+// memory, each thread accumulating the full force on its own site (no
+// third-law scatter, no atomics, so results are bit-reproducible).
+#include "k_launch.cuh"
+
+namespace sesp {
+
+static __constant__ Tables cT;
+
+void upload_tables_force(const Tables &t, cudaStream_t st) {
+    cudaMemcpyToSymbolAsync(cT, &t, sizeof(Tables), 0, cudaMemcpyHostToDevice, st);
+}
+
+constexpr int NEAR_THREADS = 128;
+constexpr int SORT_CAP = 2048;
+
+__device__ inline void cell_xyz(const Rep &r, int c, int &ix, int &iy, int &iz) {
+    int l = c - r.cell0;
+    ix = l % r.nc[0];
+    iy = (l / r.nc[0]) % r.nc[1];
+    iz = l / (r.nc[0] * r.nc[1]);
+}
+
+// ------------------------------------------------------------------ sort
+
+__global__ void k_scan(Dev d, int ncell) {
+    __shared__ int part[1024];
+    int per = (ncell + blockDim.x - 1) / blockDim.x;
+    int b = threadIdx.x * per, e = min(ncell, b + per);
+    int s = 0;
+    for (int c = b; c < e; c++) s += d.ccount[c];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int t = 0; t < blockDim.x; t++) { int v = part[t]; part[t] = acc; acc += v; }
+        d.cstart[ncell] = acc;
+    }
+    __syncthreads();
+    int acc = part[threadIdx.x];
+    for (int c = b; c < e; c++) { d.cstart[c] = acc; acc += d.ccount[c]; d.cfill[c] = 0; }
+}
+
+__global__ void k_scatter(Dev d, int nsite) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nsite) return;
+    int c = d.sloc[g];
+    d.sslot[g] = -1;
+    if (c < 0) return;
+    int slot = d.cstart[c] + atomicAdd(&d.cfill[c], 1);
+    d.srt_site[slot] = g;
+}
+
+// order the sites of each cell by site index, so the slot order (and with it
+// every floating-point sum) is independent of the scatter's atomics
+__global__ void k_sort_cells(Dev d) {
+    __shared__ int buf[SORT_CAP];
+    int c = blockIdx.x;
+    int s0 = d.cstart[c], n = d.cstart[c + 1] - s0;
+    if (threadIdx.x == 0 && n > 0) atomicMax(&d.counters[3], (unsigned long long)n);
+    if (n > SORT_CAP) {
+        if (threadIdx.x == 0) atomicAdd(&d.counters[1], 1ull);
+        return;
+    }
+    for (int t = threadIdx.x; t < n; t += blockDim.x) buf[t] = d.srt_site[s0 + t];
+    __syncthreads();
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        int v = buf[t], rank = 0;
+        for (int u = 0; u < n; u++) rank += buf[u] < v;
+        d.srt_site[s0 + rank] = v;
+        d.sslot[v] = s0 + rank;
+        d.srt_meta[s0 + rank] = make_int2(d.smol[v], (int)d.ptype[v]);
+    }
+}
+
+void launch_sort(const Dev &d, int nsite, int ncell, cudaStream_t st) {
+    k_scan<<<1, 1024, 0, st>>>(d, ncell);
+    k_scatter<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite);
+    k_sort_cells<<<ncell, 256, 0, st>>>(d);
+}
+
+// ------------------------------------------------------------------ gather
+
+__device__ inline double cell_centre(const Dev &d, const Rep &r, int a, int i) {
+    const double *t = d.axis + r.axis0 + (a > 0 ? r.nc[0] : 0) + (a > 1 ? r.nc[1] : 0);
+    return t[i];
+}
+
+__global__ void k_gather(Dev d, int nslot, int ncell, int mixed) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslot || s >= d.cstart[ncell]) return;
+    int g = d.srt_site[s];
+    double x = d.x[g], y = d.y[g], z = d.z[g];
+    double q = cT.q[d.ptype[g]];
+    d.srt_pos[s] = make_double4(x, y, z, q);
+    if (mixed) {
+        int c = d.sloc[g];
+        const Rep r = d.rep[d.crep[c]];
+        int ix, iy, iz;
+        cell_xyz(r, c, ix, iy, iz);
+        d.srt_pos32[s] = make_float4((float)(x - cell_centre(d, r, 0, ix)), (float)(y - cell_centre(d, r, 1, iy)),
+                                     (float)(z - cell_centre(d, r, 2, iz)), (float)q);
+    }
+}
+
+void launch_gather(const Dev &d, int nslot, int ncell, int mixed, cudaStream_t st) {
+    if (nslot) k_gather<<<(nslot + 255) / 256, 256, 0, st>>>(d, nslot, ncell, mixed);
+}
+
+// ------------------------------------------------------------------ solid harmonics
+
+// T_n^m = r^n P_n^m(cos theta) e^{i m phi} (Condon-Shortley phase), m >= 0,
+// built by the Cartesian recurrences
+//   T_m^m = -(2m-1)(x+iy) T_{m-1}^{m-1},  T_{m+1}^m = (2m+1) z T_m^m,
+//   T_n^m = ((2n-1) z T_{n-1}^m - (n+m-1) r^2 T_{n-2}^m) / (n-m),
+// which avoid the angles and the 1/(x^2+y^2) of the reference's spherical
+// form (src/evalLjk4.f90:42-66) and so stay accurate next to the z axis.
+template <typename R>
+struct Cx {
+    R re, im;
+};
+template <typename R>
+__device__ inline Cx<R> cmul(Cx<R> a, Cx<R> b) { return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
+template <typename R>
+__device__ inline Cx<R> cscale(Cx<R> a, R s) { return {a.re * s, a.im * s}; }
+template <typename R>
+__device__ inline Cx<R> cadd(Cx<R> a, Cx<R> b) { return {a.re + b.re, a.im + b.im}; }
+template <typename R>
+__device__ inline Cx<R> csub(Cx<R> a, Cx<R> b) { return {a.re - b.re, a.im - b.im}; }
+
+// gradient of Phi = sum_n sum_m w_m rfctr(n,m) Re(L_n^m T_n^m) (w_0 = 1, w_m = 2):
+// the potential of the local expansion L (25 coefficients, m >= 0 used)
+template <typename R>
+__device__ inline void local_grad(const R *Lre, const R *Lim, R x, R y, R z, R &gx, R &gy, R &gz, R *phi) {
+    R r2 = x * x + y * y + z * z;
+    Cx<R> Tmm = {R(1), R(0)};
+    Cx<R> dmm[3] = {{R(0), R(0)}, {R(0), R(0)}, {R(0), R(0)}};
+    R ax = 0, ay = 0, az = 0, pp = 0;
+    Cx<R> xy = {x, y};
+    for (int m = 0; m <= P; m++) {
+        if (m > 0) {
+            R f = -(R)(2 * m - 1);
+            Cx<R> nT = cscale(cmul(xy, Tmm), f);
+            Cx<R> nd0 = cscale(cadd(Tmm, cmul(xy, dmm[0])), f);
+            Cx<R> nd1 = cscale(cadd(Cx<R>{-Tmm.im, Tmm.re}, cmul(xy, dmm[1])), f);
+            Cx<R> nd2 = cscale(cmul(xy, dmm[2]), f);
+            Tmm = nT; dmm[0] = nd0; dmm[1] = nd1; dmm[2] = nd2;
+        }
+        Cx<R> T2 = Tmm, T1 = {R(0), R(0)};
+        Cx<R> d2[3] = {dmm[0], dmm[1], dmm[2]};
+        Cx<R> d1[3] = {{R(0), R(0)}, {R(0), R(0)}, {R(0), R(0)}};
+        for (int n = m; n <= P; n++) {
+            Cx<R> Tn;
+            Cx<R> dn[3];
+            if (n == m) {
+                Tn = Tmm; dn[0] = dmm[0]; dn[1] = dmm[1]; dn[2] = dmm[2];
+            } else if (n == m + 1) {
+                R f = (R)(2 * m + 1);
+                Tn = cscale(Tmm, f * z);
+                dn[0] = cscale(dmm[0], f * z);
+                dn[1] = cscale(dmm[1], f * z);
+                dn[2] = cscale(cadd(Tmm, cscale(dmm[2], z)), f);
+            } else {
+                R a = (R)(2 * n - 1), b = (R)(n + m - 1), inv = R(1) / (R)(n - m);
+                Tn = cscale(csub(cscale(T1, a * z), cscale(T2, b * r2)), inv);
+                dn[0] = cscale(csub(cscale(d1[0], a * z), cadd(cscale(T2, b * 2 * x), cscale(d2[0], b * r2))), inv);
+                dn[1] = cscale(csub(cscale(d1[1], a * z), cadd(cscale(T2, b * 2 * y), cscale(d2[1], b * r2))), inv);
+                dn[2] = cscale(csub(cadd(cscale(T1, a), cscale(d1[2], a * z)), cadd(cscale(T2, b * 2 * z), cscale(d2[2], b * r2))), inv);
+            }
+            int ic = n * (n + 1) + m;
+            R w = (m == 0 ? R(1) : R(2)) * (R)cT.rfctr[ic];
+            R lr = Lre[ic], li = Lim[ic];
+            ax += w * (lr * dn[0].re - li * dn[0].im);
+            ay += w * (lr * dn[1].re - li * dn[1].im);
+            az += w * (lr * dn[2].re - li * dn[2].im);
+            pp += w * (lr * Tn.re - li * Tn.im);
+            if (n > m) { T2 = T1; d2[0] = d1[0]; d2[1] = d1[1]; d2[2] = d1[2]; }
+            T1 = Tn; d1[0] = dn[0]; d1[1] = dn[1]; d1[2] = dn[2];
+            if (n == m) { T2 = Tn; d2[0] = dn[0]; d2[1] = dn[1]; d2[2] = dn[2]; }
+        }
+    }
+    gx = ax; gy = ay; gz = az;
+    if (phi) *phi = pp;
+}
+
+// ------------------------------------------------------------------ near field
+
+template <bool MIXED>
+struct NearSmem;
+
+template <>
+struct NearSmem<false> {
+    double4 pos[NEAR_THREADS];
+    int2 meta[NEAR_THREADS];
+    double2 lj[NTYPE * NTYPE];
+    double Lre[LP], Lim[LP];
+};
+template <>
+struct NearSmem<true> {
+    float4 pos[NEAR_THREADS];
+    int2 meta[NEAR_THREADS];
+    float2 lj[NTYPE * NTYPE];
+    float Lre[LP], Lim[LP];
+};
+
+// One CTA per cell.  Thread t owns slot t of the cell (looping if the cell
+// holds more sites than threads); for each of the 27 neighbour cells the
+// sites are staged in shared memory and every thread sums its own site's
+// force over them.  Pair term (src/evalw1w1n.f90:86-104): qq / r^3 without
+// cutoff, plus 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2 for r <= rc; sites of the
+// same molecule are skipped (src/evalSS.f90:36).  MIXED: positions relative
+// to the target cell centre in FP32, FP32 pair arithmetic, each neighbour
+// cell's partial sum added into an FP64 accumulator.
+template <bool MIXED>
+__global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int terms) {
+    typedef typename std::conditional<MIXED, float, double>::type R;
+    __shared__ NearSmem<MIXED> sm;
+    const int c = blockIdx.x;
+    const int s0 = d.cstart[c];
+    const int ni = d.cstart[c + 1] - s0;
+    if (ni == 0) return;
+    const Rep r = d.rep[d.crep[c]];
+    int ix, iy, iz;
+    cell_xyz(r, c, ix, iy, iz);
+    const double cx = cell_centre(d, r, 0, ix), cy = cell_centre(d, r, 1, iy), cz = cell_centre(d, r, 2, iz);
+    for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) {
+        if (MIXED) {
+            double2 v = d.ljt[t];
+            ((float2 *)sm.lj)[t] = make_float2((float)v.x, (float)v.y);
+        } else {
+            ((double2 *)sm.lj)[t] = d.ljt[t];
+        }
+    }
+    if (threadIdx.x < LP) {
+        double2 v = d.L4[(size_t)c * LP + threadIdx.x];
+        sm.Lre[threadIdx.x] = (R)v.x;
+        sm.Lim[threadIdx.x] = (R)v.y;
+    }
+    __syncthreads();
+    const R rc2 = (R)(RC * RC);
+    const bool do_near = terms & SESP_T_NEAR;
+    const bool do_far = terms & SESP_T_FAR;
+    for (int ib = 0; ib < ni; ib += NEAR_THREADS) {
+        const int i = ib + threadIdx.x;
+        const bool act = i < ni;
+        R xi = 0, yi = 0, zi = 0, qi = 0;
+        int mi = -1, ti = 0;
+        double xd = 0, yd = 0, zd = 0;
+        if (act) {
+            double4 p = d.srt_pos[s0 + i];
+            int2 mt = d.srt_meta[s0 + i];
+            xd = p.x; yd = p.y; zd = p.z;
+            if (MIXED) {
+                float4 p32 = d.srt_pos32[s0 + i];
+                xi = p32.x; yi = p32.y; zi = p32.z;
+            } else {
+                xi = (R)p.x; yi = (R)p.y; zi = (R)p.z;
+            }
+            qi = (R)(p.w * XPI);
+            mi = mt.x; ti = mt.y;
+        }
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        if (do_near) {
+            for (int dzc = -1; dzc <= 1; dzc++)
+                for (int dyc = -1; dyc <= 1; dyc++)
+                    for (int dxc = -1; dxc <= 1; dxc++) {
+                        int jx = ix + dxc, jy = iy + dyc, jz = iz + dzc;
+                        if (jx < 0 || jy < 0 || jz < 0 || jx >= r.nc[0] || jy >= r.nc[1] || jz >= r.nc[2]) continue;
+                        int cn = cell_index(r, jx, jy, jz);
+                        int t0 = d.cstart[cn], nt = d.cstart[cn + 1] - t0;
+                        // offset of the neighbour cell's centre from this cell's (mixed)
+                        R ox = (R)(dxc * RS), oy = (R)(dyc * RS), oz = (R)(dzc * RS);
+                        R px = 0, py = 0, pz = 0;
+                        for (int jb = 0; jb < nt; jb += NEAR_THREADS) {
+                            __syncthreads();
+                            int jn = min(NEAR_THREADS, nt - jb);
+                            if (threadIdx.x < jn) {
+                                if (MIXED) {
+                                    float4 v = d.srt_pos32[t0 + jb + threadIdx.x];
+                                    ((float4 *)sm.pos)[threadIdx.x] = make_float4(v.x + (float)ox, v.y + (float)oy, v.z + (float)oz, v.w);
+                                } else {
+                                    ((double4 *)sm.pos)[threadIdx.x] = d.srt_pos[t0 + jb + threadIdx.x];
+                                }
+                                sm.meta[threadIdx.x] = d.srt_meta[t0 + jb + threadIdx.x];
+                            }
+                            __syncthreads();
+                            if (act) {
+                                const int trow = ti * NTYPE;
+#pragma unroll 4
+                                for (int j = 0; j < jn; j++) {
+                                    R xj, yj, zj, qj;
+                                    if (MIXED) {
+                                        float4 v = ((float4 *)sm.pos)[j];
+                                        xj = v.x; yj = v.y; zj = v.z; qj = v.w;
+                                    } else {
+                                        double4 v = ((double4 *)sm.pos)[j];
+                                        xj = v.x; yj = v.y; zj = v.z; qj = v.w;
+                                    }
+                                    int2 mt = sm.meta[j];
+                                    R dx = xi - xj, dy = yi - yj, dz = zi - zj;
+                                    R r2 = dx * dx + dy * dy + dz * dz;
+                                    bool same = mt.x == mi;
+                                    r2 = same ? R(1) : r2;
+                                    R qq = same ? R(0) : qi * qj;
+                                    R ir;
+                                    if (MIXED) ir = rsqrtf((float)r2); else ir = rsqrt((double)r2);
+                                    R ir2 = ir * ir;
+                                    R ft = qq * ir * ir2;
+                                    R lx, ly;
+                                    if (MIXED) { float2 v = ((float2 *)sm.lj)[trow + mt.y]; lx = v.x; ly = v.y; }
+                                    else { double2 v = ((double2 *)sm.lj)[trow + mt.y]; lx = v.x; ly = v.y; }
+                                    R on = (r2 <= rc2 && !same) ? lx : R(0);
+                                    R r6 = ir2 * ir2 * ir2;
+                                    ft += on * r6 * (ly * r6 - R(0.5)) * ir2;
+                                    px += dx * ft; py += dy * ft; pz += dz * ft;
+                                }
+                            }
+                        }
+                        fx += (double)px; fy += (double)py; fz += (double)pz;
+                    }
+        }
+        if (act && do_far) {
+            R gx, gy, gz;
+            if (MIXED) {
+                local_grad<R>(sm.Lre, sm.Lim, xi, yi, zi, gx, gy, gz, nullptr);
+            } else {
+                local_grad<R>(sm.Lre, sm.Lim, (R)(xd - cx), (R)(yd - cy), (R)(zd - cz), gx, gy, gz, nullptr);
+            }
+            fx -= (double)(qi * gx); fy -= (double)(qi * gy); fz -= (double)(qi * gz);
+        }
+        if (act) {
+            size_t o = 3 * (size_t)(s0 + i);
+            d.nf[o] = fx; d.nf[o + 1] = fy; d.nf[o + 2] = fz;
+        }
+    }
+}
+
+void launch_near(const Dev &d, int ncell, int mixed, int terms, cudaStream_t st) {
+    if (mixed) k_near<true><<<ncell, NEAR_THREADS, 0, st>>>(d, terms);
+    else k_near<false><<<ncell, NEAR_THREADS, 0, st>>>(d, terms);
+}
+
+// ------------------------------------------------------------------ multipoles
+
+// P2M, src/computeOnm4.f90:142-162: O_n^m = sum_sites q rho^n Y(n,-m)
+//                                          = sum q rfctr(n,m) conj(T_n^m)
+__global__ void k_p2m(Dev d) {
+    const int c = blockIdx.x;
+    const int s0 = d.cstart[c], n = d.cstart[c + 1] - s0;
+    const Rep r = d.rep[d.crep[c]];
+    int ix, iy, iz;
+    cell_xyz(r, c, ix, iy, iz);
+    const double cx = cell_centre(d, r, 0, ix), cy = cell_centre(d, r, 1, iy), cz = cell_centre(d, r, 2, iz);
+    double acc[2 * LPH];
+    for (int k = 0; k < 2 * LPH; k++) acc[k] = 0.0;
+    for (int s = threadIdx.x; s < n; s += blockDim.x) {
+        double4 p = d.srt_pos[s0 + s];
+        double x = p.x - cx, y = p.y - cy, z = p.z - cz, q = p.w;
+        double r2 = x * x + y * y + z * z;
+        Cx<double> Tmm = {1.0, 0.0};
+        Cx<double> xy = {x, y};
+        int o = 0;
+        for (int m = 0; m <= P; m++) {
+            if (m > 0) Tmm = cscale(cmul(xy, Tmm), -(double)(2 * m - 1));
+            Cx<double> T2 = Tmm, T1 = Tmm;
+            for (int nn = m; nn <= P; nn++) {
+                Cx<double> Tn;
+                if (nn == m) Tn = Tmm;
+                else if (nn == m + 1) Tn = cscale(Tmm, (double)(2 * m + 1) * z);
+                else Tn = cscale(csub(cscale(T1, (double)(2 * nn - 1) * z), cscale(T2, (double)(nn + m - 1) * r2)), 1.0 / (double)(nn - m));
+                if (nn > m) T2 = T1;
+                T1 = Tn;
+                int ic = nn * (nn + 1) + m;
+                double w = q * cT.rfctr[ic];
+                // ordering index among m >= 0 coefficients: o(n,m) = n(n+1)/2 + m
+                int oi = nn * (nn + 1) / 2 + m;
+                acc[2 * oi] += w * Tn.re;
+                acc[2 * oi + 1] -= w * Tn.im;
+                o++;
+            }
+        }
+    }
+    __shared__ double red[2 * LPH][64];
+    for (int k = 0; k < 2 * LPH; k++) red[k][threadIdx.x] = acc[k];
+    __syncthreads();
+    if (threadIdx.x < 2 * LPH) {
+        double s = 0.0;
+        for (int t = 0; t < blockDim.x; t++) s += red[threadIdx.x][t];
+        red[threadIdx.x][0] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < LPH) {
+        int oi = threadIdx.x;
+        int nn = 0;
+        while ((nn + 1) * (nn + 2) / 2 <= oi) nn++;
+        int m = oi - nn * (nn + 1) / 2;
+        double re = red[2 * oi][0], im = red[2 * oi + 1][0];
+        double2 *O = d.O4 + (size_t)c * LP;
+        O[nn * (nn + 1) + m] = make_double2(re, im);
+        if (m > 0) O[nn * (nn + 1) - m] = make_double2(re, -im);
+    }
+}
+
+// output coefficient (j, k >= 0) of thread o (0..14)
+__device__ inline void out_jk(int o, int &j, int &k) {
+    j = 0;
+    while ((j + 1) * (j + 2) / 2 <= o) j++;
+    k = o - j * (j + 1) / 2;
+}
+
+__device__ inline void apply_op(const double2 *op, const double2 *in, double &re, double &im) {
+    for (int c = 0; c < LP; c++) {
+        double2 a = op[c], b = in[c];
+        re += a.x * b.x - a.y * b.y;
+        im += a.x * b.y + a.y * b.x;
+    }
+}
+
+__device__ inline void store_jk(double2 *L, int o, double re, double im, bool add) {
+    int j, k;
+    out_jk(o, j, k);
+    double2 v = add ? L[j * (j + 1) + k] : make_double2(0.0, 0.0);
+    v.x += re; v.y += im;
+    L[j * (j + 1) + k] = v;
+    if (k > 0) L[j * (j + 1) - k] = make_double2(v.x, -v.y);
+}
+
+// M2M, src/computeOnm3.f90:173-244 and src/computeOnm2.f90:13-62: parent box
+// from its 8 children (level 4 -> 3 or 3 -> 2)
+__global__ void k_m2m(Dev d, const double2 *Oc, double2 *Op, const double2 *ops, const int *brep, int level) {
+    const int b = blockIdx.x;
+    const Rep r = d.rep[brep[b]];
+    const int div = level == 3 ? 2 : 4;   // parent grid = nc / div
+    const int base_p = level == 3 ? r.l3_0 : r.l2_0;
+    const int base_c = level == 3 ? r.cell0 : r.l3_0;
+    const int np[3] = {r.nc[0] / div, r.nc[1] / div, r.nc[2] / div};
+    const int nc[3] = {np[0] * 2, np[1] * 2, np[2] * 2};
+    int l = b - base_p;
+    int px = l % np[0], py = (l / np[0]) % np[1], pz = l / (np[0] * np[1]);
+    int o = threadIdx.x;
+    if (o >= LPH) return;
+    double re = 0.0, im = 0.0;
+    for (int ch = 0; ch < 8; ch++) {
+        int cx = 2 * px + (ch & 1), cy = 2 * py + ((ch >> 1) & 1), cz = 2 * pz + ((ch >> 2) & 1);
+        int ci = base_c + cx + nc[0] * (cy + nc[1] * cz);
+        apply_op(ops + ((size_t)ch * LPH + o) * LP, Oc + (size_t)ci * LP, re, im);
+    }
+    store_jk(Op + (size_t)b * LP, o, re, im, false);
+}
+
+// L2L, src/shiftLjk2.f90:89-135 and src/shiftLjk3.f90:154-229: child box
+// from its parent (level 2 -> 3 or 3 -> 4)
+__global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const double2 *ops, const int *brep, int level) {
+    const int b = blockIdx.x;
+    const Rep r = d.rep[brep[b]];
+    const int div = level == 3 ? 2 : 1;  // child grid = nc / div
+    const int base_c = level == 3 ? r.l3_0 : r.cell0;
+    const int base_p = level == 3 ? r.l2_0 : r.l3_0;
+    const int nc[3] = {r.nc[0] / div, r.nc[1] / div, r.nc[2] / div};
+    const int np[3] = {nc[0] / 2, nc[1] / 2, nc[2] / 2};
+    int l = b - base_c;
+    int cx = l % nc[0], cy = (l / nc[0]) % nc[1], cz = l / (nc[0] * nc[1]);
+    int ch = (cx & 1) + 2 * (cy & 1) + 4 * (cz & 1);
+    int pi = base_p + cx / 2 + np[0] * (cy / 2 + np[1] * (cz / 2));
+    int o = threadIdx.x;
+    if (o >= LPH) return;
+    double re = 0.0, im = 0.0;
+    apply_op(ops + ((size_t)ch * LPH + o) * LP, Lp + (size_t)pi * LP, re, im);
+    store_jk(Lc + (size_t)b * LP, o, re, im, false);
+}
+
+// M2L over the 6^3 window of the parent's neighbours' children minus the 27
+// adjacent boxes (src/computeLjk4.f90:114-168, src/computeLjk3.f90:220-277).
+// 120 threads: 15 output coefficients x 8 source groups, reduced in a fixed order.
+__global__ void k_m2l_win(Dev d, const double2 *O, double2 *L, const double2 *ops, const int *brep, int level) {
+    const int b = blockIdx.x;
+    const Rep r = d.rep[brep[b]];
+    const int div = level == 4 ? 1 : 2;
+    const int base = level == 4 ? r.cell0 : r.l3_0;
+    const int n[3] = {r.nc[0] / div, r.nc[1] / div, r.nc[2] / div};
+    int l = b - base;
+    int t[3] = {l % n[0], (l / n[0]) % n[1], l / (n[0] * n[1])};
+    int o = threadIdx.x % LPH, g = threadIdx.x / LPH;
+    double re = 0.0, im = 0.0;
+    int k = 0;
+    for (int sz = 2 * (t[2] / 2) - 2; sz <= 2 * (t[2] / 2) + 3; sz++)
+        for (int sy = 2 * (t[1] / 2) - 2; sy <= 2 * (t[1] / 2) + 3; sy++)
+            for (int sx = 2 * (t[0] / 2) - 2; sx <= 2 * (t[0] / 2) + 3; sx++) {
+                int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
+                if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+                if (sx < 0 || sy < 0 || sz < 0 || sx >= n[0] || sy >= n[1] || sz >= n[2]) continue;
+                if ((k++ & 7) != g) continue;
+                int oi = (dx + 3) + 7 * (dy + 3) + 49 * (dz + 3);
+                apply_op(ops + ((size_t)oi * LPH + o) * LP, O + (size_t)(base + sx + n[0] * (sy + n[1] * sz)) * LP, re, im);
+            }
+    __shared__ double sre[8][LPH], sim[8][LPH];
+    sre[g][o] = re; sim[g][o] = im;
+    __syncthreads();
+    if (g == 0) {
+        double a = 0.0, c = 0.0;
+        for (int q = 0; q < 8; q++) { a += sre[q][o]; c += sim[q][o]; }
+        store_jk(L + (size_t)b * LP, o, a, c, true);
+    }
+}
+
+// M2L at L2 over all non-adjacent L2 boxes of the replica (src/computeLjk2.f90:17-72)
+__global__ void k_m2l_l2(Dev d, int d2) {
+    const int b = blockIdx.x;
+    const Rep r = d.rep[d.b2rep[b]];
+    const int *n = r.nr;
+    int l = b - r.l2_0;
+    int t[3] = {l % n[0], (l / n[0]) % n[1], l / (n[0] * n[1])};
+    int o = threadIdx.x;
+    if (o >= LPH) return;
+    double re = 0.0, im = 0.0;
+    int w = 2 * d2 + 1;
+    for (int sz = 0; sz < n[2]; sz++)
+        for (int sy = 0; sy < n[1]; sy++)
+            for (int sx = 0; sx < n[0]; sx++) {
+                int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
+                if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+                int oi = (dx + d2) + w * ((dy + d2) + w * (dz + d2));
+                apply_op(d.op_m2l2 + ((size_t)oi * LPH + o) * LP, d.O2 + (size_t)(r.l2_0 + sx + n[0] * (sy + n[1] * sz)) * LP, re, im);
+            }
+    store_jk(d.L2 + (size_t)b * LP, o, re, im, false);
+}
+
+void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int nrep, int d2, cudaStream_t st) {
+    (void)nrep;
+    k_p2m<<<ncell, 64, 0, st>>>(d);
+    k_m2m<<<n3, 32, 0, st>>>(d, d.O4, d.O3, d.op_m2m43, d.b3rep, 3);
+    k_m2m<<<n2, 32, 0, st>>>(d, d.O3, d.O2, d.op_m2m32, d.b2rep, 2);
+    k_m2l_l2<<<n2, 32, 0, st>>>(d, d2);
+    k_l2l<<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
+    k_m2l_win<<<n3, 8 * LPH, 0, st>>>(d, d.O3, d.L3, d.op_m2l3, d.b3rep, 3);
+    k_l2l<<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
+    k_m2l_win<<<ncell, 8 * LPH, 0, st>>>(d, d.O4, d.L4, d.op_m2l4, d.crep, 4);
+}
+
+// ------------------------------------------------------------------ per-site terms
+
+__device__ inline double pow13(double v) { double v2 = v * v, v4 = v2 * v2, v8 = v4 * v4; return v8 * v4 * v; }
+__device__ inline double pow12(double v) { double v2 = v * v, v4 = v2 * v2, v8 = v4 * v4; return v8 * v4; }
+
+// graphite LJ of one site over its column's carbons (src/eval_graphite.f90:80-185)
+__device__ inline void graphite_site(const Dev &d, int col, double x, double y, double z, double eps, double sg6,
+                                     double &fx, double &fy, double &fz, double *e) {
+    const double rc2 = RC * RC;
+    for (int k = d.gcol_start[col]; k < d.gcol_start[col + 1]; k++) {
+        double4 c = d.gpos[k];
+        double xij = x - c.x, yij = y - c.y, zij = z - c.z;
+        double r2 = xij * xij + yij * yij + zij * zij;
+        if (r2 <= rc2) {
+            double rsi = 1.0 / r2, r6 = rsi * rsi * rsi;
+            double flj = 48.0 * eps * sg6 * r6 * (sg6 * r6 - 0.5) * rsi;
+            fx += xij * flj; fy += yij * flj; fz += zij * flj;
+            if (e) *e += 4.0 * eps * (sg6 * sg6 * r6 * r6 - sg6 * r6);
+        }
+    }
+}
+
+// graphite acts on LJ sites that sit in their molecule's key cell in the
+// bottom layer of cells: water O (w1 and split) and surfactant sites in
+// SCentral (src/eval_graphite.f90:72-187)
+__device__ inline int graphite_column(const Dev &d, const Rep &r, int g, double &eps, double &sg6) {
+    if (!r.graphite_on) return -1;
+    int pt = d.ptype[g];
+    if (pt == 1) return -1;
+    int loc = d.sloc[g];
+    if (loc < 0 || loc != d.mkey[d.smol[g]]) return -1;
+    int ix, iy, iz;
+    cell_xyz(r, loc, ix, iy, iz);
+    if (iz != 0) return -1;
+    if (pt == 0) { eps = cT.epcw; sg6 = cT.sgcw6; } else { eps = cT.epcs[pt - 2]; sg6 = cT.sgcs6[pt - 2]; }
+    return r.gcol0 + ix + r.nc[0] * iy;
+}
+
+__global__ void k_site_forces(Dev d, int nsite, int terms) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nsite) return;
+    const Rep r = d.rep[d.mrep[d.smol[g]]];
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    int slot = d.sslot[g];
+    if ((terms & (SESP_T_NEAR | SESP_T_FAR)) && slot >= 0) {
+        fx = d.nf[3 * (size_t)slot]; fy = d.nf[3 * (size_t)slot + 1]; fz = d.nf[3 * (size_t)slot + 2];
+    }
+    double x = d.x[g], y = d.y[g], z = d.z[g];
+    if (terms & SESP_T_WALL) {  // src/eval_wall.f90:17-23
+        fx += 48.0 / pow13(x - r.rhs[0]); fx += 48.0 / pow13(r.rhs[0] + x);
+        fy += 48.0 / pow13(y - r.rhs[1]); fy += 48.0 / pow13(r.rhs[1] + y);
+        fz += 48.0 / pow13(z - r.rhs[2]); fz += 48.0 / pow13(r.rhs[2] + z);
+    }
+    if (terms & SESP_T_GRAPHITE) {
+        double eps, sg6;
+        int col = graphite_column(d, r, g, eps, sg6);
+        if (col >= 0) graphite_site(d, col, x, y, z, eps, sg6, fx, fy, fz, nullptr);
+    }
+    d.fx[g] = fx; d.fy[g] = fy; d.fz[g] = fz;
+}
+
+void launch_site_forces(const Dev &d, int nsite, int terms, cudaStream_t st) {
+    k_site_forces<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
+}
+
+// ------------------------------------------------------------------ surfactant intramolecular
+
+struct Mol29 {
+    double x[NSURF], y[NSURF], z[NSURF];
+    double fx[NSURF], fy[NSURF], fz[NSURF];
+};
+
+// src/eval_valence.f90:104-145
+__device__ double valence(Mol29 &m, bool force) {
+    double e = 0.0;
+    for (int i = 0; i < NANGLE; i++) {
+        int a = cT.ai[i], b = cT.aj[i], c = cT.ak[i];
+        double rxji = m.x[a] - m.x[b], ryji = m.y[a] - m.y[b], rzji = m.z[a] - m.z[b];
+        double rxki = m.x[c] - m.x[b], ryki = m.y[c] - m.y[b], rzki = m.z[c] - m.z[b];
+        double dp = rxji * rxki + ryji * ryki + rzji * rzki;
+        double rjin = sqrt(rxji * rxji + ryji * ryji + rzji * rzji);
+        double rkin = sqrt(rxki * rxki + ryki * ryki + rzki * rzki);
+        double th = acos(dp / rjin / rkin);
+        double costh = cos(th);
+        double dth = th - cT.th[i];
+        e += 0.5 * cT.rkth[i] * dth * dth;
+        if (!force) continue;
+        double r1 = cT.rkth[i] * dth / sin(th);
+        double fjx = rxki / rjin / rkin - costh * rxji / (rjin * rjin);
+        double fjy = ryki / rjin / rkin - costh * ryji / (rjin * rjin);
+        double fjz = rzki / rjin / rkin - costh * rzji / (rjin * rjin);
+        double fkx = rxji / rjin / rkin - costh * rxki / (rkin * rkin);
+        double fky = ryji / rjin / rkin - costh * ryki / (rkin * rkin);
+        double fkz = rzji / rjin / rkin - costh * rzki / (rkin * rkin);
+        m.fx[a] += r1 * fjx; m.fy[a] += r1 * fjy; m.fz[a] += r1 * fjz;
+        m.fx[b] -= r1 * (fjx + fkx); m.fy[b] -= r1 * (fjy + fky); m.fz[b] -= r1 * (fjz + fkz);
+        m.fx[c] += r1 * fkx; m.fy[c] += r1 * fky; m.fz[c] += r1 * fkz;
+    }
+    return e;
+}
+
+// dihedral force on the four sites from r1 = -dU/dcos(phi), written with the
+// same cross-product algebra as src/eval_dihedral.f90:116-271
+__device__ double dihedral(Mol29 &m, int i0, int i1, bool berendsen, bool force) {
+    double e = 0.0;
+    const double clampv = berendsen ? 0.999999 : 0.99999999999;
+    for (int i = i0; i < i1; i++) {
+        int iv = cT.di[i], jv = cT.dj[i], kv = cT.dk[i], lv = cT.dl[i];
+        double ax = m.x[jv] - m.x[iv], ay = m.y[jv] - m.y[iv], az = m.z[jv] - m.z[iv];   // r_ji
+        double bx = m.x[kv] - m.x[jv], by = m.y[kv] - m.y[jv], bz = m.z[kv] - m.z[jv];   // r_kj
+        double cx = m.x[lv] - m.x[kv], cy = m.y[lv] - m.y[kv], cz = m.z[lv] - m.z[kv];   // r_nk
+        double u1 = ax * by - ay * bx, u2 = ax * bz - az * bx, u3 = ay * bz - az * by;
+        double v1 = bx * cy - by * cx, v2 = bx * cz - bz * cx, v3 = by * cz - bz * cy;
+        double nu = sqrt(u1 * u1 + u2 * u2 + u3 * u3), nv = sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+        double arg = (u1 * v1 + u2 * v2 + u3 * v3) / nu / nv;
+        if (arg <= -1.0) arg = -clampv;
+        if (arg >= 1.0) arg = clampv;
+        double th = acos(arg), costh = cos(th), sinth = sin(th);
+        double r1;
+        if (berendsen) {
+            r1 = -3.0 * cT.dva[i] * sin(3.0 * th) / sinth;
+            e += cT.dva[i] * (1.0 + cos(3.0 * th));
+        } else {
+            r1 = -cT.dva[i] + 2.0 * cT.dvb[i] * sin(2.0 * th) / sinth - 3.0 * cT.dvc[i] * sin(3.0 * th) / sinth;
+            e += cT.dva[i] * (1.0 + cos(th)) + cT.dvb[i] * (1.0 - cos(2.0 * th)) + cT.dvc[i] * (1.0 + cos(3.0 * th));
+        }
+        if (!force) continue;
+        double nuv = nu * nv, nu2 = nu * nu, nv2 = nv * nv;
+        // site i
+        double fix = (bx * (-by * cy - bz * cz) + cx * (by * by + bz * bz)) / nuv;
+        double fiy = (by * (-bx * cx - bz * cz) + cy * (bx * bx + bz * bz)) / nuv;
+        double fiz = (bz * (-bx * cx - by * cy) + cz * (bx * bx + by * by)) / nuv;
+        double gix = (2.0 * ax * (-by * by - bz * bz) + 2.0 * bx * (ay * by + az * bz)) / nu2;
+        double giy = (2.0 * ay * (-bx * bx - bz * bz) + 2.0 * by * (ax * bx + az * bz)) / nu2;
+        double giz = (2.0 * az * (-bx * bx - by * by) + 2.0 * bz * (ax * bx + ay * by)) / nu2;
+        // site j
+        double fjx = (ax * (-by * cy - bz * cz) + bx * (by * cy + bz * cz) + cx * (-ay * by - az * bz - by * by - bz * bz) +
+                      2.0 * bx * (ay * cy + az * cz)) / nuv;
+        double fjy = (ay * (-bx * cx - bz * cz) + by * (bx * cx + bz * cz) + cy * (-ax * bx - az * bz - bx * bx - bz * bz) +
+                      2.0 * by * (ax * cx + az * cz)) / nuv;
+        double fjz = (az * (-bx * cx - by * cy) + bz * (bx * cx + by * cy) + cz * (-ax * bx - ay * by - bx * bx - by * by) +
+                      2.0 * bz * (ax * cx + ay * cy)) / nuv;
+        double gjx = (2.0 * ax * (by * by + bz * bz + ay * by + az * bz) + 2.0 * bx * (-ay * ay - az * az - ay * by - az * bz)) / nu2 +
+                     (2.0 * cx * (by * cy + bz * cz) + 2.0 * bx * (-cy * cy - cz * cz)) / nv2;
+        double gjy = (2.0 * ay * (bx * bx + bz * bz + ax * bx + az * bz) + 2.0 * by * (-ax * ax - az * az - ax * bx - az * bz)) / nu2 +
+                     (2.0 * cy * (bx * cx + bz * cz) + 2.0 * by * (-cx * cx - cz * cz)) / nv2;
+        double gjz = (2.0 * az * (bx * bx + by * by + ax * bx + ay * by) + 2.0 * bz * (-ax * ax - ay * ay - ax * bx - ay * by)) / nu2 +
+                     (2.0 * cz * (bx * cx + by * cy) + 2.0 * bz * (-cx * cx - cy * cy)) / nv2;
+        // site k
+        double fkx = (ax * (by * by + bz * bz + by * cy + bz * cz) + bx * (-ay * by - az * bz) + cx * (ay * by + az * bz) +
+                      2.0 * bx * (-ay * cy - az * cz)) / nuv;
+        double fky = (ay * (bx * bx + bz * bz + bx * cx + bz * cz) + by * (-ax * bx - az * bz) + cy * (ax * bx + az * bz) +
+                      2.0 * by * (-ax * cx - az * cz)) / nuv;
+        double fkz = (az * (bx * bx + by * by + bx * cx + by * cy) + bz * (-ax * bx - ay * by) + cz * (ax * bx + ay * by) +
+                      2.0 * bz * (-ax * cx - ay * cy)) / nuv;
+        double gkx = (2.0 * ax * (-ay * by - az * bz) + 2.0 * bx * (ay * ay + az * az)) / nu2 +
+                     (2.0 * cx * (-by * by - bz * bz - by * cy - bz * cz) + 2.0 * bx * (cy * cy + cz * cz + by * cy + bz * cz)) / nv2;
+        double gky = (2.0 * ay * (-ax * bx - az * bz) + 2.0 * by * (ax * ax + az * az)) / nu2 +
+                     (2.0 * cy * (-bx * bx - bz * bz - bx * cx - bz * cz) + 2.0 * by * (cx * cx + cz * cz + bx * cx + bz * cz)) / nv2;
+        double gkz = (2.0 * az * (-ax * bx - ay * by) + 2.0 * bz * (ax * ax + ay * ay)) / nu2 +
+                     (2.0 * cz * (-bx * bx - by * by - bx * cx - by * cy) + 2.0 * bz * (cx * cx + cy * cy + bx * cx + by * cy)) / nv2;
+        // site n
+        double fnx = (ax * (-by * by - bz * bz) + bx * (ay * by + az * bz)) / nuv;
+        double fny = (ay * (-bx * bx - bz * bz) + by * (ax * bx + az * bz)) / nuv;
+        double fnz = (az * (-bx * bx - by * by) + bz * (ax * bx + ay * by)) / nuv;
+        double gnx = (2.0 * cx * (by * by + bz * bz) + 2.0 * bx * (-by * cy - bz * cz)) / nv2;
+        double gny = (2.0 * cy * (bx * bx + bz * bz) + 2.0 * by * (-bx * cx - bz * cz)) / nv2;
+        double gnz = (2.0 * cz * (bx * bx + by * by) + 2.0 * bz * (-bx * cx - by * cy)) / nv2;
+        double h = 0.5 * costh;
+        m.fx[iv] += r1 * (fix - h * gix); m.fy[iv] += r1 * (fiy - h * giy); m.fz[iv] += r1 * (fiz - h * giz);
+        m.fx[jv] += r1 * (fjx - h * gjx); m.fy[jv] += r1 * (fjy - h * gjy); m.fz[jv] += r1 * (fjz - h * gjz);
+        m.fx[kv] += r1 * (fkx - h * gkx); m.fy[kv] += r1 * (fky - h * gky); m.fz[kv] += r1 * (fkz - h * gkz);
+        m.fx[lv] += r1 * (fnx - h * gnx); m.fy[lv] += r1 * (fny - h * gny); m.fz[lv] += r1 * (fnz - h * gnz);
+    }
+    return e;
+}
+
+__device__ inline double lj_eps_sg6(const Dev &d, int ti, int tj, double &sg6) {
+    double2 v = d.ljt[ti * NTYPE + tj];
+    sg6 = v.y;
+    return v.x;  // 48 eps sg6
+}
+
+// one intramolecular nonbonded pair (Coulomb + LJ without cutoff)
+__device__ inline double intra_pair(const Dev &d, Mol29 &m, int a, int b, bool force) {
+    double x = m.x[a] - m.x[b], y = m.y[a] - m.y[b], z = m.z[a] - m.z[b];
+    double rsq = x * x + y * y + z * z;
+    double rsi = 1.0 / rsq, ir = sqrt(rsi), r6 = rsi * rsi * rsi;
+    double qq = cT.q[2 + a] * cT.q[2 + b] * XPI;
+    double sg6;
+    double e48 = lj_eps_sg6(d, 2 + a, 2 + b, sg6);
+    if (force) {
+        double ft = qq * ir * rsi + e48 * r6 * (sg6 * r6 - 0.5) * rsi;
+        m.fx[a] += x * ft; m.fy[a] += y * ft; m.fz[a] += z * ft;
+        m.fx[b] -= x * ft; m.fy[b] -= y * ft; m.fz[b] -= z * ft;
+    }
+    return qq * ir + (e48 / 12.0) * (sg6 * r6 * r6 - r6);
+}
+
+// src/eval_surfactant_internal.f90:153-246
+__device__ double internal(const Dev &d, Mol29 &m, bool force) {
+    double e = 0.0;
+    for (int j = 0; j < 15; j++)
+        for (int k = j + 4; k < NSURF; k++) e += intra_pair(d, m, j, k, force);
+    for (int k = 0; k < NSELF; k++) e += intra_pair(d, m, cT.si[k], cT.sj[k], force);
+    return e;
+}
+
+// src/eval_subtract_fma.f90:14-53
+__device__ double subtract(const Dev &d, Mol29 &m, const uint32_t *mask, bool force) {
+    double e = 0.0;
+    for (int j = 0; j < NSURF; j++) {
+        uint32_t bits = mask[j];
+        while (bits) {
+            int k = __ffs(bits) - 1;
+            bits &= bits - 1;
+            double x = m.x[j] - m.x[k], y = m.y[j] - m.y[k], z = m.z[j] - m.z[k];
+            double rmn = sqrt(x * x + y * y + z * z);
+            double qq = cT.q[2 + j] * cT.q[2 + k] * XPI;
+            if (force) {
+                double fel = qq / (rmn * rmn * rmn);
+                m.fx[j] -= x * fel; m.fy[j] -= y * fel; m.fz[j] -= z * fel;
+            }
+            e -= 0.5 * qq / rmn;
+        }
+    }
+    return e;
+}
+
+__global__ void k_intra(Dev d, const int *smols, int ns, int terms, double *e_mol) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns) return;
+    int mol = smols[t];
+    int g0 = d.mfirst[mol];
+    Mol29 m;
+    for (int i = 0; i < NSURF; i++) {
+        m.x[i] = d.x[g0 + i]; m.y[i] = d.y[g0 + i]; m.z[i] = d.z[g0 + i];
+        m.fx[i] = 0.0; m.fy[i] = 0.0; m.fz[i] = 0.0;
+    }
+    bool force = e_mol == nullptr;
+    double eb = 0.0, ei = 0.0, es = 0.0;
+    if (terms & SESP_T_VALENCE) eb += valence(m, force);
+    if (terms & SESP_T_DIHEDRAL) eb += dihedral(m, 0, 18, false, force);
+    if (terms & SESP_T_BERENDSEN) eb += dihedral(m, 18, 30, true, force);
+    if (terms & SESP_T_INTERNAL) ei += internal(d, m, force);
+    if (terms & SESP_T_SUBTRACT) es += subtract(d, m, d.isub + (size_t)t * NSURF, force);
+    if (force) {
+        for (int i = 0; i < NSURF; i++) { d.fx[g0 + i] += m.fx[i]; d.fy[g0 + i] += m.fy[i]; d.fz[g0 + i] += m.fz[i]; }
+    } else {
+        e_mol[3 * t] = eb; e_mol[3 * t + 1] = ei; e_mol[3 * t + 2] = es;
+    }
+}
+
+void launch_intra(const Dev &d, const int *smols, int ns, int terms, cudaStream_t st) {
+    if (ns && (terms & (SESP_T_VALENCE | SESP_T_DIHEDRAL | SESP_T_BERENDSEN | SESP_T_INTERNAL | SESP_T_SUBTRACT)))
+        k_intra<<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, terms, nullptr);
+}
+
+// ------------------------------------------------------------------ energies (diagnostic path)
+
+// near-field pair energy (1/2 per ordered pair) and far-field potential
+// energy per slot, FP64
+__global__ void k_energy_slot(Dev d, double *e_slot) {
+    const int c = blockIdx.x;
+    const int s0 = d.cstart[c], ni = d.cstart[c + 1] - s0;
+    const Rep r = d.rep[d.crep[c]];
+    int ix, iy, iz;
+    cell_xyz(r, c, ix, iy, iz);
+    const double cx = cell_centre(d, r, 0, ix), cy = cell_centre(d, r, 1, iy), cz = cell_centre(d, r, 2, iz);
+    __shared__ double Lre[LP], Lim[LP];
+    if (threadIdx.x < LP) { double2 v = d.L4[(size_t)c * LP + threadIdx.x]; Lre[threadIdx.x] = v.x; Lim[threadIdx.x] = v.y; }
+    __syncthreads();
+    const double rc2 = RC * RC;
+    for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+        double4 pi = d.srt_pos[s0 + i];
+        int2 mi = d.srt_meta[s0 + i];
+        double ec = 0.0, el = 0.0;
+        for (int dzc = -1; dzc <= 1; dzc++)
+            for (int dyc = -1; dyc <= 1; dyc++)
+                for (int dxc = -1; dxc <= 1; dxc++) {
+                    int jx = ix + dxc, jy = iy + dyc, jz = iz + dzc;
+                    if (jx < 0 || jy < 0 || jz < 0 || jx >= r.nc[0] || jy >= r.nc[1] || jz >= r.nc[2]) continue;
+                    int cn = cell_index(r, jx, jy, jz);
+                    for (int s = d.cstart[cn]; s < d.cstart[cn + 1]; s++) {
+                        int2 mj = d.srt_meta[s];
+                        if (mj.x == mi.x) continue;
+                        double4 pj = d.srt_pos[s];
+                        double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                        double r2 = dx * dx + dy * dy + dz * dz;
+                        double ir = rsqrt(r2);
+                        ec += 0.5 * pi.w * pj.w * XPI * ir;
+                        double2 lj = d.ljt[mi.y * NTYPE + mj.y];
+                        if (r2 <= rc2 && lj.x != 0.0) {
+                            double r6 = ir * ir * ir * ir * ir * ir;
+                            el += 0.5 * (lj.x / 12.0) * (lj.y * r6 * r6 - r6);
+                        }
+                    }
+                }
+        double gx, gy, gz, phi;
+        local_grad<double>(Lre, Lim, pi.x - cx, pi.y - cy, pi.z - cz, gx, gy, gz, &phi);
+        e_slot[3 * (size_t)(s0 + i)] = ec;
+        e_slot[3 * (size_t)(s0 + i) + 1] = el;
+        e_slot[3 * (size_t)(s0 + i) + 2] = 0.5 * pi.w * XPI * phi;
+    }
+}
+
+// walls, graphite and kinetic energy per site
+__global__ void k_energy_site(Dev d, int nsite, double *e_site) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nsite) return;
+    const Rep r = d.rep[d.mrep[d.smol[g]]];
+    double x = d.x[g], y = d.y[g], z = d.z[g];
+    double ew = 4.0 / pow12(x - r.rhs[0]) + 4.0 / pow12(r.rhs[0] + x) + 4.0 / pow12(y - r.rhs[1]) +
+                4.0 / pow12(r.rhs[1] + y) + 4.0 / pow12(z - r.rhs[2]) + 4.0 / pow12(r.rhs[2] + z);
+    double eg = 0.0, fx = 0, fy = 0, fz = 0, eps, sg6;
+    int col = graphite_column(d, r, g, eps, sg6);
+    if (col >= 0) graphite_site(d, col, x, y, z, eps, sg6, fx, fy, fz, &eg);
+    double m = cT.mass[d.ptype[g]];
+    double ek = 0.5 * m * (d.vx[g] * d.vx[g] + d.vy[g] * d.vy[g] + d.vz[g] * d.vz[g]) / (DT * DT);
+    e_site[3 * (size_t)g] = ew; e_site[3 * (size_t)g + 1] = eg; e_site[3 * (size_t)g + 2] = ek;
+}
+
+void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int ns, double *e_slot, double *e_site,
+                     double *e_mol, cudaStream_t st) {
+    k_energy_slot<<<ncell, 128, 0, st>>>(d, e_slot);
+    k_energy_site<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, e_site);
+    if (ns) k_intra<<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, SESP_T_ALL, e_mol);
+}
+
+}  // namespace sesp

@@ -1,0 +1,30 @@
+// Host-side launchers of the engine's kernels (one declaration per kernel
+// family); the kernels live in k_exact.cu and k_force.cu.
+#pragma once
+
+#include "sesp_internal.cuh"
+
+namespace sesp {
+
+// k_exact.cu
+void upload_tables_exact(const Tables &t, cudaStream_t st);
+void launch_locate(const Dev &d, int nmol, cudaStream_t st);
+void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st);
+void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
+                   cudaStream_t st);
+void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit,
+                   cudaStream_t st);
+void launch_init_accel(const Dev &d, int nsite, cudaStream_t st);
+
+// k_force.cu
+void upload_tables_force(const Tables &t, cudaStream_t st);
+void launch_sort(const Dev &d, int nsite, int ncell, cudaStream_t st);
+void launch_gather(const Dev &d, int nslot, int ncell, int mixed, cudaStream_t st);
+void launch_near(const Dev &d, int ncell, int mixed, int terms, cudaStream_t st);
+void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int nrep, int d2, cudaStream_t st);
+void launch_site_forces(const Dev &d, int nsite, int terms, cudaStream_t st);
+void launch_intra(const Dev &d, const int *smols, int ns, int terms, cudaStream_t st);
+void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int ns, double *e_slot, double *e_site,
+                     double *e_mol, cudaStream_t st);
+
+}  // namespace sesp

@@ -1,0 +1,844 @@
+// C ABI of the GB300 engine (declared in include/sesp.h): context, device
+// state, host-side force-field tables and multipole translation operators,
+// and the per-step launch sequence (captured into CUDA graphs by sesp_run).
+#include <cmath>
+#include <complex>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "k_launch.cuh"
+
+using namespace sesp;
+
+namespace sesp {
+// surfactant site LJ sigma (reduced) and epsilon (reduced), src/init_arrays.f90:314-474
+void surf_lj(double *sgs, double *eps) {
+    const double s_ahy = 2.6, e_ahy = 33.5, s_aox = 3.07, e_aox = 711.76, s_ome = 3.983, e_ome = 478.12;
+    const double s_oox = 3.047, e_oox = 817.67, s_tme = 3.95, e_tme = 382.47, s_bsi = 3.385, e_bsi = 2448.0;
+    const double s_box = 2.955, e_box = 849.3, s_bme = 3.786, e_bme = 753.2;
+    const double S[NSURF] = {s_ahy, s_aox, s_ome, s_ome, s_oox, s_ome, s_ome, s_oox, s_ome, s_ome, s_oox, s_ome, s_ome, s_oox, s_ome,
+                             s_tme, s_tme, s_bsi, s_bme, s_box, s_bsi, s_bme, s_bme, s_bme, s_box, s_bsi, s_bme, s_bme, s_bme};
+    const double E[NSURF] = {e_ahy, e_aox, e_ome, e_ome, e_oox, e_ome, e_ome, e_oox, e_ome, e_ome, e_oox, e_ome, e_ome, e_oox, e_ome,
+                             e_tme, e_tme, e_bsi, e_bme, e_box, e_bsi, e_bme, e_bme, e_bme, e_box, e_bsi, e_bme, e_bme, e_bme};
+    for (int i = 0; i < NSURF; i++) { sgs[i] = S[i] / SIGMA; eps[i] = E[i] / EPSILON; }
+}
+}  // namespace sesp
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CK(call)                                                                              \
+    do {                                                                                      \
+        cudaError_t e_ = (call);                                                              \
+        if (e_ != cudaSuccess) return fail(SESP_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+// ------------------------------------------------------------------ tables (src/init_arrays.f90)
+
+double fact(int n) { double f = 1.0; for (int i = 2; i <= n; i++) f *= i; return f; }
+
+Tables make_tables() {
+    Tables T;
+    memset(&T, 0, sizeof T);
+    const double sigma = SIGMA, epsilon = EPSILON;
+    const double pi180 = 4.0 * atan(1.0) / 180.0;
+    const double hy = 1.00794, carbon = 12.011, oxygen = 15.9994, si = 28.0855;
+    const double me = carbon + 2.0 * hy, methyl = carbon + 3.0 * hy;
+    // masses (src/init_arrays.f90:266-312)
+    const double ms[NSURF] = {hy, oxygen, me, me, oxygen, me, me, oxygen, me, me, oxygen, me, me, oxygen, me, me, me,
+                              si, methyl, oxygen, si, methyl, methyl, methyl, oxygen, si, methyl, methyl, methyl};
+    T.mass[0] = oxygen / oxygen;
+    T.mass[1] = hy / oxygen;
+    for (int i = 0; i < NSURF; i++) T.mass[2 + i] = ms[i] / oxygen;
+    // charges (src/init_arrays.f90:340-474)
+    const double qs[NSURF] = {0.435, -0.700, 0.265, 0.29, -0.58, 0.29, 0.29, -0.58, 0.29, 0.29, -0.58, 0.29, 0.29, -0.58, 0.29,
+                              0.0, 0.0, 0.3, 0.0, -0.3, 0.15, 0.0, 0.0, 0.0, -0.3, 0.15, 0.0, 0.0, 0.0};
+    T.q[0] = -0.8476;
+    T.q[1] = 0.4238;
+    for (int i = 0; i < NSURF; i++) T.q[2 + i] = qs[i];
+    // surfactant constraints (src/init_arrays.f90:229-264, 509-565)
+    for (int b = 0; b < 18; b++) { T.bi[b] = b; T.bj[b] = b + 1; }
+    const int bx[10][2] = {{18, 20}, {20, 21}, {21, 22}, {21, 23}, {21, 24}, {18, 25}, {25, 26}, {26, 27}, {26, 28}, {26, 29}};
+    for (int b = 0; b < 10; b++) { T.bi[18 + b] = bx[b][0] - 1; T.bj[18 + b] = bx[b][1] - 1; }
+    const double bl[NBOND] = {0.945, 1.430, 1.516, 1.410, 1.410, 1.516, 1.410, 1.410, 1.516, 1.410, 1.410, 1.516, 1.410, 1.410,
+                              1.516, 1.540, 1.88, 1.88, 1.60, 1.60, 1.88, 1.88, 1.88, 1.60, 1.60, 1.88, 1.88, 1.88};
+    for (int b = 0; b < NBOND; b++) T.dsqs[b] = bl[b] * bl[b] / (sigma * sigma);
+    double w[3] = {1.0, 2.0 * sin(109.47 * pi180 / 2.0), 1.0};
+    for (int i = 0; i < 3; i++) T.dsqw[i] = w[i] * w[i] / (sigma * sigma);
+    // angles (src/eval_valence.f90:13-95, src/init_arrays.f90:576-695)
+    const int ang[NANGLE][3] = {{1, 2, 3}, {2, 3, 4}, {3, 4, 5}, {4, 5, 6}, {5, 6, 7}, {6, 7, 8}, {7, 8, 9}, {8, 9, 10}, {9, 10, 11},
+                                {10, 11, 12}, {11, 12, 13}, {12, 13, 14}, {13, 14, 15}, {14, 15, 16}, {15, 16, 17}, {16, 17, 18},
+                                {17, 18, 19}, {17, 18, 20}, {17, 18, 25}, {19, 18, 20}, {19, 18, 25}, {18, 25, 26}, {18, 20, 21},
+                                {20, 21, 22}, {20, 21, 23}, {20, 21, 24}, {22, 21, 24}, {22, 21, 23}, {23, 21, 24}, {25, 26, 27},
+                                {25, 26, 28}, {25, 26, 29}, {27, 26, 28}, {27, 26, 29}, {28, 26, 29}, {20, 18, 25}};
+    const double th[NANGLE] = {108.5, 108.0, 108.0, 112.0, 108.0, 108.0, 112.0, 108.0, 108.0, 112.0, 108.0, 108.0, 112.0, 108.0,
+                               114.0, 109.5, 109.5, 109.5, 109.5, 109.5, 109.5, 144.0, 144.0, 109.5, 109.5, 109.5, 109.5, 109.5,
+                               109.5, 109.5, 109.5, 109.5, 109.5, 109.5, 109.5, 109.5};
+    const double kth[NANGLE] = {519700, 519700, 519700, 519700, 519700, 519700, 519700, 519700, 519700, 519700, 519700, 519700,
+                                519700, 519700, 519700, 519700, 418400, 418400, 418400, 418400, 418400, 118400, 118400, 418400,
+                                418400, 418400, 418400, 418400, 418400, 418400, 418400, 418400, 418400, 418400, 418400, 791200};
+    for (int i = 0; i < NANGLE; i++) {
+        T.ai[i] = ang[i][0] - 1; T.aj[i] = ang[i][1] - 1; T.ak[i] = ang[i][2] - 1;
+        T.th[i] = th[i] * pi180;
+        T.rkth[i] = kth[i] / epsilon;
+    }
+    // dihedrals (src/eval_dihedral.f90:23-100, src/init_arrays.f90:697-836)
+    const int dh[NDIH][4] = {{1, 2, 3, 4}, {2, 3, 4, 5}, {3, 4, 5, 6}, {4, 5, 6, 7}, {5, 6, 7, 8}, {6, 7, 8, 9}, {7, 8, 9, 10},
+                             {8, 9, 10, 11}, {9, 10, 11, 12}, {10, 11, 12, 13}, {11, 12, 13, 14}, {12, 13, 14, 15},
+                             {13, 14, 15, 16}, {14, 15, 16, 17}, {15, 16, 17, 18}, {16, 17, 18, 19}, {16, 17, 18, 20},
+                             {16, 17, 18, 25}, {17, 18, 20, 21}, {17, 18, 25, 26}, {19, 18, 20, 21}, {19, 18, 25, 26},
+                             {18, 20, 21, 22}, {18, 20, 21, 23}, {18, 20, 21, 24}, {18, 25, 26, 27}, {18, 25, 26, 28},
+                             {18, 25, 26, 29}, {20, 18, 25, 26}, {21, 20, 18, 25}};
+    const double al[3] = {3490.0, -486.0, 3130.0}, ommo[3] = {2940.0, -888.0, 12810.0};
+    const double mmom[3] = {19860.0, -5853.0, 8956.0}, tr[3] = {5903.8, -1134.0, 13159.0};
+    const double *cf[18] = {al, ommo, mmom, mmom, ommo, mmom, mmom, ommo, mmom, mmom, ommo, mmom, mmom, ommo, tr, tr, tr, tr};
+    for (int i = 0; i < NDIH; i++) {
+        T.di[i] = dh[i][0] - 1; T.dj[i] = dh[i][1] - 1; T.dk[i] = dh[i][2] - 1; T.dl[i] = dh[i][3] - 1;
+        if (i < 18) {
+            T.dva[i] = cf[i][0] / 2.0 / epsilon; T.dvb[i] = cf[i][1] / 2.0 / epsilon; T.dvc[i] = cf[i][2] / 2.0 / epsilon;
+        } else {
+            T.dva[i] = 3770.0 / epsilon; T.dvb[i] = 0.0; T.dvc[i] = 0.0;
+        }
+    }
+    // intramolecular listed pairs (src/init_arrays.f90:127-220)
+    const int sp[NSELF][2] = {{16, 21}, {16, 22}, {16, 23}, {16, 24}, {16, 26}, {16, 27}, {16, 28}, {16, 29}, {17, 22}, {17, 23},
+                              {17, 24}, {17, 27}, {17, 28}, {17, 29}, {19, 22}, {19, 23}, {19, 24}, {19, 27}, {19, 28}, {19, 29},
+                              {20, 27}, {20, 28}, {20, 29}, {21, 26}, {21, 27}, {21, 28}, {21, 29}, {22, 25}, {22, 26}, {22, 27},
+                              {22, 28}, {22, 29}, {23, 25}, {23, 26}, {23, 27}, {23, 28}, {23, 29}, {24, 25}, {24, 26}, {24, 27},
+                              {24, 28}, {24, 29}};
+    for (int k = 0; k < NSELF; k++) { T.si[k] = sp[k][0] - 1; T.sj[k] = sp[k][1] - 1; }
+    // graphite (src/eval_graphite.f90:69-70, src/init_arrays.f90:503-506)
+    double sgs[NSURF], eps[NSURF];
+    surf_lj(sgs, eps);
+    for (int i = 0; i < NSURF; i++) {
+        double s = (3.19 / sigma + sgs[i]) / 2.0;
+        T.sgcs6[i] = s * s * s * s * s * s;
+        T.epcs[i] = sqrt((392.0 / epsilon) * eps[i]);
+    }
+    double sw = 3.19 / sigma;
+    T.sgcw6 = sw * sw * sw * sw * sw * sw;
+    T.epcw = 392.0 / epsilon;
+    for (int n = 0; n <= P; n++)
+        for (int m = -n; m <= n; m++) T.rfctr[n * (n + 1) + m] = sqrt(fact(n - abs(m)) / fact(n + abs(m)));
+    return T;
+}
+
+}  // namespace
+
+
+namespace {
+
+// LJ pair table (48 eps sg6, sg6) over the 31 site kinds; zero where the
+// reference adds no LJ (water H with anything)
+std::vector<double2> make_lj_table() {
+    double sgs[NSURF], eps[NSURF];
+    surf_lj(sgs, eps);
+    std::vector<double2> t(NTYPE * NTYPE, make_double2(0.0, 0.0));
+    auto sg = [&](int k) { return k == 0 ? 1.0 : sgs[k - 2]; };
+    auto ep = [&](int k) { return k == 0 ? 1.0 : eps[k - 2]; };
+    for (int a = 0; a < NTYPE; a++)
+        for (int b = 0; b < NTYPE; b++) {
+            if (a == 1 || b == 1) continue;
+            double s = (sg(a) + sg(b)) / 2.0;
+            double s6 = s * s * s * s * s * s;
+            double e = sqrt(ep(a) * ep(b));
+            t[a * NTYPE + b] = make_double2(48.0 * e * s6, s6);
+        }
+    return t;
+}
+
+// ------------------------------------------------------------------ translation operators (src/ifma.f90)
+
+double legendre(int l, int m, double x) {
+    if (l == -1 && m == 0) return 1.0;
+    if (m > l || l < 0) return 0.0;
+    double pmm = 1.0;
+    if (m > 0) {
+        double s = sqrt((1.0 - x) * (1.0 + x)), f = 1.0;
+        for (int i = 1; i <= m; i++) { pmm = -pmm * f * s; f += 2.0; }
+    }
+    if (l == m) return pmm;
+    double p1 = x * (2 * m + 1) * pmm;
+    if (l == m + 1) return p1;
+    double p0 = pmm, pl = 0.0;
+    for (int ll = m + 2; ll <= l; ll++) { pl = (x * (2 * ll - 1) * p1 - (ll + m - 1) * p0) / (ll - m); p0 = p1; p1 = pl; }
+    return pl;
+}
+std::complex<double> Ylm(int n, int m, double al, double be) {
+    int am = abs(m);
+    return sqrt(fact(n - am) / fact(n + am)) * legendre(n, am, cos(al)) * std::complex<double>(cos(m * be), sin(m * be));
+}
+double sgn(int n) { return (n % 2 == 0) ? 1.0 : -1.0; }
+double rAnm(int n, int m) { return sgn(n) / sqrt(fact(n - m) * fact(n + m)); }
+double iIkm1(int k, int m) { return sgn(abs((abs(k) - abs(m) - abs(k - m)) / 2)); }
+double iIkm2(int k, int m) { return sgn(abs((abs(k - m) - abs(k) - abs(m)) / 2)); }
+double iIkm3(int k, int m) { return sgn(abs((abs(m) - abs(m - k) - abs(k)) / 2)); }
+int oidx(int j, int k) { return j * (j + 1) / 2 + k; }
+int cidx(int n, int m) { return n * (n + 1) + m; }
+void sph(double x, double y, double z, double &rho, double &al, double &be) {
+    rho = sqrt(x * x + y * y + z * z);
+    al = acos(z / rho);
+    be = atan2(y, x);
+}
+
+// M2L operator at source - target vector d, src/computeLjk4.f90:134-158
+void op_m2l(double x, double y, double z, double2 *op) {
+    double rho, al, be;
+    sph(x, y, z, rho, al, be);
+    for (int j = 0; j <= P; j++)
+        for (int k = 0; k <= j; k++)
+            for (int n = 0; n <= P; n++)
+                for (int m = -n; m <= n; m++) {
+                    double rt = iIkm2(k, m) * rAnm(j, k) * rAnm(n, m) / (sgn(n) * rAnm(j + n, m - k) * pow(rho, j + n + 1));
+                    std::complex<double> c = rt * Ylm(j + n, m - k, al, be);
+                    op[oidx(j, k) * LP + cidx(n, m)] = make_double2(c.real(), c.imag());
+                }
+}
+// M2M operator at child - parent vector d, src/computeOnm3.f90:207-228
+void op_m2m(double x, double y, double z, double2 *op) {
+    double rho, al, be;
+    sph(x, y, z, rho, al, be);
+    for (int i = 0; i < LPH * LP; i++) op[i] = make_double2(0.0, 0.0);
+    for (int j = 0; j <= P; j++)
+        for (int k = 0; k <= j; k++)
+            for (int n = 0; n <= j; n++)
+                for (int m = -n; m <= n; m++) {
+                    if (j - n - abs(k - m) < 0) continue;
+                    double rt = iIkm1(k, m) * rAnm(n, m) * rAnm(j - n, k - m) * pow(rho, n) / rAnm(j, k);
+                    std::complex<double> c = rt * Ylm(n, -m, al, be);
+                    double2 &o = op[oidx(j, k) * LP + cidx(j - n, k - m)];
+                    o.x += c.real(); o.y += c.imag();
+                }
+}
+// L2L operator at parent - child vector d, src/shiftLjk3.f90:193-221
+void op_l2l(double x, double y, double z, double2 *op) {
+    double rho, al, be;
+    sph(x, y, z, rho, al, be);
+    for (int i = 0; i < LPH * LP; i++) op[i] = make_double2(0.0, 0.0);
+    for (int j = 0; j <= P; j++)
+        for (int k = 0; k <= j; k++)
+            for (int n = 0; n <= P; n++)
+                for (int m = -n; m <= n; m++) {
+                    if (n - j - abs(m - k) < 0) continue;
+                    double rt = iIkm3(k, m) * rAnm(n - j, m - k) * rAnm(j, k) * pow(rho, n - j) / (sgn(n + j) * rAnm(n, m));
+                    std::complex<double> c = rt * Ylm(n - j, m - k, al, be);
+                    double2 &o = op[oidx(j, k) * LP + cidx(n, m)];
+                    o.x += c.real(); o.y += c.imag();
+                }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ context
+
+struct sesp_ctx {
+    sesp_params p;
+    cudaStream_t st = nullptr;
+    bool uploaded = false, have_force = false;
+    int nrep = 0, nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, nwm = 0, nsm = 0, d2 = 1;
+    std::vector<Rep> reps;
+    Dev d;
+    int *wmols = nullptr, *smols = nullptr;
+    std::vector<void *> allocs;
+    int64_t steps = 0;
+    // graphs of one step with / without a rebuild
+    cudaGraphExec_t g_step[2] = {nullptr, nullptr};
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[16];
+    double t_acc[8] = {0};
+    int64_t t_n[8] = {0};
+    // host copies for downloads
+    std::vector<double> h3;
+};
+
+namespace {
+
+template <typename T>
+int dalloc(sesp_ctx *c, T **p, size_t n) {
+    void *q = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc(&q, n * sizeof(T));
+    if (e != cudaSuccess) return fail(SESP_ENOMEM, "cudaMalloc of %zu bytes: %s", n * sizeof(T), cudaGetErrorString(e));
+    cudaMemsetAsync(q, 0, n * sizeof(T), c->st);
+    c->allocs.push_back(q);
+    *p = (T *)q;
+    return 0;
+}
+
+void free_state(sesp_ctx *c) {
+    for (auto &g : c->g_step)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (void *q : c->allocs) cudaFree(q);
+    c->allocs.clear();
+    c->uploaded = false;
+    c->have_force = false;
+}
+
+// cell centres along one axis of a replica: rcen4 of the owning rank,
+// src/init_box_dimensions.f90:40-42 and :79-94
+void axis_centres(const Rep &r, int a, std::vector<double> &out) {
+    double b = (double)r.nr[a];
+    for (int k = 0; k < r.nc[a]; k++) {
+        int rk = k / 4, i = k % 4 + 1;
+        double c2 = r.rsd[a] * (rk + 1) / b - r.rhs[a] - r.rsd[a] / b / 2.0;
+        out.push_back(4.0 * RS * i / 4.0 - 2.0 * RS - 4.0 * RS / 8.0 + c2);
+    }
+}
+
+int check_ctx(sesp_ctx *c, bool need_state) {
+    if (!c) return fail(SESP_EINVAL, "null context");
+    if (need_state && !c->uploaded) return fail(SESP_ESTATE, "no state uploaded");
+    return 0;
+}
+
+int set_device(sesp_ctx *c) {
+    CK(cudaSetDevice(c->p.device));
+    return 0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ sequences
+
+namespace {
+
+void tstart(sesp_ctx *c, int k) { if (c->timing) cudaEventRecord(c->ev[2 * k], c->st); }
+void tstop(sesp_ctx *c, int k) { if (c->timing) cudaEventRecord(c->ev[2 * k + 1], c->st); }
+void tcollect(sesp_ctx *c, int k) {
+    if (!c->timing) return;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]) == cudaSuccess) { c->t_acc[k] += ms; c->t_n[k]++; }
+}
+
+void seq_force(sesp_ctx *c, int rebuild, int terms) {
+    const Dev &d = c->d;
+    const int mixed = c->p.precision == SESP_MIXED;
+    if (rebuild) {
+        tstart(c, 5);
+        cudaMemsetAsync(d.ccount, 0, sizeof(int) * c->ncell, c->st);
+        launch_locate(d, c->nmol, c->st);
+        launch_sort(d, c->nsite, c->ncell, c->st);
+        launch_isub(d, c->nsm * NSURF, c->smols, c->st);
+        tstop(c, 5);
+    }
+    launch_gather(d, c->nsite, c->ncell, mixed, c->st);
+    if (rebuild) {
+        tstart(c, 6);
+        launch_fma_build(d, c->ncell, c->n3, c->n2, c->nrep, c->d2, c->st);
+        tstop(c, 6);
+    }
+    tstart(c, 0);
+    launch_near(d, c->ncell, mixed, terms, c->st);
+    tstop(c, 0);
+    tstart(c, 4);
+    launch_site_forces(d, c->nsite, terms, c->st);
+    launch_intra(d, c->smols, c->nsm, terms, c->st);
+    tstop(c, 4);
+}
+
+void seq_move_a(sesp_ctx *c) {
+    tstart(c, 2);
+    launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit, c->st);
+    tstop(c, 2);
+}
+void seq_move_b(sesp_ctx *c) {
+    tstart(c, 3);
+    launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit, c->st);
+    tstop(c, 3);
+}
+
+void collect_all(sesp_ctx *c) {
+    if (!c->timing) return;
+    cudaStreamSynchronize(c->st);
+    for (int k = 0; k < 7; k++) tcollect(c, k);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ ABI
+
+extern "C" {
+
+int sesp_abi_version(void) { return SESP_ABI_VERSION; }
+
+int sesp_last_error(char *buf, size_t len) {
+    if (!buf || len == 0) return SESP_EINVAL;
+    snprintf(buf, len, "%s", g_err.c_str());
+    return 0;
+}
+
+int sesp_default_params(sesp_params *p) {
+    if (!p) return fail(SESP_EINVAL, "null params");
+    memset(p, 0, sizeof *p);
+    p->n_cells[0] = p->n_cells[1] = p->n_cells[2] = 12;
+    p->precision = SESP_PLAIN_FP64;
+    p->rebuild_interval = 10;
+    p->graphite_on = 1;
+    p->tr = 3.81087;
+    p->tau_steps = 7.5;
+    p->shake_tol = 0.0001;
+    p->shake_maxit = 100;
+    p->device = 0;
+    p->max_cell_sites = 0;
+    return 0;
+}
+
+int sesp_create(const sesp_params *p, sesp_ctx **out) {
+    if (!p || !out) return fail(SESP_EINVAL, "null argument");
+    for (int a = 0; a < 3; a++)
+        if (p->n_cells[a] <= 0 || p->n_cells[a] % 4) return fail(SESP_EINVAL, "n_cells must be positive multiples of 4");
+    if (p->precision != SESP_PLAIN_FP64 && p->precision != SESP_MIXED) return fail(SESP_EINVAL, "unknown precision");
+    if (p->rebuild_interval <= 0) return fail(SESP_EINVAL, "rebuild_interval must be positive");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SESP_ECUDA, "no CUDA device");
+    if (p->device < 0 || p->device >= ndev) return fail(SESP_EINVAL, "device %d out of range", p->device);
+    sesp_ctx *c = new sesp_ctx();
+    c->p = *p;
+    if (set_device(c)) { delete c; return SESP_ECUDA; }
+    if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "stream"); }
+    for (int k = 0; k < 16; k++) cudaEventCreate(&c->ev[k]);
+    Tables T = make_tables();
+    upload_tables_exact(T, c->st);
+    upload_tables_force(T, c->st);
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "table upload"); }
+    *out = c;
+    return 0;
+}
+
+int sesp_destroy(sesp_ctx *c) {
+    if (!c) return 0;
+    cudaSetDevice(c->p.device);
+    cudaStreamSynchronize(c->st);
+    free_state(c);
+    for (int k = 0; k < 16; k++) cudaEventDestroy(c->ev[k]);
+    cudaStreamDestroy(c->st);
+    delete c;
+    return 0;
+}
+
+int sesp_upload_state(sesp_ctx *c, int n_water, int n_surf, const double *pos, const double *vel, int n_carbon,
+                      const double *carbons) {
+    if (int e = check_ctx(c, false)) return e;
+    if (n_water < 0 || n_surf < 0 || n_water + n_surf == 0) return fail(SESP_EINVAL, "empty system");
+    if (!pos) return fail(SESP_EINVAL, "null positions");
+    if (n_carbon < 0 || (n_carbon > 0 && !carbons)) return fail(SESP_EINVAL, "bad carbons");
+    if (set_device(c)) return SESP_ECUDA;
+    cudaStreamSynchronize(c->st);
+    free_state(c);
+    // one replica (the batch entry points stack several the same way)
+    Rep r;
+    memset(&r, 0, sizeof r);
+    for (int a = 0; a < 3; a++) {
+        r.nc[a] = c->p.n_cells[a];
+        r.nr[a] = r.nc[a] / 4;
+        r.rsd[a] = r.nc[a] * RS;
+        r.rhs[a] = r.rsd[a] / 2.0;
+    }
+    r.nw = n_water; r.ns = n_surf;
+    r.nsite = 3 * n_water + NSURF * n_surf;
+    r.nmol = n_water + n_surf;
+    r.graphite_on = c->p.graphite_on;
+    int np = r.nsite, ncon = 3 * n_water + NBOND * n_surf, df = 3 * np - ncon;
+    double rlx = c->p.tau_steps * DT;
+    r.pnh1 = DT / df / c->p.tr / (rlx * rlx);
+    r.pnh2 = -2.0 * df * c->p.tr;
+    c->reps.assign(1, r);
+    c->nrep = 1;
+    Rep &R = c->reps[0];
+    R.cell0 = 0; R.l3_0 = 0; R.l2_0 = 0; R.site0 = 0; R.mol0 = 0; R.axis0 = 0; R.gcol0 = 0;
+    c->nsite = R.nsite; c->nmol = R.nmol;
+    c->ncell = R.nc[0] * R.nc[1] * R.nc[2];
+    c->n3 = c->ncell / 8;
+    c->n2 = c->ncell / 64;
+    c->nwm = n_water; c->nsm = n_surf;
+    c->d2 = std::max(1, std::max(R.nr[0], std::max(R.nr[1], R.nr[2])) - 1);
+    // positions must lie inside the box
+    for (int g = 0; g < c->nsite; g++)
+        for (int a = 0; a < 3; a++) {
+            double v = pos[3 * g + a];
+            if (!(v > -R.rhs[a] && v < R.rhs[a])) return fail(SESP_EINVAL, "site %d outside the box (axis %d: %g)", g, a, v);
+        }
+    Dev &d = c->d;
+    memset(&d, 0, sizeof d);
+    int N = c->nsite, M = c->nmol, C = c->ncell;
+    int e = 0;
+    double **a12[12] = {&d.x, &d.y, &d.z, &d.vx, &d.vy, &d.vz, &d.ax, &d.ay, &d.az, &d.fx, &d.fy, &d.fz};
+    for (auto q : a12) if ((e = dalloc(c, q, N))) return e;
+    if ((e = dalloc(c, &d.ptype, N)) || (e = dalloc(c, &d.smol, N)) || (e = dalloc(c, &d.mrep, M)) ||
+        (e = dalloc(c, &d.mfirst, M)) || (e = dalloc(c, &d.mkind, M)) || (e = dalloc(c, &d.mkey, M)) ||
+        (e = dalloc(c, &d.mw1, M)) || (e = dalloc(c, &d.ke, 2 * M)) || (e = dalloc(c, &d.mfail, M)) ||
+        (e = dalloc(c, &d.rep, 1)) || (e = dalloc(c, &d.eta, 1)) || (e = dalloc(c, &d.crep, C)) ||
+        (e = dalloc(c, &d.b3rep, c->n3)) || (e = dalloc(c, &d.b2rep, c->n2)) || (e = dalloc(c, &d.cstart, C + 1)) ||
+        (e = dalloc(c, &d.ccount, C)) || (e = dalloc(c, &d.cfill, C)) || (e = dalloc(c, &d.sloc, N)) ||
+        (e = dalloc(c, &d.sslot, N)) || (e = dalloc(c, &d.srt_site, N)) || (e = dalloc(c, &d.srt_pos, N)) ||
+        (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) ||
+        (e = dalloc(c, &d.isub, (size_t)NSURF * n_surf)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
+        (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * c->n3)) ||
+        (e = dalloc(c, &d.L3, (size_t)LP * c->n3)) || (e = dalloc(c, &d.O2, (size_t)LP * c->n2)) ||
+        (e = dalloc(c, &d.L2, (size_t)LP * c->n2)) || (e = dalloc(c, &d.counters, 8)) ||
+        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &c->wmols, n_water)) || (e = dalloc(c, &c->smols, n_surf)))
+        return e;
+    int w2 = 2 * c->d2 + 1;
+    if ((e = dalloc(c, &d.op_m2l4, (size_t)343 * LPH * LP)) || (e = dalloc(c, &d.op_m2l3, (size_t)343 * LPH * LP)) ||
+        (e = dalloc(c, &d.op_m2l2, (size_t)w2 * w2 * w2 * LPH * LP)) || (e = dalloc(c, &d.op_m2m43, (size_t)8 * LPH * LP)) ||
+        (e = dalloc(c, &d.op_m2m32, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_l2l23, (size_t)8 * LPH * LP)) ||
+        (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)))
+        return e;
+    // host-side static data
+    std::vector<uint8_t> ptype(N);
+    std::vector<int> smol(N), mrep(M, 0), mfirst(M), mkind(M), wm(n_water), sm(n_surf);
+    for (int m = 0; m < n_water; m++) {
+        mfirst[m] = 3 * m; mkind[m] = 0; wm[m] = m;
+        for (int t = 0; t < 3; t++) { ptype[3 * m + t] = t == 0 ? 0 : 1; smol[3 * m + t] = m; }
+    }
+    for (int q = 0; q < n_surf; q++) {
+        int m = n_water + q, g0 = 3 * n_water + NSURF * q;
+        mfirst[m] = g0; mkind[m] = 1; sm[q] = m;
+        for (int t = 0; t < NSURF; t++) { ptype[g0 + t] = (uint8_t)(2 + t); smol[g0 + t] = m; }
+    }
+    std::vector<double> axis;
+    for (int a = 0; a < 3; a++) axis_centres(R, a, axis);
+    if ((e = dalloc(c, &d.axis, axis.size()))) return e;
+    // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:187-216
+    std::vector<int> gstart(1, 0);
+    std::vector<double4> gpos;
+    double rcut = RC + sqrt(2.0) * RS / 2.0;
+    rcut *= rcut;
+    for (int iy = 0; iy < R.nc[1]; iy++)
+        for (int ix = 0; ix < R.nc[0]; ix++) {
+            double cx = axis[ix], cy = axis[R.nc[0] + iy];
+            for (int k = 0; k < n_carbon; k++) {
+                double dx = carbons[3 * k] - cx, dy = carbons[3 * k + 1] - cy;
+                if (dx * dx + dy * dy <= rcut) gpos.push_back(make_double4(carbons[3 * k], carbons[3 * k + 1], carbons[3 * k + 2], 0.0));
+            }
+            gstart.push_back((int)gpos.size());
+        }
+    if ((e = dalloc(c, &d.gcol_start, gstart.size())) || (e = dalloc(c, &d.gpos, gpos.size()))) return e;
+    // translation operators
+    std::vector<double2> ops((size_t)343 * LPH * LP, make_double2(0.0, 0.0));
+    auto fill_m2l = [&](double scale, double2 *dst) -> int {
+        for (int dz = -3; dz <= 3; dz++)
+            for (int dy = -3; dy <= 3; dy++)
+                for (int dx = -3; dx <= 3; dx++) {
+                    int oi = (dx + 3) + 7 * (dy + 3) + 49 * (dz + 3);
+                    if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+                    op_m2l(dx * scale, dy * scale, dz * scale, &ops[(size_t)oi * LPH * LP]);
+                }
+        CK(cudaMemcpyAsync(dst, ops.data(), ops.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        return 0;
+    };
+    if ((e = fill_m2l(RS, d.op_m2l4)) || (e = fill_m2l(2 * RS, d.op_m2l3))) return e;
+    {
+        std::vector<double2> o2((size_t)w2 * w2 * w2 * LPH * LP, make_double2(0.0, 0.0));
+        for (int dz = -c->d2; dz <= c->d2; dz++)
+            for (int dy = -c->d2; dy <= c->d2; dy++)
+                for (int dx = -c->d2; dx <= c->d2; dx++) {
+                    if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+                    int oi = (dx + c->d2) + w2 * ((dy + c->d2) + w2 * (dz + c->d2));
+                    op_m2l(dx * 4 * RS, dy * 4 * RS, dz * 4 * RS, &o2[(size_t)oi * LPH * LP]);
+                }
+        CK(cudaMemcpyAsync(d.op_m2l2, o2.data(), o2.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+        std::vector<double2> o8((size_t)8 * LPH * LP);
+        struct { double2 *dst; double s; int kind; } sets[4] = {
+            {d.op_m2m43, RS, 0}, {d.op_m2m32, 2 * RS, 0}, {d.op_l2l23, 2 * RS, 1}, {d.op_l2l34, RS, 1}};
+        for (auto &st : sets) {
+            for (int ch = 0; ch < 8; ch++) {
+                double v[3] = {(ch & 1) - 0.5, ((ch >> 1) & 1) - 0.5, ((ch >> 2) & 1) - 0.5};
+                if (st.kind == 0) op_m2m(v[0] * st.s, v[1] * st.s, v[2] * st.s, &o8[(size_t)ch * LPH * LP]);
+                else op_l2l(-v[0] * st.s, -v[1] * st.s, -v[2] * st.s, &o8[(size_t)ch * LPH * LP]);
+            }
+            CK(cudaMemcpyAsync(st.dst, o8.data(), o8.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+            CK(cudaStreamSynchronize(c->st));
+        }
+    }
+    std::vector<double2> ljt = make_lj_table();
+    std::vector<double> sx(N), sy(N), sz(N), vxa(N, 0.0), vya(N, 0.0), vza(N, 0.0);
+    for (int g = 0; g < N; g++) {
+        sx[g] = pos[3 * g]; sy[g] = pos[3 * g + 1]; sz[g] = pos[3 * g + 2];
+        if (vel) { vxa[g] = vel[3 * g]; vya[g] = vel[3 * g + 1]; vza[g] = vel[3 * g + 2]; }
+    }
+    std::vector<int> crep(C, 0), b3(c->n3, 0), b2(c->n2, 0);
+    double eta0 = 0.0;
+    CK(cudaMemcpyAsync(d.x, sx.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.y, sy.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.z, sz.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.vx, vxa.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.vy, vya.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.vz, vza.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.ptype, ptype.data(), N, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.smol, smol.data(), N * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.mrep, mrep.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.mfirst, mfirst.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.mkind, mkind.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    if (n_water) CK(cudaMemcpyAsync(c->wmols, wm.data(), n_water * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    if (n_surf) CK(cudaMemcpyAsync(c->smols, sm.data(), n_surf * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.rep, c->reps.data(), sizeof(Rep), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.eta, &eta0, sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.axis, axis.data(), axis.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.crep, crep.data(), C * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.b3rep, b3.data(), c->n3 * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.b2rep, b2.data(), c->n2 * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.gcol_start, gstart.data(), gstart.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    if (!gpos.empty()) CK(cudaMemcpyAsync(d.gpos, gpos.data(), gpos.size() * sizeof(double4), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.ljt, ljt.data(), ljt.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->h3.assign(3 * (size_t)N, 0.0);
+    c->uploaded = true;
+    c->have_force = false;
+    c->steps = 0;
+    return 0;
+}
+
+int sesp_download_state(sesp_ctx *c, double *pos, double *vel, double *acc) {
+    if (int e = check_ctx(c, true)) return e;
+    if (set_device(c)) return SESP_ECUDA;
+    int N = c->nsite;
+    std::vector<double> a(N), b(N), cc(N);
+    double *arrs[3][3] = {{c->d.x, c->d.y, c->d.z}, {c->d.vx, c->d.vy, c->d.vz}, {c->d.ax, c->d.ay, c->d.az}};
+    double *outs[3] = {pos, vel, acc};
+    for (int k = 0; k < 3; k++) {
+        if (!outs[k]) continue;
+        CK(cudaMemcpyAsync(a.data(), arrs[k][0], N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaMemcpyAsync(b.data(), arrs[k][1], N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaMemcpyAsync(cc.data(), arrs[k][2], N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        for (int g = 0; g < N; g++) { outs[k][3 * g] = a[g]; outs[k][3 * g + 1] = b[g]; outs[k][3 * g + 2] = cc[g]; }
+    }
+    return 0;
+}
+
+int sesp_set_state(sesp_ctx *c, const double *pos, const double *vel, const double *acc, double eta) {
+    if (int e = check_ctx(c, true)) return e;
+    if (set_device(c)) return SESP_ECUDA;
+    int N = c->nsite;
+    std::vector<double> a(N), b(N), cc(N);
+    double *arrs[3][3] = {{c->d.x, c->d.y, c->d.z}, {c->d.vx, c->d.vy, c->d.vz}, {c->d.ax, c->d.ay, c->d.az}};
+    const double *ins[3] = {pos, vel, acc};
+    for (int k = 0; k < 3; k++) {
+        if (!ins[k]) continue;
+        for (int g = 0; g < N; g++) { a[g] = ins[k][3 * g]; b[g] = ins[k][3 * g + 1]; cc[g] = ins[k][3 * g + 2]; }
+        CK(cudaMemcpyAsync(arrs[k][0], a.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(arrs[k][1], b.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(arrs[k][2], cc.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+    }
+    CK(cudaMemcpyAsync(c->d.eta, &eta, sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sesp_force_terms(sesp_ctx *c, int rebuild, int terms) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!rebuild && !c->have_force) return fail(SESP_ESTATE, "the first force call must rebuild the lists");
+    if (set_device(c)) return SESP_ECUDA;
+    seq_force(c, rebuild, terms);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+    collect_all(c);
+    c->have_force = true;
+    return 0;
+}
+
+int sesp_force(sesp_ctx *c, int rebuild) { return sesp_force_terms(c, rebuild, SESP_T_ALL); }
+
+int sesp_download_forces(sesp_ctx *c, double *f) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!f) return fail(SESP_EINVAL, "null output");
+    if (set_device(c)) return SESP_ECUDA;
+    int N = c->nsite;
+    std::vector<double> a(N), b(N), cc(N);
+    CK(cudaMemcpyAsync(a.data(), c->d.fx, N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(b.data(), c->d.fy, N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(cc.data(), c->d.fz, N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int g = 0; g < N; g++) { f[3 * g] = a[g]; f[3 * g + 1] = b[g]; f[3 * g + 2] = cc[g]; }
+    return 0;
+}
+
+int sesp_init_accel(sesp_ctx *c) {
+    if (int e = check_ctx(c, true)) return e;
+    if (set_device(c)) return SESP_ECUDA;
+    launch_init_accel(c->d, c->nsite, c->st);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sesp_move_a(sesp_ctx *c) {
+    if (int e = check_ctx(c, true)) return e;
+    if (set_device(c)) return SESP_ECUDA;
+    seq_move_a(c);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+    collect_all(c);
+    return 0;
+}
+
+int sesp_move_b(sesp_ctx *c) {
+    if (int e = check_ctx(c, true)) return e;
+    if (set_device(c)) return SESP_ECUDA;
+    seq_move_b(c);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+    collect_all(c);
+    return 0;
+}
+
+static int launch_steps(sesp_ctx *c, int kb0, int nsteps) {
+    if (int e = check_ctx(c, true)) return e;
+    if (nsteps < 0) return fail(SESP_EINVAL, "negative step count");
+    if (set_device(c)) return SESP_ECUDA;
+    for (int k = 0; k < nsteps; k++) {
+        int kb = kb0 + k;
+        int rb = (kb % c->p.rebuild_interval == 0) || !c->have_force;
+        if (c->timing) {
+            seq_move_a(c);
+            seq_force(c, rb, SESP_T_ALL);
+            seq_move_b(c);
+            collect_all(c);
+        } else {
+            cudaGraphExec_t &ge = c->g_step[rb];
+            if (!ge) {
+                cudaGraph_t g;
+                CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+                seq_move_a(c);
+                seq_force(c, rb, SESP_T_ALL);
+                seq_move_b(c);
+                CK(cudaStreamEndCapture(c->st, &g));
+                CK(cudaGraphInstantiate(&ge, g, 0));
+                cudaGraphDestroy(g);
+            }
+            CK(cudaGraphLaunch(ge, c->st));
+        }
+        c->have_force = true;
+        c->steps++;
+    }
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int sesp_step(sesp_ctx *c, int kb) {
+    int e = launch_steps(c, kb, 1);
+    if (e) return e;
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sesp_run(sesp_ctx *c, int kb0, int nsteps) {
+    int e = launch_steps(c, kb0, nsteps);
+    if (e) return e;
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sesp_run_async(sesp_ctx *c, int kb0, int nsteps) { return launch_steps(c, kb0, nsteps); }
+
+int sesp_sync(sesp_ctx *c) {
+    if (int e = check_ctx(c, false)) return e;
+    if (set_device(c)) return SESP_ECUDA;
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sesp_temperature(sesp_ctx *c, double *t) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!t) return fail(SESP_EINVAL, "null output");
+    int N = c->nsite;
+    std::vector<double> v(3 * (size_t)N);
+    if (int e = sesp_download_state(c, nullptr, v.data(), nullptr)) return e;
+    Tables T = make_tables();
+    double s = 0.0;
+    for (int g = 0; g < N; g++) {
+        int pt = g < 3 * c->nwm ? (g % 3 == 0 ? 0 : 1) : 2 + (g - 3 * c->nwm) % NSURF;
+        s += T.mass[pt] * (v[3 * g] * v[3 * g] + v[3 * g + 1] * v[3 * g + 1] + v[3 * g + 2] * v[3 * g + 2]);
+    }
+    int np = N, nc = 3 * c->nwm + NBOND * c->nsm;
+    *t = s / (DT * DT) / (3 * np - nc);
+    return 0;
+}
+
+int sesp_get_eta(sesp_ctx *c, double *eta) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!eta) return fail(SESP_EINVAL, "null output");
+    CK(cudaMemcpyAsync(eta, c->d.eta, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sesp_set_eta(sesp_ctx *c, double eta) {
+    if (int e = check_ctx(c, true)) return e;
+    CK(cudaMemcpyAsync(c->d.eta, &eta, sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sesp_energies(sesp_ctx *c, double out[8]) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    if (!c->have_force) return fail(SESP_ESTATE, "energies need a force call first (lists and expansions)");
+    if (set_device(c)) return SESP_ECUDA;
+    int N = c->nsite;
+    double *es = nullptr, *ei = nullptr, *em = nullptr;
+    CK(cudaMalloc(&es, 3 * sizeof(double) * N));
+    CK(cudaMalloc(&ei, 3 * sizeof(double) * N));
+    CK(cudaMalloc(&em, 3 * sizeof(double) * (c->nsm + 1)));
+    cudaMemsetAsync(es, 0, 3 * sizeof(double) * N, c->st);
+    launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
+    launch_energies(c->d, c->ncell, N, c->smols, c->nsm, es, ei, em, c->st);
+    std::vector<double> hs(3 * (size_t)N), hi(3 * (size_t)N), hm(3 * (size_t)(c->nsm + 1));
+    cudaMemcpyAsync(hs.data(), es, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    cudaMemcpyAsync(hi.data(), ei, hi.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    cudaMemcpyAsync(hm.data(), em, 3 * sizeof(double) * c->nsm, cudaMemcpyDeviceToHost, c->st);
+    cudaError_t err = cudaStreamSynchronize(c->st);
+    cudaFree(es); cudaFree(ei); cudaFree(em);
+    if (err != cudaSuccess) return fail(SESP_ECUDA, "energies: %s", cudaGetErrorString(err));
+    for (int k = 0; k < 8; k++) out[k] = 0.0;
+    for (int s = 0; s < N; s++) { out[0] += hs[3 * s]; out[1] += hs[3 * s + 1]; out[2] += hs[3 * s + 2]; }
+    for (int q = 0; q < c->nsm; q++) { out[4] += hm[3 * q]; out[3] += hm[3 * q + 1]; out[2] += hm[3 * q + 2]; }
+    for (int g = 0; g < N; g++) { out[5] += hi[3 * g]; out[6] += hi[3 * g + 1]; out[7] += hi[3 * g + 2]; }
+    return 0;
+}
+
+int sesp_counters(sesp_ctx *c, int64_t out[8]) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    unsigned long long h[8];
+    CK(cudaMemcpyAsync(h, c->d.counters, sizeof h, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int k = 0; k < 8; k++) out[k] = (int64_t)h[k];
+    out[3] = c->steps;
+    out[4] = (int64_t)h[3];
+    return 0;
+}
+
+int sesp_kernel_times(sesp_ctx *c, double out[8], int reset) {
+    if (int e = check_ctx(c, false)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    for (int k = 0; k < 8; k++) out[k] = c->t_n[k] ? c->t_acc[k] / c->t_n[k] : 0.0;
+    if (reset) for (int k = 0; k < 8; k++) { c->t_acc[k] = 0.0; c->t_n[k] = 0; }
+    return 0;
+}
+
+int sesp_enable_timing(sesp_ctx *c, int on) {
+    if (int e = check_ctx(c, false)) return e;
+    c->timing = on != 0;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// Internal definitions of the GB300 engine (sm_103a).
+//
+// Device layout (one context may hold several replica systems back to back):
+//  * sites in the reference's order per replica (waters O,H,H, then 29-site
+//    surfactants); FP64 structure-of-arrays positions, velocities,
+//    accelerations and forces;
+//  * L4 cells of rs = 12 A, flat over replicas; every rebuild sorts the sites
+//    by the cell they sit in (the reference's "Central" test) into contiguous
+//    slots, which the pair kernel reads cell by cell;
+//  * multipole and local expansions (25 complex coefficients, order 4) per
+//    L4, L3 and L2 box.
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+#include <cuda_runtime.h>
+
+#include "../../include/sesp.h"
+
+namespace sesp {
+
+constexpr int P = 4;
+constexpr int LP = 25;        // (P+1)^2 coefficients
+constexpr int LPH = 15;       // coefficients with m >= 0
+constexpr int NTYPE = 31;     // 0 water O, 1 water H, 2..30 surfactant sites 1..29
+constexpr int NSURF = 29;
+constexpr int NBOND = 28;
+constexpr int NANGLE = 36;
+constexpr int NDIH = 30;
+constexpr int NSELF = 42;
+constexpr int NM2L = 316;     // 7^3 - 3^3 source offsets at L4 and L3
+
+// reduced-unit constants of src/mybox.cmns:36-44 (xpi is a single-precision
+// literal in the reference, hence the float)
+constexpr double SIGMA = 3.166;
+constexpr double EPSILON = 650.2;
+constexpr double RC = 10.0 / 3.166;
+constexpr double RS = 10.0 / 3.166 + 2.0 / 3.166;
+constexpr double XPI = (double)675.05f;
+constexpr double DT = 0.00127362;
+constexpr double DTSQ2 = 0.00127362 * 0.00127362 / 2.0;
+
+struct Rep {
+    int nc[3];        // L4 cells per axis
+    int nr[3];        // L2 boxes (4^3 L4 cells each) per axis
+    int cell0;        // first L4 cell
+    int l3_0, l2_0;   // first L3 / L2 box
+    int site0, nsite; // sites
+    int mol0, nmol;   // molecules
+    int nw, ns;       // waters, surfactants
+    int axis0;        // offset of this replica's cell-centre tables (x, then y, then z)
+    int gcol0;        // first bottom-layer column of the carbon lists
+    int graphite_on;
+    int m2l2_base;    // first L2 translation operator of this replica
+    int pad;
+    double rhs[3], rsd[3];
+    double pnh1, pnh2;
+};
+
+// constant topology and force-field tables (reference values, src/init_arrays.f90)
+struct Tables {
+    double q[NTYPE];          // charges
+    double mass[NTYPE];       // masses / m_O
+    int bi[NBOND], bj[NBOND]; // surfactant constraints (0-based sites)
+    double dsqs[NBOND];
+    double dsqw[3];
+    int ai[NANGLE], aj[NANGLE], ak[NANGLE];
+    double th[NANGLE], rkth[NANGLE];
+    int di[NDIH], dj[NDIH], dk[NDIH], dl[NDIH];
+    double dva[NDIH], dvb[NDIH], dvc[NDIH];
+    int si[NSELF], sj[NSELF];
+    double sgcs6[NSURF], epcs[NSURF];   // carbon - surfactant site LJ
+    double sgcw6, epcw;                 // carbon - water O LJ
+    double rfctr[LP];                   // sqrt((n-|m|)!/(n+|m|)!) by coefficient
+};
+
+struct Dev {
+    // sites
+    double *x, *y, *z, *vx, *vy, *vz, *ax, *ay, *az, *fx, *fy, *fz;
+    uint8_t *ptype;
+    int *smol;
+    // molecules
+    int *mrep, *mfirst, *mkind, *mkey, *mw1;
+    double *ke;          // [2 * nmol]: sum m v^2 before / after SHAKE
+    int *mfail;
+    // replicas
+    Rep *rep;
+    double *eta;         // [nrep]
+    double *axis;        // cell centre tables
+    // cells
+    int *crep, *b3rep, *b2rep;
+    int *cstart, *ccount, *cfill;
+    int *sloc, *sslot;
+    int *srt_site;
+    double4 *srt_pos;    // x, y, z, q in slot order (FP64)
+    float4 *srt_pos32;   // x, y, z relative to the slot's own cell centre, q (mixed)
+    int2 *srt_meta;      // molecule, type
+    double *nf;          // near + far force by slot [3 * nslot]
+    // graphite columns of the bottom layer
+    int *gcol_start;
+    double4 *gpos;
+    // intramolecular correction lists (bit k: site k+1 of the molecule)
+    uint32_t *isub;
+    // multipoles / local expansions (double2 = complex)
+    double2 *O4, *L4, *O3, *L3, *O2, *L2;
+    double2 *op_m2l4, *op_m2l3, *op_m2l2, *op_m2m43, *op_m2m32, *op_l2l23, *op_l2l34;
+    int *m2l2_off;       // per replica: (2nr-1)^3 index map to operators
+    // LJ pair table (eps, sg6), NTYPE^2
+    double2 *ljt;
+    float2 *ljt32;
+    // counters: [0] fails, [1] overflow, [2] unlocated, [3] max cell, [5] pairs, [6] LJ pairs
+    unsigned long long *counters;
+    int max_cell;
+};
+
+
+// ---------------------------------------------------------------- helpers
+__host__ __device__ inline int cell_index(const Rep &r, int ix, int iy, int iz) {
+    return r.cell0 + ix + r.nc[0] * (iy + r.nc[1] * iz);
+}
+
+}  // namespace sesp

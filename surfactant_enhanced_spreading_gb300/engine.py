@@ -1,0 +1,223 @@
+"""Host side of the GB300 engine: a ctypes binding of ``libsesp.so``.
+
+It mirrors the reference driver's call surface (src/mybox.f90): the force
+section (``force``), the velocity-Verlet halves (``move_a`` / ``move_b``, which
+stand for move_surfactant_a + move_w1_a + move_w2_a and their ``_b``
+counterparts), ``init_accel`` and ``temperature``, plus the step loop.  There
+is no CPU fallback: constructing an :class:`Engine` without the compiled
+library or without a CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libsesp.so")
+
+PLAIN_FP64 = 0
+MIXED = 1
+
+T_NEAR, T_FAR, T_VALENCE, T_DIHEDRAL, T_BERENDSEN = 1, 2, 4, 8, 16
+T_INTERNAL, T_SUBTRACT, T_WALL, T_GRAPHITE, T_ALL = 32, 64, 128, 256, 511
+
+ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ESTATE", 5: "ECAPACITY", 6: "ESHAKE", 7: "EBUDGET"}
+
+# exported symbols of include/sesp.h
+SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_create", "sesp_destroy",
+           "sesp_upload_state", "sesp_download_state", "sesp_set_state", "sesp_force", "sesp_force_terms",
+           "sesp_download_forces", "sesp_init_accel", "sesp_move_a", "sesp_move_b", "sesp_step", "sesp_run",
+           "sesp_run_async", "sesp_sync", "sesp_temperature", "sesp_get_eta", "sesp_set_eta", "sesp_energies",
+           "sesp_counters", "sesp_kernel_times", "sesp_enable_timing"]
+
+
+class SespError(RuntimeError):
+    pass
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("n_cells", ctypes.c_int * 3), ("precision", ctypes.c_int), ("rebuild_interval", ctypes.c_int),
+                ("graphite_on", ctypes.c_int), ("tr", ctypes.c_double), ("tau_steps", ctypes.c_double),
+                ("shake_tol", ctypes.c_double), ("shake_maxit", ctypes.c_int), ("device", ctypes.c_int),
+                ("max_cell_sites", ctypes.c_int)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the engine library; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise SespError(f"engine library not built: {path} (run __graft_entry__.build())")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    dp = ctypes.POINTER(ctypes.c_double)
+    L.sesp_abi_version.restype = ctypes.c_int
+    L.sesp_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+    L.sesp_default_params.argtypes = [ctypes.POINTER(Params)]
+    L.sesp_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(P)]
+    L.sesp_destroy.argtypes = [P]
+    L.sesp_upload_state.argtypes = [P, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int, dp]
+    L.sesp_download_state.argtypes = [P, dp, dp, dp]
+    L.sesp_set_state.argtypes = [P, dp, dp, dp, ctypes.c_double]
+    L.sesp_force.argtypes = [P, ctypes.c_int]
+    L.sesp_force_terms.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    L.sesp_download_forces.argtypes = [P, dp]
+    for n in ["sesp_init_accel", "sesp_move_a", "sesp_move_b", "sesp_sync"]:
+        getattr(L, n).argtypes = [P]
+    L.sesp_step.argtypes = [P, ctypes.c_int]
+    L.sesp_run.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    L.sesp_run_async.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    L.sesp_temperature.argtypes = [P, dp]
+    L.sesp_get_eta.argtypes = [P, dp]
+    L.sesp_set_eta.argtypes = [P, ctypes.c_double]
+    L.sesp_energies.argtypes = [P, dp]
+    L.sesp_counters.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+    L.sesp_kernel_times.argtypes = [P, dp, ctypes.c_int]
+    L.sesp_enable_timing.argtypes = [P, ctypes.c_int]
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != 0:
+        buf = ctypes.create_string_buffer(512)
+        _lib.sesp_last_error(buf, 512)
+        raise SespError(f"{ERRORS.get(rc, rc)}: {buf.value.decode(errors='replace')}")
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def default_params(cells=(12, 12, 12), precision=PLAIN_FP64, **kw) -> Params:
+    L = load()
+    p = Params()
+    _check(L.sesp_default_params(ctypes.byref(p)))
+    for a in range(3):
+        p.n_cells[a] = int(cells[a])
+    p.precision = int(precision)
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Engine:
+    """One system on one GPU, driven through the C ABI."""
+
+    def __init__(self, system, precision=PLAIN_FP64, device=0, **kw):
+        L = load()
+        self.system = system
+        p = default_params(system.cells, precision, device=device, graphite_on=int(system.graphite_on), **kw)
+        h = ctypes.c_void_p()
+        _check(L.sesp_create(ctypes.byref(p), ctypes.byref(h)))
+        self._h = h
+        self.n = system.n_sites
+        pos = np.ascontiguousarray(system.pos, dtype=np.float64)
+        vel = np.ascontiguousarray(system.vel, dtype=np.float64)
+        carb = np.ascontiguousarray(system.carbons, dtype=np.float64).reshape(-1, 3)
+        nc = carb.shape[0]
+        if nc == 0:
+            carb = np.zeros((1, 3))
+        _check(L.sesp_upload_state(self._h, system.n_water, system.n_surf, _dp(pos), _dp(vel), nc, _dp(carb)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.sesp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # reference driver surface
+    def force(self, rebuild=True, terms=T_ALL):
+        _check(_lib.sesp_force_terms(self._h, int(rebuild), int(terms)))
+        return self.forces()
+
+    def forces(self):
+        f = np.empty((self.n, 3))
+        _check(_lib.sesp_download_forces(self._h, _dp(f)))
+        return f
+
+    def init_accel(self):
+        _check(_lib.sesp_init_accel(self._h))
+
+    def move_a(self):
+        _check(_lib.sesp_move_a(self._h))
+
+    def move_b(self):
+        _check(_lib.sesp_move_b(self._h))
+
+    def step(self, kb):
+        _check(_lib.sesp_step(self._h, int(kb)))
+
+    def run(self, kb0, nsteps):
+        _check(_lib.sesp_run(self._h, int(kb0), int(nsteps)))
+
+    def run_async(self, kb0, nsteps):
+        _check(_lib.sesp_run_async(self._h, int(kb0), int(nsteps)))
+
+    def sync(self):
+        _check(_lib.sesp_sync(self._h))
+
+    def state(self):
+        pos, vel, acc = (np.empty((self.n, 3)) for _ in range(3))
+        _check(_lib.sesp_download_state(self._h, _dp(pos), _dp(vel), _dp(acc)))
+        return pos, vel, acc
+
+    def set_state(self, pos=None, vel=None, acc=None, eta=0.0):
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64) for a in (pos, vel, acc)]
+        ptrs = [None if a is None else _dp(a) for a in arrs]
+        _check(_lib.sesp_set_state(self._h, *ptrs, float(eta)))
+
+    def temperature(self):
+        t = ctypes.c_double()
+        _check(_lib.sesp_temperature(self._h, ctypes.byref(t)))
+        return t.value
+
+    @property
+    def eta(self):
+        v = ctypes.c_double()
+        _check(_lib.sesp_get_eta(self._h, ctypes.byref(v)))
+        return v.value
+
+    @eta.setter
+    def eta(self, v):
+        _check(_lib.sesp_set_eta(self._h, float(v)))
+
+    def energies(self):
+        out = np.empty(8)
+        _check(_lib.sesp_energies(self._h, _dp(out)))
+        return out
+
+    def counters(self):
+        out = (ctypes.c_int64 * 8)()
+        _check(_lib.sesp_counters(self._h, out))
+        return list(out)
+
+    def enable_timing(self, on=True):
+        _check(_lib.sesp_enable_timing(self._h, int(on)))
+
+    def kernel_times(self, reset=False):
+        out = np.empty(8)
+        _check(_lib.sesp_kernel_times(self._h, _dp(out), int(reset)))
+        return out
+
+
+def mybox_start(engine: Engine):
+    """Start-up force evaluation and accelerations (src/mybox.f90:65-128)."""
+    engine.force(rebuild=True)
+    engine.init_accel()
+
+
+def mybox_loop(engine: Engine, kb0: int, nsteps: int):
+    """The step loop src/mybox.f90:130-241 (rebuild every 10th kb)."""
+    engine.run(kb0, nsteps)

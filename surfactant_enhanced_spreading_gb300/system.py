@@ -1,0 +1,269 @@
+"""Seeded synthetic systems in the reference's reduced units.
+
+The reference reads its initial state from ``data_cont2.dat`` (alternating
+position / velocity lines, waters O,H,H first, then 29-site surfactants,
+src/read_config.f90:16-38) and its carbons from ``graphite.dat``
+(src/read_graphite.f90:179-216), neither of which ships with it.  This module
+builds such states from a seed:
+
+* a hemispherical droplet of rigid 3-site waters (O-H 1 A, H-O-H 109.47 deg,
+  the constraint lengths of src/init_arrays.f90:566-574) on a seed-jittered
+  cubic lattice at 0.0334 molecules per cubic Angstrom, random orientations;
+* 29-site trisiloxane surfactants built on the bond graph of
+  src/init_arrays.f90:229-264 with the exact constraint lengths of
+  src/init_arrays.f90:509-565, placed at the droplet surface;
+* an AB-stacked graphite sheet (C-C 1.421 A, 3.41 A layer spacing, the
+  lattice of src/make_graphite.f90:18-80) of any number of layers;
+* Maxwell velocities at the reference's target temperature tr = 3.81087
+  (src/mybox.f90:48), stored as displacements per step.
+
+Positions are in sigma = 3.166 A, the box is centred on the origin and spans
+``n_cells * rs`` per axis with ``rs = 12 A`` (src/mybox.cmns:38-40,
+src/init_box_dimensions.f90:14-20).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+SIGMA = 3.166
+EPSILON = 650.2
+RC = 10.0 / SIGMA
+RS = 10.0 / SIGMA + 2.0 / SIGMA
+DT = 0.00127362
+TR = 3.81087
+N_SURF_SITE = 29
+
+# bond graph of the 29-site surfactant (1-based), src/init_arrays.f90:229-264
+SURF_BONDS = [(i, i + 1) for i in range(1, 19)] + [
+    (18, 20), (20, 21), (21, 22), (21, 23), (21, 24), (18, 25), (25, 26), (26, 27), (26, 28), (26, 29)]
+# constraint lengths in Angstrom by bond index, src/init_arrays.f90:509-565
+SURF_BOND_LEN = [0.945, 1.430, 1.516, 1.410, 1.410, 1.516, 1.410, 1.410, 1.516, 1.410, 1.410, 1.516,
+                 1.410, 1.410, 1.516, 1.540, 1.88, 1.88, 1.60, 1.60, 1.88, 1.88, 1.88, 1.60, 1.60,
+                 1.88, 1.88, 1.88]
+# masses relative to oxygen, src/init_arrays.f90:266-312
+_HY, _C, _O, _SI = 1.00794, 12.011, 15.9994, 28.0855
+_ME, _METHYL = _C + 2 * _HY, _C + 3 * _HY
+SURF_MASS = np.array([_HY, _O, _ME, _ME, _O, _ME, _ME, _O, _ME, _ME, _O, _ME, _ME, _O, _ME, _ME, _ME,
+                      _SI, _METHYL, _O, _SI, _METHYL, _METHYL, _METHYL, _O, _SI, _METHYL, _METHYL,
+                      _METHYL]) / _O
+WATER_MASS = np.array([_O, _HY, _HY]) / _O
+WATER_HH = 2.0 * math.sin(109.47 * math.pi / 180.0 / 2.0)   # Angstrom
+
+
+@dataclasses.dataclass
+class System:
+    """A state in reference order: ``pos``/``vel`` are (n_sites, 3) float64."""
+
+    n_water: int
+    n_surf: int
+    cells: tuple          # (ncx, ncy, ncz) L4 cells, multiples of 4
+    pos: np.ndarray
+    vel: np.ndarray
+    carbons: np.ndarray   # (n_c, 3) float64
+    graphite_on: bool = True
+
+    @property
+    def n_sites(self) -> int:
+        return 3 * self.n_water + N_SURF_SITE * self.n_surf
+
+    @property
+    def half_box(self) -> np.ndarray:
+        return np.array(self.cells, dtype=np.float64) * RS / 2.0
+
+    def masses(self) -> np.ndarray:
+        return np.concatenate([np.tile(WATER_MASS, self.n_water), np.tile(SURF_MASS, self.n_surf)])
+
+    def copy(self) -> "System":
+        return dataclasses.replace(self, pos=self.pos.copy(), vel=self.vel.copy(), carbons=self.carbons.copy())
+
+
+def _rand_rot(rng):
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    a, b, c, d = q
+    return np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
+                     [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                     [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
+
+
+def water_template() -> np.ndarray:
+    """O, H, H in Angstrom with O at the origin."""
+    half = 109.47 * math.pi / 180.0 / 2.0
+    return np.array([[0.0, 0.0, 0.0], [math.sin(half), 0.0, math.cos(half)],
+                     [-math.sin(half), 0.0, math.cos(half)]])
+
+
+def surfactant_template(rng, tries: int = 200) -> np.ndarray:
+    """29 sites in Angstrom satisfying every constraint length exactly.
+
+    Sites are placed along the bond tree from site 1 with near-tetrahedral
+    bond angles and random dihedrals, rejecting placements that come closer
+    than 2.6 A to a site three or more bonds away.
+    """
+    adj = {i: [] for i in range(1, 30)}
+    blen = {}
+    for b, (i, j) in enumerate(SURF_BONDS):
+        adj[i].append(j)
+        adj[j].append(i)
+        blen[(i, j)] = blen[(j, i)] = SURF_BOND_LEN[b]
+    # bond-graph distances for the clash test
+    dist = np.full((30, 30), 99, dtype=int)
+    for s in range(1, 30):
+        dist[s, s] = 0
+        frontier = [s]
+        while frontier:
+            nxt = []
+            for u in frontier:
+                for v in adj[u]:
+                    if dist[s, v] > dist[s, u] + 1:
+                        dist[s, v] = dist[s, u] + 1
+                        nxt.append(v)
+            frontier = nxt
+    for _ in range(tries):
+        pos = {1: np.zeros(3)}
+        parent = {1: None}
+        order = [1]
+        ok = True
+        k = 0
+        while k < len(order) and ok:
+            u = order[k]
+            k += 1
+            for v in adj[u]:
+                if v in pos:
+                    continue
+                for _attempt in range(60):
+                    p = parent[u]
+                    if p is None:
+                        d = rng.normal(size=3)
+                    else:
+                        b1 = pos[u] - pos[p]
+                        b1 /= np.linalg.norm(b1)
+                        perp = np.cross(b1, rng.normal(size=3))
+                        perp /= np.linalg.norm(perp)
+                        ang = math.radians(rng.uniform(105.0, 118.0))
+                        d = math.cos(math.pi - ang) * b1 + math.sin(math.pi - ang) * perp
+                    d /= np.linalg.norm(d)
+                    cand = pos[u] + blen[(u, v)] * d
+                    clash = any(dist[v, w] >= 3 and np.linalg.norm(cand - pw) < 2.6 for w, pw in pos.items())
+                    if not clash:
+                        break
+                else:
+                    ok = False
+                    break
+                pos[v] = cand
+                parent[v] = u
+                order.append(v)
+        if ok and len(pos) == 29:
+            return np.array([pos[i] for i in range(1, 30)])
+    raise RuntimeError("could not build a clash-free surfactant")
+
+
+def graphite(layers: int, half_x: float, half_y: float, z_top: float) -> np.ndarray:
+    """AB-stacked graphite (Angstrom in, Angstrom out) covering |x|<half_x, |y|<half_y."""
+    cc = 1.421
+    a1 = np.array([1.5 * cc, math.sqrt(3) / 2 * cc])
+    a2 = np.array([1.5 * cc, -math.sqrt(3) / 2 * cc])
+    basis = [np.zeros(2), np.array([cc, 0.0])]
+    n = int(2 * max(half_x, half_y) / cc) + 4
+    out = []
+    for layer in range(layers):
+        shift = np.array([cc, 0.0]) if layer % 2 else np.zeros(2)
+        z = z_top - 3.41 * layer
+        for i in range(-n, n + 1):
+            for j in range(-n, n + 1):
+                for b in basis:
+                    p = i * a1 + j * a2 + b + shift
+                    if abs(p[0]) < half_x and abs(p[1]) < half_y:
+                        out.append((p[0], p[1], z))
+    return np.array(out, dtype=np.float64)
+
+
+def maxwell(masses: np.ndarray, rng, temperature: float = TR) -> np.ndarray:
+    """Velocities as displacements per step at a reduced temperature."""
+    v = rng.normal(size=(masses.size, 3)) * np.sqrt(temperature / masses)[:, None]
+    return v * DT
+
+
+def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graphite_layers: int = 2,
+            graphite_extent: float | None = None, temperature: float = TR) -> System:
+    """Hemispherical droplet on graphite in a closed box of ``cells`` L4 cells.
+
+    The top carbon layer sits 4 A above the lower wall, inside the bottom
+    layer of cells, so the graphite term (bottom cells only,
+    src/eval_graphite.f90:72-74) acts on the first water layer.
+    """
+    rng = np.random.default_rng(seed)
+    cells = tuple(int(c) for c in cells)
+    half = np.array(cells, dtype=np.float64) * RS * SIGMA / 2.0          # Angstrom
+    z_graph = -half[2] + 4.0
+    z_base = z_graph + 3.2
+    density = 0.0334
+    radius = (3.0 * n_water / (2.0 * math.pi * density)) ** (1.0 / 3.0)
+    a = density ** (-1.0 / 3.0)
+    nlat = int(radius / a) + 3
+    pts = []
+    for i in range(-nlat, nlat + 1):
+        for j in range(-nlat, nlat + 1):
+            for k in range(0, nlat + 1):
+                p = np.array([i * a, j * a, k * a]) + rng.uniform(-0.15, 0.15, size=3) * a
+                if p[2] < 0.0:
+                    p[2] = -p[2]
+                if np.linalg.norm(p) <= radius * 1.15:
+                    pts.append(p)
+    pts = np.array(pts)
+    pts = pts[np.argsort(np.linalg.norm(pts, axis=1), kind="stable")]
+    surf_sites = []
+    if n_surf:
+        for _ in range(n_surf):
+            tmpl = surfactant_template(rng)
+            tmpl -= tmpl.mean(axis=0)
+            for _t in range(200):
+                rot = _rand_rot(rng)
+                u = rng.normal(size=3)
+                u[2] = abs(u[2])
+                u /= np.linalg.norm(u)
+                centre = u * (radius + 2.0)
+                centre[2] = max(centre[2], 8.0)
+                cand = tmpl @ rot.T + centre
+                if cand[:, 2].min() < 2.0:
+                    continue
+                if any(np.min(np.linalg.norm(cand[:, None, :] - s[None, :, :], axis=2)) < 3.5 for s in surf_sites):
+                    continue
+                surf_sites.append(cand)
+                break
+            else:
+                raise RuntimeError("could not place surfactant")
+    # waters: keep lattice points clear of surfactant sites
+    if surf_sites:
+        allsurf = np.concatenate(surf_sites)
+        keep = np.array([np.min(np.linalg.norm(allsurf - p, axis=1)) > 3.0 for p in pts])
+        pts = pts[keep]
+    if len(pts) < n_water:
+        raise RuntimeError("lattice too small for the droplet")
+    pts = pts[:n_water]
+    wt = water_template()
+    wat = np.empty((n_water, 3, 3))
+    for m in range(n_water):
+        wat[m] = wt @ _rand_rot(rng).T + pts[m]
+    pos = [wat.reshape(-1, 3)]
+    if surf_sites:
+        pos.append(np.concatenate(surf_sites))
+    pos = np.concatenate(pos)
+    pos[:, 2] += z_base
+    if np.any(np.abs(pos[:, :2]) > half[:2] - 1.0) or np.any(pos[:, 2] > half[2] - 1.0):
+        raise RuntimeError("droplet does not fit the box; use more cells")
+    ext = graphite_extent if graphite_extent is not None else min(half[0], 2.5 * radius)
+    carb = graphite(graphite_layers, min(ext, half[0]), min(ext, half[1]), z_graph) if graphite_layers else np.zeros((0, 3))
+    masses = np.concatenate([np.tile(WATER_MASS, n_water), np.tile(SURF_MASS, n_surf)])
+    vel = maxwell(masses, rng, temperature)
+    return System(n_water=n_water, n_surf=n_surf, cells=cells, pos=pos / SIGMA, vel=vel,
+                  carbons=carb / SIGMA, graphite_on=bool(graphite_layers))
+
+
+def reference_box_system(seed: int = 0) -> System:
+    """The reference's production size: 9,997 waters and 475 surfactants in the
+    12 x 12 x 12-cell walled cube (src/mybox.cmns:55-60)."""
+    return droplet(9997, 475, cells=(12, 12, 12), seed=seed)

@@ -1,0 +1,91 @@
+"""Physical checks of the oracle: finite-difference energies for every term,
+far-field accuracy against the direct Coulomb sum, SHAKE/RATTLE constraint
+residuals.  CPU only."""
+import numpy as np
+import pytest
+
+import oracle as O
+from surfactant_enhanced_spreading_gb300 import system as S
+
+
+def _energy_terms(o):
+    e = o.energies()
+    return e
+
+
+@pytest.mark.parametrize("term,idx", [(O.TERM_VALENCE | O.TERM_DIHEDRAL | O.TERM_BERENDSEN, [4]),
+                                      (O.TERM_INTERNAL, [3]), (O.TERM_WALL, [5]), (O.TERM_GRAPHITE, [6])])
+def test_finite_difference_intra_terms(term, idx):
+    s = S.droplet(60, 2, cells=(4, 4, 4), seed=11)
+    o = O.Oracle(s)
+    o.force(True, O.TERM_ALL)  # build lists
+    f = o.force(False, term)
+    pos0 = o.get(0)
+    rng = np.random.default_rng(0)
+    h = 1e-6
+    for g in rng.choice(s.n_sites, 6, replace=False):
+        for a in range(3):
+            p = pos0.copy(); p[g, a] += h; o.set(0, p); ep = o.energies()[idx].sum()
+            p = pos0.copy(); p[g, a] -= h; o.set(0, p); em = o.energies()[idx].sum()
+            fd = -(ep - em) / (2 * h)
+            assert abs(fd - f[g, a]) <= 1e-5 * max(1.0, abs(f[g, a])), (g, a, fd, f[g, a])
+    o.set(0, pos0)
+
+
+def test_finite_difference_near_field():
+    s = S.droplet(80, 1, cells=(4, 4, 4), seed=12)
+    o = O.Oracle(s)
+    f = o.force(True, O.TERM_NEAR)
+    pos0 = o.get(0)
+    rng = np.random.default_rng(1)
+    h = 1e-6
+    for g in rng.choice(s.n_sites, 6, replace=False):
+        for a in range(3):
+            p = pos0.copy(); p[g, a] += h; o.set(0, p); ep = o.energies()[:2].sum()
+            p = pos0.copy(); p[g, a] -= h; o.set(0, p); em = o.energies()[:2].sum()
+            fd = -(ep - em) / (2 * h)
+            assert abs(fd - f[g, a]) <= 1e-5 * max(1.0, abs(f[g, a])), (g, a, fd, f[g, a])
+    o.set(0, pos0)
+
+
+def test_far_field_matches_direct_coulomb():
+    """FMA far field (p = 4, 3 levels) against the direct Coulomb sum over
+    the pairs outside the near shell: the publication's <1% RMS claim."""
+    s = S.droplet(1200, 0, cells=(8, 8, 8), seed=13, graphite_layers=0)
+    o = O.Oracle(s)
+    f_far = o.force(True, O.TERM_FAR)
+    loc = o.located()
+    pos = o.get(0)
+    q = np.tile([-0.8476, 0.4238, 0.4238], s.n_water)
+    xpi = float(np.float32(675.05))
+    ncx, ncy, ncz = s.cells
+    c = np.stack([loc % ncx, (loc // ncx) % ncy, loc // (ncx * ncy)], 1)
+    d = pos[:, None, :] - pos[None, :, :]
+    r2 = (d ** 2).sum(-1)
+    far = (np.abs(c[:, None, :] - c[None, :, :]) > 1).any(-1)
+    np.fill_diagonal(r2, 1.0)
+    w = np.where(far, q[None, :] / r2 ** 1.5, 0.0)
+    f_dir = xpi * q[:, None] * (d * w[..., None]).sum(1)
+    f_near = o.force(False, O.TERM_NEAR)
+    err_far = np.sqrt(((f_far - f_dir) ** 2).sum() / (f_dir ** 2).sum())
+    err_tot = np.sqrt(((f_far - f_dir) ** 2).sum() / ((f_near + f_dir) ** 2).sum())
+    assert err_far < 5e-2      # order-4 expansion of the far part alone
+    assert err_tot < 1e-2      # RMS error of the electrostatic force
+
+
+def test_shake_rattle_residuals():
+    s = S.droplet(200, 3, cells=(8, 8, 4), seed=14)
+    o = O.Oracle(s)
+    o.force(True)
+    o.init_accel()
+    o.run(1, 5)
+    pos = o.get(0) * S.SIGMA
+    vel = o.get(1)
+    w = pos[:600].reshape(200, 3, 3)
+    d = np.linalg.norm(w[:, 1] - w[:, 0], axis=1)
+    assert np.abs(d - 1.0).max() < 2e-4 * 1.0 + 1e-12   # tolerance tol = 1e-4 on squared lengths
+    vw = vel[:600].reshape(200, 3, 3)
+    rv = ((w[:, 1] - w[:, 0]) / S.SIGMA * (vw[:, 1] - vw[:, 0])).sum(1)
+    assert np.abs(rv).max() < 1e-3 * S.DT
+    assert o.fail_count() == 0
+    assert np.isfinite(o.temperature())
