@@ -1,0 +1,351 @@
+"""Benchmark of the per-timestep force-and-integrate path.
+
+One step = move_a (Nose-Hoover predictor + SHAKE), the force section (near
+field, local-expansion force, intramolecular, walls, graphite; every 10th step
+also the cell sort, lists and far-field build) and move_b (RATTLE), exactly the
+body of the reference's step loop (src/mybox.f90:136-227).
+
+Workload (default): the single-system mixed-precision configuration with the
+reference's force field: 20,000 SPC/E waters and 200 29-site trisiloxane
+surfactants on 4-layer AB graphite, closed box of 24 x 24 x 12 cells of 12 A
+(288 x 288 x 144 A), seeded synthetic droplet.  Metric: atom-steps/s (mobile
+sites x steps / s), with ns/day at 2 fs; the plain FP64 GPU path is measured on
+the same workload and reported beside it with the mixed path's force error.
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun each rank runs its own replica on its GPU (no collective in the
+data path; replicas only), timing is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(n_water=20000, n_surf=200, cells=(24, 24, 12), graphite_layers=4, seed=2024)
+DT_FS = 2.0
+FLOPS_COUL = 18       # per ordered site pair, Coulomb only (sqrt and divide as 1 each)
+FLOPS_LJ_EXTRA = 11   # added when the pair is LJ-active within rc
+FLOPS_L2P = 25 * 40   # local-expansion force per site
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="small workload (tests / profiling)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=20)
+    return ap.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """torch.distributed only for the barrier and the max over ranks."""
+
+    def __init__(self, ws):
+        self.ws = ws
+        self.dist = None
+        if ws > 1:
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, v):
+        if not self.dist:
+            return v
+        import torch
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist:
+            self.dist.destroy_process_group()
+
+
+def make_system(small):
+    from surfactant_enhanced_spreading_gb300 import system as S
+    if small:
+        return S.droplet(2000, 20, cells=(8, 8, 8), seed=7, graphite_layers=2)
+    w = WORKLOAD
+    return S.droplet(w["n_water"], w["n_surf"], cells=w["cells"], seed=w["seed"], graphite_layers=w["graphite_layers"])
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        self.path = os.path.join("/tmp", f"sesp_clocks_{os.getpid()}.csv")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if not self.proc:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        if not rows:
+            return out
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        out = {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+               "reasons": reasons, "samples": len(rows)}
+        return out
+
+
+def run_ours(args, ws, rank, local):
+    import oracle as O  # the CPU-baseline leg only
+    from surfactant_enhanced_spreading_gb300 import engine as E
+
+    D = Dist(ws)
+    s = make_system(args.small)
+    n_sites = s.n_sites
+
+    # --- mixed path: warm-up, then K steps with per-step CUDA events, cold L2
+    eng = E.Engine(s, E.MIXED, device=local)
+    eng.force(True)
+    eng.init_accel()
+    kb = 99101
+    eng.run(kb, args.warmup)
+    kb += args.warmup
+    D.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    step_ms = eng.run_timed(kb, args.steps, flush_l2=True)
+    clk = clocks.stop()
+    kb += args.steps
+    D.barrier()
+    t_ms = D.max(float(step_ms.sum()))
+    value = ws * n_sites * args.steps / (t_ms / 1e3)
+    ms_per_step = t_ms / args.steps
+
+    # kernel launches in the timed region: 9 per step, 13 more per rebuild step
+    n_rebuild = sum(1 for k in range(kb - args.steps, kb) if k % 10 == 0)
+    launches = 9 * args.steps + 13 * n_rebuild
+
+    # --- per-kernel durations over a second pass (events around kernel families)
+    eng.enable_timing(True)
+    eng.kernel_times(reset=True)
+    eng.run(kb, 20)
+    kt = eng.kernel_times(reset=True)
+    eng.enable_timing(False)
+    kb += 20
+    ncoul, nlj = eng.pair_counts()
+    near_ms = kt[0]
+    flops = ncoul * FLOPS_COUL + nlj * FLOPS_LJ_EXTRA + n_sites * FLOPS_L2P
+    achieved = flops / (near_ms / 1e3) / 1e12 if near_ms > 0 else None
+    peak = fp32_nominal_tflops(local)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "near_field_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # --- plain FP64 GPU path on the same workload, and the mixed force error
+    plain = E.Engine(s, E.PLAIN_FP64, device=local)
+    f64 = plain.force(True)
+    mixed_ref = E.Engine(s, E.MIXED, device=local)
+    f32 = mixed_ref.force(True)
+    ferr = float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))
+    del mixed_ref
+    plain.init_accel()
+    plain.run(99101, 5)
+    p_ms = plain.run_timed(99106, args.plain_steps, flush_l2=True)
+    plain_value = n_sites * args.plain_steps / (p_ms.sum() / 1e3)
+    del plain
+
+    # --- end to end through the C ABI with host buffers: each 10-step chunk
+    # uploads the state from pinned host memory, runs, downloads the state
+    pos, vel, acc = eng.state()
+    try:
+        import torch
+        hp = torch.from_numpy(pos).pin_memory().numpy()
+        hv = torch.from_numpy(vel).pin_memory().numpy()
+        ha = torch.from_numpy(acc).pin_memory().numpy()
+    except Exception:
+        hp, hv, ha = pos, vel, acc
+    eta = eng.eta
+    chunks = max(1, args.steps // 10)
+    D.barrier()
+    t0 = time.perf_counter()
+    for c in range(chunks):
+        eng.set_state(hp, hv, ha, eta)
+        eng.run(kb, 10)
+        kb += 10
+        p2, v2, a2 = eng.state()
+        hp[...] = p2; hv[...] = v2; ha[...] = a2
+        eta = eng.eta
+    t_e2e = D.max(time.perf_counter() - t0)
+    e2e_value = ws * n_sites * 10 * chunks / t_e2e
+    state_bytes = 3 * 3 * 8 * n_sites
+    e2e = {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": state_bytes / 10,
+           "d2h_bytes_per_step": state_bytes / 10,
+           "how": "per 10-step chunk: sesp_set_state from pinned host pos/vel/acc, sesp_run(10), sesp_download_state"}
+
+    # --- CPU baseline: the oracle on the same workload, bounded sample
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(s, O, steps=2)
+
+    T = eng.temperature()
+    cnt = eng.counters()
+    D.close()
+    if rank != 0:
+        return
+    ns_day = value / n_sites * 86400 * DT_FS * 1e-6 if ws == 1 else value / ws / n_sites * 86400 * DT_FS * 1e-6
+    line = {
+        "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 pair/multipole, f64 constraints/thermostat/positions",
+        "data": "synthetic (seeded droplet; no dataset)",
+        "config": {"workload": ("small test droplet 2,000 waters + 20 surfactants, 8^3 cells" if args.small else
+                                "single system, 20,000 SPC/E waters + 200 29-site trisiloxane surfactants on 4-layer "
+                                "graphite, 24x24x12 cells (288x288x144 A), reference force field"),
+                   "n_sites": n_sites, "precision": "mixed", "rebuild_interval": 10,
+                   "l2": "flushed between timed steps (256 MB write outside the timed intervals)",
+                   "parallelism": f"replicas x{ws}"},
+        "ns_per_day": ns_day,
+        "plain_fp64": {"value": plain_value, "unit": "atom-steps/s", "steps": args.plain_steps,
+                       "ms_per_step": float(p_ms.mean())},
+        "mixed_vs_plain_speedup": value / ws / plain_value,
+        "mixed_force_rms_rel_error": ferr,
+        "roofline": {"bound": "fp32", "kernel": "k_near<mixed> (pair + fused local-expansion force)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
+                     "peak_source": "nominal FP32 FMA rate: SMs x 128 lanes x 2 x max SM clock (no FP32 figure "
+                                    "in MEASURED_PEAKS.json)",
+                     "algorithmic_flops_per_launch": flops, "pairs_coulomb": ncoul, "pairs_lj": nlj,
+                     "near_ms_per_launch": near_ms},
+        "kernel_ms": {"near": kt[0], "site_and_intra": kt[4], "move_a": kt[2], "move_b": kt[3],
+                      "rebuild_sort": kt[5], "far_build": kt[6]},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": clk,
+        "temperature": T,
+        "shake_failures": cnt[0],
+    }
+    print(json.dumps(line))
+
+
+def fp32_nominal_tflops(device):
+    try:
+        out = subprocess.run(["nvidia-smi", f"--id={device}", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits"],
+                             capture_output=True, text=True, timeout=20).stdout.strip()
+        mhz = float(out.splitlines()[0])
+    except Exception:
+        mhz = 2070.0
+    sms = 152
+    try:
+        import torch
+        sms = torch.cuda.get_device_properties(device).multi_processor_count
+    except Exception:
+        pass
+    return sms * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def cpu_baseline(s, O, steps=2):
+    """The oracle (single-threaded FP64 C restatement of the reference) on the
+    same system: one start-up force call, then `steps` full steps (the first
+    a rebuild step) timed."""
+    o = O.Oracle(s)
+    o.force(True)
+    o.init_accel()
+    t0 = time.perf_counter()
+    o.run(99110, steps)   # 99110 is a rebuild step, 99111 is not
+    dt = time.perf_counter() - t0
+    return {"value": s.n_sites * steps / dt, "unit": "atom-steps/s", "cores": 1, "kind": "port",
+            "sample": f"{steps} steps (1 rebuild + {steps - 1} plain) of the full workload, {dt:.1f} s"}
+
+
+def run_reference(args, ws, rank, local):
+    """The reference's own algorithm on the host cores: the oracle port (the
+    Fortran + MPI reference cannot be built here: no Fortran compiler or MPI)."""
+    if rank != 0:
+        return
+    import oracle as O
+    s = make_system(args.small)
+    o = O.Oracle(s)
+    o.force(True)
+    o.init_accel()
+    kb = 99110
+    for _ in range(min(args.warmup, 1)):
+        o.step(kb)
+        kb += 1
+    n = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    o.run(kb, n)
+    dt = time.perf_counter() - t0
+    value = s.n_sites * n / dt
+    line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 0, "steps": n,
+            "warmup": min(args.warmup, 1), "ms_per_step": dt / n * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded droplet)",
+            "impl": "reference",
+            "config": {"workload": "same system as the GPU arm" + (" (small)" if args.small else ""),
+                       "n_sites": s.n_sites},
+            "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": 1, "kind": "port",
+                             "sample": f"{n} steps of the full workload (bounded sample)"},
+            "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, ws, rank, local)
+    else:
+        run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -130,7 +130,16 @@ int sesp_run(sesp_ctx *ctx, int kb0, int nsteps);
 int sesp_run_async(sesp_ctx *ctx, int kb0, int nsteps);
 int sesp_sync(sesp_ctx *ctx);
 
+/* nsteps passes like sesp_run, each timed with CUDA events recorded on the
+ * engine's stream around the step's graph launch.  With flush_l2 != 0 a
+ * 256 MB buffer is written between steps, outside the timed intervals, so
+ * every step starts with a cold L2.  step_ms receives nsteps durations. */
+int sesp_run_timed(sesp_ctx *ctx, int kb0, int nsteps, int flush_l2, double *step_ms);
+
 /* diagnostics */
+/* ordered near-field site pairs and LJ-active pairs within rc of the current
+ * state and lists (sizes the pair kernel's algorithmic flop count) */
+int sesp_pair_counts(sesp_ctx *ctx, int64_t out[2]);
 int sesp_temperature(sesp_ctx *ctx, double *t);   /* src/compute_temperature.f90:240-242 */
 int sesp_get_eta(sesp_ctx *ctx, double *eta);
 int sesp_set_eta(sesp_ctx *ctx, double eta);

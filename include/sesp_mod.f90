@@ -146,5 +146,16 @@ module sesp_mod
       type(c_ptr), value :: ctx
       integer(c_int), value :: on
     end function
+    integer(c_int) function sesp_run_timed(ctx, kb0, nsteps, flush_l2, step_ms) bind(C, name="sesp_run_timed")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: kb0, nsteps, flush_l2
+      real(c_double), intent(out) :: step_ms(*)
+    end function
+    integer(c_int) function sesp_pair_counts(ctx, c) bind(C, name="sesp_pair_counts")
+      import :: c_int, c_ptr, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int64_t), intent(out) :: c(2)
+    end function
   end interface
 end module sesp_mod

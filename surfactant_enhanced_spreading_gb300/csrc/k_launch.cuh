@@ -24,6 +24,8 @@ void launch_near(const Dev &d, int ncell, int mixed, int terms, cudaStream_t st)
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int nrep, int d2, cudaStream_t st);
 void launch_site_forces(const Dev &d, int nsite, int terms, cudaStream_t st);
 void launch_intra(const Dev &d, const int *smols, int ns, int terms, cudaStream_t st);
+void launch_count_pairs(const Dev &d, int ncell, unsigned long long *out, cudaStream_t st);
+void launch_flush(void *buf, size_t bytes, cudaStream_t st);
 void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int ns, double *e_slot, double *e_site,
                      double *e_mol, cudaStream_t st);
 

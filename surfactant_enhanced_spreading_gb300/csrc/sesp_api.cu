@@ -733,6 +733,53 @@ static int launch_steps(sesp_ctx *c, int kb0, int nsteps) {
     return 0;
 }
 
+int sesp_run_timed(sesp_ctx *c, int kb0, int nsteps, int flush_l2, double *step_ms) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!step_ms || nsteps < 0) return fail(SESP_EINVAL, "bad arguments");
+    if (c->timing) return fail(SESP_ESTATE, "disable per-kernel timing first");
+    if (set_device(c)) return SESP_ECUDA;
+    const size_t fbytes = (size_t)256 << 20;
+    void *fbuf = nullptr;
+    if (flush_l2) CK(cudaMalloc(&fbuf, fbytes));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = 0;
+    for (int k = 0; k < nsteps && !rc; k++) {
+        if (flush_l2) launch_flush(fbuf, fbytes, c->st);
+        cudaEventRecord(e0, c->st);
+        rc = launch_steps(c, kb0 + k, 1);
+        cudaEventRecord(e1, c->st);
+        if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(SESP_ECUDA, "timed step failed");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        step_ms[k] = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (fbuf) cudaFree(fbuf);
+    return rc;
+}
+
+int sesp_pair_counts(sesp_ctx *c, int64_t out[2]) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    if (!c->have_force) return fail(SESP_ESTATE, "pair counts need a force call first");
+    if (set_device(c)) return SESP_ECUDA;
+    unsigned long long *dc = nullptr, h[2] = {0, 0};
+    CK(cudaMalloc(&dc, sizeof h));
+    cudaMemsetAsync(dc, 0, sizeof h, c->st);
+    launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
+    launch_count_pairs(c->d, c->ncell, dc, c->st);
+    cudaMemcpyAsync(h, dc, sizeof h, cudaMemcpyDeviceToHost, c->st);
+    cudaError_t err = cudaStreamSynchronize(c->st);
+    cudaFree(dc);
+    if (err != cudaSuccess) return fail(SESP_ECUDA, "pair counts: %s", cudaGetErrorString(err));
+    out[0] = (int64_t)h[0];
+    out[1] = (int64_t)h[1];
+    return 0;
+}
+
 int sesp_step(sesp_ctx *c, int kb) {
     int e = launch_steps(c, kb, 1);
     if (e) return e;

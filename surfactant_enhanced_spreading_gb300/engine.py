@@ -30,7 +30,7 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_upload_state", "sesp_download_state", "sesp_set_state", "sesp_force", "sesp_force_terms",
            "sesp_download_forces", "sesp_init_accel", "sesp_move_a", "sesp_move_b", "sesp_step", "sesp_run",
            "sesp_run_async", "sesp_sync", "sesp_temperature", "sesp_get_eta", "sesp_set_eta", "sesp_energies",
-           "sesp_counters", "sesp_kernel_times", "sesp_enable_timing"]
+           "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts"]
 
 
 class SespError(RuntimeError):
@@ -80,6 +80,8 @@ def load(path: str = LIB_PATH):
     L.sesp_counters.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.sesp_kernel_times.argtypes = [P, dp, ctypes.c_int]
     L.sesp_enable_timing.argtypes = [P, ctypes.c_int]
+    L.sesp_run_timed.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+    L.sesp_pair_counts.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     _lib = L
     return L
 
@@ -205,6 +207,17 @@ class Engine:
 
     def enable_timing(self, on=True):
         _check(_lib.sesp_enable_timing(self._h, int(on)))
+
+    def run_timed(self, kb0, nsteps, flush_l2=True):
+        """Per-step device times (ms) from CUDA events on the engine's stream."""
+        out = np.empty(int(nsteps))
+        _check(_lib.sesp_run_timed(self._h, int(kb0), int(nsteps), int(flush_l2), _dp(out)))
+        return out
+
+    def pair_counts(self):
+        out = (ctypes.c_int64 * 2)()
+        _check(_lib.sesp_pair_counts(self._h, out))
+        return int(out[0]), int(out[1])
 
     def kernel_times(self, reset=False):
         out = np.empty(8)
