@@ -101,6 +101,19 @@ int sesp_download_state(sesp_ctx *ctx, double *pos, double *vel, double *acc);
 /* velocities and accelerations in, e.g. to resume a saved state */
 int sesp_set_state(sesp_ctx *ctx, const double *pos, const double *vel, const double *acc, double eta);
 
+/* several independent systems ("replicas") in one context, laid out back to
+ * back and advanced together by every launch (batched ensembles).  Per
+ * replica q: n_water[q], n_surf[q], its cells n_cells[3q..3q+2] and n_carbon[q];
+ * pos / vel hold the replicas' sites one after the other, carbons their
+ * carbons.  Each replica keeps its own thermostat variable.  Every other
+ * entry point then acts on all replicas; state arrays are concatenated. */
+int sesp_upload_batch(sesp_ctx *ctx, int n_rep, const int *n_water, const int *n_surf, const int *n_cells,
+                      const double *pos, const double *vel, const int *n_carbon, const double *carbons);
+/* number of replicas in the context (negative on error) */
+int sesp_replica_count(sesp_ctx *ctx);
+/* the thermostat variable of every replica */
+int sesp_get_eta_batch(sesp_ctx *ctx, double *eta);
+
 /* the force section.  rebuild = 1 replaces src/mybox.f90:142-152 (molecule
  * re-keying), :163-175 (list builders, multipoles and translations) and
  * :183-223 (all force kernels); rebuild = 0 replaces src/mybox.f90:179-223

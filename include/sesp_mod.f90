@@ -157,5 +157,22 @@ module sesp_mod
       type(c_ptr), value :: ctx
       integer(c_int64_t), intent(out) :: c(2)
     end function
+    integer(c_int) function sesp_upload_batch(ctx, n_rep, n_water, n_surf, n_cells, pos, vel, n_carbon, carbons) &
+        bind(C, name="sesp_upload_batch")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: n_rep
+      integer(c_int), intent(in) :: n_water(*), n_surf(*), n_cells(*), n_carbon(*)
+      real(c_double), intent(in) :: pos(*), vel(*), carbons(*)
+    end function
+    integer(c_int) function sesp_replica_count(ctx) bind(C, name="sesp_replica_count")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function sesp_get_eta_batch(ctx, eta) bind(C, name="sesp_get_eta_batch")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: eta(*)
+    end function
   end interface
 end module sesp_mod

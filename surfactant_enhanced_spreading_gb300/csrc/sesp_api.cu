@@ -431,104 +431,132 @@ int sesp_destroy(sesp_ctx *c) {
     return 0;
 }
 
-int sesp_upload_state(sesp_ctx *c, int n_water, int n_surf, const double *pos, const double *vel, int n_carbon,
-                      const double *carbons) {
-    if (int e = check_ctx(c, false)) return e;
-    if (n_water < 0 || n_surf < 0 || n_water + n_surf == 0) return fail(SESP_EINVAL, "empty system");
-    if (!pos) return fail(SESP_EINVAL, "null positions");
-    if (n_carbon < 0 || (n_carbon > 0 && !carbons)) return fail(SESP_EINVAL, "bad carbons");
+}  // extern "C"
+
+namespace {
+
+struct RepIn {
+    int nw, ns, nc[3], ncarb;
+    const double *pos, *vel, *carb;
+};
+
+// Lay out one or more replica systems back to back and upload them.
+int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     if (set_device(c)) return SESP_ECUDA;
     cudaStreamSynchronize(c->st);
     free_state(c);
-    // one replica (the batch entry points stack several the same way)
-    Rep r;
-    memset(&r, 0, sizeof r);
-    for (int a = 0; a < 3; a++) {
-        r.nc[a] = c->p.n_cells[a];
-        r.nr[a] = r.nc[a] / 4;
-        r.rsd[a] = r.nc[a] * RS;
-        r.rhs[a] = r.rsd[a] / 2.0;
-    }
-    r.nw = n_water; r.ns = n_surf;
-    r.nsite = 3 * n_water + NSURF * n_surf;
-    r.nmol = n_water + n_surf;
-    r.graphite_on = c->p.graphite_on;
-    int np = r.nsite, ncon = 3 * n_water + NBOND * n_surf, df = 3 * np - ncon;
-    double rlx = c->p.tau_steps * DT;
-    r.pnh1 = DT / df / c->p.tr / (rlx * rlx);
-    r.pnh2 = -2.0 * df * c->p.tr;
-    c->reps.assign(1, r);
-    c->nrep = 1;
-    Rep &R = c->reps[0];
-    R.cell0 = 0; R.l3_0 = 0; R.l2_0 = 0; R.site0 = 0; R.mol0 = 0; R.axis0 = 0; R.gcol0 = 0;
-    c->nsite = R.nsite; c->nmol = R.nmol;
-    c->ncell = R.nc[0] * R.nc[1] * R.nc[2];
-    c->n3 = c->ncell / 8;
-    c->n2 = c->ncell / 64;
-    c->nwm = n_water; c->nsm = n_surf;
-    c->d2 = std::max(1, std::max(R.nr[0], std::max(R.nr[1], R.nr[2])) - 1);
-    // positions must lie inside the box
-    for (int g = 0; g < c->nsite; g++)
+    const int R = (int)in.size();
+    c->reps.assign(R, Rep());
+    int nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, naxis = 0, ncol = 0, nwm = 0, nsm = 0, d2 = 1;
+    for (int q = 0; q < R; q++) {
+        const RepIn &ri = in[q];
+        Rep &r = c->reps[q];
+        memset(&r, 0, sizeof r);
         for (int a = 0; a < 3; a++) {
-            double v = pos[3 * g + a];
-            if (!(v > -R.rhs[a] && v < R.rhs[a])) return fail(SESP_EINVAL, "site %d outside the box (axis %d: %g)", g, a, v);
+            if (ri.nc[a] <= 0 || ri.nc[a] % 4) return fail(SESP_EINVAL, "replica %d: cells must be positive multiples of 4", q);
+            r.nc[a] = ri.nc[a];
+            r.nr[a] = r.nc[a] / 4;
+            r.rsd[a] = r.nc[a] * RS;
+            r.rhs[a] = r.rsd[a] / 2.0;
+            d2 = std::max(d2, r.nr[a] - 1);
         }
+        if (ri.nw < 0 || ri.ns < 0 || ri.nw + ri.ns == 0) return fail(SESP_EINVAL, "replica %d: empty system", q);
+        if (!ri.pos) return fail(SESP_EINVAL, "replica %d: null positions", q);
+        if (ri.ncarb < 0 || (ri.ncarb > 0 && !ri.carb)) return fail(SESP_EINVAL, "replica %d: bad carbons", q);
+        r.nw = ri.nw; r.ns = ri.ns;
+        r.nsite = 3 * ri.nw + NSURF * ri.ns;
+        r.nmol = ri.nw + ri.ns;
+        r.graphite_on = c->p.graphite_on;
+        int np = r.nsite, ncon = 3 * ri.nw + NBOND * ri.ns, df = 3 * np - ncon;
+        double rlx = c->p.tau_steps * DT;
+        r.pnh1 = DT / df / c->p.tr / (rlx * rlx);
+        r.pnh2 = -2.0 * df * c->p.tr;
+        r.site0 = nsite; r.mol0 = nmol; r.cell0 = ncell; r.l3_0 = n3; r.l2_0 = n2; r.axis0 = naxis; r.gcol0 = ncol;
+        int cc = r.nc[0] * r.nc[1] * r.nc[2];
+        nsite += r.nsite; nmol += r.nmol; ncell += cc; n3 += cc / 8; n2 += cc / 64;
+        naxis += r.nc[0] + r.nc[1] + r.nc[2]; ncol += r.nc[0] * r.nc[1];
+        nwm += ri.nw; nsm += ri.ns;
+        for (int g = 0; g < r.nsite; g++)
+            for (int a = 0; a < 3; a++) {
+                double v = ri.pos[3 * g + a];
+                if (!(v > -r.rhs[a] && v < r.rhs[a]))
+                    return fail(SESP_EINVAL, "replica %d: site %d outside the box (axis %d: %g)", q, g, a, v);
+            }
+    }
+    c->nrep = R; c->nsite = nsite; c->nmol = nmol; c->ncell = ncell; c->n3 = n3; c->n2 = n2;
+    c->nwm = nwm; c->nsm = nsm; c->d2 = d2;
     Dev &d = c->d;
     memset(&d, 0, sizeof d);
-    int N = c->nsite, M = c->nmol, C = c->ncell;
+    int N = nsite, M = nmol, C = ncell;
     int e = 0;
     double **a12[12] = {&d.x, &d.y, &d.z, &d.vx, &d.vy, &d.vz, &d.ax, &d.ay, &d.az, &d.fx, &d.fy, &d.fz};
     for (auto q : a12) if ((e = dalloc(c, q, N))) return e;
     if ((e = dalloc(c, &d.ptype, N)) || (e = dalloc(c, &d.smol, N)) || (e = dalloc(c, &d.mrep, M)) ||
         (e = dalloc(c, &d.mfirst, M)) || (e = dalloc(c, &d.mkind, M)) || (e = dalloc(c, &d.mkey, M)) ||
         (e = dalloc(c, &d.mw1, M)) || (e = dalloc(c, &d.ke, 2 * M)) || (e = dalloc(c, &d.mfail, M)) ||
-        (e = dalloc(c, &d.rep, 1)) || (e = dalloc(c, &d.eta, 1)) || (e = dalloc(c, &d.crep, C)) ||
-        (e = dalloc(c, &d.b3rep, c->n3)) || (e = dalloc(c, &d.b2rep, c->n2)) || (e = dalloc(c, &d.cstart, C + 1)) ||
+        (e = dalloc(c, &d.rep, R)) || (e = dalloc(c, &d.eta, R)) || (e = dalloc(c, &d.crep, C)) ||
+        (e = dalloc(c, &d.b3rep, n3)) || (e = dalloc(c, &d.b2rep, n2)) || (e = dalloc(c, &d.cstart, C + 1)) ||
         (e = dalloc(c, &d.ccount, C)) || (e = dalloc(c, &d.cfill, C)) || (e = dalloc(c, &d.sloc, N)) ||
         (e = dalloc(c, &d.sslot, N)) || (e = dalloc(c, &d.srt_site, N)) || (e = dalloc(c, &d.srt_pos, N)) ||
         (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) ||
-        (e = dalloc(c, &d.isub, (size_t)NSURF * n_surf)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
-        (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * c->n3)) ||
-        (e = dalloc(c, &d.L3, (size_t)LP * c->n3)) || (e = dalloc(c, &d.O2, (size_t)LP * c->n2)) ||
-        (e = dalloc(c, &d.L2, (size_t)LP * c->n2)) || (e = dalloc(c, &d.counters, 8)) ||
-        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &c->wmols, n_water)) || (e = dalloc(c, &c->smols, n_surf)))
+        (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
+        (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
+        (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
+        (e = dalloc(c, &d.L2, (size_t)LP * n2)) || (e = dalloc(c, &d.counters, 8)) ||
+        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)))
         return e;
-    int w2 = 2 * c->d2 + 1;
+    int w2 = 2 * d2 + 1;
     if ((e = dalloc(c, &d.op_m2l4, (size_t)343 * LPH * LP)) || (e = dalloc(c, &d.op_m2l3, (size_t)343 * LPH * LP)) ||
         (e = dalloc(c, &d.op_m2l2, (size_t)w2 * w2 * w2 * LPH * LP)) || (e = dalloc(c, &d.op_m2m43, (size_t)8 * LPH * LP)) ||
         (e = dalloc(c, &d.op_m2m32, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_l2l23, (size_t)8 * LPH * LP)) ||
         (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)))
         return e;
-    // host-side static data
+    // static per-site / per-molecule / per-box data
     std::vector<uint8_t> ptype(N);
-    std::vector<int> smol(N), mrep(M, 0), mfirst(M), mkind(M), wm(n_water), sm(n_surf);
-    for (int m = 0; m < n_water; m++) {
-        mfirst[m] = 3 * m; mkind[m] = 0; wm[m] = m;
-        for (int t = 0; t < 3; t++) { ptype[3 * m + t] = t == 0 ? 0 : 1; smol[3 * m + t] = m; }
-    }
-    for (int q = 0; q < n_surf; q++) {
-        int m = n_water + q, g0 = 3 * n_water + NSURF * q;
-        mfirst[m] = g0; mkind[m] = 1; sm[q] = m;
-        for (int t = 0; t < NSURF; t++) { ptype[g0 + t] = (uint8_t)(2 + t); smol[g0 + t] = m; }
-    }
-    std::vector<double> axis;
-    for (int a = 0; a < 3; a++) axis_centres(R, a, axis);
-    if ((e = dalloc(c, &d.axis, axis.size()))) return e;
-    // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:187-216
+    std::vector<int> smol(N), mrep(M), mfirst(M), mkind(M), wm, sm, crep(C), b3(n3), b2(n2);
+    std::vector<double> axis, sx(N), sy(N), sz(N), vxa(N, 0.0), vya(N, 0.0), vza(N, 0.0), eta0(R, 0.0);
     std::vector<int> gstart(1, 0);
     std::vector<double4> gpos;
     double rcut = RC + sqrt(2.0) * RS / 2.0;
     rcut *= rcut;
-    for (int iy = 0; iy < R.nc[1]; iy++)
-        for (int ix = 0; ix < R.nc[0]; ix++) {
-            double cx = axis[ix], cy = axis[R.nc[0] + iy];
-            for (int k = 0; k < n_carbon; k++) {
-                double dx = carbons[3 * k] - cx, dy = carbons[3 * k + 1] - cy;
-                if (dx * dx + dy * dy <= rcut) gpos.push_back(make_double4(carbons[3 * k], carbons[3 * k + 1], carbons[3 * k + 2], 0.0));
-            }
-            gstart.push_back((int)gpos.size());
+    for (int q = 0; q < R; q++) {
+        const Rep &r = c->reps[q];
+        const RepIn &ri = in[q];
+        for (int m = 0; m < ri.nw; m++) {
+            int gm = r.mol0 + m, g0 = r.site0 + 3 * m;
+            mfirst[gm] = g0; mkind[gm] = 0; mrep[gm] = q; wm.push_back(gm);
+            for (int t = 0; t < 3; t++) { ptype[g0 + t] = t == 0 ? 0 : 1; smol[g0 + t] = gm; }
         }
-    if ((e = dalloc(c, &d.gcol_start, gstart.size())) || (e = dalloc(c, &d.gpos, gpos.size()))) return e;
+        for (int k = 0; k < ri.ns; k++) {
+            int gm = r.mol0 + ri.nw + k, g0 = r.site0 + 3 * ri.nw + NSURF * k;
+            mfirst[gm] = g0; mkind[gm] = 1; mrep[gm] = q; sm.push_back(gm);
+            for (int t = 0; t < NSURF; t++) { ptype[g0 + t] = (uint8_t)(2 + t); smol[g0 + t] = gm; }
+        }
+        for (int g = 0; g < r.nsite; g++) {
+            sx[r.site0 + g] = ri.pos[3 * g]; sy[r.site0 + g] = ri.pos[3 * g + 1]; sz[r.site0 + g] = ri.pos[3 * g + 2];
+            if (ri.vel) { vxa[r.site0 + g] = ri.vel[3 * g]; vya[r.site0 + g] = ri.vel[3 * g + 1]; vza[r.site0 + g] = ri.vel[3 * g + 2]; }
+        }
+        int cc = r.nc[0] * r.nc[1] * r.nc[2];
+        for (int k = 0; k < cc; k++) crep[r.cell0 + k] = q;
+        for (int k = 0; k < cc / 8; k++) b3[r.l3_0 + k] = q;
+        for (int k = 0; k < cc / 64; k++) b2[r.l2_0 + k] = q;
+        size_t a0 = axis.size();
+        for (int a = 0; a < 3; a++) axis_centres(r, a, axis);
+        // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:187-216
+        for (int iy = 0; iy < r.nc[1]; iy++)
+            for (int ix = 0; ix < r.nc[0]; ix++) {
+                double cx = axis[a0 + ix], cy = axis[a0 + r.nc[0] + iy];
+                for (int k = 0; k < ri.ncarb; k++) {
+                    double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
+                    if (dx * dx + dy * dy <= rcut)
+                        gpos.push_back(make_double4(ri.carb[3 * k], ri.carb[3 * k + 1], ri.carb[3 * k + 2], 0.0));
+                }
+                gstart.push_back((int)gpos.size());
+            }
+    }
+    if ((e = dalloc(c, &d.axis, axis.size())) || (e = dalloc(c, &d.gcol_start, gstart.size())) ||
+        (e = dalloc(c, &d.gpos, gpos.size())))
+        return e;
     // translation operators
     std::vector<double2> ops((size_t)343 * LPH * LP, make_double2(0.0, 0.0));
     auto fill_m2l = [&](double scale, double2 *dst) -> int {
@@ -546,14 +574,15 @@ int sesp_upload_state(sesp_ctx *c, int n_water, int n_surf, const double *pos, c
     if ((e = fill_m2l(RS, d.op_m2l4)) || (e = fill_m2l(2 * RS, d.op_m2l3))) return e;
     {
         std::vector<double2> o2((size_t)w2 * w2 * w2 * LPH * LP, make_double2(0.0, 0.0));
-        for (int dz = -c->d2; dz <= c->d2; dz++)
-            for (int dy = -c->d2; dy <= c->d2; dy++)
-                for (int dx = -c->d2; dx <= c->d2; dx++) {
+        for (int dz = -d2; dz <= d2; dz++)
+            for (int dy = -d2; dy <= d2; dy++)
+                for (int dx = -d2; dx <= d2; dx++) {
                     if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-                    int oi = (dx + c->d2) + w2 * ((dy + c->d2) + w2 * (dz + c->d2));
+                    int oi = (dx + d2) + w2 * ((dy + d2) + w2 * (dz + d2));
                     op_m2l(dx * 4 * RS, dy * 4 * RS, dz * 4 * RS, &o2[(size_t)oi * LPH * LP]);
                 }
         CK(cudaMemcpyAsync(d.op_m2l2, o2.data(), o2.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
         std::vector<double2> o8((size_t)8 * LPH * LP);
         struct { double2 *dst; double s; int kind; } sets[4] = {
             {d.op_m2m43, RS, 0}, {d.op_m2m32, 2 * RS, 0}, {d.op_l2l23, 2 * RS, 1}, {d.op_l2l34, RS, 1}};
@@ -568,13 +597,6 @@ int sesp_upload_state(sesp_ctx *c, int n_water, int n_surf, const double *pos, c
         }
     }
     std::vector<double2> ljt = make_lj_table();
-    std::vector<double> sx(N), sy(N), sz(N), vxa(N, 0.0), vya(N, 0.0), vza(N, 0.0);
-    for (int g = 0; g < N; g++) {
-        sx[g] = pos[3 * g]; sy[g] = pos[3 * g + 1]; sz[g] = pos[3 * g + 2];
-        if (vel) { vxa[g] = vel[3 * g]; vya[g] = vel[3 * g + 1]; vza[g] = vel[3 * g + 2]; }
-    }
-    std::vector<int> crep(C, 0), b3(c->n3, 0), b2(c->n2, 0);
-    double eta0 = 0.0;
     CK(cudaMemcpyAsync(d.x, sx.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.y, sy.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.z, sz.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
@@ -586,22 +608,67 @@ int sesp_upload_state(sesp_ctx *c, int n_water, int n_surf, const double *pos, c
     CK(cudaMemcpyAsync(d.mrep, mrep.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.mfirst, mfirst.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.mkind, mkind.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
-    if (n_water) CK(cudaMemcpyAsync(c->wmols, wm.data(), n_water * sizeof(int), cudaMemcpyHostToDevice, c->st));
-    if (n_surf) CK(cudaMemcpyAsync(c->smols, sm.data(), n_surf * sizeof(int), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(d.rep, c->reps.data(), sizeof(Rep), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(d.eta, &eta0, sizeof(double), cudaMemcpyHostToDevice, c->st));
+    if (nwm) CK(cudaMemcpyAsync(c->wmols, wm.data(), nwm * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    if (nsm) CK(cudaMemcpyAsync(c->smols, sm.data(), nsm * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.rep, c->reps.data(), R * sizeof(Rep), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.eta, eta0.data(), R * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.axis, axis.data(), axis.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.crep, crep.data(), C * sizeof(int), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(d.b3rep, b3.data(), c->n3 * sizeof(int), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(d.b2rep, b2.data(), c->n2 * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.b3rep, b3.data(), n3 * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.b2rep, b2.data(), n2 * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.gcol_start, gstart.data(), gstart.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
     if (!gpos.empty()) CK(cudaMemcpyAsync(d.gpos, gpos.data(), gpos.size() * sizeof(double4), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.ljt, ljt.data(), ljt.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
-    c->h3.assign(3 * (size_t)N, 0.0);
     c->uploaded = true;
     c->have_force = false;
     c->steps = 0;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sesp_upload_state(sesp_ctx *c, int n_water, int n_surf, const double *pos, const double *vel, int n_carbon,
+                      const double *carbons) {
+    if (int e = check_ctx(c, false)) return e;
+    RepIn r;
+    r.nw = n_water; r.ns = n_surf; r.ncarb = n_carbon;
+    for (int a = 0; a < 3; a++) r.nc[a] = c->p.n_cells[a];
+    r.pos = pos; r.vel = vel; r.carb = carbons;
+    return upload_impl(c, std::vector<RepIn>(1, r));
+}
+
+int sesp_upload_batch(sesp_ctx *c, int n_rep, const int *n_water, const int *n_surf, const int *n_cells,
+                      const double *pos, const double *vel, const int *n_carbon, const double *carbons) {
+    if (int e = check_ctx(c, false)) return e;
+    if (n_rep <= 0 || !n_water || !n_surf || !n_cells || !pos || !n_carbon) return fail(SESP_EINVAL, "bad batch arguments");
+    std::vector<RepIn> in(n_rep);
+    size_t so = 0, co = 0;
+    for (int q = 0; q < n_rep; q++) {
+        RepIn &r = in[q];
+        r.nw = n_water[q]; r.ns = n_surf[q]; r.ncarb = n_carbon[q];
+        for (int a = 0; a < 3; a++) r.nc[a] = n_cells[3 * q + a];
+        r.pos = pos + 3 * so;
+        r.vel = vel ? vel + 3 * so : nullptr;
+        r.carb = carbons ? carbons + 3 * co : nullptr;
+        so += (size_t)3 * r.nw + (size_t)NSURF * r.ns;
+        co += r.ncarb;
+    }
+    return upload_impl(c, in);
+}
+
+int sesp_replica_count(sesp_ctx *c) {
+    if (!c) return -fail(SESP_EINVAL, "null context");
+    return c->nrep;
+}
+
+int sesp_get_eta_batch(sesp_ctx *c, double *eta) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!eta) return fail(SESP_EINVAL, "null output");
+    CK(cudaMemcpyAsync(eta, c->d.eta, c->nrep * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
     return 0;
 }
 
@@ -811,12 +878,16 @@ int sesp_temperature(sesp_ctx *c, double *t) {
     if (int e = sesp_download_state(c, nullptr, v.data(), nullptr)) return e;
     Tables T = make_tables();
     double s = 0.0;
-    for (int g = 0; g < N; g++) {
-        int pt = g < 3 * c->nwm ? (g % 3 == 0 ? 0 : 1) : 2 + (g - 3 * c->nwm) % NSURF;
-        s += T.mass[pt] * (v[3 * g] * v[3 * g] + v[3 * g + 1] * v[3 * g + 1] + v[3 * g + 2] * v[3 * g + 2]);
+    long dof = 0;
+    for (const Rep &r : c->reps) {
+        for (int g = 0; g < r.nsite; g++) {
+            int pt = g < 3 * r.nw ? (g % 3 == 0 ? 0 : 1) : 2 + (g - 3 * r.nw) % NSURF;
+            size_t k = 3 * (size_t)(r.site0 + g);
+            s += T.mass[pt] * (v[k] * v[k] + v[k + 1] * v[k + 1] + v[k + 2] * v[k + 2]);
+        }
+        dof += 3L * r.nsite - (3L * r.nw + (long)NBOND * r.ns);
     }
-    int np = N, nc = 3 * c->nwm + NBOND * c->nsm;
-    *t = s / (DT * DT) / (3 * np - nc);
+    *t = s / (DT * DT) / (double)dof;   // src/compute_temperature.f90:240-242
     return 0;
 }
 
@@ -830,7 +901,8 @@ int sesp_get_eta(sesp_ctx *c, double *eta) {
 
 int sesp_set_eta(sesp_ctx *c, double eta) {
     if (int e = check_ctx(c, true)) return e;
-    CK(cudaMemcpyAsync(c->d.eta, &eta, sizeof(double), cudaMemcpyHostToDevice, c->st));
+    std::vector<double> v(c->nrep, eta);
+    CK(cudaMemcpyAsync(c->d.eta, v.data(), c->nrep * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
     return 0;
 }

@@ -30,7 +30,8 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_upload_state", "sesp_download_state", "sesp_set_state", "sesp_force", "sesp_force_terms",
            "sesp_download_forces", "sesp_init_accel", "sesp_move_a", "sesp_move_b", "sesp_step", "sesp_run",
            "sesp_run_async", "sesp_sync", "sesp_temperature", "sesp_get_eta", "sesp_set_eta", "sesp_energies",
-           "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts"]
+           "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts",
+           "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch"]
 
 
 class SespError(RuntimeError):
@@ -82,6 +83,10 @@ def load(path: str = LIB_PATH):
     L.sesp_enable_timing.argtypes = [P, ctypes.c_int]
     L.sesp_run_timed.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
     L.sesp_pair_counts.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.sesp_upload_batch.argtypes = [P, ctypes.c_int, ip, ip, ip, dp, dp, ip, dp]
+    L.sesp_replica_count.argtypes = [P]
+    L.sesp_get_eta_batch.argtypes = [P, dp]
     _lib = L
     return L
 
@@ -114,6 +119,9 @@ class Engine:
 
     def __init__(self, system, precision=PLAIN_FP64, device=0, **kw):
         L = load()
+        if isinstance(system, (list, tuple)):
+            self._init_batch(list(system), precision, device, **kw)
+            return
         self.system = system
         p = default_params(system.cells, precision, device=device, graphite_on=int(system.graphite_on), **kw)
         h = ctypes.c_void_p()
@@ -127,6 +135,36 @@ class Engine:
         if nc == 0:
             carb = np.zeros((1, 3))
         _check(L.sesp_upload_state(self._h, system.n_water, system.n_surf, _dp(pos), _dp(vel), nc, _dp(carb)))
+
+    def _init_batch(self, systems, precision, device, **kw):
+        """Several replica systems advanced together by every launch."""
+        L = _lib
+        self.systems = systems
+        self.system = systems[0]
+        graphite = int(any(s.graphite_on for s in systems))
+        p = default_params(systems[0].cells, precision, device=device, graphite_on=graphite, **kw)
+        h = ctypes.c_void_p()
+        _check(L.sesp_create(ctypes.byref(p), ctypes.byref(h)))
+        self._h = h
+        nw = (ctypes.c_int * len(systems))(*[s.n_water for s in systems])
+        ns = (ctypes.c_int * len(systems))(*[s.n_surf for s in systems])
+        cells = (ctypes.c_int * (3 * len(systems)))(*[int(c) for s in systems for c in s.cells])
+        ncarb = (ctypes.c_int * len(systems))(*[s.carbons.reshape(-1, 3).shape[0] for s in systems])
+        pos = np.ascontiguousarray(np.concatenate([s.pos for s in systems]), dtype=np.float64)
+        vel = np.ascontiguousarray(np.concatenate([s.vel for s in systems]), dtype=np.float64)
+        carb = np.ascontiguousarray(np.concatenate([s.carbons.reshape(-1, 3) for s in systems] + [np.zeros((1, 3))]),
+                                    dtype=np.float64)
+        _check(L.sesp_upload_batch(self._h, len(systems), nw, ns, cells, _dp(pos), _dp(vel), ncarb, _dp(carb)))
+        self.n = pos.shape[0]
+        self.offsets = np.cumsum([0] + [s.n_sites for s in systems])
+
+    def replica_count(self):
+        return int(_lib.sesp_replica_count(self._h))
+
+    def etas(self):
+        out = np.empty(self.replica_count())
+        _check(_lib.sesp_get_eta_batch(self._h, _dp(out)))
+        return out
 
     def close(self):
         if getattr(self, "_h", None):

@@ -217,29 +217,35 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
     pts = pts[np.argsort(np.linalg.norm(pts, axis=1), kind="stable")]
     surf_sites = []
     if n_surf:
+        placed = np.zeros((0, 3))
         for _ in range(n_surf):
             tmpl = surfactant_template(rng)
             tmpl -= tmpl.mean(axis=0)
-            for _t in range(200):
+            for _t in range(400):
                 rot = _rand_rot(rng)
                 u = rng.normal(size=3)
-                u[2] = abs(u[2])
+                u[2] = abs(u[2]) + 0.15
                 u /= np.linalg.norm(u)
-                centre = u * (radius + 2.0)
-                centre[2] = max(centre[2], 8.0)
+                # a shell around the droplet surface, thicker as it fills
+                centre = u * (radius + 3.0 + rng.uniform(0.0, 4.0 + 0.05 * len(surf_sites)))
                 cand = tmpl @ rot.T + centre
                 if cand[:, 2].min() < 2.0:
-                    continue
-                if any(np.min(np.linalg.norm(cand[:, None, :] - s[None, :, :], axis=2)) < 3.5 for s in surf_sites):
+                    cand[:, 2] += 2.0 - cand[:, 2].min()
+                if placed.shape[0] and np.min(np.linalg.norm(cand[:, None, :] - placed[None, :, :], axis=2)) < 3.5:
                     continue
                 surf_sites.append(cand)
+                placed = np.concatenate([placed, cand])
                 break
             else:
                 raise RuntimeError("could not place surfactant")
     # waters: keep lattice points clear of surfactant sites
     if surf_sites:
         allsurf = np.concatenate(surf_sites)
-        keep = np.array([np.min(np.linalg.norm(allsurf - p, axis=1)) > 3.0 for p in pts])
+        keep = np.ones(len(pts), dtype=bool)
+        for k0 in range(0, len(pts), 2048):
+            blk = pts[k0:k0 + 2048]
+            d2 = ((blk[:, None, :] - allsurf[None, :, :]) ** 2).sum(-1)
+            keep[k0:k0 + 2048] = d2.min(axis=1) > 9.0
         pts = pts[keep]
     if len(pts) < n_water:
         raise RuntimeError("lattice too small for the droplet")

@@ -16,7 +16,7 @@ def _energy_terms(o):
 @pytest.mark.parametrize("term,idx", [(O.TERM_VALENCE | O.TERM_DIHEDRAL | O.TERM_BERENDSEN, [4]),
                                       (O.TERM_INTERNAL, [3]), (O.TERM_WALL, [5]), (O.TERM_GRAPHITE, [6])])
 def test_finite_difference_intra_terms(term, idx):
-    s = S.droplet(60, 2, cells=(4, 4, 4), seed=11)
+    s = S.droplet(60, 2, cells=(8, 8, 4), seed=11)
     o = O.Oracle(s)
     o.force(True, O.TERM_ALL)  # build lists
     f = o.force(False, term)
@@ -33,7 +33,7 @@ def test_finite_difference_intra_terms(term, idx):
 
 
 def test_finite_difference_near_field():
-    s = S.droplet(80, 1, cells=(4, 4, 4), seed=12)
+    s = S.droplet(80, 1, cells=(8, 8, 4), seed=12)
     o = O.Oracle(s)
     f = o.force(True, O.TERM_NEAR)
     pos0 = o.get(0)

@@ -51,7 +51,7 @@ def test_wall_golden():
 
 
 def test_generator_constraints_exact():
-    s = S.droplet(40, 2, cells=(4, 4, 4), seed=3)
+    s = S.droplet(40, 2, cells=(8, 8, 4), seed=3)
     pos = s.pos * S.SIGMA
     w = pos[:120].reshape(40, 3, 3)
     assert np.allclose(np.linalg.norm(w[:, 1] - w[:, 0], axis=1), 1.0, atol=1e-12)

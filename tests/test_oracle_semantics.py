@@ -10,7 +10,7 @@ import oracle as O
 from surfactant_enhanced_spreading_gb300 import system as S
 
 
-@pytest.mark.parametrize("nw,ns,cells,seed", [(300, 0, (4, 4, 4), 0), (300, 4, (4, 4, 4), 1), (700, 10, (8, 8, 4), 2)])
+@pytest.mark.parametrize("nw,ns,cells,seed", [(300, 0, (4, 4, 4), 0), (300, 4, (8, 8, 4), 1), (700, 10, (8, 8, 4), 2)])
 def test_literal_lists_equal_located_rule(nw, ns, cells, seed):
     s = S.droplet(nw, ns, cells=cells, seed=seed)
     o = O.Oracle(s)
@@ -22,14 +22,14 @@ def test_literal_lists_equal_located_rule(nw, ns, cells, seed):
 
 
 def test_near_third_law():
-    s = S.droplet(400, 5, cells=(4, 4, 4), seed=4)
+    s = S.droplet(400, 5, cells=(8, 8, 4), seed=4)
     o = O.Oracle(s)
     f = o.force(True, O.TERM_NEAR)
     assert np.abs(f.sum(0)).max() / np.abs(f).max() < 1e-12
 
 
 def test_w1_w2_split_and_keys():
-    s = S.droplet(500, 3, cells=(4, 4, 4), seed=5)
+    s = S.droplet(500, 3, cells=(8, 8, 4), seed=5)
     o = O.Oracle(s)
     o.force(True, O.TERM_NEAR)
     key, w1 = o.keys()
@@ -42,7 +42,7 @@ def test_w1_w2_split_and_keys():
 
 
 def test_pair_counts_match_located_rule():
-    s = S.droplet(300, 2, cells=(4, 4, 4), seed=6)
+    s = S.droplet(300, 2, cells=(8, 8, 4), seed=6)
     o = O.Oracle(s)
     o.force(True, O.TERM_NEAR)
     ncoul, nlj = o.pair_counts()
