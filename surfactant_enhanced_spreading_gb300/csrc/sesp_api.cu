@@ -262,6 +262,7 @@ struct sesp_ctx {
     cudaEvent_t ev[16];
     double t_acc[8] = {0};
     int64_t t_n[8] = {0};
+    bool t_rec[8] = {false};
     // host copies for downloads
     std::vector<double> h3;
 };
@@ -317,12 +318,19 @@ int set_device(sesp_ctx *c) {
 
 namespace {
 
-void tstart(sesp_ctx *c, int k) { if (c->timing) cudaEventRecord(c->ev[2 * k], c->st); }
-void tstop(sesp_ctx *c, int k) { if (c->timing) cudaEventRecord(c->ev[2 * k + 1], c->st); }
-void tcollect(sesp_ctx *c, int k) {
+void tstart(sesp_ctx *c, int k) {
     if (!c->timing) return;
+    cudaEventRecord(c->ev[2 * k], c->st);
+    c->t_rec[k] = true;
+}
+void tstop(sesp_ctx *c, int k) { if (c->timing) cudaEventRecord(c->ev[2 * k + 1], c->st); }
+// only families recorded since the last collection are read
+void tcollect(sesp_ctx *c, int k) {
+    if (!c->timing || !c->t_rec[k]) return;
+    c->t_rec[k] = false;
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, c->ev[2 * k], c->ev[2 * k + 1]) == cudaSuccess) { c->t_acc[k] += ms; c->t_n[k]++; }
+    else cudaGetLastError();
 }
 
 void seq_force(sesp_ctx *c, int rebuild, int terms) {

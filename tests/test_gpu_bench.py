@@ -1,0 +1,31 @@
+"""bench.py runs end to end on a small droplet and prints one valid JSON line."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_bench_small_json():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--small", "--steps", "10", "--warmup", "3",
+                        "--no-cpu-baseline", "--plain-steps", "5"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    for k in ["metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "roofline", "e2e", "clocks",
+              "gpu_launches", "plain_fp64", "mixed_force_rms_rel_error"]:
+        assert k in line, k
+    assert line["value"] > 0 and line["e2e"]["value"] > 0
+    assert line["mixed_force_rms_rel_error"] < 1e-5
+    assert line["roofline"]["achieved"] and line["roofline"]["achieved"] > 0
+
+
+def test_bench_reference_arm_small():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--small", "--steps", "1",
+                        "--warmup", "0"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0

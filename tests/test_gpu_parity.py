@@ -132,3 +132,18 @@ def test_invalid_inputs_raise():
     eng = E.Engine(s)
     with pytest.raises(E.SespError):
         eng.force(False)  # the first force call must build the lists
+
+
+def test_kernel_timing_path(sys_small):
+    eng = E.Engine(sys_small, E.MIXED)
+    eng.force(True)
+    eng.init_accel()
+    eng.enable_timing(True)
+    eng.run(99101, 12)   # crosses one rebuild step
+    t = eng.kernel_times(reset=True)
+    eng.enable_timing(False)
+    assert t[0] > 0 and t[2] > 0 and t[3] > 0 and t[5] > 0 and t[6] > 0
+    ms = eng.run_timed(99113, 5, flush_l2=True)
+    assert (ms > 0).all()
+    nc, nl = eng.pair_counts()
+    assert nc > nl > 0
