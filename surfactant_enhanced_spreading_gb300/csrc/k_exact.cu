@@ -213,11 +213,150 @@ __global__ void k_move_a(Dev d, const int *mols, int nm, double tol, int maxit) 
     if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
 }
 
+// The surfactant halves with the bond graph of src/init_arrays.f90:229-264
+// unrolled at compile time, so the 29 iterated positions (SHAKE) or
+// velocities (RATTLE) live in registers; the fixed positions and the velocity
+// copies sit in shared memory.  Same Gauss-Seidel order and arithmetic as the
+// generic kernel above (and as src/move_surfactant_a.f90 / _b.f90).
+__device__ constexpr int SBI[NBOND] = {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17,
+                                        17, 19, 20, 20, 20, 17, 24, 25, 25, 25};
+__device__ constexpr int SBJ[NBOND] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18,
+                                        19, 20, 21, 22, 23, 24, 25, 26, 27, 28};
+constexpr int SURF_BLOCK = 32;
+
+__global__ void __launch_bounds__(SURF_BLOCK) k_move_a_surf(Dev d, const int *mols, int nm, double tol, int maxit) {
+    __shared__ double s_rm[NSURF], s_dsq[NBOND];
+    if (threadIdx.x < NSURF) s_rm[threadIdx.x] = 1.0 / cT.mass[2 + threadIdx.x];
+    if (threadIdx.x < NBOND) s_dsq[threadIdx.x] = cT.dsqs[threadIdx.x];
+    __syncthreads();
+    volatile double *vrm = s_rm, *vdsq = s_dsq;
+    __shared__ double sr[3][NSURF][SURF_BLOCK];
+    __shared__ double sv[3][NSURF][SURF_BLOCK];
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nm) return;
+    const int l = threadIdx.x;
+    int m = mols[t];
+    int g0 = d.mfirst[m];
+    double escale = 1.0 - d.eta[d.mrep[m]] * DT / 2.0;
+    double px[NSURF], py[NSURF], pz[NSURF];
+    double ke0 = 0.0;
+#pragma unroll
+    for (int i = 0; i < NSURF; i++) {
+        int g = g0 + i;
+        double vxg = d.vx[g], vyg = d.vy[g], vzg = d.vz[g];
+        ke0 += cT.mass[2 + i] * (vxg * vxg + vyg * vyg + vzg * vzg);
+        sr[0][i][l] = d.x[g]; sr[1][i][l] = d.y[g]; sr[2][i][l] = d.z[g];
+        px[i] = d.x[g] + vxg * escale + d.ax[g];
+        py[i] = d.y[g] + vyg * escale + d.ay[g];
+        pz[i] = d.z[g] + vzg * escale + d.az[g];
+        sv[0][i][l] = vxg * escale + d.ax[g];
+        sv[1][i][l] = vyg * escale + d.ay[g];
+        sv[2][i][l] = vzg * escale + d.az[g];
+    }
+    const double tol2 = 2.0 * tol;
+    volatile double(*vr)[NSURF][SURF_BLOCK] = sr;
+    volatile double(*vv)[NSURF][SURF_BLOCK] = sv;
+    int it = 0;
+    bool ldone = false;
+    while (!ldone && it <= maxit) {
+        ldone = true;
+#pragma unroll
+        for (int b = 0; b < NBOND; b++) {
+            const int i = SBI[b], j = SBJ[b];
+            double pxab = px[i] - px[j], pyab = py[i] - py[j], pzab = pz[i] - pz[j];
+            double pabsq = pxab * pxab + pyab * pyab + pzab * pzab;
+            double rabsq = vdsq[b];
+            double diffsq = rabsq - pabsq;
+            if (fabs(diffsq) > rabsq * tol2) {
+                double rxab = vr[0][i][l] - vr[0][j][l], ryab = vr[1][i][l] - vr[1][j][l], rzab = vr[2][i][l] - vr[2][j][l];
+                double rpab = rxab * pxab + ryab * pyab + rzab * pzab;
+                double rma = vrm[i], rmb = vrm[j];
+                double gab = diffsq / (2.0 * (rma + rmb) * rpab);
+                double dx = rxab * gab, dy = ryab * gab, dz = rzab * gab;
+                px[i] = px[i] + rma * dx; py[i] = py[i] + rma * dy; pz[i] = pz[i] + rma * dz;
+                px[j] = px[j] - rmb * dx; py[j] = py[j] - rmb * dy; pz[j] = pz[j] - rmb * dz;
+                vv[0][i][l] = vv[0][i][l] + rma * dx; vv[1][i][l] = vv[1][i][l] + rma * dy; vv[2][i][l] = vv[2][i][l] + rma * dz;
+                vv[0][j][l] = vv[0][j][l] - rmb * dx; vv[1][j][l] = vv[1][j][l] - rmb * dy; vv[2][j][l] = vv[2][j][l] - rmb * dz;
+                ldone = false;
+            }
+        }
+        it++;
+    }
+    double ke1 = 0.0;
+#pragma unroll
+    for (int i = 0; i < NSURF; i++) {
+        int g = g0 + i;
+        double vx = sv[0][i][l], vy = sv[1][i][l], vz = sv[2][i][l];
+        d.x[g] = px[i]; d.y[g] = py[i]; d.z[g] = pz[i];
+        d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
+        ke1 += cT.mass[2 + i] * (vx * vx + vy * vy + vz * vz);
+    }
+    d.ke[2 * m] = ke0;
+    d.ke[2 * m + 1] = ke1;
+    if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+}
+
+__global__ void __launch_bounds__(SURF_BLOCK) k_move_b_surf(Dev d, const int *mols, int nm, double tol, int maxit) {
+    __shared__ double s_rm[NSURF], s_dsq[NBOND];
+    if (threadIdx.x < NSURF) s_rm[threadIdx.x] = 1.0 / cT.mass[2 + threadIdx.x];
+    if (threadIdx.x < NBOND) s_dsq[threadIdx.x] = cT.dsqs[threadIdx.x];
+    __syncthreads();
+    volatile double *vrm = s_rm, *vdsq = s_dsq;
+    __shared__ double sr[3][NSURF][SURF_BLOCK];
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nm) return;
+    const int l = threadIdx.x;
+    int m = mols[t];
+    int g0 = d.mfirst[m];
+    double escale = 2.0 / (2.0 + d.eta[d.mrep[m]] * DT);
+    double vx[NSURF], vy[NSURF], vz[NSURF];
+#pragma unroll
+    for (int i = 0; i < NSURF; i++) {
+        int g = g0 + i;
+        double mi = cT.mass[2 + i];
+        sr[0][i][l] = d.x[g]; sr[1][i][l] = d.y[g]; sr[2][i][l] = d.z[g];
+        double axg = d.fx[g] * DTSQ2 / mi, ayg = d.fy[g] * DTSQ2 / mi, azg = d.fz[g] * DTSQ2 / mi;
+        d.ax[g] = axg; d.ay[g] = ayg; d.az[g] = azg;
+        vx[i] = escale * (d.vx[g] + axg);
+        vy[i] = escale * (d.vy[g] + ayg);
+        vz[i] = escale * (d.vz[g] + azg);
+    }
+    volatile double(*vr)[NSURF][SURF_BLOCK] = sr;
+    int it = 0;
+    bool ldone = false;
+    while (!ldone && it <= maxit) {
+        ldone = true;
+#pragma unroll
+        for (int b = 0; b < NBOND; b++) {
+            const int i = SBI[b], j = SBJ[b];
+            double vxab = vx[i] - vx[j], vyab = vy[i] - vy[j], vzab = vz[i] - vz[j];
+            double rxab = vr[0][i][l] - vr[0][j][l], ryab = vr[1][i][l] - vr[1][j][l], rzab = vr[2][i][l] - vr[2][j][l];
+            double rvab = rxab * vxab + ryab * vyab + rzab * vzab;
+            rvab = rvab / DT;
+            double rma = vrm[i], rmb = vrm[j];
+            double gab = -rvab / ((rma + rmb) * vdsq[b]);
+            if (fabs(gab) > tol) {
+                double dx = rxab * gab, dy = ryab * gab, dz = rzab * gab;
+                vx[i] = vx[i] + rma * dx * DT; vy[i] = vy[i] + rma * dy * DT; vz[i] = vz[i] + rma * dz * DT;
+                vx[j] = vx[j] - rmb * dx * DT; vy[j] = vy[j] - rmb * dy * DT; vz[j] = vz[j] - rmb * dz * DT;
+                ldone = false;
+            }
+        }
+        it++;
+    }
+#pragma unroll
+    for (int i = 0; i < NSURF; i++) {
+        int g = g0 + i;
+        d.vx[g] = vx[i]; d.vy[g] = vy[i]; d.vz[g] = vz[i];
+    }
+    if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+}
+
 // eta update of src/move_w2_a.f90:145-157, one block per replica, fixed
 // summation order (thread-strided partial sums, then a tree)
 __global__ void k_eta(Dev d) {
     const Rep r = d.rep[blockIdx.x];
-    __shared__ double s0[256], s1[256];
+    __shared__ double s0[1024], s1[1024];
     double a = 0.0, b = 0.0;
     for (int m = r.mol0 + threadIdx.x; m < r.mol0 + r.nmol; m += blockDim.x) { a += d.ke[2 * m]; b += d.ke[2 * m + 1]; }
     s0[threadIdx.x] = a; s1[threadIdx.x] = b;
@@ -301,13 +440,13 @@ void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream
 }
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
                    cudaStream_t st) {
-    if (ns) k_move_a<NSURF><<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, tol, maxit);
+    if (ns) k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
     if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
-    k_eta<<<nrep, 256, 0, st>>>(d);
+    k_eta<<<nrep, 1024, 0, st>>>(d);
 }
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit,
                    cudaStream_t st) {
-    if (ns) k_move_b<NSURF><<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, tol, maxit);
+    if (ns) k_move_b_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
     if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
 }
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st) {

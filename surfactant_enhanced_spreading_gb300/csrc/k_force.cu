@@ -316,12 +316,14 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int terms) {
                                     if (MIXED) ir = rsqrtf((float)r2); else ir = rsqrt((double)r2);
                                     R ir2 = ir * ir;
                                     R ft = qq * ir * ir2;
-                                    R lx, ly;
-                                    if (MIXED) { float2 v = ((float2 *)sm.lj)[trow + mt.y]; lx = v.x; ly = v.y; }
-                                    else { double2 v = ((double2 *)sm.lj)[trow + mt.y]; lx = v.x; ly = v.y; }
-                                    R on = (r2 <= rc2 && !same) ? lx : R(0);
-                                    R r6 = ir2 * ir2 * ir2;
-                                    ft += on * r6 * (ly * r6 - R(0.5)) * ir2;
+                                    if (mt.y != 1) {   // water H carries no LJ; uniform across the warp
+                                        R lx, ly;
+                                        if (MIXED) { float2 v = ((float2 *)sm.lj)[trow + mt.y]; lx = v.x; ly = v.y; }
+                                        else { double2 v = ((double2 *)sm.lj)[trow + mt.y]; lx = v.x; ly = v.y; }
+                                        R on = (r2 <= rc2 && !same) ? lx : R(0);
+                                        R r6 = ir2 * ir2 * ir2;
+                                        ft += on * r6 * (ly * r6 - R(0.5)) * ir2;
+                                    }
                                     px += dx * ft; py += dy * ft; pz += dz * ft;
                                 }
                             }
@@ -481,27 +483,102 @@ __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const double2 *ops,
 
 // M2L over the 6^3 window of the parent's neighbours' children minus the 27
 // adjacent boxes (src/computeLjk4.f90:114-168, src/computeLjk3.f90:220-277).
-// 120 threads: 15 output coefficients x 8 source groups, reduced in a fixed order.
-__global__ void k_m2l_win(Dev d, const double2 *O, double2 *L, const double2 *ops, const int *brep, int level) {
-    const int b = blockIdx.x;
-    const Rep r = d.rep[brep[b]];
-    const int div = level == 4 ? 1 : 2;
+// The 8 children of one parent share that window, so one CTA takes a parent:
+// it stages the 216 window multipoles in shared memory once, streams the
+// translation operators offset by offset (each applied to every child whose
+// source at that offset is in the window) and accumulates the 8 x 15 output
+// coefficients in registers.  R is the arithmetic precision.
+constexpr int M2L_NB = 8;   // operators staged per pass
+
+template <typename R>
+struct C2 {
+    R x, y;
+};
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_m2l_grp(Dev d, const double2 *O, double2 *L, const C2<R> *ops,
+                                                  const int *prep, int level) {
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C2<R> *sO = (C2<R> *)smraw;                  // [216][LP]
+    C2<R> *sOp = sO + 216 * LP;                  // [M2L_NB][LPH][LP]
+    const int p = blockIdx.x;
+    const Rep r = d.rep[prep[p]];
+    const int div = level == 4 ? 1 : 2;          // child grid = nc / div
     const int base = level == 4 ? r.cell0 : r.l3_0;
+    const int pbase = level == 4 ? r.l3_0 : r.l2_0;
     const int n[3] = {r.nc[0] / div, r.nc[1] / div, r.nc[2] / div};
-    int l = b - base;
+    const int np[3] = {n[0] / 2, n[1] / 2, n[2] / 2};
+    int l = p - pbase;
+    const int pc[3] = {l % np[0], (l / np[0]) % np[1], l / (np[0] * np[1])};
+    const int w0[3] = {2 * pc[0] - 2, 2 * pc[1] - 2, 2 * pc[2] - 2};
+    for (int idx = threadIdx.x; idx < 216 * LP; idx += blockDim.x) {
+        int cell = idx / LP, c = idx % LP;
+        int sx = w0[0] + cell % 6, sy = w0[1] + (cell / 6) % 6, sz = w0[2] + cell / 36;
+        C2<R> v = {R(0), R(0)};
+        if (sx >= 0 && sy >= 0 && sz >= 0 && sx < n[0] && sy < n[1] && sz < n[2]) {
+            double2 o = O[(size_t)(base + sx + n[0] * (sy + n[1] * sz)) * LP + c];
+            v.x = (R)o.x; v.y = (R)o.y;
+        }
+        sO[idx] = v;
+    }
+    const int t = threadIdx.x / LPH, o = threadIdx.x % LPH;
+    const bool act = threadIdx.x < 8 * LPH;
+    // this child's position in the window (2 or 3 per axis) and in the grid
+    const int lc[3] = {2 + (t & 1), 2 + ((t >> 1) & 1), 2 + ((t >> 2) & 1)};
+    const int gc[3] = {w0[0] + lc[0], w0[1] + lc[1], w0[2] + lc[2]};
+    R are = 0, aim = 0;
+    for (int d0 = 0; d0 < 343; d0 += M2L_NB) {
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < M2L_NB * LPH * LP; idx += blockDim.x) {
+            int k = idx / (LPH * LP);
+            if (d0 + k < 343) sOp[idx] = ops[(size_t)(d0 + k) * LPH * LP + idx % (LPH * LP)];
+        }
+        __syncthreads();
+        if (!act) continue;
+        for (int k = 0; k < M2L_NB && d0 + k < 343; k++) {
+            int oi = d0 + k;
+            int dx = oi % 7 - 3, dy = (oi / 7) % 7 - 3, dz = oi / 49 - 3;
+            if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+            int sx = lc[0] + dx, sy = lc[1] + dy, sz = lc[2] + dz;
+            if (sx < 0 || sy < 0 || sz < 0 || sx > 5 || sy > 5 || sz > 5) continue;
+            if (gc[0] + dx < 0 || gc[1] + dy < 0 || gc[2] + dz < 0 || gc[0] + dx >= n[0] || gc[1] + dy >= n[1] ||
+                gc[2] + dz >= n[2])
+                continue;
+            const C2<R> *op = sOp + ((size_t)k * LPH + o) * LP;
+            const C2<R> *src = sO + (size_t)(sx + 6 * (sy + 6 * sz)) * LP;
+#pragma unroll 5
+            for (int c = 0; c < LP; c++) {
+                C2<R> a = op[c], b = src[c];
+                are += a.x * b.x - a.y * b.y;
+                aim += a.x * b.y + a.y * b.x;
+            }
+        }
+    }
+    if (act) {
+        int child = base + gc[0] + n[0] * (gc[1] + n[1] * gc[2]);
+        store_jk(L + (size_t)child * LP, o, (double)are, (double)aim, true);
+    }
+}
+
+// M2L at L2 over all non-adjacent L2 boxes of the replica (src/computeLjk2.f90:17-72);
+// 120 threads: 15 outputs x 8 source groups, reduced in a fixed order
+__global__ void k_m2l_l2(Dev d, int d2) {
+    const int b = blockIdx.x;
+    const Rep r = d.rep[d.b2rep[b]];
+    const int *n = r.nr;
+    int l = b - r.l2_0;
     int t[3] = {l % n[0], (l / n[0]) % n[1], l / (n[0] * n[1])};
     int o = threadIdx.x % LPH, g = threadIdx.x / LPH;
     double re = 0.0, im = 0.0;
-    int k = 0;
-    for (int sz = 2 * (t[2] / 2) - 2; sz <= 2 * (t[2] / 2) + 3; sz++)
-        for (int sy = 2 * (t[1] / 2) - 2; sy <= 2 * (t[1] / 2) + 3; sy++)
-            for (int sx = 2 * (t[0] / 2) - 2; sx <= 2 * (t[0] / 2) + 3; sx++) {
+    int w = 2 * d2 + 1, k = 0;
+    for (int sz = 0; sz < n[2]; sz++)
+        for (int sy = 0; sy < n[1]; sy++)
+            for (int sx = 0; sx < n[0]; sx++) {
                 int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
                 if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-                if (sx < 0 || sy < 0 || sz < 0 || sx >= n[0] || sy >= n[1] || sz >= n[2]) continue;
                 if ((k++ & 7) != g) continue;
-                int oi = (dx + 3) + 7 * (dy + 3) + 49 * (dz + 3);
-                apply_op(ops + ((size_t)oi * LPH + o) * LP, O + (size_t)(base + sx + n[0] * (sy + n[1] * sz)) * LP, re, im);
+                int oi = (dx + d2) + w * ((dy + d2) + w * (dz + d2));
+                apply_op(d.op_m2l2 + ((size_t)oi * LPH + o) * LP, d.O2 + (size_t)(r.l2_0 + sx + n[0] * (sy + n[1] * sz)) * LP, re, im);
             }
     __shared__ double sre[8][LPH], sim[8][LPH];
     sre[g][o] = re; sim[g][o] = im;
@@ -509,42 +586,35 @@ __global__ void k_m2l_win(Dev d, const double2 *O, double2 *L, const double2 *op
     if (g == 0) {
         double a = 0.0, c = 0.0;
         for (int q = 0; q < 8; q++) { a += sre[q][o]; c += sim[q][o]; }
-        store_jk(L + (size_t)b * LP, o, a, c, true);
+        store_jk(d.L2 + (size_t)b * LP, o, a, c, false);
     }
 }
 
-// M2L at L2 over all non-adjacent L2 boxes of the replica (src/computeLjk2.f90:17-72)
-__global__ void k_m2l_l2(Dev d, int d2) {
-    const int b = blockIdx.x;
-    const Rep r = d.rep[d.b2rep[b]];
-    const int *n = r.nr;
-    int l = b - r.l2_0;
-    int t[3] = {l % n[0], (l / n[0]) % n[1], l / (n[0] * n[1])};
-    int o = threadIdx.x;
-    if (o >= LPH) return;
-    double re = 0.0, im = 0.0;
-    int w = 2 * d2 + 1;
-    for (int sz = 0; sz < n[2]; sz++)
-        for (int sy = 0; sy < n[1]; sy++)
-            for (int sx = 0; sx < n[0]; sx++) {
-                int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
-                if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-                int oi = (dx + d2) + w * ((dy + d2) + w * (dz + d2));
-                apply_op(d.op_m2l2 + ((size_t)oi * LPH + o) * LP, d.O2 + (size_t)(r.l2_0 + sx + n[0] * (sy + n[1] * sz)) * LP, re, im);
-            }
-    store_jk(d.L2 + (size_t)b * LP, o, re, im, false);
+template <typename R>
+size_t m2l_smem() { return sizeof(C2<R>) * (216 * LP + M2L_NB * LPH * LP); }
+
+// opt-in shared-memory sizes; called once per context creation (the
+// attribute is per device, so every context sets it for its own device)
+void init_force_kernels() {
+    cudaFuncSetAttribute(k_m2l_grp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<double>());
+    cudaFuncSetAttribute(k_m2l_grp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<float>());
 }
 
-void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int nrep, int d2, cudaStream_t st) {
-    (void)nrep;
+void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {
     k_p2m<<<ncell, 64, 0, st>>>(d);
     k_m2m<<<n3, 32, 0, st>>>(d, d.O4, d.O3, d.op_m2m43, d.b3rep, 3);
     k_m2m<<<n2, 32, 0, st>>>(d, d.O3, d.O2, d.op_m2m32, d.b2rep, 2);
-    k_m2l_l2<<<n2, 32, 0, st>>>(d, d2);
+    k_m2l_l2<<<n2, 8 * LPH, 0, st>>>(d, d2);
     k_l2l<<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
-    k_m2l_win<<<n3, 8 * LPH, 0, st>>>(d, d.O3, d.L3, d.op_m2l3, d.b3rep, 3);
-    k_l2l<<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
-    k_m2l_win<<<ncell, 8 * LPH, 0, st>>>(d, d.O4, d.L4, d.op_m2l4, d.crep, 4);
+    if (mixed) {
+        k_m2l_grp<float><<<n2, 128, m2l_smem<float>(), st>>>(d, d.O3, d.L3, (const C2<float> *)d.op32_m2l3, d.b2rep, 3);
+        k_l2l<<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
+        k_m2l_grp<float><<<n3, 128, m2l_smem<float>(), st>>>(d, d.O4, d.L4, (const C2<float> *)d.op32_m2l4, d.b3rep, 4);
+    } else {
+        k_m2l_grp<double><<<n2, 128, m2l_smem<double>(), st>>>(d, d.O3, d.L3, (const C2<double> *)d.op_m2l3, d.b2rep, 3);
+        k_l2l<<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
+        k_m2l_grp<double><<<n3, 128, m2l_smem<double>(), st>>>(d, d.O4, d.L4, (const C2<double> *)d.op_m2l4, d.b3rep, 4);
+    }
 }
 
 // ------------------------------------------------------------------ per-site terms
@@ -600,209 +670,287 @@ __global__ void k_site_forces(Dev d, int nsite, int terms) {
         fy += 48.0 / pow13(y - r.rhs[1]); fy += 48.0 / pow13(r.rhs[1] + y);
         fz += 48.0 / pow13(z - r.rhs[2]); fz += 48.0 / pow13(r.rhs[2] + z);
     }
-    if (terms & SESP_T_GRAPHITE) {
-        double eps, sg6;
-        int col = graphite_column(d, r, g, eps, sg6);
-        if (col >= 0) graphite_site(d, col, x, y, z, eps, sg6, fx, fy, fz, nullptr);
-    }
     d.fx[g] = fx; d.fy[g] = fy; d.fz[g] = fz;
 }
 
-void launch_site_forces(const Dev &d, int nsite, int terms, cudaStream_t st) {
+// sites the graphite acts on, listed at every rebuild (their cells are frozen
+// until the next one); list order does not enter any sum
+__global__ void k_graphite_list(Dev d, int nsite) {
+    int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nsite) return;
+    const Rep r = d.rep[d.mrep[d.smol[g]]];
+    double eps, sg6;
+    if (graphite_column(d, r, g, eps, sg6) >= 0) d.gsite[atomicAdd(d.gcount, 1)] = g;
+}
+
+// graphite LJ (src/eval_graphite.f90:80-185), one warp per listed site: the
+// lanes split the column's carbons and a fixed shuffle tree sums them
+template <typename R>
+__global__ void k_graphite(Dev d) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int n = *d.gcount;
+    const R rc2 = (R)(RC * RC);
+    for (int k = warp; k < n; k += nwarp) {
+        int g = d.gsite[k];
+        const Rep r = d.rep[d.mrep[d.smol[g]]];
+        double eps, sg6;
+        int col = graphite_column(d, r, g, eps, sg6);
+        double xd = d.x[g], yd = d.y[g], zd = d.z[g];
+        R e48 = (R)(48.0 * eps * sg6), s6 = (R)sg6;
+        R fx = 0, fy = 0, fz = 0;
+        for (int q = d.gcol_start[col] + lane; q < d.gcol_start[col + 1]; q += 32) {
+            double4 c = d.gpos[q];
+            R xij = (R)(xd - c.x), yij = (R)(yd - c.y), zij = (R)(zd - c.z);
+            R r2 = xij * xij + yij * yij + zij * zij;
+            if (r2 <= rc2) {
+                R rsi = R(1) / r2, r6 = rsi * rsi * rsi;
+                R flj = e48 * r6 * (s6 * r6 - R(0.5)) * rsi;
+                fx += xij * flj; fy += yij * flj; fz += zij * flj;
+            }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+            fx += __shfl_down_sync(0xffffffffu, fx, off);
+            fy += __shfl_down_sync(0xffffffffu, fy, off);
+            fz += __shfl_down_sync(0xffffffffu, fz, off);
+        }
+        if (lane == 0) { d.fx[g] += (double)fx; d.fy[g] += (double)fy; d.fz[g] += (double)fz; }
+    }
+}
+
+void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st) {
+    cudaMemsetAsync(d.gcount, 0, sizeof(int), st);
+    k_graphite_list<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite);
+}
+
+void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st) {
     k_site_forces<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
+    if (terms & SESP_T_GRAPHITE) {
+        if (mixed) k_graphite<float><<<152 * 4, 256, 0, st>>>(d);
+        else k_graphite<double><<<152 * 4, 256, 0, st>>>(d);
+    }
 }
 
 // ------------------------------------------------------------------ surfactant intramolecular
 
-struct Mol29 {
+// positions of one surfactant (shared memory in the force kernel)
+struct Pos29 {
     double x[NSURF], y[NSURF], z[NSURF];
-    double fx[NSURF], fy[NSURF], fz[NSURF];
 };
 
-// src/eval_valence.f90:104-145
-__device__ double valence(Mol29 &m, bool force) {
-    double e = 0.0;
-    for (int i = 0; i < NANGLE; i++) {
-        int a = cT.ai[i], b = cT.aj[i], c = cT.ak[i];
-        double rxji = m.x[a] - m.x[b], ryji = m.y[a] - m.y[b], rzji = m.z[a] - m.z[b];
-        double rxki = m.x[c] - m.x[b], ryki = m.y[c] - m.y[b], rzki = m.z[c] - m.z[b];
-        double dp = rxji * rxki + ryji * ryki + rzji * rzki;
-        double rjin = sqrt(rxji * rxji + ryji * ryji + rzji * rzji);
-        double rkin = sqrt(rxki * rxki + ryki * ryki + rzki * rzki);
-        double th = acos(dp / rjin / rkin);
-        double costh = cos(th);
-        double dth = th - cT.th[i];
-        e += 0.5 * cT.rkth[i] * dth * dth;
-        if (!force) continue;
-        double r1 = cT.rkth[i] * dth / sin(th);
-        double fjx = rxki / rjin / rkin - costh * rxji / (rjin * rjin);
-        double fjy = ryki / rjin / rkin - costh * ryji / (rjin * rjin);
-        double fjz = rzki / rjin / rkin - costh * rzji / (rjin * rjin);
-        double fkx = rxji / rjin / rkin - costh * rxki / (rkin * rkin);
-        double fky = ryji / rjin / rkin - costh * ryki / (rkin * rkin);
-        double fkz = rzji / rjin / rkin - costh * rzki / (rkin * rkin);
-        m.fx[a] += r1 * fjx; m.fy[a] += r1 * fjy; m.fz[a] += r1 * fjz;
-        m.fx[b] -= r1 * (fjx + fkx); m.fy[b] -= r1 * (fjy + fky); m.fz[b] -= r1 * (fjz + fkz);
-        m.fx[c] += r1 * fkx; m.fy[c] += r1 * fky; m.fz[c] += r1 * fkz;
-    }
-    return e;
+// one harmonic angle (src/eval_valence.f90:104-145): forces on its 3 sites
+__device__ double angle_term(const Pos29 &m, int i, double f[3][3]) {
+    int a = cT.ai[i], b = cT.aj[i], c = cT.ak[i];
+    double rxji = m.x[a] - m.x[b], ryji = m.y[a] - m.y[b], rzji = m.z[a] - m.z[b];
+    double rxki = m.x[c] - m.x[b], ryki = m.y[c] - m.y[b], rzki = m.z[c] - m.z[b];
+    double dp = rxji * rxki + ryji * ryki + rzji * rzki;
+    double rjin = sqrt(rxji * rxji + ryji * ryji + rzji * rzji);
+    double rkin = sqrt(rxki * rxki + ryki * ryki + rzki * rzki);
+    double th = acos(dp / rjin / rkin);
+    double costh = cos(th);
+    double dth = th - cT.th[i];
+    double r1 = cT.rkth[i] * dth / sin(th);
+    double fjx = rxki / rjin / rkin - costh * rxji / (rjin * rjin);
+    double fjy = ryki / rjin / rkin - costh * ryji / (rjin * rjin);
+    double fjz = rzki / rjin / rkin - costh * rzji / (rjin * rjin);
+    double fkx = rxji / rjin / rkin - costh * rxki / (rkin * rkin);
+    double fky = ryji / rjin / rkin - costh * ryki / (rkin * rkin);
+    double fkz = rzji / rjin / rkin - costh * rzki / (rkin * rkin);
+    f[0][0] = r1 * fjx; f[0][1] = r1 * fjy; f[0][2] = r1 * fjz;
+    f[1][0] = -r1 * (fjx + fkx); f[1][1] = -r1 * (fjy + fky); f[1][2] = -r1 * (fjz + fkz);
+    f[2][0] = r1 * fkx; f[2][1] = r1 * fky; f[2][2] = r1 * fkz;
+    return 0.5 * cT.rkth[i] * dth * dth;
 }
 
-// dihedral force on the four sites from r1 = -dU/dcos(phi), written with the
-// same cross-product algebra as src/eval_dihedral.f90:116-271
-__device__ double dihedral(Mol29 &m, int i0, int i1, bool berendsen, bool force) {
-    double e = 0.0;
+// one dihedral: r1 = -dU/dcos(phi) applied with the cross-product algebra of
+// src/eval_dihedral.f90:116-271 (triple cosine, dihedrals 1-18) or
+// src/eval_dihedral_berendsen.f90 (cos 3 phi, dihedrals 19-30)
+__device__ double dihedral_term(const Pos29 &m, int i, double f[4][3]) {
+    const bool berendsen = i >= 18;
     const double clampv = berendsen ? 0.999999 : 0.99999999999;
-    for (int i = i0; i < i1; i++) {
-        int iv = cT.di[i], jv = cT.dj[i], kv = cT.dk[i], lv = cT.dl[i];
-        double ax = m.x[jv] - m.x[iv], ay = m.y[jv] - m.y[iv], az = m.z[jv] - m.z[iv];   // r_ji
-        double bx = m.x[kv] - m.x[jv], by = m.y[kv] - m.y[jv], bz = m.z[kv] - m.z[jv];   // r_kj
-        double cx = m.x[lv] - m.x[kv], cy = m.y[lv] - m.y[kv], cz = m.z[lv] - m.z[kv];   // r_nk
-        double u1 = ax * by - ay * bx, u2 = ax * bz - az * bx, u3 = ay * bz - az * by;
-        double v1 = bx * cy - by * cx, v2 = bx * cz - bz * cx, v3 = by * cz - bz * cy;
-        double nu = sqrt(u1 * u1 + u2 * u2 + u3 * u3), nv = sqrt(v1 * v1 + v2 * v2 + v3 * v3);
-        double arg = (u1 * v1 + u2 * v2 + u3 * v3) / nu / nv;
-        if (arg <= -1.0) arg = -clampv;
-        if (arg >= 1.0) arg = clampv;
-        double th = acos(arg), costh = cos(th), sinth = sin(th);
-        double r1;
-        if (berendsen) {
-            r1 = -3.0 * cT.dva[i] * sin(3.0 * th) / sinth;
-            e += cT.dva[i] * (1.0 + cos(3.0 * th));
-        } else {
-            r1 = -cT.dva[i] + 2.0 * cT.dvb[i] * sin(2.0 * th) / sinth - 3.0 * cT.dvc[i] * sin(3.0 * th) / sinth;
-            e += cT.dva[i] * (1.0 + cos(th)) + cT.dvb[i] * (1.0 - cos(2.0 * th)) + cT.dvc[i] * (1.0 + cos(3.0 * th));
-        }
-        if (!force) continue;
-        double nuv = nu * nv, nu2 = nu * nu, nv2 = nv * nv;
-        // site i
-        double fix = (bx * (-by * cy - bz * cz) + cx * (by * by + bz * bz)) / nuv;
-        double fiy = (by * (-bx * cx - bz * cz) + cy * (bx * bx + bz * bz)) / nuv;
-        double fiz = (bz * (-bx * cx - by * cy) + cz * (bx * bx + by * by)) / nuv;
-        double gix = (2.0 * ax * (-by * by - bz * bz) + 2.0 * bx * (ay * by + az * bz)) / nu2;
-        double giy = (2.0 * ay * (-bx * bx - bz * bz) + 2.0 * by * (ax * bx + az * bz)) / nu2;
-        double giz = (2.0 * az * (-bx * bx - by * by) + 2.0 * bz * (ax * bx + ay * by)) / nu2;
-        // site j
-        double fjx = (ax * (-by * cy - bz * cz) + bx * (by * cy + bz * cz) + cx * (-ay * by - az * bz - by * by - bz * bz) +
-                      2.0 * bx * (ay * cy + az * cz)) / nuv;
-        double fjy = (ay * (-bx * cx - bz * cz) + by * (bx * cx + bz * cz) + cy * (-ax * bx - az * bz - bx * bx - bz * bz) +
-                      2.0 * by * (ax * cx + az * cz)) / nuv;
-        double fjz = (az * (-bx * cx - by * cy) + bz * (bx * cx + by * cy) + cz * (-ax * bx - ay * by - bx * bx - by * by) +
-                      2.0 * bz * (ax * cx + ay * cy)) / nuv;
-        double gjx = (2.0 * ax * (by * by + bz * bz + ay * by + az * bz) + 2.0 * bx * (-ay * ay - az * az - ay * by - az * bz)) / nu2 +
-                     (2.0 * cx * (by * cy + bz * cz) + 2.0 * bx * (-cy * cy - cz * cz)) / nv2;
-        double gjy = (2.0 * ay * (bx * bx + bz * bz + ax * bx + az * bz) + 2.0 * by * (-ax * ax - az * az - ax * bx - az * bz)) / nu2 +
-                     (2.0 * cy * (bx * cx + bz * cz) + 2.0 * by * (-cx * cx - cz * cz)) / nv2;
-        double gjz = (2.0 * az * (bx * bx + by * by + ax * bx + ay * by) + 2.0 * bz * (-ax * ax - ay * ay - ax * bx - ay * by)) / nu2 +
-                     (2.0 * cz * (bx * cx + by * cy) + 2.0 * bz * (-cx * cx - cy * cy)) / nv2;
-        // site k
-        double fkx = (ax * (by * by + bz * bz + by * cy + bz * cz) + bx * (-ay * by - az * bz) + cx * (ay * by + az * bz) +
-                      2.0 * bx * (-ay * cy - az * cz)) / nuv;
-        double fky = (ay * (bx * bx + bz * bz + bx * cx + bz * cz) + by * (-ax * bx - az * bz) + cy * (ax * bx + az * bz) +
-                      2.0 * by * (-ax * cx - az * cz)) / nuv;
-        double fkz = (az * (bx * bx + by * by + bx * cx + by * cy) + bz * (-ax * bx - ay * by) + cz * (ax * bx + ay * by) +
-                      2.0 * bz * (-ax * cx - ay * cy)) / nuv;
-        double gkx = (2.0 * ax * (-ay * by - az * bz) + 2.0 * bx * (ay * ay + az * az)) / nu2 +
-                     (2.0 * cx * (-by * by - bz * bz - by * cy - bz * cz) + 2.0 * bx * (cy * cy + cz * cz + by * cy + bz * cz)) / nv2;
-        double gky = (2.0 * ay * (-ax * bx - az * bz) + 2.0 * by * (ax * ax + az * az)) / nu2 +
-                     (2.0 * cy * (-bx * bx - bz * bz - bx * cx - bz * cz) + 2.0 * by * (cx * cx + cz * cz + bx * cx + bz * cz)) / nv2;
-        double gkz = (2.0 * az * (-ax * bx - ay * by) + 2.0 * bz * (ax * ax + ay * ay)) / nu2 +
-                     (2.0 * cz * (-bx * bx - by * by - bx * cx - by * cy) + 2.0 * bz * (cx * cx + cy * cy + bx * cx + by * cy)) / nv2;
-        // site n
-        double fnx = (ax * (-by * by - bz * bz) + bx * (ay * by + az * bz)) / nuv;
-        double fny = (ay * (-bx * bx - bz * bz) + by * (ax * bx + az * bz)) / nuv;
-        double fnz = (az * (-bx * bx - by * by) + bz * (ax * bx + ay * by)) / nuv;
-        double gnx = (2.0 * cx * (by * by + bz * bz) + 2.0 * bx * (-by * cy - bz * cz)) / nv2;
-        double gny = (2.0 * cy * (bx * bx + bz * bz) + 2.0 * by * (-bx * cx - bz * cz)) / nv2;
-        double gnz = (2.0 * cz * (bx * bx + by * by) + 2.0 * bz * (-bx * cx - by * cy)) / nv2;
-        double h = 0.5 * costh;
-        m.fx[iv] += r1 * (fix - h * gix); m.fy[iv] += r1 * (fiy - h * giy); m.fz[iv] += r1 * (fiz - h * giz);
-        m.fx[jv] += r1 * (fjx - h * gjx); m.fy[jv] += r1 * (fjy - h * gjy); m.fz[jv] += r1 * (fjz - h * gjz);
-        m.fx[kv] += r1 * (fkx - h * gkx); m.fy[kv] += r1 * (fky - h * gky); m.fz[kv] += r1 * (fkz - h * gkz);
-        m.fx[lv] += r1 * (fnx - h * gnx); m.fy[lv] += r1 * (fny - h * gny); m.fz[lv] += r1 * (fnz - h * gnz);
+    int iv = cT.di[i], jv = cT.dj[i], kv = cT.dk[i], lv = cT.dl[i];
+    double ax = m.x[jv] - m.x[iv], ay = m.y[jv] - m.y[iv], az = m.z[jv] - m.z[iv];   // r_ji
+    double bx = m.x[kv] - m.x[jv], by = m.y[kv] - m.y[jv], bz = m.z[kv] - m.z[jv];   // r_kj
+    double cx = m.x[lv] - m.x[kv], cy = m.y[lv] - m.y[kv], cz = m.z[lv] - m.z[kv];   // r_nk
+    double u1 = ax * by - ay * bx, u2 = ax * bz - az * bx, u3 = ay * bz - az * by;
+    double v1 = bx * cy - by * cx, v2 = bx * cz - bz * cx, v3 = by * cz - bz * cy;
+    double nu = sqrt(u1 * u1 + u2 * u2 + u3 * u3), nv = sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+    double arg = (u1 * v1 + u2 * v2 + u3 * v3) / nu / nv;
+    if (arg <= -1.0) arg = -clampv;
+    if (arg >= 1.0) arg = clampv;
+    double th = acos(arg), costh = cos(th), sinth = sin(th);
+    double r1, e;
+    if (berendsen) {
+        r1 = -3.0 * cT.dva[i] * sin(3.0 * th) / sinth;
+        e = cT.dva[i] * (1.0 + cos(3.0 * th));
+    } else {
+        r1 = -cT.dva[i] + 2.0 * cT.dvb[i] * sin(2.0 * th) / sinth - 3.0 * cT.dvc[i] * sin(3.0 * th) / sinth;
+        e = cT.dva[i] * (1.0 + cos(th)) + cT.dvb[i] * (1.0 - cos(2.0 * th)) + cT.dvc[i] * (1.0 + cos(3.0 * th));
     }
+    double nuv = nu * nv, nu2 = nu * nu, nv2 = nv * nv;
+    double fix = (bx * (-by * cy - bz * cz) + cx * (by * by + bz * bz)) / nuv;
+    double fiy = (by * (-bx * cx - bz * cz) + cy * (bx * bx + bz * bz)) / nuv;
+    double fiz = (bz * (-bx * cx - by * cy) + cz * (bx * bx + by * by)) / nuv;
+    double gix = (2.0 * ax * (-by * by - bz * bz) + 2.0 * bx * (ay * by + az * bz)) / nu2;
+    double giy = (2.0 * ay * (-bx * bx - bz * bz) + 2.0 * by * (ax * bx + az * bz)) / nu2;
+    double giz = (2.0 * az * (-bx * bx - by * by) + 2.0 * bz * (ax * bx + ay * by)) / nu2;
+    double fjx = (ax * (-by * cy - bz * cz) + bx * (by * cy + bz * cz) + cx * (-ay * by - az * bz - by * by - bz * bz) +
+                  2.0 * bx * (ay * cy + az * cz)) / nuv;
+    double fjy = (ay * (-bx * cx - bz * cz) + by * (bx * cx + bz * cz) + cy * (-ax * bx - az * bz - bx * bx - bz * bz) +
+                  2.0 * by * (ax * cx + az * cz)) / nuv;
+    double fjz = (az * (-bx * cx - by * cy) + bz * (bx * cx + by * cy) + cz * (-ax * bx - ay * by - bx * bx - by * by) +
+                  2.0 * bz * (ax * cx + ay * cy)) / nuv;
+    double gjx = (2.0 * ax * (by * by + bz * bz + ay * by + az * bz) + 2.0 * bx * (-ay * ay - az * az - ay * by - az * bz)) / nu2 +
+                 (2.0 * cx * (by * cy + bz * cz) + 2.0 * bx * (-cy * cy - cz * cz)) / nv2;
+    double gjy = (2.0 * ay * (bx * bx + bz * bz + ax * bx + az * bz) + 2.0 * by * (-ax * ax - az * az - ax * bx - az * bz)) / nu2 +
+                 (2.0 * cy * (bx * cx + bz * cz) + 2.0 * by * (-cx * cx - cz * cz)) / nv2;
+    double gjz = (2.0 * az * (bx * bx + by * by + ax * bx + ay * by) + 2.0 * bz * (-ax * ax - ay * ay - ax * bx - ay * by)) / nu2 +
+                 (2.0 * cz * (bx * cx + by * cy) + 2.0 * bz * (-cx * cx - cy * cy)) / nv2;
+    double fkx = (ax * (by * by + bz * bz + by * cy + bz * cz) + bx * (-ay * by - az * bz) + cx * (ay * by + az * bz) +
+                  2.0 * bx * (-ay * cy - az * cz)) / nuv;
+    double fky = (ay * (bx * bx + bz * bz + bx * cx + bz * cz) + by * (-ax * bx - az * bz) + cy * (ax * bx + az * bz) +
+                  2.0 * by * (-ax * cx - az * cz)) / nuv;
+    double fkz = (az * (bx * bx + by * by + bx * cx + by * cy) + bz * (-ax * bx - ay * by) + cz * (ax * bx + ay * by) +
+                  2.0 * bz * (-ax * cx - ay * cy)) / nuv;
+    double gkx = (2.0 * ax * (-ay * by - az * bz) + 2.0 * bx * (ay * ay + az * az)) / nu2 +
+                 (2.0 * cx * (-by * by - bz * bz - by * cy - bz * cz) + 2.0 * bx * (cy * cy + cz * cz + by * cy + bz * cz)) / nv2;
+    double gky = (2.0 * ay * (-ax * bx - az * bz) + 2.0 * by * (ax * ax + az * az)) / nu2 +
+                 (2.0 * cy * (-bx * bx - bz * bz - bx * cx - bz * cz) + 2.0 * by * (cx * cx + cz * cz + bx * cx + bz * cz)) / nv2;
+    double gkz = (2.0 * az * (-ax * bx - ay * by) + 2.0 * bz * (ax * ax + ay * ay)) / nu2 +
+                 (2.0 * cz * (-bx * bx - by * by - bx * cx - by * cy) + 2.0 * bz * (cx * cx + cy * cy + bx * cx + by * cy)) / nv2;
+    double fnx = (ax * (-by * by - bz * bz) + bx * (ay * by + az * bz)) / nuv;
+    double fny = (ay * (-bx * bx - bz * bz) + by * (ax * bx + az * bz)) / nuv;
+    double fnz = (az * (-bx * bx - by * by) + bz * (ax * bx + ay * by)) / nuv;
+    double gnx = (2.0 * cx * (by * by + bz * bz) + 2.0 * bx * (-by * cy - bz * cz)) / nv2;
+    double gny = (2.0 * cy * (bx * bx + bz * bz) + 2.0 * by * (-bx * cx - bz * cz)) / nv2;
+    double gnz = (2.0 * cz * (bx * bx + by * by) + 2.0 * bz * (-bx * cx - by * cy)) / nv2;
+    double h = 0.5 * costh;
+    f[0][0] = r1 * (fix - h * gix); f[0][1] = r1 * (fiy - h * giy); f[0][2] = r1 * (fiz - h * giz);
+    f[1][0] = r1 * (fjx - h * gjx); f[1][1] = r1 * (fjy - h * gjy); f[1][2] = r1 * (fjz - h * gjz);
+    f[2][0] = r1 * (fkx - h * gkx); f[2][1] = r1 * (fky - h * gky); f[2][2] = r1 * (fkz - h * gkz);
+    f[3][0] = r1 * (fnx - h * gnx); f[3][1] = r1 * (fny - h * gny); f[3][2] = r1 * (fnz - h * gnz);
     return e;
 }
 
-__device__ inline double lj_eps_sg6(const Dev &d, int ti, int tj, double &sg6) {
-    double2 v = d.ljt[ti * NTYPE + tj];
-    sg6 = v.y;
-    return v.x;  // 48 eps sg6
-}
-
-// one intramolecular nonbonded pair (Coulomb + LJ without cutoff)
-__device__ inline double intra_pair(const Dev &d, Mol29 &m, int a, int b, bool force) {
+// one intramolecular nonbonded pair, Coulomb + LJ without cutoff
+// (src/eval_surfactant_internal.f90:169-200, 206-242)
+__device__ inline double ipair_term(const Dev &d, const Pos29 &m, int a, int b, double f[2][3]) {
     double x = m.x[a] - m.x[b], y = m.y[a] - m.y[b], z = m.z[a] - m.z[b];
     double rsq = x * x + y * y + z * z;
     double rsi = 1.0 / rsq, ir = sqrt(rsi), r6 = rsi * rsi * rsi;
     double qq = cT.q[2 + a] * cT.q[2 + b] * XPI;
-    double sg6;
-    double e48 = lj_eps_sg6(d, 2 + a, 2 + b, sg6);
-    if (force) {
-        double ft = qq * ir * rsi + e48 * r6 * (sg6 * r6 - 0.5) * rsi;
-        m.fx[a] += x * ft; m.fy[a] += y * ft; m.fz[a] += z * ft;
-        m.fx[b] -= x * ft; m.fy[b] -= y * ft; m.fz[b] -= z * ft;
-    }
-    return qq * ir + (e48 / 12.0) * (sg6 * r6 * r6 - r6);
+    double2 lj = d.ljt[(2 + a) * NTYPE + 2 + b];   // (48 eps sg6, sg6)
+    double ft = qq * ir * rsi + lj.x * r6 * (lj.y * r6 - 0.5) * rsi;
+    f[0][0] = x * ft; f[0][1] = y * ft; f[0][2] = z * ft;
+    f[1][0] = -x * ft; f[1][1] = -y * ft; f[1][2] = -z * ft;
+    return qq * ir + (lj.x / 12.0) * (lj.y * r6 * r6 - r6);
 }
 
-// src/eval_surfactant_internal.f90:153-246
-__device__ double internal(const Dev &d, Mol29 &m, bool force) {
+// the far-field correction of one site (src/eval_subtract_fma.f90:14-53):
+// minus the Coulomb force of its own molecule's sites outside its 27-cell block
+__device__ inline double subtract_site(const Pos29 &m, int j, uint32_t bits, double f[3]) {
     double e = 0.0;
-    for (int j = 0; j < 15; j++)
-        for (int k = j + 4; k < NSURF; k++) e += intra_pair(d, m, j, k, force);
-    for (int k = 0; k < NSELF; k++) e += intra_pair(d, m, cT.si[k], cT.sj[k], force);
+    f[0] = f[1] = f[2] = 0.0;
+    while (bits) {
+        int k = __ffs(bits) - 1;
+        bits &= bits - 1;
+        double x = m.x[j] - m.x[k], y = m.y[j] - m.y[k], z = m.z[j] - m.z[k];
+        double rmn = sqrt(x * x + y * y + z * z);
+        double qq = cT.q[2 + j] * cT.q[2 + k] * XPI;
+        double fel = qq / (rmn * rmn * rmn);
+        f[0] -= x * fel; f[1] -= y * fel; f[2] -= z * fel;
+        e -= 0.5 * qq / rmn;
+    }
     return e;
 }
 
-// src/eval_subtract_fma.f90:14-53
-__device__ double subtract(const Dev &d, Mol29 &m, const uint32_t *mask, bool force) {
-    double e = 0.0;
-    for (int j = 0; j < NSURF; j++) {
-        uint32_t bits = mask[j];
-        while (bits) {
-            int k = __ffs(bits) - 1;
-            bits &= bits - 1;
-            double x = m.x[j] - m.x[k], y = m.y[j] - m.y[k], z = m.z[j] - m.z[k];
-            double rmn = sqrt(x * x + y * y + z * z);
-            double qq = cT.q[2 + j] * cT.q[2 + k] * XPI;
-            if (force) {
-                double fel = qq / (rmn * rmn * rmn);
-                m.fx[j] -= x * fel; m.fy[j] -= y * fel; m.fz[j] -= z * fel;
-            }
-            e -= 0.5 * qq / rmn;
+// One block per surfactant: the 36 angles, 30 dihedrals and 312
+// intramolecular pairs are spread over the threads, each writing its site
+// forces to its own slots in shared memory; then thread s sums the slots of
+// site s in the fixed order of the contribution table (deterministic, no
+// atomics) and adds its far-field correction.
+constexpr int NIPAIR = 270 + NSELF;                 // k >= j+4 pairs of sites 1..15, then the 42 listed
+constexpr int NSLOT = NANGLE * 3 + NDIH * 4 + NIPAIR * 2;
+constexpr int NTERM = NANGLE + NDIH + NIPAIR;
+
+struct IntraMap {
+    short off[NSURF + 1];  // slots of site s: list[off[s] .. off[s+1])
+    short list[NSLOT];
+    unsigned char pa[NIPAIR], pb[NIPAIR];
+};
+static __constant__ IntraMap cMap;
+
+void upload_intra_map(const void *host_map, cudaStream_t st) {
+    cudaMemcpyToSymbolAsync(cMap, host_map, sizeof(IntraMap), 0, cudaMemcpyHostToDevice, st);
+}
+size_t intra_map_size() { return sizeof(IntraMap); }
+
+__global__ void __launch_bounds__(128) k_intra_block(Dev d, const int *smols, int terms) {
+    __shared__ Pos29 m;
+    __shared__ double sf[NSLOT][3];
+    const int t = blockIdx.x;
+    const int g0 = d.mfirst[smols[t]];
+    if (threadIdx.x < NSURF) {
+        m.x[threadIdx.x] = d.x[g0 + threadIdx.x];
+        m.y[threadIdx.x] = d.y[g0 + threadIdx.x];
+        m.z[threadIdx.x] = d.z[g0 + threadIdx.x];
+    }
+    __syncthreads();
+    for (int w = threadIdx.x; w < NTERM; w += blockDim.x) {
+        if (w < NANGLE) {
+            double f[3][3] = {{0}};
+            if (terms & SESP_T_VALENCE) angle_term(m, w, f);
+            for (int k = 0; k < 3; k++) for (int c = 0; c < 3; c++) sf[w * 3 + k][c] = f[k][c];
+        } else if (w < NANGLE + NDIH) {
+            int i = w - NANGLE;
+            double f[4][3] = {{0}};
+            if ((i < 18 && (terms & SESP_T_DIHEDRAL)) || (i >= 18 && (terms & SESP_T_BERENDSEN))) dihedral_term(m, i, f);
+            for (int k = 0; k < 4; k++) for (int c = 0; c < 3; c++) sf[NANGLE * 3 + i * 4 + k][c] = f[k][c];
+        } else {
+            int q = w - NANGLE - NDIH;
+            double f[2][3] = {{0}};
+            if (terms & SESP_T_INTERNAL) ipair_term(d, m, cMap.pa[q], cMap.pb[q], f);
+            int s0 = NANGLE * 3 + NDIH * 4 + 2 * q;
+            for (int k = 0; k < 2; k++) for (int c = 0; c < 3; c++) sf[s0 + k][c] = f[k][c];
         }
     }
-    return e;
-}
-
-__global__ void k_intra(Dev d, const int *smols, int ns, int terms, double *e_mol) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ns) return;
-    int mol = smols[t];
-    int g0 = d.mfirst[mol];
-    Mol29 m;
-    for (int i = 0; i < NSURF; i++) {
-        m.x[i] = d.x[g0 + i]; m.y[i] = d.y[g0 + i]; m.z[i] = d.z[g0 + i];
-        m.fx[i] = 0.0; m.fy[i] = 0.0; m.fz[i] = 0.0;
-    }
-    bool force = e_mol == nullptr;
-    double eb = 0.0, ei = 0.0, es = 0.0;
-    if (terms & SESP_T_VALENCE) eb += valence(m, force);
-    if (terms & SESP_T_DIHEDRAL) eb += dihedral(m, 0, 18, false, force);
-    if (terms & SESP_T_BERENDSEN) eb += dihedral(m, 18, 30, true, force);
-    if (terms & SESP_T_INTERNAL) ei += internal(d, m, force);
-    if (terms & SESP_T_SUBTRACT) es += subtract(d, m, d.isub + (size_t)t * NSURF, force);
-    if (force) {
-        for (int i = 0; i < NSURF; i++) { d.fx[g0 + i] += m.fx[i]; d.fy[g0 + i] += m.fy[i]; d.fz[g0 + i] += m.fz[i]; }
-    } else {
-        e_mol[3 * t] = eb; e_mol[3 * t + 1] = ei; e_mol[3 * t + 2] = es;
+    __syncthreads();
+    if (threadIdx.x < NSURF) {
+        int s = threadIdx.x;
+        double fx = 0.0, fy = 0.0, fz = 0.0;
+        for (int k = cMap.off[s]; k < cMap.off[s + 1]; k++) {
+            int sl = cMap.list[k];
+            fx += sf[sl][0]; fy += sf[sl][1]; fz += sf[sl][2];
+        }
+        if (terms & SESP_T_SUBTRACT) {
+            double f[3];
+            subtract_site(m, s, d.isub[(size_t)t * NSURF + s], f);
+            fx += f[0]; fy += f[1]; fz += f[2];
+        }
+        d.fx[g0 + s] += fx; d.fy[g0 + s] += fy; d.fz[g0 + s] += fz;
     }
 }
 
 void launch_intra(const Dev &d, const int *smols, int ns, int terms, cudaStream_t st) {
     if (ns && (terms & (SESP_T_VALENCE | SESP_T_DIHEDRAL | SESP_T_BERENDSEN | SESP_T_INTERNAL | SESP_T_SUBTRACT)))
-        k_intra<<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, terms, nullptr);
+        k_intra_block<<<ns, 128, 0, st>>>(d, smols, terms);
+}
+
+// energies of one surfactant's intramolecular terms (diagnostic path)
+__global__ void k_intra_energy(Dev d, const int *smols, int ns, double *e_mol) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns) return;
+    int g0 = d.mfirst[smols[t]];
+    Pos29 m;
+    for (int i = 0; i < NSURF; i++) { m.x[i] = d.x[g0 + i]; m.y[i] = d.y[g0 + i]; m.z[i] = d.z[g0 + i]; }
+    double eb = 0.0, ei = 0.0, es = 0.0;
+    double f4[4][3], f3[3][3], f2[2][3], f1[3];
+    for (int i = 0; i < NANGLE; i++) eb += angle_term(m, i, f3);
+    for (int i = 0; i < NDIH; i++) eb += dihedral_term(m, i, f4);
+    for (int q = 0; q < NIPAIR; q++) ei += ipair_term(d, m, cMap.pa[q], cMap.pb[q], f2);
+    for (int j = 0; j < NSURF; j++) es += subtract_site(m, j, d.isub[(size_t)t * NSURF + j], f1);
+    e_mol[3 * t] = eb; e_mol[3 * t + 1] = ei; e_mol[3 * t + 2] = es;
 }
 
 // ------------------------------------------------------------------ energies (diagnostic path)
@@ -920,7 +1068,7 @@ void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int n
                      double *e_mol, cudaStream_t st) {
     k_energy_slot<<<ncell, 128, 0, st>>>(d, e_slot);
     k_energy_site<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, e_site);
-    if (ns) k_intra<<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, SESP_T_ALL, e_mol);
+    if (ns) k_intra_energy<<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, e_mol);
 }
 
 }  // namespace sesp

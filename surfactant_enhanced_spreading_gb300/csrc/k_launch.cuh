@@ -21,8 +21,12 @@ void upload_tables_force(const Tables &t, cudaStream_t st);
 void launch_sort(const Dev &d, int nsite, int ncell, cudaStream_t st);
 void launch_gather(const Dev &d, int nslot, int ncell, int mixed, cudaStream_t st);
 void launch_near(const Dev &d, int ncell, int mixed, int terms, cudaStream_t st);
-void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int nrep, int d2, cudaStream_t st);
-void launch_site_forces(const Dev &d, int nsite, int terms, cudaStream_t st);
+void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st);
+void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st);
+void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st);
+void init_force_kernels();
+void upload_intra_map(const void *host_map, cudaStream_t st);
+size_t intra_map_size();
 void launch_intra(const Dev &d, const int *smols, int ns, int terms, cudaStream_t st);
 void launch_count_pairs(const Dev &d, int ncell, unsigned long long *out, cudaStream_t st);
 void launch_flush(void *buf, size_t bytes, cudaStream_t st);

@@ -142,6 +142,40 @@ Tables make_tables() {
 
 namespace {
 
+// contribution table of the intramolecular kernel: term slots per site.
+// Layout (matches IntraMap in k_force.cu): short off[30], short list[852],
+// uchar pa[312], uchar pb[312].  Slots: angle a -> 3a + {i, vertex, k};
+// dihedral i -> 108 + 4i + {i, j, k, l}; pair q -> 228 + 2q + {a, b}.
+std::vector<unsigned char> make_intra_map(const Tables &T) {
+    const int npair = 270 + NSELF, nslot = NANGLE * 3 + NDIH * 4 + npair * 2;
+    std::vector<int> pa, pb;
+    for (int j = 0; j < 15; j++)
+        for (int k = j + 4; k < NSURF; k++) { pa.push_back(j); pb.push_back(k); }
+    for (int k = 0; k < NSELF; k++) { pa.push_back(T.si[k]); pb.push_back(T.sj[k]); }
+    std::vector<std::vector<short>> per(NSURF);
+    for (int a = 0; a < NANGLE; a++) {
+        per[T.ai[a]].push_back((short)(3 * a)); per[T.aj[a]].push_back((short)(3 * a + 1)); per[T.ak[a]].push_back((short)(3 * a + 2));
+    }
+    for (int i = 0; i < NDIH; i++) {
+        int b = NANGLE * 3 + 4 * i;
+        per[T.di[i]].push_back((short)b); per[T.dj[i]].push_back((short)(b + 1));
+        per[T.dk[i]].push_back((short)(b + 2)); per[T.dl[i]].push_back((short)(b + 3));
+    }
+    for (int q = 0; q < npair; q++) {
+        int b = NANGLE * 3 + NDIH * 4 + 2 * q;
+        per[pa[q]].push_back((short)b); per[pb[q]].push_back((short)(b + 1));
+    }
+    std::vector<short> off(NSURF + 1, 0), list;
+    for (int s = 0; s < NSURF; s++) { off[s] = (short)list.size(); for (short v : per[s]) list.push_back(v); }
+    off[NSURF] = (short)list.size();
+    std::vector<unsigned char> out(intra_map_size(), 0);
+    memcpy(out.data(), off.data(), sizeof(short) * (NSURF + 1));
+    memcpy(out.data() + sizeof(short) * (NSURF + 1), list.data(), sizeof(short) * nslot);
+    size_t o = sizeof(short) * (NSURF + 1 + nslot);
+    for (int q = 0; q < npair; q++) { out[o + q] = (unsigned char)pa[q]; out[o + npair + q] = (unsigned char)pb[q]; }
+    return out;
+}
+
 // LJ pair table (48 eps sg6, sg6) over the 31 site kinds; zero where the
 // reference adds no LJ (water H with anything)
 std::vector<double2> make_lj_table() {
@@ -342,19 +376,20 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         launch_locate(d, c->nmol, c->st);
         launch_sort(d, c->nsite, c->ncell, c->st);
         launch_isub(d, c->nsm * NSURF, c->smols, c->st);
+        launch_graphite_list(d, c->nsite, c->st);
         tstop(c, 5);
     }
     launch_gather(d, c->nsite, c->ncell, mixed, c->st);
     if (rebuild) {
         tstart(c, 6);
-        launch_fma_build(d, c->ncell, c->n3, c->n2, c->nrep, c->d2, c->st);
+        launch_fma_build(d, c->ncell, c->n3, c->n2, mixed, c->d2, c->st);
         tstop(c, 6);
     }
     tstart(c, 0);
     launch_near(d, c->ncell, mixed, terms, c->st);
     tstop(c, 0);
     tstart(c, 4);
-    launch_site_forces(d, c->nsite, terms, c->st);
+    launch_site_forces(d, c->nsite, terms, mixed, c->st);
     launch_intra(d, c->smols, c->nsm, terms, c->st);
     tstop(c, 4);
 }
@@ -420,7 +455,12 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (set_device(c)) { delete c; return SESP_ECUDA; }
     if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "stream"); }
     for (int k = 0; k < 16; k++) cudaEventCreate(&c->ev[k]);
+    init_force_kernels();
     Tables T = make_tables();
+    {
+        std::vector<unsigned char> map = make_intra_map(T);
+        upload_intra_map(map.data(), c->st);
+    }
     upload_tables_exact(T, c->st);
     upload_tables_force(T, c->st);
     if (cudaStreamSynchronize(c->st) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "table upload"); }
@@ -517,7 +557,8 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     if ((e = dalloc(c, &d.op_m2l4, (size_t)343 * LPH * LP)) || (e = dalloc(c, &d.op_m2l3, (size_t)343 * LPH * LP)) ||
         (e = dalloc(c, &d.op_m2l2, (size_t)w2 * w2 * w2 * LPH * LP)) || (e = dalloc(c, &d.op_m2m43, (size_t)8 * LPH * LP)) ||
         (e = dalloc(c, &d.op_m2m32, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_l2l23, (size_t)8 * LPH * LP)) ||
-        (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)))
+        (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op32_m2l4, (size_t)343 * LPH * LP)) ||
+        (e = dalloc(c, &d.op32_m2l3, (size_t)343 * LPH * LP)))
         return e;
     // static per-site / per-molecule / per-box data
     std::vector<uint8_t> ptype(N);
@@ -563,11 +604,11 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
             }
     }
     if ((e = dalloc(c, &d.axis, axis.size())) || (e = dalloc(c, &d.gcol_start, gstart.size())) ||
-        (e = dalloc(c, &d.gpos, gpos.size())))
+        (e = dalloc(c, &d.gpos, gpos.size())) || (e = dalloc(c, &d.gsite, N)) || (e = dalloc(c, &d.gcount, 1)))
         return e;
     // translation operators
     std::vector<double2> ops((size_t)343 * LPH * LP, make_double2(0.0, 0.0));
-    auto fill_m2l = [&](double scale, double2 *dst) -> int {
+    auto fill_m2l = [&](double scale, double2 *dst, float2 *dst32) -> int {
         for (int dz = -3; dz <= 3; dz++)
             for (int dy = -3; dy <= 3; dy++)
                 for (int dx = -3; dx <= 3; dx++) {
@@ -576,10 +617,13 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
                     op_m2l(dx * scale, dy * scale, dz * scale, &ops[(size_t)oi * LPH * LP]);
                 }
         CK(cudaMemcpyAsync(dst, ops.data(), ops.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+        std::vector<float2> o32(ops.size());
+        for (size_t i = 0; i < ops.size(); i++) o32[i] = make_float2((float)ops[i].x, (float)ops[i].y);
+        CK(cudaMemcpyAsync(dst32, o32.data(), o32.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
         CK(cudaStreamSynchronize(c->st));
         return 0;
     };
-    if ((e = fill_m2l(RS, d.op_m2l4)) || (e = fill_m2l(2 * RS, d.op_m2l3))) return e;
+    if ((e = fill_m2l(RS, d.op_m2l4, d.op32_m2l4)) || (e = fill_m2l(2 * RS, d.op_m2l3, d.op32_m2l3))) return e;
     {
         std::vector<double2> o2((size_t)w2 * w2 * w2 * LPH * LP, make_double2(0.0, 0.0));
         for (int dz = -d2; dz <= d2; dz++)

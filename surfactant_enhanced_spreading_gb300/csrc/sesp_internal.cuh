@@ -99,11 +99,13 @@ struct Dev {
     // graphite columns of the bottom layer
     int *gcol_start;
     double4 *gpos;
+    int *gsite, *gcount;   // sites the graphite acts on (rebuilt with the lists)
     // intramolecular correction lists (bit k: site k+1 of the molecule)
     uint32_t *isub;
     // multipoles / local expansions (double2 = complex)
     double2 *O4, *L4, *O3, *L3, *O2, *L2;
     double2 *op_m2l4, *op_m2l3, *op_m2l2, *op_m2m43, *op_m2m32, *op_l2l23, *op_l2l34;
+    float2 *op32_m2l4, *op32_m2l3;   // FP32 copies for the mixed path
     int *m2l2_off;       // per replica: (2nr-1)^3 index map to operators
     // LJ pair table (eps, sg6), NTYPE^2
     double2 *ljt;
