@@ -89,7 +89,7 @@ class Dist:
 def make_system(small):
     from surfactant_enhanced_spreading_gb300 import system as S
     if small:
-        return S.droplet(2000, 20, cells=(8, 8, 8), seed=7, graphite_layers=2)
+        return S.droplet(6000, 60, cells=(16, 16, 8), seed=7, graphite_layers=2)
     w = WORKLOAD
     return S.droplet(w["n_water"], w["n_surf"], cells=w["cells"], seed=w["seed"], graphite_layers=w["graphite_layers"])
 
@@ -247,7 +247,7 @@ def run_ours(args, ws, rank, local):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 pair/multipole, f64 constraints/thermostat/positions",
         "data": "synthetic (seeded droplet; no dataset)",
-        "config": {"workload": ("small test droplet 2,000 waters + 20 surfactants, 8^3 cells" if args.small else
+        "config": {"workload": ("small droplet 6,000 waters + 60 surfactants, 16x16x8 cells" if args.small else
                                 "single system, 20,000 SPC/E waters + 200 29-site trisiloxane surfactants on 4-layer "
                                 "graphite, 24x24x12 cells (288x288x144 A), reference force field"),
                    "n_sites": n_sites, "precision": "mixed", "rebuild_interval": 10,

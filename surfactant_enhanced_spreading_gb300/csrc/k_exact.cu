@@ -438,16 +438,31 @@ void launch_locate(const Dev &d, int nmol, cudaStream_t st) {
 void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st) {
     if (nsurf_sites) k_isub<<<(nsurf_sites + 127) / 128, 128, 0, st>>>(d, nsurf_sites, surf_mols);
 }
+// The surfactant halves are serial chains per molecule on a few SMs, so they
+// run on a side stream concurrently with the water halves (fork / join by
+// events, which CUDA-graph capture records as graph edges).
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
-                   cudaStream_t st) {
-    if (ns) k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
+                   cudaStream_t st, const SideStream &side) {
+    if (ns) {
+        cudaEventRecord(side.fork, st);
+        cudaStreamWaitEvent(side.st, side.fork, 0);
+        k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, side.st>>>(d, smols, ns, tol, maxit);
+        cudaEventRecord(side.join, side.st);
+    }
     if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+    if (ns) cudaStreamWaitEvent(st, side.join, 0);
     k_eta<<<nrep, 1024, 0, st>>>(d);
 }
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit,
-                   cudaStream_t st) {
-    if (ns) k_move_b_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
+                   cudaStream_t st, const SideStream &side) {
+    if (ns) {
+        cudaEventRecord(side.fork, st);
+        cudaStreamWaitEvent(side.st, side.fork, 0);
+        k_move_b_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, side.st>>>(d, smols, ns, tol, maxit);
+        cudaEventRecord(side.join, side.st);
+    }
     if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+    if (ns) cudaStreamWaitEvent(st, side.join, 0);
 }
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st) {
     k_init_accel<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite);

@@ -195,35 +195,82 @@ __device__ inline void local_grad(const R *Lre, const R *Lim, R x, R y, R z, R &
 
 // ------------------------------------------------------------------ near field
 
+constexpr int NEAR_CHUNK = 2 * NEAR_THREADS;   // partner sites staged per pass
+
 template <bool MIXED>
 struct NearSmem;
 
 template <>
 struct NearSmem<false> {
-    double4 pos[NEAR_THREADS];
-    int2 meta[NEAR_THREADS];
+    double4 pos[NEAR_CHUNK];
+    int meta[NEAR_CHUNK];     // molecule << 5 | site kind
     double2 lj[NTYPE * NTYPE];
     double Lre[LP], Lim[LP];
 };
 template <>
 struct NearSmem<true> {
-    float4 pos[NEAR_THREADS];
-    int2 meta[NEAR_THREADS];
+    float4 pos[NEAR_CHUNK];
+    int meta[NEAR_CHUNK];
     float2 lj[NTYPE * NTYPE];
     float Lre[LP], Lim[LP];
 };
 
-// One CTA per cell.  Thread t owns slot t of the cell (looping if the cell
-// holds more sites than threads); for each of the 27 neighbour cells the
-// sites are staged in shared memory and every thread sums its own site's
-// force over them.  Pair term (src/evalw1w1n.f90:86-104): qq / r^3 without
-// cutoff, plus 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2 for r <= rc; sites of the
-// same molecule are skipped (src/evalSS.f90:36).  MIXED: positions relative
-// to the target cell centre in FP32, FP32 pair arithmetic, each neighbour
-// cell's partial sum added into an FP64 accumulator.
+// 1/sqrt(r2) in FP64 from the FP32 hardware estimate and two Newton steps
+// (relative error of the seed ~2^-22, after two steps at the FP64 rounding level)
+__device__ inline double rsqrt_fp64(double r2) {
+    double y = (double)rsqrtf((float)r2);
+    double h = 0.5 * r2;
+    y = y * (1.5 - h * y * y);
+    y = y * (1.5 - h * y * y);
+    return y;
+}
+
+// Accumulate one partner's force on one site (src/evalw1w1n.f90:86-104 form):
+// qq / r^3 without cutoff plus 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2 within rc;
+// zero for a partner of the same molecule (src/evalSS.f90:36).
+template <typename R>
+__device__ __forceinline__ void pair_acc(R xi, R yi, R zi, R qi, int mi, int trow, R xj, R yj, R zj, R qj, int meta,
+                                         const typename std::conditional<std::is_same<R, float>::value, float2, double2>::type *lj,
+                                         R rc2, R &px, R &py, R &pz) {
+    R dx = xi - xj, dy = yi - yj, dz = zi - zj;
+    R r2 = dx * dx + dy * dy + dz * dz;
+    const bool same = (meta >> 5) == mi;
+    const int tj = meta & 31;
+    r2 = same ? R(1) : r2;
+    R qq = same ? R(0) : qi * qj;
+    R ir;
+    if (std::is_same<R, float>::value) ir = rsqrtf((float)r2); else ir = rsqrt_fp64((double)r2);
+    R ir2 = ir * ir;
+    R ft = qq * ir * ir2;
+    if (tj != 1) {   // water H carries no LJ; uniform across the warp (one partner per step)
+        auto v = lj[trow + tj];
+        R on = (r2 <= rc2 && !same) ? (R)v.x : R(0);
+        R r6 = ir2 * ir2 * ir2;
+        ft += on * r6 * ((R)v.y * r6 - R(0.5)) * ir2;
+    }
+    px += dx * ft; py += dy * ft; pz += dz * ft;
+}
+
+// error-free two-sum of FP32 values into a (hi, lo) pair
+__device__ __forceinline__ void two_sum(float &hi, float &lo, float v) {
+    float s = hi + v;
+    float bp = s - hi;
+    float err = (hi - (s - bp)) + (v - bp);
+    hi = s;
+    lo += err;
+}
+
+// One CTA per cell, two sites per thread (t and t + NEAR_THREADS).  The 27
+// neighbour cells are visited as 9 rows of up to 3 cells, which are
+// contiguous in slot order, and staged through shared memory; every thread
+// sums the full force on its own sites (no third-law scatter, no atomics).
+// The local-expansion force of src/evalLjk4.f90 is fused into the epilogue.
+// MIXED: FP32 positions relative to the target cell centre, FP32 pair terms,
+// each row's partial sum added into an FP32 (hi, lo) two-sum accumulator.
 template <bool MIXED>
 __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int terms) {
     typedef typename std::conditional<MIXED, float, double>::type R;
+    typedef typename std::conditional<MIXED, float2, double2>::type R2;
     __shared__ NearSmem<MIXED> sm;
     const int c = blockIdx.x;
     const int s0 = d.cstart[c];
@@ -234,12 +281,8 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int terms) {
     cell_xyz(r, c, ix, iy, iz);
     const double cx = cell_centre(d, r, 0, ix), cy = cell_centre(d, r, 1, iy), cz = cell_centre(d, r, 2, iz);
     for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) {
-        if (MIXED) {
-            double2 v = d.ljt[t];
-            ((float2 *)sm.lj)[t] = make_float2((float)v.x, (float)v.y);
-        } else {
-            ((double2 *)sm.lj)[t] = d.ljt[t];
-        }
+        double2 v = d.ljt[t];
+        sm.lj[t] = R2{(R)v.x, (R)v.y};
     }
     if (threadIdx.x < LP) {
         double2 v = d.L4[(size_t)c * LP + threadIdx.x];
@@ -250,100 +293,105 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int terms) {
     const R rc2 = (R)(RC * RC);
     const bool do_near = terms & SESP_T_NEAR;
     const bool do_far = terms & SESP_T_FAR;
-    for (int ib = 0; ib < ni; ib += NEAR_THREADS) {
-        const int i = ib + threadIdx.x;
-        const bool act = i < ni;
-        R xi = 0, yi = 0, zi = 0, qi = 0;
-        int mi = -1, ti = 0;
-        double xd = 0, yd = 0, zd = 0;
-        if (act) {
-            double4 p = d.srt_pos[s0 + i];
-            int2 mt = d.srt_meta[s0 + i];
-            xd = p.x; yd = p.y; zd = p.z;
-            if (MIXED) {
-                float4 p32 = d.srt_pos32[s0 + i];
-                xi = p32.x; yi = p32.y; zi = p32.z;
-            } else {
-                xi = (R)p.x; yi = (R)p.y; zi = (R)p.z;
-            }
-            qi = (R)(p.w * XPI);
-            mi = mt.x; ti = mt.y;
+    for (int ib = 0; ib < ni; ib += 2 * NEAR_THREADS) {
+        const int i0 = ib + threadIdx.x, i1 = ib + NEAR_THREADS + threadIdx.x;
+        const bool a0 = i0 < ni, a1 = i1 < ni;
+        // the second slot is skipped by whole warps when none of their lanes has one
+        const bool warp2 = __any_sync(0xffffffffu, a1);
+        R x0 = 0, y0 = 0, z0 = 0, q0 = 0, x1 = 0, y1 = 0, z1 = 0, q1 = 0;
+        int m0 = -1, m1 = -1, t0r = 0, t1r = 0;
+        double xd0 = 0, yd0 = 0, zd0 = 0, xd1 = 0, yd1 = 0, zd1 = 0;
+        if (a0) {
+            double4 p = d.srt_pos[s0 + i0];
+            int2 mt = d.srt_meta[s0 + i0];
+            xd0 = p.x; yd0 = p.y; zd0 = p.z;
+            if (MIXED) { float4 p32 = d.srt_pos32[s0 + i0]; x0 = p32.x; y0 = p32.y; z0 = p32.z; }
+            else { x0 = (R)p.x; y0 = (R)p.y; z0 = (R)p.z; }
+            q0 = (R)(p.w * XPI); m0 = mt.x; t0r = mt.y * NTYPE;
         }
-        double fx = 0.0, fy = 0.0, fz = 0.0;
+        if (a1) {
+            double4 p = d.srt_pos[s0 + i1];
+            int2 mt = d.srt_meta[s0 + i1];
+            xd1 = p.x; yd1 = p.y; zd1 = p.z;
+            if (MIXED) { float4 p32 = d.srt_pos32[s0 + i1]; x1 = p32.x; y1 = p32.y; z1 = p32.z; }
+            else { x1 = (R)p.x; y1 = (R)p.y; z1 = (R)p.z; }
+            q1 = (R)(p.w * XPI); m1 = mt.x; t1r = mt.y * NTYPE;
+        }
+        // accumulators: FP64 for the plain path, FP32 two-sum pairs for the mixed one
+        double fx0 = 0, fy0 = 0, fz0 = 0, fx1 = 0, fy1 = 0, fz1 = 0;
+        float hx0 = 0, hy0 = 0, hz0 = 0, lx0 = 0, ly0 = 0, lz0 = 0;
+        float hx1 = 0, hy1 = 0, hz1 = 0, lx1 = 0, ly1 = 0, lz1 = 0;
         if (do_near) {
             for (int dzc = -1; dzc <= 1; dzc++)
-                for (int dyc = -1; dyc <= 1; dyc++)
-                    for (int dxc = -1; dxc <= 1; dxc++) {
-                        int jx = ix + dxc, jy = iy + dyc, jz = iz + dzc;
-                        if (jx < 0 || jy < 0 || jz < 0 || jx >= r.nc[0] || jy >= r.nc[1] || jz >= r.nc[2]) continue;
-                        int cn = cell_index(r, jx, jy, jz);
-                        int t0 = d.cstart[cn], nt = d.cstart[cn + 1] - t0;
-                        // offset of the neighbour cell's centre from this cell's (mixed)
-                        R ox = (R)(dxc * RS), oy = (R)(dyc * RS), oz = (R)(dzc * RS);
-                        R px = 0, py = 0, pz = 0;
-                        for (int jb = 0; jb < nt; jb += NEAR_THREADS) {
-                            __syncthreads();
-                            int jn = min(NEAR_THREADS, nt - jb);
-                            if (threadIdx.x < jn) {
-                                if (MIXED) {
-                                    float4 v = d.srt_pos32[t0 + jb + threadIdx.x];
-                                    ((float4 *)sm.pos)[threadIdx.x] = make_float4(v.x + (float)ox, v.y + (float)oy, v.z + (float)oz, v.w);
-                                } else {
-                                    ((double4 *)sm.pos)[threadIdx.x] = d.srt_pos[t0 + jb + threadIdx.x];
-                                }
-                                sm.meta[threadIdx.x] = d.srt_meta[t0 + jb + threadIdx.x];
-                            }
-                            __syncthreads();
-                            if (act) {
-                                const int trow = ti * NTYPE;
-#pragma unroll 4
-                                for (int j = 0; j < jn; j++) {
-                                    R xj, yj, zj, qj;
-                                    if (MIXED) {
-                                        float4 v = ((float4 *)sm.pos)[j];
-                                        xj = v.x; yj = v.y; zj = v.z; qj = v.w;
-                                    } else {
-                                        double4 v = ((double4 *)sm.pos)[j];
-                                        xj = v.x; yj = v.y; zj = v.z; qj = v.w;
-                                    }
-                                    int2 mt = sm.meta[j];
-                                    R dx = xi - xj, dy = yi - yj, dz = zi - zj;
-                                    R r2 = dx * dx + dy * dy + dz * dz;
-                                    bool same = mt.x == mi;
-                                    r2 = same ? R(1) : r2;
-                                    R qq = same ? R(0) : qi * qj;
-                                    R ir;
-                                    if (MIXED) ir = rsqrtf((float)r2); else ir = rsqrt((double)r2);
-                                    R ir2 = ir * ir;
-                                    R ft = qq * ir * ir2;
-                                    if (mt.y != 1) {   // water H carries no LJ; uniform across the warp
-                                        R lx, ly;
-                                        if (MIXED) { float2 v = ((float2 *)sm.lj)[trow + mt.y]; lx = v.x; ly = v.y; }
-                                        else { double2 v = ((double2 *)sm.lj)[trow + mt.y]; lx = v.x; ly = v.y; }
-                                        R on = (r2 <= rc2 && !same) ? lx : R(0);
-                                        R r6 = ir2 * ir2 * ir2;
-                                        ft += on * r6 * (ly * r6 - R(0.5)) * ir2;
-                                    }
-                                    px += dx * ft; py += dy * ft; pz += dz * ft;
-                                }
+                for (int dyc = -1; dyc <= 1; dyc++) {
+                    const int jy = iy + dyc, jz = iz + dzc;
+                    if (jy < 0 || jz < 0 || jy >= r.nc[1] || jz >= r.nc[2]) continue;
+                    const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+                    const int c0 = cell_index(r, jx0, jy, jz);
+                    const int t0 = d.cstart[c0], tend = d.cstart[c0 + (jx1 - jx0) + 1];
+                    // slot bounds of the row's second and third cells (mixed offsets)
+                    const int b1 = jx1 > jx0 ? d.cstart[c0 + 1] : tend;
+                    const int b2 = jx1 - jx0 == 2 ? d.cstart[c0 + 2] : tend;
+                    const R oy = (R)(dyc * RS), oz = (R)(dzc * RS);
+                    R px0 = 0, py0 = 0, pz0 = 0, px1 = 0, py1 = 0, pz1 = 0;
+                    for (int jb = t0; jb < tend; jb += NEAR_CHUNK) {
+                        const int jn = min(NEAR_CHUNK, tend - jb);
+                        __syncthreads();
+                        for (int k = threadIdx.x; k < jn; k += NEAR_THREADS) {
+                            const int sl = jb + k;
+                            int2 mt = d.srt_meta[sl];
+                            sm.meta[k] = (mt.x << 5) | mt.y;
+                            if (MIXED) {
+                                const int cxj = jx0 + (sl >= b1) + (sl >= b2);
+                                const float ox = (float)((cxj - ix) * RS);
+                                float4 v = d.srt_pos32[sl];
+                                ((float4 *)sm.pos)[k] = make_float4(v.x + ox, v.y + (float)oy, v.z + (float)oz, v.w);
+                            } else {
+                                ((double4 *)sm.pos)[k] = d.srt_pos[sl];
                             }
                         }
-                        fx += (double)px; fy += (double)py; fz += (double)pz;
+                        __syncthreads();
+                        const R2 *lj = (const R2 *)sm.lj;
+                        if (a0) {
+#pragma unroll 4
+                            for (int j = 0; j < jn; j++) {
+                                R xj, yj, zj, qj;
+                                if (MIXED) { float4 v = ((float4 *)sm.pos)[j]; xj = v.x; yj = v.y; zj = v.z; qj = v.w; }
+                                else { double4 v = ((double4 *)sm.pos)[j]; xj = v.x; yj = v.y; zj = v.z; qj = v.w; }
+                                const int mj = sm.meta[j];
+                                pair_acc<R>(x0, y0, z0, q0, m0, t0r, xj, yj, zj, qj, mj, lj, rc2, px0, py0, pz0);
+                                if (warp2 && a1) pair_acc<R>(x1, y1, z1, q1, m1, t1r, xj, yj, zj, qj, mj, lj, rc2, px1, py1, pz1);
+                            }
+                        }
                     }
+                    if (MIXED) {
+                        two_sum(hx0, lx0, (float)px0); two_sum(hy0, ly0, (float)py0); two_sum(hz0, lz0, (float)pz0);
+                        two_sum(hx1, lx1, (float)px1); two_sum(hy1, ly1, (float)py1); two_sum(hz1, lz1, (float)pz1);
+                    } else {
+                        fx0 += (double)px0; fy0 += (double)py0; fz0 += (double)pz0;
+                        fx1 += (double)px1; fy1 += (double)py1; fz1 += (double)pz1;
+                    }
+                }
         }
-        if (act && do_far) {
+        if (MIXED) {
+            fx0 = (double)hx0 + (double)lx0; fy0 = (double)hy0 + (double)ly0; fz0 = (double)hz0 + (double)lz0;
+            fx1 = (double)hx1 + (double)lx1; fy1 = (double)hy1 + (double)ly1; fz1 = (double)hz1 + (double)lz1;
+        }
+        if (do_far) {
             R gx, gy, gz;
-            if (MIXED) {
-                local_grad<R>(sm.Lre, sm.Lim, xi, yi, zi, gx, gy, gz, nullptr);
-            } else {
-                local_grad<R>(sm.Lre, sm.Lim, (R)(xd - cx), (R)(yd - cy), (R)(zd - cz), gx, gy, gz, nullptr);
+            if (a0) {
+                if (MIXED) local_grad<R>(sm.Lre, sm.Lim, x0, y0, z0, gx, gy, gz, nullptr);
+                else local_grad<R>(sm.Lre, sm.Lim, (R)(xd0 - cx), (R)(yd0 - cy), (R)(zd0 - cz), gx, gy, gz, nullptr);
+                fx0 -= (double)(q0 * gx); fy0 -= (double)(q0 * gy); fz0 -= (double)(q0 * gz);
             }
-            fx -= (double)(qi * gx); fy -= (double)(qi * gy); fz -= (double)(qi * gz);
+            if (a1) {
+                if (MIXED) local_grad<R>(sm.Lre, sm.Lim, x1, y1, z1, gx, gy, gz, nullptr);
+                else local_grad<R>(sm.Lre, sm.Lim, (R)(xd1 - cx), (R)(yd1 - cy), (R)(zd1 - cz), gx, gy, gz, nullptr);
+                fx1 -= (double)(q1 * gx); fy1 -= (double)(q1 * gy); fz1 -= (double)(q1 * gz);
+            }
         }
-        if (act) {
-            size_t o = 3 * (size_t)(s0 + i);
-            d.nf[o] = fx; d.nf[o + 1] = fy; d.nf[o + 2] = fz;
-        }
+        if (a0) { size_t o = 3 * (size_t)(s0 + i0); d.nf[o] = fx0; d.nf[o + 1] = fy0; d.nf[o + 2] = fz0; }
+        if (a1) { size_t o = 3 * (size_t)(s0 + i1); d.nf[o] = fx1; d.nf[o + 1] = fy1; d.nf[o + 2] = fz1; }
     }
 }
 

@@ -6,14 +6,20 @@
 
 namespace sesp {
 
+// a second stream with fork / join events for work that overlaps the main stream
+struct SideStream {
+    cudaStream_t st;
+    cudaEvent_t fork, join;
+};
+
 // k_exact.cu
 void upload_tables_exact(const Tables &t, cudaStream_t st);
 void launch_locate(const Dev &d, int nmol, cudaStream_t st);
 void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st);
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
-                   cudaStream_t st);
+                   cudaStream_t st, const SideStream &side);
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit,
-                   cudaStream_t st);
+                   cudaStream_t st, const SideStream &side);
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st);
 
 // k_force.cu

@@ -282,6 +282,7 @@ void op_l2l(double x, double y, double z, double2 *op) {
 struct sesp_ctx {
     sesp_params p;
     cudaStream_t st = nullptr;
+    SideStream side = {nullptr, nullptr, nullptr};
     bool uploaded = false, have_force = false;
     int nrep = 0, nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, nwm = 0, nsm = 0, d2 = 1;
     std::vector<Rep> reps;
@@ -396,12 +397,12 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
 
 void seq_move_a(sesp_ctx *c) {
     tstart(c, 2);
-    launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit, c->st);
+    launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit, c->st, c->side);
     tstop(c, 2);
 }
 void seq_move_b(sesp_ctx *c) {
     tstart(c, 3);
-    launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit, c->st);
+    launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit, c->st, c->side);
     tstop(c, 3);
 }
 
@@ -455,6 +456,12 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (set_device(c)) { delete c; return SESP_ECUDA; }
     if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "stream"); }
     for (int k = 0; k < 16; k++) cudaEventCreate(&c->ev[k]);
+    if (cudaStreamCreateWithFlags(&c->side.st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming) != cudaSuccess) {
+        delete c;
+        return fail(SESP_ECUDA, "side stream");
+    }
     init_force_kernels();
     Tables T = make_tables();
     {
@@ -474,6 +481,9 @@ int sesp_destroy(sesp_ctx *c) {
     cudaStreamSynchronize(c->st);
     free_state(c);
     for (int k = 0; k < 16; k++) cudaEventDestroy(c->ev[k]);
+    cudaEventDestroy(c->side.fork);
+    cudaEventDestroy(c->side.join);
+    cudaStreamDestroy(c->side.st);
     cudaStreamDestroy(c->st);
     delete c;
     return 0;
