@@ -142,6 +142,11 @@ int sesp_run(sesp_ctx *ctx, int kb0, int nsteps);
 /* the same without waiting for completion; sesp_sync waits */
 int sesp_run_async(sesp_ctx *ctx, int kb0, int nsteps);
 int sesp_sync(sesp_ctx *ctx);
+/* 0 when all work launched on the context has finished, 1 while some is
+ * still running, negative on error (never blocks) */
+int sesp_query(sesp_ctx *ctx);
+/* device memory held by the context's state, in bytes */
+int sesp_device_bytes(sesp_ctx *ctx, int64_t *bytes);
 
 /* nsteps passes like sesp_run, each timed with CUDA events recorded on the
  * engine's stream around the step's graph launch.  With flush_l2 != 0 a

@@ -174,5 +174,14 @@ module sesp_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: eta(*)
     end function
+    integer(c_int) function sesp_query(ctx) bind(C, name="sesp_query")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function sesp_device_bytes(ctx, bytes) bind(C, name="sesp_device_bytes")
+      import :: c_int, c_ptr, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int64_t), intent(out) :: bytes
+    end function
   end interface
 end module sesp_mod

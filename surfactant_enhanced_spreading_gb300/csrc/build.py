@@ -21,7 +21,7 @@ LIB = os.path.join(PKG, "libsesp.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
-          "--expt-relaxed-constexpr"]
+          "--expt-relaxed-constexpr", "-diag-suppress", "1444"]
 UNITS = [("k_exact.cu", ["-fmad=false"]), ("k_force.cu", []), ("sesp_api.cu", [])]
 HEADERS = ["sesp_internal.cuh", "k_launch.cuh", os.path.join("..", "..", "include", "sesp.h")]
 

@@ -205,14 +205,12 @@ struct NearSmem<false> {
     double4 pos[NEAR_CHUNK];
     int meta[NEAR_CHUNK];     // molecule << 5 | site kind
     double2 lj[NTYPE * NTYPE];
-    double Lre[LP], Lim[LP];
 };
 template <>
 struct NearSmem<true> {
     float4 pos[NEAR_CHUNK];
     int meta[NEAR_CHUNK];
-    float2 lj[NTYPE * NTYPE];
-    float Lre[LP], Lim[LP];
+    float2 lj[NTYPE];         // per kind: (sqrt(48 eps), sigma / 2); zero eps for water H
 };
 
 // 1/sqrt(r2) in FP64 from the FP32 hardware estimate and two Newton steps
@@ -225,32 +223,6 @@ __device__ inline double rsqrt_fp64(double r2) {
     return y;
 }
 
-// Accumulate one partner's force on one site (src/evalw1w1n.f90:86-104 form):
-// qq / r^3 without cutoff plus 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2 within rc;
-// zero for a partner of the same molecule (src/evalSS.f90:36).
-template <typename R>
-__device__ __forceinline__ void pair_acc(R xi, R yi, R zi, R qi, int mi, int trow, R xj, R yj, R zj, R qj, int meta,
-                                         const typename std::conditional<std::is_same<R, float>::value, float2, double2>::type *lj,
-                                         R rc2, R &px, R &py, R &pz) {
-    R dx = xi - xj, dy = yi - yj, dz = zi - zj;
-    R r2 = dx * dx + dy * dy + dz * dz;
-    const bool same = (meta >> 5) == mi;
-    const int tj = meta & 31;
-    r2 = same ? R(1) : r2;
-    R qq = same ? R(0) : qi * qj;
-    R ir;
-    if (std::is_same<R, float>::value) ir = rsqrtf((float)r2); else ir = rsqrt_fp64((double)r2);
-    R ir2 = ir * ir;
-    R ft = qq * ir * ir2;
-    if (tj != 1) {   // water H carries no LJ; uniform across the warp (one partner per step)
-        auto v = lj[trow + tj];
-        R on = (r2 <= rc2 && !same) ? (R)v.x : R(0);
-        R r6 = ir2 * ir2 * ir2;
-        ft += on * r6 * ((R)v.y * r6 - R(0.5)) * ir2;
-    }
-    px += dx * ft; py += dy * ft; pz += dz * ft;
-}
-
 // error-free two-sum of FP32 values into a (hi, lo) pair
 __device__ __forceinline__ void two_sum(float &hi, float &lo, float v) {
     float s = hi + v;
@@ -260,144 +232,249 @@ __device__ __forceinline__ void two_sum(float &hi, float &lo, float v) {
     lo += err;
 }
 
-// One CTA per cell, two sites per thread (t and t + NEAR_THREADS).  The 27
-// neighbour cells are visited as 9 rows of up to 3 cells, which are
-// contiguous in slot order, and staged through shared memory; every thread
-// sums the full force on its own sites (no third-law scatter, no atomics).
-// The local-expansion force of src/evalLjk4.f90 is fused into the epilogue.
+// One partner's force on one site (src/evalw1w1n.f90:86-104 form): qq / r^3
+// without cutoff plus 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2 within rc; zero
+// for a partner of the same molecule (src/evalSS.f90:36).  FP64 takes the
+// pair's (48 eps sg6, sg6) from the table; FP32 combines per-kind
+// (sqrt(48 eps), sigma/2) by the Lorentz-Berthelot rule of
+// src/init_arrays.f90:476-502.
+__device__ __forceinline__ void pair_acc64(double xi, double yi, double zi, double qi, int mi, int trow, double4 pj,
+                                           int meta, const double2 *lj, double rc2, double &px, double &py, double &pz) {
+    double dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+    double r2 = dx * dx + dy * dy + dz * dz;
+    const bool same = (meta >> 5) == mi;
+    const int tj = meta & 31;
+    r2 = same ? 1.0 : r2;
+    double qq = same ? 0.0 : qi * pj.w;
+    double ir = rsqrt_fp64(r2);
+    double ir2 = ir * ir;
+    double ft = qq * ir * ir2;
+    if (tj != 1) {   // water H carries no LJ; uniform across the warp (one partner per step)
+        double2 v = lj[trow + tj];
+        double on = (r2 <= rc2 && !same) ? v.x : 0.0;
+        double r6 = ir2 * ir2 * ir2;
+        ft += on * r6 * (v.y * r6 - 0.5) * ir2;
+    }
+    px += dx * ft; py += dy * ft; pz += dz * ft;
+}
+
+__device__ __forceinline__ void pair_acc32(float xi, float yi, float zi, float qi, int mi, float2 li, float4 pj, int meta,
+                                           const float2 *lj, float rc2, float &px, float &py, float &pz) {
+    float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
+    float r2 = dx * dx + dy * dy + dz * dz;
+    const bool same = (meta >> 5) == mi;
+    const int tj = meta & 31;
+    r2 = same ? 1.f : r2;
+    float qq = same ? 0.f : qi * pj.w;
+    float ir = rsqrtf(r2);
+    float ir2 = ir * ir;
+    float ft = qq * ir * ir2;
+    if (tj != 1) {
+        float2 v = lj[tj];
+        float e = li.x * v.x;                 // 48 eps_ij
+        float s = li.y + v.y, s2 = s * s, s6 = s2 * s2 * s2;
+        float on = (r2 <= rc2 && !same) ? e * s6 : 0.f;
+        float r6 = ir2 * ir2 * ir2;
+        ft += on * r6 * (s6 * r6 - 0.5f) * ir2;
+    }
+    px += dx * ft; py += dy * ft; pz += dz * ft;
+}
+
+// Near field, one CTA per (cell, dz plane of neighbour cells).  Each plane is
+// 3 rows of up to 3 cells, contiguous in slot order, staged through shared
+// memory; each thread sums the force of the plane on two sites of the cell
+// (t and t + NEAR_THREADS).  The plane's partial force is written per slot;
+// k_near_finish adds the three planes in a fixed order.  No third-law
+// scatter and no atomics, so every result is bit-reproducible.
 // MIXED: FP32 positions relative to the target cell centre, FP32 pair terms,
-// each row's partial sum added into an FP32 (hi, lo) two-sum accumulator.
+// rows summed in an FP32 (hi, lo) two-sum pair.
 template <bool MIXED>
-__global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int terms) {
-    typedef typename std::conditional<MIXED, float, double>::type R;
-    typedef typename std::conditional<MIXED, float2, double2>::type R2;
+__global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot) {
     __shared__ NearSmem<MIXED> sm;
-    const int c = blockIdx.x;
+    const int c = blockIdx.x / 3;
+    const int plane = blockIdx.x % 3;
+    const int dzc = plane - 1;
     const int s0 = d.cstart[c];
     const int ni = d.cstart[c + 1] - s0;
     if (ni == 0) return;
     const Rep r = d.rep[d.crep[c]];
     int ix, iy, iz;
     cell_xyz(r, c, ix, iy, iz);
-    const double cx = cell_centre(d, r, 0, ix), cy = cell_centre(d, r, 1, iy), cz = cell_centre(d, r, 2, iz);
-    for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) {
-        double2 v = d.ljt[t];
-        sm.lj[t] = R2{(R)v.x, (R)v.y};
+    double *part = d.near_part + (size_t)plane * 3 * nslot;
+    const int jz = iz + dzc;
+    if (jz < 0 || jz >= r.nc[2]) {
+        for (int i = threadIdx.x; i < ni; i += NEAR_THREADS) {
+            size_t o = 3 * (size_t)(s0 + i);
+            part[o] = 0.0; part[o + 1] = 0.0; part[o + 2] = 0.0;
+        }
+        return;
     }
-    if (threadIdx.x < LP) {
-        double2 v = d.L4[(size_t)c * LP + threadIdx.x];
-        sm.Lre[threadIdx.x] = (R)v.x;
-        sm.Lim[threadIdx.x] = (R)v.y;
+    if constexpr (MIXED) {
+        if (threadIdx.x < NTYPE) ((float2 *)sm.lj)[threadIdx.x] = d.lj_kind[threadIdx.x];
+    } else {
+        for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) ((double2 *)sm.lj)[t] = d.ljt[t];
     }
     __syncthreads();
-    const R rc2 = (R)(RC * RC);
-    const bool do_near = terms & SESP_T_NEAR;
-    const bool do_far = terms & SESP_T_FAR;
+    const int i0 = threadIdx.x, i1 = NEAR_THREADS + threadIdx.x;
     for (int ib = 0; ib < ni; ib += 2 * NEAR_THREADS) {
-        const int i0 = ib + threadIdx.x, i1 = ib + NEAR_THREADS + threadIdx.x;
-        const bool a0 = i0 < ni, a1 = i1 < ni;
-        // the second slot is skipped by whole warps when none of their lanes has one
+        const int ia = ib + i0, ibb = ib + i1;
+        const bool a0 = ia < ni, a1 = ibb < ni;
         const bool warp2 = __any_sync(0xffffffffu, a1);
-        R x0 = 0, y0 = 0, z0 = 0, q0 = 0, x1 = 0, y1 = 0, z1 = 0, q1 = 0;
-        int m0 = -1, m1 = -1, t0r = 0, t1r = 0;
-        double xd0 = 0, yd0 = 0, zd0 = 0, xd1 = 0, yd1 = 0, zd1 = 0;
-        if (a0) {
-            double4 p = d.srt_pos[s0 + i0];
-            int2 mt = d.srt_meta[s0 + i0];
-            xd0 = p.x; yd0 = p.y; zd0 = p.z;
-            if (MIXED) { float4 p32 = d.srt_pos32[s0 + i0]; x0 = p32.x; y0 = p32.y; z0 = p32.z; }
-            else { x0 = (R)p.x; y0 = (R)p.y; z0 = (R)p.z; }
-            q0 = (R)(p.w * XPI); m0 = mt.x; t0r = mt.y * NTYPE;
-        }
-        if (a1) {
-            double4 p = d.srt_pos[s0 + i1];
-            int2 mt = d.srt_meta[s0 + i1];
-            xd1 = p.x; yd1 = p.y; zd1 = p.z;
-            if (MIXED) { float4 p32 = d.srt_pos32[s0 + i1]; x1 = p32.x; y1 = p32.y; z1 = p32.z; }
-            else { x1 = (R)p.x; y1 = (R)p.y; z1 = (R)p.z; }
-            q1 = (R)(p.w * XPI); m1 = mt.x; t1r = mt.y * NTYPE;
-        }
-        // accumulators: FP64 for the plain path, FP32 two-sum pairs for the mixed one
-        double fx0 = 0, fy0 = 0, fz0 = 0, fx1 = 0, fy1 = 0, fz1 = 0;
-        float hx0 = 0, hy0 = 0, hz0 = 0, lx0 = 0, ly0 = 0, lz0 = 0;
-        float hx1 = 0, hy1 = 0, hz1 = 0, lx1 = 0, ly1 = 0, lz1 = 0;
-        if (do_near) {
-            for (int dzc = -1; dzc <= 1; dzc++)
-                for (int dyc = -1; dyc <= 1; dyc++) {
-                    const int jy = iy + dyc, jz = iz + dzc;
-                    if (jy < 0 || jz < 0 || jy >= r.nc[1] || jz >= r.nc[2]) continue;
-                    const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
-                    const int c0 = cell_index(r, jx0, jy, jz);
-                    const int t0 = d.cstart[c0], tend = d.cstart[c0 + (jx1 - jx0) + 1];
-                    // slot bounds of the row's second and third cells (mixed offsets)
-                    const int b1 = jx1 > jx0 ? d.cstart[c0 + 1] : tend;
-                    const int b2 = jx1 - jx0 == 2 ? d.cstart[c0 + 2] : tend;
-                    const R oy = (R)(dyc * RS), oz = (R)(dzc * RS);
-                    R px0 = 0, py0 = 0, pz0 = 0, px1 = 0, py1 = 0, pz1 = 0;
-                    for (int jb = t0; jb < tend; jb += NEAR_CHUNK) {
-                        const int jn = min(NEAR_CHUNK, tend - jb);
-                        __syncthreads();
-                        for (int k = threadIdx.x; k < jn; k += NEAR_THREADS) {
-                            const int sl = jb + k;
-                            int2 mt = d.srt_meta[sl];
-                            sm.meta[k] = (mt.x << 5) | mt.y;
-                            if (MIXED) {
-                                const int cxj = jx0 + (sl >= b1) + (sl >= b2);
-                                const float ox = (float)((cxj - ix) * RS);
-                                float4 v = d.srt_pos32[sl];
-                                ((float4 *)sm.pos)[k] = make_float4(v.x + ox, v.y + (float)oy, v.z + (float)oz, v.w);
-                            } else {
-                                ((double4 *)sm.pos)[k] = d.srt_pos[sl];
-                            }
-                        }
-                        __syncthreads();
-                        const R2 *lj = (const R2 *)sm.lj;
-                        if (a0) {
-#pragma unroll 4
-                            for (int j = 0; j < jn; j++) {
-                                R xj, yj, zj, qj;
-                                if (MIXED) { float4 v = ((float4 *)sm.pos)[j]; xj = v.x; yj = v.y; zj = v.z; qj = v.w; }
-                                else { double4 v = ((double4 *)sm.pos)[j]; xj = v.x; yj = v.y; zj = v.z; qj = v.w; }
-                                const int mj = sm.meta[j];
-                                pair_acc<R>(x0, y0, z0, q0, m0, t0r, xj, yj, zj, qj, mj, lj, rc2, px0, py0, pz0);
-                                if (warp2 && a1) pair_acc<R>(x1, y1, z1, q1, m1, t1r, xj, yj, zj, qj, mj, lj, rc2, px1, py1, pz1);
-                            }
-                        }
-                    }
-                    if (MIXED) {
-                        two_sum(hx0, lx0, (float)px0); two_sum(hy0, ly0, (float)py0); two_sum(hz0, lz0, (float)pz0);
-                        two_sum(hx1, lx1, (float)px1); two_sum(hy1, ly1, (float)py1); two_sum(hz1, lz1, (float)pz1);
-                    } else {
-                        fx0 += (double)px0; fy0 += (double)py0; fz0 += (double)pz0;
-                        fx1 += (double)px1; fy1 += (double)py1; fz1 += (double)pz1;
-                    }
-                }
-        }
-        if (MIXED) {
-            fx0 = (double)hx0 + (double)lx0; fy0 = (double)hy0 + (double)ly0; fz0 = (double)hz0 + (double)lz0;
-            fx1 = (double)hx1 + (double)lx1; fy1 = (double)hy1 + (double)ly1; fz1 = (double)hz1 + (double)lz1;
-        }
-        if (do_far) {
-            R gx, gy, gz;
+        if constexpr (MIXED) {
+            float x0 = 0, y0 = 0, z0 = 0, q0 = 0, x1 = 0, y1 = 0, z1 = 0, q1 = 0;
+            int m0 = -1, m1 = -1;
+            float2 l0 = {0.f, 0.f}, l1 = {0.f, 0.f};
             if (a0) {
-                if (MIXED) local_grad<R>(sm.Lre, sm.Lim, x0, y0, z0, gx, gy, gz, nullptr);
-                else local_grad<R>(sm.Lre, sm.Lim, (R)(xd0 - cx), (R)(yd0 - cy), (R)(zd0 - cz), gx, gy, gz, nullptr);
-                fx0 -= (double)(q0 * gx); fy0 -= (double)(q0 * gy); fz0 -= (double)(q0 * gz);
+                float4 p = d.srt_pos32[s0 + ia];
+                int2 mt = d.srt_meta[s0 + ia];
+                x0 = p.x; y0 = p.y; z0 = p.z; q0 = p.w * (float)XPI; m0 = mt.x; l0 = d.lj_kind[mt.y];
             }
             if (a1) {
-                if (MIXED) local_grad<R>(sm.Lre, sm.Lim, x1, y1, z1, gx, gy, gz, nullptr);
-                else local_grad<R>(sm.Lre, sm.Lim, (R)(xd1 - cx), (R)(yd1 - cy), (R)(zd1 - cz), gx, gy, gz, nullptr);
-                fx1 -= (double)(q1 * gx); fy1 -= (double)(q1 * gy); fz1 -= (double)(q1 * gz);
+                float4 p = d.srt_pos32[s0 + ibb];
+                int2 mt = d.srt_meta[s0 + ibb];
+                x1 = p.x; y1 = p.y; z1 = p.z; q1 = p.w * (float)XPI; m1 = mt.x; l1 = d.lj_kind[mt.y];
             }
+            float hx0 = 0, hy0 = 0, hz0 = 0, lx0 = 0, ly0 = 0, lz0 = 0;
+            float hx1 = 0, hy1 = 0, hz1 = 0, lx1 = 0, ly1 = 0, lz1 = 0;
+            const float rc2 = (float)(RC * RC);
+            const float oz = (float)(dzc * RS);
+            for (int dyc = -1; dyc <= 1; dyc++) {
+                const int jy = iy + dyc;
+                if (jy < 0 || jy >= r.nc[1]) continue;
+                const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+                const int c0 = cell_index(r, jx0, jy, jz);
+                const int t0 = d.cstart[c0], tend = d.cstart[c0 + (jx1 - jx0) + 1];
+                const int b1 = jx1 > jx0 ? d.cstart[c0 + 1] : tend;
+                const int b2 = jx1 - jx0 == 2 ? d.cstart[c0 + 2] : tend;
+                const float oy = (float)(dyc * RS);
+                float px0 = 0, py0 = 0, pz0 = 0, px1 = 0, py1 = 0, pz1 = 0;
+                for (int jb = t0; jb < tend; jb += NEAR_CHUNK) {
+                    const int jn = min(NEAR_CHUNK, tend - jb);
+                    __syncthreads();
+                    for (int k = threadIdx.x; k < jn; k += NEAR_THREADS) {
+                        const int sl = jb + k;
+                        int2 mt = d.srt_meta[sl];
+                        sm.meta[k] = (mt.x << 5) | mt.y;
+                        const int cxj = jx0 + (sl >= b1) + (sl >= b2);
+                        const float ox = (float)((cxj - ix) * RS);
+                        float4 v = d.srt_pos32[sl];
+                        sm.pos[k] = make_float4(v.x + ox, v.y + oy, v.z + oz, v.w);
+                    }
+                    __syncthreads();
+                    if (a0) {
+#pragma unroll 4
+                        for (int j = 0; j < jn; j++) {
+                            float4 pj = sm.pos[j];
+                            int mj = sm.meta[j];
+                            pair_acc32(x0, y0, z0, q0, m0, l0, pj, mj, (const float2 *)sm.lj, rc2, px0, py0, pz0);
+                            if (warp2 && a1) pair_acc32(x1, y1, z1, q1, m1, l1, pj, mj, (const float2 *)sm.lj, rc2, px1, py1, pz1);
+                        }
+                    }
+                }
+                two_sum(hx0, lx0, px0); two_sum(hy0, ly0, py0); two_sum(hz0, lz0, pz0);
+                two_sum(hx1, lx1, px1); two_sum(hy1, ly1, py1); two_sum(hz1, lz1, pz1);
+            }
+            if (a0) {
+                size_t o = 3 * (size_t)(s0 + ia);
+                part[o] = (double)hx0 + (double)lx0; part[o + 1] = (double)hy0 + (double)ly0; part[o + 2] = (double)hz0 + (double)lz0;
+            }
+            if (a1) {
+                size_t o = 3 * (size_t)(s0 + ibb);
+                part[o] = (double)hx1 + (double)lx1; part[o + 1] = (double)hy1 + (double)ly1; part[o + 2] = (double)hz1 + (double)lz1;
+            }
+        } else {
+            double x0 = 0, y0 = 0, z0 = 0, q0 = 0, x1 = 0, y1 = 0, z1 = 0, q1 = 0;
+            int m0 = -1, m1 = -1, t0r = 0, t1r = 0;
+            if (a0) {
+                double4 p = d.srt_pos[s0 + ia];
+                int2 mt = d.srt_meta[s0 + ia];
+                x0 = p.x; y0 = p.y; z0 = p.z; q0 = p.w * XPI; m0 = mt.x; t0r = mt.y * NTYPE;
+            }
+            if (a1) {
+                double4 p = d.srt_pos[s0 + ibb];
+                int2 mt = d.srt_meta[s0 + ibb];
+                x1 = p.x; y1 = p.y; z1 = p.z; q1 = p.w * XPI; m1 = mt.x; t1r = mt.y * NTYPE;
+            }
+            double fx0 = 0, fy0 = 0, fz0 = 0, fx1 = 0, fy1 = 0, fz1 = 0;
+            const double rc2 = RC * RC;
+            for (int dyc = -1; dyc <= 1; dyc++) {
+                const int jy = iy + dyc;
+                if (jy < 0 || jy >= r.nc[1]) continue;
+                const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+                const int c0 = cell_index(r, jx0, jy, jz);
+                const int t0 = d.cstart[c0], tend = d.cstart[c0 + (jx1 - jx0) + 1];
+                for (int jb = t0; jb < tend; jb += NEAR_CHUNK) {
+                    const int jn = min(NEAR_CHUNK, tend - jb);
+                    __syncthreads();
+                    for (int k = threadIdx.x; k < jn; k += NEAR_THREADS) {
+                        int2 mt = d.srt_meta[jb + k];
+                        sm.meta[k] = (mt.x << 5) | mt.y;
+                        sm.pos[k] = d.srt_pos[jb + k];
+                    }
+                    __syncthreads();
+                    if (a0) {
+#pragma unroll 2
+                        for (int j = 0; j < jn; j++) {
+                            double4 pj = sm.pos[j];
+                            int mj = sm.meta[j];
+                            pair_acc64(x0, y0, z0, q0, m0, t0r, pj, mj, (const double2 *)sm.lj, rc2, fx0, fy0, fz0);
+                            if (warp2 && a1) pair_acc64(x1, y1, z1, q1, m1, t1r, pj, mj, (const double2 *)sm.lj, rc2, fx1, fy1, fz1);
+                        }
+                    }
+                }
+            }
+            if (a0) { size_t o = 3 * (size_t)(s0 + ia); part[o] = fx0; part[o + 1] = fy0; part[o + 2] = fz0; }
+            if (a1) { size_t o = 3 * (size_t)(s0 + ibb); part[o] = fx1; part[o + 1] = fy1; part[o + 2] = fz1; }
         }
-        if (a0) { size_t o = 3 * (size_t)(s0 + i0); d.nf[o] = fx0; d.nf[o + 1] = fy0; d.nf[o + 2] = fz0; }
-        if (a1) { size_t o = 3 * (size_t)(s0 + i1); d.nf[o] = fx1; d.nf[o + 1] = fy1; d.nf[o + 2] = fz1; }
     }
 }
 
-void launch_near(const Dev &d, int ncell, int mixed, int terms, cudaStream_t st) {
-    if (mixed) k_near<true><<<ncell, NEAR_THREADS, 0, st>>>(d, terms);
-    else k_near<false><<<ncell, NEAR_THREADS, 0, st>>>(d, terms);
+// Sum of the three planes (fixed order) plus the local-expansion force of
+// src/evalLjk4.f90:31-282 for every slot; writes nf.
+template <bool MIXED>
+__global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
+    typedef typename std::conditional<MIXED, float, double>::type R;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nslot || s >= d.cstart[ncell]) return;
+    double fx = 0.0, fy = 0.0, fz = 0.0;
+    if (terms & SESP_T_NEAR) {
+        for (int pl = 0; pl < 3; pl++) {
+            const double *p = d.near_part + (size_t)pl * 3 * nslot + 3 * (size_t)s;
+            fx += p[0]; fy += p[1]; fz += p[2];
+        }
+    }
+    if (terms & SESP_T_FAR) {
+        const int g = d.srt_site[s];
+        const int c = d.sloc[g];
+        R Lre[LP], Lim[LP];
+        const double2 *L = d.L4 + (size_t)c * LP;
+        for (int k = 0; k < LP; k++) { double2 v = L[k]; Lre[k] = (R)v.x; Lim[k] = (R)v.y; }
+        R x, y, z;
+        double4 pd = d.srt_pos[s];
+        if (MIXED) {
+            float4 p = d.srt_pos32[s];
+            x = p.x; y = p.y; z = p.z;
+        } else {
+            const Rep r = d.rep[d.crep[c]];
+            int ix, iy, iz;
+            cell_xyz(r, c, ix, iy, iz);
+            x = (R)(pd.x - cell_centre(d, r, 0, ix)); y = (R)(pd.y - cell_centre(d, r, 1, iy)); z = (R)(pd.z - cell_centre(d, r, 2, iz));
+        }
+        R gx, gy, gz;
+        local_grad<R>(Lre, Lim, x, y, z, gx, gy, gz, nullptr);
+        R q = (R)(pd.w * XPI);
+        fx -= (double)(q * gx); fy -= (double)(q * gy); fz -= (double)(q * gz);
+    }
+    d.nf[3 * (size_t)s] = fx; d.nf[3 * (size_t)s + 1] = fy; d.nf[3 * (size_t)s + 2] = fz;
+}
+
+void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, cudaStream_t st) {
+    if (terms & SESP_T_NEAR) {
+        if (mixed) k_near<true><<<3 * ncell, NEAR_THREADS, 0, st>>>(d, nslot);
+        else k_near<false><<<3 * ncell, NEAR_THREADS, 0, st>>>(d, nslot);
+    }
+    if (mixed) k_near_finish<true><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
+    else k_near_finish<false><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
 }
 
 // ------------------------------------------------------------------ multipoles

@@ -17,16 +17,16 @@ void upload_tables_exact(const Tables &t, cudaStream_t st);
 void launch_locate(const Dev &d, int nmol, cudaStream_t st);
 void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st);
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
-                   cudaStream_t st, const SideStream &side);
-void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit,
-                   cudaStream_t st, const SideStream &side);
+                   int fast, cudaStream_t st);
+void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit, int fast,
+                   cudaStream_t st);
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st);
 
 // k_force.cu
 void upload_tables_force(const Tables &t, cudaStream_t st);
 void launch_sort(const Dev &d, int nsite, int ncell, cudaStream_t st);
 void launch_gather(const Dev &d, int nslot, int ncell, int mixed, cudaStream_t st);
-void launch_near(const Dev &d, int ncell, int mixed, int terms, cudaStream_t st);
+void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, cudaStream_t st);
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st);
 void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st);
 void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st);

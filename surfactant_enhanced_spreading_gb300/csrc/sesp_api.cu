@@ -142,6 +142,19 @@ Tables make_tables() {
 
 namespace {
 
+// per site kind (sqrt(48 eps), sigma / 2) for the FP32 pair kernel, which
+// combines them by the Lorentz-Berthelot rule of src/init_arrays.f90:476-502:
+// 48 eps_ij = sqrt(48 eps_i) sqrt(48 eps_j), sigma_ij = sigma_i/2 + sigma_j/2
+std::vector<float2> make_lj_kinds() {
+    double sgs[NSURF], eps[NSURF];
+    surf_lj(sgs, eps);
+    std::vector<float2> t(NTYPE);
+    t[0] = make_float2((float)sqrt(48.0), 0.5f);     // water O: sigma = epsilon = 1
+    t[1] = make_float2(0.f, 0.f);                     // water H: no LJ
+    for (int k = 0; k < NSURF; k++) t[2 + k] = make_float2((float)sqrt(48.0 * eps[k]), (float)(sgs[k] / 2.0));
+    return t;
+}
+
 // contribution table of the intramolecular kernel: term slots per site.
 // Layout (matches IntraMap in k_force.cu): short off[30], short list[852],
 // uchar pa[312], uchar pb[312].  Slots: angle a -> 3a + {i, vertex, k};
@@ -289,6 +302,7 @@ struct sesp_ctx {
     Dev d;
     int *wmols = nullptr, *smols = nullptr;
     std::vector<void *> allocs;
+    size_t bytes = 0;
     int64_t steps = 0;
     // graphs of one step with / without a rebuild
     cudaGraphExec_t g_step[2] = {nullptr, nullptr};
@@ -312,6 +326,7 @@ int dalloc(sesp_ctx *c, T **p, size_t n) {
     if (e != cudaSuccess) return fail(SESP_ENOMEM, "cudaMalloc of %zu bytes: %s", n * sizeof(T), cudaGetErrorString(e));
     cudaMemsetAsync(q, 0, n * sizeof(T), c->st);
     c->allocs.push_back(q);
+    c->bytes += n * sizeof(T);
     *p = (T *)q;
     return 0;
 }
@@ -321,6 +336,7 @@ void free_state(sesp_ctx *c) {
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     for (void *q : c->allocs) cudaFree(q);
     c->allocs.clear();
+    c->bytes = 0;
     c->uploaded = false;
     c->have_force = false;
 }
@@ -387,7 +403,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         tstop(c, 6);
     }
     tstart(c, 0);
-    launch_near(d, c->ncell, mixed, terms, c->st);
+    launch_near(d, c->ncell, c->nsite, mixed, terms, c->st);
     tstop(c, 0);
     tstart(c, 4);
     launch_site_forces(d, c->nsite, terms, mixed, c->st);
@@ -397,12 +413,14 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
 
 void seq_move_a(sesp_ctx *c) {
     tstart(c, 2);
-    launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit, c->st, c->side);
+    launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit,
+                  c->p.precision == SESP_MIXED, c->st);
     tstop(c, 2);
 }
 void seq_move_b(sesp_ctx *c) {
     tstart(c, 3);
-    launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit, c->st, c->side);
+    launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit,
+                  c->p.precision == SESP_MIXED, c->st);
     tstop(c, 3);
 }
 
@@ -556,12 +574,12 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.b3rep, n3)) || (e = dalloc(c, &d.b2rep, n2)) || (e = dalloc(c, &d.cstart, C + 1)) ||
         (e = dalloc(c, &d.ccount, C)) || (e = dalloc(c, &d.cfill, C)) || (e = dalloc(c, &d.sloc, N)) ||
         (e = dalloc(c, &d.sslot, N)) || (e = dalloc(c, &d.srt_site, N)) || (e = dalloc(c, &d.srt_pos, N)) ||
-        (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) ||
+        (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) || (e = dalloc(c, &d.near_part, 9 * (size_t)N)) ||
         (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
         (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
         (e = dalloc(c, &d.L2, (size_t)LP * n2)) || (e = dalloc(c, &d.counters, 8)) ||
-        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)))
+        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &d.lj_kind, NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)))
         return e;
     int w2 = 2 * d2 + 1;
     if ((e = dalloc(c, &d.op_m2l4, (size_t)343 * LPH * LP)) || (e = dalloc(c, &d.op_m2l3, (size_t)343 * LPH * LP)) ||
@@ -659,6 +677,8 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         }
     }
     std::vector<double2> ljt = make_lj_table();
+    std::vector<float2> ljk = make_lj_kinds();
+    CK(cudaMemcpyAsync(d.lj_kind, ljk.data(), ljk.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.x, sx.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.y, sy.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.z, sz.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
@@ -924,6 +944,22 @@ int sesp_run(sesp_ctx *c, int kb0, int nsteps) {
 }
 
 int sesp_run_async(sesp_ctx *c, int kb0, int nsteps) { return launch_steps(c, kb0, nsteps); }
+
+int sesp_query(sesp_ctx *c) {
+    if (!c) return -fail(SESP_EINVAL, "null context");
+    if (set_device(c)) return -SESP_ECUDA;
+    cudaError_t e = cudaStreamQuery(c->st);
+    if (e == cudaSuccess) return 0;
+    if (e == cudaErrorNotReady) return 1;
+    return -fail(SESP_ECUDA, "stream query: %s", cudaGetErrorString(e));
+}
+
+int sesp_device_bytes(sesp_ctx *c, int64_t *bytes) {
+    if (int e = check_ctx(c, false)) return e;
+    if (!bytes) return fail(SESP_EINVAL, "null output");
+    *bytes = (int64_t)c->bytes;
+    return 0;
+}
 
 int sesp_sync(sesp_ctx *c) {
     if (int e = check_ctx(c, false)) return e;

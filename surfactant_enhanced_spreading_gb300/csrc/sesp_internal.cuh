@@ -96,6 +96,7 @@ struct Dev {
     float4 *srt_pos32;   // x, y, z relative to the slot's own cell centre, q (mixed)
     int2 *srt_meta;      // molecule, type
     double *nf;          // near + far force by slot [3 * nslot]
+    double *near_part;   // per dz plane partial near force [3][3 * nslot]
     // graphite columns of the bottom layer
     int *gcol_start;
     double4 *gpos;
@@ -109,7 +110,7 @@ struct Dev {
     int *m2l2_off;       // per replica: (2nr-1)^3 index map to operators
     // LJ pair table (eps, sg6), NTYPE^2
     double2 *ljt;
-    float2 *ljt32;
+    float2 *lj_kind;     // per site kind (sqrt(48 eps), sigma / 2), zero eps for water H
     // counters: [0] fails, [1] overflow, [2] unlocated, [3] max cell, [5] pairs, [6] LJ pairs
     unsigned long long *counters;
     int max_cell;

@@ -31,7 +31,7 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_download_forces", "sesp_init_accel", "sesp_move_a", "sesp_move_b", "sesp_step", "sesp_run",
            "sesp_run_async", "sesp_sync", "sesp_temperature", "sesp_get_eta", "sesp_set_eta", "sesp_energies",
            "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts",
-           "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch"]
+           "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes"]
 
 
 class SespError(RuntimeError):
@@ -87,6 +87,8 @@ def load(path: str = LIB_PATH):
     L.sesp_upload_batch.argtypes = [P, ctypes.c_int, ip, ip, ip, dp, dp, ip, dp]
     L.sesp_replica_count.argtypes = [P]
     L.sesp_get_eta_batch.argtypes = [P, dp]
+    L.sesp_query.argtypes = [P]
+    L.sesp_device_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     _lib = L
     return L
 
@@ -207,6 +209,18 @@ class Engine:
 
     def sync(self):
         _check(_lib.sesp_sync(self._h))
+
+    def busy(self) -> bool:
+        """True while work launched on this context is still running (non-blocking)."""
+        rc = _lib.sesp_query(self._h)
+        if rc < 0:
+            _check(-rc)
+        return rc == 1
+
+    def device_bytes(self) -> int:
+        v = ctypes.c_int64()
+        _check(_lib.sesp_device_bytes(self._h, ctypes.byref(v)))
+        return v.value
 
     def state(self):
         pos, vel, acc = (np.empty((self.n, 3)) for _ in range(3))

@@ -89,6 +89,16 @@ def _rand_rot(rng):
                      [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
 
 
+def _rand_rots(rng, n):
+    """n uniformly random rotation matrices (unit quaternions)."""
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    a, b, c, d = q.T
+    return np.stack([np.stack([a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)], -1),
+                     np.stack([2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)], -1),
+                     np.stack([2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d], -1)], 1)
+
+
 def water_template() -> np.ndarray:
     """O, H, H in Angstrom with O at the origin."""
     half = 109.47 * math.pi / 180.0 / 2.0
@@ -166,19 +176,18 @@ def graphite(layers: int, half_x: float, half_y: float, z_top: float) -> np.ndar
     cc = 1.421
     a1 = np.array([1.5 * cc, math.sqrt(3) / 2 * cc])
     a2 = np.array([1.5 * cc, -math.sqrt(3) / 2 * cc])
-    basis = [np.zeros(2), np.array([cc, 0.0])]
     n = int(2 * max(half_x, half_y) / cc) + 4
+    i, j = np.meshgrid(np.arange(-n, n + 1), np.arange(-n, n + 1), indexing="ij")
+    base = i.ravel()[:, None] * a1 + j.ravel()[:, None] * a2
     out = []
     for layer in range(layers):
         shift = np.array([cc, 0.0]) if layer % 2 else np.zeros(2)
         z = z_top - 3.41 * layer
-        for i in range(-n, n + 1):
-            for j in range(-n, n + 1):
-                for b in basis:
-                    p = i * a1 + j * a2 + b + shift
-                    if abs(p[0]) < half_x and abs(p[1]) < half_y:
-                        out.append((p[0], p[1], z))
-    return np.array(out, dtype=np.float64)
+        for b in (np.zeros(2), np.array([cc, 0.0])):
+            p = base + b + shift
+            keep = (np.abs(p[:, 0]) < half_x) & (np.abs(p[:, 1]) < half_y)
+            out.append(np.column_stack([p[keep], np.full(keep.sum(), z)]))
+    return np.concatenate(out).astype(np.float64)
 
 
 def maxwell(masses: np.ndarray, rng, temperature: float = TR) -> np.ndarray:
@@ -204,23 +213,21 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
     radius = (3.0 * n_water / (2.0 * math.pi * density)) ** (1.0 / 3.0)
     a = density ** (-1.0 / 3.0)
     nlat = int(radius / a) + 3
-    pts = []
-    for i in range(-nlat, nlat + 1):
-        for j in range(-nlat, nlat + 1):
-            for k in range(0, nlat + 1):
-                p = np.array([i * a, j * a, k * a]) + rng.uniform(-0.15, 0.15, size=3) * a
-                if p[2] < 0.0:
-                    p[2] = -p[2]
-                if np.linalg.norm(p) <= radius * 1.15:
-                    pts.append(p)
-    pts = np.array(pts)
+    g = np.arange(-nlat, nlat + 1, dtype=np.float64)
+    gx, gy, gz = np.meshgrid(g, g, np.arange(0, nlat + 1, dtype=np.float64), indexing="ij")
+    pts = np.stack([gx.ravel(), gy.ravel(), gz.ravel()], axis=1) * a
+    pts = pts + rng.uniform(-0.15, 0.15, size=pts.shape) * a
+    pts[:, 2] = np.abs(pts[:, 2])
+    pts = pts[np.linalg.norm(pts, axis=1) <= radius * 1.15]
     pts = pts[np.argsort(np.linalg.norm(pts, axis=1), kind="stable")]
     surf_sites = []
     if n_surf:
-        placed = np.zeros((0, 3))
-        for _ in range(n_surf):
-            tmpl = surfactant_template(rng)
-            tmpl -= tmpl.mean(axis=0)
+        # a library of clash-free conformations, each placed with its own rotation
+        library = [surfactant_template(rng) for _ in range(min(n_surf, 16))]
+        library = [t - t.mean(axis=0) for t in library]
+        centres = []
+        for k in range(n_surf):
+            tmpl = library[k % len(library)]
             for _t in range(400):
                 rot = _rand_rot(rng)
                 u = rng.normal(size=3)
@@ -231,10 +238,18 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
                 cand = tmpl @ rot.T + centre
                 if cand[:, 2].min() < 2.0:
                     cand[:, 2] += 2.0 - cand[:, 2].min()
-                if placed.shape[0] and np.min(np.linalg.norm(cand[:, None, :] - placed[None, :, :], axis=2)) < 3.5:
+                cc = cand.mean(axis=0)
+                clash = False
+                if centres:
+                    near = np.nonzero(np.linalg.norm(np.array(centres) - cc, axis=1) < 32.0)[0]
+                    for q in near:
+                        if np.min(np.linalg.norm(cand[:, None, :] - surf_sites[q][None, :, :], axis=2)) < 3.5:
+                            clash = True
+                            break
+                if clash:
                     continue
                 surf_sites.append(cand)
-                placed = np.concatenate([placed, cand])
+                centres.append(cc)
                 break
             else:
                 raise RuntimeError("could not place surfactant")
@@ -251,9 +266,8 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
         raise RuntimeError("lattice too small for the droplet")
     pts = pts[:n_water]
     wt = water_template()
-    wat = np.empty((n_water, 3, 3))
-    for m in range(n_water):
-        wat[m] = wt @ _rand_rot(rng).T + pts[m]
+    rots = _rand_rots(rng, n_water)
+    wat = np.einsum("ij,mkj->mik", wt, rots) + pts[:, None, :]
     pos = [wat.reshape(-1, 3)]
     if surf_sites:
         pos.append(np.concatenate(surf_sites))

@@ -147,3 +147,38 @@ def test_kernel_timing_path(sys_small):
     assert (ms > 0).all()
     nc, nl = eng.pair_counts()
     assert nc > nl > 0
+
+
+def test_mixed_trajectory_100_steps():
+    """The mixed path (FP32 pair / multipole terms, reciprocal constraint
+    updates) stays close to the FP64 oracle over 100 steps."""
+    s = S.droplet(400, 4, cells=(8, 8, 8), seed=23)
+    eng, orc = E.Engine(s, E.MIXED), O.Oracle(s)
+    eng.force(True); orc.force(True)
+    eng.init_accel(); orc.init_accel()
+    eng.run(99101, 100)
+    orc.run(99101, 100)
+    p_g, _, _ = eng.state()
+    assert np.abs(p_g - orc.get(0)).max() < 1e-4
+
+
+def _nve_drift(precision, steps=400, every=50):
+    """Energy drift (reduced energy per step) with the thermostat off."""
+    s = S.droplet(500, 4, cells=(8, 8, 8), seed=41)
+    eng = E.Engine(s, precision, tau_steps=1e12)
+    eng.force(True)
+    eng.init_accel()
+    es = []
+    kb = 99101
+    for k in range(steps // every):
+        eng.run(kb, every)
+        kb += every
+        es.append(eng.energies().sum())
+    t = np.arange(len(es)) * every
+    return np.polyfit(t, np.array(es), 1)[0], abs(np.mean(es))
+
+
+def test_mixed_energy_drift_not_worse_than_plain():
+    dp, scale = _nve_drift(E.PLAIN_FP64)
+    dm, _ = _nve_drift(E.MIXED)
+    assert abs(dm) <= 2.0 * abs(dp) + 1e-6 * scale, (dm, dp)
