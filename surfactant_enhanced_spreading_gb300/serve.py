@@ -1,0 +1,248 @@
+"""Request loop for spreading runs on one GPU, with continuous batching.
+
+A request is one droplet run: its initial state (a seeded droplet of waters
+and surfactants on graphite, built by the client), a step count and an arrival
+time.  The server admits requests in arrival order as long as their device
+memory fits the HBM budget, gives each its own engine context (own CUDA
+stream, state resident on the device), and advances every admitted run by
+chunks of `chunk` steps launched asynchronously: chunks of different runs
+execute concurrently on the GPU, and a run that arrives while others are
+running starts as soon as memory allows.  Finished runs are downloaded,
+their memory is released and the next requests are admitted.
+
+Every run is independent of the others (its own context; all kernels are
+deterministic), so its result is bit-identical whether it runs alone or in
+the mix - which tests/test_gpu_serve.py checks.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+import time
+
+import numpy as np
+
+from . import engine as E
+from . import system as S
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    system: S.System
+    steps: int
+    arrival: float = 0.0        # seconds after the start of the run
+
+
+@dataclasses.dataclass
+class Result:
+    rid: int
+    n_sites: int
+    steps: int
+    arrival: float
+    admitted: float
+    finished: float
+    pos: np.ndarray | None = None
+    vel: np.ndarray | None = None
+    eta: float = 0.0
+
+    @property
+    def latency(self) -> float:
+        return self.finished - self.arrival
+
+
+def cells_for(n_water: int, n_surf: int) -> tuple:
+    """A closed box (multiples of 4 cells of 12 A) that holds the droplet the
+    generator builds for these counts."""
+    radius = (3.0 * n_water / (2.0 * math.pi * 0.0334)) ** (1.0 / 3.0)
+    shell = 14.0 if n_surf else 2.0
+    half_xy = radius + shell + 0.02 * n_surf + 8.0
+    height = 7.2 + radius + shell + 0.02 * n_surf + 8.0
+    cx = 4 * math.ceil(2.0 * half_xy / 12.0 / 4.0)
+    cz = 4 * math.ceil(2.0 * height / 12.0 / 4.0)
+    return (max(cx, 4), max(cx, 4), max(cz, 4))
+
+
+def make_request(rid: int, n_water: int, n_surf: int, steps: int, seed: int, arrival: float = 0.0) -> Request:
+    cells = list(cells_for(n_water, n_surf))
+    for _ in range(4):
+        try:
+            s = S.droplet(n_water, n_surf, cells=tuple(cells), seed=seed)
+            return Request(rid=rid, system=s, steps=steps, arrival=arrival)
+        except RuntimeError as e:
+            if "does not fit" not in str(e):
+                raise
+            cells = [c + 4 for c in cells]
+    raise RuntimeError(f"no box found for {n_water} waters and {n_surf} surfactants")
+
+
+def estimate_bytes(system: S.System) -> int:
+    """Upper estimate of an engine's device memory for this system."""
+    n = system.n_sites
+    nmol = system.n_water + system.n_surf
+    ncell = int(np.prod(system.cells))
+    per_site = 12 * 8 + 1 + 4 * 5 + 32 + 16 + 8 + 24 + 72 + 4
+    per_cell = 4 * 4 + 2 * 25 * 16 + 2 * 25 * 16 // 8
+    ncarb_cols = system.carbons.reshape(-1, 3).shape[0] * 12
+    fixed = 343 * 375 * (16 + 8) * 2 + 16 * 375 * 16 * 4 + (1 << 20)
+    return int(n * per_site + nmol * 40 + ncell * per_cell + ncarb_cols * 32 + fixed)
+
+
+class Server:
+    def __init__(self, budget_bytes: int, precision: int = E.MIXED, chunk: int = 100, max_active: int = 64,
+                 device: int = 0, keep_state: bool = True):
+        self.budget = int(budget_bytes)
+        self.precision = precision
+        self.chunk = int(chunk)
+        self.max_active = int(max_active)
+        self.device = device
+        self.keep_state = keep_state
+        self.peak_used = 0          # largest admitted estimate total seen by the last run()
+
+    def run(self, requests: list[Request], clock=time.perf_counter) -> list[Result]:
+        pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
+        for r in pending:
+            if estimate_bytes(r.system) > self.budget:
+                raise E.SespError(f"EBUDGET: request {r.rid} needs more than the whole budget")
+        active = []
+        results = []
+        used = 0
+        self.peak_used = 0
+        t0 = clock()
+        while pending or active:
+            now = clock() - t0
+            # admission in arrival order while the budget allows (no overtaking)
+            while pending and pending[0].arrival <= now and len(active) < self.max_active:
+                req = pending[0]
+                est = estimate_bytes(req.system)
+                if used + est > self.budget:
+                    break
+                pending.pop(0)
+                eng = E.Engine(req.system, self.precision, device=self.device)
+                eng.force(True)
+                eng.init_accel()
+                nbytes = max(est, eng.device_bytes())
+                used += nbytes
+                self.peak_used = max(self.peak_used, used)
+                active.append({"req": req, "eng": eng, "done": 0, "kb": 99101, "bytes": nbytes,
+                               "admitted": clock() - t0, "running": False})
+            progressed = False
+            for a in list(active):
+                eng = a["eng"]
+                if a["running"] and eng.busy():
+                    continue
+                a["running"] = False
+                req = a["req"]
+                if a["done"] < req.steps:
+                    n = min(self.chunk, req.steps - a["done"])
+                    eng.run_async(a["kb"], n)
+                    a["kb"] += n
+                    a["done"] += n
+                    a["running"] = True
+                    progressed = True
+                    continue
+                eng.sync()
+                fin = clock() - t0
+                res = Result(rid=req.rid, n_sites=req.system.n_sites, steps=req.steps, arrival=req.arrival,
+                             admitted=a["admitted"], finished=fin)
+                if self.keep_state:
+                    pos, vel, _ = eng.state()
+                    res.pos, res.vel, res.eta = pos, vel, eng.eta
+                eng.close()
+                used -= a["bytes"]
+                active.remove(a)
+                results.append(res)
+                progressed = True
+            if not progressed:
+                if pending and not active:
+                    # idle until the next arrival
+                    wait = pending[0].arrival - (clock() - t0)
+                    if wait > 0:
+                        time.sleep(min(wait, 0.01))
+                else:
+                    time.sleep(0.0002)
+        return sorted(results, key=lambda r: r.rid)
+
+
+def summarize(results: list[Result], wall: float | None = None) -> dict:
+    lat = np.array([r.latency for r in results])
+    atom_steps = float(sum(r.n_sites * r.steps for r in results))
+    span = wall if wall is not None else (max(r.finished for r in results) - min(r.arrival for r in results))
+    return {"requests": len(results), "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
+            "atom_steps_per_s": atom_steps / span if span > 0 else None, "span_s": span}
+
+
+def poisson_requests(n: int, rate_per_s: float, seed: int, water=(1000, 50000), surf=(0, 500), steps=(500, 5000),
+                     step_quantum: int = 100) -> list[Request]:
+    """Seeded Poisson arrivals of seeded droplet runs."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for k in range(n):
+        t += rng.exponential(1.0 / rate_per_s)
+        nw = int(rng.integers(water[0], water[1] + 1))
+        ns = int(rng.integers(surf[0], surf[1] + 1))
+        st = int(rng.integers(steps[0] // step_quantum, steps[1] // step_quantum + 1)) * step_quantum
+        out.append(make_request(k, nw, ns, st, seed=int(rng.integers(1 << 30)), arrival=t))
+    return out
+
+
+def run_one_at_a_time(requests: list[Request], precision: int, device: int = 0, chunk: int = 100) -> list[Result]:
+    """The same requests served strictly one after another in arrival order
+    (no overlap), for comparison with Server.run: a request starts at its
+    arrival or when the previous one finished, whichever is later."""
+    out = []
+    t0 = time.perf_counter()
+    for req in sorted(requests, key=lambda r: (r.arrival, r.rid)):
+        wait = req.arrival - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        start = time.perf_counter() - t0
+        eng = E.Engine(req.system, precision, device=device)
+        E.mybox_start(eng)
+        kb = 99101
+        for k in range(0, req.steps, chunk):
+            n = min(chunk, req.steps - k)
+            eng.run(kb, n)
+            kb += n
+        eng.sync()
+        pos, vel, _ = eng.state()
+        out.append(Result(rid=req.rid, n_sites=req.system.n_sites, steps=req.steps, arrival=req.arrival,
+                          admitted=start, finished=time.perf_counter() - t0, pos=pos, vel=vel, eta=eng.eta))
+        eng.close()
+    return out
+
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="Serve seeded droplet runs with Poisson arrivals on one GPU.")
+    ap.add_argument("--requests", type=int, default=24)
+    ap.add_argument("--rate", type=float, default=8.0, help="arrivals per second")
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--budget-gb", type=float, default=8.0)
+    ap.add_argument("--chunk", type=int, default=100)
+    ap.add_argument("--water", type=int, nargs=2, default=(1000, 20000))
+    ap.add_argument("--surf", type=int, nargs=2, default=(0, 200))
+    ap.add_argument("--steps", type=int, nargs=2, default=(500, 2000))
+    ap.add_argument("--compare-plain", action="store_true",
+                    help="also serve the same requests one at a time on the plain FP64 path")
+    a = ap.parse_args(argv)
+    reqs = poisson_requests(a.requests, a.rate, a.seed, water=tuple(a.water), surf=tuple(a.surf),
+                            steps=tuple(a.steps))
+    srv = Server(int(a.budget_gb * 2**30), precision=E.MIXED, chunk=a.chunk)
+    # warm the library and the device once so the first request does not pay for it
+    warm = make_request(-1, 300, 3, 100, seed=1)
+    srv.run([warm])
+    res = srv.run(reqs)
+    out = {"mode": "continuous batching, mixed precision", "budget_bytes": srv.budget,
+           "peak_admitted_bytes": srv.peak_used, **summarize(res)}
+    if a.compare_plain:
+        seq = run_one_at_a_time(reqs, E.PLAIN_FP64, chunk=a.chunk)
+        out["one_at_a_time_plain_fp64"] = summarize(seq)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -255,13 +255,9 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
                 raise RuntimeError("could not place surfactant")
     # waters: keep lattice points clear of surfactant sites
     if surf_sites:
-        allsurf = np.concatenate(surf_sites)
-        keep = np.ones(len(pts), dtype=bool)
-        for k0 in range(0, len(pts), 2048):
-            blk = pts[k0:k0 + 2048]
-            d2 = ((blk[:, None, :] - allsurf[None, :, :]) ** 2).sum(-1)
-            keep[k0:k0 + 2048] = d2.min(axis=1) > 9.0
-        pts = pts[keep]
+        from scipy.spatial import cKDTree
+        dmin, _ = cKDTree(np.concatenate(surf_sites)).query(pts, k=1)
+        pts = pts[dmin > 3.0]
     if len(pts) < n_water:
         raise RuntimeError("lattice too small for the droplet")
     pts = pts[:n_water]
