@@ -45,6 +45,8 @@ class Result:
     pos: np.ndarray | None = None
     vel: np.ndarray | None = None
     eta: float = 0.0
+    device_bytes: int = 0
+    estimate_bytes: int = 0
 
     @property
     def latency(self) -> float:
@@ -77,15 +79,28 @@ def make_request(rid: int, n_water: int, n_surf: int, steps: int, seed: int, arr
 
 
 def estimate_bytes(system: S.System) -> int:
-    """Upper estimate of an engine's device memory for this system."""
+    """Upper estimate of an engine's device memory for this system, from the
+    engine's allocation list: per-site, per-molecule and per-cell arrays, the
+    multipole tables of the three levels, the translation operators and the
+    per-column carbon lists (each carbon lies within reach of at most about
+    8 bottom-layer columns), with a 10 % margin."""
     n = system.n_sites
     nmol = system.n_water + system.n_surf
-    ncell = int(np.prod(system.cells))
-    per_site = 12 * 8 + 1 + 4 * 5 + 32 + 16 + 8 + 24 + 72 + 4
-    per_cell = 4 * 4 + 2 * 25 * 16 + 2 * 25 * 16 // 8
-    ncarb_cols = system.carbons.reshape(-1, 3).shape[0] * 12
-    fixed = 343 * 375 * (16 + 8) * 2 + 16 * 375 * 16 * 4 + (1 << 20)
-    return int(n * per_site + nmol * 40 + ncell * per_cell + ncarb_cols * 32 + fixed)
+    nc = np.array(system.cells, dtype=np.int64)
+    ncell = int(np.prod(nc))
+    n3, n2 = ncell // 8, ncell // 64
+    d2 = max(1, int((nc // 4).max()) - 1)
+    w2 = 2 * d2 + 1
+    per_site = 12 * 8 + 1 + 4 * 4 + 32 + 16 + 8 + 3 * 8 + 9 * 8
+    per_mol = 5 * 4 + 2 * 8 + 4 + 4
+    cz = 25 * 16
+    cells = ncell * (4 * 4 + 2 * cz) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
+    ops = (2 * 343 + w2 ** 3 + 4 * 8) * 15 * 25 * 16 + 2 * 343 * 15 * 25 * 8
+    ncarb = system.carbons.reshape(-1, 3).shape[0]
+    graphite = 12 * ncarb * 32 + int(nc[0] * nc[1] + 1) * 4 + int(nc.sum()) * 8 + n * 4
+    surf = 29 * system.n_surf * 4
+    total = n * per_site + nmol * per_mol + cells + ops + graphite + surf + 4096
+    return int(1.1 * total) + (1 << 20)
 
 
 class Server:
@@ -121,10 +136,11 @@ class Server:
                 eng = E.Engine(req.system, self.precision, device=self.device)
                 eng.force(True)
                 eng.init_accel()
-                nbytes = max(est, eng.device_bytes())
+                actual = eng.device_bytes()
+                nbytes = max(est, actual)
                 used += nbytes
                 self.peak_used = max(self.peak_used, used)
-                active.append({"req": req, "eng": eng, "done": 0, "kb": 99101, "bytes": nbytes,
+                active.append({"req": req, "eng": eng, "done": 0, "kb": 99101, "bytes": nbytes, "actual": actual, "est": est,
                                "admitted": clock() - t0, "running": False})
             progressed = False
             for a in list(active):
@@ -144,7 +160,8 @@ class Server:
                 eng.sync()
                 fin = clock() - t0
                 res = Result(rid=req.rid, n_sites=req.system.n_sites, steps=req.steps, arrival=req.arrival,
-                             admitted=a["admitted"], finished=fin)
+                             admitted=a["admitted"], finished=fin, device_bytes=a["actual"],
+                             estimate_bytes=a["est"])
                 if self.keep_state:
                     pos, vel, _ = eng.state()
                     res.pos, res.vel, res.eta = pos, vel, eng.eta

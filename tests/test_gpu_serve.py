@@ -34,6 +34,7 @@ def test_budget_limits_concurrency():
     srv = serve.Server(budget_bytes=int(1.5 * biggest), precision=E.MIXED, chunk=100, keep_state=False)
     res = srv.run(reqs)
     assert len(res) == len(reqs)
+    assert all(0 < r.device_bytes <= r.estimate_bytes for r in res), [(r.device_bytes, r.estimate_bytes) for r in res]
     assert srv.peak_used <= srv.budget
     s = serve.summarize(res)
     assert 0 < s["p50_latency_s"] <= s["p99_latency_s"]
