@@ -166,6 +166,19 @@ int sesp_set_eta(sesp_ctx *ctx, double eta);
  * correction, [3] intramolecular pairs, [4] angles + dihedrals, [5] walls,
  * [6] graphite, [7] kinetic */
 int sesp_energies(sesp_ctx *ctx, double out[8]);
+/* The energies of sesp_energies, bit for bit, without allocating: no
+ * cudaMalloc or cudaFree (sesp_energies does both on every call, and cudaFree
+ * waits for every stream on the device).  For callers that share the GPU with
+ * runs they must not stall, or that have handed out all device memory.  Its
+ * scratch is one fixed array in the library (6.1 MiB on every GPU that loads
+ * it); contexts above SESP_NOALLOC_MAX_SITES sites or SESP_NOALLOC_MAX_SURF
+ * surfactants get SESP_EINVAL.  The first call on a device looks up the
+ * array's device address, so make it before any stream capture.  Calls on one
+ * device share the array and take turns under a lock.  No counterpart in the
+ * reference, which computes no energies. */
+#define SESP_NOALLOC_MAX_SITES 131072
+#define SESP_NOALLOC_MAX_SURF 4096
+int sesp_energies_static(sesp_ctx *ctx, double out[8]);
 /* counts: [0] SHAKE/RATTLE non-convergences since upload, [1] capacity
  * overflows, [2] sites in no cell, [3] steps done, [4] max sites in a cell,
  * [5] near-field ordered pairs of the last rebuild, [6] LJ-eligible pairs */

@@ -130,6 +130,12 @@ module sesp_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: e(8)
     end function
+    ! sesp_energies without allocating (fixed scratch; at most 131072 sites)
+    integer(c_int) function sesp_energies_static(ctx, e) bind(C, name="sesp_energies_static")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: e(8)
+    end function
     integer(c_int) function sesp_counters(ctx, c) bind(C, name="sesp_counters")
       import :: c_int, c_ptr, c_int64_t
       type(c_ptr), value :: ctx

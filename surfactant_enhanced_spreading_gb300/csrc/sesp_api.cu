@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1029,6 +1030,96 @@ int sesp_energies(sesp_ctx *c, double out[8]) {
     for (int s = 0; s < N; s++) { out[0] += hs[3 * s]; out[1] += hs[3 * s + 1]; out[2] += hs[3 * s + 2]; }
     for (int q = 0; q < c->nsm; q++) { out[4] += hm[3 * q]; out[3] += hm[3 * q + 1]; out[2] += hm[3 * q + 2]; }
     for (int g = 0; g < N; g++) { out[5] += hi[3 * g]; out[6] += hi[3 * g + 1]; out[7] += hi[3 * g + 2]; }
+    return 0;
+}
+
+// ------------------------------------------------------------------ energies without allocation
+//
+// sesp_energies takes its per-site scratch from cudaMalloc and gives it back
+// with cudaFree on every call.  Callers that share the GPU with runs they must
+// not disturb cannot afford that: cudaFree waits for all work on the device,
+// so a monitoring call from a loop that keeps several contexts busy at once
+// (the request loop of the serving layer, where every admitted run has its own
+// stream) would stall every run, and once an HBM budget has been handed out in
+// full a cudaMalloc can fail.  sesp_energies_static computes the same eight
+// energies with its scratch in one fixed array compiled into this library.
+//
+// The array holds SESP_NOALLOC_MAX_SITES x 6 + (SESP_NOALLOC_MAX_SURF + 1) x 3
+// + 8 doubles (6.1 MiB); every GPU that loads the library keeps it until the
+// process exits.  In host code its name is only a stand-in: its device
+// address is looked up with cudaGetSymbolAddress, once per device, by the
+// first call on that device, with that device current.  That first call
+// should therefore come before any stream capture.  All calls on one device
+// share the array and it keeps the last call's contents: each call clears the
+// per-slot part (slots that no site occupies are summed as zeros), and calls
+// hold a per-device lock until their result has reached the host, because two
+// calls whose work overlapped on the GPU would race on the array.
+static __device__ __align__(256) double sesp_energy_scratch[6 * (size_t)SESP_NOALLOC_MAX_SITES +
+                                                             3 * ((size_t)SESP_NOALLOC_MAX_SURF + 1) + 8];
+
+namespace {
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_lock[NOALLOC_MAX_DEVICES];
+double *g_noalloc_scratch[NOALLOC_MAX_DEVICES];   // device address per device, null until looked up
+
+// The eight totals, each summed by one thread in the order sesp_energies sums
+// them on the host (sites in order, then surfactants), so both entry points
+// give the same bits.
+__global__ void k_energy_totals(const double *e_slot, const double *e_site, const double *e_mol, int nsite, int ns,
+                                double *out) {
+    const int k = threadIdx.x;
+    if (k >= 8) return;
+    double s = 0.0;
+    if (k <= 2) {
+        for (int i = 0; i < nsite; i++) s += e_slot[3 * (size_t)i + k];
+        if (k == 2)
+            for (int q = 0; q < ns; q++) s += e_mol[3 * q + 2];
+    } else if (k == 3) {
+        for (int q = 0; q < ns; q++) s += e_mol[3 * q + 1];
+    } else if (k == 4) {
+        for (int q = 0; q < ns; q++) s += e_mol[3 * q];
+    } else {
+        for (int g = 0; g < nsite; g++) s += e_site[3 * (size_t)g + (k - 5)];
+    }
+    out[k] = s;
+}
+
+}  // namespace
+
+int sesp_energies_static(sesp_ctx *c, double out[8]) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    if (c->nsite > SESP_NOALLOC_MAX_SITES || c->nsm > SESP_NOALLOC_MAX_SURF)
+        return fail(SESP_EINVAL,
+                    "sesp_energies_static: %d sites and %d surfactants exceed its fixed scratch (at most %d sites "
+                    "and %d surfactants); call sesp_energies instead",
+                    c->nsite, c->nsm, SESP_NOALLOC_MAX_SITES, SESP_NOALLOC_MAX_SURF);
+    if (!c->have_force) return fail(SESP_ESTATE, "energies need a force call first (lists and expansions)");
+    const int dev = c->p.device;
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
+        return fail(SESP_EINVAL, "sesp_energies_static: device %d is beyond the %d it serves", dev, NOALLOC_MAX_DEVICES);
+    if (set_device(c)) return SESP_ECUDA;
+    std::lock_guard<std::mutex> hold(g_noalloc_lock[dev]);
+    if (!g_noalloc_scratch[dev]) {
+        double *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void **)&p, sesp_energy_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(SESP_ECUDA, "sesp_energies_static: device address of the scratch: %s", cudaGetErrorString(e));
+        g_noalloc_scratch[dev] = p;
+    }
+    const int N = c->nsite;
+    double *es = g_noalloc_scratch[dev];
+    double *ei = es + 3 * (size_t)SESP_NOALLOC_MAX_SITES;
+    double *em = ei + 3 * (size_t)SESP_NOALLOC_MAX_SITES;
+    double *tot = em + 3 * ((size_t)SESP_NOALLOC_MAX_SURF + 1);
+    CK(cudaMemsetAsync(es, 0, 3 * sizeof(double) * N, c->st));
+    launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
+    launch_energies(c->d, c->ncell, N, c->smols, c->nsm, es, ei, em, c->st);
+    k_energy_totals<<<1, 32, 0, c->st>>>(es, ei, em, N, c->nsm, tot);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, tot, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
     return 0;
 }
 

@@ -31,7 +31,8 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_download_forces", "sesp_init_accel", "sesp_move_a", "sesp_move_b", "sesp_step", "sesp_run",
            "sesp_run_async", "sesp_sync", "sesp_temperature", "sesp_get_eta", "sesp_set_eta", "sesp_energies",
            "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts",
-           "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes"]
+           "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes",
+           "sesp_energies_static"]
 
 
 class SespError(RuntimeError):
@@ -89,6 +90,7 @@ def load(path: str = LIB_PATH):
     L.sesp_get_eta_batch.argtypes = [P, dp]
     L.sesp_query.argtypes = [P]
     L.sesp_device_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
+    L.sesp_energies_static.argtypes = [P, dp]
     _lib = L
     return L
 
@@ -250,6 +252,15 @@ class Engine:
     def energies(self):
         out = np.empty(8)
         _check(_lib.sesp_energies(self._h, _dp(out)))
+        return out
+
+    def energies_static(self):
+        """The same eight energies through sesp_energies_static: no device
+        allocation, so a loop that shares the GPU with other runs can call it
+        without the device-wide wait of cudaFree (at most 131,072 sites and
+        4,096 surfactants per context)."""
+        out = np.empty(8)
+        _check(_lib.sesp_energies_static(self._h, _dp(out)))
         return out
 
     def counters(self):
