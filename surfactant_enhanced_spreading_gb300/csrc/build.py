@@ -1,11 +1,12 @@
 """Build recipe of the engine library ``libsesp.so`` (sm_103a only).
 
-Three translation units are compiled in parallel with nvcc and linked into a
+Four translation units are compiled in parallel with nvcc and linked into a
 shared library next to this file's package:
 
-* ``k_exact.cu`` with ``-fmad=false``: cell assignment and the SHAKE/RATTLE
-  integrator, whose discrete decisions and iteration counts must round like
-  the reference's separately rounded Fortran arithmetic;
+* ``k_exact.cu`` with ``-fmad=false``: cell assignment and the FP64
+  SHAKE/RATTLE integrator, whose discrete decisions and iteration counts must
+  round like the reference's separately rounded Fortran arithmetic;
+* ``k_constraint32.cu``: the mixed path's FP32 constraint sweeps;
 * ``k_force.cu``: pair, multipole and intramolecular kernels;
 * ``sesp_api.cu``: the C ABI (host code compiled without contraction so the
   force-field tables and translation operators are reproducible).
@@ -22,7 +23,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", "-diag-suppress", "1444"]
-UNITS = [("k_exact.cu", ["-fmad=false"]), ("k_force.cu", []), ("sesp_api.cu", [])]
+UNITS = [("k_exact.cu", ["-fmad=false"]), ("k_constraint32.cu", []), ("k_force.cu", []), ("sesp_api.cu", [])]
 HEADERS = ["sesp_internal.cuh", "k_launch.cuh", os.path.join("..", "..", "include", "sesp.h")]
 
 

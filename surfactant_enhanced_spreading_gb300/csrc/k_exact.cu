@@ -153,16 +153,7 @@ struct MolTopo<NSURF> {
 // move_*_a for one molecule: Nose-Hoover scaled predictor, SHAKE
 // (src/move_w1_a.f90:36-134, src/move_surfactant_a.f90:36-134), and the
 // kinetic sums before and after (src/nh_water1.f90, src/nh_surfactant.f90)
-// 1/x in FP64 from the FP32 hardware estimate and two Newton steps (the
-// mixed path's replacement for divisions; the plain path divides exactly)
-__device__ inline double rcp_fp64(double x) {
-    double y = (double)__frcp_rn((float)x);
-    y = y * (2.0 - x * y);
-    y = y * (2.0 - x * y);
-    return y;
-}
-
-template <int NSITE, bool FAST>
+template <int NSITE>
 __global__ void k_move_a(Dev d, const int *mols, int nm, double tol, int maxit) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nm) return;
@@ -199,7 +190,7 @@ __global__ void k_move_a(Dev d, const int *mols, int nm, double tol, int maxit) 
                 double rxab = rx[i] - rx[j], ryab = ry[i] - ry[j], rzab = rz[i] - rz[j];
                 double rpab = rxab * pxab + ryab * pyab + rzab * pzab;
                 double rma = 1.0 / MolTopo<NSITE>::mass(i), rmb = 1.0 / MolTopo<NSITE>::mass(j);
-                double gab = FAST ? diffsq * rcp_fp64(2.0 * (rma + rmb) * rpab) : diffsq / (2.0 * (rma + rmb) * rpab);
+                double gab = diffsq / (2.0 * (rma + rmb) * rpab);
                 double dx = rxab * gab, dy = ryab * gab, dz = rzab * gab;
                 px[i] = px[i] + rma * dx; py[i] = py[i] + rma * dy; pz[i] = pz[i] + rma * dz;
                 px[j] = px[j] - rmb * dx; py[j] = py[j] - rmb * dy; pz[j] = pz[j] - rmb * dz;
@@ -233,19 +224,12 @@ __device__ constexpr int SBJ[NBOND] = {1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13
                                         19, 20, 21, 22, 23, 24, 25, 26, 27, 28};
 constexpr int SURF_BLOCK = 32;
 
-template <bool FAST>
 __global__ void __launch_bounds__(SURF_BLOCK) k_move_a_surf(Dev d, const int *mols, int nm, double tol, int maxit) {
-    __shared__ double s_rm[NSURF], s_dsq[NBOND], s_fa[NBOND], s_fb[NBOND];
+    __shared__ double s_rm[NSURF], s_dsq[NBOND];
     if (threadIdx.x < NSURF) s_rm[threadIdx.x] = 1.0 / cT.mass[2 + threadIdx.x];
-    if (threadIdx.x < NBOND) {
-        const int b = threadIdx.x;
-        s_dsq[b] = cT.dsqs[b];
-        double rs = 1.0 / cT.mass[2 + SBI[b]] + 1.0 / cT.mass[2 + SBJ[b]];
-        s_fa[b] = 2.0 * rs;                          // SHAKE denominator factor
-        s_fb[b] = (1.0 / DT) / (rs * cT.dsqs[b]);    // RATTLE factor (fast path)
-    }
+    if (threadIdx.x < NBOND) s_dsq[threadIdx.x] = cT.dsqs[threadIdx.x];
     __syncthreads();
-    volatile double *vrm = s_rm, *vdsq = s_dsq, *vfa = s_fa, *vfb = s_fb;
+    volatile double *vrm = s_rm, *vdsq = s_dsq;
     __shared__ double sr[3][NSURF][SURF_BLOCK];
     __shared__ double sv[3][NSURF][SURF_BLOCK];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -287,7 +271,7 @@ __global__ void __launch_bounds__(SURF_BLOCK) k_move_a_surf(Dev d, const int *mo
                 double rxab = vr[0][i][l] - vr[0][j][l], ryab = vr[1][i][l] - vr[1][j][l], rzab = vr[2][i][l] - vr[2][j][l];
                 double rpab = rxab * pxab + ryab * pyab + rzab * pzab;
                 double rma = vrm[i], rmb = vrm[j];
-                double gab = FAST ? diffsq * rcp_fp64(vfa[b] * rpab) : diffsq / (2.0 * (rma + rmb) * rpab);
+                double gab = diffsq / (2.0 * (rma + rmb) * rpab);
                 double dx = rxab * gab, dy = ryab * gab, dz = rzab * gab;
                 px[i] = px[i] + rma * dx; py[i] = py[i] + rma * dy; pz[i] = pz[i] + rma * dz;
                 px[j] = px[j] - rmb * dx; py[j] = py[j] - rmb * dy; pz[j] = pz[j] - rmb * dz;
@@ -312,19 +296,12 @@ __global__ void __launch_bounds__(SURF_BLOCK) k_move_a_surf(Dev d, const int *mo
     if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
 }
 
-template <bool FAST>
 __global__ void __launch_bounds__(SURF_BLOCK) k_move_b_surf(Dev d, const int *mols, int nm, double tol, int maxit) {
-    __shared__ double s_rm[NSURF], s_dsq[NBOND], s_fa[NBOND], s_fb[NBOND];
+    __shared__ double s_rm[NSURF], s_dsq[NBOND];
     if (threadIdx.x < NSURF) s_rm[threadIdx.x] = 1.0 / cT.mass[2 + threadIdx.x];
-    if (threadIdx.x < NBOND) {
-        const int b = threadIdx.x;
-        s_dsq[b] = cT.dsqs[b];
-        double rs = 1.0 / cT.mass[2 + SBI[b]] + 1.0 / cT.mass[2 + SBJ[b]];
-        s_fa[b] = 2.0 * rs;                          // SHAKE denominator factor
-        s_fb[b] = (1.0 / DT) / (rs * cT.dsqs[b]);    // RATTLE factor (fast path)
-    }
+    if (threadIdx.x < NBOND) s_dsq[threadIdx.x] = cT.dsqs[threadIdx.x];
     __syncthreads();
-    volatile double *vrm = s_rm, *vdsq = s_dsq, *vfa = s_fa, *vfb = s_fb;
+    volatile double *vrm = s_rm, *vdsq = s_dsq;
     __shared__ double sr[3][NSURF][SURF_BLOCK];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nm) return;
@@ -356,13 +333,8 @@ __global__ void __launch_bounds__(SURF_BLOCK) k_move_b_surf(Dev d, const int *mo
             double rxab = vr[0][i][l] - vr[0][j][l], ryab = vr[1][i][l] - vr[1][j][l], rzab = vr[2][i][l] - vr[2][j][l];
             double rvab = rxab * vxab + ryab * vyab + rzab * vzab;
             double rma = vrm[i], rmb = vrm[j];
-            double gab;
-            if (FAST) {
-                gab = -rvab * vfb[b];
-            } else {
-                rvab = rvab / DT;
-                gab = -rvab / ((rma + rmb) * vdsq[b]);
-            }
+            rvab = rvab / DT;
+            double gab = -rvab / ((rma + rmb) * vdsq[b]);
             if (fabs(gab) > tol) {
                 double dx = rxab * gab, dy = ryab * gab, dz = rzab * gab;
                 vx[i] = vx[i] + rma * dx * DT; vy[i] = vy[i] + rma * dy * DT; vz[i] = vz[i] + rma * dz * DT;
@@ -401,7 +373,7 @@ __global__ void k_eta(Dev d) {
 
 // move_*_b for one molecule: acceleration from force, friction, RATTLE
 // (src/move_w1_b.f90:30-119, src/move_surfactant_b.f90:30-118)
-template <int NSITE, bool FAST>
+template <int NSITE>
 __global__ void k_move_b(Dev d, const int *mols, int nm, double tol, int maxit) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nm) return;
@@ -430,13 +402,8 @@ __global__ void k_move_b(Dev d, const int *mols, int nm, double tol, int maxit) 
             double rxab = rx[i] - rx[j], ryab = ry[i] - ry[j], rzab = rz[i] - rz[j];
             double rvab = rxab * vxab + ryab * vyab + rzab * vzab;
             double rma = 1.0 / MolTopo<NSITE>::mass(i), rmb = 1.0 / MolTopo<NSITE>::mass(j);
-            double gab;
-            if (FAST) {
-                gab = -rvab * ((1.0 / DT) / ((rma + rmb) * MolTopo<NSITE>::dsq(b)));
-            } else {
-                rvab = rvab / DT;
-                gab = -rvab / ((rma + rmb) * MolTopo<NSITE>::dsq(b));
-            }
+            rvab = rvab / DT;
+            double gab = -rvab / ((rma + rmb) * MolTopo<NSITE>::dsq(b));
             if (fabs(gab) > tol) {
                 double dx = rxab * gab, dy = ryab * gab, dz = rzab * gab;
                 vx[i] = vx[i] + rma * dx * DT; vy[i] = vy[i] + rma * dy * DT; vz[i] = vz[i] + rma * dz * DT;
@@ -473,27 +440,25 @@ void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream
 }
 // fast = 1 (mixed path): reciprocal products instead of FP64 divisions in the
 // constraint iterations; fast = 0 divides exactly as the reference does.
+// fast = 1 (mixed path): the FP32 constraint sweeps of k_constraint32.cu;
+// fast = 0: the FP64 sweeps above, dividing exactly as the reference does.
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
                    int fast, cudaStream_t st) {
-    const int sb = (ns + SURF_BLOCK - 1) / SURF_BLOCK, wb = (nw + 127) / 128;
     if (fast) {
-        if (ns) k_move_a_surf<true><<<sb, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
-        if (nw) k_move_a<3, true><<<wb, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+        launch_move_a32(d, wmols, nw, smols, ns, st, tol, maxit);
     } else {
-        if (ns) k_move_a_surf<false><<<sb, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
-        if (nw) k_move_a<3, false><<<wb, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+        if (ns) k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
+        if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
     }
     k_eta<<<nrep, 1024, 0, st>>>(d);
 }
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit, int fast,
                    cudaStream_t st) {
-    const int sb = (ns + SURF_BLOCK - 1) / SURF_BLOCK, wb = (nw + 127) / 128;
     if (fast) {
-        if (ns) k_move_b_surf<true><<<sb, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
-        if (nw) k_move_b<3, true><<<wb, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+        launch_move_b32(d, wmols, nw, smols, ns, st, tol, maxit);
     } else {
-        if (ns) k_move_b_surf<false><<<sb, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
-        if (nw) k_move_b<3, false><<<wb, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+        if (ns) k_move_b_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
+        if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
     }
 }
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st) {

@@ -22,6 +22,14 @@ void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int
                    cudaStream_t st);
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st);
 
+// k_constraint32.cu (mixed path); false if the uploaded bond graph is not
+// the one the kernels are specialised for
+bool upload_tables_fast(const Tables &t, cudaStream_t st);
+void launch_move_a32(const Dev &d, const int *wmols, int nw, const int *smols, int ns, cudaStream_t st, double tol,
+                     int maxit);
+void launch_move_b32(const Dev &d, const int *wmols, int nw, const int *smols, int ns, cudaStream_t st, double tol,
+                     int maxit);
+
 // k_force.cu
 void upload_tables_force(const Tables &t, cudaStream_t st);
 void launch_sort(const Dev &d, int nsite, int ncell, cudaStream_t st);

@@ -489,6 +489,7 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     }
     upload_tables_exact(T, c->st);
     upload_tables_force(T, c->st);
+    if (!upload_tables_fast(T, c->st)) { delete c; return fail(SESP_ECUDA, "constraint table upload"); }
     if (cudaStreamSynchronize(c->st) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "table upload"); }
     *out = c;
     return 0;

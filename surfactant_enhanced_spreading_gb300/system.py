@@ -234,7 +234,9 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
                 u[2] = abs(u[2]) + 0.15
                 u /= np.linalg.norm(u)
                 # a shell around the droplet surface, thicker as it fills
-                centre = u * (radius + 3.0 + rng.uniform(0.0, 4.0 + 0.05 * len(surf_sites)))
+                # ... widened further after repeated clashes (crowded small droplets)
+                widen = 0.1 * max(0, _t - 100)
+                centre = u * (radius + 3.0 + rng.uniform(0.0, 4.0 + 0.05 * len(surf_sites) + widen))
                 cand = tmpl @ rot.T + centre
                 if cand[:, 2].min() < 2.0:
                     cand[:, 2] += 2.0 - cand[:, 2].min()
