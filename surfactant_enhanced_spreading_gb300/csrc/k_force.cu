@@ -80,6 +80,7 @@ __global__ void k_sort_cells(Dev d) {
         d.srt_site[s0 + rank] = v;
         d.sslot[v] = s0 + rank;
         d.srt_meta[s0 + rank] = make_int2(d.smol[v], (int)d.ptype[v]);
+        d.srt_key[s0 + rank] = d.smol[v] << 5 | (int)d.ptype[v];
     }
 }
 
@@ -195,24 +196,6 @@ __device__ inline void local_grad(const R *Lre, const R *Lim, R x, R y, R z, R &
 
 // ------------------------------------------------------------------ near field
 
-constexpr int NEAR_CHUNK = 2 * NEAR_THREADS;   // partner sites staged per pass
-
-template <bool MIXED>
-struct NearSmem;
-
-template <>
-struct NearSmem<false> {
-    double4 pos[NEAR_CHUNK];
-    int meta[NEAR_CHUNK];     // molecule << 5 | site kind
-    double2 lj[NTYPE * NTYPE];
-};
-template <>
-struct NearSmem<true> {
-    float4 pos[NEAR_CHUNK];
-    int meta[NEAR_CHUNK];
-    float2 lj[NTYPE];         // per kind: (sqrt(48 eps), sigma / 2); zero eps for water H
-};
-
 // 1/sqrt(r2) in FP64 from the FP32 hardware estimate and two Newton steps
 // (relative error of the seed ~2^-22, after two steps at the FP64 rounding level)
 __device__ inline double rsqrt_fp64(double r2) {
@@ -223,229 +206,306 @@ __device__ inline double rsqrt_fp64(double r2) {
     return y;
 }
 
-// error-free two-sum of FP32 values into a (hi, lo) pair
-__device__ __forceinline__ void two_sum(float &hi, float &lo, float v) {
-    float s = hi + v;
-    float bp = s - hi;
-    float err = (hi - (s - bp)) + (v - bp);
-    hi = s;
-    lo += err;
-}
+// Work items, rebuilt with the cell lists: one per (target cell, partner row,
+// chunk of NEAR_TILE target sites).  A partner row is the (up to) 3 cells at
+// (dy, dz) from the target cell along x, contiguous in slot order; the 9 rows
+// (3 planes x 3 rows) of a cell cover its 27-cell shell.
+// item.x = cell, item.y = (plane * 3 + row) << 8 | chunk.
+constexpr int NEAR_TILE = 64;   // target sites per item: 2 per lane of one warp
 
-// One partner's force on one site (src/evalw1w1n.f90:86-104 form): qq / r^3
-// without cutoff plus 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2 within rc; zero
-// for a partner of the same molecule (src/evalSS.f90:36).  FP64 takes the
-// pair's (48 eps sg6, sg6) from the table; FP32 combines per-kind
-// (sqrt(48 eps), sigma/2) by the Lorentz-Berthelot rule of
-// src/init_arrays.f90:476-502.
-__device__ __forceinline__ void pair_acc64(double xi, double yi, double zi, double qi, int mi, int trow, double4 pj,
-                                           int meta, const double2 *lj, double rc2, double &px, double &py, double &pz) {
-    double dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-    double r2 = dx * dx + dy * dy + dz * dz;
-    const bool same = (meta >> 5) == mi;
-    const int tj = meta & 31;
-    r2 = same ? 1.0 : r2;
-    double qq = same ? 0.0 : qi * pj.w;
-    double ir = rsqrt_fp64(r2);
-    double ir2 = ir * ir;
-    double ft = qq * ir * ir2;
-    if (tj != 1) {   // water H carries no LJ; uniform across the warp (one partner per step)
-        double2 v = lj[trow + tj];
-        double on = (r2 <= rc2 && !same) ? v.x : 0.0;
-        double r6 = ir2 * ir2 * ir2;
-        ft += on * r6 * (v.y * r6 - 0.5) * ir2;
+__device__ inline int near_row_mask(const Rep &r, int iy, int iz) {
+    int mask = 0;
+    for (int pl = 0; pl < 3; pl++) {
+        const int jz = iz + pl - 1;
+        if (jz < 0 || jz >= r.nc[2]) continue;
+        for (int rw = 0; rw < 3; rw++) {
+            const int jy = iy + rw - 1;
+            if (jy < 0 || jy >= r.nc[1]) continue;
+            mask |= 1 << (pl * 3 + rw);
+        }
     }
-    px += dx * ft; py += dy * ft; pz += dz * ft;
+    return mask;
 }
 
-__device__ __forceinline__ void pair_acc32(float xi, float yi, float zi, float qi, int mi, float2 li, float4 pj, int meta,
-                                           const float2 *lj, float rc2, float &px, float &py, float &pz) {
-    float dx = xi - pj.x, dy = yi - pj.y, dz = zi - pj.z;
-    float r2 = dx * dx + dy * dy + dz * dz;
-    const bool same = (meta >> 5) == mi;
-    const int tj = meta & 31;
-    r2 = same ? 1.f : r2;
-    float qq = same ? 0.f : qi * pj.w;
-    float ir = rsqrtf(r2);
-    float ir2 = ir * ir;
-    float ft = qq * ir * ir2;
-    if (tj != 1) {
-        float2 v = lj[tj];
-        float e = li.x * v.x;                 // 48 eps_ij
-        float s = li.y + v.y, s2 = s * s, s6 = s2 * s2 * s2;
-        float on = (r2 <= rc2 && !same) ? e * s6 : 0.f;
-        float r6 = ir2 * ir2 * ir2;
-        ft += on * r6 * (s6 * r6 - 0.5f) * ir2;
+__global__ void k_near_items_count(Dev d, int ncell) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int ni = d.cstart[c + 1] - d.cstart[c];
+    int n = 0;
+    if (ni > 0) {
+        const Rep r = d.rep[d.crep[c]];
+        int ix, iy, iz;
+        cell_xyz(r, c, ix, iy, iz);
+        n = __popc(near_row_mask(r, iy, iz)) * ((ni + NEAR_TILE - 1) / NEAR_TILE);
     }
-    px += dx * ft; py += dy * ft; pz += dz * ft;
+    d.near_icount[c] = n;
 }
 
-// Near field, one CTA per (cell, dz plane of neighbour cells).  Each plane is
-// 3 rows of up to 3 cells, contiguous in slot order, staged through shared
-// memory; each thread sums the force of the plane on two sites of the cell
-// (t and t + NEAR_THREADS).  The plane's partial force is written per slot;
-// k_near_finish adds the three planes in a fixed order.  No third-law
-// scatter and no atomics, so every result is bit-reproducible.
-// MIXED: FP32 positions relative to the target cell centre, FP32 pair terms,
-// rows summed in an FP32 (hi, lo) two-sum pair.
-template <bool MIXED>
-__global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot) {
-    __shared__ NearSmem<MIXED> sm;
-    const int c = blockIdx.x / 3;
-    const int plane = blockIdx.x % 3;
-    const int dzc = plane - 1;
-    const int s0 = d.cstart[c];
-    const int ni = d.cstart[c + 1] - s0;
+// exclusive scan of the item counts in place (one block), total to near_ctl[1]
+__global__ void k_near_items_scan(Dev d, int ncell) {
+    __shared__ int part[1024];
+    const int per = (ncell + blockDim.x - 1) / blockDim.x;
+    const int b = threadIdx.x * per, e = min(ncell, b + per);
+    int s = 0;
+    for (int c = b; c < e; c++) s += d.near_icount[c];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int t = 0; t < blockDim.x; t++) { int v = part[t]; part[t] = acc; acc += v; }
+        d.near_ctl[1] = acc;
+    }
+    __syncthreads();
+    int acc = part[threadIdx.x];
+    for (int c = b; c < e; c++) { int v = d.near_icount[c]; d.near_icount[c] = acc; acc += v; }
+}
+
+__global__ void k_near_items_fill(Dev d, int ncell) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncell) return;
+    const int ni = d.cstart[c + 1] - d.cstart[c];
     if (ni == 0) return;
     const Rep r = d.rep[d.crep[c]];
     int ix, iy, iz;
     cell_xyz(r, c, ix, iy, iz);
-    double *part = d.near_part + (size_t)plane * 3 * nslot;
-    const int jz = iz + dzc;
-    if (jz < 0 || jz >= r.nc[2]) {
-        for (int i = threadIdx.x; i < ni; i += NEAR_THREADS) {
-            size_t o = 3 * (size_t)(s0 + i);
-            part[o] = 0.0; part[o + 1] = 0.0; part[o + 2] = 0.0;
-        }
-        return;
+    const int mask = near_row_mask(r, iy, iz);
+    const int nch = (ni + NEAR_TILE - 1) / NEAR_TILE;
+    int k = d.near_icount[c];
+    for (int pr = 0; pr < 9; pr++)
+        if (mask >> pr & 1)
+            for (int ch = 0; ch < nch; ch++) d.near_items[k++] = make_int2(c, pr << 8 | ch);
+}
+
+void launch_near_items(const Dev &d, int ncell, cudaStream_t st) {
+    k_near_items_count<<<(ncell + 255) / 256, 256, 0, st>>>(d, ncell);
+    k_near_items_scan<<<1, 1024, 0, st>>>(d, ncell);
+    k_near_items_fill<<<(ncell + 255) / 256, 256, 0, st>>>(d, ncell);
+}
+
+// One partner's force on the two target sites of a lane (src/evalw1w1n.f90:86-104
+// form): qq / r^3 without cutoff plus 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2
+// within rc; zero for a partner of the same molecule (src/evalSS.f90:36).  The
+// LJ part runs only when some lane of the warp has a target within rc of the
+// partner (the partner is the same for the whole warp).
+// FP32: per-kind (sqrt(48 eps), sigma/2) combined by the Lorentz-Berthelot
+// rule of src/init_arrays.f90:476-502.  FP64: the pair's (48 eps sg6, sg6)
+// from the table.
+struct Tgt32 {
+    float x, y, z, q;   // position relative to the target cell's centre, shifted into the partner cell's frame; q * xpi
+    int m;              // molecule
+    float2 l;           // (sqrt(48 eps), sigma / 2)
+};
+struct Tgt64 {
+    double x, y, z, q;
+    int m, trow;        // molecule, type * NTYPE
+};
+
+__device__ __forceinline__ void pair2_acc32(const Tgt32 &a, const Tgt32 &b, bool two, float4 pj, int key,
+                                            const float2 *lj, float rc2, float (&fa)[3], float (&fb)[3]) {
+    const int mj = key >> 5, tj = key & 31;
+    const float dxa = a.x - pj.x, dya = a.y - pj.y, dza = a.z - pj.z;
+    const bool samea = mj == a.m;
+    const float r2a = samea ? 1.f : dxa * dxa + dya * dya + dza * dza;
+    const float ira = rsqrtf(r2a), ir2a = ira * ira;
+    float fta = (samea ? 0.f : a.q * pj.w) * ira * ir2a;
+    float dxb = 0.f, dyb = 0.f, dzb = 0.f, r2b = 1.f, ir2b = 0.f, ftb = 0.f;
+    bool sameb = true;
+    if (two) {
+        dxb = b.x - pj.x; dyb = b.y - pj.y; dzb = b.z - pj.z;
+        sameb = mj == b.m;
+        r2b = sameb ? 1.f : dxb * dxb + dyb * dyb + dzb * dzb;
+        const float irb = rsqrtf(r2b);
+        ir2b = irb * irb;
+        ftb = (sameb ? 0.f : b.q * pj.w) * irb * ir2b;
     }
+    if (tj != 1) {   // water H carries no LJ
+        const bool na = r2a <= rc2 && !samea, nb = two && r2b <= rc2 && !sameb;
+        if (__any_sync(0xffffffffu, na || nb)) {
+            const float2 v = lj[tj];
+            {
+                const float e = a.l.x * v.x, sg = a.l.y + v.y, s2 = sg * sg, s6 = s2 * s2 * s2;
+                const float on = na ? e * s6 : 0.f;
+                const float r6 = ir2a * ir2a * ir2a;
+                fta += on * r6 * (s6 * r6 - 0.5f) * ir2a;
+            }
+            if (two) {
+                const float e = b.l.x * v.x, sg = b.l.y + v.y, s2 = sg * sg, s6 = s2 * s2 * s2;
+                const float on = nb ? e * s6 : 0.f;
+                const float r6 = ir2b * ir2b * ir2b;
+                ftb += on * r6 * (s6 * r6 - 0.5f) * ir2b;
+            }
+        }
+    }
+    fa[0] += dxa * fta; fa[1] += dya * fta; fa[2] += dza * fta;
+    if (two) { fb[0] += dxb * ftb; fb[1] += dyb * ftb; fb[2] += dzb * ftb; }
+}
+
+__device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool two, double4 pj, int key,
+                                            const double2 *lj, double rc2, double (&fa)[3], double (&fb)[3]) {
+    const int mj = key >> 5, tj = key & 31;
+    const double dxa = a.x - pj.x, dya = a.y - pj.y, dza = a.z - pj.z;
+    const bool samea = mj == a.m;
+    const double r2a = samea ? 1.0 : dxa * dxa + dya * dya + dza * dza;
+    const double ira = rsqrt_fp64(r2a), ir2a = ira * ira;
+    double fta = (samea ? 0.0 : a.q * pj.w) * ira * ir2a;
+    double dxb = 0.0, dyb = 0.0, dzb = 0.0, r2b = 1.0, ir2b = 0.0, ftb = 0.0;
+    bool sameb = true;
+    if (two) {
+        dxb = b.x - pj.x; dyb = b.y - pj.y; dzb = b.z - pj.z;
+        sameb = mj == b.m;
+        r2b = sameb ? 1.0 : dxb * dxb + dyb * dyb + dzb * dzb;
+        const double irb = rsqrt_fp64(r2b);
+        ir2b = irb * irb;
+        ftb = (sameb ? 0.0 : b.q * pj.w) * irb * ir2b;
+    }
+    if (tj != 1) {
+        const bool na = r2a <= rc2 && !samea, nb = two && r2b <= rc2 && !sameb;
+        if (__any_sync(0xffffffffu, na || nb)) {   // a zero LJ term leaves the sum unchanged, so skipping it is exact
+            {
+                const double2 v = lj[a.trow + tj];
+                const double on = na ? v.x : 0.0;
+                const double r6 = ir2a * ir2a * ir2a;
+                fta += on * r6 * (v.y * r6 - 0.5) * ir2a;
+            }
+            if (two) {
+                const double2 v = lj[b.trow + tj];
+                const double on = nb ? v.x : 0.0;
+                const double r6 = ir2b * ir2b * ir2b;
+                ftb += on * r6 * (v.y * r6 - 0.5) * ir2b;
+            }
+        }
+    }
+    fa[0] += dxa * fta; fa[1] += dya * fta; fa[2] += dza * fta;
+    if (two) { fb[0] += dxb * ftb; fb[1] += dyb * ftb; fb[2] += dzb * ftb; }
+}
+
+// Near field as a persistent kernel: each warp takes items from a global
+// counter until none are left, and for its item sums the force of one
+// partner row on 64 target sites (2 per lane), reading the partners straight
+// from L1 (one broadcast load per partner for the whole warp).  Each item
+// writes its own partial per slot (near_part[plane * 3 + row]); k_near_finish
+// adds the 9 partials in a fixed order.  Which warp takes which item does not
+// change any arithmetic, so results are bit-reproducible.
+// MIXED: FP32 positions relative to the cell centres, FP32 pair terms summed
+// in FP32 over one row (at most 3 cells).
+template <bool MIXED>
+__global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot) {
+    __shared__ float2 s_lj32[NTYPE];
+    __shared__ double2 s_lj64[MIXED ? 1 : NTYPE * NTYPE];
     if constexpr (MIXED) {
-        if (threadIdx.x < NTYPE) ((float2 *)sm.lj)[threadIdx.x] = d.lj_kind[threadIdx.x];
+        if (threadIdx.x < NTYPE) s_lj32[threadIdx.x] = d.lj_kind[threadIdx.x];
     } else {
-        for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) ((double2 *)sm.lj)[t] = d.ljt[t];
+        for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) s_lj64[t] = d.ljt[t];
     }
     __syncthreads();
-    const int i0 = threadIdx.x, i1 = NEAR_THREADS + threadIdx.x;
-    for (int ib = 0; ib < ni; ib += 2 * NEAR_THREADS) {
-        const int ia = ib + i0, ibb = ib + i1;
-        const bool a0 = ia < ni, a1 = ibb < ni;
-        const bool warp2 = __any_sync(0xffffffffu, a1);
+    const int lane = threadIdx.x & 31;
+    const int nitems = d.near_ctl[1];
+    const float4 *__restrict__ pos32 = d.srt_pos32;
+    const double4 *__restrict__ pos64 = d.srt_pos;
+    const int *__restrict__ keys = d.srt_key;
+    for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(&d.near_ctl[0], 1);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= nitems) break;
+        const int2 item = d.near_items[k];
+        const int c = item.x, pr = item.y >> 8, chunk = item.y & 255;
+        const int dzc = pr / 3 - 1, dyc = pr % 3 - 1;
+        const int s0 = d.cstart[c], ni = d.cstart[c + 1] - s0;
+        const int i0 = chunk * NEAR_TILE + lane, i1 = i0 + 32;
+        const bool a0 = i0 < ni, a1 = i1 < ni;
+        const bool two = __any_sync(0xffffffffu, a1);
+        const Rep r = d.rep[d.crep[c]];
+        int ix, iy, iz;
+        cell_xyz(r, c, ix, iy, iz);
+        const int jy = iy + dyc, jz = iz + dzc;
+        const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+        double *part = d.near_part + (size_t)pr * 3 * nslot;
         if constexpr (MIXED) {
-            float x0 = 0, y0 = 0, z0 = 0, q0 = 0, x1 = 0, y1 = 0, z1 = 0, q1 = 0;
-            int m0 = -1, m1 = -1;
-            float2 l0 = {0.f, 0.f}, l1 = {0.f, 0.f};
+            Tgt32 ta = {0.f, 0.f, 0.f, 0.f, -1, {0.f, 0.f}}, tb = ta;
             if (a0) {
-                float4 p = d.srt_pos32[s0 + ia];
-                int2 mt = d.srt_meta[s0 + ia];
-                x0 = p.x; y0 = p.y; z0 = p.z; q0 = p.w * (float)XPI; m0 = mt.x; l0 = d.lj_kind[mt.y];
+                const float4 p = pos32[s0 + i0];
+                const int kk = keys[s0 + i0];
+                ta = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, s_lj32[kk & 31]};
             }
             if (a1) {
-                float4 p = d.srt_pos32[s0 + ibb];
-                int2 mt = d.srt_meta[s0 + ibb];
-                x1 = p.x; y1 = p.y; z1 = p.z; q1 = p.w * (float)XPI; m1 = mt.x; l1 = d.lj_kind[mt.y];
+                const float4 p = pos32[s0 + i1];
+                const int kk = keys[s0 + i1];
+                tb = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, s_lj32[kk & 31]};
             }
-            float hx0 = 0, hy0 = 0, hz0 = 0, lx0 = 0, ly0 = 0, lz0 = 0;
-            float hx1 = 0, hy1 = 0, hz1 = 0, lx1 = 0, ly1 = 0, lz1 = 0;
             const float rc2 = (float)(RC * RC);
-            const float oz = (float)(dzc * RS);
-            for (int dyc = -1; dyc <= 1; dyc++) {
-                const int jy = iy + dyc;
-                if (jy < 0 || jy >= r.nc[1]) continue;
-                const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
-                const int c0 = cell_index(r, jx0, jy, jz);
-                const int t0 = d.cstart[c0], tend = d.cstart[c0 + (jx1 - jx0) + 1];
-                const int b1 = jx1 > jx0 ? d.cstart[c0 + 1] : tend;
-                const int b2 = jx1 - jx0 == 2 ? d.cstart[c0 + 2] : tend;
-                const float oy = (float)(dyc * RS);
-                float px0 = 0, py0 = 0, pz0 = 0, px1 = 0, py1 = 0, pz1 = 0;
-                for (int jb = t0; jb < tend; jb += NEAR_CHUNK) {
-                    const int jn = min(NEAR_CHUNK, tend - jb);
-                    __syncthreads();
-                    for (int k = threadIdx.x; k < jn; k += NEAR_THREADS) {
-                        const int sl = jb + k;
-                        int2 mt = d.srt_meta[sl];
-                        sm.meta[k] = (mt.x << 5) | mt.y;
-                        const int cxj = jx0 + (sl >= b1) + (sl >= b2);
-                        const float ox = (float)((cxj - ix) * RS);
-                        float4 v = d.srt_pos32[sl];
-                        sm.pos[k] = make_float4(v.x + ox, v.y + oy, v.z + oz, v.w);
-                    }
-                    __syncthreads();
-                    if (a0) {
+            const float sy = (float)(-dyc * RS), sz = (float)(-dzc * RS);
+            float fa[3] = {0.f, 0.f, 0.f}, fb[3] = {0.f, 0.f, 0.f};
+            for (int jx = jx0; jx <= jx1; jx++) {
+                const int cn = cell_index(r, jx, jy, jz);
+                const int t0 = d.cstart[cn], t1 = d.cstart[cn + 1];
+                const float sx = (float)((ix - jx) * RS);
+                Tgt32 ua = ta, ub = tb;   // targets in the partner cell's frame
+                ua.x += sx; ua.y += sy; ua.z += sz;
+                ub.x += sx; ub.y += sy; ub.z += sz;
 #pragma unroll 4
-                        for (int j = 0; j < jn; j++) {
-                            float4 pj = sm.pos[j];
-                            int mj = sm.meta[j];
-                            pair_acc32(x0, y0, z0, q0, m0, l0, pj, mj, (const float2 *)sm.lj, rc2, px0, py0, pz0);
-                            if (warp2 && a1) pair_acc32(x1, y1, z1, q1, m1, l1, pj, mj, (const float2 *)sm.lj, rc2, px1, py1, pz1);
-                        }
-                    }
-                }
-                two_sum(hx0, lx0, px0); two_sum(hy0, ly0, py0); two_sum(hz0, lz0, pz0);
-                two_sum(hx1, lx1, px1); two_sum(hy1, ly1, py1); two_sum(hz1, lz1, pz1);
+                for (int sl = t0; sl < t1; sl++) pair2_acc32(ua, ub, two, pos32[sl], keys[sl], s_lj32, rc2, fa, fb);
             }
             if (a0) {
-                size_t o = 3 * (size_t)(s0 + ia);
-                part[o] = (double)hx0 + (double)lx0; part[o + 1] = (double)hy0 + (double)ly0; part[o + 2] = (double)hz0 + (double)lz0;
+                const size_t o = 3 * (size_t)(s0 + i0);
+                part[o] = fa[0]; part[o + 1] = fa[1]; part[o + 2] = fa[2];
             }
             if (a1) {
-                size_t o = 3 * (size_t)(s0 + ibb);
-                part[o] = (double)hx1 + (double)lx1; part[o + 1] = (double)hy1 + (double)ly1; part[o + 2] = (double)hz1 + (double)lz1;
+                const size_t o = 3 * (size_t)(s0 + i1);
+                part[o] = fb[0]; part[o + 1] = fb[1]; part[o + 2] = fb[2];
             }
         } else {
-            double x0 = 0, y0 = 0, z0 = 0, q0 = 0, x1 = 0, y1 = 0, z1 = 0, q1 = 0;
-            int m0 = -1, m1 = -1, t0r = 0, t1r = 0;
+            Tgt64 ta = {0.0, 0.0, 0.0, 0.0, -1, 0}, tb = ta;
             if (a0) {
-                double4 p = d.srt_pos[s0 + ia];
-                int2 mt = d.srt_meta[s0 + ia];
-                x0 = p.x; y0 = p.y; z0 = p.z; q0 = p.w * XPI; m0 = mt.x; t0r = mt.y * NTYPE;
+                const double4 p = pos64[s0 + i0];
+                const int kk = keys[s0 + i0];
+                ta = {p.x, p.y, p.z, p.w * XPI, kk >> 5, (kk & 31) * NTYPE};
             }
             if (a1) {
-                double4 p = d.srt_pos[s0 + ibb];
-                int2 mt = d.srt_meta[s0 + ibb];
-                x1 = p.x; y1 = p.y; z1 = p.z; q1 = p.w * XPI; m1 = mt.x; t1r = mt.y * NTYPE;
+                const double4 p = pos64[s0 + i1];
+                const int kk = keys[s0 + i1];
+                tb = {p.x, p.y, p.z, p.w * XPI, kk >> 5, (kk & 31) * NTYPE};
             }
-            double fx0 = 0, fy0 = 0, fz0 = 0, fx1 = 0, fy1 = 0, fz1 = 0;
             const double rc2 = RC * RC;
-            for (int dyc = -1; dyc <= 1; dyc++) {
-                const int jy = iy + dyc;
-                if (jy < 0 || jy >= r.nc[1]) continue;
-                const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
-                const int c0 = cell_index(r, jx0, jy, jz);
-                const int t0 = d.cstart[c0], tend = d.cstart[c0 + (jx1 - jx0) + 1];
-                for (int jb = t0; jb < tend; jb += NEAR_CHUNK) {
-                    const int jn = min(NEAR_CHUNK, tend - jb);
-                    __syncthreads();
-                    for (int k = threadIdx.x; k < jn; k += NEAR_THREADS) {
-                        int2 mt = d.srt_meta[jb + k];
-                        sm.meta[k] = (mt.x << 5) | mt.y;
-                        sm.pos[k] = d.srt_pos[jb + k];
-                    }
-                    __syncthreads();
-                    if (a0) {
+            double fa[3] = {0.0, 0.0, 0.0}, fb[3] = {0.0, 0.0, 0.0};
+            const int ca = cell_index(r, jx0, jy, jz);
+            const int t0 = d.cstart[ca], t1 = d.cstart[ca + (jx1 - jx0) + 1];
 #pragma unroll 2
-                        for (int j = 0; j < jn; j++) {
-                            double4 pj = sm.pos[j];
-                            int mj = sm.meta[j];
-                            pair_acc64(x0, y0, z0, q0, m0, t0r, pj, mj, (const double2 *)sm.lj, rc2, fx0, fy0, fz0);
-                            if (warp2 && a1) pair_acc64(x1, y1, z1, q1, m1, t1r, pj, mj, (const double2 *)sm.lj, rc2, fx1, fy1, fz1);
-                        }
-                    }
-                }
+            for (int sl = t0; sl < t1; sl++) pair2_acc64(ta, tb, two, pos64[sl], keys[sl], s_lj64, rc2, fa, fb);
+            if (a0) {
+                const size_t o = 3 * (size_t)(s0 + i0);
+                part[o] = fa[0]; part[o + 1] = fa[1]; part[o + 2] = fa[2];
             }
-            if (a0) { size_t o = 3 * (size_t)(s0 + ia); part[o] = fx0; part[o + 1] = fy0; part[o + 2] = fz0; }
-            if (a1) { size_t o = 3 * (size_t)(s0 + ibb); part[o] = fx1; part[o + 1] = fy1; part[o + 2] = fz1; }
+            if (a1) {
+                const size_t o = 3 * (size_t)(s0 + i1);
+                part[o] = fb[0]; part[o + 1] = fb[1]; part[o + 2] = fb[2];
+            }
         }
     }
 }
 
-// Sum of the three planes (fixed order) plus the local-expansion force of
+// Sum of the 9 row partials (fixed order) plus the local-expansion force of
 // src/evalLjk4.f90:31-282 for every slot; writes nf.
 template <bool MIXED>
 __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     typedef typename std::conditional<MIXED, float, double>::type R;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nslot || s >= d.cstart[ncell]) return;
+    const int g = d.srt_site[s];
+    const int c = d.sloc[g];
+    const Rep r = d.rep[d.crep[c]];
+    int ix, iy, iz;
+    cell_xyz(r, c, ix, iy, iz);
     double fx = 0.0, fy = 0.0, fz = 0.0;
     if (terms & SESP_T_NEAR) {
-        for (int pl = 0; pl < 3; pl++) {
-            const double *p = d.near_part + (size_t)pl * 3 * nslot + 3 * (size_t)s;
+        const int mask = near_row_mask(r, iy, iz);
+        for (int pr = 0; pr < 9; pr++) {
+            if (!(mask >> pr & 1)) continue;
+            const double *p = d.near_part + (size_t)pr * 3 * nslot + 3 * (size_t)s;
             fx += p[0]; fy += p[1]; fz += p[2];
         }
     }
     if (terms & SESP_T_FAR) {
-        const int g = d.srt_site[s];
-        const int c = d.sloc[g];
         R Lre[LP], Lim[LP];
         const double2 *L = d.L4 + (size_t)c * LP;
         for (int k = 0; k < LP; k++) { double2 v = L[k]; Lre[k] = (R)v.x; Lim[k] = (R)v.y; }
@@ -455,9 +515,6 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
             float4 p = d.srt_pos32[s];
             x = p.x; y = p.y; z = p.z;
         } else {
-            const Rep r = d.rep[d.crep[c]];
-            int ix, iy, iz;
-            cell_xyz(r, c, ix, iy, iz);
             x = (R)(pd.x - cell_centre(d, r, 0, ix)); y = (R)(pd.y - cell_centre(d, r, 1, iy)); z = (R)(pd.z - cell_centre(d, r, 2, iz));
         }
         R gx, gy, gz;
@@ -468,10 +525,13 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     d.nf[3 * (size_t)s] = fx; d.nf[3 * (size_t)s + 1] = fy; d.nf[3 * (size_t)s + 2] = fz;
 }
 
+static int g_near_grid[2] = {0, 0};
+
 void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, cudaStream_t st) {
     if (terms & SESP_T_NEAR) {
-        if (mixed) k_near<true><<<3 * ncell, NEAR_THREADS, 0, st>>>(d, nslot);
-        else k_near<false><<<3 * ncell, NEAR_THREADS, 0, st>>>(d, nslot);
+        cudaMemsetAsync(d.near_ctl, 0, sizeof(int), st);
+        if (mixed) k_near<true><<<g_near_grid[1], NEAR_THREADS, 0, st>>>(d, nslot);
+        else k_near<false><<<g_near_grid[0], NEAR_THREADS, 0, st>>>(d, nslot);
     }
     if (mixed) k_near_finish<true><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
     else k_near_finish<false><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
@@ -721,6 +781,13 @@ size_t m2l_smem() { return sizeof(C2<R>) * (216 * LP + M2L_NB * LPH * LP); }
 // opt-in shared-memory sizes; called once per context creation (the
 // attribute is per device, so every context sets it for its own device)
 void init_force_kernels() {
+    int dev = 0, nsm = 0, nb0 = 0, nb1 = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb0, k_near<false>, NEAR_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_near<true>, NEAR_THREADS, 0);
+    g_near_grid[0] = nsm * (nb0 > 0 ? nb0 : 1);
+    g_near_grid[1] = nsm * (nb1 > 0 ? nb1 : 1);
     cudaFuncSetAttribute(k_m2l_grp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<double>());
     cudaFuncSetAttribute(k_m2l_grp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<float>());
 }

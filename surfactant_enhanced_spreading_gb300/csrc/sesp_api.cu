@@ -393,6 +393,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         cudaMemsetAsync(d.ccount, 0, sizeof(int) * c->ncell, c->st);
         launch_locate(d, c->nmol, c->st);
         launch_sort(d, c->nsite, c->ncell, c->st);
+        launch_near_items(d, c->ncell, c->st);
         launch_isub(d, c->nsm * NSURF, c->smols, c->st);
         launch_graphite_list(d, c->nsite, c->st);
         tstop(c, 5);
@@ -576,7 +577,9 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.b3rep, n3)) || (e = dalloc(c, &d.b2rep, n2)) || (e = dalloc(c, &d.cstart, C + 1)) ||
         (e = dalloc(c, &d.ccount, C)) || (e = dalloc(c, &d.cfill, C)) || (e = dalloc(c, &d.sloc, N)) ||
         (e = dalloc(c, &d.sslot, N)) || (e = dalloc(c, &d.srt_site, N)) || (e = dalloc(c, &d.srt_pos, N)) ||
-        (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) || (e = dalloc(c, &d.near_part, 9 * (size_t)N)) ||
+        (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.srt_key, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) ||
+        (e = dalloc(c, &d.near_part, 27 * (size_t)N)) || (e = dalloc(c, &d.near_items, 9 * ((size_t)N / 64 + C) + 16)) ||
+        (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 2)) ||
         (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
         (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
@@ -703,6 +706,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     CK(cudaMemcpyAsync(d.gcol_start, gstart.data(), gstart.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
     if (!gpos.empty()) CK(cudaMemcpyAsync(d.gpos, gpos.data(), gpos.size() * sizeof(double4), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.ljt, ljt.data(), ljt.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemsetAsync(d.near_ctl, 0, 2 * sizeof(int), c->st));   // no near-field items before the first rebuild
     CK(cudaStreamSynchronize(c->st));
     c->uploaded = true;
     c->have_force = false;

@@ -95,8 +95,12 @@ struct Dev {
     double4 *srt_pos;    // x, y, z, q in slot order (FP64)
     float4 *srt_pos32;   // x, y, z relative to the slot's own cell centre, q (mixed)
     int2 *srt_meta;      // molecule, type
+    int *srt_key;        // molecule << 5 | type
     double *nf;          // near + far force by slot [3 * nslot]
-    double *near_part;   // per dz plane partial near force [3][3 * nslot]
+    double *near_part;   // per partner row partial near force [9][3 * nslot]
+    int2 *near_items;    // near-field work items (cell, row << 8 | chunk)
+    int *near_icount;    // per cell: item count, then first item
+    int *near_ctl;       // [0] item counter of the running launch, [1] item count
     // graphite columns of the bottom layer
     int *gcol_start;
     double4 *gpos;
