@@ -673,19 +673,75 @@ __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const double2 *ops,
 // translation operators offset by offset (each applied to every child whose
 // source at that offset is in the window) and accumulates the 8 x 15 output
 // coefficients in registers.  R is the arithmetic precision.
-constexpr int M2L_NB = 8;   // operators staged per pass
+// M2L with the operator of src/computeLjk4.f90:134-158 factored as
+//   op[(j,k),(n,m)] = cf[(j,k),(n,m)] * H_{j+n}^{m-k}(d),  H_l^q = Y_l^q(d) / |d|^(l+1),
+// d the source - target vector and H_l^{-q} = conj(H_l^q): per offset 45
+// complex H instead of 375 operator entries, so the tables stay in L1/L2
+// and the kernels need no operator staging.  cf holds the offset-independent
+// iIkm2(k,m) rAnm(j,k) rAnm(n,m) / (sgn(n) rAnm(j+n,m-k)).
+constexpr int NH = 45;   // (l, q), l = 0..8, q = 0..l
 
 template <typename R>
 struct C2 {
     R x, y;
 };
-
 template <typename R>
-__global__ void __launch_bounds__(128) k_m2l_grp(Dev d, const double2 *O, double2 *L, const C2<R> *ops,
-                                                  const int *prep, int level) {
+struct M2LCfg;
+template <>
+struct M2LCfg<float> {
+    static constexpr int NG = 4;   // source groups per CTA
+};
+template <>
+struct M2LCfg<double> {
+    static constexpr int NG = 2;
+};
+
+// the 25 terms of output coefficient o: index of H, coefficient for the real
+// and the imaginary part of H (the sign of the latter conjugates H for m < k)
+template <typename R>
+__device__ inline void m2l_terms(int o, const R *cf, int (&h)[LP], R (&cr)[LP], R (&ci)[LP]) {
+    int j, k;
+    out_jk(o, j, k);
+#pragma unroll
+    for (int nm = 0; nm < LP; nm++) {
+        const int n = nm < 1 ? 0 : nm < 4 ? 1 : nm < 9 ? 2 : nm < 16 ? 3 : 4;
+        const int m = nm - n * (n + 1);
+        const int l = j + n, q = m - k;
+        h[nm] = l * (l + 1) / 2 + (q < 0 ? -q : q);
+        const R c = cf[o * LP + nm];
+        cr[nm] = c;
+        ci[nm] = q < 0 ? -c : c;
+    }
+}
+
+template <typename R, typename S>
+__device__ __forceinline__ void m2l_acc(const C2<R> *__restrict__ H, const S *src, const int (&h)[LP],
+                                        const R (&cr)[LP], const R (&ci)[LP], R &re, R &im) {
+#pragma unroll
+    for (int nm = 0; nm < LP; nm++) {
+        const C2<R> hv = H[h[nm]];
+        const S mv = src[nm];
+        const R mx = (R)mv.x, my = (R)mv.y;
+        const R t1 = cr[nm] * hv.x, t2 = ci[nm] * hv.y;
+        re += t1 * mx - t2 * my;
+        im += t1 * my + t2 * mx;
+    }
+}
+
+// M2L at L4 and L3 (src/computeLjk4.f90, src/computeLjk3.f90): one CTA per
+// parent box, its 8 children x 15 outputs x NG source groups; the parent's
+// 6x6x6 window of child-level multipoles is staged in shared memory and each
+// group takes every NG-th of the 343 offsets; the groups' sums are added in
+// a fixed order and accumulated into L.
+template <typename R>
+__global__ void __launch_bounds__(128 * M2LCfg<R>::NG) k_m2l_win(Dev d, const double2 *O, double2 *L,
+                                                                 const C2<R> *Htab, const R *cf, const int *prep,
+                                                                 int level) {
+    constexpr int NG = M2LCfg<R>::NG;
     extern __shared__ __align__(16) unsigned char smraw[];
     C2<R> *sO = (C2<R> *)smraw;                  // [216][LP]
-    C2<R> *sOp = sO + 216 * LP;                  // [M2L_NB][LPH][LP]
+    R *scf = (R *)(sO + 216 * LP);               // [LPH * LP]
+    R *sre = scf + LPH * LP, *sim = sre + NG * 128;
     const int p = blockIdx.x;
     const Rep r = d.rep[prep[p]];
     const int div = level == 4 ? 1 : 2;          // child grid = nc / div
@@ -693,90 +749,98 @@ __global__ void __launch_bounds__(128) k_m2l_grp(Dev d, const double2 *O, double
     const int pbase = level == 4 ? r.l3_0 : r.l2_0;
     const int n[3] = {r.nc[0] / div, r.nc[1] / div, r.nc[2] / div};
     const int np[3] = {n[0] / 2, n[1] / 2, n[2] / 2};
-    int l = p - pbase;
+    const int l = p - pbase;
     const int pc[3] = {l % np[0], (l / np[0]) % np[1], l / (np[0] * np[1])};
     const int w0[3] = {2 * pc[0] - 2, 2 * pc[1] - 2, 2 * pc[2] - 2};
     for (int idx = threadIdx.x; idx < 216 * LP; idx += blockDim.x) {
-        int cell = idx / LP, c = idx % LP;
-        int sx = w0[0] + cell % 6, sy = w0[1] + (cell / 6) % 6, sz = w0[2] + cell / 36;
+        const int cell = idx / LP, c = idx % LP;
+        const int sx = w0[0] + cell % 6, sy = w0[1] + (cell / 6) % 6, sz = w0[2] + cell / 36;
         C2<R> v = {R(0), R(0)};
         if (sx >= 0 && sy >= 0 && sz >= 0 && sx < n[0] && sy < n[1] && sz < n[2]) {
-            double2 o = O[(size_t)(base + sx + n[0] * (sy + n[1] * sz)) * LP + c];
+            const double2 o = O[(size_t)(base + sx + n[0] * (sy + n[1] * sz)) * LP + c];
             v.x = (R)o.x; v.y = (R)o.y;
         }
         sO[idx] = v;
     }
-    const int t = threadIdx.x / LPH, o = threadIdx.x % LPH;
-    const bool act = threadIdx.x < 8 * LPH;
+    for (int idx = threadIdx.x; idx < LPH * LP; idx += blockDim.x) scf[idx] = cf[idx];
+    __syncthreads();
+    const int g = threadIdx.x >> 7, u = threadIdx.x & 127;
+    const bool act = u < 8 * LPH;
+    const int t = u / LPH, o = u % LPH;
     // this child's position in the window (2 or 3 per axis) and in the grid
     const int lc[3] = {2 + (t & 1), 2 + ((t >> 1) & 1), 2 + ((t >> 2) & 1)};
     const int gc[3] = {w0[0] + lc[0], w0[1] + lc[1], w0[2] + lc[2]};
-    R are = 0, aim = 0;
-    for (int d0 = 0; d0 < 343; d0 += M2L_NB) {
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < M2L_NB * LPH * LP; idx += blockDim.x) {
-            int k = idx / (LPH * LP);
-            if (d0 + k < 343) sOp[idx] = ops[(size_t)(d0 + k) * LPH * LP + idx % (LPH * LP)];
-        }
-        __syncthreads();
-        if (!act) continue;
-        for (int k = 0; k < M2L_NB && d0 + k < 343; k++) {
-            int oi = d0 + k;
-            int dx = oi % 7 - 3, dy = (oi / 7) % 7 - 3, dz = oi / 49 - 3;
+    R re = 0, im = 0;
+    if (act) {
+        int h[LP];
+        R cr[LP], ci[LP];
+        m2l_terms<R>(o, scf, h, cr, ci);
+        for (int oi = g; oi < 343; oi += NG) {
+            const int dx = oi % 7 - 3, dy = (oi / 7) % 7 - 3, dz = oi / 49 - 3;
             if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-            int sx = lc[0] + dx, sy = lc[1] + dy, sz = lc[2] + dz;
+            const int sx = lc[0] + dx, sy = lc[1] + dy, sz = lc[2] + dz;
             if (sx < 0 || sy < 0 || sz < 0 || sx > 5 || sy > 5 || sz > 5) continue;
             if (gc[0] + dx < 0 || gc[1] + dy < 0 || gc[2] + dz < 0 || gc[0] + dx >= n[0] || gc[1] + dy >= n[1] ||
                 gc[2] + dz >= n[2])
                 continue;
-            const C2<R> *op = sOp + ((size_t)k * LPH + o) * LP;
-            const C2<R> *src = sO + (size_t)(sx + 6 * (sy + 6 * sz)) * LP;
-#pragma unroll 5
-            for (int c = 0; c < LP; c++) {
-                C2<R> a = op[c], b = src[c];
-                are += a.x * b.x - a.y * b.y;
-                aim += a.x * b.y + a.y * b.x;
-            }
+            m2l_acc<R>(Htab + (size_t)oi * NH, sO + (size_t)(sx + 6 * (sy + 6 * sz)) * LP, h, cr, ci, re, im);
         }
     }
-    if (act) {
-        int child = base + gc[0] + n[0] * (gc[1] + n[1] * gc[2]);
-        store_jk(L + (size_t)child * LP, o, (double)are, (double)aim, true);
-    }
-}
-
-// M2L at L2 over all non-adjacent L2 boxes of the replica (src/computeLjk2.f90:17-72);
-// 120 threads: 15 outputs x 8 source groups, reduced in a fixed order
-__global__ void k_m2l_l2(Dev d, int d2) {
-    const int b = blockIdx.x;
-    const Rep r = d.rep[d.b2rep[b]];
-    const int *n = r.nr;
-    int l = b - r.l2_0;
-    int t[3] = {l % n[0], (l / n[0]) % n[1], l / (n[0] * n[1])};
-    int o = threadIdx.x % LPH, g = threadIdx.x / LPH;
-    double re = 0.0, im = 0.0;
-    int w = 2 * d2 + 1, k = 0;
-    for (int sz = 0; sz < n[2]; sz++)
-        for (int sy = 0; sy < n[1]; sy++)
-            for (int sx = 0; sx < n[0]; sx++) {
-                int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
-                if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-                if ((k++ & 7) != g) continue;
-                int oi = (dx + d2) + w * ((dy + d2) + w * (dz + d2));
-                apply_op(d.op_m2l2 + ((size_t)oi * LPH + o) * LP, d.O2 + (size_t)(r.l2_0 + sx + n[0] * (sy + n[1] * sz)) * LP, re, im);
-            }
-    __shared__ double sre[8][LPH], sim[8][LPH];
-    sre[g][o] = re; sim[g][o] = im;
+    sre[threadIdx.x] = re;
+    sim[threadIdx.x] = im;
     __syncthreads();
-    if (g == 0) {
-        double a = 0.0, c = 0.0;
-        for (int q = 0; q < 8; q++) { a += sre[q][o]; c += sim[q][o]; }
-        store_jk(d.L2 + (size_t)b * LP, o, a, c, false);
+    if (g == 0 && act) {
+        R a = 0, b = 0;
+        for (int q = 0; q < NG; q++) { a += sre[q * 128 + u]; b += sim[q * 128 + u]; }
+        const int child = base + gc[0] + n[0] * (gc[1] + n[1] * gc[2]);
+        store_jk(L + (size_t)child * LP, o, (double)a, (double)b, true);
     }
 }
 
 template <typename R>
-size_t m2l_smem() { return sizeof(C2<R>) * (216 * LP + M2L_NB * LPH * LP); }
+size_t m2l_smem() { return sizeof(C2<R>) * 216 * LP + sizeof(R) * (LPH * LP + 2 * M2LCfg<R>::NG * 128); }
+
+// M2L at L2 over all non-adjacent L2 boxes of the replica (src/computeLjk2.f90:17-72):
+// one CTA per target box, 15 outputs x 8 source groups, reduced in a fixed order
+template <typename R>
+__global__ void __launch_bounds__(128) k_m2l_all(Dev d, const C2<R> *Htab, const R *cf, int d2) {
+    __shared__ R scf[LPH * LP];
+    __shared__ R sre[8][LPH], sim[8][LPH];
+    const int b = blockIdx.x;
+    const Rep r = d.rep[d.b2rep[b]];
+    const int *n = r.nr;
+    const int l = b - r.l2_0;
+    const int t[3] = {l % n[0], (l / n[0]) % n[1], l / (n[0] * n[1])};
+    for (int idx = threadIdx.x; idx < LPH * LP; idx += blockDim.x) scf[idx] = cf[idx];
+    __syncthreads();
+    const int o = threadIdx.x % LPH, g = threadIdx.x / LPH;
+    const bool act = threadIdx.x < 8 * LPH;
+    R re = 0, im = 0;
+    if (act) {
+        int h[LP];
+        R cr[LP], ci[LP];
+        m2l_terms<R>(o, scf, h, cr, ci);
+        const int w = 2 * d2 + 1;
+        int k = 0;
+        for (int sz = 0; sz < n[2]; sz++)
+            for (int sy = 0; sy < n[1]; sy++)
+                for (int sx = 0; sx < n[0]; sx++) {
+                    const int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
+                    if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+                    if ((k++ & 7) != g) continue;
+                    const int oi = (dx + d2) + w * ((dy + d2) + w * (dz + d2));
+                    m2l_acc<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + sx + n[0] * (sy + n[1] * sz)) * LP, h,
+                               cr, ci, re, im);
+                }
+    }
+    if (act) { sre[g][o] = re; sim[g][o] = im; }
+    __syncthreads();
+    if (g == 0 && act) {
+        R a = 0, c = 0;
+        for (int q = 0; q < 8; q++) { a += sre[q][o]; c += sim[q][o]; }
+        store_jk(d.L2 + (size_t)b * LP, o, (double)a, (double)c, false);
+    }
+}
 
 // opt-in shared-memory sizes; called once per context creation (the
 // attribute is per device, so every context sets it for its own device)
@@ -788,24 +852,30 @@ void init_force_kernels() {
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_near<true>, NEAR_THREADS, 0);
     g_near_grid[0] = nsm * (nb0 > 0 ? nb0 : 1);
     g_near_grid[1] = nsm * (nb1 > 0 ? nb1 : 1);
-    cudaFuncSetAttribute(k_m2l_grp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<double>());
-    cudaFuncSetAttribute(k_m2l_grp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<float>());
+    cudaFuncSetAttribute(k_m2l_win<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<double>());
+    cudaFuncSetAttribute(k_m2l_win<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<float>());
 }
 
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {
     k_p2m<<<ncell, 64, 0, st>>>(d);
     k_m2m<<<n3, 32, 0, st>>>(d, d.O4, d.O3, d.op_m2m43, d.b3rep, 3);
     k_m2m<<<n2, 32, 0, st>>>(d, d.O3, d.O2, d.op_m2m32, d.b2rep, 2);
-    k_m2l_l2<<<n2, 8 * LPH, 0, st>>>(d, d2);
-    k_l2l<<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
     if (mixed) {
-        k_m2l_grp<float><<<n2, 128, m2l_smem<float>(), st>>>(d, d.O3, d.L3, (const C2<float> *)d.op32_m2l3, d.b2rep, 3);
+        k_m2l_all<float><<<n2, 128, 0, st>>>(d, (const C2<float> *)d.h32_m2l2, d.m2l_cf32, d2);
+        k_l2l<<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
+        k_m2l_win<float><<<n2, 128 * M2LCfg<float>::NG, m2l_smem<float>(), st>>>(
+            d, d.O3, d.L3, (const C2<float> *)d.h32_m2l3, d.m2l_cf32, d.b2rep, 3);
         k_l2l<<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
-        k_m2l_grp<float><<<n3, 128, m2l_smem<float>(), st>>>(d, d.O4, d.L4, (const C2<float> *)d.op32_m2l4, d.b3rep, 4);
+        k_m2l_win<float><<<n3, 128 * M2LCfg<float>::NG, m2l_smem<float>(), st>>>(
+            d, d.O4, d.L4, (const C2<float> *)d.h32_m2l4, d.m2l_cf32, d.b3rep, 4);
     } else {
-        k_m2l_grp<double><<<n2, 128, m2l_smem<double>(), st>>>(d, d.O3, d.L3, (const C2<double> *)d.op_m2l3, d.b2rep, 3);
+        k_m2l_all<double><<<n2, 128, 0, st>>>(d, (const C2<double> *)d.h_m2l2, d.m2l_cf, d2);
+        k_l2l<<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
+        k_m2l_win<double><<<n2, 128 * M2LCfg<double>::NG, m2l_smem<double>(), st>>>(
+            d, d.O3, d.L3, (const C2<double> *)d.h_m2l3, d.m2l_cf, d.b2rep, 3);
         k_l2l<<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
-        k_m2l_grp<double><<<n3, 128, m2l_smem<double>(), st>>>(d, d.O4, d.L4, (const C2<double> *)d.op_m2l4, d.b3rep, 4);
+        k_m2l_win<double><<<n3, 128 * M2LCfg<double>::NG, m2l_smem<double>(), st>>>(
+            d, d.O4, d.L4, (const C2<double> *)d.h_m2l4, d.m2l_cf, d.b3rep, 4);
     }
 }
 

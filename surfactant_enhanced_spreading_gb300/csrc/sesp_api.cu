@@ -243,18 +243,27 @@ void sph(double x, double y, double z, double &rho, double &al, double &be) {
     be = atan2(y, x);
 }
 
-// M2L operator at source - target vector d, src/computeLjk4.f90:134-158
-void op_m2l(double x, double y, double z, double2 *op) {
+// M2L factors (src/computeLjk4.f90:134-158): the operator entry for output
+// (j,k) and input (n,m) at source - target vector d is
+//   iIkm2(k,m) rAnm(j,k) rAnm(n,m) / (sgn(n) rAnm(j+n,m-k)) * Y(j+n,m-k) / rho^(j+n+1);
+// the first factor is the same for every offset (m2l_coef), the second is
+// H_{j+n}^{m-k} (harm_m2l stores l = 0..8, q = 0..l; H_l^{-q} = conj(H_l^q)).
+void harm_m2l(double x, double y, double z, double2 *h) {
     double rho, al, be;
     sph(x, y, z, rho, al, be);
+    for (int l = 0; l <= 2 * P; l++)
+        for (int q = 0; q <= l; q++) {
+            std::complex<double> c = Ylm(l, q, al, be) / pow(rho, l + 1);
+            h[l * (l + 1) / 2 + q] = make_double2(c.real(), c.imag());
+        }
+}
+void m2l_coef(double *cf) {
     for (int j = 0; j <= P; j++)
         for (int k = 0; k <= j; k++)
             for (int n = 0; n <= P; n++)
-                for (int m = -n; m <= n; m++) {
-                    double rt = iIkm2(k, m) * rAnm(j, k) * rAnm(n, m) / (sgn(n) * rAnm(j + n, m - k) * pow(rho, j + n + 1));
-                    std::complex<double> c = rt * Ylm(j + n, m - k, al, be);
-                    op[oidx(j, k) * LP + cidx(n, m)] = make_double2(c.real(), c.imag());
-                }
+                for (int m = -n; m <= n; m++)
+                    cf[oidx(j, k) * LP + cidx(n, m)] =
+                        iIkm2(k, m) * rAnm(j, k) * rAnm(n, m) / (sgn(n) * rAnm(j + n, m - k));
 }
 // M2M operator at child - parent vector d, src/computeOnm3.f90:207-228
 void op_m2m(double x, double y, double z, double2 *op) {
@@ -587,11 +596,13 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &d.lj_kind, NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)))
         return e;
     int w2 = 2 * d2 + 1;
-    if ((e = dalloc(c, &d.op_m2l4, (size_t)343 * LPH * LP)) || (e = dalloc(c, &d.op_m2l3, (size_t)343 * LPH * LP)) ||
-        (e = dalloc(c, &d.op_m2l2, (size_t)w2 * w2 * w2 * LPH * LP)) || (e = dalloc(c, &d.op_m2m43, (size_t)8 * LPH * LP)) ||
-        (e = dalloc(c, &d.op_m2m32, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_l2l23, (size_t)8 * LPH * LP)) ||
-        (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op32_m2l4, (size_t)343 * LPH * LP)) ||
-        (e = dalloc(c, &d.op32_m2l3, (size_t)343 * LPH * LP)))
+    const size_t nh2 = (size_t)w2 * w2 * w2 * NHARM;
+    if ((e = dalloc(c, &d.h_m2l4, (size_t)343 * NHARM)) || (e = dalloc(c, &d.h_m2l3, (size_t)343 * NHARM)) ||
+        (e = dalloc(c, &d.h_m2l2, nh2)) || (e = dalloc(c, &d.h32_m2l4, (size_t)343 * NHARM)) ||
+        (e = dalloc(c, &d.h32_m2l3, (size_t)343 * NHARM)) || (e = dalloc(c, &d.h32_m2l2, nh2)) ||
+        (e = dalloc(c, &d.m2l_cf, (size_t)LPH * LP)) || (e = dalloc(c, &d.m2l_cf32, (size_t)LPH * LP)) ||
+        (e = dalloc(c, &d.op_m2m43, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_m2m32, (size_t)8 * LPH * LP)) ||
+        (e = dalloc(c, &d.op_l2l23, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)))
         return e;
     // static per-site / per-molecule / per-box data
     std::vector<uint8_t> ptype(N);
@@ -640,33 +651,43 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.gpos, gpos.size())) || (e = dalloc(c, &d.gsite, N)) || (e = dalloc(c, &d.gcount, 1)))
         return e;
     // translation operators
-    std::vector<double2> ops((size_t)343 * LPH * LP, make_double2(0.0, 0.0));
-    auto fill_m2l = [&](double scale, double2 *dst, float2 *dst32) -> int {
-        for (int dz = -3; dz <= 3; dz++)
-            for (int dy = -3; dy <= 3; dy++)
-                for (int dx = -3; dx <= 3; dx++) {
-                    int oi = (dx + 3) + 7 * (dy + 3) + 49 * (dz + 3);
-                    if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-                    op_m2l(dx * scale, dy * scale, dz * scale, &ops[(size_t)oi * LPH * LP]);
-                }
-        CK(cudaMemcpyAsync(dst, ops.data(), ops.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
-        std::vector<float2> o32(ops.size());
-        for (size_t i = 0; i < ops.size(); i++) o32[i] = make_float2((float)ops[i].x, (float)ops[i].y);
-        CK(cudaMemcpyAsync(dst32, o32.data(), o32.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
+    // M2L factors: H per offset at L4 (cell edge rs), L3 (2 rs) and L2 (4 rs), and the coefficients
+    auto put = [&](const std::vector<double2> &h, double2 *dst, float2 *dst32) -> int {
+        std::vector<float2> h32(h.size());
+        for (size_t i = 0; i < h.size(); i++) h32[i] = make_float2((float)h[i].x, (float)h[i].y);
+        CK(cudaMemcpyAsync(dst, h.data(), h.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(dst32, h32.data(), h32.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
         CK(cudaStreamSynchronize(c->st));
         return 0;
     };
-    if ((e = fill_m2l(RS, d.op_m2l4, d.op32_m2l4)) || (e = fill_m2l(2 * RS, d.op_m2l3, d.op32_m2l3))) return e;
+    auto fill_win = [&](double scale, double2 *dst, float2 *dst32) -> int {
+        std::vector<double2> h((size_t)343 * NHARM, make_double2(0.0, 0.0));
+        for (int dz = -3; dz <= 3; dz++)
+            for (int dy = -3; dy <= 3; dy++)
+                for (int dx = -3; dx <= 3; dx++) {
+                    if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+                    const int oi = (dx + 3) + 7 * (dy + 3) + 49 * (dz + 3);
+                    harm_m2l(dx * scale, dy * scale, dz * scale, &h[(size_t)oi * NHARM]);
+                }
+        return put(h, dst, dst32);
+    };
+    if ((e = fill_win(RS, d.h_m2l4, d.h32_m2l4)) || (e = fill_win(2 * RS, d.h_m2l3, d.h32_m2l3))) return e;
     {
-        std::vector<double2> o2((size_t)w2 * w2 * w2 * LPH * LP, make_double2(0.0, 0.0));
+        std::vector<double2> h(nh2, make_double2(0.0, 0.0));
         for (int dz = -d2; dz <= d2; dz++)
             for (int dy = -d2; dy <= d2; dy++)
                 for (int dx = -d2; dx <= d2; dx++) {
                     if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-                    int oi = (dx + d2) + w2 * ((dy + d2) + w2 * (dz + d2));
-                    op_m2l(dx * 4 * RS, dy * 4 * RS, dz * 4 * RS, &o2[(size_t)oi * LPH * LP]);
+                    const int oi = (dx + d2) + w2 * ((dy + d2) + w2 * (dz + d2));
+                    harm_m2l(dx * 4 * RS, dy * 4 * RS, dz * 4 * RS, &h[(size_t)oi * NHARM]);
                 }
-        CK(cudaMemcpyAsync(d.op_m2l2, o2.data(), o2.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+        if ((e = put(h, d.h_m2l2, d.h32_m2l2))) return e;
+        std::vector<double> cf(LPH * LP);
+        std::vector<float> cf32(LPH * LP);
+        m2l_coef(cf.data());
+        for (int i = 0; i < LPH * LP; i++) cf32[i] = (float)cf[i];
+        CK(cudaMemcpyAsync(d.m2l_cf, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(d.m2l_cf32, cf32.data(), cf32.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
         CK(cudaStreamSynchronize(c->st));
         std::vector<double2> o8((size_t)8 * LPH * LP);
         struct { double2 *dst; double s; int kind; } sets[4] = {

@@ -28,6 +28,7 @@ constexpr int NBOND = 28;
 constexpr int NANGLE = 36;
 constexpr int NDIH = 30;
 constexpr int NSELF = 42;
+constexpr int NHARM = 45;    // M2L factors H_l^q, l = 0..2P, q = 0..l
 constexpr int NM2L = 316;     // 7^3 - 3^3 source offsets at L4 and L3
 
 // reduced-unit constants of src/mybox.cmns:36-44 (xpi is a single-precision
@@ -51,8 +52,7 @@ struct Rep {
     int axis0;        // offset of this replica's cell-centre tables (x, then y, then z)
     int gcol0;        // first bottom-layer column of the carbon lists
     int graphite_on;
-    int m2l2_base;    // first L2 translation operator of this replica
-    int pad;
+    int pad0, pad;
     double rhs[3], rsd[3];
     double pnh1, pnh2;
 };
@@ -109,9 +109,13 @@ struct Dev {
     uint32_t *isub;
     // multipoles / local expansions (double2 = complex)
     double2 *O4, *L4, *O3, *L3, *O2, *L2;
-    double2 *op_m2l4, *op_m2l3, *op_m2l2, *op_m2m43, *op_m2m32, *op_l2l23, *op_l2l34;
-    float2 *op32_m2l4, *op32_m2l3;   // FP32 copies for the mixed path
-    int *m2l2_off;       // per replica: (2nr-1)^3 index map to operators
+    double2 *op_m2m43, *op_m2m32, *op_l2l23, *op_l2l34;
+    // M2L factors: H_l^q of every offset (45 per offset; L4 and L3 7^3 offsets,
+    // L2 (2 d2 + 1)^3) and the offset-independent coefficients (15 x 25)
+    double2 *h_m2l4, *h_m2l3, *h_m2l2;
+    float2 *h32_m2l4, *h32_m2l3, *h32_m2l2;   // FP32 copies for the mixed path
+    double *m2l_cf;
+    float *m2l_cf32;
     // LJ pair table (eps, sg6), NTYPE^2
     double2 *ljt;
     float2 *lj_kind;     // per site kind (sqrt(48 eps), sigma / 2), zero eps for water H
