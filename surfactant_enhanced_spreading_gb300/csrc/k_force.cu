@@ -946,7 +946,9 @@ __global__ void k_graphite_list(Dev d, int nsite) {
 }
 
 // graphite LJ (src/eval_graphite.f90:80-185), one warp per listed site: the
-// lanes split the column's carbons and a fixed shuffle tree sums them
+// lanes split the column's carbons and a fixed shuffle tree sums them.
+// FP32 (mixed path): site and carbons relative to the column centre, so each
+// carbon costs FP32 arithmetic only.
 template <typename R>
 __global__ void k_graphite(Dev d) {
     const int lane = threadIdx.x & 31;
@@ -962,14 +964,30 @@ __global__ void k_graphite(Dev d) {
         double xd = d.x[g], yd = d.y[g], zd = d.z[g];
         R e48 = (R)(48.0 * eps * sg6), s6 = (R)sg6;
         R fx = 0, fy = 0, fz = 0;
-        for (int q = d.gcol_start[col] + lane; q < d.gcol_start[col + 1]; q += 32) {
-            double4 c = d.gpos[q];
-            R xij = (R)(xd - c.x), yij = (R)(yd - c.y), zij = (R)(zd - c.z);
-            R r2 = xij * xij + yij * yij + zij * zij;
-            if (r2 <= rc2) {
-                R rsi = R(1) / r2, r6 = rsi * rsi * rsi;
-                R flj = e48 * r6 * (s6 * r6 - R(0.5)) * rsi;
-                fx += xij * flj; fy += yij * flj; fz += zij * flj;
+        if constexpr (std::is_same<R, float>::value) {
+            const int lc = col - r.gcol0, ix = lc % r.nc[0], iy = lc / r.nc[0];
+            const float xs = (float)(xd - cell_centre(d, r, 0, ix)), ys = (float)(yd - cell_centre(d, r, 1, iy)),
+                        zs = (float)(zd - cell_centre(d, r, 2, 0));
+            for (int q = d.gcol_start[col] + lane; q < d.gcol_start[col + 1]; q += 32) {
+                const float4 c = d.gpos32[q];
+                const float xij = xs - c.x, yij = ys - c.y, zij = zs - c.z;
+                const float r2 = xij * xij + yij * yij + zij * zij;
+                if (r2 <= rc2) {
+                    const float rsi = __fdividef(1.f, r2), r6 = rsi * rsi * rsi;
+                    const float flj = e48 * r6 * (s6 * r6 - 0.5f) * rsi;
+                    fx += xij * flj; fy += yij * flj; fz += zij * flj;
+                }
+            }
+        } else {
+            for (int q = d.gcol_start[col] + lane; q < d.gcol_start[col + 1]; q += 32) {
+                double4 c = d.gpos[q];
+                R xij = (R)(xd - c.x), yij = (R)(yd - c.y), zij = (R)(zd - c.z);
+                R r2 = xij * xij + yij * yij + zij * zij;
+                if (r2 <= rc2) {
+                    R rsi = R(1) / r2, r6 = rsi * rsi * rsi;
+                    R flj = e48 * r6 * (s6 * r6 - R(0.5)) * rsi;
+                    fx += xij * flj; fy += yij * flj; fz += zij * flj;
+                }
             }
         }
         for (int off = 16; off > 0; off >>= 1) {
@@ -996,98 +1014,123 @@ void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStrea
 
 // ------------------------------------------------------------------ surfactant intramolecular
 
-// positions of one surfactant (shared memory in the force kernel)
+// positions of one surfactant (shared memory in the force kernel); the FP32
+// form holds them relative to the molecule's first site
+template <typename R = double>
 struct Pos29 {
-    double x[NSURF], y[NSURF], z[NSURF];
+    R x[NSURF], y[NSURF], z[NSURF];
 };
 
 // one harmonic angle (src/eval_valence.f90:104-145): forces on its 3 sites
-__device__ double angle_term(const Pos29 &m, int i, double f[3][3]) {
+template <typename R>
+__device__ R angle_term(const Pos29<R> &m, int i, R f[3][3]) {
     int a = cT.ai[i], b = cT.aj[i], c = cT.ak[i];
-    double rxji = m.x[a] - m.x[b], ryji = m.y[a] - m.y[b], rzji = m.z[a] - m.z[b];
-    double rxki = m.x[c] - m.x[b], ryki = m.y[c] - m.y[b], rzki = m.z[c] - m.z[b];
-    double dp = rxji * rxki + ryji * ryki + rzji * rzki;
-    double rjin = sqrt(rxji * rxji + ryji * ryji + rzji * rzji);
-    double rkin = sqrt(rxki * rxki + ryki * ryki + rzki * rzki);
-    double th = acos(dp / rjin / rkin);
-    double costh = cos(th);
-    double dth = th - cT.th[i];
-    double r1 = cT.rkth[i] * dth / sin(th);
-    double fjx = rxki / rjin / rkin - costh * rxji / (rjin * rjin);
-    double fjy = ryki / rjin / rkin - costh * ryji / (rjin * rjin);
-    double fjz = rzki / rjin / rkin - costh * rzji / (rjin * rjin);
-    double fkx = rxji / rjin / rkin - costh * rxki / (rkin * rkin);
-    double fky = ryji / rjin / rkin - costh * ryki / (rkin * rkin);
-    double fkz = rzji / rjin / rkin - costh * rzki / (rkin * rkin);
+    R rxji = m.x[a] - m.x[b], ryji = m.y[a] - m.y[b], rzji = m.z[a] - m.z[b];
+    R rxki = m.x[c] - m.x[b], ryki = m.y[c] - m.y[b], rzki = m.z[c] - m.z[b];
+    R dp = rxji * rxki + ryji * ryki + rzji * rzki;
+    R rjin = sqrt(rxji * rxji + ryji * ryji + rzji * rzji);
+    R rkin = sqrt(rxki * rxki + ryki * ryki + rzki * rzki);
+    R th = acos(dp / rjin / rkin);
+    R costh = cos(th);
+    R dth = th - (R)cT.th[i];
+    R r1 = (R)cT.rkth[i] * dth / sin(th);
+    R fjx = rxki / rjin / rkin - costh * rxji / (rjin * rjin);
+    R fjy = ryki / rjin / rkin - costh * ryji / (rjin * rjin);
+    R fjz = rzki / rjin / rkin - costh * rzji / (rjin * rjin);
+    R fkx = rxji / rjin / rkin - costh * rxki / (rkin * rkin);
+    R fky = ryji / rjin / rkin - costh * ryki / (rkin * rkin);
+    R fkz = rzji / rjin / rkin - costh * rzki / (rkin * rkin);
     f[0][0] = r1 * fjx; f[0][1] = r1 * fjy; f[0][2] = r1 * fjz;
     f[1][0] = -r1 * (fjx + fkx); f[1][1] = -r1 * (fjy + fky); f[1][2] = -r1 * (fjz + fkz);
     f[2][0] = r1 * fkx; f[2][1] = r1 * fky; f[2][2] = r1 * fkz;
-    return 0.5 * cT.rkth[i] * dth * dth;
+    return R(0.5) * (R)cT.rkth[i] * dth * dth;
 }
 
 // one dihedral: r1 = -dU/dcos(phi) applied with the cross-product algebra of
 // src/eval_dihedral.f90:116-271 (triple cosine, dihedrals 1-18) or
 // src/eval_dihedral_berendsen.f90 (cos 3 phi, dihedrals 19-30)
-__device__ double dihedral_term(const Pos29 &m, int i, double f[4][3]) {
+// FP32: with c = cos(phi) the ratios are the exact identities
+// sin(2 phi) / sin(phi) = 2c and sin(3 phi) / sin(phi) = 4c^2 - 1, which need
+// neither acos nor a division by sin(phi) (the FP64 form follows the reference).
+template <typename R>
+__device__ R dihedral_term(const Pos29<R> &m, int i, R f[4][3]) {
     const bool berendsen = i >= 18;
-    const double clampv = berendsen ? 0.999999 : 0.99999999999;
     int iv = cT.di[i], jv = cT.dj[i], kv = cT.dk[i], lv = cT.dl[i];
-    double ax = m.x[jv] - m.x[iv], ay = m.y[jv] - m.y[iv], az = m.z[jv] - m.z[iv];   // r_ji
-    double bx = m.x[kv] - m.x[jv], by = m.y[kv] - m.y[jv], bz = m.z[kv] - m.z[jv];   // r_kj
-    double cx = m.x[lv] - m.x[kv], cy = m.y[lv] - m.y[kv], cz = m.z[lv] - m.z[kv];   // r_nk
-    double u1 = ax * by - ay * bx, u2 = ax * bz - az * bx, u3 = ay * bz - az * by;
-    double v1 = bx * cy - by * cx, v2 = bx * cz - bz * cx, v3 = by * cz - bz * cy;
-    double nu = sqrt(u1 * u1 + u2 * u2 + u3 * u3), nv = sqrt(v1 * v1 + v2 * v2 + v3 * v3);
-    double arg = (u1 * v1 + u2 * v2 + u3 * v3) / nu / nv;
-    if (arg <= -1.0) arg = -clampv;
-    if (arg >= 1.0) arg = clampv;
-    double th = acos(arg), costh = cos(th), sinth = sin(th);
-    double r1, e;
-    if (berendsen) {
-        r1 = -3.0 * cT.dva[i] * sin(3.0 * th) / sinth;
-        e = cT.dva[i] * (1.0 + cos(3.0 * th));
+    R ax = m.x[jv] - m.x[iv], ay = m.y[jv] - m.y[iv], az = m.z[jv] - m.z[iv];   // r_ji
+    R bx = m.x[kv] - m.x[jv], by = m.y[kv] - m.y[jv], bz = m.z[kv] - m.z[jv];   // r_kj
+    R cx = m.x[lv] - m.x[kv], cy = m.y[lv] - m.y[kv], cz = m.z[lv] - m.z[kv];   // r_nk
+    R u1 = ax * by - ay * bx, u2 = ax * bz - az * bx, u3 = ay * bz - az * by;
+    R v1 = bx * cy - by * cx, v2 = bx * cz - bz * cx, v3 = by * cz - bz * cy;
+    R nu = sqrt(u1 * u1 + u2 * u2 + u3 * u3), nv = sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+    R arg = (u1 * v1 + u2 * v2 + u3 * v3) / nu / nv;
+    R r1, e, costh;
+    const R dva = (R)cT.dva[i], dvb = (R)cT.dvb[i], dvc = (R)cT.dvc[i];
+    if constexpr (std::is_same<R, double>::value) {
+        const double clampv = berendsen ? 0.999999 : 0.99999999999;
+        if (arg <= -1.0) arg = -clampv;
+        if (arg >= 1.0) arg = clampv;
+        double th = acos(arg), sinth = sin(th);
+        costh = cos(th);
+        if (berendsen) {
+            r1 = -3.0 * dva * sin(3.0 * th) / sinth;
+            e = dva * (1.0 + cos(3.0 * th));
+        } else {
+            r1 = -dva + 2.0 * dvb * sin(2.0 * th) / sinth - 3.0 * dvc * sin(3.0 * th) / sinth;
+            e = dva * (1.0 + cos(th)) + dvb * (1.0 - cos(2.0 * th)) + dvc * (1.0 + cos(3.0 * th));
+        }
     } else {
-        r1 = -cT.dva[i] + 2.0 * cT.dvb[i] * sin(2.0 * th) / sinth - 3.0 * cT.dvc[i] * sin(3.0 * th) / sinth;
-        e = cT.dva[i] * (1.0 + cos(th)) + cT.dvb[i] * (1.0 - cos(2.0 * th)) + cT.dvc[i] * (1.0 + cos(3.0 * th));
+        const R clampv = berendsen ? R(0.999999) : R(1);
+        if (arg <= R(-1)) arg = -clampv;
+        if (arg >= R(1)) arg = clampv;
+        const R c = arg, c2 = c * c;
+        costh = c;
+        const R s3 = R(4) * c2 - R(1), c3 = (R(4) * c2 - R(3)) * c;
+        if (berendsen) {
+            r1 = R(-3) * dva * s3;
+            e = dva * (R(1) + c3);
+        } else {
+            r1 = -dva + R(4) * dvb * c - R(3) * dvc * s3;
+            e = dva * (R(1) + c) + dvb * (R(2) - R(2) * c2) + dvc * (R(1) + c3);
+        }
     }
-    double nuv = nu * nv, nu2 = nu * nu, nv2 = nv * nv;
-    double fix = (bx * (-by * cy - bz * cz) + cx * (by * by + bz * bz)) / nuv;
-    double fiy = (by * (-bx * cx - bz * cz) + cy * (bx * bx + bz * bz)) / nuv;
-    double fiz = (bz * (-bx * cx - by * cy) + cz * (bx * bx + by * by)) / nuv;
-    double gix = (2.0 * ax * (-by * by - bz * bz) + 2.0 * bx * (ay * by + az * bz)) / nu2;
-    double giy = (2.0 * ay * (-bx * bx - bz * bz) + 2.0 * by * (ax * bx + az * bz)) / nu2;
-    double giz = (2.0 * az * (-bx * bx - by * by) + 2.0 * bz * (ax * bx + ay * by)) / nu2;
-    double fjx = (ax * (-by * cy - bz * cz) + bx * (by * cy + bz * cz) + cx * (-ay * by - az * bz - by * by - bz * bz) +
-                  2.0 * bx * (ay * cy + az * cz)) / nuv;
-    double fjy = (ay * (-bx * cx - bz * cz) + by * (bx * cx + bz * cz) + cy * (-ax * bx - az * bz - bx * bx - bz * bz) +
-                  2.0 * by * (ax * cx + az * cz)) / nuv;
-    double fjz = (az * (-bx * cx - by * cy) + bz * (bx * cx + by * cy) + cz * (-ax * bx - ay * by - bx * bx - by * by) +
-                  2.0 * bz * (ax * cx + ay * cy)) / nuv;
-    double gjx = (2.0 * ax * (by * by + bz * bz + ay * by + az * bz) + 2.0 * bx * (-ay * ay - az * az - ay * by - az * bz)) / nu2 +
-                 (2.0 * cx * (by * cy + bz * cz) + 2.0 * bx * (-cy * cy - cz * cz)) / nv2;
-    double gjy = (2.0 * ay * (bx * bx + bz * bz + ax * bx + az * bz) + 2.0 * by * (-ax * ax - az * az - ax * bx - az * bz)) / nu2 +
-                 (2.0 * cy * (bx * cx + bz * cz) + 2.0 * by * (-cx * cx - cz * cz)) / nv2;
-    double gjz = (2.0 * az * (bx * bx + by * by + ax * bx + ay * by) + 2.0 * bz * (-ax * ax - ay * ay - ax * bx - ay * by)) / nu2 +
-                 (2.0 * cz * (bx * cx + by * cy) + 2.0 * bz * (-cx * cx - cy * cy)) / nv2;
-    double fkx = (ax * (by * by + bz * bz + by * cy + bz * cz) + bx * (-ay * by - az * bz) + cx * (ay * by + az * bz) +
-                  2.0 * bx * (-ay * cy - az * cz)) / nuv;
-    double fky = (ay * (bx * bx + bz * bz + bx * cx + bz * cz) + by * (-ax * bx - az * bz) + cy * (ax * bx + az * bz) +
-                  2.0 * by * (-ax * cx - az * cz)) / nuv;
-    double fkz = (az * (bx * bx + by * by + bx * cx + by * cy) + bz * (-ax * bx - ay * by) + cz * (ax * bx + ay * by) +
-                  2.0 * bz * (-ax * cx - ay * cy)) / nuv;
-    double gkx = (2.0 * ax * (-ay * by - az * bz) + 2.0 * bx * (ay * ay + az * az)) / nu2 +
-                 (2.0 * cx * (-by * by - bz * bz - by * cy - bz * cz) + 2.0 * bx * (cy * cy + cz * cz + by * cy + bz * cz)) / nv2;
-    double gky = (2.0 * ay * (-ax * bx - az * bz) + 2.0 * by * (ax * ax + az * az)) / nu2 +
-                 (2.0 * cy * (-bx * bx - bz * bz - bx * cx - bz * cz) + 2.0 * by * (cx * cx + cz * cz + bx * cx + bz * cz)) / nv2;
-    double gkz = (2.0 * az * (-ax * bx - ay * by) + 2.0 * bz * (ax * ax + ay * ay)) / nu2 +
-                 (2.0 * cz * (-bx * bx - by * by - bx * cx - by * cy) + 2.0 * bz * (cx * cx + cy * cy + bx * cx + by * cy)) / nv2;
-    double fnx = (ax * (-by * by - bz * bz) + bx * (ay * by + az * bz)) / nuv;
-    double fny = (ay * (-bx * bx - bz * bz) + by * (ax * bx + az * bz)) / nuv;
-    double fnz = (az * (-bx * bx - by * by) + bz * (ax * bx + ay * by)) / nuv;
-    double gnx = (2.0 * cx * (by * by + bz * bz) + 2.0 * bx * (-by * cy - bz * cz)) / nv2;
-    double gny = (2.0 * cy * (bx * bx + bz * bz) + 2.0 * by * (-bx * cx - bz * cz)) / nv2;
-    double gnz = (2.0 * cz * (bx * bx + by * by) + 2.0 * bz * (-bx * cx - by * cy)) / nv2;
-    double h = 0.5 * costh;
+    R nuv = nu * nv, nu2 = nu * nu, nv2 = nv * nv;
+    R fix = (bx * (-by * cy - bz * cz) + cx * (by * by + bz * bz)) / nuv;
+    R fiy = (by * (-bx * cx - bz * cz) + cy * (bx * bx + bz * bz)) / nuv;
+    R fiz = (bz * (-bx * cx - by * cy) + cz * (bx * bx + by * by)) / nuv;
+    R gix = (R(2) * ax * (-by * by - bz * bz) + R(2) * bx * (ay * by + az * bz)) / nu2;
+    R giy = (R(2) * ay * (-bx * bx - bz * bz) + R(2) * by * (ax * bx + az * bz)) / nu2;
+    R giz = (R(2) * az * (-bx * bx - by * by) + R(2) * bz * (ax * bx + ay * by)) / nu2;
+    R fjx = (ax * (-by * cy - bz * cz) + bx * (by * cy + bz * cz) + cx * (-ay * by - az * bz - by * by - bz * bz) +
+                  R(2) * bx * (ay * cy + az * cz)) / nuv;
+    R fjy = (ay * (-bx * cx - bz * cz) + by * (bx * cx + bz * cz) + cy * (-ax * bx - az * bz - bx * bx - bz * bz) +
+                  R(2) * by * (ax * cx + az * cz)) / nuv;
+    R fjz = (az * (-bx * cx - by * cy) + bz * (bx * cx + by * cy) + cz * (-ax * bx - ay * by - bx * bx - by * by) +
+                  R(2) * bz * (ax * cx + ay * cy)) / nuv;
+    R gjx = (R(2) * ax * (by * by + bz * bz + ay * by + az * bz) + R(2) * bx * (-ay * ay - az * az - ay * by - az * bz)) / nu2 +
+                 (R(2) * cx * (by * cy + bz * cz) + R(2) * bx * (-cy * cy - cz * cz)) / nv2;
+    R gjy = (R(2) * ay * (bx * bx + bz * bz + ax * bx + az * bz) + R(2) * by * (-ax * ax - az * az - ax * bx - az * bz)) / nu2 +
+                 (R(2) * cy * (bx * cx + bz * cz) + R(2) * by * (-cx * cx - cz * cz)) / nv2;
+    R gjz = (R(2) * az * (bx * bx + by * by + ax * bx + ay * by) + R(2) * bz * (-ax * ax - ay * ay - ax * bx - ay * by)) / nu2 +
+                 (R(2) * cz * (bx * cx + by * cy) + R(2) * bz * (-cx * cx - cy * cy)) / nv2;
+    R fkx = (ax * (by * by + bz * bz + by * cy + bz * cz) + bx * (-ay * by - az * bz) + cx * (ay * by + az * bz) +
+                  R(2) * bx * (-ay * cy - az * cz)) / nuv;
+    R fky = (ay * (bx * bx + bz * bz + bx * cx + bz * cz) + by * (-ax * bx - az * bz) + cy * (ax * bx + az * bz) +
+                  R(2) * by * (-ax * cx - az * cz)) / nuv;
+    R fkz = (az * (bx * bx + by * by + bx * cx + by * cy) + bz * (-ax * bx - ay * by) + cz * (ax * bx + ay * by) +
+                  R(2) * bz * (-ax * cx - ay * cy)) / nuv;
+    R gkx = (R(2) * ax * (-ay * by - az * bz) + R(2) * bx * (ay * ay + az * az)) / nu2 +
+                 (R(2) * cx * (-by * by - bz * bz - by * cy - bz * cz) + R(2) * bx * (cy * cy + cz * cz + by * cy + bz * cz)) / nv2;
+    R gky = (R(2) * ay * (-ax * bx - az * bz) + R(2) * by * (ax * ax + az * az)) / nu2 +
+                 (R(2) * cy * (-bx * bx - bz * bz - bx * cx - bz * cz) + R(2) * by * (cx * cx + cz * cz + bx * cx + bz * cz)) / nv2;
+    R gkz = (R(2) * az * (-ax * bx - ay * by) + R(2) * bz * (ax * ax + ay * ay)) / nu2 +
+                 (R(2) * cz * (-bx * bx - by * by - bx * cx - by * cy) + R(2) * bz * (cx * cx + cy * cy + bx * cx + by * cy)) / nv2;
+    R fnx = (ax * (-by * by - bz * bz) + bx * (ay * by + az * bz)) / nuv;
+    R fny = (ay * (-bx * bx - bz * bz) + by * (ax * bx + az * bz)) / nuv;
+    R fnz = (az * (-bx * bx - by * by) + bz * (ax * bx + ay * by)) / nuv;
+    R gnx = (R(2) * cx * (by * by + bz * bz) + R(2) * bx * (-by * cy - bz * cz)) / nv2;
+    R gny = (R(2) * cy * (bx * bx + bz * bz) + R(2) * by * (-bx * cx - bz * cz)) / nv2;
+    R gnz = (R(2) * cz * (bx * bx + by * by) + R(2) * bz * (-bx * cx - by * cy)) / nv2;
+    R h = R(0.5) * costh;
     f[0][0] = r1 * (fix - h * gix); f[0][1] = r1 * (fiy - h * giy); f[0][2] = r1 * (fiz - h * giz);
     f[1][0] = r1 * (fjx - h * gjx); f[1][1] = r1 * (fjy - h * gjy); f[1][2] = r1 * (fjz - h * gjz);
     f[2][0] = r1 * (fkx - h * gkx); f[2][1] = r1 * (fky - h * gky); f[2][2] = r1 * (fkz - h * gkz);
@@ -1097,32 +1140,35 @@ __device__ double dihedral_term(const Pos29 &m, int i, double f[4][3]) {
 
 // one intramolecular nonbonded pair, Coulomb + LJ without cutoff
 // (src/eval_surfactant_internal.f90:169-200, 206-242)
-__device__ inline double ipair_term(const Dev &d, const Pos29 &m, int a, int b, double f[2][3]) {
-    double x = m.x[a] - m.x[b], y = m.y[a] - m.y[b], z = m.z[a] - m.z[b];
-    double rsq = x * x + y * y + z * z;
-    double rsi = 1.0 / rsq, ir = sqrt(rsi), r6 = rsi * rsi * rsi;
-    double qq = cT.q[2 + a] * cT.q[2 + b] * XPI;
-    double2 lj = d.ljt[(2 + a) * NTYPE + 2 + b];   // (48 eps sg6, sg6)
-    double ft = qq * ir * rsi + lj.x * r6 * (lj.y * r6 - 0.5) * rsi;
+template <typename R>
+__device__ inline R ipair_term(const Dev &d, const Pos29<R> &m, int a, int b, R f[2][3]) {
+    R x = m.x[a] - m.x[b], y = m.y[a] - m.y[b], z = m.z[a] - m.z[b];
+    R rsq = x * x + y * y + z * z;
+    R rsi = R(1) / rsq, ir = sqrt(rsi), r6 = rsi * rsi * rsi;
+    R qq = (R)(cT.q[2 + a] * cT.q[2 + b] * XPI);
+    const double2 lj = d.ljt[(2 + a) * NTYPE + 2 + b];   // (48 eps sg6, sg6)
+    const R e48 = (R)lj.x, s6 = (R)lj.y;
+    R ft = qq * ir * rsi + e48 * r6 * (s6 * r6 - R(0.5)) * rsi;
     f[0][0] = x * ft; f[0][1] = y * ft; f[0][2] = z * ft;
     f[1][0] = -x * ft; f[1][1] = -y * ft; f[1][2] = -z * ft;
-    return qq * ir + (lj.x / 12.0) * (lj.y * r6 * r6 - r6);
+    return qq * ir + (e48 / R(12)) * (s6 * r6 * r6 - r6);
 }
 
 // the far-field correction of one site (src/eval_subtract_fma.f90:14-53):
 // minus the Coulomb force of its own molecule's sites outside its 27-cell block
-__device__ inline double subtract_site(const Pos29 &m, int j, uint32_t bits, double f[3]) {
-    double e = 0.0;
-    f[0] = f[1] = f[2] = 0.0;
+template <typename R>
+__device__ inline R subtract_site(const Pos29<R> &m, int j, uint32_t bits, R f[3]) {
+    R e = 0;
+    f[0] = f[1] = f[2] = 0;
     while (bits) {
         int k = __ffs(bits) - 1;
         bits &= bits - 1;
-        double x = m.x[j] - m.x[k], y = m.y[j] - m.y[k], z = m.z[j] - m.z[k];
-        double rmn = sqrt(x * x + y * y + z * z);
-        double qq = cT.q[2 + j] * cT.q[2 + k] * XPI;
-        double fel = qq / (rmn * rmn * rmn);
+        R x = m.x[j] - m.x[k], y = m.y[j] - m.y[k], z = m.z[j] - m.z[k];
+        R rmn = sqrt(x * x + y * y + z * z);
+        R qq = (R)(cT.q[2 + j] * cT.q[2 + k] * XPI);
+        R fel = qq / (rmn * rmn * rmn);
         f[0] -= x * fel; f[1] -= y * fel; f[2] -= z * fel;
-        e -= 0.5 * qq / rmn;
+        e -= R(0.5) * qq / rmn;
     }
     return e;
 }
@@ -1148,31 +1194,38 @@ void upload_intra_map(const void *host_map, cudaStream_t st) {
 }
 size_t intra_map_size() { return sizeof(IntraMap); }
 
+template <typename R>
 __global__ void __launch_bounds__(128) k_intra_block(Dev d, const int *smols, int terms) {
-    __shared__ Pos29 m;
-    __shared__ double sf[NSLOT][3];
+    __shared__ Pos29<R> m;
+    __shared__ R sf[NSLOT][3];
     const int t = blockIdx.x;
     const int g0 = d.mfirst[smols[t]];
     if (threadIdx.x < NSURF) {
-        m.x[threadIdx.x] = d.x[g0 + threadIdx.x];
-        m.y[threadIdx.x] = d.y[g0 + threadIdx.x];
-        m.z[threadIdx.x] = d.z[g0 + threadIdx.x];
+        if constexpr (std::is_same<R, double>::value) {
+            m.x[threadIdx.x] = d.x[g0 + threadIdx.x];
+            m.y[threadIdx.x] = d.y[g0 + threadIdx.x];
+            m.z[threadIdx.x] = d.z[g0 + threadIdx.x];
+        } else {
+            m.x[threadIdx.x] = (R)(d.x[g0 + threadIdx.x] - d.x[g0]);
+            m.y[threadIdx.x] = (R)(d.y[g0 + threadIdx.x] - d.y[g0]);
+            m.z[threadIdx.x] = (R)(d.z[g0 + threadIdx.x] - d.z[g0]);
+        }
     }
     __syncthreads();
     for (int w = threadIdx.x; w < NTERM; w += blockDim.x) {
         if (w < NANGLE) {
-            double f[3][3] = {{0}};
-            if (terms & SESP_T_VALENCE) angle_term(m, w, f);
+            R f[3][3] = {{0}};
+            if (terms & SESP_T_VALENCE) angle_term<R>(m, w, f);
             for (int k = 0; k < 3; k++) for (int c = 0; c < 3; c++) sf[w * 3 + k][c] = f[k][c];
         } else if (w < NANGLE + NDIH) {
             int i = w - NANGLE;
-            double f[4][3] = {{0}};
-            if ((i < 18 && (terms & SESP_T_DIHEDRAL)) || (i >= 18 && (terms & SESP_T_BERENDSEN))) dihedral_term(m, i, f);
+            R f[4][3] = {{0}};
+            if ((i < 18 && (terms & SESP_T_DIHEDRAL)) || (i >= 18 && (terms & SESP_T_BERENDSEN))) dihedral_term<R>(m, i, f);
             for (int k = 0; k < 4; k++) for (int c = 0; c < 3; c++) sf[NANGLE * 3 + i * 4 + k][c] = f[k][c];
         } else {
             int q = w - NANGLE - NDIH;
-            double f[2][3] = {{0}};
-            if (terms & SESP_T_INTERNAL) ipair_term(d, m, cMap.pa[q], cMap.pb[q], f);
+            R f[2][3] = {{0}};
+            if (terms & SESP_T_INTERNAL) ipair_term<R>(d, m, cMap.pa[q], cMap.pb[q], f);
             int s0 = NANGLE * 3 + NDIH * 4 + 2 * q;
             for (int k = 0; k < 2; k++) for (int c = 0; c < 3; c++) sf[s0 + k][c] = f[k][c];
         }
@@ -1180,23 +1233,25 @@ __global__ void __launch_bounds__(128) k_intra_block(Dev d, const int *smols, in
     __syncthreads();
     if (threadIdx.x < NSURF) {
         int s = threadIdx.x;
-        double fx = 0.0, fy = 0.0, fz = 0.0;
+        R fx = 0, fy = 0, fz = 0;
         for (int k = cMap.off[s]; k < cMap.off[s + 1]; k++) {
             int sl = cMap.list[k];
             fx += sf[sl][0]; fy += sf[sl][1]; fz += sf[sl][2];
         }
         if (terms & SESP_T_SUBTRACT) {
-            double f[3];
-            subtract_site(m, s, d.isub[(size_t)t * NSURF + s], f);
+            R f[3];
+            subtract_site<R>(m, s, d.isub[(size_t)t * NSURF + s], f);
             fx += f[0]; fy += f[1]; fz += f[2];
         }
-        d.fx[g0 + s] += fx; d.fy[g0 + s] += fy; d.fz[g0 + s] += fz;
+        d.fx[g0 + s] += (double)fx; d.fy[g0 + s] += (double)fy; d.fz[g0 + s] += (double)fz;
     }
 }
 
-void launch_intra(const Dev &d, const int *smols, int ns, int terms, cudaStream_t st) {
-    if (ns && (terms & (SESP_T_VALENCE | SESP_T_DIHEDRAL | SESP_T_BERENDSEN | SESP_T_INTERNAL | SESP_T_SUBTRACT)))
-        k_intra_block<<<ns, 128, 0, st>>>(d, smols, terms);
+void launch_intra(const Dev &d, const int *smols, int ns, int terms, int mixed, cudaStream_t st) {
+    if (ns && (terms & (SESP_T_VALENCE | SESP_T_DIHEDRAL | SESP_T_BERENDSEN | SESP_T_INTERNAL | SESP_T_SUBTRACT))) {
+        if (mixed) k_intra_block<float><<<ns, 128, 0, st>>>(d, smols, terms);
+        else k_intra_block<double><<<ns, 128, 0, st>>>(d, smols, terms);
+    }
 }
 
 // energies of one surfactant's intramolecular terms (diagnostic path)
@@ -1204,14 +1259,14 @@ __global__ void k_intra_energy(Dev d, const int *smols, int ns, double *e_mol) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ns) return;
     int g0 = d.mfirst[smols[t]];
-    Pos29 m;
+    Pos29<double> m;
     for (int i = 0; i < NSURF; i++) { m.x[i] = d.x[g0 + i]; m.y[i] = d.y[g0 + i]; m.z[i] = d.z[g0 + i]; }
     double eb = 0.0, ei = 0.0, es = 0.0;
     double f4[4][3], f3[3][3], f2[2][3], f1[3];
-    for (int i = 0; i < NANGLE; i++) eb += angle_term(m, i, f3);
-    for (int i = 0; i < NDIH; i++) eb += dihedral_term(m, i, f4);
-    for (int q = 0; q < NIPAIR; q++) ei += ipair_term(d, m, cMap.pa[q], cMap.pb[q], f2);
-    for (int j = 0; j < NSURF; j++) es += subtract_site(m, j, d.isub[(size_t)t * NSURF + j], f1);
+    for (int i = 0; i < NANGLE; i++) eb += angle_term<double>(m, i, f3);
+    for (int i = 0; i < NDIH; i++) eb += dihedral_term<double>(m, i, f4);
+    for (int q = 0; q < NIPAIR; q++) ei += ipair_term<double>(d, m, cMap.pa[q], cMap.pb[q], f2);
+    for (int j = 0; j < NSURF; j++) es += subtract_site<double>(m, j, d.isub[(size_t)t * NSURF + j], f1);
     e_mol[3 * t] = eb; e_mol[3 * t + 1] = ei; e_mol[3 * t + 2] = es;
 }
 

@@ -42,7 +42,7 @@ void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st);
 void init_force_kernels();
 void upload_intra_map(const void *host_map, cudaStream_t st);
 size_t intra_map_size();
-void launch_intra(const Dev &d, const int *smols, int ns, int terms, cudaStream_t st);
+void launch_intra(const Dev &d, const int *smols, int ns, int terms, int mixed, cudaStream_t st);
 void launch_count_pairs(const Dev &d, int ncell, unsigned long long *out, cudaStream_t st);
 void launch_flush(void *buf, size_t bytes, cudaStream_t st);
 void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int ns, double *e_slot, double *e_site,

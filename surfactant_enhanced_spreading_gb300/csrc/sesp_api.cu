@@ -418,7 +418,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
     tstop(c, 0);
     tstart(c, 4);
     launch_site_forces(d, c->nsite, terms, mixed, c->st);
-    launch_intra(d, c->smols, c->nsm, terms, c->st);
+    launch_intra(d, c->smols, c->nsm, terms, mixed, c->st);
     tstop(c, 4);
 }
 
@@ -610,6 +610,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     std::vector<double> axis, sx(N), sy(N), sz(N), vxa(N, 0.0), vya(N, 0.0), vza(N, 0.0), eta0(R, 0.0);
     std::vector<int> gstart(1, 0);
     std::vector<double4> gpos;
+    std::vector<float4> gpos32;   // relative to the column's (x, y) centre and the bottom cell layer's z centre
     double rcut = RC + sqrt(2.0) * RS / 2.0;
     rcut *= rcut;
     for (int q = 0; q < R; q++) {
@@ -638,17 +639,20 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:187-216
         for (int iy = 0; iy < r.nc[1]; iy++)
             for (int ix = 0; ix < r.nc[0]; ix++) {
-                double cx = axis[a0 + ix], cy = axis[a0 + r.nc[0] + iy];
+                double cx = axis[a0 + ix], cy = axis[a0 + r.nc[0] + iy], cz = axis[a0 + r.nc[0] + r.nc[1]];
                 for (int k = 0; k < ri.ncarb; k++) {
                     double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
-                    if (dx * dx + dy * dy <= rcut)
+                    if (dx * dx + dy * dy <= rcut) {
                         gpos.push_back(make_double4(ri.carb[3 * k], ri.carb[3 * k + 1], ri.carb[3 * k + 2], 0.0));
+                        gpos32.push_back(make_float4((float)dx, (float)dy, (float)(ri.carb[3 * k + 2] - cz), 0.f));
+                    }
                 }
                 gstart.push_back((int)gpos.size());
             }
     }
     if ((e = dalloc(c, &d.axis, axis.size())) || (e = dalloc(c, &d.gcol_start, gstart.size())) ||
-        (e = dalloc(c, &d.gpos, gpos.size())) || (e = dalloc(c, &d.gsite, N)) || (e = dalloc(c, &d.gcount, 1)))
+        (e = dalloc(c, &d.gpos, gpos.size())) || (e = dalloc(c, &d.gpos32, gpos32.size())) ||
+        (e = dalloc(c, &d.gsite, N)) || (e = dalloc(c, &d.gcount, 1)))
         return e;
     // translation operators
     // M2L factors: H per offset at L4 (cell edge rs), L3 (2 rs) and L2 (4 rs), and the coefficients
@@ -726,6 +730,8 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     CK(cudaMemcpyAsync(d.b2rep, b2.data(), n2 * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.gcol_start, gstart.data(), gstart.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
     if (!gpos.empty()) CK(cudaMemcpyAsync(d.gpos, gpos.data(), gpos.size() * sizeof(double4), cudaMemcpyHostToDevice, c->st));
+    if (!gpos32.empty())
+        CK(cudaMemcpyAsync(d.gpos32, gpos32.data(), gpos32.size() * sizeof(float4), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.ljt, ljt.data(), ljt.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemsetAsync(d.near_ctl, 0, 2 * sizeof(int), c->st));   // no near-field items before the first rebuild
     CK(cudaStreamSynchronize(c->st));

@@ -104,6 +104,7 @@ struct Dev {
     // graphite columns of the bottom layer
     int *gcol_start;
     double4 *gpos;
+    float4 *gpos32;      // the same carbons relative to the column centre (x, y) and the bottom layer's centre (z)
     int *gsite, *gcount;   // sites the graphite acts on (rebuilt with the lists)
     // intramolecular correction lists (bit k: site k+1 of the molecule)
     uint32_t *isub;

@@ -97,7 +97,7 @@ def estimate_bytes(system: S.System) -> int:
     cells = ncell * (4 * 4 + 2 * cz + 4 + 9 * 8) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
     ops = (2 * 343 + w2 ** 3 + 4 * 8) * 15 * 25 * 16 + 2 * 343 * 15 * 25 * 8
     ncarb = system.carbons.reshape(-1, 3).shape[0]
-    graphite = 12 * ncarb * 32 + int(nc[0] * nc[1] + 1) * 4 + int(nc.sum()) * 8 + n * 4
+    graphite = 12 * ncarb * 48 + int(nc[0] * nc[1] + 1) * 4 + int(nc.sum()) * 8 + n * 4
     surf = 29 * system.n_surf * 4
     total = n * per_site + nmol * per_mol + cells + ops + graphite + surf + 4096
     return int(1.1 * total) + (1 << 20)
