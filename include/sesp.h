@@ -47,9 +47,12 @@ extern "C" {
 
 /* precision of the force path */
 #define SESP_PLAIN_FP64 0  /* every force term in FP64                       */
-#define SESP_MIXED 1       /* FP32 pair and local-expansion arithmetic with
-                              compensated per-site accumulation; FP64 for the
-                              constraints, thermostat, positions and sums     */
+#define SESP_MIXED 1       /* FP32 pair, multipole and bonded arithmetic; FP64
+                              for the constraint iterations, thermostat,
+                              kinetic sums, positions and energy sums         */
+#define SESP_MIXED_FP32C 2 /* SESP_MIXED with the constraint iterations in
+                              FP32 (FP64 state and predictors, FP64 decisions
+                              near the tolerance threshold)                   */
 
 /* force terms (bit mask for sesp_force_terms) */
 #define SESP_T_NEAR 1        /* short-range LJ + Coulomb, src/eval[wS]*.f90   */
@@ -69,7 +72,7 @@ typedef struct {
     int n_cells[3];        /* L4 cells per axis, multiples of 4; the reference
                               uses 12 x 12 x 12 (3 x 3 x 3 ranks of 4^3 cells,
                               src/mybox.cmns:55-57, src/init_box_dimensions.f90) */
-    int precision;         /* SESP_PLAIN_FP64 or SESP_MIXED                   */
+    int precision;         /* SESP_PLAIN_FP64, SESP_MIXED or SESP_MIXED_FP32C */
     int rebuild_interval;  /* steps between list / far-field rebuilds; ifar = 10
                               (src/mybox.f90:24)                               */
     int graphite_on;       /* apply src/eval_graphite.f90                     */

@@ -8,7 +8,7 @@ module sesp_mod
   use iso_c_binding
   implicit none
 
-  integer(c_int), parameter :: SESP_PLAIN_FP64 = 0, SESP_MIXED = 1
+  integer(c_int), parameter :: SESP_PLAIN_FP64 = 0, SESP_MIXED = 1, SESP_MIXED_FP32C = 2
   integer(c_int), parameter :: SESP_T_ALL = 511
 
   type, bind(C) :: sesp_params

@@ -6,7 +6,7 @@ shared library next to this file's package:
 * ``k_exact.cu`` with ``-fmad=false``: cell assignment and the FP64
   SHAKE/RATTLE integrator, whose discrete decisions and iteration counts must
   round like the reference's separately rounded Fortran arithmetic;
-* ``k_constraint32.cu``: the mixed path's FP32 constraint sweeps;
+* ``k_constraint.cu``: the mixed paths' constraint sweeps (FP64, or FP32);
 * ``k_force.cu``: pair, multipole and intramolecular kernels;
 * ``sesp_api.cu``: the C ABI (host code compiled without contraction so the
   force-field tables and translation operators are reproducible).
@@ -23,7 +23,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", "-diag-suppress", "1444"]
-UNITS = [("k_exact.cu", ["-fmad=false"]), ("k_constraint32.cu", []), ("k_force.cu", []), ("sesp_api.cu", [])]
+UNITS = [("k_exact.cu", ["-fmad=false"]), ("k_constraint.cu", []), ("k_force.cu", []), ("sesp_api.cu", [])]
 HEADERS = ["sesp_internal.cuh", "k_launch.cuh", os.path.join("..", "..", "include", "sesp.h")]
 
 

@@ -42,7 +42,8 @@ struct Fast32 {
     float dsq_w[3], fa_w[3], fb_w[3];
     float dsq_s[NBOND], fa_s[NBOND], fb_s[NBOND];
     double dsq64_w[3], dsq64_s[NBOND];
-    double mass64[NTYPE], rm64[NTYPE];
+    double fa64_w[3], fa64_s[NBOND], fb64_w[3], fb64_s[NBOND];
+    double mass64[NTYPE], rm64[NTYPE], rmdt64[NTYPE];
 };
 __constant__ Fast32 cF;
 
@@ -62,9 +63,12 @@ struct G32<3> {
     __device__ static constexpr int bi(int b) { return b; }
     __device__ static constexpr int bj(int b) { return b == 2 ? 0 : b + 1; }
     __device__ static constexpr int kind(int i) { return i == 0 ? 0 : 1; }
-    __device__ static float dsq(int b) { return cF.dsq_w[b]; }
-    __device__ static float fa(int b) { return cF.fa_w[b]; }
-    __device__ static float fb(int b) { return cF.fb_w[b]; }
+    template <typename C>
+    __device__ static C dsq(int b) { if constexpr (sizeof(C) == 4) return cF.dsq_w[b]; else return cF.dsq64_w[b]; }
+    template <typename C>
+    __device__ static C fa(int b) { if constexpr (sizeof(C) == 4) return cF.fa_w[b]; else return cF.fa64_w[b]; }
+    template <typename C>
+    __device__ static C fb(int b) { if constexpr (sizeof(C) == 4) return cF.fb_w[b]; else return cF.fb64_w[b]; }
     __device__ static double dsq64(int b) { return cF.dsq64_w[b]; }
 };
 template <>
@@ -73,9 +77,12 @@ struct G32<NSURF> {
     __device__ static constexpr int bi(int b) { return sbi32(b); }
     __device__ static constexpr int bj(int b) { return b + 1; }
     __device__ static constexpr int kind(int i) { return 2 + i; }
-    __device__ static float dsq(int b) { return cF.dsq_s[b]; }
-    __device__ static float fa(int b) { return cF.fa_s[b]; }
-    __device__ static float fb(int b) { return cF.fb_s[b]; }
+    template <typename C>
+    __device__ static C dsq(int b) { if constexpr (sizeof(C) == 4) return cF.dsq_s[b]; else return cF.dsq64_s[b]; }
+    template <typename C>
+    __device__ static C fa(int b) { if constexpr (sizeof(C) == 4) return cF.fa_s[b]; else return cF.fa64_s[b]; }
+    template <typename C>
+    __device__ static C fb(int b) { if constexpr (sizeof(C) == 4) return cF.fb_s[b]; else return cF.fb64_s[b]; }
     __device__ static double dsq64(int b) { return cF.dsq64_s[b]; }
 };
 
@@ -118,76 +125,122 @@ __device__ __noinline__ bool rattle_active64(const Dev &d, int gi, int gj, int k
     return fabs(g) > tol;
 }
 
-constexpr float BAND = 0.02f;   // relative half-width of the FP64 decision band
+constexpr float BAND = 0.02f;   // relative half-width of the FP64 decision band of the FP32 sweeps
 constexpr unsigned FULL = 0xffffffffu;
 
-// One SHAKE bond update.  k = {P.x, P.y, P.z, R.x, R.y, R.z, D0, R.P}.
-template <int NS, int B>
-__device__ __forceinline__ bool shake_step(const Dev &d, int g0, const float (&k)[8], float (&cx)[NS],
-                                           float (&cy)[NS], float (&cz)[NS], float tol2, double tol2d) {
-    using Gr = G32<NS>;
-    constexpr int i = Gr::bi(B), j = Gr::bj(B);
-    const float dx = cx[i] - cx[j], dy = cy[i] - cy[j], dz = cz[i] - cz[j];
-    const float pc = k[0] * dx + k[1] * dy + k[2] * dz;
-    const float cc = dx * dx + dy * dy + dz * dz;
-    const float diffsq = k[6] - (2.f * pc + cc);
-    const float thr = Gr::dsq(B) * tol2;
-    bool act = fabsf(diffsq) > thr;
-    if (fabsf(fabsf(diffsq) - thr) < BAND * thr)
-        act = shake_active64(d, g0 + i, g0 + j, cx[i], cy[i], cz[i], cx[j], cy[j], cz[j], Gr::dsq64(B), tol2d);
+// |x| > t for t > 0: on the IEEE bit patterns for FP64, so the test runs on
+// the integer pipe (GB300's FP64 pipe takes ~19 cycles per warp instruction
+// whatever the active lanes, and 64 cycles of latency)
+__device__ __forceinline__ bool gt_abs(double x, double t) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > __double_as_longlong(t);
+}
+__device__ __forceinline__ bool gt_abs(float x, float t) { return fabsf(x) > t; }
+
+// a / b.  FP32: the hardware estimate.  FP64: the FP32 estimate y of 1/b and
+// one Newton correction of the quotient, q = a y + y (a - b a y), relative
+// error ~2^-46.
+template <typename C>
+__device__ __forceinline__ C quot(C a, C b) {
+    if constexpr (sizeof(C) == 4) {
+        return __fdividef(a, b);
+    } else {
+        const double y = (double)__fdividef(1.f, (float)b);
+        const double q = a * y;
+        return fma(y, fma(-b, q, a), q);
+    }
+}
+
+// Per-bond constants, formed once per call in FP64 and rounded to C.
+// SHAKE: predictor and old bond vectors P and R, the correction directions
+// R / m_i and R / m_j, D0 = d^2 - |P|^2, R.P, the threshold 2 tol d^2 and
+// 2 (1/m_i + 1/m_j).
+template <typename C>
+struct ShakeK {
+    C p[3], r[3], a[3], b[3], d0, rp, thr, fa;
+};
+// RATTLE: bond vector R, the correction directions R dt / m_i and R dt / m_j,
+// R.V of the velocity predictor and (1/dt) / ((1/m_i + 1/m_j) d^2).
+template <typename C>
+struct RattleK {
+    C r[3], a[3], b[3], rv, fb;
+};
+
+template <typename C>
+__device__ inline void shake_make(double rx, double ry, double rz, double px, double py, double pz, double dsq,
+                                  double rmi, double rmj, double tol2, ShakeK<C> &k) {
+    k.p[0] = (C)px; k.p[1] = (C)py; k.p[2] = (C)pz;
+    k.r[0] = (C)rx; k.r[1] = (C)ry; k.r[2] = (C)rz;
+    k.a[0] = (C)(rmi * rx); k.a[1] = (C)(rmi * ry); k.a[2] = (C)(rmi * rz);
+    k.b[0] = (C)(rmj * rx); k.b[1] = (C)(rmj * ry); k.b[2] = (C)(rmj * rz);
+    k.d0 = (C)(dsq - (px * px + py * py + pz * pz));
+    k.rp = (C)(rx * px + ry * py + rz * pz);
+    k.thr = (C)(dsq * tol2);
+    k.fa = (C)(2.0 * (rmi + rmj));
+}
+template <typename C>
+__device__ inline void rattle_make(double rx, double ry, double rz, double wx, double wy, double wz, double dti,
+                                   double dtj, double fb, RattleK<C> &k) {
+    k.r[0] = (C)rx; k.r[1] = (C)ry; k.r[2] = (C)rz;
+    k.a[0] = (C)(dti * rx); k.a[1] = (C)(dti * ry); k.a[2] = (C)(dti * rz);
+    k.b[0] = (C)(dtj * rx); k.b[1] = (C)(dtj * ry); k.b[2] = (C)(dtj * rz);
+    k.rv = (C)(rx * wx + ry * wy + rz * wz);
+    k.fb = (C)fb;
+}
+
+// One SHAKE bond update on the corrections of its two sites; true if the
+// bond was corrected.  The residual is d^2 - |P + c|^2 = (D0 - c.c) - 2 P.c
+// and R.(P + c) = R.P + R.c, c the difference of the sites' corrections, so
+// nothing cancels.  SPEC: form the quotient before the tolerance test (a
+// shorter dependency chain for latency-bound callers).
+template <typename C, bool SPEC>
+__device__ __forceinline__ bool shake_bond(const Dev &d, int gi, int gj, double dsq64, double tol2d, const ShakeK<C> &k,
+                                           C &xi, C &yi, C &zi, C &xj, C &yj, C &zj) {
+    const C dx = xi - xj, dy = yi - yj, dz = zi - zj;
+    const C pc = k.p[0] * dx + k.p[1] * dy + k.p[2] * dz;
+    const C cc = dx * dx + dy * dy + dz * dz;
+    const C rd = k.r[0] * dx + k.r[1] * dy + k.r[2] * dz;
+    const C diffsq = (k.d0 - cc) - C(2) * pc;
+    C gab = C(0);
+    if constexpr (SPEC) gab = quot<C>(diffsq, k.fa * (k.rp + rd));
+    bool act = gt_abs(diffsq, k.thr);
+    if constexpr (sizeof(C) == 4) {
+        if (fabsf(fabsf(diffsq) - k.thr) < BAND * k.thr)
+            act = shake_active64(d, gi, gj, xi, yi, zi, xj, yj, zj, dsq64, tol2d);
+    }
     if (act) {
-        const float rpab = k[7] + (k[3] * dx + k[4] * dy + k[5] * dz);
-        const float gab = __fdividef(diffsq, Gr::fa(B) * rpab);
-        const float ga = cF.rm[Gr::kind(i)] * gab, gb = cF.rm[Gr::kind(j)] * gab;
-        cx[i] += k[3] * ga; cy[i] += k[4] * ga; cz[i] += k[5] * ga;
-        cx[j] -= k[3] * gb; cy[j] -= k[4] * gb; cz[j] -= k[5] * gb;
+        if constexpr (!SPEC) gab = quot<C>(diffsq, k.fa * (k.rp + rd));
+        xi += k.a[0] * gab; yi += k.a[1] * gab; zi += k.a[2] * gab;
+        xj -= k.b[0] * gab; yj -= k.b[1] * gab; zj -= k.b[2] * gab;
     }
     return act;
 }
 
-// One RATTLE bond update.  k = {R.x, R.y, R.z, R.V}.
-template <int NS, int B>
-__device__ __forceinline__ bool rattle_step(const Dev &d, int g0, const float (&k)[4], float (&cx)[NS],
-                                            float (&cy)[NS], float (&cz)[NS], float tol, double told) {
-    using Gr = G32<NS>;
-    constexpr int i = Gr::bi(B), j = Gr::bj(B);
-    const float dx = cx[i] - cx[j], dy = cy[i] - cy[j], dz = cz[i] - cz[j];
-    const float gab = -(k[3] + (k[0] * dx + k[1] * dy + k[2] * dz)) * Gr::fb(B);
-    bool act = fabsf(gab) > tol;
-    if (fabsf(fabsf(gab) - tol) < BAND * tol)
-        act = rattle_active64(d, g0 + i, g0 + j, Gr::kind(i), Gr::kind(j), cx[i], cy[i], cz[i], cx[j], cy[j], cz[j],
-                              Gr::dsq64(B), told);
+// One RATTLE bond update: g = -R.(V + c) (1/dt) / ((1/m_i + 1/m_j) d^2).
+template <typename C>
+__device__ __forceinline__ bool rattle_bond(const Dev &d, int gi, int gj, int ki, int kj, double dsq64, double told,
+                                            C tolc, const RattleK<C> &k, C &xi, C &yi, C &zi, C &xj, C &yj, C &zj) {
+    const C dx = xi - xj, dy = yi - yj, dz = zi - zj;
+    const C gab = -(k.rv + (k.r[0] * dx + k.r[1] * dy + k.r[2] * dz)) * k.fb;
+    bool act = gt_abs(gab, tolc);
+    if constexpr (sizeof(C) == 4) {
+        if (fabsf(fabsf(gab) - tolc) < BAND * tolc)
+            act = rattle_active64(d, gi, gj, ki, kj, xi, yi, zi, xj, yj, zj, dsq64, told);
+    }
     if (act) {
-        const float ga = cF.rmdt[Gr::kind(i)] * gab, gb = cF.rmdt[Gr::kind(j)] * gab;
-        cx[i] += k[0] * ga; cy[i] += k[1] * ga; cz[i] += k[2] * ga;
-        cx[j] -= k[0] * gb; cy[j] -= k[1] * gb; cz[j] -= k[2] * gb;
+        xi += k.a[0] * gab; yi += k.a[1] * gab; zi += k.a[2] * gab;
+        xj -= k.b[0] * gab; yj -= k.b[1] * gab; zj -= k.b[2] * gab;
     }
     return act;
-}
-
-// SHAKE constants of one bond from FP64 old positions r and predictors p
-__device__ inline void shake_consts(double rxi, double ryi, double rzi, double rxj, double ryj, double rzj, double pxi,
-                                    double pyi, double pzi, double pxj, double pyj, double pzj, double dsq,
-                                    float (&k)[8]) {
-    const double rx = rxi - rxj, ry = ryi - ryj, rz = rzi - rzj;
-    const double px = pxi - pxj, py = pyi - pyj, pz = pzi - pzj;
-    k[0] = (float)px; k[1] = (float)py; k[2] = (float)pz;
-    k[3] = (float)rx; k[4] = (float)ry; k[5] = (float)rz;
-    k[6] = (float)(dsq - (px * px + py * py + pz * pz));
-    k[7] = (float)(rx * px + ry * py + rz * pz);
-}
-
-// static-index unrolling helper: f(integral_constant<B>) for B = 0..N-1
-template <int B, int N, typename F>
-__device__ __forceinline__ void unroll(F &&f) {
-    if constexpr (B < N) {
-        f(std::integral_constant<int, B>{});
-        unroll<B + 1, N>(f);
-    }
 }
 
 // ---------------------------------------------------------------- waters
 
+// bonds (0,1), (1,2), (2,0); kinds 0 (O), 1 (H)
+__device__ constexpr int wbi(int b) { return b; }
+__device__ constexpr int wbj(int b) { return b == 2 ? 0 : b + 1; }
+__device__ constexpr int wkind(int i) { return i == 0 ? 0 : 1; }
+
+template <typename C>
 __global__ void __launch_bounds__(128) k_move_a32w(Dev d, const int *mols, int nm, double tol, int maxit) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nm) return;
@@ -201,7 +254,7 @@ __global__ void __launch_bounds__(128) k_move_a32w(Dev d, const int *mols, int n
         const int g = g0 + i;
         double vx = d.vx[g], vy = d.vy[g], vz = d.vz[g], ax = d.ax[g], ay = d.ay[g], az = d.az[g];
         rx[i] = d.x[g]; ry[i] = d.y[g]; rz[i] = d.z[g];
-        ke0 = __dadd_rn(ke0, __dmul_rn(cF.mass64[G32<3>::kind(i)],
+        ke0 = __dadd_rn(ke0, __dmul_rn(cF.mass64[wkind(i)],
                                        __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
         px[i] = pred_a(rx[i], vx, ax, escale);
         py[i] = pred_a(ry[i], vy, ay, escale);
@@ -211,23 +264,26 @@ __global__ void __launch_bounds__(128) k_move_a32w(Dev d, const int *mols, int n
         d.vy[g] = vel_a(vy, ay, escale);
         d.vz[g] = vel_a(vz, az, escale);
     }
-    float k[3][8];
+    const double tol2d = 2.0 * tol;
+    ShakeK<C> k[3];
 #pragma unroll
     for (int b = 0; b < 3; b++) {
-        const int i = G32<3>::bi(b), j = G32<3>::bj(b);
-        shake_consts(rx[i], ry[i], rz[i], rx[j], ry[j], rz[j], px[i], py[i], pz[i], px[j], py[j], pz[j],
-                     G32<3>::dsq64(b), k[b]);
+        const int i = wbi(b), j = wbj(b);
+        shake_make<C>(rx[i] - rx[j], ry[i] - ry[j], rz[i] - rz[j], px[i] - px[j], py[i] - py[j], pz[i] - pz[j],
+                      cF.dsq64_w[b], cF.rm64[wkind(i)], cF.rm64[wkind(j)], tol2d, k[b]);
     }
-    float cx[3] = {0.f, 0.f, 0.f}, cy[3] = {0.f, 0.f, 0.f}, cz[3] = {0.f, 0.f, 0.f};
-    const float tol2 = (float)(2.0 * tol);
-    const double tol2d = 2.0 * tol;
+    C cx[3] = {0, 0, 0}, cy[3] = {0, 0, 0}, cz[3] = {0, 0, 0};
     int it = 0;
     bool ldone = false;
     while (!ldone && it <= maxit) {
         ldone = true;
-        unroll<0, 3>([&](auto B) {
-            if (shake_step<3, decltype(B)::value>(d, g0, k[B], cx, cy, cz, tol2, tol2d)) ldone = false;
-        });
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const int i = wbi(b), j = wbj(b);
+            if (shake_bond<C, false>(d, g0 + i, g0 + j, cF.dsq64_w[b], tol2d, k[b], cx[i], cy[i], cz[i], cx[j], cy[j],
+                                     cz[j]))
+                ldone = false;
+        }
         it++;
     }
     double ke1 = 0.0;
@@ -240,7 +296,7 @@ __global__ void __launch_bounds__(128) k_move_a32w(Dev d, const int *mols, int n
         double vx = __dadd_rn(d.vx[g], (double)cx[i]), vy = __dadd_rn(d.vy[g], (double)cy[i]),
                vz = __dadd_rn(d.vz[g], (double)cz[i]);
         d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
-        ke1 = __dadd_rn(ke1, __dmul_rn(cF.mass64[G32<3>::kind(i)],
+        ke1 = __dadd_rn(ke1, __dmul_rn(cF.mass64[wkind(i)],
                                        __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
     }
     d.ke[2 * m] = ke0;
@@ -248,6 +304,7 @@ __global__ void __launch_bounds__(128) k_move_a32w(Dev d, const int *mols, int n
     if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
 }
 
+template <typename C>
 __global__ void __launch_bounds__(128) k_move_b32w(Dev d, const int *mols, int nm, double tol, int maxit) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= nm) return;
@@ -258,7 +315,7 @@ __global__ void __launch_bounds__(128) k_move_b32w(Dev d, const int *mols, int n
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const int g = g0 + i;
-        const double mi = cF.mass64[G32<3>::kind(i)];
+        const double mi = cF.mass64[wkind(i)];
         double ax = __ddiv_rn(__dmul_rn(d.fx[g], DTSQ2), mi), ay = __ddiv_rn(__dmul_rn(d.fy[g], DTSQ2), mi),
                az = __ddiv_rn(__dmul_rn(d.fz[g], DTSQ2), mi);
         d.ax[g] = ax; d.ay[g] = ay; d.az[g] = az;
@@ -268,23 +325,26 @@ __global__ void __launch_bounds__(128) k_move_b32w(Dev d, const int *mols, int n
         d.vx[g] = vx[i]; d.vy[g] = vy[i]; d.vz[g] = vz[i];
         rx[i] = d.x[g]; ry[i] = d.y[g]; rz[i] = d.z[g];
     }
-    float k[3][4];
+    RattleK<C> k[3];
 #pragma unroll
     for (int b = 0; b < 3; b++) {
-        const int i = G32<3>::bi(b), j = G32<3>::bj(b);
-        const double ex = rx[i] - rx[j], ey = ry[i] - ry[j], ez = rz[i] - rz[j];
-        k[b][0] = (float)ex; k[b][1] = (float)ey; k[b][2] = (float)ez;
-        k[b][3] = (float)(ex * (vx[i] - vx[j]) + ey * (vy[i] - vy[j]) + ez * (vz[i] - vz[j]));
+        const int i = wbi(b), j = wbj(b);
+        rattle_make<C>(rx[i] - rx[j], ry[i] - ry[j], rz[i] - rz[j], vx[i] - vx[j], vy[i] - vy[j], vz[i] - vz[j],
+                       cF.rmdt64[wkind(i)], cF.rmdt64[wkind(j)], cF.fb64_w[b], k[b]);
     }
-    float cx[3] = {0.f, 0.f, 0.f}, cy[3] = {0.f, 0.f, 0.f}, cz[3] = {0.f, 0.f, 0.f};
-    const float tolf = (float)tol;
+    C cx[3] = {0, 0, 0}, cy[3] = {0, 0, 0}, cz[3] = {0, 0, 0};
+    const C tolc = (C)tol;
     int it = 0;
     bool ldone = false;
     while (!ldone && it <= maxit) {
         ldone = true;
-        unroll<0, 3>([&](auto B) {
-            if (rattle_step<3, decltype(B)::value>(d, g0, k[B], cx, cy, cz, tolf, tol)) ldone = false;
-        });
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const int i = wbi(b), j = wbj(b);
+            if (rattle_bond<C>(d, g0 + i, g0 + j, wkind(i), wkind(j), cF.dsq64_w[b], tol, tolc, k[b], cx[i], cy[i],
+                               cz[i], cx[j], cy[j], cz[j]))
+                ldone = false;
+        }
         it++;
     }
 #pragma unroll
@@ -305,10 +365,24 @@ __device__ inline double warp_sum(double v) {
     return v;   // lane 0
 }
 
+// Gauss-Seidel sweeps as a wavefront: sweep k starts WF_LAG bonds after
+// sweep k - 1 and runs on lane k mod WF_LANES, one bond per lane and step.
+// Two bonds that share a site are never more than 7 apart in the bond order
+// (site 17: bonds 16 and 23), so with a lag of 8 every site sees the
+// updates of the sequential order, in that order, and no two lanes touch the
+// same site in one step: the result is that of the sequential sweeps.
+// Sweeps started after the first sweep without a correction make no
+// correction either (they see the same, converged state), so the state at
+// that point is final.  No more than maxit + 1 sweeps run, as in the
+// sequential loop.  One warp per molecule; its 29 lanes do the per-site FP64
+// work and form the bond constants.
+constexpr int WF_LAG = 8;
+constexpr int WF_LANES = 4;   // ceil(NBOND / WF_LAG) sweeps in flight
+
+template <typename C>
 __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm, double tol, int maxit) {
-    __shared__ float sk[NBOND][8];
-    __shared__ float sc[3][NSURF];
-    __shared__ int sfail;
+    __shared__ ShakeK<C> sk[NBOND];
+    __shared__ C sc[3][NSURF];
     if (blockIdx.x >= nm) return;
     const int lane = threadIdx.x;
     const int m = mols[blockIdx.x];
@@ -328,52 +402,46 @@ __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm
         d.vx[g] = vel_a(vx, ax, escale);
         d.vy[g] = vel_a(vy, ay, escale);
         d.vz[g] = vel_a(vz, az, escale);
+        sc[0][lane] = sc[1][lane] = sc[2][lane] = C(0);
     }
     const double ke0 = warp_sum(ke);
+    const double tol2d = 2.0 * tol;
     {   // bond lane: sites sbi32(lane) and lane + 1
         const int bi = lane < NBOND ? sbi32(lane) : 0, bj = lane < NBOND ? lane + 1 : 0;
-        const double rxi = __shfl_sync(FULL, rx, bi), ryi = __shfl_sync(FULL, ry, bi), rzi = __shfl_sync(FULL, rz, bi);
-        const double rxj = __shfl_sync(FULL, rx, bj), ryj = __shfl_sync(FULL, ry, bj), rzj = __shfl_sync(FULL, rz, bj);
-        const double pxi = __shfl_sync(FULL, px, bi), pyi = __shfl_sync(FULL, py, bi), pzi = __shfl_sync(FULL, pz, bi);
-        const double pxj = __shfl_sync(FULL, px, bj), pyj = __shfl_sync(FULL, py, bj), pzj = __shfl_sync(FULL, pz, bj);
-        if (lane < NBOND) {
-            float k[8];
-            shake_consts(rxi, ryi, rzi, rxj, ryj, rzj, pxi, pyi, pzi, pxj, pyj, pzj, cF.dsq64_s[lane], k);
-#pragma unroll
-            for (int q = 0; q < 8; q++) sk[lane][q] = k[q];
-        }
+        const double ex = __shfl_sync(FULL, rx, bi) - __shfl_sync(FULL, rx, bj);
+        const double ey = __shfl_sync(FULL, ry, bi) - __shfl_sync(FULL, ry, bj);
+        const double ez = __shfl_sync(FULL, rz, bi) - __shfl_sync(FULL, rz, bj);
+        const double qx = __shfl_sync(FULL, px, bi) - __shfl_sync(FULL, px, bj);
+        const double qy = __shfl_sync(FULL, py, bi) - __shfl_sync(FULL, py, bj);
+        const double qz = __shfl_sync(FULL, pz, bi) - __shfl_sync(FULL, pz, bj);
+        if (lane < NBOND)
+            shake_make<C>(ex, ey, ez, qx, qy, qz, cF.dsq64_s[lane], cF.rm64[2 + bi], cF.rm64[2 + bj], tol2d, sk[lane]);
     }
-    __syncwarp();   // bond constants and the predictor stores, for lane 0
-    if (lane == 0) {
-        float cx[NSURF], cy[NSURF], cz[NSURF];
-#pragma unroll
-        for (int i = 0; i < NSURF; i++) cx[i] = cy[i] = cz[i] = 0.f;
-        volatile float(*vk)[8] = sk;
-        float kc[8], kn[8];
-#pragma unroll
-        for (int q = 0; q < 8; q++) kc[q] = vk[0][q];
-        const float tol2 = (float)(2.0 * tol);
-        const double tol2d = 2.0 * tol;
-        int it = 0;
-        bool ldone = false;
-        while (!ldone && it <= maxit) {
-            ldone = true;
-            unroll<0, NBOND>([&](auto B) {
-                constexpr int b = decltype(B)::value;
-                constexpr int bn = b + 1 < NBOND ? b + 1 : 0;
-#pragma unroll
-                for (int q = 0; q < 8; q++) kn[q] = vk[bn][q];   // next bond's constants, ahead of use
-                if (shake_step<NSURF, b>(d, g0, kc, cx, cy, cz, tol2, tol2d)) ldone = false;
-#pragma unroll
-                for (int q = 0; q < 8; q++) kc[q] = kn[q];
-            });
-            it++;
+    __syncwarp();   // bond constants, zeroed corrections and the predictor stores
+    int kmine = lane, fail = 0;
+    bool changed = false;
+    for (int t = 0;; t++) {
+        bool clean = false, last = false;
+        const int b = t - WF_LAG * kmine;
+        if (lane < WF_LANES && kmine <= maxit && b >= 0 && b < NBOND) {
+            const int i = sbi32(b), j = b + 1;
+            C xi = sc[0][i], yi = sc[1][i], zi = sc[2][i], xj = sc[0][j], yj = sc[1][j], zj = sc[2][j];
+            if (shake_bond<C, true>(d, g0 + i, g0 + j, cF.dsq64_s[b], tol2d, sk[b], xi, yi, zi, xj, yj, zj)) {
+                sc[0][i] = xi; sc[1][i] = yi; sc[2][i] = zi;
+                sc[0][j] = xj; sc[1][j] = yj; sc[2][j] = zj;
+                changed = true;
+            }
+            if (b == NBOND - 1) {
+                clean = !changed;
+                last = changed && kmine == maxit;
+                changed = false;
+                kmine += WF_LANES;
+            }
         }
-#pragma unroll
-        for (int i = 0; i < NSURF; i++) { sc[0][i] = cx[i]; sc[1][i] = cy[i]; sc[2][i] = cz[i]; }
-        sfail = !ldone;
+        __syncwarp();
+        if (__any_sync(FULL, clean)) break;
+        if (__any_sync(FULL, last)) { fail = 1; break; }
     }
-    __syncwarp();
     double ke1 = 0.0;
     if (site) {
         const double cxi = sc[0][lane], cyi = sc[1][lane], czi = sc[2][lane];
@@ -388,14 +456,14 @@ __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm
     if (lane == 0) {
         d.ke[2 * m] = ke0;
         d.ke[2 * m + 1] = ke1;
-        if (sfail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+        if (fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
     }
 }
 
+template <typename C>
 __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm, double tol, int maxit) {
-    __shared__ float sk[NBOND][4];
-    __shared__ float sc[3][NSURF];
-    __shared__ int sfail;
+    __shared__ RattleK<C> sk[NBOND];
+    __shared__ C sc[3][NSURF];
     if (blockIdx.x >= nm) return;
     const int lane = threadIdx.x;
     const int m = mols[blockIdx.x];
@@ -414,6 +482,7 @@ __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm
         vz = __dmul_rn(escale, __dadd_rn(d.vz[g], az));
         d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
         rx = d.x[g]; ry = d.y[g]; rz = d.z[g];
+        sc[0][lane] = sc[1][lane] = sc[2][lane] = C(0);
     }
     {
         const int bi = lane < NBOND ? sbi32(lane) : 0, bj = lane < NBOND ? lane + 1 : 0;
@@ -423,47 +492,42 @@ __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm
         const double wx = __shfl_sync(FULL, vx, bi) - __shfl_sync(FULL, vx, bj);
         const double wy = __shfl_sync(FULL, vy, bi) - __shfl_sync(FULL, vy, bj);
         const double wz = __shfl_sync(FULL, vz, bi) - __shfl_sync(FULL, vz, bj);
-        if (lane < NBOND) {
-            sk[lane][0] = (float)ex; sk[lane][1] = (float)ey; sk[lane][2] = (float)ez;
-            sk[lane][3] = (float)(ex * wx + ey * wy + ez * wz);
-        }
+        if (lane < NBOND)
+            rattle_make<C>(ex, ey, ez, wx, wy, wz, cF.rmdt64[2 + bi], cF.rmdt64[2 + bj], cF.fb64_s[lane], sk[lane]);
     }
     __syncwarp();
-    if (lane == 0) {
-        float cx[NSURF], cy[NSURF], cz[NSURF];
-#pragma unroll
-        for (int i = 0; i < NSURF; i++) cx[i] = cy[i] = cz[i] = 0.f;
-        volatile float(*vk)[4] = sk;
-        float kc[4], kn[4];
-#pragma unroll
-        for (int q = 0; q < 4; q++) kc[q] = vk[0][q];
-        const float tolf = (float)tol;
-        int it = 0;
-        bool ldone = false;
-        while (!ldone && it <= maxit) {
-            ldone = true;
-            unroll<0, NBOND>([&](auto B) {
-                constexpr int b = decltype(B)::value;
-                constexpr int bn = b + 1 < NBOND ? b + 1 : 0;
-#pragma unroll
-                for (int q = 0; q < 4; q++) kn[q] = vk[bn][q];
-                if (rattle_step<NSURF, b>(d, g0, kc, cx, cy, cz, tolf, tol)) ldone = false;
-#pragma unroll
-                for (int q = 0; q < 4; q++) kc[q] = kn[q];
-            });
-            it++;
+    const C tolc = (C)tol;
+    int kmine = lane, fail = 0;
+    bool changed = false;
+    for (int t = 0;; t++) {
+        bool clean = false, last = false;
+        const int b = t - WF_LAG * kmine;
+        if (lane < WF_LANES && kmine <= maxit && b >= 0 && b < NBOND) {
+            const int i = sbi32(b), j = b + 1;
+            C xi = sc[0][i], yi = sc[1][i], zi = sc[2][i], xj = sc[0][j], yj = sc[1][j], zj = sc[2][j];
+            if (rattle_bond<C>(d, g0 + i, g0 + j, 2 + i, 2 + j, cF.dsq64_s[b], tol, tolc, sk[b], xi, yi, zi, xj, yj,
+                               zj)) {
+                sc[0][i] = xi; sc[1][i] = yi; sc[2][i] = zi;
+                sc[0][j] = xj; sc[1][j] = yj; sc[2][j] = zj;
+                changed = true;
+            }
+            if (b == NBOND - 1) {
+                clean = !changed;
+                last = changed && kmine == maxit;
+                changed = false;
+                kmine += WF_LANES;
+            }
         }
-#pragma unroll
-        for (int i = 0; i < NSURF; i++) { sc[0][i] = cx[i]; sc[1][i] = cy[i]; sc[2][i] = cz[i]; }
-        sfail = !ldone;
+        __syncwarp();
+        if (__any_sync(FULL, clean)) break;
+        if (__any_sync(FULL, last)) { fail = 1; break; }
     }
-    __syncwarp();
     if (site) {
         d.vx[g] = __dadd_rn(vx, (double)sc[0][lane]);
         d.vy[g] = __dadd_rn(vy, (double)sc[1][lane]);
         d.vz[g] = __dadd_rn(vz, (double)sc[2][lane]);
     }
-    if (lane == 0 && sfail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    if (lane == 0 && fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
 }
 
 }  // namespace
@@ -477,35 +541,53 @@ bool upload_tables_fast(const Tables &t, cudaStream_t st) {
         f.rm64[k] = 1.0 / t.mass[k];
         f.rm[k] = (float)(1.0 / t.mass[k]);
         f.rmdt[k] = (float)(DT / t.mass[k]);
+        f.rmdt64[k] = DT / t.mass[k];
     }
     for (int b = 0; b < 3; b++) {
         const int ki = b == 0 ? 0 : 1, kj = b == 2 ? 0 : 1;
         const double rs = 1.0 / t.mass[ki] + 1.0 / t.mass[kj];
         f.dsq64_w[b] = t.dsqw[b];
         f.dsq_w[b] = (float)t.dsqw[b];
-        f.fa_w[b] = (float)(2.0 * rs);
-        f.fb_w[b] = (float)((1.0 / DT) / (rs * t.dsqw[b]));
+        f.fa64_w[b] = 2.0 * rs;
+        f.fb64_w[b] = (1.0 / DT) / (rs * t.dsqw[b]);
+        f.fa_w[b] = (float)f.fa64_w[b];
+        f.fb_w[b] = (float)f.fb64_w[b];
     }
     for (int b = 0; b < NBOND; b++) {
         const double rs = 1.0 / t.mass[2 + t.bi[b]] + 1.0 / t.mass[2 + t.bj[b]];
         f.dsq64_s[b] = t.dsqs[b];
         f.dsq_s[b] = (float)t.dsqs[b];
-        f.fa_s[b] = (float)(2.0 * rs);
-        f.fb_s[b] = (float)((1.0 / DT) / (rs * t.dsqs[b]));
+        f.fa64_s[b] = 2.0 * rs;
+        f.fb64_s[b] = (1.0 / DT) / (rs * t.dsqs[b]);
+        f.fa_s[b] = (float)f.fa64_s[b];
+        f.fb_s[b] = (float)f.fb64_s[b];
     }
     return cudaMemcpyToSymbolAsync(cF, &f, sizeof f, 0, cudaMemcpyHostToDevice, st) == cudaSuccess;
 }
 
+// fp32: 1 for FP32 sweeps, 0 for FP64 sweeps.  Surfactants first, then
+// waters, on one stream: run side by side, the FP64-pipe-bound water sweeps
+// stall the latency-bound surfactant wavefronts.
 void launch_move_a32(const Dev &d, const int *wmols, int nw, const int *smols, int ns, cudaStream_t st, double tol,
-                     int maxit) {
-    if (ns) k_move_a32s<<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
-    if (nw) k_move_a32w<<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+                     int maxit, int fp32) {
+    if (fp32) {
+        if (ns) k_move_a32s<float><<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
+        if (nw) k_move_a32w<float><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+    } else {
+        if (ns) k_move_a32s<double><<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
+        if (nw) k_move_a32w<double><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+    }
 }
 
 void launch_move_b32(const Dev &d, const int *wmols, int nw, const int *smols, int ns, cudaStream_t st, double tol,
-                     int maxit) {
-    if (ns) k_move_b32s<<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
-    if (nw) k_move_b32w<<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+                     int maxit, int fp32) {
+    if (fp32) {
+        if (ns) k_move_b32s<float><<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
+        if (nw) k_move_b32w<float><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+    } else {
+        if (ns) k_move_b32s<double><<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
+        if (nw) k_move_b32w<double><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+    }
 }
 
 }  // namespace sesp

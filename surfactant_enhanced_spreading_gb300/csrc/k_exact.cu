@@ -438,14 +438,13 @@ void launch_locate(const Dev &d, int nmol, cudaStream_t st) {
 void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st) {
     if (nsurf_sites) k_isub<<<(nsurf_sites + 127) / 128, 128, 0, st>>>(d, nsurf_sites, surf_mols);
 }
-// fast = 1 (mixed path): reciprocal products instead of FP64 divisions in the
-// constraint iterations; fast = 0 divides exactly as the reference does.
-// fast = 1 (mixed path): the FP32 constraint sweeps of k_constraint32.cu;
-// fast = 0: the FP64 sweeps above, dividing exactly as the reference does.
+// fast = 0 (plain path): the FP64 sweeps above, dividing exactly as the
+// reference does; fast = 1 / 2 (mixed paths): the FP64 / FP32 sweeps of
+// k_constraint.cu.
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
                    int fast, cudaStream_t st) {
     if (fast) {
-        launch_move_a32(d, wmols, nw, smols, ns, st, tol, maxit);
+        launch_move_a32(d, wmols, nw, smols, ns, st, tol, maxit, fast == 2);
     } else {
         if (ns) k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
@@ -455,7 +454,7 @@ void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit, int fast,
                    cudaStream_t st) {
     if (fast) {
-        launch_move_b32(d, wmols, nw, smols, ns, st, tol, maxit);
+        launch_move_b32(d, wmols, nw, smols, ns, st, tol, maxit, fast == 2);
     } else {
         if (ns) k_move_b_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);

@@ -6,12 +6,6 @@
 
 namespace sesp {
 
-// a second stream with fork / join events for work that overlaps the main stream
-struct SideStream {
-    cudaStream_t st;
-    cudaEvent_t fork, join;
-};
-
 // k_exact.cu
 void upload_tables_exact(const Tables &t, cudaStream_t st);
 void launch_locate(const Dev &d, int nmol, cudaStream_t st);
@@ -22,13 +16,13 @@ void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int
                    cudaStream_t st);
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st);
 
-// k_constraint32.cu (mixed path); false if the uploaded bond graph is not
-// the one the kernels are specialised for
+// k_constraint.cu (mixed paths: FP64 or FP32 sweeps); false if the uploaded
+// bond graph is not the one the kernels are specialised for
 bool upload_tables_fast(const Tables &t, cudaStream_t st);
 void launch_move_a32(const Dev &d, const int *wmols, int nw, const int *smols, int ns, cudaStream_t st, double tol,
-                     int maxit);
+                     int maxit, int fp32);
 void launch_move_b32(const Dev &d, const int *wmols, int nw, const int *smols, int ns, cudaStream_t st, double tol,
-                     int maxit);
+                     int maxit, int fp32);
 
 // k_force.cu
 void upload_tables_force(const Tables &t, cudaStream_t st);

@@ -305,7 +305,6 @@ void op_l2l(double x, double y, double z, double2 *op) {
 struct sesp_ctx {
     sesp_params p;
     cudaStream_t st = nullptr;
-    SideStream side = {nullptr, nullptr, nullptr};
     bool uploaded = false, have_force = false;
     int nrep = 0, nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, nwm = 0, nsm = 0, d2 = 1;
     std::vector<Rep> reps;
@@ -396,7 +395,7 @@ void tcollect(sesp_ctx *c, int k) {
 
 void seq_force(sesp_ctx *c, int rebuild, int terms) {
     const Dev &d = c->d;
-    const int mixed = c->p.precision == SESP_MIXED;
+    const int mixed = c->p.precision != SESP_PLAIN_FP64;
     if (rebuild) {
         tstart(c, 5);
         cudaMemsetAsync(d.ccount, 0, sizeof(int) * c->ncell, c->st);
@@ -425,13 +424,13 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
 void seq_move_a(sesp_ctx *c) {
     tstart(c, 2);
     launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit,
-                  c->p.precision == SESP_MIXED, c->st);
+                  c->p.precision, c->st);
     tstop(c, 2);
 }
 void seq_move_b(sesp_ctx *c) {
     tstart(c, 3);
     launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit,
-                  c->p.precision == SESP_MIXED, c->st);
+                  c->p.precision, c->st);
     tstop(c, 3);
 }
 
@@ -475,7 +474,8 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (!p || !out) return fail(SESP_EINVAL, "null argument");
     for (int a = 0; a < 3; a++)
         if (p->n_cells[a] <= 0 || p->n_cells[a] % 4) return fail(SESP_EINVAL, "n_cells must be positive multiples of 4");
-    if (p->precision != SESP_PLAIN_FP64 && p->precision != SESP_MIXED) return fail(SESP_EINVAL, "unknown precision");
+    if (p->precision != SESP_PLAIN_FP64 && p->precision != SESP_MIXED && p->precision != SESP_MIXED_FP32C)
+        return fail(SESP_EINVAL, "unknown precision");
     if (p->rebuild_interval <= 0) return fail(SESP_EINVAL, "rebuild_interval must be positive");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SESP_ECUDA, "no CUDA device");
@@ -485,12 +485,6 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (set_device(c)) { delete c; return SESP_ECUDA; }
     if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "stream"); }
     for (int k = 0; k < 16; k++) cudaEventCreate(&c->ev[k]);
-    if (cudaStreamCreateWithFlags(&c->side.st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->side.fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->side.join, cudaEventDisableTiming) != cudaSuccess) {
-        delete c;
-        return fail(SESP_ECUDA, "side stream");
-    }
     init_force_kernels();
     Tables T = make_tables();
     {
@@ -511,9 +505,6 @@ int sesp_destroy(sesp_ctx *c) {
     cudaStreamSynchronize(c->st);
     free_state(c);
     for (int k = 0; k < 16; k++) cudaEventDestroy(c->ev[k]);
-    cudaEventDestroy(c->side.fork);
-    cudaEventDestroy(c->side.join);
-    cudaStreamDestroy(c->side.st);
     cudaStreamDestroy(c->st);
     delete c;
     return 0;

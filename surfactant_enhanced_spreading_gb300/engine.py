@@ -18,7 +18,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libsesp.so")
 
 PLAIN_FP64 = 0
-MIXED = 1
+MIXED = 1          # FP32 force arithmetic, FP64 constraint iterations
+MIXED_FP32C = 2    # MIXED with FP32 constraint iterations
 
 T_NEAR, T_FAR, T_VALENCE, T_DIHEDRAL, T_BERENDSEN = 1, 2, 4, 8, 16
 T_INTERNAL, T_SUBTRACT, T_WALL, T_GRAPHITE, T_ALL = 32, 64, 128, 256, 511

@@ -94,14 +94,15 @@ def _flips_ok(a, b, typical, worst, frac=0.01):
     return np.mean(dev > typical) <= frac and dev.max() < worst, (np.median(dev), np.mean(dev > typical), dev.max())
 
 
-def test_mixed_constraint_halves(sys_small):
+@pytest.mark.parametrize("mode", [E.MIXED, E.MIXED_FP32C])
+def test_mixed_constraint_halves(sys_small, mode):
     """FP32 SHAKE/RATTLE sweeps of the mixed path against the FP64 sweeps on
     identical inputs.  The FP32 sweeps round the constraint residual at
     ~1e-9 absolute (corrections of ~1e-3 sigma carried in FP32) and decide
     near-threshold cases in FP64 on their own state, so results agree to
     ~1e-9 except where a residual sits on the threshold (bounded by the
     constraint tolerance, 1e-4)."""
-    ep, em = E.Engine(sys_small, E.PLAIN_FP64), E.Engine(sys_small, E.MIXED)
+    ep, em = E.Engine(sys_small, E.PLAIN_FP64), E.Engine(sys_small, mode)
     ep.force(True); em.force(True)
     ep.init_accel()
     p0, v0, a0 = ep.state()
@@ -190,11 +191,12 @@ def test_kernel_timing_path(sys_small):
     assert nc > nl > 0
 
 
-def test_mixed_trajectory_100_steps():
-    """The mixed path (FP32 pair / multipole terms, reciprocal constraint
-    updates) stays close to the FP64 oracle over 100 steps."""
+@pytest.mark.parametrize("mode", [E.MIXED, E.MIXED_FP32C])
+def test_mixed_trajectory_100_steps(mode):
+    """The mixed paths (FP32 pair / multipole / bonded terms; FP64 or FP32
+    constraint sweeps) stay close to the FP64 oracle over 100 steps."""
     s = S.droplet(400, 4, cells=(8, 8, 8), seed=23)
-    eng, orc = E.Engine(s, E.MIXED), O.Oracle(s)
+    eng, orc = E.Engine(s, mode), O.Oracle(s)
     eng.force(True); orc.force(True)
     eng.init_accel(); orc.init_accel()
     eng.run(99101, 100)
@@ -219,7 +221,8 @@ def _nve_drift(precision, steps=400, every=50):
     return np.polyfit(t, np.array(es), 1)[0], abs(np.mean(es))
 
 
-def test_mixed_energy_drift_not_worse_than_plain():
+@pytest.mark.parametrize("mode", [E.MIXED, E.MIXED_FP32C])
+def test_mixed_energy_drift_not_worse_than_plain(mode):
     dp, scale = _nve_drift(E.PLAIN_FP64)
-    dm, _ = _nve_drift(E.MIXED)
+    dm, _ = _nve_drift(mode)
     assert abs(dm) <= 2.0 * abs(dp) + 1e-6 * scale, (dm, dp)
