@@ -19,6 +19,11 @@ TERM_NEAR, TERM_FAR, TERM_VALENCE, TERM_DIHEDRAL, TERM_BERENDSEN = 1, 2, 4, 8, 1
 TERM_INTERNAL, TERM_SUBTRACT, TERM_WALL, TERM_GRAPHITE, TERM_ALL = 32, 64, 128, 256, 511
 
 
+def threads() -> int:
+    """OpenMP threads the oracle's pair kernels and FMA passes use."""
+    return int(lib().orc_threads())
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -32,6 +37,7 @@ def lib():
         for name in ["orc_destroy", "orc_move_a_api", "orc_move_b_api", "orc_init_accel_api"]:
             getattr(L, name).argtypes = [P]
         L.orc_force.argtypes = [P, ctypes.c_int]
+        L.orc_threads.restype = ctypes.c_int
         L.orc_force_terms.argtypes = [P, ctypes.c_int, ctypes.c_int]
         L.orc_step.argtypes = [P, ctypes.c_int]
         L.orc_run.argtypes = [P, ctypes.c_int, ctypes.c_int]

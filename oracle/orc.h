@@ -122,6 +122,7 @@ void orc_build_lists(orc_sys *s);
 void orc_buildinternal(orc_sys *s);
 
 /* pair kernels (src/eval[wS]*.f90) */
+int orc_threads(void);                       /* OpenMP threads of the pair kernels and the FMA (1 without OpenMP) */
 void orc_eval_pairs_intracell(orc_sys *s);   /* called from src/up_downSR_isr.f90:324-329 */
 void orc_eval_pairs_neighbour(orc_sys *s);   /* src/mybox.f90:185-217 */
 

@@ -196,11 +196,14 @@ void orc_fma_build(orc_sys *s) {
     memset(s->cL3, 0, sizeof(double complex) * LP * n3);
     memset(s->cL4, 0, sizeof(double complex) * LP * s->ncell);
 
-    /* P2M, src/computeOnm4.f90:24-162 */
-    int mx = max_located(s) + 1;
+    /* P2M, src/computeOnm4.f90:24-162 (cells in parallel, scratch per thread) */
+    const int mx = max_located(s) + 1;
+#pragma omp parallel
+    {
     int *site = (int *)malloc(sizeof(int) * mx);
     double *q = (double *)malloc(sizeof(double) * mx);
     double *rho = (double *)malloc(sizeof(double) * mx), *al = (double *)malloc(sizeof(double) * mx), *be = (double *)malloc(sizeof(double) * mx);
+#pragma omp for schedule(dynamic, 4)
     for (int c = 0; c < s->ncell; c++) {
         double cx, cy, cz;
         orc_rcen4(s, c, &cx, &cy, &cz);
@@ -215,8 +218,10 @@ void orc_fma_build(orc_sys *s) {
             }
     }
     free(site); free(q); free(rho); free(al); free(be);
+    }
 
-    /* M2M L4 -> L3, src/computeOnm3.f90:173-244 */
+    /* M2M L4 -> L3, src/computeOnm3.f90:173-244 (each parent on its own) */
+#pragma omp parallel for schedule(static)
     for (int z3 = 0; z3 < n3z; z3++)
         for (int y3 = 0; y3 < n3y; y3++)
             for (int x3 = 0; x3 < n3x; x3++) {
@@ -233,6 +238,7 @@ void orc_fma_build(orc_sys *s) {
                 }
             }
     /* M2M L3 -> L2, src/computeOnm2.f90:13-62 */
+#pragma omp parallel for schedule(dynamic, 1)
     for (int rank = 0; rank < s->nrank; rank++) {
         int rx, ry, rz;
         orc_rank_xyz(s, rank, &rx, &ry, &rz);
@@ -247,6 +253,7 @@ void orc_fma_build(orc_sys *s) {
         }
     }
     /* M2L at L2 over non-adjacent L2 boxes, src/computeLjk2.f90:17-72 */
+#pragma omp parallel for schedule(dynamic, 1)
     for (int rank = 0; rank < s->nrank; rank++) {
         int rx, ry, rz;
         orc_rank_xyz(s, rank, &rx, &ry, &rz);
@@ -263,6 +270,7 @@ void orc_fma_build(orc_sys *s) {
                 }
     }
     /* L2L L2 -> L3, src/shiftLjk2.f90:89-135 */
+#pragma omp parallel for schedule(dynamic, 1)
     for (int rank = 0; rank < s->nrank; rank++) {
         int rx, ry, rz;
         orc_rank_xyz(s, rank, &rx, &ry, &rz);
@@ -277,6 +285,7 @@ void orc_fma_build(orc_sys *s) {
         }
     }
     /* M2L at L3 over the 6^3 window, src/computeLjk3.f90:220-277 */
+#pragma omp parallel for schedule(dynamic, 1)
     for (int rank = 0; rank < s->nrank; rank++) {
         int rx, ry, rz;
         orc_rank_xyz(s, rank, &rx, &ry, &rz);
@@ -300,6 +309,7 @@ void orc_fma_build(orc_sys *s) {
         }
     }
     /* L2L L3 -> L4, src/shiftLjk3.f90:154-229 */
+#pragma omp parallel for schedule(static)
     for (int z3 = 0; z3 < n3z; z3++)
         for (int y3 = 0; y3 < n3y; y3++)
             for (int x3 = 0; x3 < n3x; x3++) {
@@ -314,7 +324,9 @@ void orc_fma_build(orc_sys *s) {
                     l2l(Lp, c3[0] - c4[0], c3[1] - c4[1], c3[2] - c4[2], &s->cL4[(size_t)LP * c]);
                 }
             }
-    /* M2L at L4 over the 6^3 window of each L3 parent, src/computeLjk4.f90:58-172 */
+    /* M2L at L4 over the 6^3 window of each L3 parent, src/computeLjk4.f90:58-172
+     * (every target cell on its own, in parallel) */
+#pragma omp parallel for schedule(dynamic, 4)
     for (int c = 0; c < s->ncell; c++) {
         int ix, iy, iz;
         orc_cell_xyz(s, c, &ix, &iy, &iz);
@@ -368,9 +380,12 @@ static void l2p(const double complex *L, double rx, double ry, double rz, double
 }
 
 void orc_evalLjk4(orc_sys *s) {
-    int mx = max_located(s) + 1;
+    const int mx = max_located(s) + 1;
+#pragma omp parallel
+    {
     int *site = (int *)malloc(sizeof(int) * mx);
     double *q = (double *)malloc(sizeof(double) * mx);
+#pragma omp for schedule(dynamic, 4)
     for (int c = 0; c < s->ncell; c++) {
         double cx, cy, cz;
         orc_rcen4(s, c, &cx, &cy, &cz);
@@ -382,6 +397,7 @@ void orc_evalLjk4(orc_sys *s) {
         }
     }
     free(site); free(q);
+    }
 }
 
 /* far-field energy 1/2 sum_i q_i xpi phi(r_i) (the reference computes none) */

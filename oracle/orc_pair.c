@@ -13,8 +13,19 @@
 #include "orc.h"
 
 #include <math.h>
+#include <stdlib.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define T ORC_T
+
+/* Forces and pair counts accumulate per thread (the kernels' cell loops are
+ * shared among the threads of an OpenMP team, statically, so every thread
+ * sees the same cells on every call) and are added in thread order after
+ * the kernels: deterministic for a given thread count. */
+static _Thread_local double *tl_f;        /* [3 * nsite]: x, y, z interleaved */
+static _Thread_local int64_t tl_nc, tl_nl;
 
 /* ljmode: 0 none, 1 water O-O (48 r6 (r6 - 1/2)), 2 tabulated (eps, sg6) */
 static inline void pterm(orc_sys *s, int gi, int gj, double qq, int ljmode, double eps, double sg6, int n3l) {
@@ -25,17 +36,18 @@ static inline void pterm(orc_sys *s, int gi, int gj, double qq, int ljmode, doub
     double rij = sqrt(rijsq);
     double fel = qq / (rij * rij * rij);
     double flj = 0.0;
-    s->npair_coul += n3l ? 2 : 1;
+    tl_nc += n3l ? 2 : 1;
     if (ljmode && rij <= ORC_RC) {
         double rsi = 1.0 / rijsq;
         double r6 = rsi * rsi * rsi;
         double rpl = ljmode == 1 ? 48.0 * r6 * (r6 - 0.5) : 48.0 * eps * sg6 * r6 * (sg6 * r6 - 0.5);
         flj = rpl * rsi;
-        s->npair_lj += n3l ? 2 : 1;
+        tl_nl += n3l ? 2 : 1;
     }
     double ft = fel + flj;
-    s->fx[gi] += xij * ft; s->fy[gi] += yij * ft; s->fz[gi] += zij * ft;
-    if (n3l) { s->fx[gj] -= xij * ft; s->fy[gj] -= yij * ft; s->fz[gj] -= zij * ft; }
+    double *fi = tl_f + 3 * (size_t)gi;
+    fi[0] += xij * ft; fi[1] += yij * ft; fi[2] += zij * ft;
+    if (n3l) { double *fj = tl_f + 3 * (size_t)gj; fj[0] -= xij * ft; fj[1] -= yij * ft; fj[2] -= zij * ft; }
 }
 
 static inline double qw(int t) { return T.rqw[t]; }
@@ -55,6 +67,7 @@ static void evalw1w1(orc_sys *s) {
     double qq[4][4];
     double qOqO = T.rqw[1] * T.rqw[1] * ORC_XPI, qOqH = T.rqw[1] * T.rqw[2] * ORC_XPI, qHqH = T.rqw[2] * T.rqw[3] * ORC_XPI;
     qq[1][1] = qOqO; qq[1][2] = qq[1][3] = qq[2][1] = qq[3][1] = qOqH; qq[2][2] = qq[2][3] = qq[3][2] = qq[3][3] = qHqH;
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_mlist *L = &s->cw1[c];
         for (int a = 0; a < L->n; a++)
@@ -70,6 +83,7 @@ static void evalw1w1n(orc_sys *s) {
     double qq[4][4];
     double qOqO = T.rqw[1] * T.rqw[1] * ORC_XPI, qOqH = T.rqw[1] * T.rqw[2] * ORC_XPI, qHqH = T.rqw[2] * T.rqw[3] * ORC_XPI;
     qq[1][1] = qOqO; qq[1][2] = qq[1][3] = qq[2][1] = qq[3][1] = qOqH; qq[2][2] = qq[2][3] = qq[3][2] = qq[3][3] = qHqH;
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_mlist *L = &s->cw1[c];
         for (int a = 0; a < L->n; a++)
@@ -109,6 +123,7 @@ static void w1_vs_list(orc_sys *s, int c, orc_list *J, int jwater, int qH, int n
 
 /* src/evalw1w2.f90:13-86 */
 static void evalw1w2(orc_sys *s) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         /* per i atom: W2Central (third law) then W226 (i side, H charge) */
         orc_mlist *L = &s->cw1[c];
@@ -127,6 +142,7 @@ static void evalw1w2(orc_sys *s) {
 
 /* src/evalw1w2n.f90:13-87 */
 static void evalw1w2n(orc_sys *s) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_mlist *L = &s->cw1[c];
         for (int a = 0; a < L->n; a++)
@@ -144,12 +160,14 @@ static void evalw1w2n(orc_sys *s) {
 
 /* src/evalw1w2nn.f90:102-139 */
 static void evalw1w2nn(orc_sys *s) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) w1_vs_list(s, c, &s->W2nn[c], 1, 1, 0);
 }
 
 /* src/evalw1s.f90:13-98, src/evalw1sn.f90, src/evalw1snn.f90: Central lists
  * with third law, 26 lists i side; src/evalw1snnn.f90 i side only */
 static void evalw1s_family(orc_sys *s, orc_list *C, orc_list *N26) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_mlist *L = &s->cw1[c];
         for (int a = 0; a < L->n; a++)
@@ -180,6 +198,7 @@ static void evalw1snnn(orc_sys *s) { evalw1s_family(s, NULL, s->Snnn); }
  * src/evalw2w1n.f90:15-112 (LJ if i is water O), src/evalw2nw1n.f90 (no LJ),
  * src/evalSw1n.f90, src/evalSnw1n.f90, src/evalSnnw1n.f90 (LJ with the O) */
 static void list_vs_w1n(orc_sys *s, orc_list *IL, int iwater, int qHi) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &IL[c];
         for (int a = 0; a < L->n; a++) {
@@ -212,6 +231,7 @@ static inline int same_mol(const orc_ent *a, const orc_ent *b) { return a->mol =
 
 /* src/evalw2w2.f90:129-226 */
 static void evalw2w2(orc_sys *s) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &s->W2C[c];
         for (int a = 0; a + 1 < L->n; a++) {
@@ -238,6 +258,7 @@ static void evalw2w2(orc_sys *s) {
 /* src/evalw2w2n.f90: W2Central x W2nCentral (third law, H charge), W2Central
  * x W2n26 (LJ O-O), W2nCentral x W226 */
 static void evalw2w2n(orc_sys *s) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &s->W2C[c];
         for (int a = 0; a < L->n; a++) {
@@ -261,6 +282,7 @@ static void evalw2w2n(orc_sys *s) {
 
 /* src/evalw2w2nn.f90 */
 static void evalw2w2nn(orc_sys *s) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &s->W2C[c];
         for (int a = 0; a < L->n; a++) {
@@ -276,6 +298,7 @@ static void evalw2w2nn(orc_sys *s) {
  * (Central third law, 26 i side) with LJ for water O; surfactant Central x
  * W226 (H charge).  src/evalw2snnn.f90: W2Central x Snnn only. */
 static void evalw2s_family(orc_sys *s, orc_list *C, orc_list *N26, orc_list *SI) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &s->W2C[c];
         for (int a = 0; a < L->n; a++) {
@@ -312,6 +335,7 @@ static void evalw2snnn(orc_sys *s) { evalw2s_family(s, NULL, s->Snnn, NULL); }
 
 /* src/evalw2nw2n.f90: W2nCentral pairs (third law) and x W2n26 */
 static void evalw2nw2n(orc_sys *s) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &s->W2nC[c];
         double rqq = qw(2) * ORC_XPI;
@@ -332,6 +356,7 @@ static void evalw2nw2n(orc_sys *s) {
 
 /* src/evalw2nw2nn.f90 */
 static void evalw2nw2nn(orc_sys *s) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &s->W2nC[c];
         double rqq = qw(2) * ORC_XPI;
@@ -346,6 +371,7 @@ static void evalw2nw2nn(orc_sys *s) {
  * (Central third law, 26 i side), Coulomb only; surfactant Central x W2n26
  * with LJ against the water O.  src/evalw2nSnnn.f90: W2nCentral x Snnn. */
 static void evalw2nS_family(orc_sys *s, orc_list *C, orc_list *N26, orc_list *SI) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &s->W2nC[c];
         double rqq = qw(2) * ORC_XPI;
@@ -381,6 +407,7 @@ static void evalw2nSnnn(orc_sys *s) { evalw2nS_family(s, NULL, s->Snnn, NULL); }
 /* surfactant list x W2nn (Coulomb, H charge): src/evalSw2nn.f90,
  * src/evalSnw2nn.f90, src/evalSnnw2nn.f90 */
 static void s_vs_w2nn(orc_sys *s, orc_list *IL) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &IL[c];
         for (int a = 0; a < L->n; a++) {
@@ -400,6 +427,7 @@ static inline void ss_term(orc_sys *s, orc_ent *ei, orc_ent *ej, int n3l) {
  * its 26 partner list, both excluding same-molecule pairs:
  * src/evalSS.f90:13-124, src/evalSnSn.f90, src/evalSnnSnn.f90 */
 static void ss_same(orc_sys *s, orc_list *C, orc_list *N26) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &C[c];
         for (int a = 0; a + 1 < L->n; a++)
@@ -417,6 +445,7 @@ static void ss_same(orc_sys *s, orc_list *C, orc_list *N26) {
  * B's Central list against A's 26 list: src/evalSSn.f90:13-148,
  * src/evalSSnn.f90, src/evalSnSnn.f90 */
 static void ss_cross(orc_sys *s, orc_list *AC, orc_list *BC, orc_list *B26, orc_list *A26) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &AC[c];
         for (int a = 0; a < L->n; a++) {
@@ -436,6 +465,7 @@ static void ss_cross(orc_sys *s, orc_list *AC, orc_list *BC, orc_list *B26, orc_
 /* Central list against Snnn, i side: src/evalSSnnn.f90, src/evalSnSnnn.f90,
  * src/evalSnnSnnn.f90 */
 static void ss_nnn(orc_sys *s, orc_list *AC) {
+    #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {
         orc_list *L = &AC[c];
         for (int a = 0; a < L->n; a++) {
@@ -464,7 +494,7 @@ static void evalSnw2nn(orc_sys *s) { s_vs_w2nn(s, s->SnC); }
 static void evalSnnw2nn(orc_sys *s) { s_vs_w2nn(s, s->SnnC); }
 
 /* intra-cell kernels in the order of src/up_downSR_isr.f90:324-329 */
-void orc_eval_pairs_intracell(orc_sys *s) {
+static void intracell_kernels(orc_sys *s) {
     evalw1w1(s);
     evalw1w2(s);
     evalw1s(s);
@@ -474,7 +504,7 @@ void orc_eval_pairs_intracell(orc_sys *s) {
 }
 
 /* neighbour kernels in the order of src/mybox.f90:185-217 */
-void orc_eval_pairs_neighbour(orc_sys *s) {
+static void neighbour_kernels(orc_sys *s) {
     evalw1w1n(s);
     evalw1w2n(s);
     evalw1w2nn(s);
@@ -509,3 +539,46 @@ void orc_eval_pairs_neighbour(orc_sys *s) {
     evalSnnSnn(s);
     evalSnnSnnn(s);
 }
+
+int orc_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* run a group of kernels in an OpenMP team with per-thread force buffers,
+ * then add the buffers to the forces in thread order */
+static void run_team(orc_sys *s, void (*kernels)(orc_sys *)) {
+    const int nt = orc_threads();
+    const size_t n3 = 3 * (size_t)s->nsite;
+    double *buf = (double *)calloc(n3 * nt + 1, sizeof(double));
+    int64_t *cnt = (int64_t *)calloc(2 * (size_t)nt, sizeof(int64_t));
+#pragma omp parallel num_threads(nt)
+    {
+        int t = 0;
+#ifdef _OPENMP
+        t = omp_get_thread_num();
+#endif
+        tl_f = buf + n3 * t;
+        tl_nc = tl_nl = 0;
+        kernels(s);
+        cnt[2 * t] = tl_nc;
+        cnt[2 * t + 1] = tl_nl;
+#pragma omp barrier
+#pragma omp for schedule(static)
+        for (int g = 0; g < s->nsite; g++)
+            for (int u = 0; u < nt; u++) {
+                const double *f = buf + n3 * u + 3 * (size_t)g;
+                s->fx[g] += f[0]; s->fy[g] += f[1]; s->fz[g] += f[2];
+            }
+        tl_f = NULL;
+    }
+    for (int u = 0; u < nt; u++) { s->npair_coul += cnt[2 * u]; s->npair_lj += cnt[2 * u + 1]; }
+    free(buf);
+    free(cnt);
+}
+
+void orc_eval_pairs_intracell(orc_sys *s) { run_team(s, intracell_kernels); }
+void orc_eval_pairs_neighbour(orc_sys *s) { run_team(s, neighbour_kernels); }

@@ -12,7 +12,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_bench_small_json():
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--small", "--steps", "10", "--warmup", "3",
-                        "--no-cpu-baseline", "--plain-steps", "5"], capture_output=True, text=True, timeout=600)
+                        "--no-cpu-baseline", "--plain-steps", "5", "--replicas", "4", "--requests", "3"],
+                       capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-3000:]
     line = json.loads(r.stdout.strip().splitlines()[-1])
     for k in ["metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "roofline", "e2e", "clocks",
@@ -21,6 +22,10 @@ def test_bench_small_json():
     assert line["value"] > 0 and line["e2e"]["value"] > 0
     assert line["mixed_force_rms_rel_error"] < 1e-5
     assert line["roofline"]["achieved"] and line["roofline"]["achieved"] > 0
+    b = line["batched"]
+    assert b["replicas"] == 4 and b["mixed"]["value"] > 0 and b["plain_fp64"]["value"] > 0
+    sv = line["served"]
+    assert sv["requests"] == 3 and 0 < sv["p50_latency_s"] <= sv["p99_latency_s"]
 
 
 def test_bench_reference_arm_small():
