@@ -130,6 +130,21 @@ module sesp_mod
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: e(8)
     end function
+    integer(c_int) function sesp_autotune(ctx, out) bind(C, name="sesp_autotune")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), intent(out) :: out(3)
+    end function
+    integer(c_int) function sesp_tuning(ctx, out) bind(C, name="sesp_tuning")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), intent(out) :: out(3)
+    end function
+    integer(c_int) function sesp_set_tuning(ctx, tile, ctas_per_sm) bind(C, name="sesp_set_tuning")
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: tile, ctas_per_sm
+    end function
     ! sesp_energies without allocating (fixed scratch; at most 131072 sites)
     integer(c_int) function sesp_energies_static(ctx, e) bind(C, name="sesp_energies_static")
       import :: c_int, c_ptr, c_double

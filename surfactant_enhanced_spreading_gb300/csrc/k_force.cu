@@ -207,11 +207,11 @@ __device__ inline double rsqrt_fp64(double r2) {
 }
 
 // Work items, rebuilt with the cell lists: one per (target cell, partner row,
-// chunk of NEAR_TILE target sites).  A partner row is the (up to) 3 cells at
+// chunk of `tile` target sites).  A partner row is the (up to) 3 cells at
 // (dy, dz) from the target cell along x, contiguous in slot order; the 9 rows
-// (3 planes x 3 rows) of a cell cover its 27-cell shell.
+// (3 planes x 3 rows) of a cell cover its 27-cell shell.  tile is 64 (two
+// target sites per lane of a warp) or 32 (one); the autotuner picks it.
 // item.x = cell, item.y = (plane * 3 + row) << 8 | chunk.
-constexpr int NEAR_TILE = 64;   // target sites per item: 2 per lane of one warp
 
 __device__ inline int near_row_mask(const Rep &r, int iy, int iz) {
     int mask = 0;
@@ -227,7 +227,7 @@ __device__ inline int near_row_mask(const Rep &r, int iy, int iz) {
     return mask;
 }
 
-__global__ void k_near_items_count(Dev d, int ncell) {
+__global__ void k_near_items_count(Dev d, int ncell, int tile) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const int ni = d.cstart[c + 1] - d.cstart[c];
@@ -236,7 +236,7 @@ __global__ void k_near_items_count(Dev d, int ncell) {
         const Rep r = d.rep[d.crep[c]];
         int ix, iy, iz;
         cell_xyz(r, c, ix, iy, iz);
-        n = __popc(near_row_mask(r, iy, iz)) * ((ni + NEAR_TILE - 1) / NEAR_TILE);
+        n = __popc(near_row_mask(r, iy, iz)) * ((ni + tile - 1) / tile);
     }
     d.near_icount[c] = n;
 }
@@ -260,7 +260,7 @@ __global__ void k_near_items_scan(Dev d, int ncell) {
     for (int c = b; c < e; c++) { int v = d.near_icount[c]; d.near_icount[c] = acc; acc += v; }
 }
 
-__global__ void k_near_items_fill(Dev d, int ncell) {
+__global__ void k_near_items_fill(Dev d, int ncell, int tile) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
     const int ni = d.cstart[c + 1] - d.cstart[c];
@@ -269,17 +269,17 @@ __global__ void k_near_items_fill(Dev d, int ncell) {
     int ix, iy, iz;
     cell_xyz(r, c, ix, iy, iz);
     const int mask = near_row_mask(r, iy, iz);
-    const int nch = (ni + NEAR_TILE - 1) / NEAR_TILE;
+    const int nch = (ni + tile - 1) / tile;
     int k = d.near_icount[c];
     for (int pr = 0; pr < 9; pr++)
         if (mask >> pr & 1)
             for (int ch = 0; ch < nch; ch++) d.near_items[k++] = make_int2(c, pr << 8 | ch);
 }
 
-void launch_near_items(const Dev &d, int ncell, cudaStream_t st) {
-    k_near_items_count<<<(ncell + 255) / 256, 256, 0, st>>>(d, ncell);
+void launch_near_items(const Dev &d, int ncell, int tile, cudaStream_t st) {
+    k_near_items_count<<<(ncell + 255) / 256, 256, 0, st>>>(d, ncell, tile);
     k_near_items_scan<<<1, 1024, 0, st>>>(d, ncell);
-    k_near_items_fill<<<(ncell + 255) / 256, 256, 0, st>>>(d, ncell);
+    k_near_items_fill<<<(ncell + 255) / 256, 256, 0, st>>>(d, ncell, tile);
 }
 
 // One partner's force on the two target sites of a lane (src/evalw1w1n.f90:86-104
@@ -389,7 +389,7 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 // MIXED: FP32 positions relative to the cell centres, FP32 pair terms summed
 // in FP32 over one row (at most 3 cells).
 template <bool MIXED>
-__global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot) {
+__global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int tile) {
     __shared__ float2 s_lj32[NTYPE];
     __shared__ double2 s_lj64[MIXED ? 1 : NTYPE * NTYPE];
     if constexpr (MIXED) {
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot) {
         const int c = item.x, pr = item.y >> 8, chunk = item.y & 255;
         const int dzc = pr / 3 - 1, dyc = pr % 3 - 1;
         const int s0 = d.cstart[c], ni = d.cstart[c + 1] - s0;
-        const int i0 = chunk * NEAR_TILE + lane, i1 = i0 + 32;
+        const int i0 = chunk * tile + lane, i1 = tile == 64 ? i0 + 32 : ni;
         const bool a0 = i0 < ni, a1 = i1 < ni;
         const bool two = __any_sync(0xffffffffu, a1);
         const Rep r = d.rep[d.crep[c]];
@@ -525,13 +525,18 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     d.nf[3 * (size_t)s] = fx; d.nf[3 * (size_t)s + 1] = fy; d.nf[3 * (size_t)s + 2] = fz;
 }
 
-static int g_near_grid[2] = {0, 0};
+int near_max_ctas_per_sm(int mixed) {
+    int nb = 0;
+    if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true>, NEAR_THREADS, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<false>, NEAR_THREADS, 0);
+    return nb > 0 ? nb : 1;
+}
 
-void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, cudaStream_t st) {
+void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st) {
     if (terms & SESP_T_NEAR) {
         cudaMemsetAsync(d.near_ctl, 0, sizeof(int), st);
-        if (mixed) k_near<true><<<g_near_grid[1], NEAR_THREADS, 0, st>>>(d, nslot);
-        else k_near<false><<<g_near_grid[0], NEAR_THREADS, 0, st>>>(d, nslot);
+        if (mixed) k_near<true><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+        else k_near<false><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
     }
     if (mixed) k_near_finish<true><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
     else k_near_finish<false><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
@@ -845,13 +850,6 @@ __global__ void __launch_bounds__(128) k_m2l_all(Dev d, const C2<R> *Htab, const
 // opt-in shared-memory sizes; called once per context creation (the
 // attribute is per device, so every context sets it for its own device)
 void init_force_kernels() {
-    int dev = 0, nsm = 0, nb0 = 0, nb1 = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb0, k_near<false>, NEAR_THREADS, 0);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb1, k_near<true>, NEAR_THREADS, 0);
-    g_near_grid[0] = nsm * (nb0 > 0 ? nb0 : 1);
-    g_near_grid[1] = nsm * (nb1 > 0 ? nb1 : 1);
     cudaFuncSetAttribute(k_m2l_win<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<double>());
     cudaFuncSetAttribute(k_m2l_win<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<float>());
 }

@@ -1,6 +1,7 @@
 // C ABI of the GB300 engine (declared in include/sesp.h): context, device
 // state, host-side force-field tables and multipole translation operators,
 // and the per-step launch sequence (captured into CUDA graphs by sesp_run).
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -315,6 +316,8 @@ struct sesp_ctx {
     int64_t steps = 0;
     // graphs of one step with / without a rebuild
     cudaGraphExec_t g_step[2] = {nullptr, nullptr};
+    NearShape near = {64, 0};   // pair-field launch shape (autotuned or set; results do not depend on it)
+    int n_sm = 0;               // streaming multiprocessors of the device
     // timing
     bool timing = false;
     cudaEvent_t ev[16];
@@ -401,7 +404,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         cudaMemsetAsync(d.ccount, 0, sizeof(int) * c->ncell, c->st);
         launch_locate(d, c->nmol, c->st);
         launch_sort(d, c->nsite, c->ncell, c->st);
-        launch_near_items(d, c->ncell, c->st);
+        launch_near_items(d, c->ncell, c->near.tile, c->st);
         launch_isub(d, c->nsm * NSURF, c->smols, c->st);
         launch_graphite_list(d, c->nsite, c->st);
         tstop(c, 5);
@@ -413,7 +416,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         tstop(c, 6);
     }
     tstart(c, 0);
-    launch_near(d, c->ncell, c->nsite, mixed, terms, c->st);
+    launch_near(d, c->ncell, c->nsite, mixed, terms, c->near, c->st);
     tstop(c, 0);
     tstart(c, 4);
     launch_site_forces(d, c->nsite, terms, mixed, c->st);
@@ -486,6 +489,12 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "stream"); }
     for (int k = 0; k < 16; k++) cudaEventCreate(&c->ev[k]);
     init_force_kernels();
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, dev);
+        c->near.grid = c->n_sm * near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64);
+    }
     Tables T = make_tables();
     {
         std::vector<unsigned char> map = make_intra_map(T);
@@ -578,7 +587,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.ccount, C)) || (e = dalloc(c, &d.cfill, C)) || (e = dalloc(c, &d.sloc, N)) ||
         (e = dalloc(c, &d.sslot, N)) || (e = dalloc(c, &d.srt_site, N)) || (e = dalloc(c, &d.srt_pos, N)) ||
         (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.srt_key, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) ||
-        (e = dalloc(c, &d.near_part, 27 * (size_t)N)) || (e = dalloc(c, &d.near_items, 9 * ((size_t)N / 64 + C) + 16)) ||
+        (e = dalloc(c, &d.near_part, 27 * (size_t)N)) || (e = dalloc(c, &d.near_items, 9 * ((size_t)N / 32 + C) + 16)) ||
         (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 2)) ||
         (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
@@ -932,6 +941,88 @@ int sesp_run_timed(sesp_ctx *c, int kb0, int nsteps, int flush_l2, double *step_
     cudaEventDestroy(e1);
     if (fbuf) cudaFree(fbuf);
     return rc;
+}
+
+// ------------------------------------------------------------------ autotuning of the pair-field launch
+
+namespace {
+void drop_graphs(sesp_ctx *c) {
+    for (auto &g : c->g_step)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+}  // namespace
+
+int sesp_set_tuning(sesp_ctx *c, int tile, int ctas_per_sm) {
+    if (int e = check_ctx(c, true)) return e;
+    const int mixed = c->p.precision != SESP_PLAIN_FP64;
+    if (tile != 32 && tile != 64) return fail(SESP_EINVAL, "tile must be 32 or 64");
+    if (ctas_per_sm < 1 || ctas_per_sm > near_max_ctas_per_sm(mixed))
+        return fail(SESP_EINVAL, "ctas_per_sm must be 1..%d", near_max_ctas_per_sm(mixed));
+    if (set_device(c)) return SESP_ECUDA;
+    const bool retile = tile != c->near.tile;
+    c->near = {tile, c->n_sm * ctas_per_sm};
+    if (retile && c->have_force) launch_near_items(c->d, c->ncell, tile, c->st);   // items of the current lists
+    drop_graphs(c);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
+int sesp_tuning(sesp_ctx *c, int out[3]) {
+    if (int e = check_ctx(c, false)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    out[0] = c->near.tile;
+    out[1] = c->n_sm ? c->near.grid / c->n_sm : 0;
+    out[2] = near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64);
+    return 0;
+}
+
+// Times the pair field on the current state for every candidate shape (tile
+// 64 or 32 sites per work item; 1/4, 1/2, 3/4 or all of the CTAs per SM the
+// kernel can hold), median of 5 launches each, and keeps the fastest.
+int sesp_autotune(sesp_ctx *c, int out[3]) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    if (!c->have_force) return fail(SESP_ESTATE, "autotuning needs a force call first (cell lists)");
+    if (set_device(c)) return SESP_ECUDA;
+    const int mixed = c->p.precision != SESP_PLAIN_FP64;
+    const int mx = near_max_ctas_per_sm(mixed);
+    int cands[4] = {mx, (3 * mx) / 4, mx / 2, mx / 4};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    NearShape pick = c->near;
+    for (int tile : {64, 32}) {
+        launch_near_items(c->d, c->ncell, tile, c->st);
+        for (int k = 0; k < 4; k++) {
+            const int cps = cands[k];
+            if (cps < 1 || (k > 0 && cps == cands[k - 1])) continue;
+            const NearShape sh = {tile, c->n_sm * cps};
+            launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st);   // warm
+            float t[5];
+            for (int r = 0; r < 5; r++) {
+                cudaEventRecord(e0, c->st);
+                launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st);
+                cudaEventRecord(e1, c->st);
+                cudaEventSynchronize(e1);
+                cudaEventElapsedTime(&t[r], e0, e1);
+            }
+            std::sort(t, t + 5);
+            if (t[2] < best) { best = t[2]; pick = sh; }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->near = pick;
+    launch_near_items(c->d, c->ncell, pick.tile, c->st);
+    drop_graphs(c);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+    out[0] = pick.tile;
+    out[1] = pick.grid / c->n_sm;
+    out[2] = mx;
+    return 0;
 }
 
 int sesp_pair_counts(sesp_ctx *c, int64_t out[2]) {

@@ -33,7 +33,7 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_run_async", "sesp_sync", "sesp_temperature", "sesp_get_eta", "sesp_set_eta", "sesp_energies",
            "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts",
            "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes",
-           "sesp_energies_static"]
+           "sesp_energies_static", "sesp_autotune", "sesp_tuning", "sesp_set_tuning"]
 
 
 class SespError(RuntimeError):
@@ -92,6 +92,9 @@ def load(path: str = LIB_PATH):
     L.sesp_query.argtypes = [P]
     L.sesp_device_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.sesp_energies_static.argtypes = [P, dp]
+    L.sesp_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
+    L.sesp_tuning.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
+    L.sesp_set_tuning.argtypes = [P, ctypes.c_int, ctypes.c_int]
     _lib = L
     return L
 
@@ -254,6 +257,22 @@ class Engine:
         out = np.empty(8)
         _check(_lib.sesp_energies(self._h, _dp(out)))
         return out
+
+    def autotune(self):
+        """Pick the pair field's launch shape by timing the candidates on the
+        current state (results do not depend on it); returns
+        (tile, ctas_per_sm, largest ctas_per_sm)."""
+        out = (ctypes.c_int * 3)()
+        _check(_lib.sesp_autotune(self._h, out))
+        return tuple(out)
+
+    def tuning(self):
+        out = (ctypes.c_int * 3)()
+        _check(_lib.sesp_tuning(self._h, out))
+        return tuple(out)
+
+    def set_tuning(self, tile, ctas_per_sm):
+        _check(_lib.sesp_set_tuning(self._h, int(tile), int(ctas_per_sm)))
 
     def energies_static(self):
         """The same eight energies through sesp_energies_static: no device
