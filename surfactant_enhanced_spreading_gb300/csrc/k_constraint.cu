@@ -379,10 +379,34 @@ __device__ inline double warp_sum(double v) {
 constexpr int WF_LAG = 8;
 constexpr int WF_LANES = 4;   // ceil(NBOND / WF_LAG) sweeps in flight
 
+// Shared-memory layout of one molecule's bond records and site corrections:
+// field-major, index skewed by one slot every 8 (i -> i + i / 8), so the four
+// lanes of a wavefront step (bonds b, b-8, b-16, b-24 and their sites) fall
+// on different banks.
+__device__ __forceinline__ int skew8(int i) { return i + (i >> 3); }
+constexpr int SK = 32;   // padded length (largest skewed index 28 + 3)
+template <typename C, int NF>
+struct BondRecords {
+    C v[NF][SK];
+    template <typename K>
+    __device__ void put(int b, const K &k) {
+        const C *f = reinterpret_cast<const C *>(&k);
+#pragma unroll
+        for (int q = 0; q < NF; q++) v[q][skew8(b)] = f[q];
+    }
+    template <typename K>
+    __device__ void get(int b, K &k) const {
+        C *f = reinterpret_cast<C *>(&k);
+#pragma unroll
+        for (int q = 0; q < NF; q++) f[q] = v[q][skew8(b)];
+    }
+};
+
 template <typename C>
 __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm, double tol, int maxit) {
-    __shared__ ShakeK<C> sk[NBOND];
-    __shared__ C sc[3][NSURF];
+    static_assert(sizeof(ShakeK<C>) == 16 * sizeof(C), "ShakeK is 16 values");
+    __shared__ BondRecords<C, 16> sk;
+    __shared__ C sc[3][SK];
     if (blockIdx.x >= nm) return;
     const int lane = threadIdx.x;
     const int m = mols[blockIdx.x];
@@ -402,7 +426,7 @@ __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm
         d.vx[g] = vel_a(vx, ax, escale);
         d.vy[g] = vel_a(vy, ay, escale);
         d.vz[g] = vel_a(vz, az, escale);
-        sc[0][lane] = sc[1][lane] = sc[2][lane] = C(0);
+        sc[0][skew8(lane)] = sc[1][skew8(lane)] = sc[2][skew8(lane)] = C(0);
     }
     const double ke0 = warp_sum(ke);
     const double tol2d = 2.0 * tol;
@@ -414,8 +438,11 @@ __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm
         const double qx = __shfl_sync(FULL, px, bi) - __shfl_sync(FULL, px, bj);
         const double qy = __shfl_sync(FULL, py, bi) - __shfl_sync(FULL, py, bj);
         const double qz = __shfl_sync(FULL, pz, bi) - __shfl_sync(FULL, pz, bj);
-        if (lane < NBOND)
-            shake_make<C>(ex, ey, ez, qx, qy, qz, cF.dsq64_s[lane], cF.rm64[2 + bi], cF.rm64[2 + bj], tol2d, sk[lane]);
+        if (lane < NBOND) {
+            ShakeK<C> k;
+            shake_make<C>(ex, ey, ez, qx, qy, qz, cF.dsq64_s[lane], cF.rm64[2 + bi], cF.rm64[2 + bj], tol2d, k);
+            sk.put(lane, k);
+        }
     }
     __syncwarp();   // bond constants, zeroed corrections and the predictor stores
     int kmine = lane, fail = 0;
@@ -424,11 +451,13 @@ __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm
         bool clean = false, last = false;
         const int b = t - WF_LAG * kmine;
         if (lane < WF_LANES && kmine <= maxit && b >= 0 && b < NBOND) {
-            const int i = sbi32(b), j = b + 1;
-            C xi = sc[0][i], yi = sc[1][i], zi = sc[2][i], xj = sc[0][j], yj = sc[1][j], zj = sc[2][j];
-            if (shake_bond<C, true>(d, g0 + i, g0 + j, cF.dsq64_s[b], tol2d, sk[b], xi, yi, zi, xj, yj, zj)) {
-                sc[0][i] = xi; sc[1][i] = yi; sc[2][i] = zi;
-                sc[0][j] = xj; sc[1][j] = yj; sc[2][j] = zj;
+            const int i = sbi32(b), j = b + 1, si = skew8(i), sj = skew8(j);
+            ShakeK<C> k;
+            sk.get(b, k);
+            C xi = sc[0][si], yi = sc[1][si], zi = sc[2][si], xj = sc[0][sj], yj = sc[1][sj], zj = sc[2][sj];
+            if (shake_bond<C, false>(d, g0 + i, g0 + j, cF.dsq64_s[b], tol2d, k, xi, yi, zi, xj, yj, zj)) {
+                sc[0][si] = xi; sc[1][si] = yi; sc[2][si] = zi;
+                sc[0][sj] = xj; sc[1][sj] = yj; sc[2][sj] = zj;
                 changed = true;
             }
             if (b == NBOND - 1) {
@@ -444,7 +473,7 @@ __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm
     }
     double ke1 = 0.0;
     if (site) {
-        const double cxi = sc[0][lane], cyi = sc[1][lane], czi = sc[2][lane];
+        const double cxi = sc[0][skew8(lane)], cyi = sc[1][skew8(lane)], czi = sc[2][skew8(lane)];
         d.x[g] = __dadd_rn(px, cxi);
         d.y[g] = __dadd_rn(py, cyi);
         d.z[g] = __dadd_rn(pz, czi);
@@ -462,8 +491,9 @@ __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm
 
 template <typename C>
 __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm, double tol, int maxit) {
-    __shared__ RattleK<C> sk[NBOND];
-    __shared__ C sc[3][NSURF];
+    static_assert(sizeof(RattleK<C>) == 11 * sizeof(C), "RattleK is 11 values");
+    __shared__ BondRecords<C, 11> sk;
+    __shared__ C sc[3][SK];
     if (blockIdx.x >= nm) return;
     const int lane = threadIdx.x;
     const int m = mols[blockIdx.x];
@@ -482,7 +512,7 @@ __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm
         vz = __dmul_rn(escale, __dadd_rn(d.vz[g], az));
         d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
         rx = d.x[g]; ry = d.y[g]; rz = d.z[g];
-        sc[0][lane] = sc[1][lane] = sc[2][lane] = C(0);
+        sc[0][skew8(lane)] = sc[1][skew8(lane)] = sc[2][skew8(lane)] = C(0);
     }
     {
         const int bi = lane < NBOND ? sbi32(lane) : 0, bj = lane < NBOND ? lane + 1 : 0;
@@ -492,8 +522,11 @@ __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm
         const double wx = __shfl_sync(FULL, vx, bi) - __shfl_sync(FULL, vx, bj);
         const double wy = __shfl_sync(FULL, vy, bi) - __shfl_sync(FULL, vy, bj);
         const double wz = __shfl_sync(FULL, vz, bi) - __shfl_sync(FULL, vz, bj);
-        if (lane < NBOND)
-            rattle_make<C>(ex, ey, ez, wx, wy, wz, cF.rmdt64[2 + bi], cF.rmdt64[2 + bj], cF.fb64_s[lane], sk[lane]);
+        if (lane < NBOND) {
+            RattleK<C> k;
+            rattle_make<C>(ex, ey, ez, wx, wy, wz, cF.rmdt64[2 + bi], cF.rmdt64[2 + bj], cF.fb64_s[lane], k);
+            sk.put(lane, k);
+        }
     }
     __syncwarp();
     const C tolc = (C)tol;
@@ -503,12 +536,13 @@ __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm
         bool clean = false, last = false;
         const int b = t - WF_LAG * kmine;
         if (lane < WF_LANES && kmine <= maxit && b >= 0 && b < NBOND) {
-            const int i = sbi32(b), j = b + 1;
-            C xi = sc[0][i], yi = sc[1][i], zi = sc[2][i], xj = sc[0][j], yj = sc[1][j], zj = sc[2][j];
-            if (rattle_bond<C>(d, g0 + i, g0 + j, 2 + i, 2 + j, cF.dsq64_s[b], tol, tolc, sk[b], xi, yi, zi, xj, yj,
-                               zj)) {
-                sc[0][i] = xi; sc[1][i] = yi; sc[2][i] = zi;
-                sc[0][j] = xj; sc[1][j] = yj; sc[2][j] = zj;
+            const int i = sbi32(b), j = b + 1, si = skew8(i), sj = skew8(j);
+            RattleK<C> k;
+            sk.get(b, k);
+            C xi = sc[0][si], yi = sc[1][si], zi = sc[2][si], xj = sc[0][sj], yj = sc[1][sj], zj = sc[2][sj];
+            if (rattle_bond<C>(d, g0 + i, g0 + j, 2 + i, 2 + j, cF.dsq64_s[b], tol, tolc, k, xi, yi, zi, xj, yj, zj)) {
+                sc[0][si] = xi; sc[1][si] = yi; sc[2][si] = zi;
+                sc[0][sj] = xj; sc[1][sj] = yj; sc[2][sj] = zj;
                 changed = true;
             }
             if (b == NBOND - 1) {
@@ -523,9 +557,9 @@ __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm
         if (__any_sync(FULL, last)) { fail = 1; break; }
     }
     if (site) {
-        d.vx[g] = __dadd_rn(vx, (double)sc[0][lane]);
-        d.vy[g] = __dadd_rn(vy, (double)sc[1][lane]);
-        d.vz[g] = __dadd_rn(vz, (double)sc[2][lane]);
+        d.vx[g] = __dadd_rn(vx, (double)sc[0][skew8(lane)]);
+        d.vy[g] = __dadd_rn(vy, (double)sc[1][skew8(lane)]);
+        d.vz[g] = __dadd_rn(vz, (double)sc[2][skew8(lane)]);
     }
     if (lane == 0 && fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
 }

@@ -260,6 +260,8 @@ __global__ void k_near_items_scan(Dev d, int ncell) {
     for (int c = b; c < e; c++) { int v = d.near_icount[c]; d.near_icount[c] = acc; acc += v; }
 }
 
+// Items in cell order into near_items_tmp, each with a cost class:
+// floor(log2(targets x partners in its row)).
 __global__ void k_near_items_fill(Dev d, int ncell, int tile) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= ncell) return;
@@ -270,16 +272,49 @@ __global__ void k_near_items_fill(Dev d, int ncell, int tile) {
     cell_xyz(r, c, ix, iy, iz);
     const int mask = near_row_mask(r, iy, iz);
     const int nch = (ni + tile - 1) / tile;
+    const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+    int *bcount = d.near_ctl + 2;
     int k = d.near_icount[c];
-    for (int pr = 0; pr < 9; pr++)
-        if (mask >> pr & 1)
-            for (int ch = 0; ch < nch; ch++) d.near_items[k++] = make_int2(c, pr << 8 | ch);
+    for (int pr = 0; pr < 9; pr++) {
+        if (!(mask >> pr & 1)) continue;
+        const int c0 = cell_index(r, jx0, iy + pr % 3 - 1, iz + pr / 3 - 1);
+        const int npart = d.cstart[c0 + (jx1 - jx0) + 1] - d.cstart[c0];
+        for (int ch = 0; ch < nch; ch++) {
+            const int nt = min(tile, ni - ch * tile);
+            const int cls = 31 - __clz(nt * npart + 1);
+            d.near_items_tmp[k] = make_int2(c, pr << 8 | ch);
+            d.near_cls[k] = cls;
+            atomicAdd(&bcount[cls], 1);
+            k++;
+        }
+    }
 }
 
-void launch_near_items(const Dev &d, int ncell, int tile, cudaStream_t st) {
+// start of each cost class in the final order, most expensive class first
+__global__ void k_near_items_classes(Dev d) {
+    if (threadIdx.x != 0) return;
+    int *bcount = d.near_ctl + 2, *bnext = d.near_ctl + 34;
+    int acc = 0;
+    for (int b = 31; b >= 0; b--) { bnext[b] = acc; acc += bcount[b]; }
+}
+
+// Items into near_items by class.  Within a class the order depends on
+// thread timing; it only decides which warp takes which item first, and every
+// item's arithmetic is the same whatever its position.
+__global__ void k_near_items_place(Dev d) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= d.near_ctl[1]) return;
+    const int pos = atomicAdd(&d.near_ctl[34 + d.near_cls[k]], 1);
+    d.near_items[pos] = d.near_items_tmp[k];
+}
+
+void launch_near_items(const Dev &d, int ncell, int nitems_max, int tile, cudaStream_t st) {
+    cudaMemsetAsync(d.near_ctl + 2, 0, 64 * sizeof(int), st);
     k_near_items_count<<<(ncell + 255) / 256, 256, 0, st>>>(d, ncell, tile);
     k_near_items_scan<<<1, 1024, 0, st>>>(d, ncell);
     k_near_items_fill<<<(ncell + 255) / 256, 256, 0, st>>>(d, ncell, tile);
+    k_near_items_classes<<<1, 32, 0, st>>>(d);
+    k_near_items_place<<<(nitems_max + 255) / 256, 256, 0, st>>>(d);
 }
 
 // One partner's force on the two target sites of a lane (src/evalw1w1n.f90:86-104
@@ -546,6 +581,7 @@ void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const
 
 // P2M, src/computeOnm4.f90:142-162: O_n^m = sum_sites q rho^n Y(n,-m)
 //                                          = sum q rfctr(n,m) conj(T_n^m)
+template <typename R>
 __global__ void k_p2m(Dev d) {
     const int c = blockIdx.x;
     const int s0 = d.cstart[c], n = d.cstart[c + 1] - s0;
@@ -553,27 +589,33 @@ __global__ void k_p2m(Dev d) {
     int ix, iy, iz;
     cell_xyz(r, c, ix, iy, iz);
     const double cx = cell_centre(d, r, 0, ix), cy = cell_centre(d, r, 1, iy), cz = cell_centre(d, r, 2, iz);
-    double acc[2 * LPH];
-    for (int k = 0; k < 2 * LPH; k++) acc[k] = 0.0;
+    R acc[2 * LPH];
+    for (int k = 0; k < 2 * LPH; k++) acc[k] = R(0);
     for (int s = threadIdx.x; s < n; s += blockDim.x) {
-        double4 p = d.srt_pos[s0 + s];
-        double x = p.x - cx, y = p.y - cy, z = p.z - cz, q = p.w;
-        double r2 = x * x + y * y + z * z;
-        Cx<double> Tmm = {1.0, 0.0};
-        Cx<double> xy = {x, y};
+        R x, y, z, q;
+        if constexpr (sizeof(R) == 4) {   // cell-relative FP32 positions of the mixed path
+            const float4 p = d.srt_pos32[s0 + s];
+            x = p.x; y = p.y; z = p.z; q = p.w;
+        } else {
+            const double4 p = d.srt_pos[s0 + s];
+            x = p.x - cx; y = p.y - cy; z = p.z - cz; q = p.w;
+        }
+        R r2 = x * x + y * y + z * z;
+        Cx<R> Tmm = {R(1), R(0)};
+        Cx<R> xy = {x, y};
         int o = 0;
         for (int m = 0; m <= P; m++) {
-            if (m > 0) Tmm = cscale(cmul(xy, Tmm), -(double)(2 * m - 1));
-            Cx<double> T2 = Tmm, T1 = Tmm;
+            if (m > 0) Tmm = cscale(cmul(xy, Tmm), -(R)(2 * m - 1));
+            Cx<R> T2 = Tmm, T1 = Tmm;
             for (int nn = m; nn <= P; nn++) {
-                Cx<double> Tn;
+                Cx<R> Tn;
                 if (nn == m) Tn = Tmm;
-                else if (nn == m + 1) Tn = cscale(Tmm, (double)(2 * m + 1) * z);
-                else Tn = cscale(csub(cscale(T1, (double)(2 * nn - 1) * z), cscale(T2, (double)(nn + m - 1) * r2)), 1.0 / (double)(nn - m));
+                else if (nn == m + 1) Tn = cscale(Tmm, (R)(2 * m + 1) * z);
+                else Tn = cscale(csub(cscale(T1, (R)(2 * nn - 1) * z), cscale(T2, (R)(nn + m - 1) * r2)), R(1) / (R)(nn - m));
                 if (nn > m) T2 = T1;
                 T1 = Tn;
                 int ic = nn * (nn + 1) + m;
-                double w = q * cT.rfctr[ic];
+                R w = q * (R)cT.rfctr[ic];
                 // ordering index among m >= 0 coefficients: o(n,m) = n(n+1)/2 + m
                 int oi = nn * (nn + 1) / 2 + m;
                 acc[2 * oi] += w * Tn.re;
@@ -582,11 +624,11 @@ __global__ void k_p2m(Dev d) {
             }
         }
     }
-    __shared__ double red[2 * LPH][64];
+    __shared__ R red[2 * LPH][64];
     for (int k = 0; k < 2 * LPH; k++) red[k][threadIdx.x] = acc[k];
     __syncthreads();
     if (threadIdx.x < 2 * LPH) {
-        double s = 0.0;
+        R s = R(0);
         for (int t = 0; t < blockDim.x; t++) s += red[threadIdx.x][t];
         red[threadIdx.x][0] = s;
     }
@@ -596,7 +638,7 @@ __global__ void k_p2m(Dev d) {
         int nn = 0;
         while ((nn + 1) * (nn + 2) / 2 <= oi) nn++;
         int m = oi - nn * (nn + 1) / 2;
-        double re = red[2 * oi][0], im = red[2 * oi + 1][0];
+        double re = (double)red[2 * oi][0], im = (double)red[2 * oi + 1][0];
         double2 *O = d.O4 + (size_t)c * LP;
         O[nn * (nn + 1) + m] = make_double2(re, im);
         if (m > 0) O[nn * (nn + 1) - m] = make_double2(re, -im);
@@ -610,14 +652,6 @@ __device__ inline void out_jk(int o, int &j, int &k) {
     k = o - j * (j + 1) / 2;
 }
 
-__device__ inline void apply_op(const double2 *op, const double2 *in, double &re, double &im) {
-    for (int c = 0; c < LP; c++) {
-        double2 a = op[c], b = in[c];
-        re += a.x * b.x - a.y * b.y;
-        im += a.x * b.y + a.y * b.x;
-    }
-}
-
 __device__ inline void store_jk(double2 *L, int o, double re, double im, bool add) {
     int j, k;
     out_jk(o, j, k);
@@ -629,7 +663,24 @@ __device__ inline void store_jk(double2 *L, int o, double re, double im, bool ad
 
 // M2M, src/computeOnm3.f90:173-244 and src/computeOnm2.f90:13-62: parent box
 // from its 8 children (level 4 -> 3 or 3 -> 2)
-__global__ void k_m2m(Dev d, const double2 *Oc, double2 *Op, const double2 *ops, const int *brep, int level) {
+template <typename R, typename OP>
+__device__ inline void apply_op_r(const OP *op, const double2 *in, R &re, R &im) {
+#pragma unroll 5
+    for (int c = 0; c < LP; c++) {
+        const OP a = op[c];
+        const double2 b = in[c];
+        const R ax = (R)a.x, ay = (R)a.y, bx = (R)b.x, by = (R)b.y;
+        re += ax * bx - ay * by;
+        im += ax * by + ay * bx;
+    }
+}
+
+// one CTA per parent: thread (child, output) applies one child's operator,
+// the 8 children are added in a fixed order
+template <typename R, typename OP>
+__global__ void __launch_bounds__(128) k_m2m(Dev d, const double2 *Oc, double2 *Op, const OP *ops, const int *brep,
+                                             int level) {
+    __shared__ R sre[8][LPH], sim[8][LPH];
     const int b = blockIdx.x;
     const Rep r = d.rep[brep[b]];
     const int div = level == 3 ? 2 : 4;   // parent grid = nc / div
@@ -637,22 +688,29 @@ __global__ void k_m2m(Dev d, const double2 *Oc, double2 *Op, const double2 *ops,
     const int base_c = level == 3 ? r.cell0 : r.l3_0;
     const int np[3] = {r.nc[0] / div, r.nc[1] / div, r.nc[2] / div};
     const int nc[3] = {np[0] * 2, np[1] * 2, np[2] * 2};
-    int l = b - base_p;
-    int px = l % np[0], py = (l / np[0]) % np[1], pz = l / (np[0] * np[1]);
-    int o = threadIdx.x;
-    if (o >= LPH) return;
-    double re = 0.0, im = 0.0;
-    for (int ch = 0; ch < 8; ch++) {
-        int cx = 2 * px + (ch & 1), cy = 2 * py + ((ch >> 1) & 1), cz = 2 * pz + ((ch >> 2) & 1);
-        int ci = base_c + cx + nc[0] * (cy + nc[1] * cz);
-        apply_op(ops + ((size_t)ch * LPH + o) * LP, Oc + (size_t)ci * LP, re, im);
+    const int l = b - base_p;
+    const int px = l % np[0], py = (l / np[0]) % np[1], pz = l / (np[0] * np[1]);
+    const int ch = threadIdx.x / LPH, o = threadIdx.x % LPH;
+    if (ch < 8) {
+        const int cx = 2 * px + (ch & 1), cy = 2 * py + ((ch >> 1) & 1), cz = 2 * pz + ((ch >> 2) & 1);
+        const int ci = base_c + cx + nc[0] * (cy + nc[1] * cz);
+        R re = 0, im = 0;
+        apply_op_r<R>(ops + ((size_t)ch * LPH + o) * LP, Oc + (size_t)ci * LP, re, im);
+        sre[ch][o] = re;
+        sim[ch][o] = im;
     }
-    store_jk(Op + (size_t)b * LP, o, re, im, false);
+    __syncthreads();
+    if (threadIdx.x < LPH) {
+        R re = 0, im = 0;
+        for (int k = 0; k < 8; k++) { re += sre[k][threadIdx.x]; im += sim[k][threadIdx.x]; }
+        store_jk(Op + (size_t)b * LP, threadIdx.x, (double)re, (double)im, false);
+    }
 }
 
 // L2L, src/shiftLjk2.f90:89-135 and src/shiftLjk3.f90:154-229: child box
 // from its parent (level 2 -> 3 or 3 -> 4)
-__global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const double2 *ops, const int *brep, int level) {
+template <typename R, typename OP>
+__global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, const int *brep, int level) {
     const int b = blockIdx.x;
     const Rep r = d.rep[brep[b]];
     const int div = level == 3 ? 2 : 1;  // child grid = nc / div
@@ -666,18 +724,11 @@ __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const double2 *ops,
     int pi = base_p + cx / 2 + np[0] * (cy / 2 + np[1] * (cz / 2));
     int o = threadIdx.x;
     if (o >= LPH) return;
-    double re = 0.0, im = 0.0;
-    apply_op(ops + ((size_t)ch * LPH + o) * LP, Lp + (size_t)pi * LP, re, im);
-    store_jk(Lc + (size_t)b * LP, o, re, im, false);
+    R re = 0, im = 0;
+    apply_op_r<R>(ops + ((size_t)ch * LPH + o) * LP, Lp + (size_t)pi * LP, re, im);
+    store_jk(Lc + (size_t)b * LP, o, (double)re, (double)im, false);
 }
 
-// M2L over the 6^3 window of the parent's neighbours' children minus the 27
-// adjacent boxes (src/computeLjk4.f90:114-168, src/computeLjk3.f90:220-277).
-// The 8 children of one parent share that window, so one CTA takes a parent:
-// it stages the 216 window multipoles in shared memory once, streams the
-// translation operators offset by offset (each applied to every child whose
-// source at that offset is in the window) and accumulates the 8 x 15 output
-// coefficients in registers.  R is the arithmetic precision.
 // M2L with the operator of src/computeLjk4.f90:134-158 factored as
 //   op[(j,k),(n,m)] = cf[(j,k),(n,m)] * H_{j+n}^{m-k}(d),  H_l^q = Y_l^q(d) / |d|^(l+1),
 // d the source - target vector and H_l^{-q} = conj(H_l^q): per offset 45
@@ -855,23 +906,26 @@ void init_force_kernels() {
 }
 
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {
-    k_p2m<<<ncell, 64, 0, st>>>(d);
-    k_m2m<<<n3, 32, 0, st>>>(d, d.O4, d.O3, d.op_m2m43, d.b3rep, 3);
-    k_m2m<<<n2, 32, 0, st>>>(d, d.O3, d.O2, d.op_m2m32, d.b2rep, 2);
     if (mixed) {
+        k_p2m<float><<<ncell, 64, 0, st>>>(d);
+        k_m2m<float><<<n3, 128, 0, st>>>(d, d.O4, d.O3, d.op32_m2m43, d.b3rep, 3);
+        k_m2m<float><<<n2, 128, 0, st>>>(d, d.O3, d.O2, d.op32_m2m32, d.b2rep, 2);
         k_m2l_all<float><<<n2, 128, 0, st>>>(d, (const C2<float> *)d.h32_m2l2, d.m2l_cf32, d2);
-        k_l2l<<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
+        k_l2l<float><<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op32_l2l23, d.b3rep, 3);
         k_m2l_win<float><<<n2, 128 * M2LCfg<float>::NG, m2l_smem<float>(), st>>>(
             d, d.O3, d.L3, (const C2<float> *)d.h32_m2l3, d.m2l_cf32, d.b2rep, 3);
-        k_l2l<<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
+        k_l2l<float><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op32_l2l34, d.crep, 4);
         k_m2l_win<float><<<n3, 128 * M2LCfg<float>::NG, m2l_smem<float>(), st>>>(
             d, d.O4, d.L4, (const C2<float> *)d.h32_m2l4, d.m2l_cf32, d.b3rep, 4);
     } else {
+        k_p2m<double><<<ncell, 64, 0, st>>>(d);
+        k_m2m<double><<<n3, 128, 0, st>>>(d, d.O4, d.O3, d.op_m2m43, d.b3rep, 3);
+        k_m2m<double><<<n2, 128, 0, st>>>(d, d.O3, d.O2, d.op_m2m32, d.b2rep, 2);
         k_m2l_all<double><<<n2, 128, 0, st>>>(d, (const C2<double> *)d.h_m2l2, d.m2l_cf, d2);
-        k_l2l<<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
+        k_l2l<double><<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
         k_m2l_win<double><<<n2, 128 * M2LCfg<double>::NG, m2l_smem<double>(), st>>>(
             d, d.O3, d.L3, (const C2<double> *)d.h_m2l3, d.m2l_cf, d.b2rep, 3);
-        k_l2l<<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
+        k_l2l<double><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
         k_m2l_win<double><<<n3, 128 * M2LCfg<double>::NG, m2l_smem<double>(), st>>>(
             d, d.O4, d.L4, (const C2<double> *)d.h_m2l4, d.m2l_cf, d.b3rep, 4);
     }

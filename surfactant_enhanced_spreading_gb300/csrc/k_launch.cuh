@@ -33,7 +33,7 @@ struct NearShape {
     int tile;   // target sites per work item: 64 or 32
     int grid;   // CTAs of the persistent kernel
 };
-void launch_near_items(const Dev &d, int ncell, int tile, cudaStream_t st);
+void launch_near_items(const Dev &d, int ncell, int nitems_max, int tile, cudaStream_t st);
 int near_max_ctas_per_sm(int mixed);
 void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st);
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st);

@@ -343,6 +343,9 @@ int dalloc(sesp_ctx *c, T **p, size_t n) {
     return 0;
 }
 
+// work items of the pair field: at most 9 rows x ceil(sites / 32) chunks per cell
+size_t near_items_max(int nsite, int ncell) { return 9 * ((size_t)nsite / 32 + ncell) + 16; }
+
 void free_state(sesp_ctx *c) {
     for (auto &g : c->g_step)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
@@ -404,7 +407,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         cudaMemsetAsync(d.ccount, 0, sizeof(int) * c->ncell, c->st);
         launch_locate(d, c->nmol, c->st);
         launch_sort(d, c->nsite, c->ncell, c->st);
-        launch_near_items(d, c->ncell, c->near.tile, c->st);
+        launch_near_items(d, c->ncell, (int)near_items_max(c->nsite, c->ncell), c->near.tile, c->st);
         launch_isub(d, c->nsm * NSURF, c->smols, c->st);
         launch_graphite_list(d, c->nsite, c->st);
         tstop(c, 5);
@@ -587,8 +590,9 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.ccount, C)) || (e = dalloc(c, &d.cfill, C)) || (e = dalloc(c, &d.sloc, N)) ||
         (e = dalloc(c, &d.sslot, N)) || (e = dalloc(c, &d.srt_site, N)) || (e = dalloc(c, &d.srt_pos, N)) ||
         (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.srt_key, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) ||
-        (e = dalloc(c, &d.near_part, 27 * (size_t)N)) || (e = dalloc(c, &d.near_items, 9 * ((size_t)N / 32 + C) + 16)) ||
-        (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 2)) ||
+        (e = dalloc(c, &d.near_part, 27 * (size_t)N)) || (e = dalloc(c, &d.near_items, near_items_max(N, C))) ||
+        (e = dalloc(c, &d.near_items_tmp, near_items_max(N, C))) || (e = dalloc(c, &d.near_cls, near_items_max(N, C))) ||
+        (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 66)) ||
         (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
         (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
@@ -602,7 +606,9 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.h32_m2l3, (size_t)343 * NHARM)) || (e = dalloc(c, &d.h32_m2l2, nh2)) ||
         (e = dalloc(c, &d.m2l_cf, (size_t)LPH * LP)) || (e = dalloc(c, &d.m2l_cf32, (size_t)LPH * LP)) ||
         (e = dalloc(c, &d.op_m2m43, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_m2m32, (size_t)8 * LPH * LP)) ||
-        (e = dalloc(c, &d.op_l2l23, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)))
+        (e = dalloc(c, &d.op_l2l23, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)) ||
+        (e = dalloc(c, &d.op32_m2m43, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op32_m2m32, (size_t)8 * LPH * LP)) ||
+        (e = dalloc(c, &d.op32_l2l23, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op32_l2l34, (size_t)8 * LPH * LP)))
         return e;
     // static per-site / per-molecule / per-box data
     std::vector<uint8_t> ptype(N);
@@ -694,15 +700,19 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         CK(cudaMemcpyAsync(d.m2l_cf32, cf32.data(), cf32.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
         CK(cudaStreamSynchronize(c->st));
         std::vector<double2> o8((size_t)8 * LPH * LP);
-        struct { double2 *dst; double s; int kind; } sets[4] = {
-            {d.op_m2m43, RS, 0}, {d.op_m2m32, 2 * RS, 0}, {d.op_l2l23, 2 * RS, 1}, {d.op_l2l34, RS, 1}};
+        struct { double2 *dst; float2 *dst32; double s; int kind; } sets[4] = {
+            {d.op_m2m43, d.op32_m2m43, RS, 0}, {d.op_m2m32, d.op32_m2m32, 2 * RS, 0},
+            {d.op_l2l23, d.op32_l2l23, 2 * RS, 1}, {d.op_l2l34, d.op32_l2l34, RS, 1}};
         for (auto &st : sets) {
             for (int ch = 0; ch < 8; ch++) {
                 double v[3] = {(ch & 1) - 0.5, ((ch >> 1) & 1) - 0.5, ((ch >> 2) & 1) - 0.5};
                 if (st.kind == 0) op_m2m(v[0] * st.s, v[1] * st.s, v[2] * st.s, &o8[(size_t)ch * LPH * LP]);
                 else op_l2l(-v[0] * st.s, -v[1] * st.s, -v[2] * st.s, &o8[(size_t)ch * LPH * LP]);
             }
+            std::vector<float2> o8f(o8.size());
+            for (size_t i = 0; i < o8.size(); i++) o8f[i] = make_float2((float)o8[i].x, (float)o8[i].y);
             CK(cudaMemcpyAsync(st.dst, o8.data(), o8.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+            CK(cudaMemcpyAsync(st.dst32, o8f.data(), o8f.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
             CK(cudaStreamSynchronize(c->st));
         }
     }
@@ -733,7 +743,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     if (!gpos32.empty())
         CK(cudaMemcpyAsync(d.gpos32, gpos32.data(), gpos32.size() * sizeof(float4), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.ljt, ljt.data(), ljt.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemsetAsync(d.near_ctl, 0, 2 * sizeof(int), c->st));   // no near-field items before the first rebuild
+    CK(cudaMemsetAsync(d.near_ctl, 0, 66 * sizeof(int), c->st));   // no near-field items before the first rebuild
     CK(cudaStreamSynchronize(c->st));
     c->uploaded = true;
     c->have_force = false;
@@ -961,7 +971,7 @@ int sesp_set_tuning(sesp_ctx *c, int tile, int ctas_per_sm) {
     if (set_device(c)) return SESP_ECUDA;
     const bool retile = tile != c->near.tile;
     c->near = {tile, c->n_sm * ctas_per_sm};
-    if (retile && c->have_force) launch_near_items(c->d, c->ncell, tile, c->st);   // items of the current lists
+    if (retile && c->have_force) launch_near_items(c->d, c->ncell, (int)near_items_max(c->nsite, c->ncell), tile, c->st);   // items of the current lists
     drop_graphs(c);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->st));
@@ -994,7 +1004,7 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     float best = 1e30f;
     NearShape pick = c->near;
     for (int tile : {64, 32}) {
-        launch_near_items(c->d, c->ncell, tile, c->st);
+        launch_near_items(c->d, c->ncell, (int)near_items_max(c->nsite, c->ncell), tile, c->st);
         for (int k = 0; k < 4; k++) {
             const int cps = cands[k];
             if (cps < 1 || (k > 0 && cps == cands[k - 1])) continue;
@@ -1015,7 +1025,7 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     c->near = pick;
-    launch_near_items(c->d, c->ncell, pick.tile, c->st);
+    launch_near_items(c->d, c->ncell, (int)near_items_max(c->nsite, c->ncell), pick.tile, c->st);
     drop_graphs(c);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->st));

@@ -98,9 +98,12 @@ struct Dev {
     int *srt_key;        // molecule << 5 | type
     double *nf;          // near + far force by slot [3 * nslot]
     double *near_part;   // per partner row partial near force [9][3 * nslot]
-    int2 *near_items;    // near-field work items (cell, row << 8 | chunk)
+    int2 *near_items;    // near-field work items (cell, row << 8 | chunk), most expensive first
+    int2 *near_items_tmp;   // the same in cell order
+    int *near_cls;       // cost class of each item in cell order
     int *near_icount;    // per cell: item count, then first item
-    int *near_ctl;       // [0] item counter of the running launch, [1] item count
+    int *near_ctl;       // [0] item counter of the running launch, [1] item count,
+                         // [2..33] items per cost class, [34..65] next slot per class
     // graphite columns of the bottom layer
     int *gcol_start;
     double4 *gpos;
@@ -111,6 +114,7 @@ struct Dev {
     // multipoles / local expansions (double2 = complex)
     double2 *O4, *L4, *O3, *L3, *O2, *L2;
     double2 *op_m2m43, *op_m2m32, *op_l2l23, *op_l2l34;
+    float2 *op32_m2m43, *op32_m2m32, *op32_l2l23, *op32_l2l34;   // FP32 copies for the mixed path
     // M2L factors: H_l^q of every offset (45 per offset; L4 and L3 7^3 offsets,
     // L2 (2 d2 + 1)^3) and the offset-independent coefficients (15 x 25)
     double2 *h_m2l4, *h_m2l3, *h_m2l2;
