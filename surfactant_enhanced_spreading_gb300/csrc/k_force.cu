@@ -741,17 +741,6 @@ template <typename R>
 struct C2 {
     R x, y;
 };
-template <typename R>
-struct M2LCfg;
-template <>
-struct M2LCfg<float> {
-    static constexpr int NG = 4;   // source groups per CTA
-};
-template <>
-struct M2LCfg<double> {
-    static constexpr int NG = 2;
-};
-
 // the 25 terms of output coefficient o: index of H, coefficient for the real
 // and the imaginary part of H (the sign of the latter conjugates H for m < k)
 template <typename R>
@@ -785,19 +774,30 @@ __device__ __forceinline__ void m2l_acc(const C2<R> *__restrict__ H, const S *sr
 }
 
 // M2L at L4 and L3 (src/computeLjk4.f90, src/computeLjk3.f90): one CTA per
-// parent box, its 8 children x 15 outputs x NG source groups; the parent's
-// 6x6x6 window of child-level multipoles is staged in shared memory and each
-// group takes every NG-th of the 343 offsets; the groups' sums are added in
-// a fixed order and accumulated into L.
+// parent box; the parent's 6x6x6 window of child-level multipoles is staged
+// in shared memory.  Thread (output o, group g) takes every M2L_G-th of the
+// 343 offsets; per offset it forms the 25 products cf * H once and applies
+// them to all 8 children (25 complex MACs each), so an H value is loaded once
+// per offset and output instead of once per child.  The groups' sums are
+// added in a fixed order and accumulated into L.
+constexpr int M2L_G = 16;   // offset groups per CTA
+constexpr int M2L_THREADS = LPH * M2L_G;
+
 template <typename R>
-__global__ void __launch_bounds__(128 * M2LCfg<R>::NG) k_m2l_win(Dev d, const double2 *O, double2 *L,
-                                                                 const C2<R> *Htab, const R *cf, const int *prep,
-                                                                 int level) {
-    constexpr int NG = M2LCfg<R>::NG;
+size_t m2l_smem() {
+    return sizeof(C2<R>) * 216 * LP + sizeof(R) * (2 * LPH * LP + 2 * M2L_G * 8 * LPH) + sizeof(int) * LPH * LP;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(M2L_THREADS) k_m2l_win(Dev d, const double2 *O, double2 *L, const C2<R> *Htab,
+                                                         const R *cf, const int *prep, int level) {
     extern __shared__ __align__(16) unsigned char smraw[];
     C2<R> *sO = (C2<R> *)smraw;                  // [216][LP]
-    R *scf = (R *)(sO + 216 * LP);               // [LPH * LP]
-    R *sre = scf + LPH * LP, *sim = sre + NG * 128;
+    R *scr = (R *)(sO + 216 * LP);               // [LPH][LP] coefficient for Re H
+    R *sci = scr + LPH * LP;                     // [LPH][LP] coefficient for Im H (conjugation folded in)
+    R *sre = sci + LPH * LP;                     // [M2L_G][8][LPH]
+    R *sim = sre + M2L_G * 8 * LPH;
+    int *sh = (int *)(sim + M2L_G * 8 * LPH);    // [LPH][LP] index of H
     const int p = blockIdx.x;
     const Rep r = d.rep[prep[p]];
     const int div = level == 4 ? 1 : 2;          // child grid = nc / div
@@ -818,43 +818,68 @@ __global__ void __launch_bounds__(128 * M2LCfg<R>::NG) k_m2l_win(Dev d, const do
         }
         sO[idx] = v;
     }
-    for (int idx = threadIdx.x; idx < LPH * LP; idx += blockDim.x) scf[idx] = cf[idx];
+    for (int idx = threadIdx.x; idx < LPH * LP; idx += blockDim.x) {
+        const int o = idx / LP, nm = idx % LP;
+        int j, k;
+        out_jk(o, j, k);
+        const int nn = nm < 1 ? 0 : nm < 4 ? 1 : nm < 9 ? 2 : nm < 16 ? 3 : 4;
+        const int m = nm - nn * (nn + 1);
+        const int ll = j + nn, q = m - k;
+        const R c = cf[idx];
+        sh[idx] = ll * (ll + 1) / 2 + (q < 0 ? -q : q);
+        scr[idx] = c;
+        sci[idx] = q < 0 ? -c : c;
+    }
     __syncthreads();
-    const int g = threadIdx.x >> 7, u = threadIdx.x & 127;
-    const bool act = u < 8 * LPH;
-    const int t = u / LPH, o = u % LPH;
-    // this child's position in the window (2 or 3 per axis) and in the grid
-    const int lc[3] = {2 + (t & 1), 2 + ((t >> 1) & 1), 2 + ((t >> 2) & 1)};
-    const int gc[3] = {w0[0] + lc[0], w0[1] + lc[1], w0[2] + lc[2]};
-    R re = 0, im = 0;
-    if (act) {
-        int h[LP];
-        R cr[LP], ci[LP];
-        m2l_terms<R>(o, scf, h, cr, ci);
-        for (int oi = g; oi < 343; oi += NG) {
-            const int dx = oi % 7 - 3, dy = (oi / 7) % 7 - 3, dz = oi / 49 - 3;
-            if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-            const int sx = lc[0] + dx, sy = lc[1] + dy, sz = lc[2] + dz;
+    const int o = threadIdx.x % LPH, g = threadIdx.x / LPH;
+    R are[8], aim[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) are[t] = aim[t] = R(0);
+    for (int oi = g; oi < 343; oi += M2L_G) {
+        const int dx = oi % 7 - 3, dy = (oi / 7) % 7 - 3, dz = oi / 49 - 3;
+        if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+        const C2<R> *H = Htab + (size_t)oi * NH;
+        R t1[LP], t2[LP];
+#pragma unroll
+        for (int nm = 0; nm < LP; nm++) {
+            const C2<R> hv = H[sh[o * LP + nm]];
+            t1[nm] = scr[o * LP + nm] * hv.x;
+            t2[nm] = sci[o * LP + nm] * hv.y;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            // child t sits at window position 2 + (t bits) per axis
+            const int sx = 2 + (t & 1) + dx, sy = 2 + ((t >> 1) & 1) + dy, sz = 2 + ((t >> 2) & 1) + dz;
             if (sx < 0 || sy < 0 || sz < 0 || sx > 5 || sy > 5 || sz > 5) continue;
-            if (gc[0] + dx < 0 || gc[1] + dy < 0 || gc[2] + dz < 0 || gc[0] + dx >= n[0] || gc[1] + dy >= n[1] ||
-                gc[2] + dz >= n[2])
-                continue;
-            m2l_acc<R>(Htab + (size_t)oi * NH, sO + (size_t)(sx + 6 * (sy + 6 * sz)) * LP, h, cr, ci, re, im);
+            const int gx = w0[0] + sx, gy = w0[1] + sy, gz = w0[2] + sz;
+            if (gx < 0 || gy < 0 || gz < 0 || gx >= n[0] || gy >= n[1] || gz >= n[2]) continue;
+            const C2<R> *src = sO + (size_t)(sx + 6 * (sy + 6 * sz)) * LP;
+            R re = are[t], im = aim[t];
+#pragma unroll
+            for (int nm = 0; nm < LP; nm++) {
+                const C2<R> mv = src[nm];
+                re += t1[nm] * mv.x - t2[nm] * mv.y;
+                im += t1[nm] * mv.y + t2[nm] * mv.x;
+            }
+            are[t] = re;
+            aim[t] = im;
         }
     }
-    sre[threadIdx.x] = re;
-    sim[threadIdx.x] = im;
+#pragma unroll
+    for (int t = 0; t < 8; t++) {
+        sre[(g * 8 + t) * LPH + o] = are[t];
+        sim[(g * 8 + t) * LPH + o] = aim[t];
+    }
     __syncthreads();
-    if (g == 0 && act) {
+    if (threadIdx.x < 8 * LPH) {
+        const int t = threadIdx.x / LPH, oo = threadIdx.x % LPH;
         R a = 0, b = 0;
-        for (int q = 0; q < NG; q++) { a += sre[q * 128 + u]; b += sim[q * 128 + u]; }
+        for (int q = 0; q < M2L_G; q++) { a += sre[(q * 8 + t) * LPH + oo]; b += sim[(q * 8 + t) * LPH + oo]; }
+        const int gc[3] = {w0[0] + 2 + (t & 1), w0[1] + 2 + ((t >> 1) & 1), w0[2] + 2 + ((t >> 2) & 1)};
         const int child = base + gc[0] + n[0] * (gc[1] + n[1] * gc[2]);
-        store_jk(L + (size_t)child * LP, o, (double)a, (double)b, true);
+        store_jk(L + (size_t)child * LP, oo, (double)a, (double)b, true);
     }
 }
-
-template <typename R>
-size_t m2l_smem() { return sizeof(C2<R>) * 216 * LP + sizeof(R) * (LPH * LP + 2 * M2LCfg<R>::NG * 128); }
 
 // M2L at L2 over all non-adjacent L2 boxes of the replica (src/computeLjk2.f90:17-72):
 // one CTA per target box, 15 outputs x 8 source groups, reduced in a fixed order
@@ -912,10 +937,10 @@ void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2
         k_m2m<float><<<n2, 128, 0, st>>>(d, d.O3, d.O2, d.op32_m2m32, d.b2rep, 2);
         k_m2l_all<float><<<n2, 128, 0, st>>>(d, (const C2<float> *)d.h32_m2l2, d.m2l_cf32, d2);
         k_l2l<float><<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op32_l2l23, d.b3rep, 3);
-        k_m2l_win<float><<<n2, 128 * M2LCfg<float>::NG, m2l_smem<float>(), st>>>(
+        k_m2l_win<float><<<n2, M2L_THREADS, m2l_smem<float>(), st>>>(
             d, d.O3, d.L3, (const C2<float> *)d.h32_m2l3, d.m2l_cf32, d.b2rep, 3);
         k_l2l<float><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op32_l2l34, d.crep, 4);
-        k_m2l_win<float><<<n3, 128 * M2LCfg<float>::NG, m2l_smem<float>(), st>>>(
+        k_m2l_win<float><<<n3, M2L_THREADS, m2l_smem<float>(), st>>>(
             d, d.O4, d.L4, (const C2<float> *)d.h32_m2l4, d.m2l_cf32, d.b3rep, 4);
     } else {
         k_p2m<double><<<ncell, 64, 0, st>>>(d);
@@ -923,10 +948,10 @@ void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2
         k_m2m<double><<<n2, 128, 0, st>>>(d, d.O3, d.O2, d.op_m2m32, d.b2rep, 2);
         k_m2l_all<double><<<n2, 128, 0, st>>>(d, (const C2<double> *)d.h_m2l2, d.m2l_cf, d2);
         k_l2l<double><<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
-        k_m2l_win<double><<<n2, 128 * M2LCfg<double>::NG, m2l_smem<double>(), st>>>(
+        k_m2l_win<double><<<n2, M2L_THREADS, m2l_smem<double>(), st>>>(
             d, d.O3, d.L3, (const C2<double> *)d.h_m2l3, d.m2l_cf, d.b2rep, 3);
         k_l2l<double><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
-        k_m2l_win<double><<<n3, 128 * M2LCfg<double>::NG, m2l_smem<double>(), st>>>(
+        k_m2l_win<double><<<n3, M2L_THREADS, m2l_smem<double>(), st>>>(
             d, d.O4, d.L4, (const C2<double> *)d.h_m2l4, d.m2l_cf, d.b3rep, 4);
     }
 }
