@@ -67,9 +67,9 @@ typedef struct orc_sys {
     /* per cell atom lists (src/mybox.cmns:152-167) */
     orc_list *W2C, *W226, *W2nC, *W2n26, *W2nn;
     orc_list *SC, *S26, *SnC, *Sn26, *SnnC, *Snn26, *Snnn;
-    /* isub: per surfactant site 28 slots, 0-terminated (src/mybox.cmns:201) */
+    /* isub: per surfactant site 28 slots, 0-terminated (src/mybox.cmns:187) */
     int *isub;
-    /* FMA coefficients (src/mybox.cmns:204-205) */
+    /* FMA coefficients (src/mybox.cmns:189-190) */
     double complex *cO4, *cO3, *cO2, *cL4, *cL3, *cL2;
     /* graphite (fixed carbons) */
     int nc;

@@ -22,7 +22,7 @@ static inline double neg1pow(int n) { return (n % 2 == 0) ? 1.0 : -1.0; }
 
 /* Associated Legendre function with the Condon-Shortley phase, restated from
  * its standard three-term recurrence in l (P_m^m, P_{m+1}^m, then upward).
- * Conventions of src/rLegendreP.f90:109-118: P(-1,0) = 1 and P(l,m) = 0 for m > l. */
+ * Conventions of src/rLegendreP.f90:11-19: P(-1,0) = 1 and P(l,m) = 0 for m > l. */
 static double legendre(int l, int m, double x) {
     if (l == -1 && m == 0) return 1.0;
     if (m > l) return 0.0;
@@ -146,7 +146,7 @@ static void m2l(const double complex *O, double dx, double dy, double dz, double
 }
 
 /* M2M of child coefficients O at vector d (child centre - parent centre)
- * into the parent's Op, src/computeOnm3.f90:197-238 */
+ * into the parent's Op, src/computeOnm3.f90:47-94 */
 static void m2m(const double complex *O, double dx, double dy, double dz, double complex *Op) {
     double rho, al, be;
     sph(dx, dy, dz, &rho, &al, &be);
@@ -166,7 +166,7 @@ static void m2m(const double complex *O, double dx, double dy, double dz, double
 }
 
 /* L2L of parent coefficients L at vector d (parent centre - child centre)
- * into the child's Lc, src/shiftLjk3.f90:189-221 */
+ * into the child's Lc, src/shiftLjk3.f90:44-87 */
 static void l2l(const double complex *L, double dx, double dy, double dz, double complex *Lc) {
     double rho, al, be;
     sph(dx, dy, dz, &rho, &al, &be);
@@ -220,7 +220,7 @@ void orc_fma_build(orc_sys *s) {
     free(site); free(q); free(rho); free(al); free(be);
     }
 
-    /* M2M L4 -> L3, src/computeOnm3.f90:173-244 (each parent on its own) */
+    /* M2M L4 -> L3, src/computeOnm3.f90:27-98 (each parent on its own) */
 #pragma omp parallel for schedule(static)
     for (int z3 = 0; z3 < n3z; z3++)
         for (int y3 = 0; y3 < n3y; y3++)
@@ -269,7 +269,7 @@ void orc_fma_build(orc_sys *s) {
                     m2l(&s->cO2[(size_t)LP * l], cl[0] - c2[0], cl[1] - c2[1], cl[2] - c2[2], &s->cL2[(size_t)LP * rank]);
                 }
     }
-    /* L2L L2 -> L3, src/shiftLjk2.f90:89-135 */
+    /* L2L L2 -> L3, src/shiftLjk2.f90:16-60 */
 #pragma omp parallel for schedule(dynamic, 1)
     for (int rank = 0; rank < s->nrank; rank++) {
         int rx, ry, rz;
@@ -284,7 +284,7 @@ void orc_fma_build(orc_sys *s) {
             l2l(&s->cL2[(size_t)LP * rank], c2[0] - c3[0], c2[1] - c3[1], c2[2] - c3[2], &s->cL3[(size_t)LP * l3]);
         }
     }
-    /* M2L at L3 over the 6^3 window, src/computeLjk3.f90:220-277 */
+    /* M2L at L3 over the 6^3 window, src/computeLjk3.f90:45-102 */
 #pragma omp parallel for schedule(dynamic, 1)
     for (int rank = 0; rank < s->nrank; rank++) {
         int rx, ry, rz;
@@ -308,7 +308,7 @@ void orc_fma_build(orc_sys *s) {
                     }
         }
     }
-    /* L2L L3 -> L4, src/shiftLjk3.f90:154-229 */
+    /* L2L L3 -> L4, src/shiftLjk3.f90:27-91 */
 #pragma omp parallel for schedule(static)
     for (int z3 = 0; z3 < n3z; z3++)
         for (int y3 = 0; y3 < n3y; y3++)

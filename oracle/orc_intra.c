@@ -186,7 +186,7 @@ static inline double intra_pair(orc_sys *s, int gj, int gk, int jt, int kt, int 
     return qq / rctr + 4.0 * eps * (sg6 * sg6 * r6 * r6 - sg6 * r6);
 }
 
-/* src/eval_surfactant_internal.f90:148-248: sites j = 1..15 with k >= j+4,
+/* src/eval_surfactant_internal.f90:17-110: sites j = 1..15 with k >= j+4,
  * then the 42 listed pairs; LJ without cutoff */
 static double internal_mol(orc_sys *s, int g0, int do_force) {
     double e = 0.0;
@@ -248,10 +248,10 @@ static double wall_energy(const orc_sys *s) {
     return e;
 }
 
-/* src/eval_graphite.f90:60-194: LJ against the fixed carbons within rc, for
+/* src/eval_graphite.f90:13-132: LJ against the fixed carbons within rc, for
  * water O (w1 and split) and for surfactant sites Central in their own key
  * cell, only in the bottom layer of cells.  Carbons are taken per cell column
- * as src/read_graphite.f90:187-216 pre-filters them. */
+ * as src/read_graphite.f90:9-35 pre-filters them. */
 static double graphite_site(orc_sys *s, int g, double eps, double sg6, double cx, double cy, int do_force) {
     double e = 0.0;
     double rcut = (ORC_RC + sqrt(2.0) * ORC_RS / 2.0);

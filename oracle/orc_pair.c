@@ -158,7 +158,7 @@ static void evalw1w2n(orc_sys *s) {
     }
 }
 
-/* src/evalw1w2nn.f90:102-139 */
+/* src/evalw1w2nn.f90:12-49 */
 static void evalw1w2nn(orc_sys *s) {
     #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) w1_vs_list(s, c, &s->W2nn[c], 1, 1, 0);
@@ -229,7 +229,7 @@ static inline int same_mol(const orc_ent *a, const orc_ent *b) { return a->mol =
 
 /* ---- split water (w2) i side ---- */
 
-/* src/evalw2w2.f90:129-226 */
+/* src/evalw2w2.f90:14-112 */
 static void evalw2w2(orc_sys *s) {
     #pragma omp for schedule(static, 1)
     for (int c = 0; c < s->ncell; c++) {

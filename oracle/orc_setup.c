@@ -166,7 +166,7 @@ void orc_rank_xyz(const orc_sys *s, int rank, int *rx, int *ry, int *rz) {
     *rx = rank % s->nrx; *ry = (rank / s->nrx) % s->nry; *rz = rank / (s->nrx * s->nry);
 }
 
-/* ibox2 - 1, src/ibox.f90:300-312 */
+/* ibox2 - 1, src/ibox.f90:127-139 */
 int orc_rank_of(const orc_sys *s, double x, double y, double z) {
     int ix = (int)((x + s->rhsx) * s->nrx / s->rsdx);
     int iy = (int)((y + s->rhsy) * s->nry / s->rsdy);
@@ -189,7 +189,7 @@ void orc_rcen2(const orc_sys *s, int rank, double *cx, double *cy, double *cz) {
 
 static int clamp4(int v) { return v < 0 ? 0 : (v > 3 ? 3 : v); }
 
-/* ibox64 - 1, src/ibox.f90:345-359 (result clamped to the rank's 4x4x4 cells) */
+/* ibox64 - 1, src/ibox.f90:172-186 (result clamped to the rank's 4x4x4 cells) */
 int orc_local64(const orc_sys *s, int rank, double x, double y, double z) {
     double cx, cy, cz;
     orc_rcen2(s, rank, &cx, &cy, &cz);
@@ -230,19 +230,19 @@ void orc_rcen4(const orc_sys *s, int c, double *cx, double *cy, double *cz) {
     *cz = 4.0 * rs * k / 4.0 - 2.0 * rs - 4.0 * rs / 8.0 + c2z;
 }
 
-/* src/ibox.f90:274-297 */
+/* src/ibox.f90:101-124 */
 int orc_isCentral(double x, double y, double z, double cx, double cy, double cz) {
     double rs2 = ORC_RS / 2.0;
     return (x < cx + rs2 && x >= cx - rs2) && (y < cy + rs2 && y >= cy - rs2) && (z < cz + rs2 && z >= cz - rs2);
 }
 
-/* src/ibox.f90:248-271 */
+/* src/ibox.f90:75-98 */
 int orc_isNearest(double x, double y, double z, double cx, double cy, double cz) {
     double r15 = 1.5 * ORC_RS;
     return (x < cx + r15 && x >= cx - r15) && (y < cy + r15 && y >= cy - r15) && (z < cz + r15 && z >= cz - r15);
 }
 
-/* neighbour order kmid(1..26), src/buildW2n.f90:98-111 */
+/* neighbour order kmid(1..26), src/buildW2n.f90:24-37 */
 const int ORC_KMID[26][3] = {
     {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {-1, 1, 0}, {-1, 0, 0}, {-1, -1, 0}, {0, -1, 0}, {1, -1, 0},
     {1, 0, 1}, {1, 1, 1}, {0, 1, 1}, {-1, 1, 1}, {-1, 0, 1}, {-1, -1, 1}, {0, -1, 1}, {1, -1, 1},
@@ -407,9 +407,9 @@ void orc_build_lists(orc_sys *s) {
     }
 }
 
-/* src/buildinternal.f90:59-121: per surfactant site, the sites of its own
+/* src/buildinternal.f90:13-63: per surfactant site, the sites of its own
  * molecule outside the 27-cell block of the site's cell (10^3 grid of the
- * key rank, ibox1000 and rcen1000 at src/ibox.f90:379-393,
+ * key rank, ibox1000 and rcen1000 at src/ibox.f90:206-220,
  * src/init_box_dimensions.f90:155-170). */
 void orc_buildinternal(orc_sys *s) {
     memset(s->isub, 0, sizeof(int) * 28 * ORC_NSURF_SITE * (size_t)s->ns);

@@ -13,7 +13,7 @@ void upload_tables_exact(const Tables &t, cudaStream_t st) {
     cudaMemcpyToSymbolAsync(cT, &t, sizeof(Tables), 0, cudaMemcpyHostToDevice, st);
 }
 
-// ibox2 - 1 along one axis, src/ibox.f90:300-312
+// ibox2 - 1 along one axis, src/ibox.f90:127-139
 __device__ inline int rank_axis(const Rep &r, int a, double v) {
     int k = (int)((v + r.rhs[a]) * r.nr[a] / r.rsd[a]);
     return k < 0 ? 0 : (k >= r.nr[a] ? r.nr[a] - 1 : k);
@@ -23,7 +23,7 @@ __device__ inline double rcen2_axis(const Rep &r, int a, int rk) {
     double b = (double)r.nr[a];
     return r.rsd[a] * (rk + 1) / b - r.rhs[a] - r.rsd[a] / b / 2.0;
 }
-// ibox64 along one axis relative to a rank centre, src/ibox.f90:345-359
+// ibox64 along one axis relative to a rank centre, src/ibox.f90:172-186
 __device__ inline int local_axis(double v, double c2) {
     int k = (int)((v - c2 + 2.0 * RS) / RS);
     return k < 0 ? 0 : (k > 3 ? 3 : k);
@@ -33,7 +33,7 @@ __device__ inline int key_axis(const Rep &r, int a, double v, int *rk) {
     *rk = rank_axis(r, a, v);
     return 4 * (*rk) + local_axis(v, rcen2_axis(r, a, *rk));
 }
-// isCentral along one axis (src/ibox.f90:274-297): the cell whose
+// isCentral along one axis (src/ibox.f90:101-124): the cell whose
 // [centre - rs/2, centre + rs/2) holds v, -1 if none
 __device__ inline int central_axis(const double *cen, int n, double v, double rhs) {
     int k0 = (int)floor((v + rhs) / RS);
@@ -97,8 +97,8 @@ __global__ void k_locate(Dev d, int nmol) {
 }
 
 // Sites of each surfactant that lie outside the 27-cell block of a site's
-// own cell (src/buildinternal.f90:71-121); cells on the 10^3 grid of the
-// key rank (ibox1000, rcen1000: src/ibox.f90:379-393,
+// own cell (src/buildinternal.f90:13-63); cells on the 10^3 grid of the
+// key rank (ibox1000, rcen1000: src/ibox.f90:206-220,
 // src/init_box_dimensions.f90:155-170).  One thread per surfactant site.
 __global__ void k_isub(Dev d, int nsurf_sites, const int *surf_mol_of) {
     int t = blockIdx.x * blockDim.x + threadIdx.x;

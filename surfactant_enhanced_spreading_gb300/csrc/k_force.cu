@@ -661,7 +661,7 @@ __device__ inline void store_jk(double2 *L, int o, double re, double im, bool ad
     if (k > 0) L[j * (j + 1) - k] = make_double2(v.x, -v.y);
 }
 
-// M2M, src/computeOnm3.f90:173-244 and src/computeOnm2.f90:13-62: parent box
+// M2M, src/computeOnm3.f90:27-98 and src/computeOnm2.f90:13-62: parent box
 // from its 8 children (level 4 -> 3 or 3 -> 2)
 template <typename R, typename OP>
 __device__ inline void apply_op_r(const OP *op, const double2 *in, R &re, R &im) {
@@ -707,7 +707,7 @@ __global__ void __launch_bounds__(128) k_m2m(Dev d, const double2 *Oc, double2 *
     }
 }
 
-// L2L, src/shiftLjk2.f90:89-135 and src/shiftLjk3.f90:154-229: child box
+// L2L, src/shiftLjk2.f90:16-60 and src/shiftLjk3.f90:27-91: child box
 // from its parent (level 2 -> 3 or 3 -> 4)
 template <typename R, typename OP>
 __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, const int *brep, int level) {
@@ -961,7 +961,7 @@ void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2
 __device__ inline double pow13(double v) { double v2 = v * v, v4 = v2 * v2, v8 = v4 * v4; return v8 * v4 * v; }
 __device__ inline double pow12(double v) { double v2 = v * v, v4 = v2 * v2, v8 = v4 * v4; return v8 * v4; }
 
-// graphite LJ of one site over its column's carbons (src/eval_graphite.f90:80-185)
+// graphite LJ of one site over its column's carbons (src/eval_graphite.f90:104-126)
 __device__ inline void graphite_site(const Dev &d, int col, double x, double y, double z, double eps, double sg6,
                                      double &fx, double &fy, double &fz, double *e) {
     const double rc2 = RC * RC;
@@ -980,7 +980,7 @@ __device__ inline void graphite_site(const Dev &d, int col, double x, double y, 
 
 // graphite acts on LJ sites that sit in their molecule's key cell in the
 // bottom layer of cells: water O (w1 and split) and surfactant sites in
-// SCentral (src/eval_graphite.f90:72-187)
+// SCentral (src/eval_graphite.f90:13-132)
 __device__ inline int graphite_column(const Dev &d, const Rep &r, int g, double &eps, double &sg6) {
     if (!r.graphite_on) return -1;
     int pt = d.ptype[g];
@@ -1022,7 +1022,7 @@ __global__ void k_graphite_list(Dev d, int nsite) {
     if (graphite_column(d, r, g, eps, sg6) >= 0) d.gsite[atomicAdd(d.gcount, 1)] = g;
 }
 
-// graphite LJ (src/eval_graphite.f90:80-185), one warp per listed site: the
+// graphite LJ (src/eval_graphite.f90:104-126), one warp per listed site: the
 // lanes split the column's carbons and a fixed shuffle tree sums them.
 // FP32 (mixed path): site and carbons relative to the column centre, so each
 // carbon costs FP32 arithmetic only.
@@ -1216,7 +1216,7 @@ __device__ R dihedral_term(const Pos29<R> &m, int i, R f[4][3]) {
 }
 
 // one intramolecular nonbonded pair, Coulomb + LJ without cutoff
-// (src/eval_surfactant_internal.f90:169-200, 206-242)
+// (src/eval_surfactant_internal.f90:33-66, 70-108)
 template <typename R>
 __device__ inline R ipair_term(const Dev &d, const Pos29<R> &m, int a, int b, R f[2][3]) {
     R x = m.x[a] - m.x[b], y = m.y[a] - m.y[b], z = m.z[a] - m.z[b];

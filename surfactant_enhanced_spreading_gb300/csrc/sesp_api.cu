@@ -123,7 +123,7 @@ Tables make_tables() {
                               {22, 28}, {22, 29}, {23, 25}, {23, 26}, {23, 27}, {23, 28}, {23, 29}, {24, 25}, {24, 26}, {24, 27},
                               {24, 28}, {24, 29}};
     for (int k = 0; k < NSELF; k++) { T.si[k] = sp[k][0] - 1; T.sj[k] = sp[k][1] - 1; }
-    // graphite (src/eval_graphite.f90:69-70, src/init_arrays.f90:503-506)
+    // graphite (src/eval_graphite.f90:10-11, src/init_arrays.f90:512-515)
     double sgs[NSURF], eps[NSURF];
     surf_lj(sgs, eps);
     for (int i = 0; i < NSURF; i++) {
@@ -266,7 +266,7 @@ void m2l_coef(double *cf) {
                     cf[oidx(j, k) * LP + cidx(n, m)] =
                         iIkm2(k, m) * rAnm(j, k) * rAnm(n, m) / (sgn(n) * rAnm(j + n, m - k));
 }
-// M2M operator at child - parent vector d, src/computeOnm3.f90:207-228
+// M2M operator at child - parent vector d, src/computeOnm3.f90:51-81
 void op_m2m(double x, double y, double z, double2 *op) {
     double rho, al, be;
     sph(x, y, z, rho, al, be);
@@ -282,7 +282,7 @@ void op_m2m(double x, double y, double z, double2 *op) {
                     o.x += c.real(); o.y += c.imag();
                 }
 }
-// L2L operator at parent - child vector d, src/shiftLjk3.f90:193-221
+// L2L operator at parent - child vector d, src/shiftLjk3.f90:46-76
 void op_l2l(double x, double y, double z, double2 *op) {
     double rho, al, be;
     sph(x, y, z, rho, al, be);
@@ -642,7 +642,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         for (int k = 0; k < cc / 64; k++) b2[r.l2_0 + k] = q;
         size_t a0 = axis.size();
         for (int a = 0; a < 3; a++) axis_centres(r, a, axis);
-        // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:187-216
+        // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:9-35
         for (int iy = 0; iy < r.nc[1]; iy++)
             for (int ix = 0; ix < r.nc[0]; ix++) {
                 double cx = axis[a0 + ix], cy = axis[a0 + r.nc[0] + iy], cz = axis[a0 + r.nc[0] + r.nc[1]];

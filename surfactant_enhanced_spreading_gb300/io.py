@@ -8,7 +8,7 @@ in sigma; on reading the reference adds exp(-9) to every coordinate (so no
 site lies exactly on a cell face).  A velocity is stored as v / 0.01 + 0.5
 (v in sigma per step) and read back as (stored - 0.5) * 0.01.
 
-Snapshots (src/write_pdb.f90:19-170): HETATM records
+Snapshots (src/write_pdb.f90:19-169): HETATM records
 `(a6,i5,a5,a4,i6,f12.3,f8.3,f8.3)` with coordinates in Angstrom; waters go
 33,333 molecules per file named data<7-digit step><a, b, ...>.pdb, the
 surfactants into data<7-digit step>s.pdb.
@@ -91,7 +91,7 @@ def read_config(path: str, n_water: int, n_surf: int, box_half: np.ndarray | Non
 
 
 def pdb_stem(step: int) -> str:
-    """data<step as 7 digits, zero padded> (src/write_pdb.f90:26-68)."""
+    """data<step as 7 digits, zero padded> (src/write_pdb.f90:25-69)."""
     return "data" + str(int(step)).zfill(7)[-7:]
 
 

@@ -3,7 +3,7 @@
 The reference reads its initial state from ``data_cont2.dat`` (alternating
 position / velocity lines, waters O,H,H first, then 29-site surfactants,
 src/read_config.f90:16-38) and its carbons from ``graphite.dat``
-(src/read_graphite.f90:179-216), neither of which ships with it.  This module
+(src/read_graphite.f90:19-33), neither of which ships with it.  This module
 builds such states from a seed:
 
 * a hemispherical droplet of rigid 3-site waters (O-H 1 A, H-O-H 109.47 deg,
@@ -202,7 +202,7 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
 
     The top carbon layer sits 4 A above the lower wall, inside the bottom
     layer of cells, so the graphite term (bottom cells only,
-    src/eval_graphite.f90:72-74) acts on the first water layer.
+    src/eval_graphite.f90:13-15) acts on the first water layer.
     """
     rng = np.random.default_rng(seed)
     cells = tuple(int(c) for c in cells)
