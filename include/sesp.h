@@ -195,6 +195,32 @@ int sesp_energies_static(sesp_ctx *ctx, double out[8]);
  * overflows, [2] sites in no cell, [3] steps done, [4] max sites in a cell,
  * [5] near-field ordered pairs of the last rebuild, [6] LJ-eligible pairs */
 int sesp_counters(sesp_ctx *ctx, int64_t out[8]);
+/* The reference's consistency checks, from the cell lists of the last force
+ * call, 8 values per replica (out holds 8 x sesp_replica_count):
+ *   [0] molecules whose sites all lie in a cell, [1] molecules uploaded,
+ *   [2] total charge of the sites in cells, [3] water O in cells,
+ *   [4] water H in cells, [5] waters uploaded, [6] sites in no cell,
+ *   [7] the warning bits of sesp_check_flags.
+ * Replaces the counts and messages of get_molecule_count
+ * (src/get_molecule_count.f90:16-57: "MOLECULES LOST") and of computeOnm4
+ * (src/computeOnm4.f90:18-212: total charge, O:H ratio, missing oxygen),
+ * which print and carry on. */
+int sesp_checks(sesp_ctx *ctx, double *out);
+#define SESP_CHECK_MOLECULES_LOST 1   /* [0] != [1] */
+#define SESP_CHECK_CHARGE 2           /* [2]^2 > 0.001 */
+#define SESP_CHECK_OH_RATIO 4         /* integer [4] / [3] != 2 (H without O counts too) */
+#define SESP_CHECK_MISSING_OXYGEN 8   /* [3] != [5] */
+/* Warning bits of one replica's counts c[0..6] (layout of sesp_checks); a
+ * host function, no GPU needed (src/get_molecule_count.f90:57,
+ * src/computeOnm4.f90:210-212). */
+int sesp_check_flags(const double c[7]);
+/* Velocities scaled by sqrt(target / T), T the temperature of
+ * sesp_temperature before the call (returned in t_before unless null);
+ * src/compute_temperature.f90's rescaling variant
+ * (src/compute_temperature_rescale.f90:242-276) with its target 3.9 as
+ * SESP_RESCALE_TARGET.  SESP_EINVAL unless target > 0 and T > 0. */
+#define SESP_RESCALE_TARGET 3.9
+int sesp_rescale_temperature(sesp_ctx *ctx, double target, double *t_before);
 /* average device time in ms per launch of each kernel family since the last
  * reset, measured with CUDA events on the engine's stream:
  * [0] near field, [1] local-expansion force, [2] move_a, [3] move_b,

@@ -156,6 +156,23 @@ module sesp_mod
       type(c_ptr), value :: ctx
       integer(c_int64_t), intent(out) :: c(8)
     end function
+    ! get_molecule_count and computeOnm4 checks, 8 values per replica
+    integer(c_int) function sesp_checks(ctx, c) bind(C, name="sesp_checks")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: c(*)
+    end function
+    integer(c_int) function sesp_check_flags(c) bind(C, name="sesp_check_flags")
+      import :: c_int, c_double
+      real(c_double), intent(in) :: c(7)
+    end function
+    ! compute_temperature_rescale: v = sqrt(target / T) v (the reference's target is 3.9)
+    integer(c_int) function sesp_rescale_temperature(ctx, target, t_before) bind(C, name="sesp_rescale_temperature")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), value :: target
+      real(c_double), intent(out) :: t_before
+    end function
     integer(c_int) function sesp_kernel_times(ctx, t, reset) bind(C, name="sesp_kernel_times")
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: ctx

@@ -1259,6 +1259,111 @@ int sesp_counters(sesp_ctx *c, int64_t out[8]) {
     return 0;
 }
 
+}  // extern "C"
+
+namespace {
+
+constexpr int CHECK_THREADS = 256;
+
+// The counts of sesp_checks for one replica per block: molecules located
+// whole, charge of the slots (srt_pos.w = q of the site), water O / H and
+// unlocated sites.  Each thread strides over its share, then one fixed tree
+// sums the block, so the charge total does not depend on timing.
+__global__ void k_checks(Dev d, double *out) {
+    __shared__ double s_q[CHECK_THREADS];
+    __shared__ long long s_n[4][CHECK_THREADS];
+    const Rep r = d.rep[blockIdx.x];
+    const int t = threadIdx.x;
+    long long mol_ok = 0, n_o = 0, n_h = 0, n_out = 0;
+    double q = 0.0;
+    for (int m = t; m < r.nmol; m += CHECK_THREADS) {
+        const int g0 = d.mfirst[r.mol0 + m];
+        const int ns = d.mkind[r.mol0 + m] == 0 ? 3 : NSURF;
+        int ok = 1;
+        for (int k = 0; k < ns; k++) ok &= d.sloc[g0 + k] >= 0;
+        mol_ok += ok;
+    }
+    for (int g = r.site0 + t; g < r.site0 + r.nsite; g += CHECK_THREADS) {
+        if (d.sloc[g] < 0) { n_out++; continue; }
+        const int pt = d.ptype[g];
+        n_o += pt == 0;
+        n_h += pt == 1;
+    }
+    const int s0 = d.cstart[r.cell0], s1 = d.cstart[r.cell0 + r.nc[0] * r.nc[1] * r.nc[2]];
+    for (int s = s0 + t; s < s1; s += CHECK_THREADS) q += d.srt_pos[s].w;
+    s_q[t] = q;
+    s_n[0][t] = mol_ok; s_n[1][t] = n_o; s_n[2][t] = n_h; s_n[3][t] = n_out;
+    __syncthreads();
+    for (int w = CHECK_THREADS / 2; w > 0; w >>= 1) {
+        if (t < w) {
+            s_q[t] += s_q[t + w];
+            for (int k = 0; k < 4; k++) s_n[k][t] += s_n[k][t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+        double *o = out + 8 * (size_t)blockIdx.x;
+        o[0] = (double)s_n[0][0]; o[1] = (double)r.nmol; o[2] = s_q[0];
+        o[3] = (double)s_n[1][0]; o[4] = (double)s_n[2][0]; o[5] = (double)r.nw;
+        o[6] = (double)s_n[3][0]; o[7] = 0.0;
+    }
+}
+
+__global__ void k_scale_velocities(Dev d, int nsite, double f) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nsite) return;
+    d.vx[g] = f * d.vx[g]; d.vy[g] = f * d.vy[g]; d.vz[g] = f * d.vz[g];
+}
+
+}  // namespace
+
+extern "C" {
+
+int sesp_check_flags(const double c[7]) {
+    if (!c) return 0;
+    int f = 0;
+    if (c[0] != c[1]) f |= SESP_CHECK_MOLECULES_LOST;
+    if (c[2] * c[2] > 0.001) f |= SESP_CHECK_CHARGE;
+    const long long n_o = (long long)c[3], n_h = (long long)c[4];
+    // the reference divides H by O as integers; with no O it would divide by
+    // zero, here H without O is flagged and an empty system is not
+    if (n_o > 0 ? n_h / n_o != 2 : n_h != 0) f |= SESP_CHECK_OH_RATIO;
+    if (c[3] != c[5]) f |= SESP_CHECK_MISSING_OXYGEN;
+    return f;
+}
+
+int sesp_checks(sesp_ctx *c, double *out) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    if (!c->have_force) return fail(SESP_ESTATE, "checks need a force call first (cell lists)");
+    if (set_device(c)) return SESP_ECUDA;
+    double *dout = nullptr;
+    CK(cudaMallocAsync((void **)&dout, 8 * sizeof(double) * c->nrep, c->st));
+    k_checks<<<c->nrep, CHECK_THREADS, 0, c->st>>>(c->d, dout);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, 8 * sizeof(double) * c->nrep, cudaMemcpyDeviceToHost, c->st);
+    cudaFreeAsync(dout, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) return fail(SESP_ECUDA, "sesp_checks: %s", cudaGetErrorString(e));
+    for (int q = 0; q < c->nrep; q++) out[8 * q + 7] = (double)sesp_check_flags(out + 8 * q);
+    return 0;
+}
+
+int sesp_rescale_temperature(sesp_ctx *c, double target, double *t_before) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!(target > 0.0)) return fail(SESP_EINVAL, "target temperature %g is not positive", target);
+    double t = 0.0;
+    if (int e = sesp_temperature(c, &t)) return e;
+    if (!(t > 0.0)) return fail(SESP_EINVAL, "temperature %g cannot be rescaled", t);
+    if (set_device(c)) return SESP_ECUDA;
+    const double f = sqrt(target / t);   // tscale, src/compute_temperature_rescale.f90:243
+    k_scale_velocities<<<(c->nsite + 255) / 256, 256, 0, c->st>>>(c->d, c->nsite, f);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+    if (t_before) *t_before = t;
+    return 0;
+}
+
 int sesp_kernel_times(sesp_ctx *c, double out[8], int reset) {
     if (int e = check_ctx(c, false)) return e;
     if (!out) return fail(SESP_EINVAL, "null output");

@@ -20,6 +20,9 @@ LIB_PATH = os.path.join(_HERE, "libsesp.so")
 PLAIN_FP64 = 0
 MIXED = 1          # FP32 force arithmetic, FP64 constraint iterations
 MIXED_FP32C = 2    # MIXED with FP32 constraint iterations
+# warning bits of Engine.checks (sesp_check_flags)
+CHECK_MOLECULES_LOST, CHECK_CHARGE, CHECK_OH_RATIO, CHECK_MISSING_OXYGEN = 1, 2, 4, 8
+RESCALE_TARGET = 3.9   # target of the reference's temperature-rescaling variant
 
 T_NEAR, T_FAR, T_VALENCE, T_DIHEDRAL, T_BERENDSEN = 1, 2, 4, 8, 16
 T_INTERNAL, T_SUBTRACT, T_WALL, T_GRAPHITE, T_ALL = 32, 64, 128, 256, 511
@@ -33,7 +36,8 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_run_async", "sesp_sync", "sesp_temperature", "sesp_get_eta", "sesp_set_eta", "sesp_energies",
            "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts",
            "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes",
-           "sesp_energies_static", "sesp_autotune", "sesp_tuning", "sesp_set_tuning"]
+           "sesp_energies_static", "sesp_autotune", "sesp_tuning", "sesp_set_tuning", "sesp_checks",
+           "sesp_check_flags", "sesp_rescale_temperature"]
 
 
 class SespError(RuntimeError):
@@ -95,8 +99,20 @@ def load(path: str = LIB_PATH):
     L.sesp_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.sesp_tuning.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.sesp_set_tuning.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    L.sesp_checks.argtypes = [P, dp]
+    L.sesp_check_flags.argtypes = [dp]
+    L.sesp_rescale_temperature.argtypes = [P, ctypes.c_double, dp]
     _lib = L
     return L
+
+
+def check_flags(counts) -> int:
+    """Warning bits of one replica's counts (first 7 values of a checks row);
+    host code of the library, no GPU needed."""
+    c = np.ascontiguousarray(counts, dtype=np.float64)[:7]
+    if c.size != 7:
+        raise ValueError("check_flags needs 7 counts")
+    return int(load().sesp_check_flags(_dp(c)))
 
 
 def _check(rc: int):
@@ -273,6 +289,22 @@ class Engine:
 
     def set_tuning(self, tile, ctas_per_sm):
         _check(_lib.sesp_set_tuning(self._h, int(tile), int(ctas_per_sm)))
+
+    def checks(self):
+        """The reference's consistency checks per replica (rows of 8): molecules
+        located whole, molecules uploaded, total charge in the cells, water O
+        and H in the cells, waters uploaded, sites in no cell, warning bits
+        (CHECK_* constants)."""
+        out = np.empty((self.replica_count(), 8))
+        _check(_lib.sesp_checks(self._h, _dp(out)))
+        return out
+
+    def rescale_temperature(self, target=RESCALE_TARGET):
+        """Scale the velocities to the temperature `target` (the reference's
+        rescaling variant uses 3.9); returns the temperature before."""
+        t = ctypes.c_double()
+        _check(_lib.sesp_rescale_temperature(self._h, float(target), ctypes.byref(t)))
+        return t.value
 
     def energies_static(self):
         """The same eight energies through sesp_energies_static: no device

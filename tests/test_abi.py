@@ -44,3 +44,23 @@ def test_fortran_interface_module_lists_every_entry_point():
     src = open(os.path.join(ROOT, "include", "sesp_mod.f90")).read().lower()
     for n in _declared():
         assert f'name="{n}"' in src, n
+
+
+def test_check_flags_follow_the_reference_rules():
+    """Warning rules of get_molecule_count and computeOnm4, host side."""
+    from surfactant_enhanced_spreading_gb300 import engine as E
+    from surfactant_enhanced_spreading_gb300.csrc import build
+    build.build()
+    ok = [1010, 1010, 1e-12, 1000, 2000, 1000, 0]
+    assert E.check_flags(ok) == 0
+    assert E.check_flags([1009, 1010, 0, 1000, 2000, 1000, 3]) == E.CHECK_MOLECULES_LOST
+    assert E.check_flags([1010, 1010, 0.0316, 1000, 2000, 1000, 0]) == 0           # q^2 = 0.000999
+    assert E.check_flags([1010, 1010, 0.032, 1000, 2000, 1000, 0]) == E.CHECK_CHARGE
+    assert E.check_flags([1010, 1010, -0.032, 1000, 2000, 1000, 0]) == E.CHECK_CHARGE
+    # integer H / O: 2999 / 1000 = 2 passes, 1999 / 1000 = 1 does not
+    assert E.check_flags([1010, 1010, 0, 1000, 2999, 1000, 0]) == 0
+    assert E.check_flags([1010, 1010, 0, 1000, 1999, 1000, 0]) == E.CHECK_OH_RATIO
+    assert E.check_flags([1010, 1010, 0, 999, 1998, 1000, 0]) == E.CHECK_MISSING_OXYGEN
+    assert E.check_flags([10, 10, 0, 0, 0, 0, 0]) == 0                             # surfactants only
+    assert E.check_flags([10, 10, 0, 0, 2, 0, 0]) == E.CHECK_OH_RATIO
+    assert E.check_flags([9, 10, 0.5, 0, 2, 1, 3]) == 15
