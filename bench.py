@@ -217,7 +217,8 @@ def run_ours(args, ws, rank, local):
     kb = 99101
     eng.run(kb, args.warmup)
     kb += args.warmup
-    tile, ctas, ctas_max = eng.autotune()   # pair-field launch shape (no effect on results)
+    tile, ctas, ctas_max = eng.autotune()   # launch shapes (no effect on results)
+    surf_warps = eng.constraint_tuning()[0]
     eng.run(kb, 1)
     kb += 1
     D.barrier()
@@ -232,12 +233,12 @@ def run_ours(args, ws, rank, local):
     ms_per_step = t_ms / args.steps
 
     # kernel launches in the timed region for this workload (waters, surfactants
-    # and graphite present): 11 per step (gather, pair field + finish, site
-    # forces, graphite, intramolecular, 3 for move_a, 2 for move_b) and 17 more
-    # per rebuild step (locate, sort 3, work items 3, isub, graphite list, P2M,
-    # 2 M2M, 3 M2L, 2 L2L)
+    # and graphite present): 9 per step (gather, pair field + finish, site
+    # forces, graphite, intramolecular, constraint half + eta for move_a, the
+    # constraint half for move_b) and 20 more per rebuild step (locate, sort 3,
+    # work items 3, isub, graphite list, water order 3, P2M, 2 M2M, 3 M2L, 2 L2L)
     n_rebuild = sum(1 for k in range(kb - args.steps, kb) if k % 10 == 0)
-    launches = 11 * args.steps + 17 * n_rebuild
+    launches = 9 * args.steps + 20 * n_rebuild
 
     # --- per-kernel durations over a second pass (events around kernel families)
     eng.enable_timing(True)
@@ -339,6 +340,7 @@ def run_ours(args, ws, rank, local):
                    "l2": "flushed between timed steps (256 MB write outside the timed intervals)",
                    "pair_field_shape": {"tile": tile, "ctas_per_sm": ctas, "ctas_per_sm_max": ctas_max,
                                         "how": "sesp_autotune before the timed steps"},
+                   "constraint_shape": {"surf_warps_per_cta": surf_warps, "how": "sesp_autotune"},
                    "parallelism": f"replicas x{ws}"},
         "ns_per_day": ns_day,
         "plain_fp64": {"value": plain_value, "unit": "atom-steps/s", "steps": args.plain_steps,

@@ -1,33 +1,41 @@
-// Constraint halves of the mixed path: SHAKE (move_*_a) and RATTLE
-// (move_*_b) iterated in FP32 (src/move_w1_a.f90:36-134,
-// src/move_surfactant_a.f90:36-134, src/move_w1_b.f90:30-119,
-// src/move_surfactant_b.f90:30-118).
+// Constraint halves of the mixed paths: SHAKE (move_*_a) and RATTLE
+// (move_*_b) for waters and surfactants in one persistent launch per half
+// (src/move_w1_a.f90:36-134, src/move_surfactant_a.f90:36-134,
+// src/move_w1_b.f90:30-119, src/move_surfactant_b.f90:30-118).
 //
-// GB300 issues FP64 at a small fraction of its FP32 rate, and a Gauss-Seidel
-// sweep is one long dependent chain per molecule, so the FP64 sweeps of the
-// plain path cost ~1000 cycles per bond.  Here the FP64 state is split once
-// per call into
+// The FP64 state is split once per call into
 //   * the FP64 predictor (positions for SHAKE, velocities for RATTLE), which
 //     is written to the state arrays at the start, and
-//   * FP32 corrections per site, which the sweeps update.
-// Each bond's constants are formed once in FP64 and rounded to FP32: for
-// SHAKE the predictor bond vector P, the old bond vector R, D0 = d^2 - |P|^2
-// and R.P; for RATTLE R and R.V (V the predictor velocity difference).  A
-// sweep then evaluates, with c the difference of the two sites' corrections,
+//   * corrections per site (type C: FP64 for SESP_MIXED, FP32 for
+//     SESP_MIXED_FP32C), which the Gauss-Seidel sweeps update.
+// Each bond's constants are formed once in FP64 and rounded to C: for SHAKE
+// the predictor bond vector P, the old bond vector R, D0 = d^2 - |P|^2 and
+// R.P; for RATTLE R and R.V (V the predictor velocity difference).  A sweep
+// then evaluates, with c the difference of the two sites' corrections,
 //     d^2 - |P + c|^2 = D0 - (2 P.c + c.c),     R.(P + c) = R.P + R.c,
 //     R.(V + c) = R.V + R.c,
-// so nothing cancels in FP32: the residual carries ~1e-10 absolute error
-// against a threshold of 2e-4 d^2 (SHAKE) or an equivalent 1e-4 (RATTLE).  A
-// residual within 2 % of its threshold is recomputed in FP64 from the
-// predictor plus the corrections, so the sweeps take the decisions an FP64
-// evaluation of the same state takes.  At the end the corrections are added
-// to the FP64 state.  Same bond order, tolerance tests, iteration limit and
-// failure counting as the FP64 kernels; only the rounding differs.
+// so nothing cancels.  With FP32 corrections a residual within 2 % of its
+// threshold is recomputed in FP64 from the predictor plus the corrections, so
+// the sweeps take the decisions an FP64 evaluation of the same state takes.
+// At the end the corrections are added to the FP64 state.  Same bond order,
+// tolerance tests, iteration limit and failure counting as the FP64 kernels
+// of the plain path; only the rounding differs.
 //
-// Waters: one thread per molecule.  Surfactants: one warp per molecule, its
-// 29 lanes doing the per-site FP64 work and the bond constants in parallel,
-// lane 0 the serial sweeps (the bond constants stream from shared memory one
-// bond ahead of use).
+// Scheduling.  GB300 issues FP64 at one warp instruction per ~19 cycles per
+// SM whatever the active lanes, with ~64 cycles of dependent latency.  A water
+// (one thread, 3 bonds) is FP64-throughput work; a surfactant (one warp, 28
+// bonds swept as a wavefront) is one long FP64 dependency chain, latency
+// work.  One launch of gridDim = SM count CTAs of 8 warps runs both: the
+// first n_scta CTAs start s_warps warps each on the surfactant queue (few
+// chains per SM, so they do not wait behind water instructions), every other
+// warp takes items of 32 waters from the water queue, and surfactant warps
+// join the water queue when no surfactant is left.  The water list is ordered
+// by each molecule's sweep count in the previous call (most first, reordered
+// at every list rebuild), so the 32 lanes of an item iterate alike and the
+// longest items start first.  Which warp takes which molecule changes no
+// result: every molecule is computed alone and its kinetic sums are stored
+// per molecule.  The queues are atomic counters; the last CTA to finish
+// resets them for the next launch.  Nothing waits on another CTA.
 #include <type_traits>
 
 #include "k_launch.cuh"
@@ -37,12 +45,8 @@ namespace sesp {
 namespace {
 
 struct Fast32 {
-    float rm[NTYPE];            // 1 / mass by site kind
-    float rmdt[NTYPE];          // DT / mass
-    float dsq_w[3], fa_w[3], fb_w[3];
-    float dsq_s[NBOND], fa_s[NBOND], fb_s[NBOND];
     double dsq64_w[3], dsq64_s[NBOND];
-    double fa64_w[3], fa64_s[NBOND], fb64_w[3], fb64_s[NBOND];
+    double fb64_w[3], fb64_s[NBOND];
     double mass64[NTYPE], rm64[NTYPE], rmdt64[NTYPE];
 };
 __constant__ Fast32 cF;
@@ -55,50 +59,12 @@ __host__ __device__ constexpr int sbi32(int b) {
     return b < 18 ? b : b == 18 ? 17 : b == 19 ? 19 : b <= 22 ? 20 : b == 23 ? 17 : b == 24 ? 24 : 25;
 }
 
-template <int NS>
-struct G32;
-template <>
-struct G32<3> {
-    static constexpr int NB = 3, BLOCK = 128;
-    __device__ static constexpr int bi(int b) { return b; }
-    __device__ static constexpr int bj(int b) { return b == 2 ? 0 : b + 1; }
-    __device__ static constexpr int kind(int i) { return i == 0 ? 0 : 1; }
-    template <typename C>
-    __device__ static C dsq(int b) { if constexpr (sizeof(C) == 4) return cF.dsq_w[b]; else return cF.dsq64_w[b]; }
-    template <typename C>
-    __device__ static C fa(int b) { if constexpr (sizeof(C) == 4) return cF.fa_w[b]; else return cF.fa64_w[b]; }
-    template <typename C>
-    __device__ static C fb(int b) { if constexpr (sizeof(C) == 4) return cF.fb_w[b]; else return cF.fb64_w[b]; }
-    __device__ static double dsq64(int b) { return cF.dsq64_w[b]; }
-};
-template <>
-struct G32<NSURF> {
-    static constexpr int NB = NBOND, BLOCK = 32;
-    __device__ static constexpr int bi(int b) { return sbi32(b); }
-    __device__ static constexpr int bj(int b) { return b + 1; }
-    __device__ static constexpr int kind(int i) { return 2 + i; }
-    template <typename C>
-    __device__ static C dsq(int b) { if constexpr (sizeof(C) == 4) return cF.dsq_s[b]; else return cF.dsq64_s[b]; }
-    template <typename C>
-    __device__ static C fa(int b) { if constexpr (sizeof(C) == 4) return cF.fa_s[b]; else return cF.fa64_s[b]; }
-    template <typename C>
-    __device__ static C fb(int b) { if constexpr (sizeof(C) == 4) return cF.fb_s[b]; else return cF.fb64_s[b]; }
-    __device__ static double dsq64(int b) { return cF.dsq64_s[b]; }
-};
-
 // the FP64 predictors of the FP64 kernels, rounded the same way
 __device__ inline double pred_a(double x, double v, double a, double escale) {
     return __dadd_rn(__dadd_rn(x, __dmul_rn(v, escale)), a);
 }
 __device__ inline double vel_a(double v, double a, double escale) { return __dadd_rn(__dmul_rn(v, escale), a); }
 
-// v as hi + lo, both FP32 (hi the rounded value, lo the rounded remainder)
-template <typename F>
-__device__ inline void split(double v, F &hi, F &lo) {
-    const float h = (float)v;
-    hi = h;
-    lo = (float)__dsub_rn(v, (double)h);
-}
 
 // SHAKE decision in FP64 for a residual near its threshold: predictor
 // difference (state arrays hold the predictor) plus the FP32 corrections
@@ -240,11 +206,9 @@ __device__ constexpr int wbi(int b) { return b; }
 __device__ constexpr int wbj(int b) { return b == 2 ? 0 : b + 1; }
 __device__ constexpr int wkind(int i) { return i == 0 ? 0 : 1; }
 
+// SHAKE half of one water (one thread); returns the sweeps it ran
 template <typename C>
-__global__ void __launch_bounds__(128) k_move_a32w(Dev d, const int *mols, int nm, double tol, int maxit) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nm) return;
-    const int m = mols[t];
+__device__ __forceinline__ int water_a(const Dev &d, int m, double tol, int maxit) {
     const int g0 = d.mfirst[m];
     const double escale = __dsub_rn(1.0, __dmul_rn(d.eta[d.mrep[m]], DT) * 0.5);
     double rx[3], ry[3], rz[3], px[3], py[3], pz[3];
@@ -302,13 +266,12 @@ __global__ void __launch_bounds__(128) k_move_a32w(Dev d, const int *mols, int n
     d.ke[2 * m] = ke0;
     d.ke[2 * m + 1] = ke1;
     if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    return it;
 }
 
+// RATTLE half of one water (one thread); returns the sweeps it ran
 template <typename C>
-__global__ void __launch_bounds__(128) k_move_b32w(Dev d, const int *mols, int nm, double tol, int maxit) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nm) return;
-    const int m = mols[t];
+__device__ __forceinline__ int water_b(const Dev &d, int m, double tol, int maxit) {
     const int g0 = d.mfirst[m];
     const double escale = __ddiv_rn(2.0, __dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[m]], DT)));
     double rx[3], ry[3], rz[3], vx[3], vy[3], vz[3];
@@ -355,6 +318,7 @@ __global__ void __launch_bounds__(128) k_move_b32w(Dev d, const int *mols, int n
         d.vz[g] = __dadd_rn(vz[i], (double)cz[i]);
     }
     if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    return it;
 }
 
 // ---------------------------------------------------------------- surfactants
@@ -401,15 +365,20 @@ struct BondRecords {
         for (int q = 0; q < NF; q++) f[q] = v[q][skew8(b)];
     }
 };
+// one surfactant warp's shared memory
+template <typename C, int NF>
+struct SurfSmem {
+    BondRecords<C, NF> sk;
+    C sc[3][SK];
+};
 
+// SHAKE half of one surfactant (the whole warp)
 template <typename C>
-__global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm, double tol, int maxit) {
+__device__ __forceinline__ void surf_a(const Dev &d, int m, double tol, int maxit, SurfSmem<C, 16> &sm) {
     static_assert(sizeof(ShakeK<C>) == 16 * sizeof(C), "ShakeK is 16 values");
-    __shared__ BondRecords<C, 16> sk;
-    __shared__ C sc[3][SK];
-    if (blockIdx.x >= nm) return;
-    const int lane = threadIdx.x;
-    const int m = mols[blockIdx.x];
+    auto &sk = sm.sk;
+    auto &sc = sm.sc;
+    const int lane = threadIdx.x & 31;
     const int g0 = d.mfirst[m];
     const double escale = __dsub_rn(1.0, __dmul_rn(d.eta[d.mrep[m]], DT) * 0.5);
     const bool site = lane < NSURF;
@@ -487,16 +456,16 @@ __global__ void __launch_bounds__(32) k_move_a32s(Dev d, const int *mols, int nm
         d.ke[2 * m + 1] = ke1;
         if (fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
     }
+    __syncwarp();   // the shared records are reused by the warp's next molecule
 }
 
+// RATTLE half of one surfactant (the whole warp)
 template <typename C>
-__global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm, double tol, int maxit) {
+__device__ __forceinline__ void surf_b(const Dev &d, int m, double tol, int maxit, SurfSmem<C, 11> &sm) {
     static_assert(sizeof(RattleK<C>) == 11 * sizeof(C), "RattleK is 11 values");
-    __shared__ BondRecords<C, 11> sk;
-    __shared__ C sc[3][SK];
-    if (blockIdx.x >= nm) return;
-    const int lane = threadIdx.x;
-    const int m = mols[blockIdx.x];
+    auto &sk = sm.sk;
+    auto &sc = sm.sc;
+    const int lane = threadIdx.x & 31;
     const int g0 = d.mfirst[m];
     const double escale = __ddiv_rn(2.0, __dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[m]], DT)));
     const bool site = lane < NSURF;
@@ -562,6 +531,115 @@ __global__ void __launch_bounds__(32) k_move_b32s(Dev d, const int *mols, int nm
         d.vz[g] = __dadd_rn(vz, (double)sc[2][skew8(lane)]);
     }
     if (lane == 0 && fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    __syncwarp();   // the shared records are reused by the warp's next molecule
+}
+
+// ---------------------------------------------------------------- the persistent launch
+
+constexpr int CW = 8;                 // warps per CTA
+constexpr int CW_THREADS = 32 * CW;
+
+struct CPlan {
+    const int *smols;   // surfactant molecules
+    const int *wlist;   // water molecules in work order
+    uint8_t *wsw;       // per molecule: sweeps of this half's last call (waters)
+    unsigned *ctl;      // [0] next surfactant, [1] next water item, [2] CTAs finished
+    int ns, nw;
+    int n_scta;         // CTAs that start on the surfactant queue
+    int s_warps;        // surfactant warps in each of them
+};
+
+template <typename C, bool SHAKE>
+__global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double tol, int maxit) {
+    constexpr int NF = SHAKE ? 16 : 11;
+    extern __shared__ __align__(16) unsigned char cs_smem[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool surf_cta = (int)blockIdx.x < p.n_scta;
+    if (surf_cta && warp < p.s_warps) {
+        SurfSmem<C, NF> &sm = reinterpret_cast<SurfSmem<C, NF> *>(cs_smem)[warp];
+        for (;;) {
+            unsigned s = 0;
+            if (lane == 0) s = atomicAdd(&p.ctl[0], 1u);
+            s = __shfl_sync(FULL, s, 0);
+            if (s >= (unsigned)p.ns) break;
+            if constexpr (SHAKE) surf_a<C>(d, p.smols[s], tol, maxit, sm);
+            else surf_b<C>(d, p.smols[s], tol, maxit, sm);
+        }
+    }
+    // the other warps of a surfactant CTA stay idle, so its chains keep the SM's FP64 pipe
+    if (!surf_cta || warp < p.s_warps) {
+        for (;;) {
+            unsigned item = 0;
+            if (lane == 0) item = atomicAdd(&p.ctl[1], 1u);
+            item = __shfl_sync(FULL, item, 0);
+            const long long t0 = 32LL * item;
+            if (t0 >= p.nw) break;
+            const int t = (int)t0 + lane;
+            if (t < p.nw) {
+                const int m = p.wlist[t];
+                const int sweeps = SHAKE ? water_a<C>(d, m, tol, maxit) : water_b<C>(d, m, tol, maxit);
+                p.wsw[m] = (uint8_t)(sweeps < 255 ? sweeps : 255);
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        // every CTA counts itself once it has left both queues; the last one
+        // (all others have stopped taking work) resets them for the next launch
+        __threadfence();
+        if (atomicAdd(&p.ctl[2], 1u) == gridDim.x - 1) { p.ctl[0] = 0u; p.ctl[1] = 0u; p.ctl[2] = 0u; }
+    }
+}
+
+// ---------------------------------------------------------------- water order
+
+// Counting sort of the water list by the sweeps of the last call, most
+// first, for each half (bins 0..127; placement within a bin is free)
+constexpr int WS_BINS = 128;
+__device__ __forceinline__ int wbin(uint8_t s) { return WS_BINS - 1 - (s < WS_BINS - 1 ? (int)s : WS_BINS - 1); }
+
+__global__ void k_worder_count(const int *wmols, int nw, const uint8_t *swa, const uint8_t *swb, int *off) {
+    __shared__ int h[2 * WS_BINS];
+    for (int k = threadIdx.x; k < 2 * WS_BINS; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nw; t += gridDim.x * blockDim.x) {
+        const int m = wmols[t];
+        atomicAdd(&h[wbin(swa[m])], 1);
+        atomicAdd(&h[WS_BINS + wbin(swb[m])], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * WS_BINS; k += blockDim.x)
+        if (h[k]) atomicAdd(&off[k], h[k]);
+}
+
+__global__ void k_worder_scan(int *off) {   // one thread per half: exclusive scan of its bins
+    int *o = off + threadIdx.x * WS_BINS;
+    int acc = 0;
+    for (int k = 0; k < WS_BINS; k++) { const int v = o[k]; o[k] = acc; acc += v; }
+}
+
+__global__ void k_worder_place(const int *wmols, int nw, const uint8_t *swa, const uint8_t *swb, int *off, int *la,
+                               int *lb) {
+    __shared__ int cnt[2 * WS_BINS], base[2 * WS_BINS];
+    for (int k = threadIdx.x; k < 2 * WS_BINS; k += blockDim.x) cnt[k] = 0;
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    int m = -1, ba = 0, bb = 0, ra = 0, rb = 0;
+    if (t < nw) {
+        m = wmols[t];
+        ba = wbin(swa[m]);
+        bb = WS_BINS + wbin(swb[m]);
+        ra = atomicAdd(&cnt[ba], 1);
+        rb = atomicAdd(&cnt[bb], 1);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * WS_BINS; k += blockDim.x)
+        if (cnt[k]) base[k] = atomicAdd(&off[k], cnt[k]);
+    __syncthreads();
+    if (m >= 0) {
+        la[base[ba] + ra] = m;
+        lb[base[bb] + rb] = m;
+    }
 }
 
 }  // namespace
@@ -573,55 +651,66 @@ bool upload_tables_fast(const Tables &t, cudaStream_t st) {
     for (int k = 0; k < NTYPE; k++) {
         f.mass64[k] = t.mass[k];
         f.rm64[k] = 1.0 / t.mass[k];
-        f.rm[k] = (float)(1.0 / t.mass[k]);
-        f.rmdt[k] = (float)(DT / t.mass[k]);
         f.rmdt64[k] = DT / t.mass[k];
     }
     for (int b = 0; b < 3; b++) {
         const int ki = b == 0 ? 0 : 1, kj = b == 2 ? 0 : 1;
         const double rs = 1.0 / t.mass[ki] + 1.0 / t.mass[kj];
         f.dsq64_w[b] = t.dsqw[b];
-        f.dsq_w[b] = (float)t.dsqw[b];
-        f.fa64_w[b] = 2.0 * rs;
         f.fb64_w[b] = (1.0 / DT) / (rs * t.dsqw[b]);
-        f.fa_w[b] = (float)f.fa64_w[b];
-        f.fb_w[b] = (float)f.fb64_w[b];
     }
     for (int b = 0; b < NBOND; b++) {
         const double rs = 1.0 / t.mass[2 + t.bi[b]] + 1.0 / t.mass[2 + t.bj[b]];
         f.dsq64_s[b] = t.dsqs[b];
-        f.dsq_s[b] = (float)t.dsqs[b];
-        f.fa64_s[b] = 2.0 * rs;
         f.fb64_s[b] = (1.0 / DT) / (rs * t.dsqs[b]);
-        f.fa_s[b] = (float)f.fa64_s[b];
-        f.fb_s[b] = (float)f.fb64_s[b];
     }
     return cudaMemcpyToSymbolAsync(cF, &f, sizeof f, 0, cudaMemcpyHostToDevice, st) == cudaSuccess;
 }
 
-// fp32: 1 for FP32 sweeps, 0 for FP64 sweeps.  Surfactants first, then
-// waters, on one stream: run side by side, the FP64-pipe-bound water sweeps
-// stall the latency-bound surfactant wavefronts.
-void launch_move_a32(const Dev &d, const int *wmols, int nw, const int *smols, int ns, cudaStream_t st, double tol,
-                     int maxit, int fp32) {
-    if (fp32) {
-        if (ns) k_move_a32s<float><<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
-        if (nw) k_move_a32w<float><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
-    } else {
-        if (ns) k_move_a32s<double><<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
-        if (nw) k_move_a32w<double><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
-    }
+int constraint_max_surf_warps() { return CW; }
+
+namespace {
+template <typename C, bool SHAKE>
+void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, const ConstraintShape &sh, double tol,
+                        int maxit, cudaStream_t st) {
+    constexpr int NF = SHAKE ? 16 : 11;
+    CPlan p;
+    p.smols = smols;
+    p.wlist = SHAKE ? d.wlist_a : d.wlist_b;
+    p.wsw = SHAKE ? d.wsw_a : d.wsw_b;
+    p.ctl = d.cctl + (SHAKE ? 0 : 4);
+    p.ns = ns;
+    p.nw = nw;
+    p.s_warps = sh.s_warps < 1 ? 1 : (sh.s_warps > CW ? CW : sh.s_warps);
+    const int need = (ns + p.s_warps - 1) / p.s_warps;
+    p.n_scta = ns ? (need < sh.grid ? need : sh.grid) : 0;
+    const size_t smem = p.n_scta ? (size_t)p.s_warps * sizeof(SurfSmem<C, NF>) : 0;
+    k_constrain<C, SHAKE><<<sh.grid, CW_THREADS, smem, st>>>(d, p, tol, maxit);
+}
+}  // namespace
+
+// fp32: 1 for FP32 sweeps, 0 for FP64 sweeps
+void launch_move_a32(const Dev &d, int nw, const int *smols, int ns, const ConstraintShape &sh, cudaStream_t st,
+                     double tol, int maxit, int fp32) {
+    if (!nw && !ns) return;
+    if (fp32) launch_constrain_t<float, true>(d, smols, ns, nw, sh, tol, maxit, st);
+    else launch_constrain_t<double, true>(d, smols, ns, nw, sh, tol, maxit, st);
 }
 
-void launch_move_b32(const Dev &d, const int *wmols, int nw, const int *smols, int ns, cudaStream_t st, double tol,
-                     int maxit, int fp32) {
-    if (fp32) {
-        if (ns) k_move_b32s<float><<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
-        if (nw) k_move_b32w<float><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
-    } else {
-        if (ns) k_move_b32s<double><<<ns, 32, 0, st>>>(d, smols, ns, tol, maxit);
-        if (nw) k_move_b32w<double><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
-    }
+void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, const ConstraintShape &sh, cudaStream_t st,
+                     double tol, int maxit, int fp32) {
+    if (!nw && !ns) return;
+    if (fp32) launch_constrain_t<float, false>(d, smols, ns, nw, sh, tol, maxit, st);
+    else launch_constrain_t<double, false>(d, smols, ns, nw, sh, tol, maxit, st);
+}
+
+void launch_water_order(const Dev &d, const int *wmols, int nw, cudaStream_t st) {
+    if (!nw) return;
+    cudaMemsetAsync(d.wsort_off, 0, 2 * WS_BINS * sizeof(int), st);
+    const int nb = (nw + 255) / 256;
+    k_worder_count<<<nb < 256 ? nb : 256, 256, 0, st>>>(wmols, nw, d.wsw_a, d.wsw_b, d.wsort_off);
+    k_worder_scan<<<1, 2, 0, st>>>(d.wsort_off);
+    k_worder_place<<<nb, 256, 0, st>>>(wmols, nw, d.wsw_a, d.wsw_b, d.wsort_off, d.wlist_a, d.wlist_b);
 }
 
 }  // namespace sesp

@@ -352,22 +352,43 @@ __global__ void __launch_bounds__(SURF_BLOCK) k_move_b_surf(Dev d, const int *mo
     if (!ldone) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
 }
 
-// eta update of src/move_w2_a.f90:145-157, one block per replica, fixed
-// summation order (thread-strided partial sums, then a tree)
-__global__ void k_eta(Dev d) {
-    const Rep r = d.rep[blockIdx.x];
-    __shared__ double s0[1024], s1[1024];
+// eta update of src/move_w2_a.f90:145-157.  ETA_BLOCKS blocks per replica
+// each sum a fixed contiguous share of its molecules' kinetic sums
+// (thread-strided, then a tree); the last of them to finish adds the shares
+// in block order and updates eta.  The summation order is fixed, whichever
+// block finishes last; nothing waits.
+constexpr int ETA_BLOCKS = 32, ETA_THREADS = 256;
+__global__ void __launch_bounds__(ETA_THREADS) k_eta(Dev d) {
+    const int rep = blockIdx.x / ETA_BLOCKS, j = blockIdx.x % ETA_BLOCKS;
+    const Rep r = d.rep[rep];
+    __shared__ double s0[ETA_THREADS], s1[ETA_THREADS];
+    __shared__ bool last;
+    const int per = (r.nmol + ETA_BLOCKS - 1) / ETA_BLOCKS;
+    const int m0 = r.mol0 + j * per, m1 = min(r.mol0 + r.nmol, m0 + per);
     double a = 0.0, b = 0.0;
-    for (int m = r.mol0 + threadIdx.x; m < r.mol0 + r.nmol; m += blockDim.x) { a += d.ke[2 * m]; b += d.ke[2 * m + 1]; }
+    for (int m = m0 + threadIdx.x; m < m1; m += ETA_THREADS) { a += d.ke[2 * m]; b += d.ke[2 * m + 1]; }
     s0[threadIdx.x] = a; s1[threadIdx.x] = b;
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    for (int w = ETA_THREADS / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) { s0[threadIdx.x] += s0[threadIdx.x + w]; s1[threadIdx.x] += s1[threadIdx.x + w]; }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        double sum1 = s0[0] / (DT * DT), sum2 = s1[0] / (DT * DT);
-        d.eta[blockIdx.x] = d.eta[blockIdx.x] + r.pnh1 * (sum1 + r.pnh2 + sum2);
+        d.eta_part[2 * blockIdx.x] = s0[0];
+        d.eta_part[2 * blockIdx.x + 1] = s1[0];
+        __threadfence();
+        last = atomicAdd(&d.eta_ctl[rep], 1u) == ETA_BLOCKS - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const volatile double *p = d.eta_part + 2 * ETA_BLOCKS * rep;
+        double sum1 = 0.0, sum2 = 0.0;
+        for (int k = 0; k < ETA_BLOCKS; k++) { sum1 += p[2 * k]; sum2 += p[2 * k + 1]; }
+        sum1 = sum1 / (DT * DT);
+        sum2 = sum2 / (DT * DT);
+        d.eta[rep] = d.eta[rep] + r.pnh1 * (sum1 + r.pnh2 + sum2);
+        d.eta_ctl[rep] = 0u;
     }
 }
 
@@ -442,19 +463,19 @@ void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream
 // reference does; fast = 1 / 2 (mixed paths): the FP64 / FP32 sweeps of
 // k_constraint.cu.
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
-                   int fast, cudaStream_t st) {
+                   int fast, const ConstraintShape &sh, cudaStream_t st) {
     if (fast) {
-        launch_move_a32(d, wmols, nw, smols, ns, st, tol, maxit, fast == 2);
+        launch_move_a32(d, nw, smols, ns, sh, st, tol, maxit, fast == 2);
     } else {
         if (ns) k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
     }
-    k_eta<<<nrep, 1024, 0, st>>>(d);
+    k_eta<<<nrep * ETA_BLOCKS, ETA_THREADS, 0, st>>>(d);
 }
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit, int fast,
-                   cudaStream_t st) {
+                   const ConstraintShape &sh, cudaStream_t st) {
     if (fast) {
-        launch_move_b32(d, wmols, nw, smols, ns, st, tol, maxit, fast == 2);
+        launch_move_b32(d, nw, smols, ns, sh, st, tol, maxit, fast == 2);
     } else {
         if (ns) k_move_b_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);

@@ -317,6 +317,7 @@ struct sesp_ctx {
     // graphs of one step with / without a rebuild
     cudaGraphExec_t g_step[2] = {nullptr, nullptr};
     NearShape near = {64, 0};   // pair-field launch shape (autotuned or set; results do not depend on it)
+    ConstraintShape cshape = {0, 2};   // constraint halves of the mixed paths (likewise)
     int n_sm = 0;               // streaming multiprocessors of the device
     // timing
     bool timing = false;
@@ -410,6 +411,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         launch_near_items(d, c->ncell, (int)near_items_max(c->nsite, c->ncell), c->near.tile, c->st);
         launch_isub(d, c->nsm * NSURF, c->smols, c->st);
         launch_graphite_list(d, c->nsite, c->st);
+        if (mixed) launch_water_order(d, c->wmols, c->nwm, c->st);
         tstop(c, 5);
     }
     launch_gather(d, c->nsite, c->ncell, mixed, c->st);
@@ -430,13 +432,13 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
 void seq_move_a(sesp_ctx *c) {
     tstart(c, 2);
     launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit,
-                  c->p.precision, c->st);
+                  c->p.precision, c->cshape, c->st);
     tstop(c, 2);
 }
 void seq_move_b(sesp_ctx *c) {
     tstart(c, 3);
     launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit,
-                  c->p.precision, c->st);
+                  c->p.precision, c->cshape, c->st);
     tstop(c, 3);
 }
 
@@ -497,6 +499,7 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, dev);
         c->near.grid = c->n_sm * near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64);
+        c->cshape.grid = c->n_sm;
     }
     Tables T = make_tables();
     {
@@ -597,7 +600,10 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
         (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
         (e = dalloc(c, &d.L2, (size_t)LP * n2)) || (e = dalloc(c, &d.counters, 8)) ||
-        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &d.lj_kind, NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)))
+        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &d.lj_kind, NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)) ||
+        (e = dalloc(c, &d.wlist_a, nwm)) || (e = dalloc(c, &d.wlist_b, nwm)) || (e = dalloc(c, &d.wsw_a, M)) ||
+        (e = dalloc(c, &d.wsw_b, M)) || (e = dalloc(c, &d.cctl, 8)) || (e = dalloc(c, &d.wsort_off, 256)) ||
+        (e = dalloc(c, &d.eta_part, 64 * (size_t)R)) || (e = dalloc(c, &d.eta_ctl, R)))
         return e;
     int w2 = 2 * d2 + 1;
     const size_t nh2 = (size_t)w2 * w2 * w2 * NHARM;
@@ -730,7 +736,11 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     CK(cudaMemcpyAsync(d.mrep, mrep.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.mfirst, mfirst.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.mkind, mkind.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
-    if (nwm) CK(cudaMemcpyAsync(c->wmols, wm.data(), nwm * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    if (nwm) {
+        CK(cudaMemcpyAsync(c->wmols, wm.data(), nwm * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(d.wlist_a, wm.data(), nwm * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(d.wlist_b, wm.data(), nwm * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    }
     if (nsm) CK(cudaMemcpyAsync(c->smols, sm.data(), nsm * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.rep, c->reps.data(), R * sizeof(Rep), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.eta, eta0.data(), R * sizeof(double), cudaMemcpyHostToDevice, c->st));
@@ -987,9 +997,86 @@ int sesp_tuning(sesp_ctx *c, int out[3]) {
     return 0;
 }
 
+int sesp_set_constraint_tuning(sesp_ctx *c, int surf_warps) {
+    if (int e = check_ctx(c, false)) return e;
+    if (surf_warps < 1 || surf_warps > constraint_max_surf_warps())
+        return fail(SESP_EINVAL, "surf_warps must be 1..%d", constraint_max_surf_warps());
+    c->cshape.s_warps = surf_warps;
+    drop_graphs(c);
+    return 0;
+}
+
+int sesp_constraint_tuning(sesp_ctx *c, int out[2]) {
+    if (int e = check_ctx(c, false)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    out[0] = c->cshape.s_warps;
+    out[1] = constraint_max_surf_warps();
+    return 0;
+}
+
+namespace {
+// Times both constraint halves of the mixed paths for every surfactant-warp
+// count (median of 3), restoring the state the halves change before every
+// trial and at the end, and keeps the fastest.
+int tune_constraints(sesp_ctx *c) {
+    const Dev &d = c->d;
+    const size_t N = c->nsite, M = c->nmol, R = c->nrep;
+    struct Arr { void *p; size_t bytes; };
+    const Arr arrs[] = {{d.x, 8 * N}, {d.y, 8 * N}, {d.z, 8 * N}, {d.vx, 8 * N}, {d.vy, 8 * N}, {d.vz, 8 * N},
+                        {d.ax, 8 * N}, {d.ay, 8 * N}, {d.az, 8 * N}, {d.ke, 16 * M}, {d.mfail, 4 * M},
+                        {d.eta, 8 * R}, {d.counters, 64}, {d.wsw_a, M}, {d.wsw_b, M}};
+    size_t total = 0;
+    for (const Arr &a : arrs) total += (a.bytes + 255) & ~(size_t)255;
+    unsigned char *save = nullptr;
+    CK(cudaMalloc(&save, total));
+    auto copy = [&](bool out) {
+        size_t off = 0;
+        for (const Arr &a : arrs) {
+            if (out) cudaMemcpyAsync(save + off, a.p, a.bytes, cudaMemcpyDeviceToDevice, c->st);
+            else cudaMemcpyAsync(a.p, save + off, a.bytes, cudaMemcpyDeviceToDevice, c->st);
+            off += (a.bytes + 255) & ~(size_t)255;
+        }
+    };
+    copy(true);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    int pick = c->cshape.s_warps;
+    for (int sw : {1, 2, 3, 4, 6, 8}) {
+        if (sw > constraint_max_surf_warps()) continue;
+        const ConstraintShape sh = {c->cshape.grid, sw};
+        float t[3];
+        for (int r = 0; r < 3; r++) {
+            copy(false);
+            cudaEventRecord(e0, c->st);
+            launch_move_a(d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit,
+                          c->p.precision, sh, c->st);
+            launch_move_b(d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit, c->p.precision, sh,
+                          c->st);
+            cudaEventRecord(e1, c->st);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&t[r], e0, e1);
+        }
+        std::sort(t, t + 3);
+        if (t[1] < best) { best = t[1]; pick = sw; }
+    }
+    copy(false);
+    cudaError_t err = cudaStreamSynchronize(c->st);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(save);
+    if (err != cudaSuccess) return fail(SESP_ECUDA, "constraint autotuning: %s", cudaGetErrorString(err));
+    c->cshape.s_warps = pick;
+    return 0;
+}
+}  // namespace
+
 // Times the pair field on the current state for every candidate shape (tile
 // 64 or 32 sites per work item; 1/4, 1/2, 3/4 or all of the CTAs per SM the
-// kernel can hold), median of 5 launches each, and keeps the fastest.
+// kernel can hold), median of 5 launches each, and keeps the fastest; on the
+// mixed paths with surfactants, then the constraint halves' surfactant warps
+// per CTA (the state is restored afterwards).
 int sesp_autotune(sesp_ctx *c, int out[3]) {
     if (int e = check_ctx(c, true)) return e;
     if (!out) return fail(SESP_EINVAL, "null output");
@@ -1026,6 +1113,8 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     cudaEventDestroy(e1);
     c->near = pick;
     launch_near_items(c->d, c->ncell, (int)near_items_max(c->nsite, c->ncell), pick.tile, c->st);
+    if (mixed && c->nsm > 0)
+        if (int e = tune_constraints(c)) return e;
     drop_graphs(c);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->st));

@@ -83,9 +83,18 @@ struct Dev {
     int *mrep, *mfirst, *mkind, *mkey, *mw1;
     double *ke;          // [2 * nmol]: sum m v^2 before / after SHAKE
     int *mfail;
+    // constraint halves of the mixed paths: water work order per half, sweeps
+    // of each water's last call per half, queue counters ([0..2] SHAKE,
+    // [4..6] RATTLE) and the bins of the reordering
+    int *wlist_a, *wlist_b;
+    uint8_t *wsw_a, *wsw_b;
+    unsigned *cctl;
+    int *wsort_off;
     // replicas
     Rep *rep;
     double *eta;         // [nrep]
+    double *eta_part;    // [nrep][32][2] partial kinetic sums of the eta update
+    unsigned *eta_ctl;   // [nrep] blocks of the eta update finished
     double *axis;        // cell centre tables
     // cells
     int *crep, *b3rep, *b2rep;

@@ -37,7 +37,7 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts",
            "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes",
            "sesp_energies_static", "sesp_autotune", "sesp_tuning", "sesp_set_tuning", "sesp_checks",
-           "sesp_check_flags", "sesp_rescale_temperature"]
+           "sesp_check_flags", "sesp_rescale_temperature", "sesp_set_constraint_tuning", "sesp_constraint_tuning"]
 
 
 class SespError(RuntimeError):
@@ -99,6 +99,8 @@ def load(path: str = LIB_PATH):
     L.sesp_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.sesp_tuning.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.sesp_set_tuning.argtypes = [P, ctypes.c_int, ctypes.c_int]
+    L.sesp_set_constraint_tuning.argtypes = [P, ctypes.c_int]
+    L.sesp_constraint_tuning.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.sesp_checks.argtypes = [P, dp]
     L.sesp_check_flags.argtypes = [dp]
     L.sesp_rescale_temperature.argtypes = [P, ctypes.c_double, dp]
@@ -289,6 +291,15 @@ class Engine:
 
     def set_tuning(self, tile, ctas_per_sm):
         _check(_lib.sesp_set_tuning(self._h, int(tile), int(ctas_per_sm)))
+
+    def constraint_tuning(self):
+        """(surfactant warps per CTA of the mixed constraint halves, largest)."""
+        out = (ctypes.c_int * 2)()
+        _check(_lib.sesp_constraint_tuning(self._h, out))
+        return tuple(out)
+
+    def set_constraint_tuning(self, surf_warps):
+        _check(_lib.sesp_set_constraint_tuning(self._h, int(surf_warps)))
 
     def checks(self):
         """The reference's consistency checks per replica (rows of 8): molecules

@@ -53,3 +53,44 @@ def test_invalid_shapes_are_refused(sys_small):
         eng.set_tuning(64, 0)
     with pytest.raises(E.SespError, match="ESTATE"):
         eng.autotune()   # no force call yet
+
+
+@pytest.mark.parametrize("precision", [E.MIXED, E.MIXED_FP32C])
+def test_constraint_shapes_give_identical_trajectories(precision):
+    """Surfactant warps per CTA of the constraint halves, and the water order
+    that every rebuild derives from the previous sweeps, change no bit."""
+    s = S.droplet(900, 30, cells=(8, 8, 8), seed=5)
+    runs = []
+    for sw in (1, 3, 8, None):
+        eng = E.Engine(s, precision)
+        eng.force(True)
+        if sw is None:
+            eng.autotune()
+            assert 1 <= eng.constraint_tuning()[0] <= 8
+        else:
+            eng.set_constraint_tuning(sw)
+            assert eng.constraint_tuning() == (sw, 8)
+        eng.init_accel()
+        eng.run(99101, 25)
+        runs.append(eng.state() + (eng.eta, eng.counters()[0]))
+        eng.close()
+    for r in runs[1:]:
+        for a, b in zip(runs[0], r):
+            assert np.array_equal(a, b)
+
+
+def test_autotune_restores_the_state():
+    s = S.droplet(700, 12, cells=(8, 8, 8), seed=6)
+    eng = E.Engine(s, E.MIXED)
+    E.mybox_start(eng)
+    eng.run(99101, 7)
+    before = eng.state() + (eng.eta,)
+    eng.autotune()
+    after = eng.state() + (eng.eta,)
+    for a, b in zip(before, after):
+        assert np.array_equal(a, b)
+    with pytest.raises(E.SespError, match="EINVAL"):
+        eng.set_constraint_tuning(0)
+    with pytest.raises(E.SespError, match="EINVAL"):
+        eng.set_constraint_tuning(9)
+    eng.close()
