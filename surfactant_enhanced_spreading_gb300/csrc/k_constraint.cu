@@ -9,10 +9,11 @@
 //   * corrections per site (type C: FP64 for SESP_MIXED, FP32 for
 //     SESP_MIXED_FP32C), which the Gauss-Seidel sweeps update.
 // Each bond's constants are formed once in FP64 and rounded to C: for SHAKE
-// the predictor bond vector P, the old bond vector R, D0 = d^2 - |P|^2 and
-// R.P; for RATTLE R and R.V (V the predictor velocity difference).  A sweep
-// then evaluates, with c the difference of the two sites' corrections,
-//     d^2 - |P + c|^2 = D0 - (2 P.c + c.c),     R.(P + c) = R.P + R.c,
+// from the predictor bond vector P, the old bond vector R, D0 = d^2 - |P|^2
+// and R.P; for RATTLE from R and R.V (V the predictor velocity difference).
+// A sweep then evaluates, with c the difference of the two sites'
+// corrections,
+//     d^2 - |P + c|^2 = D0 - c.(c + 2P),     R.(P + c) = R.P + R.c,
 //     R.(V + c) = R.V + R.c,
 // so nothing cancels.  With FP32 corrections a residual within 2 % of its
 // threshold is recomputed in FP64 from the predictor plus the corrections, so
@@ -102,91 +103,91 @@ __device__ __forceinline__ bool gt_abs(double x, double t) {
 }
 __device__ __forceinline__ bool gt_abs(float x, float t) { return fabsf(x) > t; }
 
-// a / b.  FP32: the hardware estimate.  FP64: the FP32 estimate y of 1/b and
-// one Newton correction of the quotient, q = a y + y (a - b a y), relative
-// error ~2^-46.
-template <typename C>
-__device__ __forceinline__ C quot(C a, C b) {
-    if constexpr (sizeof(C) == 4) {
-        return __fdividef(a, b);
-    } else {
-        const double y = (double)__fdividef(1.f, (float)b);
-        const double q = a * y;
-        return fma(y, fma(-b, q, a), q);
-    }
-}
-
 // Per-bond constants, formed once per call in FP64 and rounded to C.
-// SHAKE: predictor and old bond vectors P and R, the correction directions
-// R / m_i and R / m_j, D0 = d^2 - |P|^2, R.P, the threshold 2 tol d^2 and
-// 2 (1/m_i + 1/m_j).
+// SHAKE, with P and R the predictor and old bond vectors, rp = R.P and
+// y0 = 1 / (2 (1/m_i + 1/m_j) rp): 2P, R y0 / rp, the correction
+// directions R / m_i and R / m_j, D0 = d^2 - |P|^2, y0 and the threshold
+// 2 tol d^2 (and one unused slot, so a record is 16 values).
 template <typename C>
 struct ShakeK {
-    C p[3], r[3], a[3], b[3], d0, rp, thr, fa;
+    C p2[3], r1[3], a[3], b[3], d0, y0, thr, pad;
 };
-// RATTLE: bond vector R, the correction directions R dt / m_i and R dt / m_j,
-// R.V of the velocity predictor and (1/dt) / ((1/m_i + 1/m_j) d^2).
+// RATTLE, with fb = (1/dt) / ((1/m_i + 1/m_j) d^2): -fb R, the correction
+// directions R dt / m_i and R dt / m_j, -fb R.V of the velocity predictor
+// (and one unused slot: 11 values).
 template <typename C>
 struct RattleK {
-    C r[3], a[3], b[3], rv, fb;
+    C rs[3], a[3], b[3], rvs, pad;
 };
 
 template <typename C>
 __device__ inline void shake_make(double rx, double ry, double rz, double px, double py, double pz, double dsq,
                                   double rmi, double rmj, double tol2, ShakeK<C> &k) {
-    k.p[0] = (C)px; k.p[1] = (C)py; k.p[2] = (C)pz;
-    k.r[0] = (C)rx; k.r[1] = (C)ry; k.r[2] = (C)rz;
+    const double rp = rx * px + ry * py + rz * pz;
+    const double y0 = 1.0 / (2.0 * (rmi + rmj) * rp);
+    const double y1 = y0 / rp;
+    k.p2[0] = (C)(2.0 * px); k.p2[1] = (C)(2.0 * py); k.p2[2] = (C)(2.0 * pz);
+    k.r1[0] = (C)(y1 * rx); k.r1[1] = (C)(y1 * ry); k.r1[2] = (C)(y1 * rz);
     k.a[0] = (C)(rmi * rx); k.a[1] = (C)(rmi * ry); k.a[2] = (C)(rmi * rz);
     k.b[0] = (C)(rmj * rx); k.b[1] = (C)(rmj * ry); k.b[2] = (C)(rmj * rz);
     k.d0 = (C)(dsq - (px * px + py * py + pz * pz));
-    k.rp = (C)(rx * px + ry * py + rz * pz);
+    k.y0 = (C)y0;
     k.thr = (C)(dsq * tol2);
-    k.fa = (C)(2.0 * (rmi + rmj));
+    k.pad = C(0);
 }
 template <typename C>
 __device__ inline void rattle_make(double rx, double ry, double rz, double wx, double wy, double wz, double dti,
                                    double dtj, double fb, RattleK<C> &k) {
-    k.r[0] = (C)rx; k.r[1] = (C)ry; k.r[2] = (C)rz;
+    k.rs[0] = (C)(-fb * rx); k.rs[1] = (C)(-fb * ry); k.rs[2] = (C)(-fb * rz);
     k.a[0] = (C)(dti * rx); k.a[1] = (C)(dti * ry); k.a[2] = (C)(dti * rz);
     k.b[0] = (C)(dtj * rx); k.b[1] = (C)(dtj * ry); k.b[2] = (C)(dtj * rz);
-    k.rv = (C)(rx * wx + ry * wy + rz * wz);
-    k.fb = (C)fb;
+    k.rvs = (C)(-fb * (rx * wx + ry * wy + rz * wz));
+    k.pad = C(0);
 }
 
 // One SHAKE bond update on the corrections of its two sites; true if the
-// bond was corrected.  The residual is d^2 - |P + c|^2 = (D0 - c.c) - 2 P.c
-// and R.(P + c) = R.P + R.c, c the difference of the sites' corrections, so
-// nothing cancels.  SPEC: form the quotient before the tolerance test (a
-// shorter dependency chain for latency-bound callers).
-template <typename C, bool SPEC>
+// bond was corrected.  With c the difference of the sites' corrections the
+// residual is d^2 - |P + c|^2 = D0 - c.(c + 2P), formed as one chain of
+// FMAs from D0, so nothing cancels.  The step divides it by
+// 2 (1/m_i + 1/m_j) R.(P + c); with R.c / R.P of order the bond's relative
+// violation (~1e-3) the reciprocal is taken to first order,
+// y0 (1 - R.c / R.P), which moves the step by ~(R.c / R.P)^2 and so changes
+// how fast the sweeps converge by nothing measurable, never what they
+// converge to: the tolerance test is on the residual itself.  Dependent
+// chain per bond: 7 operations (a full quotient took 13).
+template <typename C>
 __device__ __forceinline__ bool shake_bond(const Dev &d, int gi, int gj, double dsq64, double tol2d, const ShakeK<C> &k,
                                            C &xi, C &yi, C &zi, C &xj, C &yj, C &zj) {
     const C dx = xi - xj, dy = yi - yj, dz = zi - zj;
-    const C pc = k.p[0] * dx + k.p[1] * dy + k.p[2] * dz;
-    const C cc = dx * dx + dy * dy + dz * dz;
-    const C rd = k.r[0] * dx + k.r[1] * dy + k.r[2] * dz;
-    const C diffsq = (k.d0 - cc) - C(2) * pc;
-    C gab = C(0);
-    if constexpr (SPEC) gab = quot<C>(diffsq, k.fa * (k.rp + rd));
+    const C wx = dx + k.p2[0], wy = dy + k.p2[1], wz = dz + k.p2[2];
+    C diffsq = fma(-dx, wx, k.d0);
+    diffsq = fma(-dy, wy, diffsq);
+    diffsq = fma(-dz, wz, diffsq);
+    C ys = fma(-k.r1[0], dx, k.y0);
+    ys = fma(-k.r1[1], dy, ys);
+    ys = fma(-k.r1[2], dz, ys);
     bool act = gt_abs(diffsq, k.thr);
     if constexpr (sizeof(C) == 4) {
         if (fabsf(fabsf(diffsq) - k.thr) < BAND * k.thr)
             act = shake_active64(d, gi, gj, xi, yi, zi, xj, yj, zj, dsq64, tol2d);
     }
     if (act) {
-        if constexpr (!SPEC) gab = quot<C>(diffsq, k.fa * (k.rp + rd));
+        const C gab = diffsq * ys;
         xi += k.a[0] * gab; yi += k.a[1] * gab; zi += k.a[2] * gab;
         xj -= k.b[0] * gab; yj -= k.b[1] * gab; zj -= k.b[2] * gab;
     }
     return act;
 }
 
-// One RATTLE bond update: g = -R.(V + c) (1/dt) / ((1/m_i + 1/m_j) d^2).
+// One RATTLE bond update: g = -fb R.(V + c) = -fb R.V + (-fb R).c, one FMA
+// chain (the factor fb folded into the constants).
 template <typename C>
 __device__ __forceinline__ bool rattle_bond(const Dev &d, int gi, int gj, int ki, int kj, double dsq64, double told,
                                             C tolc, const RattleK<C> &k, C &xi, C &yi, C &zi, C &xj, C &yj, C &zj) {
     const C dx = xi - xj, dy = yi - yj, dz = zi - zj;
-    const C gab = -(k.rv + (k.r[0] * dx + k.r[1] * dy + k.r[2] * dz)) * k.fb;
+    C gab = fma(k.rs[0], dx, k.rvs);
+    gab = fma(k.rs[1], dy, gab);
+    gab = fma(k.rs[2], dz, gab);
     bool act = gt_abs(gab, tolc);
     if constexpr (sizeof(C) == 4) {
         if (fabsf(fabsf(gab) - tolc) < BAND * tolc)
@@ -244,7 +245,7 @@ __device__ __forceinline__ int water_a(const Dev &d, int m, double tol, int maxi
 #pragma unroll
         for (int b = 0; b < 3; b++) {
             const int i = wbi(b), j = wbj(b);
-            if (shake_bond<C, false>(d, g0 + i, g0 + j, cF.dsq64_w[b], tol2d, k[b], cx[i], cy[i], cz[i], cx[j], cy[j],
+            if (shake_bond<C>(d, g0 + i, g0 + j, cF.dsq64_w[b], tol2d, k[b], cx[i], cy[i], cz[i], cx[j], cy[j],
                                      cz[j]))
                 ldone = false;
         }
@@ -424,7 +425,7 @@ __device__ __forceinline__ void surf_a(const Dev &d, int m, double tol, int maxi
             ShakeK<C> k;
             sk.get(b, k);
             C xi = sc[0][si], yi = sc[1][si], zi = sc[2][si], xj = sc[0][sj], yj = sc[1][sj], zj = sc[2][sj];
-            if (shake_bond<C, false>(d, g0 + i, g0 + j, cF.dsq64_s[b], tol2d, k, xi, yi, zi, xj, yj, zj)) {
+            if (shake_bond<C>(d, g0 + i, g0 + j, cF.dsq64_s[b], tol2d, k, xi, yi, zi, xj, yj, zj)) {
                 sc[0][si] = xi; sc[1][si] = yi; sc[2][si] = zi;
                 sc[0][sj] = xj; sc[1][sj] = yj; sc[2][sj] = zj;
                 changed = true;
