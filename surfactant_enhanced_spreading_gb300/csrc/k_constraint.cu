@@ -24,13 +24,14 @@
 //
 // Scheduling.  GB300 issues FP64 at one warp instruction per ~19 cycles per
 // SM whatever the active lanes, with ~64 cycles of dependent latency.  A water
-// (one thread, 3 bonds) is FP64-throughput work; a surfactant (one warp, 28
-// bonds swept as a wavefront) is one long FP64 dependency chain, latency
-// work.  One launch of gridDim = SM count CTAs of 8 warps runs both: the
-// first n_scta CTAs start s_warps warps each on the surfactant queue (few
-// chains per SM, so they do not wait behind water instructions), every other
-// warp takes items of 32 waters from the water queue, and surfactant warps
-// join the water queue when no surfactant is left.  The water list is ordered
+// (one thread, 3 bonds) is FP64-throughput work; a surfactant (4 lanes, 28
+// bonds swept as a wavefront, 8 molecules per warp) is one long FP64
+// dependency chain, latency work.  One launch of gridDim = SM count CTAs of
+// 8 warps runs both: the first n_scta CTAs start s_warps warps each on the
+// surfactant queue (groups of 8 molecules; few chains per SM, so they do not
+// wait behind water instructions), every other warp takes items of 32 waters
+// from the water queue, and surfactant warps join the water queue when no
+// surfactant is left.  The water list is ordered
 // by each molecule's sweep count in the previous call (most first, reordered
 // at every list rebuild), so the 32 lanes of an item iterate alike and the
 // longest items start first.  Which warp takes which molecule changes no
@@ -325,110 +326,95 @@ __device__ __forceinline__ int water_b(const Dev &d, int m, double tol, int maxi
 
 // ---------------------------------------------------------------- surfactants
 
-__device__ inline double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(FULL, v, o);
-    return v;   // lane 0
-}
-
 // Gauss-Seidel sweeps as a wavefront: sweep k starts WF_LAG bonds after
-// sweep k - 1 and runs on lane k mod WF_LANES, one bond per lane and step.
-// Two bonds that share a site are never more than 7 apart in the bond order
-// (site 17: bonds 16 and 23), so with a lag of 8 every site sees the
-// updates of the sequential order, in that order, and no two lanes touch the
-// same site in one step: the result is that of the sequential sweeps.
+// sweep k - 1 and runs on wavefront lane k mod WF_LANES, one bond per lane
+// and step.  Two bonds that share a site are never more than 7 apart in the
+// bond order (site 17: bonds 16 and 23), so with a lag of 8 every site sees
+// the updates of the sequential order, in that order, and no two lanes touch
+// the same site in one step: the result is that of the sequential sweeps.
 // Sweeps started after the first sweep without a correction make no
 // correction either (they see the same, converged state), so the state at
 // that point is final.  No more than maxit + 1 sweeps run, as in the
-// sequential loop.  One warp per molecule; its 29 lanes do the per-site FP64
-// work and form the bond constants.
+// sequential loop.
+//
+// A warp carries MPW = 8 molecules, one per group of 4 lanes: a wavefront
+// step is then one warp instruction stream for 8 molecules, so every FP64
+// warp instruction (~19 cycles of the SM's FP64 pipe whatever the active
+// lanes) serves 32 lanes instead of 4.  Each group stops when its molecule
+// has converged or failed; the warp stops when all have.
 constexpr int WF_LAG = 8;
 constexpr int WF_LANES = 4;   // ceil(NBOND / WF_LAG) sweeps in flight
+constexpr int MPW = 32 / WF_LANES;   // molecules per warp
 
-// Shared-memory layout of one molecule's bond records and site corrections:
-// field-major, index skewed by one slot every 8 (i -> i + i / 8), so the four
-// lanes of a wavefront step (bonds b, b-8, b-16, b-24 and their sites) fall
-// on different banks.
+// Shared memory of one molecule: bond records and site corrections
+// field-major with the index skewed by one slot every 8 (i -> i + i / 8), so
+// the four lanes of a wavefront step (bonds b, b-8, b-16, b-24 and their
+// sites) fall on different banks; the FP64 site vectors of the setup; and a
+// stagger of 4 slots, so that the 8 molecules of a warp, whose lanes access
+// the same offsets in the same step, fall on different banks as well.
 __device__ __forceinline__ int skew8(int i) { return i + (i >> 3); }
 constexpr int SK = 32;   // padded length (largest skewed index 28 + 3)
 template <typename C, int NF>
-struct BondRecords {
-    C v[NF][SK];
+struct MolSmem {
+    C rec[NF][SK];
+    C sc[3][SK];
+    double sv[6][SK];   // per site: old position, then predictor position (SHAKE) or velocity (RATTLE)
+    C stagger[4];
     template <typename K>
     __device__ void put(int b, const K &k) {
         const C *f = reinterpret_cast<const C *>(&k);
 #pragma unroll
-        for (int q = 0; q < NF; q++) v[q][skew8(b)] = f[q];
+        for (int q = 0; q < NF; q++) rec[q][skew8(b)] = f[q];
     }
     template <typename K>
     __device__ void get(int b, K &k) const {
         C *f = reinterpret_cast<C *>(&k);
 #pragma unroll
-        for (int q = 0; q < NF; q++) f[q] = v[q][skew8(b)];
+        for (int q = 0; q < NF; q++) f[q] = rec[q][skew8(b)];
     }
-};
-// one surfactant warp's shared memory
-template <typename C, int NF>
-struct SurfSmem {
-    BondRecords<C, NF> sk;
-    C sc[3][SK];
 };
 
-// SHAKE half of one surfactant (the whole warp)
-template <typename C>
-__device__ __forceinline__ void surf_a(const Dev &d, int m, double tol, int maxit, SurfSmem<C, 16> &sm) {
-    static_assert(sizeof(ShakeK<C>) == 16 * sizeof(C), "ShakeK is 16 values");
-    auto &sk = sm.sk;
-    auto &sc = sm.sc;
-    const int lane = threadIdx.x & 31;
-    const int g0 = d.mfirst[m];
-    const double escale = __dsub_rn(1.0, __dmul_rn(d.eta[d.mrep[m]], DT) * 0.5);
-    const bool site = lane < NSURF;
-    const int g = g0 + (site ? lane : 0);
-    double rx = 0.0, ry = 0.0, rz = 0.0, px = 0.0, py = 0.0, pz = 0.0, ke = 0.0;
-    if (site) {
-        double vx = d.vx[g], vy = d.vy[g], vz = d.vz[g], ax = d.ax[g], ay = d.ay[g], az = d.az[g];
-        rx = d.x[g]; ry = d.y[g]; rz = d.z[g];
-        ke = __dmul_rn(cF.mass64[2 + lane], __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz)));
-        px = pred_a(rx, vx, ax, escale);
-        py = pred_a(ry, vy, ay, escale);
-        pz = pred_a(rz, vz, az, escale);
-        d.x[g] = px; d.y[g] = py; d.z[g] = pz;
-        d.vx[g] = vel_a(vx, ax, escale);
-        d.vy[g] = vel_a(vy, ay, escale);
-        d.vz[g] = vel_a(vz, az, escale);
-        sc[0][skew8(lane)] = sc[1][skew8(lane)] = sc[2][skew8(lane)] = C(0);
-    }
-    const double ke0 = warp_sum(ke);
+// sum over the 4 lanes of a group (fixed order), result in every lane of it
+__device__ __forceinline__ double group_sum(double v) {
+    v += __shfl_xor_sync(FULL, v, 1);
+    v += __shfl_xor_sync(FULL, v, 2);
+    return v;
+}
+
+// The wavefront of SHAKE (SHAKE = true) or RATTLE over the 8 molecules of a
+// warp.  Lane (g, w): molecule g, wavefront lane w.  Returns through fail
+// whether its molecule ran out of sweeps.
+template <typename C, bool SHAKE>
+__device__ __forceinline__ void surf_wavefront(const Dev &d, MolSmem<C, SHAKE ? 16 : 11> &sm, int g0, bool live,
+                                               double tol, int maxit, bool &fail) {
+    const int lane = threadIdx.x & 31, w = lane & (WF_LANES - 1), grp = lane >> 2;
+    const unsigned gmask = 0xFu << (4 * grp);
     const double tol2d = 2.0 * tol;
-    {   // bond lane: sites sbi32(lane) and lane + 1
-        const int bi = lane < NBOND ? sbi32(lane) : 0, bj = lane < NBOND ? lane + 1 : 0;
-        const double ex = __shfl_sync(FULL, rx, bi) - __shfl_sync(FULL, rx, bj);
-        const double ey = __shfl_sync(FULL, ry, bi) - __shfl_sync(FULL, ry, bj);
-        const double ez = __shfl_sync(FULL, rz, bi) - __shfl_sync(FULL, rz, bj);
-        const double qx = __shfl_sync(FULL, px, bi) - __shfl_sync(FULL, px, bj);
-        const double qy = __shfl_sync(FULL, py, bi) - __shfl_sync(FULL, py, bj);
-        const double qz = __shfl_sync(FULL, pz, bi) - __shfl_sync(FULL, pz, bj);
-        if (lane < NBOND) {
-            ShakeK<C> k;
-            shake_make<C>(ex, ey, ez, qx, qy, qz, cF.dsq64_s[lane], cF.rm64[2 + bi], cF.rm64[2 + bj], tol2d, k);
-            sk.put(lane, k);
-        }
-    }
-    __syncwarp();   // bond constants, zeroed corrections and the predictor stores
-    int kmine = lane, fail = 0;
-    bool changed = false;
+    const C tolc = (C)tol;
+    int kmine = w;
+    bool changed = false, done = !live;
+    fail = false;
     for (int t = 0;; t++) {
         bool clean = false, last = false;
         const int b = t - WF_LAG * kmine;
-        if (lane < WF_LANES && kmine <= maxit && b >= 0 && b < NBOND) {
+        if (!done && kmine <= maxit && b >= 0 && b < NBOND) {
             const int i = sbi32(b), j = b + 1, si = skew8(i), sj = skew8(j);
-            ShakeK<C> k;
-            sk.get(b, k);
-            C xi = sc[0][si], yi = sc[1][si], zi = sc[2][si], xj = sc[0][sj], yj = sc[1][sj], zj = sc[2][sj];
-            if (shake_bond<C>(d, g0 + i, g0 + j, cF.dsq64_s[b], tol2d, k, xi, yi, zi, xj, yj, zj)) {
-                sc[0][si] = xi; sc[1][si] = yi; sc[2][si] = zi;
-                sc[0][sj] = xj; sc[1][sj] = yj; sc[2][sj] = zj;
+            C xi = sm.sc[0][si], yi = sm.sc[1][si], zi = sm.sc[2][si];
+            C xj = sm.sc[0][sj], yj = sm.sc[1][sj], zj = sm.sc[2][sj];
+            bool act;
+            if constexpr (SHAKE) {
+                ShakeK<C> k;
+                sm.get(b, k);
+                act = shake_bond<C>(d, g0 + i, g0 + j, cF.dsq64_s[b], tol2d, k, xi, yi, zi, xj, yj, zj);
+            } else {
+                RattleK<C> k;
+                sm.get(b, k);
+                act = rattle_bond<C>(d, g0 + i, g0 + j, 2 + i, 2 + j, cF.dsq64_s[b], tol, tolc, k, xi, yi, zi, xj, yj,
+                                     zj);
+            }
+            if (act) {
+                sm.sc[0][si] = xi; sm.sc[1][si] = yi; sm.sc[2][si] = zi;
+                sm.sc[0][sj] = xj; sm.sc[1][sj] = yj; sm.sc[2][sj] = zj;
                 changed = true;
             }
             if (b == NBOND - 1) {
@@ -439,113 +425,149 @@ __device__ __forceinline__ void surf_a(const Dev &d, int m, double tol, int maxi
             }
         }
         __syncwarp();
-        if (__any_sync(FULL, clean)) break;
-        if (__any_sync(FULL, last)) { fail = 1; break; }
+        const unsigned bc = __ballot_sync(FULL, clean), bl = __ballot_sync(FULL, last);
+        if (!done) {
+            if (bc & gmask) done = true;
+            else if (bl & gmask) { done = true; fail = true; }
+        }
+        if (__all_sync(FULL, done)) break;
     }
+}
+
+// SHAKE half of up to 8 surfactants (the whole warp): molecules mols[0..n)
+template <typename C>
+__device__ __forceinline__ void surf_a(const Dev &d, const int *mols, int n, double tol, int maxit,
+                                       MolSmem<C, 16> *sms) {
+    static_assert(sizeof(ShakeK<C>) == 16 * sizeof(C), "ShakeK is 16 values");
+    const int lane = threadIdx.x & 31, w = lane & (WF_LANES - 1), grp = lane >> 2;
+    const bool live = grp < n;
+    const int m = live ? mols[grp] : 0;
+    const int g0 = live ? d.mfirst[m] : 0;
+    MolSmem<C, 16> &sm = sms[grp];
+    // sites w, w + 4, ...: predictor, kinetic sum before, FP64 site vectors
+    double ke0 = 0.0;
+    if (live) {
+        const double escale = __dsub_rn(1.0, __dmul_rn(d.eta[d.mrep[m]], DT) * 0.5);
+        for (int s = w; s < NSURF; s += WF_LANES) {
+            const int g = g0 + s;
+            double vx = d.vx[g], vy = d.vy[g], vz = d.vz[g], ax = d.ax[g], ay = d.ay[g], az = d.az[g];
+            const double rx = d.x[g], ry = d.y[g], rz = d.z[g];
+            ke0 = __dadd_rn(ke0, __dmul_rn(cF.mass64[2 + s],
+                                           __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
+            const double px = pred_a(rx, vx, ax, escale), py = pred_a(ry, vy, ay, escale), pz = pred_a(rz, vz, az, escale);
+            d.x[g] = px; d.y[g] = py; d.z[g] = pz;
+            d.vx[g] = vel_a(vx, ax, escale);
+            d.vy[g] = vel_a(vy, ay, escale);
+            d.vz[g] = vel_a(vz, az, escale);
+            sm.sv[0][s] = rx; sm.sv[1][s] = ry; sm.sv[2][s] = rz;
+            sm.sv[3][s] = px; sm.sv[4][s] = py; sm.sv[5][s] = pz;
+            sm.sc[0][skew8(s)] = sm.sc[1][skew8(s)] = sm.sc[2][skew8(s)] = C(0);
+        }
+    }
+    ke0 = group_sum(ke0);
+    __syncwarp();
+    // bonds w, w + 4, ...: constants
+    if (live) {
+        const double tol2d = 2.0 * tol;
+        for (int b = w; b < NBOND; b += WF_LANES) {
+            const int i = sbi32(b), j = b + 1;
+            ShakeK<C> k;
+            shake_make<C>(sm.sv[0][i] - sm.sv[0][j], sm.sv[1][i] - sm.sv[1][j], sm.sv[2][i] - sm.sv[2][j],
+                          sm.sv[3][i] - sm.sv[3][j], sm.sv[4][i] - sm.sv[4][j], sm.sv[5][i] - sm.sv[5][j],
+                          cF.dsq64_s[b], cF.rm64[2 + i], cF.rm64[2 + j], tol2d, k);
+            sm.put(b, k);
+        }
+    }
+    __syncwarp();
+    bool fail;
+    surf_wavefront<C, true>(d, sm, g0, live, tol, maxit, fail);
     double ke1 = 0.0;
-    if (site) {
-        const double cxi = sc[0][skew8(lane)], cyi = sc[1][skew8(lane)], czi = sc[2][skew8(lane)];
-        d.x[g] = __dadd_rn(px, cxi);
-        d.y[g] = __dadd_rn(py, cyi);
-        d.z[g] = __dadd_rn(pz, czi);
-        double vx = __dadd_rn(d.vx[g], cxi), vy = __dadd_rn(d.vy[g], cyi), vz = __dadd_rn(d.vz[g], czi);
-        d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
-        ke1 = __dmul_rn(cF.mass64[2 + lane], __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz)));
+    if (live) {
+        for (int s = w; s < NSURF; s += WF_LANES) {
+            const int g = g0 + s;
+            const double cxi = sm.sc[0][skew8(s)], cyi = sm.sc[1][skew8(s)], czi = sm.sc[2][skew8(s)];
+            d.x[g] = __dadd_rn(sm.sv[3][s], cxi);
+            d.y[g] = __dadd_rn(sm.sv[4][s], cyi);
+            d.z[g] = __dadd_rn(sm.sv[5][s], czi);
+            const double vx = __dadd_rn(d.vx[g], cxi), vy = __dadd_rn(d.vy[g], cyi), vz = __dadd_rn(d.vz[g], czi);
+            d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
+            ke1 = __dadd_rn(ke1, __dmul_rn(cF.mass64[2 + s],
+                                           __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
+        }
     }
-    ke1 = warp_sum(ke1);
-    if (lane == 0) {
+    ke1 = group_sum(ke1);
+    if (live && w == 0) {
         d.ke[2 * m] = ke0;
         d.ke[2 * m + 1] = ke1;
         if (fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
     }
-    __syncwarp();   // the shared records are reused by the warp's next molecule
+    __syncwarp();   // the shared records are reused by the warp's next molecules
 }
 
-// RATTLE half of one surfactant (the whole warp)
+// RATTLE half of up to 8 surfactants (the whole warp)
 template <typename C>
-__device__ __forceinline__ void surf_b(const Dev &d, int m, double tol, int maxit, SurfSmem<C, 11> &sm) {
+__device__ __forceinline__ void surf_b(const Dev &d, const int *mols, int n, double tol, int maxit,
+                                       MolSmem<C, 11> *sms) {
     static_assert(sizeof(RattleK<C>) == 11 * sizeof(C), "RattleK is 11 values");
-    auto &sk = sm.sk;
-    auto &sc = sm.sc;
-    const int lane = threadIdx.x & 31;
-    const int g0 = d.mfirst[m];
-    const double escale = __ddiv_rn(2.0, __dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[m]], DT)));
-    const bool site = lane < NSURF;
-    const int g = g0 + (site ? lane : 0);
-    double rx = 0.0, ry = 0.0, rz = 0.0, vx = 0.0, vy = 0.0, vz = 0.0;
-    if (site) {
-        const double mi = cF.mass64[2 + lane];
-        double ax = __ddiv_rn(__dmul_rn(d.fx[g], DTSQ2), mi), ay = __ddiv_rn(__dmul_rn(d.fy[g], DTSQ2), mi),
-               az = __ddiv_rn(__dmul_rn(d.fz[g], DTSQ2), mi);
-        d.ax[g] = ax; d.ay[g] = ay; d.az[g] = az;
-        vx = __dmul_rn(escale, __dadd_rn(d.vx[g], ax));
-        vy = __dmul_rn(escale, __dadd_rn(d.vy[g], ay));
-        vz = __dmul_rn(escale, __dadd_rn(d.vz[g], az));
-        d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
-        rx = d.x[g]; ry = d.y[g]; rz = d.z[g];
-        sc[0][skew8(lane)] = sc[1][skew8(lane)] = sc[2][skew8(lane)] = C(0);
-    }
-    {
-        const int bi = lane < NBOND ? sbi32(lane) : 0, bj = lane < NBOND ? lane + 1 : 0;
-        const double ex = __shfl_sync(FULL, rx, bi) - __shfl_sync(FULL, rx, bj);
-        const double ey = __shfl_sync(FULL, ry, bi) - __shfl_sync(FULL, ry, bj);
-        const double ez = __shfl_sync(FULL, rz, bi) - __shfl_sync(FULL, rz, bj);
-        const double wx = __shfl_sync(FULL, vx, bi) - __shfl_sync(FULL, vx, bj);
-        const double wy = __shfl_sync(FULL, vy, bi) - __shfl_sync(FULL, vy, bj);
-        const double wz = __shfl_sync(FULL, vz, bi) - __shfl_sync(FULL, vz, bj);
-        if (lane < NBOND) {
-            RattleK<C> k;
-            rattle_make<C>(ex, ey, ez, wx, wy, wz, cF.rmdt64[2 + bi], cF.rmdt64[2 + bj], cF.fb64_s[lane], k);
-            sk.put(lane, k);
+    const int lane = threadIdx.x & 31, w = lane & (WF_LANES - 1), grp = lane >> 2;
+    const bool live = grp < n;
+    const int m = live ? mols[grp] : 0;
+    const int g0 = live ? d.mfirst[m] : 0;
+    MolSmem<C, 11> &sm = sms[grp];
+    if (live) {
+        const double escale = __ddiv_rn(2.0, __dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[m]], DT)));
+        for (int s = w; s < NSURF; s += WF_LANES) {
+            const int g = g0 + s;
+            const double mi = cF.mass64[2 + s];
+            const double ax = __ddiv_rn(__dmul_rn(d.fx[g], DTSQ2), mi), ay = __ddiv_rn(__dmul_rn(d.fy[g], DTSQ2), mi),
+                         az = __ddiv_rn(__dmul_rn(d.fz[g], DTSQ2), mi);
+            d.ax[g] = ax; d.ay[g] = ay; d.az[g] = az;
+            const double vx = __dmul_rn(escale, __dadd_rn(d.vx[g], ax));
+            const double vy = __dmul_rn(escale, __dadd_rn(d.vy[g], ay));
+            const double vz = __dmul_rn(escale, __dadd_rn(d.vz[g], az));
+            d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
+            sm.sv[0][s] = d.x[g]; sm.sv[1][s] = d.y[g]; sm.sv[2][s] = d.z[g];
+            sm.sv[3][s] = vx; sm.sv[4][s] = vy; sm.sv[5][s] = vz;
+            sm.sc[0][skew8(s)] = sm.sc[1][skew8(s)] = sm.sc[2][skew8(s)] = C(0);
         }
     }
     __syncwarp();
-    const C tolc = (C)tol;
-    int kmine = lane, fail = 0;
-    bool changed = false;
-    for (int t = 0;; t++) {
-        bool clean = false, last = false;
-        const int b = t - WF_LAG * kmine;
-        if (lane < WF_LANES && kmine <= maxit && b >= 0 && b < NBOND) {
-            const int i = sbi32(b), j = b + 1, si = skew8(i), sj = skew8(j);
+    if (live) {
+        for (int b = w; b < NBOND; b += WF_LANES) {
+            const int i = sbi32(b), j = b + 1;
             RattleK<C> k;
-            sk.get(b, k);
-            C xi = sc[0][si], yi = sc[1][si], zi = sc[2][si], xj = sc[0][sj], yj = sc[1][sj], zj = sc[2][sj];
-            if (rattle_bond<C>(d, g0 + i, g0 + j, 2 + i, 2 + j, cF.dsq64_s[b], tol, tolc, k, xi, yi, zi, xj, yj, zj)) {
-                sc[0][si] = xi; sc[1][si] = yi; sc[2][si] = zi;
-                sc[0][sj] = xj; sc[1][sj] = yj; sc[2][sj] = zj;
-                changed = true;
-            }
-            if (b == NBOND - 1) {
-                clean = !changed;
-                last = changed && kmine == maxit;
-                changed = false;
-                kmine += WF_LANES;
-            }
+            rattle_make<C>(sm.sv[0][i] - sm.sv[0][j], sm.sv[1][i] - sm.sv[1][j], sm.sv[2][i] - sm.sv[2][j],
+                           sm.sv[3][i] - sm.sv[3][j], sm.sv[4][i] - sm.sv[4][j], sm.sv[5][i] - sm.sv[5][j],
+                           cF.rmdt64[2 + i], cF.rmdt64[2 + j], cF.fb64_s[b], k);
+            sm.put(b, k);
         }
-        __syncwarp();
-        if (__any_sync(FULL, clean)) break;
-        if (__any_sync(FULL, last)) { fail = 1; break; }
     }
-    if (site) {
-        d.vx[g] = __dadd_rn(vx, (double)sc[0][skew8(lane)]);
-        d.vy[g] = __dadd_rn(vy, (double)sc[1][skew8(lane)]);
-        d.vz[g] = __dadd_rn(vz, (double)sc[2][skew8(lane)]);
+    __syncwarp();
+    bool fail;
+    surf_wavefront<C, false>(d, sm, g0, live, tol, maxit, fail);
+    if (live) {
+        for (int s = w; s < NSURF; s += WF_LANES) {
+            const int g = g0 + s;
+            d.vx[g] = __dadd_rn(sm.sv[3][s], (double)sm.sc[0][skew8(s)]);
+            d.vy[g] = __dadd_rn(sm.sv[4][s], (double)sm.sc[1][skew8(s)]);
+            d.vz[g] = __dadd_rn(sm.sv[5][s], (double)sm.sc[2][skew8(s)]);
+        }
     }
-    if (lane == 0 && fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
-    __syncwarp();   // the shared records are reused by the warp's next molecule
+    if (live && w == 0 && fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    __syncwarp();   // the shared records are reused by the warp's next molecules
 }
 
 // ---------------------------------------------------------------- the persistent launch
 
 constexpr int CW = 8;                 // warps per CTA
 constexpr int CW_THREADS = 32 * CW;
+constexpr int MAX_SURF_WARPS = 4;     // surfactant warps per CTA (shared memory: 8 molecules each)
 
 struct CPlan {
     const int *smols;   // surfactant molecules
     const int *wlist;   // water molecules in work order
     uint8_t *wsw;       // per molecule: sweeps of this half's last call (waters)
-    unsigned *ctl;      // [0] next surfactant, [1] next water item, [2] CTAs finished
+    unsigned *ctl;      // [0] next surfactant group of 8, [1] next water item, [2] CTAs finished
     int ns, nw;
     int n_scta;         // CTAs that start on the surfactant queue
     int s_warps;        // surfactant warps in each of them
@@ -558,14 +580,16 @@ __global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool surf_cta = (int)blockIdx.x < p.n_scta;
     if (surf_cta && warp < p.s_warps) {
-        SurfSmem<C, NF> &sm = reinterpret_cast<SurfSmem<C, NF> *>(cs_smem)[warp];
+        MolSmem<C, NF> *sms = reinterpret_cast<MolSmem<C, NF> *>(cs_smem) + MPW * warp;
         for (;;) {
             unsigned s = 0;
             if (lane == 0) s = atomicAdd(&p.ctl[0], 1u);
             s = __shfl_sync(FULL, s, 0);
-            if (s >= (unsigned)p.ns) break;
-            if constexpr (SHAKE) surf_a<C>(d, p.smols[s], tol, maxit, sm);
-            else surf_b<C>(d, p.smols[s], tol, maxit, sm);
+            const long long s0 = (long long)MPW * s;
+            if (s0 >= p.ns) break;
+            const int n = p.ns - (int)s0 < MPW ? p.ns - (int)s0 : MPW;
+            if constexpr (SHAKE) surf_a<C>(d, p.smols + s0, n, tol, maxit, sms);
+            else surf_b<C>(d, p.smols + s0, n, tol, maxit, sms);
         }
     }
     // the other warps of a surfactant CTA stay idle, so its chains keep the SM's FP64 pipe
@@ -669,13 +693,17 @@ bool upload_tables_fast(const Tables &t, cudaStream_t st) {
     return cudaMemcpyToSymbolAsync(cF, &f, sizeof f, 0, cudaMemcpyHostToDevice, st) == cudaSuccess;
 }
 
-int constraint_max_surf_warps() { return CW; }
+int constraint_max_surf_warps() { return MAX_SURF_WARPS; }
 
 namespace {
 template <typename C, bool SHAKE>
+constexpr size_t surf_smem(int s_warps) {
+    return (size_t)s_warps * MPW * sizeof(MolSmem<C, SHAKE ? 16 : 11>);
+}
+
+template <typename C, bool SHAKE>
 void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, const ConstraintShape &sh, double tol,
                         int maxit, cudaStream_t st) {
-    constexpr int NF = SHAKE ? 16 : 11;
     CPlan p;
     p.smols = smols;
     p.wlist = SHAKE ? d.wlist_a : d.wlist_b;
@@ -683,13 +711,25 @@ void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, const Co
     p.ctl = d.cctl + (SHAKE ? 0 : 4);
     p.ns = ns;
     p.nw = nw;
-    p.s_warps = sh.s_warps < 1 ? 1 : (sh.s_warps > CW ? CW : sh.s_warps);
-    const int need = (ns + p.s_warps - 1) / p.s_warps;
+    p.s_warps = sh.s_warps < 1 ? 1 : (sh.s_warps > MAX_SURF_WARPS ? MAX_SURF_WARPS : sh.s_warps);
+    const int groups = (ns + MPW - 1) / MPW;
+    const int need = (groups + p.s_warps - 1) / p.s_warps;
     p.n_scta = ns ? (need < sh.grid ? need : sh.grid) : 0;
-    const size_t smem = p.n_scta ? (size_t)p.s_warps * sizeof(SurfSmem<C, NF>) : 0;
+    const size_t smem = p.n_scta ? surf_smem<C, SHAKE>(p.s_warps) : 0;
     k_constrain<C, SHAKE><<<sh.grid, CW_THREADS, smem, st>>>(d, p, tol, maxit);
 }
 }  // namespace
+
+void init_constraint_kernels() {
+    cudaFuncSetAttribute(k_constrain<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)surf_smem<double, true>(MAX_SURF_WARPS));
+    cudaFuncSetAttribute(k_constrain<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)surf_smem<double, false>(MAX_SURF_WARPS));
+    cudaFuncSetAttribute(k_constrain<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)surf_smem<float, true>(MAX_SURF_WARPS));
+    cudaFuncSetAttribute(k_constrain<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)surf_smem<float, false>(MAX_SURF_WARPS));
+}
 
 // fp32: 1 for FP32 sweeps, 0 for FP64 sweeps
 void launch_move_a32(const Dev &d, int nw, const int *smols, int ns, const ConstraintShape &sh, cudaStream_t st,

@@ -494,6 +494,7 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "stream"); }
     for (int k = 0; k < 16; k++) cudaEventCreate(&c->ev[k]);
     init_force_kernels();
+    init_constraint_kernels();
     {
         int dev = 0;
         cudaGetDevice(&dev);
@@ -1043,8 +1044,7 @@ int tune_constraints(sesp_ctx *c) {
     cudaEventCreate(&e1);
     float best = 1e30f;
     int pick = c->cshape.s_warps;
-    for (int sw : {1, 2, 3, 4, 6, 8}) {
-        if (sw > constraint_max_surf_warps()) continue;
+    for (int sw = 1; sw <= constraint_max_surf_warps(); sw++) {
         const ConstraintShape sh = {c->cshape.grid, sw};
         float t[3];
         for (int r = 0; r < 3; r++) {
