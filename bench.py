@@ -218,7 +218,7 @@ def run_ours(args, ws, rank, local):
     eng.run(kb, args.warmup)
     kb += args.warmup
     tile, ctas, ctas_max = eng.autotune()   # launch shapes (no effect on results)
-    surf_warps = eng.constraint_tuning()[0]
+    surf_warps, mols_per_warp = eng.constraint_tuning()[:2]
     eng.run(kb, 1)
     kb += 1
     D.barrier()
@@ -340,7 +340,8 @@ def run_ours(args, ws, rank, local):
                    "l2": "flushed between timed steps (256 MB write outside the timed intervals)",
                    "pair_field_shape": {"tile": tile, "ctas_per_sm": ctas, "ctas_per_sm_max": ctas_max,
                                         "how": "sesp_autotune before the timed steps"},
-                   "constraint_shape": {"surf_warps_per_cta": surf_warps, "how": "sesp_autotune"},
+                   "constraint_shape": {"surf_warps_per_cta": surf_warps, "surfactants_per_warp": mols_per_warp,
+                                        "how": "sesp_autotune"},
                    "parallelism": f"replicas x{ws}"},
         "ns_per_day": ns_day,
         "plain_fp64": {"value": plain_value, "unit": "atom-steps/s", "steps": args.plain_steps,

@@ -179,13 +179,15 @@ int sesp_autotune(sesp_ctx *ctx, int out[3]);
 int sesp_tuning(sesp_ctx *ctx, int out[3]);
 int sesp_set_tuning(sesp_ctx *ctx, int tile, int ctas_per_sm);
 /* Launch shape of the constraint halves on the mixed paths: surfactant warps
- * per CTA (1..4), each carrying 8 molecules.  The surfactants' FP64 sweep
- * chains start on the first ceil(n_surf / (8 surf_warps)) CTAs (one CTA per
- * SM), waters fill every other warp.  The shape changes no result, only the time; sesp_autotune picks it
- * on the mixed paths (restoring the state its trials change).
- * out = {surf_warps, largest}.  New for the GPU build. */
-int sesp_set_constraint_tuning(sesp_ctx *ctx, int surf_warps);
-int sesp_constraint_tuning(sesp_ctx *ctx, int out[2]);
+ * per CTA (1..4) and surfactants per such warp (1..8).  The surfactants'
+ * FP64 sweep chains start on the first
+ * ceil(n_surf / (mols_per_warp surf_warps)) CTAs (one CTA per SM), waters
+ * fill every other warp.  The shape changes no result, only the time;
+ * sesp_autotune picks it on the mixed paths (restoring the state its trials
+ * change).  out = {surf_warps, mols_per_warp, largest surf_warps, largest
+ * mols_per_warp}.  New for the GPU build. */
+int sesp_set_constraint_tuning(sesp_ctx *ctx, int surf_warps, int mols_per_warp);
+int sesp_constraint_tuning(sesp_ctx *ctx, int out[4]);
 /* The energies of sesp_energies, bit for bit, without allocating: no
  * cudaMalloc or cudaFree (sesp_energies does both on every call, and cudaFree
  * waits for every stream on the device).  For callers that share the GPU with

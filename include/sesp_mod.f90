@@ -145,15 +145,16 @@ module sesp_mod
       type(c_ptr), value :: ctx
       integer(c_int), value :: tile, ctas_per_sm
     end function
-    integer(c_int) function sesp_set_constraint_tuning(ctx, surf_warps) bind(C, name="sesp_set_constraint_tuning")
+    integer(c_int) function sesp_set_constraint_tuning(ctx, surf_warps, mols_per_warp) &
+        bind(C, name="sesp_set_constraint_tuning")
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
-      integer(c_int), value :: surf_warps
+      integer(c_int), value :: surf_warps, mols_per_warp
     end function
     integer(c_int) function sesp_constraint_tuning(ctx, out) bind(C, name="sesp_constraint_tuning")
       import :: c_int, c_ptr
       type(c_ptr), value :: ctx
-      integer(c_int), intent(out) :: out(2)
+      integer(c_int), intent(out) :: out(4)
     end function
     ! sesp_energies without allocating (fixed scratch; at most 131072 sites)
     integer(c_int) function sesp_energies_static(ctx, e) bind(C, name="sesp_energies_static")

@@ -154,7 +154,8 @@ __device__ inline void rattle_make(double rx, double ry, double rz, double wx, d
 // relative error t^8, which leaves the converged state within rounding of
 // the exact quotient's (the tolerance test is on the residual itself;
 // stopping at t^4 already moved ~1 % of the sites by more than 1e-8).
-// Dependent chain per bond: 9 operations (a full quotient took 13).
+// FP64 operations per bond: 9 for the test, 16 more for a correction (with
+// a full quotient 13 more, on a longer dependent chain).
 template <typename C>
 __device__ __forceinline__ bool shake_bond(const Dev &d, int gi, int gj, double dsq64, double tol2d, const ShakeK<C> &k,
                                            C &xi, C &yi, C &zi, C &xj, C &yj, C &zj) {
@@ -163,17 +164,17 @@ __device__ __forceinline__ bool shake_bond(const Dev &d, int gi, int gj, double 
     C diffsq = fma(-dx, wx, k.d0);
     diffsq = fma(-dy, wy, diffsq);
     diffsq = fma(-dz, wz, diffsq);
-    C t = k.rr[2] * dz;
-    t = fma(k.rr[1], dy, t);
-    t = fma(k.rr[0], dx, t);
-    const C t2 = t * t;
-    const C ya = fma(-k.y0, t, k.y0), yb = fma(t, t, C(1)), yc = fma(t2, t2, C(1));
     bool act = gt_abs(diffsq, k.thr);
     if constexpr (sizeof(C) == 4) {
         if (fabsf(fabsf(diffsq) - k.thr) < BAND * k.thr)
             act = shake_active64(d, gi, gj, xi, yi, zi, xj, yj, zj, dsq64, tol2d);
     }
-    if (act) {
+    if (act) {   // the step only for a corrected bond: a bond within tolerance costs 9 operations
+        C t = k.rr[2] * dz;
+        t = fma(k.rr[1], dy, t);
+        t = fma(k.rr[0], dx, t);
+        const C t2 = t * t;
+        const C ya = fma(-k.y0, t, k.y0), yb = fma(t, t, C(1)), yc = fma(t2, t2, C(1));
         const C gab = (diffsq * ya) * (yb * yc);
         xi += k.a[0] * gab; yi += k.a[1] * gab; zi += k.a[2] * gab;
         xj -= k.b[0] * gab; yj -= k.b[1] * gab; zj -= k.b[2] * gab;
@@ -337,11 +338,14 @@ __device__ __forceinline__ int water_b(const Dev &d, int m, double tol, int maxi
 // that point is final.  No more than maxit + 1 sweeps run, as in the
 // sequential loop.
 //
-// A warp carries MPW = 8 molecules, one per group of 4 lanes: a wavefront
-// step is then one warp instruction stream for 8 molecules, so every FP64
-// warp instruction (~19 cycles of the SM's FP64 pipe whatever the active
-// lanes) serves 32 lanes instead of 4.  Each group stops when its molecule
-// has converged or failed; the warp stops when all have.
+// A warp carries up to MPW = 8 molecules, one per group of 4 lanes (the
+// launch picks how many: mpw).  An FP64 warp instruction costs a scheduler
+// partition ~64 cycles whatever its active lanes, so a wavefront step costs
+// the same for 1 molecule as for 8: more molecules per warp is more
+// throughput for many surfactants, while with one molecule per warp a step
+// whose 4 bonds all lie within tolerance more often skips the correction
+// arithmetic.  Each group stops when its molecule has converged or failed;
+// the warp stops when all have.
 constexpr int WF_LAG = 8;
 constexpr int WF_LANES = 4;   // ceil(NBOND / WF_LAG) sweeps in flight
 constexpr int MPW = 32 / WF_LANES;   // molecules per warp
@@ -567,10 +571,11 @@ struct CPlan {
     const int *smols;   // surfactant molecules
     const int *wlist;   // water molecules in work order
     uint8_t *wsw;       // per molecule: sweeps of this half's last call (waters)
-    unsigned *ctl;      // [0] next surfactant group of 8, [1] next water item, [2] CTAs finished
+    unsigned *ctl;      // [0] next surfactant group, [1] next water item, [2] CTAs finished
     int ns, nw;
     int n_scta;         // CTAs that start on the surfactant queue
     int s_warps;        // surfactant warps in each of them
+    int mpw;            // surfactants per warp (groups of 4 lanes), 1..MPW
 };
 
 template <typename C, bool SHAKE>
@@ -580,14 +585,14 @@ __global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool surf_cta = (int)blockIdx.x < p.n_scta;
     if (surf_cta && warp < p.s_warps) {
-        MolSmem<C, NF> *sms = reinterpret_cast<MolSmem<C, NF> *>(cs_smem) + MPW * warp;
+        MolSmem<C, NF> *sms = reinterpret_cast<MolSmem<C, NF> *>(cs_smem) + p.mpw * warp;
         for (;;) {
             unsigned s = 0;
             if (lane == 0) s = atomicAdd(&p.ctl[0], 1u);
             s = __shfl_sync(FULL, s, 0);
-            const long long s0 = (long long)MPW * s;
+            const long long s0 = (long long)p.mpw * s;
             if (s0 >= p.ns) break;
-            const int n = p.ns - (int)s0 < MPW ? p.ns - (int)s0 : MPW;
+            const int n = p.ns - (int)s0 < p.mpw ? p.ns - (int)s0 : p.mpw;
             if constexpr (SHAKE) surf_a<C>(d, p.smols + s0, n, tol, maxit, sms);
             else surf_b<C>(d, p.smols + s0, n, tol, maxit, sms);
         }
@@ -694,11 +699,12 @@ bool upload_tables_fast(const Tables &t, cudaStream_t st) {
 }
 
 int constraint_max_surf_warps() { return MAX_SURF_WARPS; }
+int constraint_max_mols_per_warp() { return MPW; }
 
 namespace {
 template <typename C, bool SHAKE>
-constexpr size_t surf_smem(int s_warps) {
-    return (size_t)s_warps * MPW * sizeof(MolSmem<C, SHAKE ? 16 : 11>);
+constexpr size_t surf_smem(int s_warps, int mpw) {
+    return (size_t)s_warps * mpw * sizeof(MolSmem<C, SHAKE ? 16 : 11>);
 }
 
 template <typename C, bool SHAKE>
@@ -712,23 +718,24 @@ void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, const Co
     p.ns = ns;
     p.nw = nw;
     p.s_warps = sh.s_warps < 1 ? 1 : (sh.s_warps > MAX_SURF_WARPS ? MAX_SURF_WARPS : sh.s_warps);
-    const int groups = (ns + MPW - 1) / MPW;
+    p.mpw = sh.mpw < 1 ? 1 : (sh.mpw > MPW ? MPW : sh.mpw);
+    const int groups = (ns + p.mpw - 1) / p.mpw;
     const int need = (groups + p.s_warps - 1) / p.s_warps;
     p.n_scta = ns ? (need < sh.grid ? need : sh.grid) : 0;
-    const size_t smem = p.n_scta ? surf_smem<C, SHAKE>(p.s_warps) : 0;
+    const size_t smem = p.n_scta ? surf_smem<C, SHAKE>(p.s_warps, p.mpw) : 0;
     k_constrain<C, SHAKE><<<sh.grid, CW_THREADS, smem, st>>>(d, p, tol, maxit);
 }
 }  // namespace
 
 void init_constraint_kernels() {
     cudaFuncSetAttribute(k_constrain<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)surf_smem<double, true>(MAX_SURF_WARPS));
+                         (int)surf_smem<double, true>(MAX_SURF_WARPS, MPW));
     cudaFuncSetAttribute(k_constrain<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)surf_smem<double, false>(MAX_SURF_WARPS));
+                         (int)surf_smem<double, false>(MAX_SURF_WARPS, MPW));
     cudaFuncSetAttribute(k_constrain<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)surf_smem<float, true>(MAX_SURF_WARPS));
+                         (int)surf_smem<float, true>(MAX_SURF_WARPS, MPW));
     cudaFuncSetAttribute(k_constrain<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)surf_smem<float, false>(MAX_SURF_WARPS));
+                         (int)surf_smem<float, false>(MAX_SURF_WARPS, MPW));
 }
 
 // fp32: 1 for FP32 sweeps, 0 for FP64 sweeps

@@ -14,6 +14,7 @@ void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream
 struct ConstraintShape {
     int grid;      // CTAs of the persistent launch (one per SM)
     int s_warps;   // surfactant warps per CTA that starts on the surfactant queue
+    int mpw;       // surfactants per such warp (1..8)
 };
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
                    int fast, const ConstraintShape &sh, cudaStream_t st);
@@ -31,6 +32,7 @@ void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, const Const
 // reorders the halves' water lists by the sweeps of their last call (at list rebuilds)
 void launch_water_order(const Dev &d, const int *wmols, int nw, cudaStream_t st);
 int constraint_max_surf_warps();
+int constraint_max_mols_per_warp();
 void init_constraint_kernels();   // shared-memory limits of the constraint launches
 
 // k_force.cu

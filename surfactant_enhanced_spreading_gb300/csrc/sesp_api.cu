@@ -317,7 +317,7 @@ struct sesp_ctx {
     // graphs of one step with / without a rebuild
     cudaGraphExec_t g_step[2] = {nullptr, nullptr};
     NearShape near = {64, 0};   // pair-field launch shape (autotuned or set; results do not depend on it)
-    ConstraintShape cshape = {0, 2};   // constraint halves of the mixed paths (likewise)
+    ConstraintShape cshape = {0, 4, 1};   // constraint halves of the mixed paths (likewise)
     int n_sm = 0;               // streaming multiprocessors of the device
     // timing
     bool timing = false;
@@ -998,27 +998,33 @@ int sesp_tuning(sesp_ctx *c, int out[3]) {
     return 0;
 }
 
-int sesp_set_constraint_tuning(sesp_ctx *c, int surf_warps) {
+int sesp_set_constraint_tuning(sesp_ctx *c, int surf_warps, int mols_per_warp) {
     if (int e = check_ctx(c, false)) return e;
     if (surf_warps < 1 || surf_warps > constraint_max_surf_warps())
         return fail(SESP_EINVAL, "surf_warps must be 1..%d", constraint_max_surf_warps());
+    if (mols_per_warp < 1 || mols_per_warp > constraint_max_mols_per_warp())
+        return fail(SESP_EINVAL, "mols_per_warp must be 1..%d", constraint_max_mols_per_warp());
     c->cshape.s_warps = surf_warps;
+    c->cshape.mpw = mols_per_warp;
     drop_graphs(c);
     return 0;
 }
 
-int sesp_constraint_tuning(sesp_ctx *c, int out[2]) {
+int sesp_constraint_tuning(sesp_ctx *c, int out[4]) {
     if (int e = check_ctx(c, false)) return e;
     if (!out) return fail(SESP_EINVAL, "null output");
     out[0] = c->cshape.s_warps;
-    out[1] = constraint_max_surf_warps();
+    out[1] = c->cshape.mpw;
+    out[2] = constraint_max_surf_warps();
+    out[3] = constraint_max_mols_per_warp();
     return 0;
 }
 
 namespace {
 // Times both constraint halves of the mixed paths for every surfactant-warp
-// count (median of 3), restoring the state the halves change before every
-// trial and at the end, and keeps the fastest.
+// count and surfactants per warp (1, 2, 4, 8), median of 3, restoring the
+// state the halves change before every trial and at the end, and keeps the
+// fastest.
 int tune_constraints(sesp_ctx *c) {
     const Dev &d = c->d;
     const size_t N = c->nsite, M = c->nmol, R = c->nrep;
@@ -1043,9 +1049,10 @@ int tune_constraints(sesp_ctx *c) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 1e30f;
-    int pick = c->cshape.s_warps;
-    for (int sw = 1; sw <= constraint_max_surf_warps(); sw++) {
-        const ConstraintShape sh = {c->cshape.grid, sw};
+    ConstraintShape pick = c->cshape;
+    for (int sw = 1; sw <= constraint_max_surf_warps(); sw++)
+    for (int mpw = 1; mpw <= constraint_max_mols_per_warp(); mpw *= 2) {
+        const ConstraintShape sh = {c->cshape.grid, sw, mpw};
         float t[3];
         for (int r = 0; r < 3; r++) {
             copy(false);
@@ -1059,7 +1066,7 @@ int tune_constraints(sesp_ctx *c) {
             cudaEventElapsedTime(&t[r], e0, e1);
         }
         std::sort(t, t + 3);
-        if (t[1] < best) { best = t[1]; pick = sw; }
+        if (t[1] < best) { best = t[1]; pick = sh; }
     }
     copy(false);
     cudaError_t err = cudaStreamSynchronize(c->st);
@@ -1067,7 +1074,7 @@ int tune_constraints(sesp_ctx *c) {
     cudaEventDestroy(e1);
     cudaFree(save);
     if (err != cudaSuccess) return fail(SESP_ECUDA, "constraint autotuning: %s", cudaGetErrorString(err));
-    c->cshape.s_warps = pick;
+    c->cshape = pick;
     return 0;
 }
 }  // namespace

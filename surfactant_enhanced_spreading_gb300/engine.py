@@ -99,7 +99,7 @@ def load(path: str = LIB_PATH):
     L.sesp_autotune.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.sesp_tuning.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.sesp_set_tuning.argtypes = [P, ctypes.c_int, ctypes.c_int]
-    L.sesp_set_constraint_tuning.argtypes = [P, ctypes.c_int]
+    L.sesp_set_constraint_tuning.argtypes = [P, ctypes.c_int, ctypes.c_int]
     L.sesp_constraint_tuning.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     L.sesp_checks.argtypes = [P, dp]
     L.sesp_check_flags.argtypes = [dp]
@@ -293,13 +293,14 @@ class Engine:
         _check(_lib.sesp_set_tuning(self._h, int(tile), int(ctas_per_sm)))
 
     def constraint_tuning(self):
-        """(surfactant warps per CTA of the mixed constraint halves, largest)."""
-        out = (ctypes.c_int * 2)()
+        """(surfactant warps per CTA, surfactants per warp, largest of each) of
+        the mixed constraint halves."""
+        out = (ctypes.c_int * 4)()
         _check(_lib.sesp_constraint_tuning(self._h, out))
         return tuple(out)
 
-    def set_constraint_tuning(self, surf_warps):
-        _check(_lib.sesp_set_constraint_tuning(self._h, int(surf_warps)))
+    def set_constraint_tuning(self, surf_warps, mols_per_warp=1):
+        _check(_lib.sesp_set_constraint_tuning(self._h, int(surf_warps), int(mols_per_warp)))
 
     def checks(self):
         """The reference's consistency checks per replica (rows of 8): molecules

@@ -61,15 +61,16 @@ def test_constraint_shapes_give_identical_trajectories(precision):
     that every rebuild derives from the previous sweeps, change no bit."""
     s = S.droplet(900, 30, cells=(8, 8, 8), seed=5)   # 30 surfactants: 4 groups of up to 8
     runs = []
-    for sw in (1, 2, 4, None):
+    for sw in ((1, 1), (2, 8), (4, 2), (3, 4), None):
         eng = E.Engine(s, precision)
         eng.force(True)
         if sw is None:
             eng.autotune()
-            assert 1 <= eng.constraint_tuning()[0] <= 4
+            tun = eng.constraint_tuning()
+            assert 1 <= tun[0] <= 4 and tun[1] in (1, 2, 4, 8) and tun[2:] == (4, 8)
         else:
-            eng.set_constraint_tuning(sw)
-            assert eng.constraint_tuning() == (sw, 4)
+            eng.set_constraint_tuning(*sw)
+            assert eng.constraint_tuning() == sw + (4, 8)
         eng.init_accel()
         eng.run(99101, 25)
         runs.append(eng.state() + (eng.eta, eng.counters()[0]))
@@ -90,7 +91,9 @@ def test_autotune_restores_the_state():
     for a, b in zip(before, after):
         assert np.array_equal(a, b)
     with pytest.raises(E.SespError, match="EINVAL"):
-        eng.set_constraint_tuning(0)
+        eng.set_constraint_tuning(0, 1)
     with pytest.raises(E.SespError, match="EINVAL"):
-        eng.set_constraint_tuning(5)
+        eng.set_constraint_tuning(5, 1)
+    with pytest.raises(E.SespError, match="EINVAL"):
+        eng.set_constraint_tuning(1, 9)
     eng.close()
