@@ -49,7 +49,9 @@ namespace {
 struct Fast32 {
     double dsq64_w[3], dsq64_s[NBOND];
     double fb64_w[3], fb64_s[NBOND];
+    double hfa64_w[3], hfa64_s[NBOND];     // 1 / (2 (1/m_i + 1/m_j))
     double mass64[NTYPE], rm64[NTYPE], rmdt64[NTYPE];
+    double dt2m64[NTYPE];                  // dt^2 / (2 m)
 };
 __constant__ Fast32 cF;
 
@@ -59,6 +61,14 @@ __constant__ Fast32 cF;
 // {0, 1, ..., 17, 17, 19, 20, 20, 20, 17, 24, 25, 25, 25}
 __host__ __device__ constexpr int sbi32(int b) {
     return b < 18 ? b : b == 18 ? 17 : b == 19 ? 19 : b <= 22 ? 20 : b == 23 ? 17 : b == 24 ? 24 : 25;
+}
+
+// 1 / b: the FP32 estimate and one Newton step in FP64, relative error
+// ~2^-46 (for step lengths and scale factors, whose last bits matter to
+// nothing; GB300's FP64 division costs ~15 FP64 instructions)
+__device__ __forceinline__ double recip64(double b) {
+    const double y = (double)__frcp_rn((float)b);
+    return fma(y, fma(-b, y, 1.0), y);
 }
 
 // the FP64 predictors of the FP64 kernels, rounded the same way
@@ -123,11 +133,12 @@ struct RattleK {
 
 template <typename C>
 __device__ inline void shake_make(double rx, double ry, double rz, double px, double py, double pz, double dsq,
-                                  double rmi, double rmj, double tol2, ShakeK<C> &k) {
+                                  double rmi, double rmj, double hfa, double tol2, ShakeK<C> &k) {
     const double rp = rx * px + ry * py + rz * pz;
-    const double y0 = 1.0 / (2.0 * (rmi + rmj) * rp);
+    const double irp = recip64(rp);
+    const double y0 = hfa * irp;
     k.p2[0] = (C)(2.0 * px); k.p2[1] = (C)(2.0 * py); k.p2[2] = (C)(2.0 * pz);
-    k.rr[0] = (C)(rx / rp); k.rr[1] = (C)(ry / rp); k.rr[2] = (C)(rz / rp);
+    k.rr[0] = (C)(rx * irp); k.rr[1] = (C)(ry * irp); k.rr[2] = (C)(rz * irp);
     k.a[0] = (C)(rmi * rx); k.a[1] = (C)(rmi * ry); k.a[2] = (C)(rmi * rz);
     k.b[0] = (C)(rmj * rx); k.b[1] = (C)(rmj * ry); k.b[2] = (C)(rmj * rz);
     k.d0 = (C)(dsq - (px * px + py * py + pz * pz));
@@ -238,7 +249,7 @@ __device__ __forceinline__ int water_a(const Dev &d, int m, double tol, int maxi
     for (int b = 0; b < 3; b++) {
         const int i = wbi(b), j = wbj(b);
         shake_make<C>(rx[i] - rx[j], ry[i] - ry[j], rz[i] - rz[j], px[i] - px[j], py[i] - py[j], pz[i] - pz[j],
-                      cF.dsq64_w[b], cF.rm64[wkind(i)], cF.rm64[wkind(j)], tol2d, k[b]);
+                      cF.dsq64_w[b], cF.rm64[wkind(i)], cF.rm64[wkind(j)], cF.hfa64_w[b], tol2d, k[b]);
     }
     C cx[3] = {0, 0, 0}, cy[3] = {0, 0, 0}, cz[3] = {0, 0, 0};
     int it = 0;
@@ -277,14 +288,13 @@ __device__ __forceinline__ int water_a(const Dev &d, int m, double tol, int maxi
 template <typename C>
 __device__ __forceinline__ int water_b(const Dev &d, int m, double tol, int maxit) {
     const int g0 = d.mfirst[m];
-    const double escale = __ddiv_rn(2.0, __dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[m]], DT)));
+    const double escale = 2.0 * recip64(__dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[m]], DT)));
     double rx[3], ry[3], rz[3], vx[3], vy[3], vz[3];
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const int g = g0 + i;
-        const double mi = cF.mass64[wkind(i)];
-        double ax = __ddiv_rn(__dmul_rn(d.fx[g], DTSQ2), mi), ay = __ddiv_rn(__dmul_rn(d.fy[g], DTSQ2), mi),
-               az = __ddiv_rn(__dmul_rn(d.fz[g], DTSQ2), mi);
+        const double h = cF.dt2m64[wkind(i)];
+        const double ax = d.fx[g] * h, ay = d.fy[g] * h, az = d.fz[g] * h;
         d.ax[g] = ax; d.ay[g] = ay; d.az[g] = az;
         vx[i] = __dmul_rn(escale, __dadd_rn(d.vx[g], ax));
         vy[i] = __dmul_rn(escale, __dadd_rn(d.vy[g], ay));
@@ -363,6 +373,7 @@ struct MolSmem {
     C rec[NF][SK];
     C sc[3][SK];
     double sv[6][SK];   // per site: old position, then predictor position (SHAKE) or velocity (RATTLE)
+    double kes[SK];     // per site m v^2 (SHAKE)
     C stagger[4];
     template <typename K>
     __device__ void put(int b, const K &k) {
@@ -438,97 +449,130 @@ __device__ __forceinline__ void surf_wavefront(const Dev &d, MolSmem<C, SHAKE ? 
     }
 }
 
-// SHAKE half of up to 8 surfactants (the whole warp): molecules mols[0..n)
+// Per-molecule values of the warp's molecules, held by the lanes of each
+// molecule's group and fetched by any lane with a shuffle.
+struct SurfMol {
+    int m, g0;
+    double escale;
+};
+__device__ __forceinline__ SurfMol surf_mol(const SurfMol &mine, int q) {
+    SurfMol o;
+    o.m = __shfl_sync(FULL, mine.m, 4 * q);
+    o.g0 = __shfl_sync(FULL, mine.g0, 4 * q);
+    o.escale = __shfl_sync(FULL, mine.escale, 4 * q);
+    return o;
+}
+
+// SHAKE half of up to 8 surfactants (the whole warp): molecules mols[0..n).
+// The per-site and per-bond work of the n molecules is spread over all 32
+// lanes (an FP64 warp instruction costs the same for 4 lanes as for 32), the
+// sweeps run in the molecules' groups of 4 lanes.
 template <typename C>
 __device__ __forceinline__ void surf_a(const Dev &d, const int *mols, int n, double tol, int maxit,
                                        MolSmem<C, 16> *sms) {
     static_assert(sizeof(ShakeK<C>) == 16 * sizeof(C), "ShakeK is 16 values");
     const int lane = threadIdx.x & 31, w = lane & (WF_LANES - 1), grp = lane >> 2;
     const bool live = grp < n;
-    const int m = live ? mols[grp] : 0;
-    const int g0 = live ? d.mfirst[m] : 0;
-    MolSmem<C, 16> &sm = sms[grp];
-    // sites w, w + 4, ...: predictor, kinetic sum before, FP64 site vectors
-    double ke0 = 0.0;
+    SurfMol mine = {0, 0, 0.0};
     if (live) {
-        const double escale = __dsub_rn(1.0, __dmul_rn(d.eta[d.mrep[m]], DT) * 0.5);
-        for (int s = w; s < NSURF; s += WF_LANES) {
-            const int g = g0 + s;
-            double vx = d.vx[g], vy = d.vy[g], vz = d.vz[g], ax = d.ax[g], ay = d.ay[g], az = d.az[g];
+        mine.m = mols[grp];
+        mine.g0 = d.mfirst[mine.m];
+        mine.escale = __dsub_rn(1.0, __dmul_rn(d.eta[d.mrep[mine.m]], DT) * 0.5);
+    }
+    // sites: predictor, m v^2 before, FP64 site vectors
+    for (int base = 0; base < n * NSURF; base += 32) {
+        const int it = base + lane, q = it < n * NSURF ? it / NSURF : 0, s = it - q * NSURF;
+        const SurfMol mq = surf_mol(mine, q);
+        if (it < n * NSURF) {
+            MolSmem<C, 16> &sm = sms[q];
+            const int g = mq.g0 + s;
+            const double vx = d.vx[g], vy = d.vy[g], vz = d.vz[g], ax = d.ax[g], ay = d.ay[g], az = d.az[g];
             const double rx = d.x[g], ry = d.y[g], rz = d.z[g];
-            ke0 = __dadd_rn(ke0, __dmul_rn(cF.mass64[2 + s],
-                                           __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
-            const double px = pred_a(rx, vx, ax, escale), py = pred_a(ry, vy, ay, escale), pz = pred_a(rz, vz, az, escale);
+            sm.kes[s] = __dmul_rn(cF.mass64[2 + s],
+                                  __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz)));
+            const double px = pred_a(rx, vx, ax, mq.escale), py = pred_a(ry, vy, ay, mq.escale),
+                         pz = pred_a(rz, vz, az, mq.escale);
             d.x[g] = px; d.y[g] = py; d.z[g] = pz;
-            d.vx[g] = vel_a(vx, ax, escale);
-            d.vy[g] = vel_a(vy, ay, escale);
-            d.vz[g] = vel_a(vz, az, escale);
+            d.vx[g] = vel_a(vx, ax, mq.escale);
+            d.vy[g] = vel_a(vy, ay, mq.escale);
+            d.vz[g] = vel_a(vz, az, mq.escale);
             sm.sv[0][s] = rx; sm.sv[1][s] = ry; sm.sv[2][s] = rz;
             sm.sv[3][s] = px; sm.sv[4][s] = py; sm.sv[5][s] = pz;
             sm.sc[0][skew8(s)] = sm.sc[1][skew8(s)] = sm.sc[2][skew8(s)] = C(0);
         }
     }
+    __syncwarp();
+    // bonds: constants
+    const double tol2d = 2.0 * tol;
+    for (int it = lane; it < n * NBOND; it += 32) {
+        const int q = it / NBOND, b = it - q * NBOND, i = sbi32(b), j = b + 1;
+        MolSmem<C, 16> &sm = sms[q];
+        ShakeK<C> k;
+        shake_make<C>(sm.sv[0][i] - sm.sv[0][j], sm.sv[1][i] - sm.sv[1][j], sm.sv[2][i] - sm.sv[2][j],
+                      sm.sv[3][i] - sm.sv[3][j], sm.sv[4][i] - sm.sv[4][j], sm.sv[5][i] - sm.sv[5][j],
+                      cF.dsq64_s[b], cF.rm64[2 + i], cF.rm64[2 + j], cF.hfa64_s[b], tol2d, k);
+        sm.put(b, k);
+    }
+    __syncwarp();
+    // kinetic sum before: lane w of a group adds sites w, w + 4, ..., then the group
+    double ke0 = 0.0;
+    if (live)
+        for (int s = w; s < NSURF; s += WF_LANES) ke0 = __dadd_rn(ke0, sms[grp].kes[s]);
     ke0 = group_sum(ke0);
-    __syncwarp();
-    // bonds w, w + 4, ...: constants
-    if (live) {
-        const double tol2d = 2.0 * tol;
-        for (int b = w; b < NBOND; b += WF_LANES) {
-            const int i = sbi32(b), j = b + 1;
-            ShakeK<C> k;
-            shake_make<C>(sm.sv[0][i] - sm.sv[0][j], sm.sv[1][i] - sm.sv[1][j], sm.sv[2][i] - sm.sv[2][j],
-                          sm.sv[3][i] - sm.sv[3][j], sm.sv[4][i] - sm.sv[4][j], sm.sv[5][i] - sm.sv[5][j],
-                          cF.dsq64_s[b], cF.rm64[2 + i], cF.rm64[2 + j], tol2d, k);
-            sm.put(b, k);
-        }
-    }
-    __syncwarp();
     bool fail;
-    surf_wavefront<C, true>(d, sm, g0, live, tol, maxit, fail);
-    double ke1 = 0.0;
-    if (live) {
-        for (int s = w; s < NSURF; s += WF_LANES) {
-            const int g = g0 + s;
-            const double cxi = sm.sc[0][skew8(s)], cyi = sm.sc[1][skew8(s)], czi = sm.sc[2][skew8(s)];
-            d.x[g] = __dadd_rn(sm.sv[3][s], cxi);
-            d.y[g] = __dadd_rn(sm.sv[4][s], cyi);
-            d.z[g] = __dadd_rn(sm.sv[5][s], czi);
-            const double vx = __dadd_rn(d.vx[g], cxi), vy = __dadd_rn(d.vy[g], cyi), vz = __dadd_rn(d.vz[g], czi);
-            d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
-            ke1 = __dadd_rn(ke1, __dmul_rn(cF.mass64[2 + s],
-                                           __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
-        }
+    surf_wavefront<C, true>(d, sms[grp], mine.g0, live, tol, maxit, fail);
+    // sites: positions, velocities, m v^2 after
+    for (int it = lane; it < n * NSURF; it += 32) {
+        const int q = it / NSURF, s = it - q * NSURF;
+        MolSmem<C, 16> &sm = sms[q];
+        const int g = d.mfirst[mols[q]] + s;
+        const double cxi = sm.sc[0][skew8(s)], cyi = sm.sc[1][skew8(s)], czi = sm.sc[2][skew8(s)];
+        d.x[g] = __dadd_rn(sm.sv[3][s], cxi);
+        d.y[g] = __dadd_rn(sm.sv[4][s], cyi);
+        d.z[g] = __dadd_rn(sm.sv[5][s], czi);
+        const double vx = __dadd_rn(d.vx[g], cxi), vy = __dadd_rn(d.vy[g], cyi), vz = __dadd_rn(d.vz[g], czi);
+        d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
+        sm.kes[s] = __dmul_rn(cF.mass64[2 + s],
+                              __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz)));
     }
+    __syncwarp();
+    double ke1 = 0.0;
+    if (live)
+        for (int s = w; s < NSURF; s += WF_LANES) ke1 = __dadd_rn(ke1, sms[grp].kes[s]);
     ke1 = group_sum(ke1);
     if (live && w == 0) {
-        d.ke[2 * m] = ke0;
-        d.ke[2 * m + 1] = ke1;
-        if (fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+        d.ke[2 * mine.m] = ke0;
+        d.ke[2 * mine.m + 1] = ke1;
+        if (fail) { d.mfail[mine.m] += 1; atomicAdd(&d.counters[0], 1ull); }
     }
     __syncwarp();   // the shared records are reused by the warp's next molecules
 }
 
-// RATTLE half of up to 8 surfactants (the whole warp)
+// RATTLE half of up to 8 surfactants (the whole warp), laid out as surf_a
 template <typename C>
 __device__ __forceinline__ void surf_b(const Dev &d, const int *mols, int n, double tol, int maxit,
                                        MolSmem<C, 11> *sms) {
     static_assert(sizeof(RattleK<C>) == 11 * sizeof(C), "RattleK is 11 values");
-    const int lane = threadIdx.x & 31, w = lane & (WF_LANES - 1), grp = lane >> 2;
+    const int lane = threadIdx.x & 31, grp = lane >> 2;
     const bool live = grp < n;
-    const int m = live ? mols[grp] : 0;
-    const int g0 = live ? d.mfirst[m] : 0;
-    MolSmem<C, 11> &sm = sms[grp];
+    SurfMol mine = {0, 0, 0.0};
     if (live) {
-        const double escale = __ddiv_rn(2.0, __dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[m]], DT)));
-        for (int s = w; s < NSURF; s += WF_LANES) {
-            const int g = g0 + s;
-            const double mi = cF.mass64[2 + s];
-            const double ax = __ddiv_rn(__dmul_rn(d.fx[g], DTSQ2), mi), ay = __ddiv_rn(__dmul_rn(d.fy[g], DTSQ2), mi),
-                         az = __ddiv_rn(__dmul_rn(d.fz[g], DTSQ2), mi);
+        mine.m = mols[grp];
+        mine.g0 = d.mfirst[mine.m];
+        mine.escale = 2.0 * recip64(__dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[mine.m]], DT)));
+    }
+    for (int base = 0; base < n * NSURF; base += 32) {
+        const int it = base + lane, q = it < n * NSURF ? it / NSURF : 0, s = it - q * NSURF;
+        const SurfMol mq = surf_mol(mine, q);
+        if (it < n * NSURF) {
+            MolSmem<C, 11> &sm = sms[q];
+            const int g = mq.g0 + s;
+            const double h = cF.dt2m64[2 + s];
+            const double ax = d.fx[g] * h, ay = d.fy[g] * h, az = d.fz[g] * h;
             d.ax[g] = ax; d.ay[g] = ay; d.az[g] = az;
-            const double vx = __dmul_rn(escale, __dadd_rn(d.vx[g], ax));
-            const double vy = __dmul_rn(escale, __dadd_rn(d.vy[g], ay));
-            const double vz = __dmul_rn(escale, __dadd_rn(d.vz[g], az));
+            const double vx = __dmul_rn(mq.escale, __dadd_rn(d.vx[g], ax));
+            const double vy = __dmul_rn(mq.escale, __dadd_rn(d.vy[g], ay));
+            const double vz = __dmul_rn(mq.escale, __dadd_rn(d.vz[g], az));
             d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
             sm.sv[0][s] = d.x[g]; sm.sv[1][s] = d.y[g]; sm.sv[2][s] = d.z[g];
             sm.sv[3][s] = vx; sm.sv[4][s] = vy; sm.sv[5][s] = vz;
@@ -536,28 +580,27 @@ __device__ __forceinline__ void surf_b(const Dev &d, const int *mols, int n, dou
         }
     }
     __syncwarp();
-    if (live) {
-        for (int b = w; b < NBOND; b += WF_LANES) {
-            const int i = sbi32(b), j = b + 1;
-            RattleK<C> k;
-            rattle_make<C>(sm.sv[0][i] - sm.sv[0][j], sm.sv[1][i] - sm.sv[1][j], sm.sv[2][i] - sm.sv[2][j],
-                           sm.sv[3][i] - sm.sv[3][j], sm.sv[4][i] - sm.sv[4][j], sm.sv[5][i] - sm.sv[5][j],
-                           cF.rmdt64[2 + i], cF.rmdt64[2 + j], cF.fb64_s[b], k);
-            sm.put(b, k);
-        }
+    for (int it = lane; it < n * NBOND; it += 32) {
+        const int q = it / NBOND, b = it - q * NBOND, i = sbi32(b), j = b + 1;
+        MolSmem<C, 11> &sm = sms[q];
+        RattleK<C> k;
+        rattle_make<C>(sm.sv[0][i] - sm.sv[0][j], sm.sv[1][i] - sm.sv[1][j], sm.sv[2][i] - sm.sv[2][j],
+                       sm.sv[3][i] - sm.sv[3][j], sm.sv[4][i] - sm.sv[4][j], sm.sv[5][i] - sm.sv[5][j],
+                       cF.rmdt64[2 + i], cF.rmdt64[2 + j], cF.fb64_s[b], k);
+        sm.put(b, k);
     }
     __syncwarp();
     bool fail;
-    surf_wavefront<C, false>(d, sm, g0, live, tol, maxit, fail);
-    if (live) {
-        for (int s = w; s < NSURF; s += WF_LANES) {
-            const int g = g0 + s;
-            d.vx[g] = __dadd_rn(sm.sv[3][s], (double)sm.sc[0][skew8(s)]);
-            d.vy[g] = __dadd_rn(sm.sv[4][s], (double)sm.sc[1][skew8(s)]);
-            d.vz[g] = __dadd_rn(sm.sv[5][s], (double)sm.sc[2][skew8(s)]);
-        }
+    surf_wavefront<C, false>(d, sms[grp], mine.g0, live, tol, maxit, fail);
+    for (int it = lane; it < n * NSURF; it += 32) {
+        const int q = it / NSURF, s = it - q * NSURF;
+        MolSmem<C, 11> &sm = sms[q];
+        const int g = d.mfirst[mols[q]] + s;
+        d.vx[g] = __dadd_rn(sm.sv[3][s], (double)sm.sc[0][skew8(s)]);
+        d.vy[g] = __dadd_rn(sm.sv[4][s], (double)sm.sc[1][skew8(s)]);
+        d.vz[g] = __dadd_rn(sm.sv[5][s], (double)sm.sc[2][skew8(s)]);
     }
-    if (live && w == 0 && fail) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    if (live && (lane & 3) == 0 && fail) { d.mfail[mine.m] += 1; atomicAdd(&d.counters[0], 1ull); }
     __syncwarp();   // the shared records are reused by the warp's next molecules
 }
 
@@ -683,17 +726,20 @@ bool upload_tables_fast(const Tables &t, cudaStream_t st) {
         f.mass64[k] = t.mass[k];
         f.rm64[k] = 1.0 / t.mass[k];
         f.rmdt64[k] = DT / t.mass[k];
+        f.dt2m64[k] = DTSQ2 / t.mass[k];
     }
     for (int b = 0; b < 3; b++) {
         const int ki = b == 0 ? 0 : 1, kj = b == 2 ? 0 : 1;
         const double rs = 1.0 / t.mass[ki] + 1.0 / t.mass[kj];
         f.dsq64_w[b] = t.dsqw[b];
         f.fb64_w[b] = (1.0 / DT) / (rs * t.dsqw[b]);
+        f.hfa64_w[b] = 1.0 / (2.0 * rs);
     }
     for (int b = 0; b < NBOND; b++) {
         const double rs = 1.0 / t.mass[2 + t.bi[b]] + 1.0 / t.mass[2 + t.bj[b]];
         f.dsq64_s[b] = t.dsqs[b];
         f.fb64_s[b] = (1.0 / DT) / (rs * t.dsqs[b]);
+        f.hfa64_s[b] = 1.0 / (2.0 * rs);
     }
     return cudaMemcpyToSymbolAsync(cF, &f, sizeof f, 0, cudaMemcpyHostToDevice, st) == cudaSuccess;
 }
