@@ -179,7 +179,9 @@ int sesp_autotune(sesp_ctx *ctx, int out[3]);
 int sesp_tuning(sesp_ctx *ctx, int out[3]);
 int sesp_set_tuning(sesp_ctx *ctx, int tile, int ctas_per_sm);
 /* Launch shape of the constraint halves on the mixed paths: surfactant warps
- * per CTA (1..4) and surfactants per such warp (1..8).  The surfactants'
+ * per CTA (1..4) and surfactants per such warp (1..2 on SESP_MIXED, whose
+ * FP64 sweeps take 12 lanes per molecule, 1..8 on SESP_MIXED_FP32C).  The
+ * surfactants'
  * FP64 sweep chains start on the first
  * ceil(n_surf / (mols_per_warp surf_warps)) CTAs (one CTA per SM), waters
  * fill every other warp.  The shape changes no result, only the time;

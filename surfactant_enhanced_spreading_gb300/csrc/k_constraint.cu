@@ -399,16 +399,19 @@ __device__ __forceinline__ double group_sum(double v) {
 // The wavefront of SHAKE (SHAKE = true) or RATTLE over the 8 molecules of a
 // warp.  Lane (g, w): molecule g, wavefront lane w.  Returns through fail
 // whether its molecule ran out of sweeps.
+// The wavefront with one bond per lane (FP32 corrections): lane (g, w),
+// molecule g of the warp, wavefront lane w.  Returns a ballot whose bit 4g
+// is set if molecule g ran out of sweeps.
 template <typename C, bool SHAKE>
-__device__ __forceinline__ void surf_wavefront(const Dev &d, MolSmem<C, SHAKE ? 16 : 11> &sm, int g0, bool live,
-                                               double tol, int maxit, bool &fail) {
+__device__ __forceinline__ unsigned surf_wavefront(const Dev &d, MolSmem<C, SHAKE ? 16 : 11> *sms, int g0, int n,
+                                                   double tol, int maxit) {
     const int lane = threadIdx.x & 31, w = lane & (WF_LANES - 1), grp = lane >> 2;
     const unsigned gmask = 0xFu << (4 * grp);
+    MolSmem<C, SHAKE ? 16 : 11> &sm = sms[grp < n ? grp : 0];
     const double tol2d = 2.0 * tol;
     const C tolc = (C)tol;
     int kmine = w;
-    bool changed = false, done = !live;
-    fail = false;
+    bool changed = false, done = grp >= n, fail = false;
     for (int t = 0;; t++) {
         bool clean = false, last = false;
         const int b = t - WF_LAG * kmine;
@@ -447,7 +450,97 @@ __device__ __forceinline__ void surf_wavefront(const Dev &d, MolSmem<C, SHAKE ? 
         }
         if (__all_sync(FULL, done)) break;
     }
+    return __ballot_sync(FULL, fail && w == 0);
 }
+
+// sum of v over lanes base, base + 1, base + 2 (the same bits in all three)
+__device__ __forceinline__ double tri_sum(double v, int base) {
+    const double v0 = __shfl_sync(FULL, v, base), v1 = __shfl_sync(FULL, v, base + 1),
+                 v2 = __shfl_sync(FULL, v, base + 2);
+    return (v0 + v1) + v2;
+}
+
+// The wavefront for FP64 corrections with each bond split over 3 lanes, one
+// per Cartesian component: lane 12 q + 3 w + k works on component k of
+// wavefront lane w of molecule q (q < 2; lanes 24..31 idle).  Every FP64
+// warp instruction costs the same whatever its active lanes, so splitting
+// the components takes a SHAKE bond from 25 to 18 FP64 warp instructions
+// (9 to 6 for a bond within tolerance) and a RATTLE bond from 12 to 7; the
+// two dot products go over shuffles.  Returns a ballot whose bit 12 q is set
+// if molecule q ran out of sweeps.
+template <bool SHAKE>
+__device__ __forceinline__ unsigned surf_wavefront3(const Dev &d, MolSmem<double, SHAKE ? 16 : 11> *sms, int n,
+                                                    double tol, int maxit) {
+    const int lane = threadIdx.x & 31;
+    const int q = lane < 24 ? lane / 12 : 0, r = lane - 12 * q, w = lane < 24 ? r / 3 : 0, k = lane < 24 ? r % 3 : 0;
+    const int base = lane - k;
+    const unsigned gmask = 0xFFFu << (12 * q);
+    MolSmem<double, SHAKE ? 16 : 11> &sm = sms[q < n ? q : 0];
+    double *rec = &sm.rec[0][0];
+    int kmine = w;
+    bool changed = false, done = lane >= 24 || q >= n, fail = false;
+    for (int t = 0;; t++) {
+        bool clean = false, last = false;
+        const int b = t - WF_LAG * kmine;
+        const bool valid = !done && kmine <= maxit && b >= 0 && b < NBOND;
+        const int sb = skew8(valid ? b : 0), i = valid ? sbi32(b) : 0, si = skew8(i), sj = skew8(valid ? b + 1 : 0);
+        double ci = 0.0, cj = 0.0, dx = 0.0, pr = 0.0;
+        if (valid) {
+            ci = sm.sc[k][si];
+            cj = sm.sc[k][sj];
+            dx = ci - cj;
+            pr = SHAKE ? dx * (dx + rec[k * SK + sb]) : rec[k * SK + sb] * dx;   // c_k (c_k + 2P_k)  /  -fb R_k c_k
+        }
+        const double sum = tri_sum(pr, base);
+        double gab = 0.0;
+        bool act = false;
+        if constexpr (SHAKE) {
+            const double diffsq = valid ? rec[12 * SK + sb] - sum : 0.0;   // D0 - c.(c + 2P)
+            act = valid && gt_abs(diffsq, rec[14 * SK + sb]);
+            if (__any_sync(FULL, act)) {   // the step only when some bond of the warp is corrected
+                const double tk = valid ? rec[(3 + k) * SK + sb] * dx : 0.0;
+                const double tt = tri_sum(tk, base);
+                const double y0 = valid ? rec[13 * SK + sb] : 0.0;
+                const double t2 = tt * tt;
+                const double ya = fma(-y0, tt, y0), yb = fma(tt, tt, 1.0), yc = fma(t2, t2, 1.0);
+                gab = (diffsq * ya) * (yb * yc);
+            }
+        } else {
+            gab = valid ? rec[9 * SK + sb] + sum : 0.0;   // -fb R.(V + c)
+            act = valid && gt_abs(gab, tol);
+        }
+        if (act) {
+            const int fa = SHAKE ? 6 : 3, fb = SHAKE ? 9 : 6;
+            sm.sc[k][si] = fma(rec[(fa + k) * SK + sb], gab, ci);
+            sm.sc[k][sj] = fma(-rec[(fb + k) * SK + sb], gab, cj);
+            changed = true;
+        }
+        if (valid && b == NBOND - 1) {
+            clean = !changed;
+            last = changed && kmine == maxit;
+            changed = false;
+            kmine += WF_LANES;
+        }
+        __syncwarp();
+        const unsigned bc = __ballot_sync(FULL, clean), bl = __ballot_sync(FULL, last);
+        if (!done) {
+            if (bc & gmask) done = true;
+            else if (bl & gmask) { done = true; fail = true; }
+        }
+        if (__all_sync(FULL, done)) break;
+    }
+    return __ballot_sync(FULL, fail && r == 0 && lane < 24);
+}
+
+// whether molecule g of the warp ran out of sweeps, from the wavefront's ballot
+template <typename C>
+__device__ __forceinline__ bool surf_failed(unsigned ballot, int g) {
+    return (ballot >> (sizeof(C) == 8 ? 12 * g : 4 * g)) & 1u;
+}
+
+// molecules per warp the wavefront of corrections of type C takes
+template <typename C>
+__host__ __device__ constexpr int wavefront_mols() { return sizeof(C) == 8 ? 2 : MPW; }
 
 // Per-molecule values of the warp's molecules, held by the lanes of each
 // molecule's group and fetched by any lane with a shuffle.
@@ -519,8 +612,9 @@ __device__ __forceinline__ void surf_a(const Dev &d, const int *mols, int n, dou
     if (live)
         for (int s = w; s < NSURF; s += WF_LANES) ke0 = __dadd_rn(ke0, sms[grp].kes[s]);
     ke0 = group_sum(ke0);
-    bool fail;
-    surf_wavefront<C, true>(d, sms[grp], mine.g0, live, tol, maxit, fail);
+    unsigned failed;
+    if constexpr (sizeof(C) == 8) failed = surf_wavefront3<true>(d, sms, n, tol, maxit);
+    else failed = surf_wavefront<C, true>(d, sms, mine.g0, n, tol, maxit);
     // sites: positions, velocities, m v^2 after
     for (int it = lane; it < n * NSURF; it += 32) {
         const int q = it / NSURF, s = it - q * NSURF;
@@ -543,7 +637,7 @@ __device__ __forceinline__ void surf_a(const Dev &d, const int *mols, int n, dou
     if (live && w == 0) {
         d.ke[2 * mine.m] = ke0;
         d.ke[2 * mine.m + 1] = ke1;
-        if (fail) { d.mfail[mine.m] += 1; atomicAdd(&d.counters[0], 1ull); }
+        if (surf_failed<C>(failed, grp)) { d.mfail[mine.m] += 1; atomicAdd(&d.counters[0], 1ull); }
     }
     __syncwarp();   // the shared records are reused by the warp's next molecules
 }
@@ -590,8 +684,9 @@ __device__ __forceinline__ void surf_b(const Dev &d, const int *mols, int n, dou
         sm.put(b, k);
     }
     __syncwarp();
-    bool fail;
-    surf_wavefront<C, false>(d, sms[grp], mine.g0, live, tol, maxit, fail);
+    unsigned failed;
+    if constexpr (sizeof(C) == 8) failed = surf_wavefront3<false>(d, sms, n, tol, maxit);
+    else failed = surf_wavefront<C, false>(d, sms, mine.g0, n, tol, maxit);
     for (int it = lane; it < n * NSURF; it += 32) {
         const int q = it / NSURF, s = it - q * NSURF;
         MolSmem<C, 11> &sm = sms[q];
@@ -600,7 +695,7 @@ __device__ __forceinline__ void surf_b(const Dev &d, const int *mols, int n, dou
         d.vy[g] = __dadd_rn(sm.sv[4][s], (double)sm.sc[1][skew8(s)]);
         d.vz[g] = __dadd_rn(sm.sv[5][s], (double)sm.sc[2][skew8(s)]);
     }
-    if (live && (lane & 3) == 0 && fail) { d.mfail[mine.m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    if (live && (lane & 3) == 0 && surf_failed<C>(failed, grp)) { d.mfail[mine.m] += 1; atomicAdd(&d.counters[0], 1ull); }
     __syncwarp();   // the shared records are reused by the warp's next molecules
 }
 
@@ -745,7 +840,7 @@ bool upload_tables_fast(const Tables &t, cudaStream_t st) {
 }
 
 int constraint_max_surf_warps() { return MAX_SURF_WARPS; }
-int constraint_max_mols_per_warp() { return MPW; }
+int constraint_max_mols_per_warp(int fp32) { return fp32 ? wavefront_mols<float>() : wavefront_mols<double>(); }
 
 namespace {
 template <typename C, bool SHAKE>
@@ -764,7 +859,7 @@ void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, const Co
     p.ns = ns;
     p.nw = nw;
     p.s_warps = sh.s_warps < 1 ? 1 : (sh.s_warps > MAX_SURF_WARPS ? MAX_SURF_WARPS : sh.s_warps);
-    p.mpw = sh.mpw < 1 ? 1 : (sh.mpw > MPW ? MPW : sh.mpw);
+    p.mpw = sh.mpw < 1 ? 1 : (sh.mpw > wavefront_mols<C>() ? wavefront_mols<C>() : sh.mpw);
     const int groups = (ns + p.mpw - 1) / p.mpw;
     const int need = (groups + p.s_warps - 1) / p.s_warps;
     p.n_scta = ns ? (need < sh.grid ? need : sh.grid) : 0;

@@ -32,7 +32,7 @@ void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, const Const
 // reorders the halves' water lists by the sweeps of their last call (at list rebuilds)
 void launch_water_order(const Dev &d, const int *wmols, int nw, cudaStream_t st);
 int constraint_max_surf_warps();
-int constraint_max_mols_per_warp();
+int constraint_max_mols_per_warp(int fp32);   // fp32: FP32 corrections (SESP_MIXED_FP32C)
 void init_constraint_kernels();   // shared-memory limits of the constraint launches
 
 // k_force.cu

@@ -1002,8 +1002,8 @@ int sesp_set_constraint_tuning(sesp_ctx *c, int surf_warps, int mols_per_warp) {
     if (int e = check_ctx(c, false)) return e;
     if (surf_warps < 1 || surf_warps > constraint_max_surf_warps())
         return fail(SESP_EINVAL, "surf_warps must be 1..%d", constraint_max_surf_warps());
-    if (mols_per_warp < 1 || mols_per_warp > constraint_max_mols_per_warp())
-        return fail(SESP_EINVAL, "mols_per_warp must be 1..%d", constraint_max_mols_per_warp());
+    if (mols_per_warp < 1 || mols_per_warp > constraint_max_mols_per_warp(c->p.precision == SESP_MIXED_FP32C))
+        return fail(SESP_EINVAL, "mols_per_warp must be 1..%d", constraint_max_mols_per_warp(c->p.precision == SESP_MIXED_FP32C));
     c->cshape.s_warps = surf_warps;
     c->cshape.mpw = mols_per_warp;
     drop_graphs(c);
@@ -1016,7 +1016,7 @@ int sesp_constraint_tuning(sesp_ctx *c, int out[4]) {
     out[0] = c->cshape.s_warps;
     out[1] = c->cshape.mpw;
     out[2] = constraint_max_surf_warps();
-    out[3] = constraint_max_mols_per_warp();
+    out[3] = constraint_max_mols_per_warp(c->p.precision == SESP_MIXED_FP32C);
     return 0;
 }
 
@@ -1051,7 +1051,7 @@ int tune_constraints(sesp_ctx *c) {
     float best = 1e30f;
     ConstraintShape pick = c->cshape;
     for (int sw = 1; sw <= constraint_max_surf_warps(); sw++)
-    for (int mpw = 1; mpw <= constraint_max_mols_per_warp(); mpw *= 2) {
+    for (int mpw = 1; mpw <= constraint_max_mols_per_warp(c->p.precision == SESP_MIXED_FP32C); mpw *= 2) {
         const ConstraintShape sh = {c->cshape.grid, sw, mpw};
         float t[3];
         for (int r = 0; r < 3; r++) {
