@@ -205,7 +205,9 @@ int sesp_constraint_tuning(sesp_ctx *ctx, int out[4]);
 int sesp_energies_static(sesp_ctx *ctx, double out[8]);
 /* counts: [0] SHAKE/RATTLE non-convergences since upload, [1] capacity
  * overflows, [2] sites in no cell, [3] steps done, [4] max sites in a cell,
- * [5] near-field ordered pairs of the last rebuild, [6] LJ-eligible pairs */
+ * [5] near-field ordered pairs of the last rebuild, [6] LJ-eligible pairs,
+ * [7] molecule-list entries that failed their bounds check and were skipped
+ * (always 0 unless device memory was corrupted) */
 int sesp_counters(sesp_ctx *ctx, int64_t out[8]);
 /* The reference's consistency checks, from the cell lists of the last force
  * call, 8 values per replica (out holds 8 x sesp_replica_count):

@@ -714,7 +714,16 @@ struct CPlan {
     int n_scta;         // CTAs that start on the surfactant queue
     int s_warps;        // surfactant warps in each of them
     int mpw;            // surfactants per warp (groups of 4 lanes), 1..MPW
+    int nmol, nsite;    // bounds every listed molecule is checked against
 };
+
+// a listed molecule with its nsites sites inside the state arrays; a list
+// entry that is not is counted in counters[7] and skipped, never followed
+__device__ __forceinline__ bool mol_ok(const Dev &d, const CPlan &p, int m, int nsites) {
+    if (m < 0 || m >= p.nmol) return false;
+    const int g0 = d.mfirst[m];
+    return g0 >= 0 && g0 + nsites <= p.nsite;
+}
 
 template <typename C, bool SHAKE>
 __global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double tol, int maxit) {
@@ -731,6 +740,11 @@ __global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double
             const long long s0 = (long long)p.mpw * s;
             if (s0 >= p.ns) break;
             const int n = p.ns - (int)s0 < p.mpw ? p.ns - (int)s0 : p.mpw;
+            const bool bad = lane < n && !mol_ok(d, p, p.smols[s0 + lane], NSURF);
+            if (__any_sync(FULL, bad)) {
+                if (lane == 0) atomicAdd(&d.counters[7], 1ull);
+                continue;
+            }
             if constexpr (SHAKE) surf_a<C>(d, p.smols + s0, n, tol, maxit, sms);
             else surf_b<C>(d, p.smols + s0, n, tol, maxit, sms);
         }
@@ -746,6 +760,10 @@ __global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double
             const int t = (int)t0 + lane;
             if (t < p.nw) {
                 const int m = p.wlist[t];
+                if (!mol_ok(d, p, m, 3)) {
+                    atomicAdd(&d.counters[7], 1ull);
+                    continue;
+                }
                 const int sweeps = SHAKE ? water_a<C>(d, m, tol, maxit) : water_b<C>(d, m, tol, maxit);
                 p.wsw[m] = (uint8_t)(sweeps < 255 ? sweeps : 255);
             }
@@ -788,7 +806,7 @@ __global__ void k_worder_scan(int *off) {   // one thread per half: exclusive sc
 }
 
 __global__ void k_worder_place(const int *wmols, int nw, const uint8_t *swa, const uint8_t *swb, int *off, int *la,
-                               int *lb) {
+                               int *lb, unsigned long long *bad) {
     __shared__ int cnt[2 * WS_BINS], base[2 * WS_BINS];
     for (int k = threadIdx.x; k < 2 * WS_BINS; k += blockDim.x) cnt[k] = 0;
     __syncthreads();
@@ -806,8 +824,13 @@ __global__ void k_worder_place(const int *wmols, int nw, const uint8_t *swa, con
         if (cnt[k]) base[k] = atomicAdd(&off[k], cnt[k]);
     __syncthreads();
     if (m >= 0) {
-        la[base[ba] + ra] = m;
-        lb[base[bb] + rb] = m;
+        const int pa = base[ba] + ra, pb = base[bb] + rb;
+        if (pa < nw && pb < nw) {
+            la[pa] = m;
+            lb[pb] = m;
+        } else {
+            atomicAdd(bad, 1ull);
+        }
     }
 }
 
@@ -849,8 +872,8 @@ constexpr size_t surf_smem(int s_warps, int mpw) {
 }
 
 template <typename C, bool SHAKE>
-void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, const ConstraintShape &sh, double tol,
-                        int maxit, cudaStream_t st) {
+void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, int nmol, int nsite, const ConstraintShape &sh,
+                        double tol, int maxit, cudaStream_t st) {
     CPlan p;
     p.smols = smols;
     p.wlist = SHAKE ? d.wlist_a : d.wlist_b;
@@ -858,6 +881,8 @@ void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, const Co
     p.ctl = d.cctl + (SHAKE ? 0 : 4);
     p.ns = ns;
     p.nw = nw;
+    p.nmol = nmol;
+    p.nsite = nsite;
     p.s_warps = sh.s_warps < 1 ? 1 : (sh.s_warps > MAX_SURF_WARPS ? MAX_SURF_WARPS : sh.s_warps);
     p.mpw = sh.mpw < 1 ? 1 : (sh.mpw > wavefront_mols<C>() ? wavefront_mols<C>() : sh.mpw);
     const int groups = (ns + p.mpw - 1) / p.mpw;
@@ -880,18 +905,18 @@ void init_constraint_kernels() {
 }
 
 // fp32: 1 for FP32 sweeps, 0 for FP64 sweeps
-void launch_move_a32(const Dev &d, int nw, const int *smols, int ns, const ConstraintShape &sh, cudaStream_t st,
-                     double tol, int maxit, int fp32) {
+void launch_move_a32(const Dev &d, int nw, const int *smols, int ns, int nmol, int nsite, const ConstraintShape &sh,
+                     cudaStream_t st, double tol, int maxit, int fp32) {
     if (!nw && !ns) return;
-    if (fp32) launch_constrain_t<float, true>(d, smols, ns, nw, sh, tol, maxit, st);
-    else launch_constrain_t<double, true>(d, smols, ns, nw, sh, tol, maxit, st);
+    if (fp32) launch_constrain_t<float, true>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st);
+    else launch_constrain_t<double, true>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st);
 }
 
-void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, const ConstraintShape &sh, cudaStream_t st,
-                     double tol, int maxit, int fp32) {
+void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, int nmol, int nsite, const ConstraintShape &sh,
+                     cudaStream_t st, double tol, int maxit, int fp32) {
     if (!nw && !ns) return;
-    if (fp32) launch_constrain_t<float, false>(d, smols, ns, nw, sh, tol, maxit, st);
-    else launch_constrain_t<double, false>(d, smols, ns, nw, sh, tol, maxit, st);
+    if (fp32) launch_constrain_t<float, false>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st);
+    else launch_constrain_t<double, false>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st);
 }
 
 void launch_water_order(const Dev &d, const int *wmols, int nw, cudaStream_t st) {
@@ -900,7 +925,7 @@ void launch_water_order(const Dev &d, const int *wmols, int nw, cudaStream_t st)
     const int nb = (nw + 255) / 256;
     k_worder_count<<<nb < 256 ? nb : 256, 256, 0, st>>>(wmols, nw, d.wsw_a, d.wsw_b, d.wsort_off);
     k_worder_scan<<<1, 2, 0, st>>>(d.wsort_off);
-    k_worder_place<<<nb, 256, 0, st>>>(wmols, nw, d.wsw_a, d.wsw_b, d.wsort_off, d.wlist_a, d.wlist_b);
+    k_worder_place<<<nb, 256, 0, st>>>(wmols, nw, d.wsw_a, d.wsw_b, d.wsort_off, d.wlist_a, d.wlist_b, d.counters + 7);
 }
 
 }  // namespace sesp

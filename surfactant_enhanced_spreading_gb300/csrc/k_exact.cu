@@ -462,20 +462,20 @@ void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream
 // fast = 0 (plain path): the FP64 sweeps above, dividing exactly as the
 // reference does; fast = 1 / 2 (mixed paths): the FP64 / FP32 sweeps of
 // k_constraint.cu.
-void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
-                   int fast, const ConstraintShape &sh, cudaStream_t st) {
+void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, int nmol, int nsite,
+                   double tol, int maxit, int fast, const ConstraintShape &sh, cudaStream_t st) {
     if (fast) {
-        launch_move_a32(d, nw, smols, ns, sh, st, tol, maxit, fast == 2);
+        launch_move_a32(d, nw, smols, ns, nmol, nsite, sh, st, tol, maxit, fast == 2);
     } else {
         if (ns) k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
     }
     k_eta<<<nrep * ETA_BLOCKS, ETA_THREADS, 0, st>>>(d);
 }
-void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit, int fast,
-                   const ConstraintShape &sh, cudaStream_t st) {
+void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nmol, int nsite, double tol,
+                   int maxit, int fast, const ConstraintShape &sh, cudaStream_t st) {
     if (fast) {
-        launch_move_b32(d, nw, smols, ns, sh, st, tol, maxit, fast == 2);
+        launch_move_b32(d, nw, smols, ns, nmol, nsite, sh, st, tol, maxit, fast == 2);
     } else {
         if (ns) k_move_b_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);

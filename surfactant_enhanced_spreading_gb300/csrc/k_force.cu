@@ -69,7 +69,15 @@ __global__ void k_sort_cells(Dev d) {
     int s0 = d.cstart[c], n = d.cstart[c + 1] - s0;
     if (threadIdx.x == 0 && n > 0) atomicMax(&d.counters[3], (unsigned long long)n);
     if (n > SORT_CAP) {
+        // counted as an overflow; the cell keeps the scatter's order (its sums
+        // then depend on timing), with every per-slot field still written
         if (threadIdx.x == 0) atomicAdd(&d.counters[1], 1ull);
+        for (int t = threadIdx.x; t < n; t += blockDim.x) {
+            const int v = d.srt_site[s0 + t];
+            d.sslot[v] = s0 + t;
+            d.srt_meta[s0 + t] = make_int2(d.smol[v], (int)d.ptype[v]);
+            d.srt_key[s0 + t] = d.smol[v] << 5 | (int)d.ptype[v];
+        }
         return;
     }
     for (int t = threadIdx.x; t < n; t += blockDim.x) buf[t] = d.srt_site[s0 + t];
@@ -282,7 +290,7 @@ __global__ void k_near_items_fill(Dev d, int ncell, int tile) {
         for (int ch = 0; ch < nch; ch++) {
             const int nt = min(tile, ni - ch * tile);
             const int cls = 31 - __clz(nt * npart + 1);
-            d.near_items_tmp[k] = make_int2(c, pr << 8 | ch);
+            d.near_items_tmp[k] = make_int2(c, pr << 24 | ch);
             d.near_cls[k] = cls;
             atomicAdd(&bcount[cls], 1);
             k++;
@@ -444,7 +452,7 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
         k = __shfl_sync(0xffffffffu, k, 0);
         if (k >= nitems) break;
         const int2 item = d.near_items[k];
-        const int c = item.x, pr = item.y >> 8, chunk = item.y & 255;
+        const int c = item.x, pr = item.y >> 24, chunk = item.y & 0xFFFFFF;
         const int dzc = pr / 3 - 1, dyc = pr % 3 - 1;
         const int s0 = d.cstart[c], ni = d.cstart[c + 1] - s0;
         const int i0 = chunk * tile + lane, i1 = tile == 64 ? i0 + 32 : ni;

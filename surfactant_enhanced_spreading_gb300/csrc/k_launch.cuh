@@ -16,19 +16,20 @@ struct ConstraintShape {
     int s_warps;   // surfactant warps per CTA that starts on the surfactant queue
     int mpw;       // surfactants per such warp (1..8)
 };
-void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, double tol, int maxit,
-                   int fast, const ConstraintShape &sh, cudaStream_t st);
-void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, double tol, int maxit, int fast,
-                   const ConstraintShape &sh, cudaStream_t st);
+// nmol / nsite: the state's molecules and sites (bounds of the list checks)
+void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, int nmol, int nsite,
+                   double tol, int maxit, int fast, const ConstraintShape &sh, cudaStream_t st);
+void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nmol, int nsite, double tol,
+                   int maxit, int fast, const ConstraintShape &sh, cudaStream_t st);
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st);
 
 // k_constraint.cu (mixed paths: FP64 or FP32 sweeps); false if the uploaded
 // bond graph is not the one the kernels are specialised for
 bool upload_tables_fast(const Tables &t, cudaStream_t st);
-void launch_move_a32(const Dev &d, int nw, const int *smols, int ns, const ConstraintShape &sh, cudaStream_t st,
-                     double tol, int maxit, int fp32);
-void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, const ConstraintShape &sh, cudaStream_t st,
-                     double tol, int maxit, int fp32);
+void launch_move_a32(const Dev &d, int nw, const int *smols, int ns, int nmol, int nsite, const ConstraintShape &sh,
+                     cudaStream_t st, double tol, int maxit, int fp32);
+void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, int nmol, int nsite, const ConstraintShape &sh,
+                     cudaStream_t st, double tol, int maxit, int fp32);
 // reorders the halves' water lists by the sweeps of their last call (at list rebuilds)
 void launch_water_order(const Dev &d, const int *wmols, int nw, cudaStream_t st);
 int constraint_max_surf_warps();

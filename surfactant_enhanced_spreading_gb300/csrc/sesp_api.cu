@@ -7,6 +7,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -319,6 +320,10 @@ struct sesp_ctx {
     NearShape near = {64, 0};   // pair-field launch shape (autotuned or set; results do not depend on it)
     ConstraintShape cshape = {0, 4, 1};   // constraint halves of the mixed paths (likewise)
     int n_sm = 0;               // streaming multiprocessors of the device
+    // SESP_SYNC_CHECK set in the environment: every kernel family is followed
+    // by a stream synchronisation, and the first failing family is named
+    bool sync_check = false;
+    const char *fault = nullptr;
     // timing
     bool timing = false;
     cudaEvent_t ev[16];
@@ -400,6 +405,12 @@ void tcollect(sesp_ctx *c, int k) {
     else cudaGetLastError();
 }
 
+// with sync_check, wait for the family just launched and remember the first that failed
+void family(sesp_ctx *c, const char *name) {
+    if (!c->sync_check || c->fault) return;
+    if (cudaStreamSynchronize(c->st) != cudaSuccess) c->fault = name;
+}
+
 void seq_force(sesp_ctx *c, int rebuild, int terms) {
     const Dev &d = c->d;
     const int mixed = c->p.precision != SESP_PLAIN_FP64;
@@ -407,38 +418,51 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         tstart(c, 5);
         cudaMemsetAsync(d.ccount, 0, sizeof(int) * c->ncell, c->st);
         launch_locate(d, c->nmol, c->st);
+        family(c, "locate");
         launch_sort(d, c->nsite, c->ncell, c->st);
+        family(c, "cell sort");
         launch_near_items(d, c->ncell, (int)near_items_max(c->nsite, c->ncell), c->near.tile, c->st);
+        family(c, "near-field items");
         launch_isub(d, c->nsm * NSURF, c->smols, c->st);
+        family(c, "isub");
         launch_graphite_list(d, c->nsite, c->st);
+        family(c, "graphite list");
         if (mixed) launch_water_order(d, c->wmols, c->nwm, c->st);
+        family(c, "water order");
         tstop(c, 5);
     }
     launch_gather(d, c->nsite, c->ncell, mixed, c->st);
+    family(c, "gather");
     if (rebuild) {
         tstart(c, 6);
         launch_fma_build(d, c->ncell, c->n3, c->n2, mixed, c->d2, c->st);
+        family(c, "far-field build");
         tstop(c, 6);
     }
     tstart(c, 0);
     launch_near(d, c->ncell, c->nsite, mixed, terms, c->near, c->st);
+    family(c, "near field");
     tstop(c, 0);
     tstart(c, 4);
     launch_site_forces(d, c->nsite, terms, mixed, c->st);
+    family(c, "site forces");
     launch_intra(d, c->smols, c->nsm, terms, mixed, c->st);
+    family(c, "intramolecular");
     tstop(c, 4);
 }
 
 void seq_move_a(sesp_ctx *c) {
     tstart(c, 2);
-    launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit,
+    launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit,
                   c->p.precision, c->cshape, c->st);
+    family(c, "move_a");
     tstop(c, 2);
 }
 void seq_move_b(sesp_ctx *c) {
     tstart(c, 3);
-    launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit,
+    launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit,
                   c->p.precision, c->cshape, c->st);
+    family(c, "move_b");
     tstop(c, 3);
 }
 
@@ -502,6 +526,7 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
         c->near.grid = c->n_sm * near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64);
         c->cshape.grid = c->n_sm;
     }
+    c->sync_check = getenv("SESP_SYNC_CHECK") != nullptr;
     Tables T = make_tables();
     {
         std::vector<unsigned char> map = make_intra_map(T);
@@ -851,6 +876,7 @@ int sesp_force_terms(sesp_ctx *c, int rebuild, int terms) {
     if (!rebuild && !c->have_force) return fail(SESP_ESTATE, "the first force call must rebuild the lists");
     if (set_device(c)) return SESP_ECUDA;
     seq_force(c, rebuild, terms);
+    if (c->fault) return fail(SESP_ECUDA, "kernel family '%s' failed: %s", c->fault, cudaGetErrorString(cudaGetLastError()));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->st));
     collect_all(c);
@@ -910,11 +936,13 @@ static int launch_steps(sesp_ctx *c, int kb0, int nsteps) {
     for (int k = 0; k < nsteps; k++) {
         int kb = kb0 + k;
         int rb = (kb % c->p.rebuild_interval == 0) || !c->have_force;
-        if (c->timing) {
+        if (c->timing || c->sync_check) {
             seq_move_a(c);
             seq_force(c, rb, SESP_T_ALL);
             seq_move_b(c);
             collect_all(c);
+            if (c->fault) return fail(SESP_ECUDA, "step %d: kernel family '%s' failed: %s", kb, c->fault,
+                                      cudaGetErrorString(cudaGetLastError()));
         } else {
             cudaGraphExec_t &ge = c->g_step[rb];
             if (!ge) {
@@ -1057,9 +1085,9 @@ int tune_constraints(sesp_ctx *c) {
         for (int r = 0; r < 3; r++) {
             copy(false);
             cudaEventRecord(e0, c->st);
-            launch_move_a(d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->p.shake_tol, c->p.shake_maxit,
+            launch_move_a(d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit,
                           c->p.precision, sh, c->st);
-            launch_move_b(d, c->wmols, c->nwm, c->smols, c->nsm, c->p.shake_tol, c->p.shake_maxit, c->p.precision, sh,
+            launch_move_b(d, c->wmols, c->nwm, c->smols, c->nsm, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit, c->p.precision, sh,
                           c->st);
             cudaEventRecord(e1, c->st);
             cudaEventSynchronize(e1);

@@ -107,7 +107,7 @@ struct Dev {
     int *srt_key;        // molecule << 5 | type
     double *nf;          // near + far force by slot [3 * nslot]
     double *near_part;   // per partner row partial near force [9][3 * nslot]
-    int2 *near_items;    // near-field work items (cell, row << 8 | chunk), most expensive first
+    int2 *near_items;    // near-field work items (cell, row << 24 | chunk), most expensive first
     int2 *near_items_tmp;   // the same in cell order
     int *near_cls;       // cost class of each item in cell order
     int *near_icount;    // per cell: item count, then first item

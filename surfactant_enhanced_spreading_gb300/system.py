@@ -110,8 +110,11 @@ def surfactant_template(rng, tries: int = 200) -> np.ndarray:
     """29 sites in Angstrom satisfying every constraint length exactly.
 
     Sites are placed along the bond tree from site 1 with near-tetrahedral
-    bond angles and random dihedrals, rejecting placements that come closer
-    than 2.6 A to a site three or more bonds away.
+    bond angles (105-118 degrees to the parent bond); the children of one
+    site are spread evenly in azimuth around the parent bond (random offset,
+    +-15 degrees of jitter), so branch sites stay near-tetrahedral too.
+    Placements closer than 2.6 A to a site three or more bonds away are
+    rejected.
     """
     adj = {i: [] for i in range(1, 30)}
     blen = {}
@@ -132,6 +135,7 @@ def surfactant_template(rng, tries: int = 200) -> np.ndarray:
                         dist[s, v] = dist[s, u] + 1
                         nxt.append(v)
             frontier = nxt
+    jit = math.radians(15.0)
     for _ in range(tries):
         pos = {1: np.zeros(3)}
         parent = {1: None}
@@ -141,28 +145,38 @@ def surfactant_template(rng, tries: int = 200) -> np.ndarray:
         while k < len(order) and ok:
             u = order[k]
             k += 1
-            for v in adj[u]:
-                if v in pos:
-                    continue
-                for _attempt in range(60):
-                    p = parent[u]
+            kids = [v for v in adj[u] if v not in pos]
+            p = parent[u]
+            if p is not None:
+                b1 = pos[u] - pos[p]
+                b1 /= np.linalg.norm(b1)
+                e1 = np.cross(b1, rng.normal(size=3))
+                e1 /= np.linalg.norm(e1)
+                e2 = np.cross(b1, e1)
+            for attempt in range(60):
+                phi0 = rng.uniform(0.0, 2.0 * math.pi)
+                cands = []
+                for kc, v in enumerate(kids):
                     if p is None:
                         d = rng.normal(size=3)
                     else:
-                        b1 = pos[u] - pos[p]
-                        b1 /= np.linalg.norm(b1)
-                        perp = np.cross(b1, rng.normal(size=3))
-                        perp /= np.linalg.norm(perp)
                         ang = math.radians(rng.uniform(105.0, 118.0))
+                        phi = phi0 + 2.0 * math.pi * kc / len(kids) + rng.uniform(-jit, jit)
+                        perp = math.cos(phi) * e1 + math.sin(phi) * e2
                         d = math.cos(math.pi - ang) * b1 + math.sin(math.pi - ang) * perp
                     d /= np.linalg.norm(d)
-                    cand = pos[u] + blen[(u, v)] * d
-                    clash = any(dist[v, w] >= 3 and np.linalg.norm(cand - pw) < 2.6 for w, pw in pos.items())
-                    if not clash:
+                    cands.append(pos[u] + blen[(u, v)] * d)
+                clash = False
+                for v, cand in zip(kids, cands):
+                    if any(dist[v, w] >= 3 and np.linalg.norm(cand - pw) < 2.6 for w, pw in pos.items()):
+                        clash = True
                         break
-                else:
-                    ok = False
+                if not clash:
                     break
+            else:
+                ok = False
+                break
+            for v, cand in zip(kids, cands):
                 pos[v] = cand
                 parent[v] = u
                 order.append(v)

@@ -5,6 +5,7 @@ import pytest
 
 from surfactant_enhanced_spreading_gb300 import engine as E
 from surfactant_enhanced_spreading_gb300 import serve
+from surfactant_enhanced_spreading_gb300 import system as S
 
 
 @pytest.mark.parametrize("nw,ns", [(300, 0), (600, 6), (2000, 20)])
@@ -46,3 +47,42 @@ def test_summary_percentiles():
     assert abs(s["p50_latency_s"] - 50.5) < 1e-9
     assert abs(s["p99_latency_s"] - 99.01) < 1e-9
     assert abs(s["atom_steps_per_s"] - 100 * 10 * 100 / 100.0) < 1e-9
+
+
+def test_surfactant_templates_are_clash_free():
+    """Exact constraint lengths; no two sites closer than the shortest bond;
+    sites two bonds apart (incl. two children of a branch site) at least
+    1.8 A apart; sites three or more bonds apart at least 2.6 A apart."""
+    import itertools
+    rng = np.random.default_rng(11)
+    adj = {i: set() for i in range(1, 30)}
+    for i, j in S.SURF_BONDS:
+        adj[i].add(j)
+        adj[j].add(i)
+    two = {(a, b) for u in adj for a, b in itertools.combinations(sorted(adj[u]), 2)}
+    bonded = {tuple(sorted(b)) for b in S.SURF_BONDS}
+    for _ in range(60):
+        t = S.surfactant_template(rng)
+        for b, (i, j) in enumerate(S.SURF_BONDS):
+            assert abs(np.linalg.norm(t[i - 1] - t[j - 1]) - S.SURF_BOND_LEN[b]) < 1e-9
+        for a, b in itertools.combinations(range(1, 30), 2):
+            r = np.linalg.norm(t[a - 1] - t[b - 1])
+            if (a, b) in bonded:
+                continue
+            assert r > (1.8 if (a, b) in two else 2.6) - 1e-9, (a, b, r)
+
+
+def test_crowded_request_starts_without_failures():
+    """A served-size droplet with many surfactants (21,517 waters, 270
+    surfactants) takes its first steps on the oracle without a constraint
+    failure or a non-finite coordinate."""
+    import oracle as O
+    reqs = serve.poisson_requests(3, 2.0, 777, water=(1000, 50000), surf=(0, 500), steps=(500, 5000))
+    s = reqs[2].system
+    assert (s.n_water, s.n_surf) == (21517, 270)
+    orc = O.Oracle(s)
+    orc.force(True)
+    orc.init_accel()
+    orc.run(99101, 2)
+    assert orc.fail_count() == 0
+    assert np.isfinite(orc.get(0)).all()
