@@ -8,7 +8,8 @@ builds such states from a seed:
 
 * a hemispherical droplet of rigid 3-site waters (O-H 1 A, H-O-H 109.47 deg,
   the constraint lengths of src/init_arrays.f90:566-574) on a seed-jittered
-  cubic lattice at 0.0334 molecules per cubic Angstrom, random orientations;
+  cubic lattice at 0.0334 molecules per cubic Angstrom, random orientations
+  (re-drawn until no site is within 1.5 A of another molecule's);
 * 29-site trisiloxane surfactants built on the bond graph of
   src/init_arrays.f90:229-264 with the exact constraint lengths of
   src/init_arrays.f90:509-565, placed at the droplet surface;
@@ -51,6 +52,7 @@ SURF_MASS = np.array([_HY, _O, _ME, _ME, _O, _ME, _ME, _O, _ME, _ME, _O, _ME, _M
                       _METHYL]) / _O
 WATER_MASS = np.array([_O, _HY, _HY]) / _O
 WATER_HH = 2.0 * math.sin(109.47 * math.pi / 180.0 / 2.0)   # Angstrom
+CLOSE = 1.5   # Angstrom: no two sites of different molecules closer in a generated state
 
 
 @dataclasses.dataclass
@@ -280,6 +282,26 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
     wt = water_template()
     rots = _rand_rots(rng, n_water)
     wat = np.einsum("ij,mkj->mik", wt, rots) + pts[:, None, :]
+    # re-draw the orientation of waters with a site closer than CLOSE to a
+    # site of another molecule (jittered lattice points can be ~2.2 A apart)
+    from scipy.spatial import cKDTree
+    surf_flat = np.concatenate(surf_sites) if surf_sites else np.zeros((0, 3))
+    for _pass in range(200):
+        flat = np.concatenate([wat.reshape(-1, 3), surf_flat])
+        pairs = cKDTree(flat).query_pairs(CLOSE, output_type="ndarray")
+        mol = np.concatenate([np.arange(3 * n_water) // 3, n_water + np.arange(len(surf_flat)) // N_SURF_SITE])
+        if len(pairs):
+            pairs = pairs[mol[pairs[:, 0]] != mol[pairs[:, 1]]]
+        if not len(pairs):
+            break
+        # one water of each pair (the later one on even passes, the earlier on
+        # odd ones, the water of a water-surfactant pair)
+        first = pairs[:, 0] if _pass % 2 else pairs[:, 1]
+        other = pairs[:, 1] if _pass % 2 else pairs[:, 0]
+        bad = np.unique(np.where(mol[first] < n_water, first, other) // 3)
+        wat[bad] = np.einsum("ij,mkj->mik", wt, _rand_rots(rng, len(bad))) + pts[bad][:, None, :]
+    else:
+        raise RuntimeError("could not orient the waters without close contacts")
     pos = [wat.reshape(-1, 3)]
     if surf_sites:
         pos.append(np.concatenate(surf_sites))
