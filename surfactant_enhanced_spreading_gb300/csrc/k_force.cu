@@ -63,11 +63,18 @@ __global__ void k_scatter(Dev d, int nsite) {
 
 // order the sites of each cell by site index, so the slot order (and with it
 // every floating-point sum) is independent of the scatter's atomics
+// (order within a cell: sites with LJ first - every kind but water H - then
+// water H, each group by site index; cnh[c] counts the first group, so the
+// LJ pass of the FP32 path reads a prefix of every cell)
+constexpr int SORT_HBIT = 1 << 30;   // site indices stay below 2^30
 __global__ void k_sort_cells(Dev d) {
     __shared__ int buf[SORT_CAP];
+    __shared__ int nonh;
     int c = blockIdx.x;
     int s0 = d.cstart[c], n = d.cstart[c + 1] - s0;
+    if (threadIdx.x == 0) nonh = 0;
     if (threadIdx.x == 0 && n > 0) atomicMax(&d.counters[3], (unsigned long long)n);
+    __syncthreads();
     if (n > SORT_CAP) {
         // counted as an overflow; the cell keeps the scatter's order (its sums
         // then depend on timing), with every per-slot field still written
@@ -78,13 +85,21 @@ __global__ void k_sort_cells(Dev d) {
             d.srt_meta[s0 + t] = make_int2(d.smol[v], (int)d.ptype[v]);
             d.srt_key[s0 + t] = d.smol[v] << 5 | (int)d.ptype[v];
         }
+        if (threadIdx.x == 0) d.cnh[c] = n;   // the LJ pass then checks every slot's kind
         return;
     }
-    for (int t = threadIdx.x; t < n; t += blockDim.x) buf[t] = d.srt_site[s0 + t];
-    __syncthreads();
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        int v = buf[t], rank = 0;
-        for (int u = 0; u < n; u++) rank += buf[u] < v;
+        const int v = d.srt_site[s0 + t];
+        const bool h = d.ptype[v] == 1;
+        buf[t] = v | (h ? SORT_HBIT : 0);
+        if (!h) atomicAdd(&nonh, 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) d.cnh[c] = nonh;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) {
+        const int k = buf[t], v = k & (SORT_HBIT - 1);
+        int rank = 0;
+        for (int u = 0; u < n; u++) rank += buf[u] < k;
         d.srt_site[s0 + rank] = v;
         d.sslot[v] = s0 + rank;
         d.srt_meta[s0 + rank] = make_int2(d.smol[v], (int)d.ptype[v]);
@@ -383,6 +398,26 @@ __device__ __forceinline__ void pair2_acc32(const Tgt32 &a, const Tgt32 &b, bool
     if (two) { fb[0] += dxb * ftb; fb[1] += dyb * ftb; fb[2] += dzb * ftb; }
 }
 
+// One partner's Coulomb force on the two target sites of a lane, FP32 path:
+// q_i q_j xpi / r^3, zero for a partner of the same molecule (and for the
+// site itself, whose r = 0 reciprocal the select discards).  The LJ part of
+// the FP32 path is the separate pass k_lj_field over the non-H slots.
+__device__ __forceinline__ void pair2_coul32(const Tgt32 &a, const Tgt32 &b, bool two, float4 pj, int mj,
+                                             float (&fa)[3], float (&fb)[3]) {
+    const float dxa = a.x - pj.x, dya = a.y - pj.y, dza = a.z - pj.z;
+    const float r2a = dxa * dxa + dya * dya + dza * dza;
+    const float ira = mj == a.m ? 0.f : rsqrtf(r2a);
+    const float fta = (a.q * pj.w) * ira * (ira * ira);
+    fa[0] += dxa * fta; fa[1] += dya * fta; fa[2] += dza * fta;
+    if (two) {
+        const float dxb = b.x - pj.x, dyb = b.y - pj.y, dzb = b.z - pj.z;
+        const float r2b = dxb * dxb + dyb * dyb + dzb * dzb;
+        const float irb = mj == b.m ? 0.f : rsqrtf(r2b);
+        const float ftb = (b.q * pj.w) * irb * (irb * irb);
+        fb[0] += dxb * ftb; fb[1] += dyb * ftb; fb[2] += dzb * ftb;
+    }
+}
+
 __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool two, double4 pj, int key,
                                             const double2 *lj, double rc2, double (&fa)[3], double (&fb)[3]) {
     const int mj = key >> 5, tj = key & 31;
@@ -476,7 +511,6 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
                 const int kk = keys[s0 + i1];
                 tb = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, s_lj32[kk & 31]};
             }
-            const float rc2 = (float)(RC * RC);
             const float sy = (float)(-dyc * RS), sz = (float)(-dzc * RS);
             float fa[3] = {0.f, 0.f, 0.f}, fb[3] = {0.f, 0.f, 0.f};
             for (int jx = jx0; jx <= jx1; jx++) {
@@ -487,7 +521,7 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
                 ua.x += sx; ua.y += sy; ua.z += sz;
                 ub.x += sx; ub.y += sy; ub.z += sz;
 #pragma unroll 4
-                for (int sl = t0; sl < t1; sl++) pair2_acc32(ua, ub, two, pos32[sl], keys[sl], s_lj32, rc2, fa, fb);
+                for (int sl = t0; sl < t1; sl++) pair2_coul32(ua, ub, two, pos32[sl], keys[sl] >> 5, fa, fb);
             }
             if (a0) {
                 const size_t o = 3 * (size_t)(s0 + i0);
@@ -529,6 +563,78 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
 
 // Sum of the 9 row partials (fixed order) plus the local-expansion force of
 // src/evalLjk4.f90:31-282 for every slot; writes nf.
+// LJ of the FP32 path: 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2 within rc
+// (src/evalw1w1n.f90:86-104 form), none between sites of one molecule,
+// per-kind (sqrt(48 eps), sigma / 2) combined by the Lorentz-Berthelot rule
+// of src/init_arrays.f90:476-502.  Only sites that carry LJ - every kind but
+// water H, the first cnh slots of each cell - take part, as targets and as
+// partners, over the same 27-cell block as the pair field; the pair field
+// itself then computes Coulomb only.  One CTA per cell, one thread per
+// target; all threads read the same partner (an L1 broadcast).  Each target
+// sums in a fixed order (partner cells z, y, x, then slots).
+constexpr int LJ_THREADS = 128;
+__global__ void __launch_bounds__(LJ_THREADS) k_lj_field(Dev d) {
+    __shared__ float2 s_lj[NTYPE];
+    if (threadIdx.x < NTYPE) s_lj[threadIdx.x] = d.lj_kind[threadIdx.x];
+    __syncthreads();
+    const int c = blockIdx.x;
+    const int s0 = d.cstart[c], nh = d.cnh[c];
+    if (nh == 0) return;
+    const Rep r = d.rep[d.crep[c]];
+    int ix, iy, iz;
+    cell_xyz(r, c, ix, iy, iz);
+    const float4 *__restrict__ pos32 = d.srt_pos32;
+    const int *__restrict__ keys = d.srt_key;
+    const float rc2 = (float)(RC * RC), rsf = (float)RS;
+    for (int t0 = 0; t0 < nh; t0 += LJ_THREADS) {
+        const int ti = t0 + threadIdx.x;
+        const bool act = ti < nh;
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        int m = -1;
+        float2 l = make_float2(0.f, 0.f);
+        if (act) {
+            p = pos32[s0 + ti];
+            const int k = keys[s0 + ti];
+            m = k >> 5;
+            l = s_lj[k & 31];
+        }
+        float fx = 0.f, fy = 0.f, fz = 0.f;
+        for (int dz = -1; dz <= 1; dz++) {
+            const int jz = iz + dz;
+            if (jz < 0 || jz >= r.nc[2]) continue;
+            for (int dy = -1; dy <= 1; dy++) {
+                const int jy = iy + dy;
+                if (jy < 0 || jy >= r.nc[1]) continue;
+                for (int dx = -1; dx <= 1; dx++) {
+                    const int jx = ix + dx;
+                    if (jx < 0 || jx >= r.nc[0]) continue;
+                    const int cn = cell_index(r, jx, jy, jz);
+                    const int q0 = d.cstart[cn], q1 = q0 + d.cnh[cn];
+                    // the target in the partner cell's frame
+                    const float tx = p.x - (float)dx * rsf, ty = p.y - (float)dy * rsf, tz = p.z - (float)dz * rsf;
+                    for (int sl = q0; sl < q1; sl++) {
+                        const float4 pj = pos32[sl];
+                        const int kj = keys[sl];
+                        const float ddx = tx - pj.x, ddy = ty - pj.y, ddz = tz - pj.z;
+                        const float r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                        if (r2 <= rc2 && (kj >> 5) != m && (kj & 31) != 1) {
+                            const float2 v = s_lj[kj & 31];
+                            const float e = l.x * v.x, sg = l.y + v.y, s2 = sg * sg, s6 = s2 * s2 * s2;
+                            const float ira = rsqrtf(r2), ir2 = ira * ira, r6 = ir2 * ir2 * ir2;
+                            const float ft = e * s6 * r6 * (s6 * r6 - 0.5f) * ir2;
+                            fx += ddx * ft; fy += ddy * ft; fz += ddz * ft;
+                        }
+                    }
+                }
+            }
+        }
+        if (act) {
+            float *o = d.lj_part + 3 * (size_t)(s0 + ti);
+            o[0] = fx; o[1] = fy; o[2] = fz;
+        }
+    }
+}
+
 template <bool MIXED>
 __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     typedef typename std::conditional<MIXED, float, double>::type R;
@@ -546,6 +652,10 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
             if (!(mask >> pr & 1)) continue;
             const double *p = d.near_part + (size_t)pr * 3 * nslot + 3 * (size_t)s;
             fx += p[0]; fy += p[1]; fz += p[2];
+        }
+        if (MIXED && s < d.cstart[c] + d.cnh[c]) {   // the LJ pass's slots
+            const float *q = d.lj_part + 3 * (size_t)s;
+            fx += (double)q[0]; fy += (double)q[1]; fz += (double)q[2];
         }
     }
     if (terms & SESP_T_FAR) {
@@ -578,8 +688,12 @@ int near_max_ctas_per_sm(int mixed) {
 void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st) {
     if (terms & SESP_T_NEAR) {
         cudaMemsetAsync(d.near_ctl, 0, sizeof(int), st);
-        if (mixed) k_near<true><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
-        else k_near<false><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+        if (mixed) {
+            k_near<true><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+            k_lj_field<<<ncell, LJ_THREADS, 0, st>>>(d);
+        } else {
+            k_near<false><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+        }
     }
     if (mixed) k_near_finish<true><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
     else k_near_finish<false><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
