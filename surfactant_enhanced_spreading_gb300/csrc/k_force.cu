@@ -569,25 +569,33 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
 // of src/init_arrays.f90:476-502.  Only sites that carry LJ - every kind but
 // water H, the first cnh slots of each cell - take part, as targets and as
 // partners, over the same 27-cell block as the pair field; the pair field
-// itself then computes Coulomb only.  One CTA per cell, one thread per
-// target; all threads read the same partner (an L1 broadcast).  Each target
-// sums in a fixed order (partner cells z, y, x, then slots).
-constexpr int LJ_THREADS = 128;
+// itself then computes Coulomb only.  One CTA per cell: warp (row, half)
+// takes the cell's targets 32 x half .. + 31 (one per lane) against partner
+// row `row` (up to 3 cells along x); all lanes read the same partner (an L1
+// broadcast).  The 9 row sums of a target are added in row order in shared
+// memory, so the result is reproducible.
+constexpr int LJ_HALVES = 2, LJ_THREADS = 32 * 9 * LJ_HALVES;
 __global__ void __launch_bounds__(LJ_THREADS) k_lj_field(Dev d) {
     __shared__ float2 s_lj[NTYPE];
-    if (threadIdx.x < NTYPE) s_lj[threadIdx.x] = d.lj_kind[threadIdx.x];
-    __syncthreads();
+    __shared__ float s_f[9][32 * LJ_HALVES][3];
     const int c = blockIdx.x;
     const int s0 = d.cstart[c], nh = d.cnh[c];
     if (nh == 0) return;
+    if (threadIdx.x < NTYPE) s_lj[threadIdx.x] = d.lj_kind[threadIdx.x];
     const Rep r = d.rep[d.crep[c]];
     int ix, iy, iz;
     cell_xyz(r, c, ix, iy, iz);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = warp % 9, half = warp / 9;
+    const int dy = row % 3 - 1, dz = row / 3 - 1, jy = iy + dy, jz = iz + dz;
+    const bool row_in = jy >= 0 && jy < r.nc[1] && jz >= 0 && jz < r.nc[2];
+    const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
     const float4 *__restrict__ pos32 = d.srt_pos32;
     const int *__restrict__ keys = d.srt_key;
     const float rc2 = (float)(RC * RC), rsf = (float)RS;
-    for (int t0 = 0; t0 < nh; t0 += LJ_THREADS) {
-        const int ti = t0 + threadIdx.x;
+    __syncthreads();
+    for (int t0 = 0; t0 < nh; t0 += 32 * LJ_HALVES) {
+        const int tl = half * 32 + lane, ti = t0 + tl;
         const bool act = ti < nh;
         float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
         int m = -1;
@@ -599,39 +607,36 @@ __global__ void __launch_bounds__(LJ_THREADS) k_lj_field(Dev d) {
             l = s_lj[k & 31];
         }
         float fx = 0.f, fy = 0.f, fz = 0.f;
-        for (int dz = -1; dz <= 1; dz++) {
-            const int jz = iz + dz;
-            if (jz < 0 || jz >= r.nc[2]) continue;
-            for (int dy = -1; dy <= 1; dy++) {
-                const int jy = iy + dy;
-                if (jy < 0 || jy >= r.nc[1]) continue;
-                for (int dx = -1; dx <= 1; dx++) {
-                    const int jx = ix + dx;
-                    if (jx < 0 || jx >= r.nc[0]) continue;
-                    const int cn = cell_index(r, jx, jy, jz);
-                    const int q0 = d.cstart[cn], q1 = q0 + d.cnh[cn];
-                    // the target in the partner cell's frame
-                    const float tx = p.x - (float)dx * rsf, ty = p.y - (float)dy * rsf, tz = p.z - (float)dz * rsf;
-                    for (int sl = q0; sl < q1; sl++) {
-                        const float4 pj = pos32[sl];
-                        const int kj = keys[sl];
-                        const float ddx = tx - pj.x, ddy = ty - pj.y, ddz = tz - pj.z;
-                        const float r2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                        if (r2 <= rc2 && (kj >> 5) != m && (kj & 31) != 1) {
-                            const float2 v = s_lj[kj & 31];
-                            const float e = l.x * v.x, sg = l.y + v.y, s2 = sg * sg, s6 = s2 * s2 * s2;
-                            const float ira = rsqrtf(r2), ir2 = ira * ira, r6 = ir2 * ir2 * ir2;
-                            const float ft = e * s6 * r6 * (s6 * r6 - 0.5f) * ir2;
-                            fx += ddx * ft; fy += ddy * ft; fz += ddz * ft;
-                        }
-                    }
+        if (row_in && __any_sync(0xffffffffu, act)) {
+            for (int jx = jx0; jx <= jx1; jx++) {
+                const int cn = cell_index(r, jx, jy, jz);
+                const int q0 = d.cstart[cn], q1 = q0 + d.cnh[cn];
+                // the target in the partner cell's frame
+                const float tx = p.x + (float)(ix - jx) * rsf, ty = p.y - (float)dy * rsf, tz = p.z - (float)dz * rsf;
+#pragma unroll 4
+                for (int sl = q0; sl < q1; sl++) {
+                    const float4 pj = pos32[sl];
+                    const int kj = keys[sl];
+                    const float ddx = tx - pj.x, ddy = ty - pj.y, ddz = tz - pj.z;
+                    const float r2 = ddx * ddx + ddy * ddy + ddz * ddz;
+                    const bool on = r2 <= rc2 && (kj >> 5) != m && (kj & 31) != 1;
+                    const float2 v = s_lj[kj & 31];
+                    const float e = l.x * v.x, sg = l.y + v.y, s2 = sg * sg, s6 = s2 * s2 * s2;
+                    const float ira = rsqrtf(on ? r2 : 1.f), ir2 = ira * ira, r6 = ir2 * ir2 * ir2;
+                    const float ft = on ? e * s6 * r6 * (s6 * r6 - 0.5f) * ir2 : 0.f;
+                    fx += ddx * ft; fy += ddy * ft; fz += ddz * ft;
                 }
             }
         }
-        if (act) {
-            float *o = d.lj_part + 3 * (size_t)(s0 + ti);
-            o[0] = fx; o[1] = fy; o[2] = fz;
+        s_f[row][tl][0] = fx; s_f[row][tl][1] = fy; s_f[row][tl][2] = fz;
+        __syncthreads();
+        if (threadIdx.x < 32 * LJ_HALVES && t0 + (int)threadIdx.x < nh) {
+            float gx = 0.f, gy = 0.f, gz = 0.f;
+            for (int k = 0; k < 9; k++) { gx += s_f[k][threadIdx.x][0]; gy += s_f[k][threadIdx.x][1]; gz += s_f[k][threadIdx.x][2]; }
+            float *o = d.lj_part + 3 * (size_t)(s0 + t0 + threadIdx.x);
+            o[0] = gx; o[1] = gy; o[2] = gz;
         }
+        __syncthreads();
     }
 }
 
