@@ -65,7 +65,7 @@ __global__ void k_scatter(Dev d, int nsite) {
 // every floating-point sum) is independent of the scatter's atomics
 // (order within a cell: sites with LJ first - every kind but water H - then
 // water H, each group by site index; cnh[c] counts the first group, so the
-// LJ pass of the FP32 path reads a prefix of every cell)
+// FP32 pair loop runs its LJ test on a prefix of every partner cell only)
 constexpr int SORT_HBIT = 1 << 30;   // site indices stay below 2^30
 __global__ void k_sort_cells(Dev d) {
     __shared__ int buf[SORT_CAP];
@@ -85,7 +85,7 @@ __global__ void k_sort_cells(Dev d) {
             d.srt_meta[s0 + t] = make_int2(d.smol[v], (int)d.ptype[v]);
             d.srt_key[s0 + t] = d.smol[v] << 5 | (int)d.ptype[v];
         }
-        if (threadIdx.x == 0) d.cnh[c] = n;   // the LJ pass then checks every slot's kind
+        if (threadIdx.x == 0) d.cnh[c] = n;   // the pair loop then tests every slot for LJ
         return;
     }
     for (int t = threadIdx.x; t < n; t += blockDim.x) {
@@ -398,10 +398,10 @@ __device__ __forceinline__ void pair2_acc32(const Tgt32 &a, const Tgt32 &b, bool
     if (two) { fb[0] += dxb * ftb; fb[1] += dyb * ftb; fb[2] += dzb * ftb; }
 }
 
-// One partner's Coulomb force on the two target sites of a lane, FP32 path:
-// q_i q_j xpi / r^3, zero for a partner of the same molecule (and for the
-// site itself, whose r = 0 reciprocal the select discards).  The LJ part of
-// the FP32 path is the separate pass k_lj_field over the non-H slots.
+// One water-H partner's force on the two target sites of a lane, FP32 path:
+// Coulomb only (water H carries no LJ), q_i q_j xpi / r^3, zero for a
+// partner of the same molecule (and for the site itself, whose r = 0
+// reciprocal the select discards).
 __device__ __forceinline__ void pair2_coul32(const Tgt32 &a, const Tgt32 &b, bool two, float4 pj, int mj,
                                              float (&fa)[3], float (&fb)[3]) {
     const float dxa = a.x - pj.x, dya = a.y - pj.y, dza = a.z - pj.z;
@@ -511,6 +511,7 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
                 const int kk = keys[s0 + i1];
                 tb = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, s_lj32[kk & 31]};
             }
+            const float rc2 = (float)(RC * RC);
             const float sy = (float)(-dyc * RS), sz = (float)(-dzc * RS);
             float fa[3] = {0.f, 0.f, 0.f}, fb[3] = {0.f, 0.f, 0.f};
             for (int jx = jx0; jx <= jx1; jx++) {
@@ -520,8 +521,12 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
                 Tgt32 ua = ta, ub = tb;   // targets in the partner cell's frame
                 ua.x += sx; ua.y += sy; ua.z += sz;
                 ub.x += sx; ub.y += sy; ub.z += sz;
+                // partners with LJ first (the cell sort puts water H last)
+                const int th = t0 + d.cnh[cn];
 #pragma unroll 4
-                for (int sl = t0; sl < t1; sl++) pair2_coul32(ua, ub, two, pos32[sl], keys[sl] >> 5, fa, fb);
+                for (int sl = t0; sl < th; sl++) pair2_acc32(ua, ub, two, pos32[sl], keys[sl], s_lj32, rc2, fa, fb);
+#pragma unroll 4
+                for (int sl = th; sl < t1; sl++) pair2_coul32(ua, ub, two, pos32[sl], keys[sl] >> 5, fa, fb);
             }
             if (a0) {
                 const size_t o = 3 * (size_t)(s0 + i0);
@@ -563,83 +568,6 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
 
 // Sum of the 9 row partials (fixed order) plus the local-expansion force of
 // src/evalLjk4.f90:31-282 for every slot; writes nf.
-// LJ of the FP32 path: 48 eps sg6 r^-6 (sg6 r^-6 - 1/2) / r^2 within rc
-// (src/evalw1w1n.f90:86-104 form), none between sites of one molecule,
-// per-kind (sqrt(48 eps), sigma / 2) combined by the Lorentz-Berthelot rule
-// of src/init_arrays.f90:476-502.  Only sites that carry LJ - every kind but
-// water H, the first cnh slots of each cell - take part, as targets and as
-// partners, over the same 27-cell block as the pair field; the pair field
-// itself then computes Coulomb only.  One CTA per cell: warp (row, half)
-// takes the cell's targets 32 x half .. + 31 (one per lane) against partner
-// row `row` (up to 3 cells along x); all lanes read the same partner (an L1
-// broadcast).  The 9 row sums of a target are added in row order in shared
-// memory, so the result is reproducible.
-constexpr int LJ_HALVES = 2, LJ_THREADS = 32 * 9 * LJ_HALVES;
-__global__ void __launch_bounds__(LJ_THREADS) k_lj_field(Dev d) {
-    __shared__ float2 s_lj[NTYPE];
-    __shared__ float s_f[9][32 * LJ_HALVES][3];
-    const int c = blockIdx.x;
-    const int s0 = d.cstart[c], nh = d.cnh[c];
-    if (nh == 0) return;
-    if (threadIdx.x < NTYPE) s_lj[threadIdx.x] = d.lj_kind[threadIdx.x];
-    const Rep r = d.rep[d.crep[c]];
-    int ix, iy, iz;
-    cell_xyz(r, c, ix, iy, iz);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int row = warp % 9, half = warp / 9;
-    const int dy = row % 3 - 1, dz = row / 3 - 1, jy = iy + dy, jz = iz + dz;
-    const bool row_in = jy >= 0 && jy < r.nc[1] && jz >= 0 && jz < r.nc[2];
-    const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
-    const float4 *__restrict__ pos32 = d.srt_pos32;
-    const int *__restrict__ keys = d.srt_key;
-    const float rc2 = (float)(RC * RC), rsf = (float)RS;
-    __syncthreads();
-    for (int t0 = 0; t0 < nh; t0 += 32 * LJ_HALVES) {
-        const int tl = half * 32 + lane, ti = t0 + tl;
-        const bool act = ti < nh;
-        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-        int m = -1;
-        float2 l = make_float2(0.f, 0.f);
-        if (act) {
-            p = pos32[s0 + ti];
-            const int k = keys[s0 + ti];
-            m = k >> 5;
-            l = s_lj[k & 31];
-        }
-        float fx = 0.f, fy = 0.f, fz = 0.f;
-        if (row_in && __any_sync(0xffffffffu, act)) {
-            for (int jx = jx0; jx <= jx1; jx++) {
-                const int cn = cell_index(r, jx, jy, jz);
-                const int q0 = d.cstart[cn], q1 = q0 + d.cnh[cn];
-                // the target in the partner cell's frame
-                const float tx = p.x + (float)(ix - jx) * rsf, ty = p.y - (float)dy * rsf, tz = p.z - (float)dz * rsf;
-#pragma unroll 4
-                for (int sl = q0; sl < q1; sl++) {
-                    const float4 pj = pos32[sl];
-                    const int kj = keys[sl];
-                    const float ddx = tx - pj.x, ddy = ty - pj.y, ddz = tz - pj.z;
-                    const float r2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                    const bool on = r2 <= rc2 && (kj >> 5) != m && (kj & 31) != 1;
-                    const float2 v = s_lj[kj & 31];
-                    const float e = l.x * v.x, sg = l.y + v.y, s2 = sg * sg, s6 = s2 * s2 * s2;
-                    const float ira = rsqrtf(on ? r2 : 1.f), ir2 = ira * ira, r6 = ir2 * ir2 * ir2;
-                    const float ft = on ? e * s6 * r6 * (s6 * r6 - 0.5f) * ir2 : 0.f;
-                    fx += ddx * ft; fy += ddy * ft; fz += ddz * ft;
-                }
-            }
-        }
-        s_f[row][tl][0] = fx; s_f[row][tl][1] = fy; s_f[row][tl][2] = fz;
-        __syncthreads();
-        if (threadIdx.x < 32 * LJ_HALVES && t0 + (int)threadIdx.x < nh) {
-            float gx = 0.f, gy = 0.f, gz = 0.f;
-            for (int k = 0; k < 9; k++) { gx += s_f[k][threadIdx.x][0]; gy += s_f[k][threadIdx.x][1]; gz += s_f[k][threadIdx.x][2]; }
-            float *o = d.lj_part + 3 * (size_t)(s0 + t0 + threadIdx.x);
-            o[0] = gx; o[1] = gy; o[2] = gz;
-        }
-        __syncthreads();
-    }
-}
-
 template <bool MIXED>
 __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     typedef typename std::conditional<MIXED, float, double>::type R;
@@ -657,10 +585,6 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
             if (!(mask >> pr & 1)) continue;
             const double *p = d.near_part + (size_t)pr * 3 * nslot + 3 * (size_t)s;
             fx += p[0]; fy += p[1]; fz += p[2];
-        }
-        if (MIXED && s < d.cstart[c] + d.cnh[c]) {   // the LJ pass's slots
-            const float *q = d.lj_part + 3 * (size_t)s;
-            fx += (double)q[0]; fy += (double)q[1]; fz += (double)q[2];
         }
     }
     if (terms & SESP_T_FAR) {
@@ -693,12 +617,8 @@ int near_max_ctas_per_sm(int mixed) {
 void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st) {
     if (terms & SESP_T_NEAR) {
         cudaMemsetAsync(d.near_ctl, 0, sizeof(int), st);
-        if (mixed) {
-            k_near<true><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
-            k_lj_field<<<ncell, LJ_THREADS, 0, st>>>(d);
-        } else {
-            k_near<false><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
-        }
+        if (mixed) k_near<true><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+        else k_near<false><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
     }
     if (mixed) k_near_finish<true><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
     else k_near_finish<false><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);

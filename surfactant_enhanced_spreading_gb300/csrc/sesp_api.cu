@@ -630,7 +630,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.wlist_a, nwm)) || (e = dalloc(c, &d.wlist_b, nwm)) || (e = dalloc(c, &d.wsw_a, M)) ||
         (e = dalloc(c, &d.wsw_b, M)) || (e = dalloc(c, &d.cctl, 8)) || (e = dalloc(c, &d.wsort_off, 256)) ||
         (e = dalloc(c, &d.eta_part, 64 * (size_t)R)) || (e = dalloc(c, &d.eta_ctl, R)) ||
-        (e = dalloc(c, &d.cnh, C)) || (e = dalloc(c, &d.lj_part, 3 * (size_t)N)))
+        (e = dalloc(c, &d.cnh, C)))
         return e;
     int w2 = 2 * d2 + 1;
     const size_t nh2 = (size_t)w2 * w2 * w2 * NHARM;

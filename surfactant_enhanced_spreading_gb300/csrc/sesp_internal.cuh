@@ -100,7 +100,7 @@ struct Dev {
     int *crep, *b3rep, *b2rep;
     int *cstart, *ccount, *cfill;
     int *sloc, *sslot;
-    int *cnh;            // per cell: slots with LJ (every kind but water H), which come first
+    int *cnh;            // per cell: slots with LJ (every kind but water H), which the sort puts first
     int *srt_site;
     double4 *srt_pos;    // x, y, z, q in slot order (FP64)
     float4 *srt_pos32;   // x, y, z relative to the slot's own cell centre, q (mixed)
@@ -108,7 +108,6 @@ struct Dev {
     int *srt_key;        // molecule << 5 | type
     double *nf;          // near + far force by slot [3 * nslot]
     double *near_part;   // per partner row partial near force [9][3 * nslot]
-    float *lj_part;      // LJ force per slot of the FP32 path's LJ pass [3 * nslot]
     int2 *near_items;    // near-field work items (cell, row << 24 | chunk), most expensive first
     int2 *near_items_tmp;   // the same in cell order
     int *near_cls;       // cost class of each item in cell order
