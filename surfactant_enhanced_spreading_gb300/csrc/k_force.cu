@@ -345,13 +345,13 @@ void launch_near_items(const Dev &d, int ncell, int nitems_max, int tile, cudaSt
 // within rc; zero for a partner of the same molecule (src/evalSS.f90:36).  The
 // LJ part runs only when some lane of the warp has a target within rc of the
 // partner (the partner is the same for the whole warp).
-// FP32: per-kind (sqrt(48 eps), sigma/2) combined by the Lorentz-Berthelot
-// rule of src/init_arrays.f90:476-502.  FP64: the pair's (48 eps sg6, sg6)
-// from the table.
+// The pair's (48 eps sg6, sg6) from the kind-pair table (the
+// Lorentz-Berthelot rule of src/init_arrays.f90:476-502, formed in FP64;
+// FP32 copy for the FP32 path).
 struct Tgt32 {
     float x, y, z, q;   // position relative to the target cell's centre, shifted into the partner cell's frame; q * xpi
     int m;              // molecule
-    float2 l;           // (sqrt(48 eps), sigma / 2)
+    int trow;           // kind * NTYPE: the target's row of the kind-pair table
 };
 struct Tgt64 {
     double x, y, z, q;
@@ -359,7 +359,7 @@ struct Tgt64 {
 };
 
 __device__ __forceinline__ void pair2_acc32(const Tgt32 &a, const Tgt32 &b, bool two, float4 pj, int key,
-                                            const float2 *lj, float rc2, float (&fa)[3], float (&fb)[3]) {
+                                            const float2 *ljt, float rc2, float (&fa)[3], float (&fb)[3]) {
     const int mj = key >> 5, tj = key & 31;
     const float dxa = a.x - pj.x, dya = a.y - pj.y, dza = a.z - pj.z;
     const bool samea = mj == a.m;
@@ -379,18 +379,15 @@ __device__ __forceinline__ void pair2_acc32(const Tgt32 &a, const Tgt32 &b, bool
     if (tj != 1) {   // water H carries no LJ
         const bool na = r2a <= rc2 && !samea, nb = two && r2b <= rc2 && !sameb;
         if (__any_sync(0xffffffffu, na || nb)) {
-            const float2 v = lj[tj];
             {
-                const float e = a.l.x * v.x, sg = a.l.y + v.y, s2 = sg * sg, s6 = s2 * s2 * s2;
-                const float on = na ? e * s6 : 0.f;
+                const float2 v = ljt[a.trow + tj];
                 const float r6 = ir2a * ir2a * ir2a;
-                fta += on * r6 * (s6 * r6 - 0.5f) * ir2a;
+                fta += (na ? v.x : 0.f) * r6 * (v.y * r6 - 0.5f) * ir2a;
             }
             if (two) {
-                const float e = b.l.x * v.x, sg = b.l.y + v.y, s2 = sg * sg, s6 = s2 * s2 * s2;
-                const float on = nb ? e * s6 : 0.f;
+                const float2 v = ljt[b.trow + tj];
                 const float r6 = ir2b * ir2b * ir2b;
-                ftb += on * r6 * (s6 * r6 - 0.5f) * ir2b;
+                ftb += (nb ? v.x : 0.f) * r6 * (v.y * r6 - 0.5f) * ir2b;
             }
         }
     }
@@ -468,10 +465,10 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 // in FP32 over one row (at most 3 cells).
 template <bool MIXED>
 __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int tile) {
-    __shared__ float2 s_lj32[NTYPE];
+    __shared__ float2 s_lj32[MIXED ? NTYPE * NTYPE : 1];
     __shared__ double2 s_lj64[MIXED ? 1 : NTYPE * NTYPE];
     if constexpr (MIXED) {
-        if (threadIdx.x < NTYPE) s_lj32[threadIdx.x] = d.lj_kind[threadIdx.x];
+        for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) s_lj32[t] = d.ljt32[t];
     } else {
         for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) s_lj64[t] = d.ljt[t];
     }
@@ -500,16 +497,16 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
         const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
         double *part = d.near_part + (size_t)pr * 3 * nslot;
         if constexpr (MIXED) {
-            Tgt32 ta = {0.f, 0.f, 0.f, 0.f, -1, {0.f, 0.f}}, tb = ta;
+            Tgt32 ta = {0.f, 0.f, 0.f, 0.f, -1, 0}, tb = ta;
             if (a0) {
                 const float4 p = pos32[s0 + i0];
                 const int kk = keys[s0 + i0];
-                ta = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, s_lj32[kk & 31]};
+                ta = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, (kk & 31) * NTYPE};
             }
             if (a1) {
                 const float4 p = pos32[s0 + i1];
                 const int kk = keys[s0 + i1];
-                tb = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, s_lj32[kk & 31]};
+                tb = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, (kk & 31) * NTYPE};
             }
             const float rc2 = (float)(RC * RC);
             const float sy = (float)(-dyc * RS), sz = (float)(-dzc * RS);

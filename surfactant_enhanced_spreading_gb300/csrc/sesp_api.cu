@@ -148,16 +148,6 @@ namespace {
 // per site kind (sqrt(48 eps), sigma / 2) for the FP32 pair kernel, which
 // combines them by the Lorentz-Berthelot rule of src/init_arrays.f90:476-502:
 // 48 eps_ij = sqrt(48 eps_i) sqrt(48 eps_j), sigma_ij = sigma_i/2 + sigma_j/2
-std::vector<float2> make_lj_kinds() {
-    double sgs[NSURF], eps[NSURF];
-    surf_lj(sgs, eps);
-    std::vector<float2> t(NTYPE);
-    t[0] = make_float2((float)sqrt(48.0), 0.5f);     // water O: sigma = epsilon = 1
-    t[1] = make_float2(0.f, 0.f);                     // water H: no LJ
-    for (int k = 0; k < NSURF; k++) t[2 + k] = make_float2((float)sqrt(48.0 * eps[k]), (float)(sgs[k] / 2.0));
-    return t;
-}
-
 // contribution table of the intramolecular kernel: term slots per site.
 // Layout (matches IntraMap in k_force.cu): short off[30], short list[852],
 // uchar pa[312], uchar pb[312].  Slots: angle a -> 3a + {i, vertex, k};
@@ -626,7 +616,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
         (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
         (e = dalloc(c, &d.L2, (size_t)LP * n2)) || (e = dalloc(c, &d.counters, 8)) ||
-        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &d.lj_kind, NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)) ||
+        (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &d.ljt32, NTYPE * NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)) ||
         (e = dalloc(c, &d.wlist_a, nwm)) || (e = dalloc(c, &d.wlist_b, nwm)) || (e = dalloc(c, &d.wsw_a, M)) ||
         (e = dalloc(c, &d.wsw_b, M)) || (e = dalloc(c, &d.cctl, 8)) || (e = dalloc(c, &d.wsort_off, 256)) ||
         (e = dalloc(c, &d.eta_part, 64 * (size_t)R)) || (e = dalloc(c, &d.eta_ctl, R)) ||
@@ -750,8 +740,9 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         }
     }
     std::vector<double2> ljt = make_lj_table();
-    std::vector<float2> ljk = make_lj_kinds();
-    CK(cudaMemcpyAsync(d.lj_kind, ljk.data(), ljk.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
+    std::vector<float2> ljt32(ljt.size());
+    for (size_t k = 0; k < ljt.size(); k++) ljt32[k] = make_float2((float)ljt[k].x, (float)ljt[k].y);
+    CK(cudaMemcpyAsync(d.ljt32, ljt32.data(), ljt32.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.x, sx.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.y, sy.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.z, sz.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));

@@ -133,7 +133,7 @@ struct Dev {
     float *m2l_cf32;
     // LJ pair table (eps, sg6), NTYPE^2
     double2 *ljt;
-    float2 *lj_kind;     // per site kind (sqrt(48 eps), sigma / 2), zero eps for water H
+    float2 *ljt32;       // FP32 copy of ljt
     // counters: [0] fails, [1] overflow, [2] unlocated, [3] max cell, [5] pairs, [6] LJ pairs
     unsigned long long *counters;
     int max_cell;

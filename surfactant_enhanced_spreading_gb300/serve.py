@@ -92,9 +92,9 @@ def estimate_bytes(system: S.System) -> int:
     d2 = max(1, int((nc // 4).max()) - 1)
     w2 = 2 * d2 + 1
     per_site = 12 * 8 + 1 + 4 * 4 + 32 + 16 + 8 + 4 + 3 * 8 + 27 * 8 + 6
-    per_mol = 5 * 4 + 2 * 8 + 4 + 4
+    per_mol = 5 * 4 + 2 * 8 + 4 + 4 + 2 * 4 + 2   # incl. the constraint halves' water lists and sweep counts
     cz = 25 * 16
-    cells = ncell * (4 * 4 + 2 * cz + 4 + 9 * 20) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
+    cells = ncell * (5 * 4 + 2 * cz + 4 + 9 * 20) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
     ops = (2 * 343 + w2 ** 3 + 4 * 8) * 15 * 25 * 16 + 2 * 343 * 15 * 25 * 8
     ncarb = system.carbons.reshape(-1, 3).shape[0]
     graphite = 12 * ncarb * 48 + int(nc[0] * nc[1] + 1) * 4 + int(nc.sum()) * 8 + n * 4
