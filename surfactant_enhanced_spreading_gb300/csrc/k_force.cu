@@ -358,61 +358,107 @@ struct Tgt64 {
     int m, trow;        // molecule, type * NTYPE
 };
 
-__device__ __forceinline__ void pair2_acc32(const Tgt32 &a, const Tgt32 &b, bool two, float4 pj, int key,
-                                            const float2 *ljt, float rc2, float (&fa)[3], float (&fb)[3]) {
+// FP32 path, K target sites per lane: one partner against targets t[0..K),
+// Coulomb plus, for a partner with LJ, the LJ term of each target within rc
+// (run when some lane of the warp has one); pairk_coul32 for a water-H
+// partner (no LJ), whose exclusion is a select on the reciprocal distance
+// (it also discards the site itself, at r = 0).
+template <int K>
+__device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int key, const float2 *ljt, float rc2,
+                                            float (&f)[K][3]) {
     const int mj = key >> 5, tj = key & 31;
-    const float dxa = a.x - pj.x, dya = a.y - pj.y, dza = a.z - pj.z;
-    const bool samea = mj == a.m;
-    const float r2a = samea ? 1.f : dxa * dxa + dya * dya + dza * dza;
-    const float ira = rsqrtf(r2a), ir2a = ira * ira;
-    float fta = (samea ? 0.f : a.q * pj.w) * ira * ir2a;
-    float dxb = 0.f, dyb = 0.f, dzb = 0.f, r2b = 1.f, ir2b = 0.f, ftb = 0.f;
-    bool sameb = true;
-    if (two) {
-        dxb = b.x - pj.x; dyb = b.y - pj.y; dzb = b.z - pj.z;
-        sameb = mj == b.m;
-        r2b = sameb ? 1.f : dxb * dxb + dyb * dyb + dzb * dzb;
-        const float irb = rsqrtf(r2b);
-        ir2b = irb * irb;
-        ftb = (sameb ? 0.f : b.q * pj.w) * irb * ir2b;
+    float dx[K], dy[K], dz[K], r2[K], ir2[K], ft[K];
+    bool same[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        dx[j] = t[j].x - pj.x; dy[j] = t[j].y - pj.y; dz[j] = t[j].z - pj.z;
+        same[j] = mj == t[j].m;
+        r2[j] = same[j] ? 1.f : dx[j] * dx[j] + dy[j] * dy[j] + dz[j] * dz[j];
+        const float ira = rsqrtf(r2[j]);
+        ir2[j] = ira * ira;
+        ft[j] = (same[j] ? 0.f : t[j].q * pj.w) * ira * ir2[j];
     }
     if (tj != 1) {   // water H carries no LJ
-        const bool na = r2a <= rc2 && !samea, nb = two && r2b <= rc2 && !sameb;
-        if (__any_sync(0xffffffffu, na || nb)) {
-            {
-                const float2 v = ljt[a.trow + tj];
-                const float r6 = ir2a * ir2a * ir2a;
-                fta += (na ? v.x : 0.f) * r6 * (v.y * r6 - 0.5f) * ir2a;
-            }
-            if (two) {
-                const float2 v = ljt[b.trow + tj];
-                const float r6 = ir2b * ir2b * ir2b;
-                ftb += (nb ? v.x : 0.f) * r6 * (v.y * r6 - 0.5f) * ir2b;
+        bool n[K], any = false;
+#pragma unroll
+        for (int j = 0; j < K; j++) { n[j] = r2[j] <= rc2 && !same[j]; any = any || n[j]; }
+        if (__any_sync(0xffffffffu, any)) {
+#pragma unroll
+            for (int j = 0; j < K; j++) {
+                const float2 v = ljt[t[j].trow + tj];
+                const float r6 = ir2[j] * ir2[j] * ir2[j];
+                ft[j] += (n[j] ? v.x : 0.f) * r6 * (v.y * r6 - 0.5f) * ir2[j];
             }
         }
     }
-    fa[0] += dxa * fta; fa[1] += dya * fta; fa[2] += dza * fta;
-    if (two) { fb[0] += dxb * ftb; fb[1] += dyb * ftb; fb[2] += dzb * ftb; }
+#pragma unroll
+    for (int j = 0; j < K; j++) { f[j][0] += dx[j] * ft[j]; f[j][1] += dy[j] * ft[j]; f[j][2] += dz[j] * ft[j]; }
+}
+template <int K>
+__device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int mj, float (&f)[K][3]) {
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        const float dx = t[j].x - pj.x, dy = t[j].y - pj.y, dz = t[j].z - pj.z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float ira = mj == t[j].m ? 0.f : rsqrtf(r2);
+        const float ft = (t[j].q * pj.w) * ira * (ira * ira);
+        f[j][0] += dx * ft; f[j][1] += dy * ft; f[j][2] += dz * ft;
+    }
 }
 
-// One water-H partner's force on the two target sites of a lane, FP32 path:
-// Coulomb only (water H carries no LJ), q_i q_j xpi / r^3, zero for a
-// partner of the same molecule (and for the site itself, whose r = 0
-// reciprocal the select discards).
-__device__ __forceinline__ void pair2_coul32(const Tgt32 &a, const Tgt32 &b, bool two, float4 pj, int mj,
-                                             float (&fa)[3], float (&fb)[3]) {
-    const float dxa = a.x - pj.x, dya = a.y - pj.y, dza = a.z - pj.z;
-    const float r2a = dxa * dxa + dya * dya + dza * dza;
-    const float ira = mj == a.m ? 0.f : rsqrtf(r2a);
-    const float fta = (a.q * pj.w) * ira * (ira * ira);
-    fa[0] += dxa * fta; fa[1] += dya * fta; fa[2] += dza * fta;
-    if (two) {
-        const float dxb = b.x - pj.x, dyb = b.y - pj.y, dzb = b.z - pj.z;
-        const float r2b = dxb * dxb + dyb * dyb + dzb * dzb;
-        const float irb = mj == b.m ? 0.f : rsqrtf(r2b);
-        const float ftb = (b.q * pj.w) * irb * (irb * irb);
-        fb[0] += dxb * ftb; fb[1] += dyb * ftb; fb[2] += dzb * ftb;
+// One FP32 work item with K target sites per lane (lane + 32 j of the chunk):
+// the force of partner row pr on them, written to that row's partial.
+template <int K>
+__device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int nslot, int c, int pr, int first,
+                                            int ni, int lane) {
+    const float4 *__restrict__ pos32 = d.srt_pos32;
+    const int *__restrict__ keys = d.srt_key;
+    const int dzc = pr / 3 - 1, dyc = pr % 3 - 1;
+    const int s0 = d.cstart[c];
+    const Rep r = d.rep[d.crep[c]];
+    int ix, iy, iz;
+    cell_xyz(r, c, ix, iy, iz);
+    const int jy = iy + dyc, jz = iz + dzc;
+    const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+    Tgt32 t[K];
+    bool act[K];
+#pragma unroll
+    for (int j = 0; j < K; j++) {
+        const int i = first + lane + 32 * j;
+        act[j] = i < ni;
+        t[j] = {0.f, 0.f, 0.f, 0.f, -1, 0};
+        if (act[j]) {
+            const float4 p = pos32[s0 + i];
+            const int kk = keys[s0 + i];
+            t[j] = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, (kk & 31) * NTYPE};
+        }
     }
+    const float rc2 = (float)(RC * RC);
+    const float sy = (float)(-dyc * RS), sz = (float)(-dzc * RS);
+    float f[K][3];
+#pragma unroll
+    for (int j = 0; j < K; j++) f[j][0] = f[j][1] = f[j][2] = 0.f;
+    for (int jx = jx0; jx <= jx1; jx++) {
+        const int cn = cell_index(r, jx, jy, jz);
+        const int t0 = d.cstart[cn], t1 = d.cstart[cn + 1];
+        const float sx = (float)((ix - jx) * RS);
+        Tgt32 u[K];   // targets in the partner cell's frame
+#pragma unroll
+        for (int j = 0; j < K; j++) { u[j] = t[j]; u[j].x += sx; u[j].y += sy; u[j].z += sz; }
+        // partners with LJ first (the cell sort puts water H last)
+        const int th = t0 + d.cnh[cn];
+#pragma unroll 2
+        for (int sl = t0; sl < th; sl++) pairk_acc32<K>(u, pos32[sl], keys[sl], ljt, rc2, f);
+#pragma unroll 2
+        for (int sl = th; sl < t1; sl++) pairk_coul32<K>(u, pos32[sl], keys[sl] >> 5, f);
+    }
+    double *part = d.near_part + (size_t)pr * 3 * nslot;
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        if (act[j]) {
+            const size_t o = 3 * (size_t)(s0 + first + lane + 32 * j);
+            part[o] = f[j][0]; part[o + 1] = f[j][1]; part[o + 2] = f[j][2];
+        }
 }
 
 __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool two, double4 pj, int key,
@@ -463,7 +509,7 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 // change any arithmetic, so results are bit-reproducible.
 // MIXED: FP32 positions relative to the cell centres, FP32 pair terms summed
 // in FP32 over one row (at most 3 cells).
-template <bool MIXED>
+template <bool MIXED, int KMAX>
 __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int tile) {
     __shared__ float2 s_lj32[MIXED ? NTYPE * NTYPE : 1];
     __shared__ double2 s_lj64[MIXED ? 1 : NTYPE * NTYPE];
@@ -497,42 +543,12 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
         const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
         double *part = d.near_part + (size_t)pr * 3 * nslot;
         if constexpr (MIXED) {
-            Tgt32 ta = {0.f, 0.f, 0.f, 0.f, -1, 0}, tb = ta;
-            if (a0) {
-                const float4 p = pos32[s0 + i0];
-                const int kk = keys[s0 + i0];
-                ta = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, (kk & 31) * NTYPE};
-            }
-            if (a1) {
-                const float4 p = pos32[s0 + i1];
-                const int kk = keys[s0 + i1];
-                tb = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, (kk & 31) * NTYPE};
-            }
-            const float rc2 = (float)(RC * RC);
-            const float sy = (float)(-dyc * RS), sz = (float)(-dzc * RS);
-            float fa[3] = {0.f, 0.f, 0.f}, fb[3] = {0.f, 0.f, 0.f};
-            for (int jx = jx0; jx <= jx1; jx++) {
-                const int cn = cell_index(r, jx, jy, jz);
-                const int t0 = d.cstart[cn], t1 = d.cstart[cn + 1];
-                const float sx = (float)((ix - jx) * RS);
-                Tgt32 ua = ta, ub = tb;   // targets in the partner cell's frame
-                ua.x += sx; ua.y += sy; ua.z += sz;
-                ub.x += sx; ub.y += sy; ub.z += sz;
-                // partners with LJ first (the cell sort puts water H last)
-                const int th = t0 + d.cnh[cn];
-#pragma unroll 4
-                for (int sl = t0; sl < th; sl++) pair2_acc32(ua, ub, two, pos32[sl], keys[sl], s_lj32, rc2, fa, fb);
-#pragma unroll 4
-                for (int sl = th; sl < t1; sl++) pair2_coul32(ua, ub, two, pos32[sl], keys[sl] >> 5, fa, fb);
-            }
-            if (a0) {
-                const size_t o = 3 * (size_t)(s0 + i0);
-                part[o] = fa[0]; part[o + 1] = fa[1]; part[o + 2] = fa[2];
-            }
-            if (a1) {
-                const size_t o = 3 * (size_t)(s0 + i1);
-                part[o] = fb[0]; part[o + 1] = fb[1]; part[o + 2] = fb[2];
-            }
+            // K = targets per lane: ceil(targets of the chunk / 32), at most KMAX
+            const int nt = min(tile, ni - chunk * tile), kk = (nt + 31) >> 5;
+            if (kk <= 1) near_item32<1>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else if (kk == 2 || KMAX == 2) near_item32<2>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else if (kk == 3) near_item32<(KMAX > 2 ? 3 : 2)>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else near_item32<KMAX>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
         } else {
             Tgt64 ta = {0.0, 0.0, 0.0, 0.0, -1, 0}, tb = ta;
             if (a0) {
@@ -604,18 +620,20 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     d.nf[3 * (size_t)s] = fx; d.nf[3 * (size_t)s + 1] = fy; d.nf[3 * (size_t)s + 2] = fz;
 }
 
-int near_max_ctas_per_sm(int mixed) {
+int near_max_ctas_per_sm(int mixed, int tile) {
     int nb = 0;
-    if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true>, NEAR_THREADS, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<false>, NEAR_THREADS, 0);
+    if (mixed && tile > 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 4>, NEAR_THREADS, 0);
+    else if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 2>, NEAR_THREADS, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<false, 2>, NEAR_THREADS, 0);
     return nb > 0 ? nb : 1;
 }
 
 void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st) {
     if (terms & SESP_T_NEAR) {
         cudaMemsetAsync(d.near_ctl, 0, sizeof(int), st);
-        if (mixed) k_near<true><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
-        else k_near<false><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+        if (mixed && shape.tile > 64) k_near<true, 4><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+        else if (mixed) k_near<true, 2><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+        else k_near<false, 2><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
     }
     if (mixed) k_near_finish<true><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
     else k_near_finish<false><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);

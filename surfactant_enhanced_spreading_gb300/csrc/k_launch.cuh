@@ -42,11 +42,11 @@ void launch_sort(const Dev &d, int nsite, int ncell, cudaStream_t st);
 void launch_gather(const Dev &d, int nslot, int ncell, int mixed, cudaStream_t st);
 // launch shape of the pair field (results do not depend on it)
 struct NearShape {
-    int tile;   // target sites per work item: 64 or 32
+    int tile;   // target sites per work item: 32, 64 or (FP32 path) 128, up to 4 per lane
     int grid;   // CTAs of the persistent kernel
 };
 void launch_near_items(const Dev &d, int ncell, int nitems_max, int tile, cudaStream_t st);
-int near_max_ctas_per_sm(int mixed);
+int near_max_ctas_per_sm(int mixed, int tile);
 void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st);
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st);
 void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st);

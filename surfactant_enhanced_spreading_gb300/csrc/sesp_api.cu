@@ -513,7 +513,9 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, dev);
-        c->near.grid = c->n_sm * near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64);
+        const int mixed = c->p.precision != SESP_PLAIN_FP64;
+        c->near.tile = mixed ? 128 : 64;
+        c->near.grid = c->n_sm * near_max_ctas_per_sm(mixed, c->near.tile);
         c->cshape.grid = c->n_sm;
     }
     c->sync_check = getenv("SESP_SYNC_CHECK") != nullptr;
@@ -996,9 +998,10 @@ void drop_graphs(sesp_ctx *c) {
 int sesp_set_tuning(sesp_ctx *c, int tile, int ctas_per_sm) {
     if (int e = check_ctx(c, true)) return e;
     const int mixed = c->p.precision != SESP_PLAIN_FP64;
-    if (tile != 32 && tile != 64) return fail(SESP_EINVAL, "tile must be 32 or 64");
-    if (ctas_per_sm < 1 || ctas_per_sm > near_max_ctas_per_sm(mixed))
-        return fail(SESP_EINVAL, "ctas_per_sm must be 1..%d", near_max_ctas_per_sm(mixed));
+    if (tile != 32 && tile != 64 && !(mixed && tile == 128))
+        return fail(SESP_EINVAL, "tile must be 32 or 64 (or 128 on the mixed paths)");
+    if (ctas_per_sm < 1 || ctas_per_sm > near_max_ctas_per_sm(mixed, tile))
+        return fail(SESP_EINVAL, "ctas_per_sm must be 1..%d", near_max_ctas_per_sm(mixed, tile));
     if (set_device(c)) return SESP_ECUDA;
     const bool retile = tile != c->near.tile;
     c->near = {tile, c->n_sm * ctas_per_sm};
@@ -1014,7 +1017,7 @@ int sesp_tuning(sesp_ctx *c, int out[3]) {
     if (!out) return fail(SESP_EINVAL, "null output");
     out[0] = c->near.tile;
     out[1] = c->n_sm ? c->near.grid / c->n_sm : 0;
-    out[2] = near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64);
+    out[2] = near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64, c->near.tile);
     return 0;
 }
 
@@ -1100,8 +1103,9 @@ int tune_constraints(sesp_ctx *c) {
 }  // namespace
 
 // Times the pair field on the current state for every candidate shape (tile
-// 64 or 32 sites per work item; 1/4, 1/2, 3/4 or all of the CTAs per SM the
-// kernel can hold), median of 5 launches each, and keeps the fastest; on the
+// 128 (mixed paths), 64 or 32 sites per work item; 1/4, 1/2, 3/4 or all of
+// the CTAs per SM the kernel can hold), median of 5 launches each, and keeps
+// the fastest; on the
 // mixed paths with surfactants, then the constraint halves' surfactant warps
 // per CTA (the state is restored afterwards).
 int sesp_autotune(sesp_ctx *c, int out[3]) {
@@ -1110,14 +1114,15 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     if (!c->have_force) return fail(SESP_ESTATE, "autotuning needs a force call first (cell lists)");
     if (set_device(c)) return SESP_ECUDA;
     const int mixed = c->p.precision != SESP_PLAIN_FP64;
-    const int mx = near_max_ctas_per_sm(mixed);
-    int cands[4] = {mx, (3 * mx) / 4, mx / 2, mx / 4};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
     float best = 1e30f;
     NearShape pick = c->near;
-    for (int tile : {64, 32}) {
+    for (int tile : {128, 64, 32}) {
+        if (tile == 128 && !mixed) continue;
+        const int mx = near_max_ctas_per_sm(mixed, tile);
+        const int cands[4] = {mx, (3 * mx) / 4, mx / 2, mx / 4};
         launch_near_items(c->d, c->ncell, (int)near_items_max(c->nsite, c->ncell), tile, c->st);
         for (int k = 0; k < 4; k++) {
             const int cps = cands[k];
@@ -1147,7 +1152,7 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     CK(cudaStreamSynchronize(c->st));
     out[0] = pick.tile;
     out[1] = pick.grid / c->n_sm;
-    out[2] = mx;
+    out[2] = near_max_ctas_per_sm(mixed, pick.tile);
     return 0;
 }
 

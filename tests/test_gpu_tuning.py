@@ -19,10 +19,13 @@ def test_shapes_give_identical_forces(sys_small, precision):
     eng = E.Engine(sys_small, precision)
     f0 = eng.force(True)
     tile, cps, mx = eng.autotune()
-    assert tile in (32, 64) and 1 <= cps <= mx
+    assert tile in ((32, 64, 128) if precision == E.MIXED else (32, 64)) and 1 <= cps <= mx
     assert eng.tuning() == (tile, cps, mx)
     assert np.array_equal(eng.force(True), f0)
-    for shape in [(32, 1), (64, 1), (32, mx), (64, mx), (64, max(1, mx // 2))]:
+    shapes = [(32, 1), (64, 1), (32, mx), (64, mx), (64, max(1, mx // 2))]
+    if precision == E.MIXED:
+        shapes += [(128, 1), (128, 4)]
+    for shape in shapes:
         eng.set_tuning(*shape)
         assert eng.tuning()[:2] == shape
         assert np.array_equal(eng.force(True), f0), shape
@@ -31,7 +34,7 @@ def test_shapes_give_identical_forces(sys_small, precision):
 
 def test_shapes_give_identical_trajectories(sys_small):
     runs = []
-    for shape in [(64, None), (32, 1)]:
+    for shape in [(64, None), (32, 1), (128, 2)]:
         eng = E.Engine(sys_small, E.MIXED)
         eng.force(True)
         if shape[1] is None:
@@ -41,8 +44,9 @@ def test_shapes_give_identical_trajectories(sys_small):
         eng.init_accel()
         eng.run(99101, 25)
         runs.append(eng.state())
-    for a, b in zip(runs[0], runs[1]):
-        assert np.array_equal(a, b)
+    for other in runs[1:]:
+        for a, b in zip(runs[0], other):
+            assert np.array_equal(a, b)
 
 
 def test_invalid_shapes_are_refused(sys_small):
@@ -51,6 +55,9 @@ def test_invalid_shapes_are_refused(sys_small):
         eng.set_tuning(48, 1)
     with pytest.raises(E.SespError, match="EINVAL"):
         eng.set_tuning(64, 0)
+    plain = E.Engine(sys_small, E.PLAIN_FP64)
+    with pytest.raises(E.SespError, match="EINVAL"):
+        plain.set_tuning(128, 1)   # 4 targets per lane: the FP32 path only
     with pytest.raises(E.SespError, match="ESTATE"):
         eng.autotune()   # no force call yet
 
