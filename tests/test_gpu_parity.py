@@ -213,9 +213,9 @@ def test_mixed_trajectory_100_steps(mode):
     assert eng.counters()[0] == orc.fail_count() == 0
 
 
-def _nve_drift(precision, steps=600, every=20):
+def _nve_drift(precision, seed, steps=600, every=20):
     """Energy drift (reduced energy per step) with the thermostat off."""
-    s = S.droplet(500, 4, cells=(8, 8, 8), seed=41)
+    s = S.droplet(500, 4, cells=(8, 8, 8), seed=seed)
     eng = E.Engine(s, precision, tau_steps=1e12)
     eng.force(True)
     eng.init_accel()
@@ -226,18 +226,25 @@ def _nve_drift(precision, steps=600, every=20):
         kb += every
         es.append(eng.energies().sum())
     t = np.arange(len(es)) * every
-    return np.polyfit(t, np.array(es), 1)[0], abs(np.mean(es))
+    return np.polyfit(t, np.array(es), 1)[0]
+
+
+DRIFT_SEEDS = (41, 42, 43, 44, 45, 46)
+
+
+@pytest.fixture(scope="module")
+def plain_drift():
+    return np.mean([abs(_nve_drift(E.PLAIN_FP64, k)) for k in DRIFT_SEEDS])
 
 
 @pytest.mark.parametrize("mode", [E.MIXED, E.MIXED_FP32C])
-def test_mixed_energy_drift_not_worse_than_plain(mode):
-    """NVE drift (thermostat off) of the mixed paths against the plain path's,
-    a linear fit over 600 steps.  The drift of all three is dominated by the
-    reference's loose SHAKE tolerance (1e-4); SESP_MIXED, the headline, must
-    stay within 2x the plain path's.  SESP_MIXED_FP32C, whose FP32 sweeps
-    land elsewhere inside the tolerance band, has measured up to ~3x and is
-    held to 4x; it is reported beside the headline, not as it."""
-    dp, scale = _nve_drift(E.PLAIN_FP64)
-    dm, _ = _nve_drift(mode)
-    factor = 2.0 if mode == E.MIXED else 4.0
-    assert abs(dm) <= factor * abs(dp) + 1e-6 * scale, (dm, dp)
+def test_mixed_energy_drift_not_worse_than_plain(mode, plain_drift):
+    """NVE drift (thermostat off) of the mixed paths against the plain
+    path's: linear fits over 600 steps of six freshly built droplets, which
+    are still relaxing, so one droplet's drift is mostly chaos (plain
+    0.3-1.8, mixed 0.6-2.7 reduced units per step on GB300) and the
+    comparison is of the means: measured 0.78 plain, 1.11 SESP_MIXED, 1.32
+    SESP_MIXED_FP32C.  Both mixed modes must stay within twice the plain
+    mean."""
+    dm = np.mean([abs(_nve_drift(mode, k)) for k in DRIFT_SEEDS])
+    assert dm <= 2.0 * plain_drift, (dm, plain_drift)
