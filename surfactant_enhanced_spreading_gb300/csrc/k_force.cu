@@ -1084,8 +1084,13 @@ __global__ void k_graphite_list(Dev d, int nsite) {
     if (graphite_column(d, r, g, eps, sg6) >= 0) d.gsite[atomicAdd(d.gcount, 1)] = g;
 }
 
-// graphite LJ (src/eval_graphite.f90:104-126), one warp per listed site: the
-// lanes split the column's carbons and a fixed shuffle tree sums them.
+// graphite LJ (src/eval_graphite.f90:104-126), one warp per listed site.
+// Lanes 0..GGRP-1 each take one carbon group (a graphite layer) of the
+// site's column: a group farther than rc in z is skipped, and of the others
+// only the y bins within sqrt(rc^2 - dz^2) of the site are visited (bounds
+// widened by 1e-3, far above the FP32 rounding of the window arithmetic; the
+// exact r^2 <= rc^2 test still decides every pair).  The lanes then stride
+// the visited carbons of all groups and a fixed shuffle tree sums them.
 // FP32 (mixed path): site and carbons relative to the column centre, so each
 // carbon costs FP32 arithmetic only.
 template <typename R>
@@ -1095,19 +1100,50 @@ __global__ void k_graphite(Dev d) {
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int n = *d.gcount;
     const R rc2 = (R)(RC * RC);
+    const float reach = (float)RC + 1e-3f, bin_scale = GBIN / (2.f * GYMAX);
     for (int k = warp; k < n; k += nwarp) {
         int g = d.gsite[k];
         const Rep r = d.rep[d.mrep[d.smol[g]]];
         double eps, sg6;
-        int col = graphite_column(d, r, g, eps, sg6);
-        double xd = d.x[g], yd = d.y[g], zd = d.z[g];
+        const int col = graphite_column(d, r, g, eps, sg6);
+        const double xd = d.x[g], yd = d.y[g], zd = d.z[g];
+        const int lc = col - r.gcol0, ix = lc % r.nc[0], iy = lc / r.nc[0];
+        const float xs = (float)(xd - cell_centre(d, r, 0, ix)), ys = (float)(yd - cell_centre(d, r, 1, iy)),
+                    zs = (float)(zd - cell_centre(d, r, 2, 0));
+        int s0 = 0, len = 0;
+        if (lane < GGRP) {
+            const size_t gi = (size_t)col * GGRP + lane;
+            const float2 zr = d.ggrp_z[gi];
+            const float dz = fmaxf(fmaxf(zr.x - zs, zs - zr.y), 0.f);
+            if (zr.x <= zr.y && dz < reach) {
+                const float w = sqrtf(fmaxf(reach * reach - dz * dz, 0.f)) + 1e-3f;
+                const int b0 = min(max((int)floorf((ys - w + GYMAX) * bin_scale), 0), GBIN);
+                const int b1 = min(max((int)floorf((ys + w + GYMAX) * bin_scale) + 1, 0), GBIN);
+                const int *bins = d.gbin + gi * (GBIN + 1);
+                s0 = bins[b0];
+                len = bins[b1] - s0;
+            }
+        }
+        int incl = len;   // inclusive prefix over the group lanes
+        for (int o = 1; o < GGRP; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        int st[GGRP], pe[GGRP];
+#pragma unroll
+        for (int q = 0; q < GGRP; q++) {
+            st[q] = __shfl_sync(0xffffffffu, s0, q);
+            pe[q] = __shfl_sync(0xffffffffu, incl, q);
+        }
+        const int total = pe[GGRP - 1];
         R e48 = (R)(48.0 * eps * sg6), s6 = (R)sg6;
         R fx = 0, fy = 0, fz = 0;
-        if constexpr (std::is_same<R, float>::value) {
-            const int lc = col - r.gcol0, ix = lc % r.nc[0], iy = lc / r.nc[0];
-            const float xs = (float)(xd - cell_centre(d, r, 0, ix)), ys = (float)(yd - cell_centre(d, r, 1, iy)),
-                        zs = (float)(zd - cell_centre(d, r, 2, 0));
-            for (int q = d.gcol_start[col] + lane; q < d.gcol_start[col + 1]; q += 32) {
+        for (int t = lane; t < total; t += 32) {
+            int q = st[0] + t;
+#pragma unroll
+            for (int u = 1; u < GGRP; u++)
+                if (t >= pe[u - 1]) q = st[u] + t - pe[u - 1];
+            if constexpr (std::is_same<R, float>::value) {
                 const float4 c = d.gpos32[q];
                 const float xij = xs - c.x, yij = ys - c.y, zij = zs - c.z;
                 const float r2 = xij * xij + yij * yij + zij * zij;
@@ -1116,10 +1152,8 @@ __global__ void k_graphite(Dev d) {
                     const float flj = e48 * r6 * (s6 * r6 - 0.5f) * rsi;
                     fx += xij * flj; fy += yij * flj; fz += zij * flj;
                 }
-            }
-        } else {
-            for (int q = d.gcol_start[col] + lane; q < d.gcol_start[col + 1]; q += 32) {
-                double4 c = d.gpos[q];
+            } else {
+                const double4 c = d.gpos[q];
                 R xij = (R)(xd - c.x), yij = (R)(yd - c.y), zij = (R)(zd - c.z);
                 R r2 = xij * xij + yij * yij + zij * zij;
                 if (r2 <= rc2) {

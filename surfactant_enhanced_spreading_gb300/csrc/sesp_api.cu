@@ -642,6 +642,8 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     std::vector<int> gstart(1, 0);
     std::vector<double4> gpos;
     std::vector<float4> gpos32;   // relative to the column's (x, y) centre and the bottom cell layer's z centre
+    std::vector<int> gbin;        // per column and group: GBIN + 1 bin starts (the last is the group's end)
+    std::vector<float2> ggrp_z;   // per column and group: z range in the gpos32 frame
     double rcut = RC + sqrt(2.0) * RS / 2.0;
     rcut *= rcut;
     for (int q = 0; q < R; q++) {
@@ -671,18 +673,59 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         for (int iy = 0; iy < r.nc[1]; iy++)
             for (int ix = 0; ix < r.nc[0]; ix++) {
                 double cx = axis[a0 + ix], cy = axis[a0 + r.nc[0] + iy], cz = axis[a0 + r.nc[0] + r.nc[1]];
+                std::vector<int> ks;
                 for (int k = 0; k < ri.ncarb; k++) {
                     double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
-                    if (dx * dx + dy * dy <= rcut) {
-                        gpos.push_back(make_double4(ri.carb[3 * k], ri.carb[3 * k + 1], ri.carb[3 * k + 2], 0.0));
-                        gpos32.push_back(make_float4((float)dx, (float)dy, (float)(ri.carb[3 * k + 2] - cz), 0.f));
+                    if (dx * dx + dy * dy <= rcut) ks.push_back(k);
+                }
+                // groups: the column's carbons by z (a graphite layer each, at
+                // most GGRP groups of neighbouring z), each group in order of
+                // its FP32 y with GBIN uniform y bins over [-ymax, ymax], so a
+                // site visits only the groups and the y window within rc
+                std::sort(ks.begin(), ks.end(), [&](int a, int b) {
+                    return ri.carb[3 * a + 2] != ri.carb[3 * b + 2] ? ri.carb[3 * a + 2] < ri.carb[3 * b + 2] : a < b;
+                });
+                std::vector<int> bounds(1, 0);
+                for (size_t t = 1; t < ks.size(); t++)
+                    if (ri.carb[3 * ks[t] + 2] != ri.carb[3 * ks[t - 1] + 2]) bounds.push_back((int)t);
+                bounds.push_back((int)ks.size());
+                const int nz = (int)bounds.size() - 1;
+                std::vector<int> gb(1, 0);   // group bounds: every z level, or GGRP equal runs of them
+                for (int l = 1; l <= GGRP; l++)
+                    gb.push_back(bounds[nz <= GGRP ? (l <= nz ? l : nz) : (int)((long long)nz * l / GGRP)]);
+                auto y32 = [&](int k) { return (float)(ri.carb[3 * k + 1] - cy); };
+                const int base = (int)gpos.size();
+                for (int l = 0; l < GGRP; l++) {
+                    const int b0 = gb[l], b1 = gb[l + 1];
+                    std::sort(ks.begin() + b0, ks.begin() + b1,
+                              [&](int a, int b) { return y32(a) != y32(b) ? y32(a) < y32(b) : a < b; });
+                    float zlo = 0.f, zhi = -1.f;   // empty group
+                    for (int t = b0; t < b1; t++) {
+                        const float z = (float)(ri.carb[3 * ks[t] + 2] - cz);
+                        zlo = t == b0 ? z : std::min(zlo, z);
+                        zhi = t == b0 ? z : std::max(zhi, z);
                     }
+                    ggrp_z.push_back(make_float2(zlo, zhi));
+                    // bin edge j at -ymax + j * bw: the first carbon at or above it
+                    int t = b0;
+                    for (int j = 0; j < GBIN; j++) {
+                        const double edge = -(double)GYMAX + j * ((double)GYMAX * 2.0 / GBIN);
+                        while (t < b1 && (double)y32(ks[t]) < edge) t++;
+                        gbin.push_back(base + (j ? t : b0));
+                    }
+                    gbin.push_back(base + b1);
+                }
+                for (int k : ks) {
+                    double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
+                    gpos.push_back(make_double4(ri.carb[3 * k], ri.carb[3 * k + 1], ri.carb[3 * k + 2], 0.0));
+                    gpos32.push_back(make_float4((float)dx, (float)dy, (float)(ri.carb[3 * k + 2] - cz), 0.f));
                 }
                 gstart.push_back((int)gpos.size());
             }
     }
     if ((e = dalloc(c, &d.axis, axis.size())) || (e = dalloc(c, &d.gcol_start, gstart.size())) ||
         (e = dalloc(c, &d.gpos, gpos.size())) || (e = dalloc(c, &d.gpos32, gpos32.size())) ||
+        (e = dalloc(c, &d.gbin, gbin.size())) || (e = dalloc(c, &d.ggrp_z, ggrp_z.size())) ||
         (e = dalloc(c, &d.gsite, N)) || (e = dalloc(c, &d.gcount, 1)))
         return e;
     // translation operators
@@ -772,6 +815,10 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     if (!gpos.empty()) CK(cudaMemcpyAsync(d.gpos, gpos.data(), gpos.size() * sizeof(double4), cudaMemcpyHostToDevice, c->st));
     if (!gpos32.empty())
         CK(cudaMemcpyAsync(d.gpos32, gpos32.data(), gpos32.size() * sizeof(float4), cudaMemcpyHostToDevice, c->st));
+    if (!gbin.empty()) {
+        CK(cudaMemcpyAsync(d.gbin, gbin.data(), gbin.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(d.ggrp_z, ggrp_z.data(), ggrp_z.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
+    }
     CK(cudaMemcpyAsync(d.ljt, ljt.data(), ljt.size() * sizeof(double2), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemsetAsync(d.near_ctl, 0, 66 * sizeof(int), c->st));   // no near-field items before the first rebuild
     CK(cudaStreamSynchronize(c->st));

@@ -41,6 +41,11 @@ constexpr double XPI = (double)675.05f;
 constexpr double DT = 0.00127362;
 constexpr double DTSQ2 = 0.00127362 * 0.00127362 / 2.0;
 
+constexpr int GGRP = 8;       // carbon groups per graphite column
+constexpr int GBIN = 32;      // y bins per group
+// y extent of a column's carbons about its centre: rc + half the L4 cell diagonal
+constexpr float GYMAX = (float)(RC + 1.4142135623730951 * RS / 2.0) + 1e-3f;
+
 struct Rep {
     int nc[3];        // L4 cells per axis
     int nr[3];        // L2 boxes (4^3 L4 cells each) per axis
@@ -118,6 +123,9 @@ struct Dev {
     int *gcol_start;
     double4 *gpos;
     float4 *gpos32;      // the same carbons relative to the column centre (x, y) and the bottom layer's centre (z)
+    int *gbin;           // per column GGRP groups of its carbons (z levels, each in FP32 y order):
+                         // GBIN + 1 starts of uniform y bins over [-GYMAX, GYMAX], the last one the group's end
+    float2 *ggrp_z;      // z range of each group in the gpos32 frame (lo > hi: empty)
     int *gsite, *gcount;   // sites the graphite acts on (rebuilt with the lists)
     // intramolecular correction lists (bit k: site k+1 of the molecule)
     uint32_t *isub;

@@ -83,7 +83,8 @@ def estimate_bytes(system: S.System) -> int:
     engine's allocation list: per-site, per-molecule and per-cell arrays, the
     multipole tables of the three levels, the translation operators and the
     per-column carbon lists (each carbon lies within reach of at most about
-    8 bottom-layer columns), with a 10 % margin."""
+    8 bottom-layer columns) with their 8 groups of 33 y-bin starts and a z
+    range, with a 10 % margin."""
     n = system.n_sites
     nmol = system.n_water + system.n_surf
     nc = np.array(system.cells, dtype=np.int64)
@@ -97,7 +98,8 @@ def estimate_bytes(system: S.System) -> int:
     cells = ncell * (5 * 4 + 2 * cz + 4 + 9 * 20) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
     ops = (2 * 343 + w2 ** 3 + 4 * 8) * 15 * 25 * 16 + 2 * 343 * 15 * 25 * 8
     ncarb = system.carbons.reshape(-1, 3).shape[0]
-    graphite = 12 * ncarb * 48 + int(nc[0] * nc[1] + 1) * 4 + int(nc.sum()) * 8 + n * 4
+    ncol = int(nc[0] * nc[1])
+    graphite = 12 * ncarb * 48 + (ncol + 1) * 4 + ncol * 8 * (33 * 4 + 8) + int(nc.sum()) * 8 + n * 4
     surf = 29 * system.n_surf * 4
     total = n * per_site + nmol * per_mol + cells + ops + graphite + surf + 4096
     return int(1.1 * total) + (1 << 20)
