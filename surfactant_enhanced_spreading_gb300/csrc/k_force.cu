@@ -770,9 +770,12 @@ __global__ void __launch_bounds__(128) k_m2m(Dev d, const double2 *Oc, double2 *
 }
 
 // L2L, src/shiftLjk2.f90:16-60 and src/shiftLjk3.f90:27-91: child box
-// from its parent (level 2 -> 3 or 3 -> 4)
+// from its parent (level 2 -> 3 or 3 -> 4), plus the child's M2L partial
+// sums of its G offset groups (real form, [group][25][boxes of the level]),
+// added in group order
 template <typename R, typename OP>
-__global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, const int *brep, int level) {
+__global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, const int *brep, int level,
+                      const R *part, int G, int nlev) {
     const int b = blockIdx.x;
     const Rep r = d.rep[brep[b]];
     const int div = level == 3 ? 2 : 1;  // child grid = nc / div
@@ -788,7 +791,14 @@ __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, cons
     if (o >= LPH) return;
     R re = 0, im = 0;
     apply_op_r<R>(ops + ((size_t)ch * LPH + o) * LP, Lp + (size_t)pi * LP, re, im);
-    store_jk(Lc + (size_t)b * LP, o, (double)re, (double)im, false);
+    int j, k;
+    out_jk(o, j, k);
+    R pre = 0, pim = 0;
+    for (int g = 0; g < G; g++) {
+        pre += part[((size_t)g * LP + o) * nlev + b];
+        if (k > 0) pim += part[((size_t)g * LP + LPH + o - (j + 1)) * nlev + b];
+    }
+    store_jk(Lc + (size_t)b * LP, o, (double)re + (double)pre, (double)im + (double)pim, false);
 }
 
 // M2L with the operator of src/computeLjk4.f90:134-158 factored as
@@ -835,120 +845,146 @@ __device__ __forceinline__ void m2l_acc(const C2<R> *__restrict__ H, const S *sr
     }
 }
 
-// M2L at L4 and L3 (src/computeLjk4.f90, src/computeLjk3.f90): one CTA per
-// parent box; the parent's 6x6x6 window of child-level multipoles is staged
-// in shared memory.  Thread (output o, group g) takes every M2L_G-th of the
-// 343 offsets; per offset it forms the 25 products cf * H once and applies
-// them to all 8 children (25 complex MACs each), so an H value is loaded once
-// per offset and output instead of once per child.  The groups' sums are
-// added in a fixed order and accumulated into L.
-constexpr int M2L_G = 16;   // offset groups per CTA
-constexpr int M2L_THREADS = LPH * M2L_G;
+// M2L at L4 and L3 (src/computeLjk4.f90, src/computeLjk3.f90) in real form.
+// A cell's interaction list (children of its parent's neighbours, less its
+// own neighbours) depends only on its parity class (bit a: odd index on axis
+// a): 189 offsets with each component in [-2-p, 3-p].  So for one class and
+// one offset, every target applies the same 25 x 25 real operator to its
+// source's 25 real components: a lane takes two targets of a class, the CTA
+// stages the operators of its offset group in shared memory (read as
+// broadcasts), and the sources come from the class-packed copy of the
+// multipoles, whose zero margin of 2 stands for the cells outside the box.
+// Each offset group writes its partial sums; k_l2l adds the groups in a
+// fixed order.
 
+// multipoles of L4 and L3 to the class-packed real layout (margins stay zero)
 template <typename R>
-size_t m2l_smem() {
-    return sizeof(C2<R>) * 216 * LP + sizeof(R) * (2 * LPH * LP + 2 * M2L_G * 8 * LPH) + sizeof(int) * LPH * LP;
+__global__ void k_m2l_pack(Dev d, int ncell, int n3) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (ncell + n3) * LP) return;
+    const int i = idx % LP, c = idx / LP;
+    const bool l4 = c < ncell;
+    const int cc = l4 ? c : c - ncell;
+    const Rep r = d.rep[l4 ? d.crep[cc] : d.b3rep[cc]];
+    const int div = l4 ? 1 : 2;
+    const int n0 = r.nc[0] / div, n1 = r.nc[1] / div, n2 = r.nc[2] / div;
+    const int l = cc - (l4 ? r.cell0 : r.l3_0);
+    const int x = l % n0, y = (l / n0) % n1, z = l / (n0 * n1);
+    const int p0 = n0 / 2 + 4, p1 = n1 / 2 + 4, vol = p0 * p1 * (n2 / 2 + 4);
+    const int q = (x & 1) + 2 * (y & 1) + 4 * (z & 1);
+    int n, m;
+    bool im = i >= LPH;
+    if (!im) {
+        out_jk(i, n, m);
+    } else {   // Im X_n^m, m > 0: index 15 + n(n-1)/2 + m - 1
+        const int s = i - LPH;
+        n = 1;
+        while ((n + 1) * n / 2 <= s) n++;
+        m = s - n * (n - 1) / 2 + 1;
+    }
+    const double2 v = (l4 ? d.O4 : d.O3)[(size_t)cc * LP + n * (n + 1) + m];
+    R *pk = (R *)(l4 ? d.pk4 : d.pk3) + (l4 ? r.pk4 : r.pk3);
+    pk[((size_t)q * LP + i) * vol + ((z / 2 + 2) * p1 + (y / 2 + 2)) * p0 + x / 2 + 2] = (R)(im ? v.y : v.x);
+}
+
+constexpr int M2C_CH = 4;   // operators staged per chunk
+
+// one input row of a staged operator applied to two targets
+__device__ __forceinline__ void m2c_row(const float *op, float va, float vb, float (&aa)[LP], float (&ab)[LP]) {
+#pragma unroll
+    for (int o4 = 0; o4 < M2C_LD / 4; o4++) {
+        const float4 w = *(const float4 *)(op + 4 * o4);
+        const float ws[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (4 * o4 + u < LP) {
+                aa[4 * o4 + u] += ws[u] * va;
+                ab[4 * o4 + u] += ws[u] * vb;
+            }
+    }
+}
+__device__ __forceinline__ void m2c_row(const double *op, double va, double vb, double (&aa)[LP], double (&ab)[LP]) {
+#pragma unroll
+    for (int o2 = 0; o2 < M2C_LD / 2; o2++) {
+        const double2 w = *(const double2 *)(op + 2 * o2);
+        if (2 * o2 < LP) { aa[2 * o2] += w.x * va; ab[2 * o2] += w.x * vb; }
+        if (2 * o2 + 1 < LP) { aa[2 * o2 + 1] += w.y * va; ab[2 * o2 + 1] += w.y * vb; }
+    }
 }
 
 template <typename R>
-__global__ void __launch_bounds__(M2L_THREADS) k_m2l_win(Dev d, const double2 *O, double2 *L, const C2<R> *Htab,
-                                                         const R *cf, const int *prep, int level) {
+__global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d, int ncell, int n3) {
     extern __shared__ __align__(16) unsigned char smraw[];
-    C2<R> *sO = (C2<R> *)smraw;                  // [216][LP]
-    R *scr = (R *)(sO + 216 * LP);               // [LPH][LP] coefficient for Re H
-    R *sci = scr + LPH * LP;                     // [LPH][LP] coefficient for Im H (conjugation folded in)
-    R *sre = sci + LPH * LP;                     // [M2L_G][8][LPH]
-    R *sim = sre + M2L_G * 8 * LPH;
-    int *sh = (int *)(sim + M2L_G * 8 * LPH);    // [LPH][LP] index of H
-    const int p = blockIdx.x;
-    const Rep r = d.rep[prep[p]];
-    const int div = level == 4 ? 1 : 2;          // child grid = nc / div
-    const int base = level == 4 ? r.cell0 : r.l3_0;
-    const int pbase = level == 4 ? r.l3_0 : r.l2_0;
-    const int n[3] = {r.nc[0] / div, r.nc[1] / div, r.nc[2] / div};
-    const int np[3] = {n[0] / 2, n[1] / 2, n[2] / 2};
-    const int l = p - pbase;
-    const int pc[3] = {l % np[0], (l / np[0]) % np[1], l / (np[0] * np[1])};
-    const int w0[3] = {2 * pc[0] - 2, 2 * pc[1] - 2, 2 * pc[2] - 2};
-    for (int idx = threadIdx.x; idx < 216 * LP; idx += blockDim.x) {
-        const int cell = idx / LP, c = idx % LP;
-        const int sx = w0[0] + cell % 6, sy = w0[1] + (cell / 6) % 6, sz = w0[2] + cell / 36;
-        C2<R> v = {R(0), R(0)};
-        if (sx >= 0 && sy >= 0 && sz >= 0 && sx < n[0] && sy < n[1] && sz < n[2]) {
-            const double2 o = O[(size_t)(base + sx + n[0] * (sy + n[1] * sz)) * LP + c];
-            v.x = (R)o.x; v.y = (R)o.y;
+    R *sop = (R *)smraw;   // [M2C_CH][LP][M2C_LD]
+    const int4 it = d.m2c_items[blockIdx.x];
+    const int level = it.x >> 28, cls = it.y, t0 = it.z, cnt = it.w;
+    const Rep r = d.rep[it.x & 0x0FFFFFFF];
+    const int G = d.m2c_groups, g = blockIdx.y;
+    const int k0 = g * M2C_NOFF / G, k1 = (g + 1) * M2C_NOFF / G;
+    const int div = level == 4 ? 2 : 4;   // class grid = nc / div
+    const int h0 = r.nc[0] / div, h1 = r.nc[1] / div;
+    const int p0 = h0 + 4, p1 = h1 + 4, vol = p0 * p1 * (r.nc[2] / div + 4);
+    const int px = cls & 1, py = (cls >> 1) & 1, pz = cls >> 2;
+    const R *rop = (const R *)(level == 4 ? d.rop4 : d.rop3);
+    const R *pk = (const R *)(level == 4 ? d.pk4 : d.pk3) + (level == 4 ? r.pk4 : r.pk3);
+    const int *offs = d.m2c_off + cls * M2C_NOFF;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int ta = t0 + w * 64 + lane, tb = ta + 32, last = t0 + cnt - 1;
+    // padded class-grid index of a target (loads of lanes past the tile use its last target)
+    auto pidx = [&](int t) {
+        t = min(t, last);
+        const int x = t % h0, y = (t / h0) % h1, z = t / (h0 * h1);
+        return ((z + 2) * p1 + (y + 2)) * p0 + x + 2;
+    };
+    const int ia = pidx(ta), ib = pidx(tb);
+    R aa[LP], ab[LP];
+#pragma unroll
+    for (int i = 0; i < LP; i++) aa[i] = ab[i] = R(0);
+    for (int c0 = k0; c0 < k1; c0 += M2C_CH) {
+        const int nch = min(M2C_CH, k1 - c0);
+        __syncthreads();
+        for (int idx = threadIdx.x; idx < nch * LP * M2C_LD; idx += blockDim.x) {
+            const int kk = idx / (LP * M2C_LD);
+            sop[idx] = rop[(size_t)offs[c0 + kk] * (LP * M2C_LD) + (idx - kk * (LP * M2C_LD))];
         }
-        sO[idx] = v;
-    }
-    for (int idx = threadIdx.x; idx < LPH * LP; idx += blockDim.x) {
-        const int o = idx / LP, nm = idx % LP;
-        int j, k;
-        out_jk(o, j, k);
-        const int nn = nm < 1 ? 0 : nm < 4 ? 1 : nm < 9 ? 2 : nm < 16 ? 3 : 4;
-        const int m = nm - nn * (nn + 1);
-        const int ll = j + nn, q = m - k;
-        const R c = cf[idx];
-        sh[idx] = ll * (ll + 1) / 2 + (q < 0 ? -q : q);
-        scr[idx] = c;
-        sci[idx] = q < 0 ? -c : c;
-    }
-    __syncthreads();
-    const int o = threadIdx.x % LPH, g = threadIdx.x / LPH;
-    R are[8], aim[8];
+        __syncthreads();
+        for (int kk = 0; kk < nch; kk++) {
+            const int oi = offs[c0 + kk];
+            const int ex = px + oi % 7 - 3, ey = py + (oi / 7) % 7 - 3, ez = pz + oi / 49 - 3;
+            const int q = (ex & 1) + 2 * (ey & 1) + 4 * (ez & 1);
+            const R *src = pk + (size_t)q * LP * vol + ((ez >> 1) * p1 + (ey >> 1)) * p0 + (ex >> 1);
+            const R *op = sop + kk * LP * M2C_LD;
 #pragma unroll
-    for (int t = 0; t < 8; t++) are[t] = aim[t] = R(0);
-    for (int oi = g; oi < 343; oi += M2L_G) {
-        const int dx = oi % 7 - 3, dy = (oi / 7) % 7 - 3, dz = oi / 49 - 3;
-        if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-        const C2<R> *H = Htab + (size_t)oi * NH;
-        R t1[LP], t2[LP];
-#pragma unroll
-        for (int nm = 0; nm < LP; nm++) {
-            const C2<R> hv = H[sh[o * LP + nm]];
-            t1[nm] = scr[o * LP + nm] * hv.x;
-            t2[nm] = sci[o * LP + nm] * hv.y;
-        }
-#pragma unroll
-        for (int t = 0; t < 8; t++) {
-            // child t sits at window position 2 + (t bits) per axis
-            const int sx = 2 + (t & 1) + dx, sy = 2 + ((t >> 1) & 1) + dy, sz = 2 + ((t >> 2) & 1) + dz;
-            if (sx < 0 || sy < 0 || sz < 0 || sx > 5 || sy > 5 || sz > 5) continue;
-            const int gx = w0[0] + sx, gy = w0[1] + sy, gz = w0[2] + sz;
-            if (gx < 0 || gy < 0 || gz < 0 || gx >= n[0] || gy >= n[1] || gz >= n[2]) continue;
-            const C2<R> *src = sO + (size_t)(sx + 6 * (sy + 6 * sz)) * LP;
-            R re = are[t], im = aim[t];
-#pragma unroll
-            for (int nm = 0; nm < LP; nm++) {
-                const C2<R> mv = src[nm];
-                re += t1[nm] * mv.x - t2[nm] * mv.y;
-                im += t1[nm] * mv.y + t2[nm] * mv.x;
-            }
-            are[t] = re;
-            aim[t] = im;
+            for (int i = 0; i < LP; i++) m2c_row(op + i * M2C_LD, src[(size_t)i * vol + ia], src[(size_t)i * vol + ib], aa, ab);
         }
     }
+    R *part = (R *)(level == 4 ? d.part4 : d.part3);
+    const int ncl = level == 4 ? ncell : n3;
+    const int base = level == 4 ? r.cell0 : r.l3_0, n0 = 2 * h0, n1 = 2 * h1;
+    auto cell = [&](int t) {
+        const int x = t % h0, y = (t / h0) % h1, z = t / (h0 * h1);
+        return base + (2 * x + px) + n0 * ((2 * y + py) + n1 * (2 * z + pz));
+    };
+    if (ta <= last) {
+        const int cg = cell(ta);
 #pragma unroll
-    for (int t = 0; t < 8; t++) {
-        sre[(g * 8 + t) * LPH + o] = are[t];
-        sim[(g * 8 + t) * LPH + o] = aim[t];
+        for (int i = 0; i < LP; i++) part[((size_t)g * LP + i) * ncl + cg] = aa[i];
     }
-    __syncthreads();
-    if (threadIdx.x < 8 * LPH) {
-        const int t = threadIdx.x / LPH, oo = threadIdx.x % LPH;
-        R a = 0, b = 0;
-        for (int q = 0; q < M2L_G; q++) { a += sre[(q * 8 + t) * LPH + oo]; b += sim[(q * 8 + t) * LPH + oo]; }
-        const int gc[3] = {w0[0] + 2 + (t & 1), w0[1] + 2 + ((t >> 1) & 1), w0[2] + 2 + ((t >> 2) & 1)};
-        const int child = base + gc[0] + n[0] * (gc[1] + n[1] * gc[2]);
-        store_jk(L + (size_t)child * LP, oo, (double)a, (double)b, true);
+    if (tb <= last) {
+        const int cg = cell(tb);
+#pragma unroll
+        for (int i = 0; i < LP; i++) part[((size_t)g * LP + i) * ncl + cg] = ab[i];
     }
 }
 
 // M2L at L2 over all non-adjacent L2 boxes of the replica (src/computeLjk2.f90:17-72):
-// one CTA per target box, 15 outputs x 8 source groups, reduced in a fixed order
+// one CTA per target box; each half-warp takes every 16th of the replica's
+// boxes as sources (one at a time, the same for its lanes), lane o < 15 the
+// output o; the 16 half-warps' sums are added in a fixed order
 template <typename R>
-__global__ void __launch_bounds__(128) k_m2l_all(Dev d, const C2<R> *Htab, const R *cf, int d2) {
+__global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const R *cf, int d2) {
     __shared__ R scf[LPH * LP];
-    __shared__ R sre[8][LPH], sim[8][LPH];
+    __shared__ R sre[16][LPH], sim[16][LPH];
     const int b = blockIdx.x;
     const Rep r = d.rep[d.b2rep[b]];
     const int *n = r.nr;
@@ -956,66 +992,55 @@ __global__ void __launch_bounds__(128) k_m2l_all(Dev d, const C2<R> *Htab, const
     const int t[3] = {l % n[0], (l / n[0]) % n[1], l / (n[0] * n[1])};
     for (int idx = threadIdx.x; idx < LPH * LP; idx += blockDim.x) scf[idx] = cf[idx];
     __syncthreads();
-    const int o = threadIdx.x % LPH, g = threadIdx.x / LPH;
-    const bool act = threadIdx.x < 8 * LPH;
+    const int hw = threadIdx.x >> 4, o = threadIdx.x & 15;
+    int h[LP];
+    R cr[LP], ci[LP];
+    m2l_terms<R>(o < LPH ? o : LPH - 1, scf, h, cr, ci);
+    const int w = 2 * d2 + 1, nb = n[0] * n[1] * n[2];
     R re = 0, im = 0;
-    if (act) {
-        int h[LP];
-        R cr[LP], ci[LP];
-        m2l_terms<R>(o, scf, h, cr, ci);
-        const int w = 2 * d2 + 1;
-        int k = 0;
-        for (int sz = 0; sz < n[2]; sz++)
-            for (int sy = 0; sy < n[1]; sy++)
-                for (int sx = 0; sx < n[0]; sx++) {
-                    const int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
-                    if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-                    if ((k++ & 7) != g) continue;
-                    const int oi = (dx + d2) + w * ((dy + d2) + w * (dz + d2));
-                    m2l_acc<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + sx + n[0] * (sy + n[1] * sz)) * LP, h,
-                               cr, ci, re, im);
-                }
+    for (int s = hw; s < nb; s += 16) {
+        const int sx = s % n[0], sy = (s / n[0]) % n[1], sz = s / (n[0] * n[1]);
+        const int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
+        if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+        const int oi = (dx + d2) + w * ((dy + d2) + w * (dz + d2));
+        m2l_acc<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, h, cr, ci, re, im);
     }
-    if (act) { sre[g][o] = re; sim[g][o] = im; }
+    if (o < LPH) { sre[hw][o] = re; sim[hw][o] = im; }
     __syncthreads();
-    if (g == 0 && act) {
+    if (threadIdx.x < LPH) {
         R a = 0, c = 0;
-        for (int q = 0; q < 8; q++) { a += sre[q][o]; c += sim[q][o]; }
-        store_jk(d.L2 + (size_t)b * LP, o, (double)a, (double)c, false);
+        for (int q = 0; q < 16; q++) { a += sre[q][threadIdx.x]; c += sim[q][threadIdx.x]; }
+        store_jk(d.L2 + (size_t)b * LP, threadIdx.x, (double)a, (double)c, false);
     }
 }
 
-// opt-in shared-memory sizes; called once per context creation (the
-// attribute is per device, so every context sets it for its own device)
-void init_force_kernels() {
-    cudaFuncSetAttribute(k_m2l_win<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<double>());
-    cudaFuncSetAttribute(k_m2l_win<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m2l_smem<float>());
+// opt-in shared-memory sizes, called once per context creation; every
+// force kernel now fits the default 48 KB
+void init_force_kernels() {}
+
+template <typename R>
+size_t m2c_smem() { return sizeof(R) * M2C_CH * LP * M2C_LD; }
+
+template <typename R, typename OP>
+void fma_build(const Dev &d, int ncell, int n3, int n2, int d2, const OP *m43, const OP *m32, const OP *l23,
+               const OP *l34, const C2<R> *h2, const R *cf, cudaStream_t st) {
+    k_p2m<R><<<ncell, 64, 0, st>>>(d);
+    k_m2m<R><<<n3, 128, 0, st>>>(d, d.O4, d.O3, m43, d.b3rep, 3);
+    k_m2m<R><<<n2, 128, 0, st>>>(d, d.O3, d.O2, m32, d.b2rep, 2);
+    k_m2l_pack<R><<<((ncell + n3) * LP + 255) / 256, 256, 0, st>>>(d, ncell, n3);
+    k_m2l_cls<R><<<dim3(d.m2c_nitems, d.m2c_groups), 32 * M2C_W, m2c_smem<R>(), st>>>(d, ncell, n3);
+    k_m2l_all<R><<<n2, 256, 0, st>>>(d, h2, cf, d2);
+    k_l2l<R><<<n3, 32, 0, st>>>(d, d.L2, d.L3, l23, d.b3rep, 3, (const R *)d.part3, d.m2c_groups, n3);
+    k_l2l<R><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, l34, d.crep, 4, (const R *)d.part4, d.m2c_groups, ncell);
 }
 
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {
-    if (mixed) {
-        k_p2m<float><<<ncell, 64, 0, st>>>(d);
-        k_m2m<float><<<n3, 128, 0, st>>>(d, d.O4, d.O3, d.op32_m2m43, d.b3rep, 3);
-        k_m2m<float><<<n2, 128, 0, st>>>(d, d.O3, d.O2, d.op32_m2m32, d.b2rep, 2);
-        k_m2l_all<float><<<n2, 128, 0, st>>>(d, (const C2<float> *)d.h32_m2l2, d.m2l_cf32, d2);
-        k_l2l<float><<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op32_l2l23, d.b3rep, 3);
-        k_m2l_win<float><<<n2, M2L_THREADS, m2l_smem<float>(), st>>>(
-            d, d.O3, d.L3, (const C2<float> *)d.h32_m2l3, d.m2l_cf32, d.b2rep, 3);
-        k_l2l<float><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op32_l2l34, d.crep, 4);
-        k_m2l_win<float><<<n3, M2L_THREADS, m2l_smem<float>(), st>>>(
-            d, d.O4, d.L4, (const C2<float> *)d.h32_m2l4, d.m2l_cf32, d.b3rep, 4);
-    } else {
-        k_p2m<double><<<ncell, 64, 0, st>>>(d);
-        k_m2m<double><<<n3, 128, 0, st>>>(d, d.O4, d.O3, d.op_m2m43, d.b3rep, 3);
-        k_m2m<double><<<n2, 128, 0, st>>>(d, d.O3, d.O2, d.op_m2m32, d.b2rep, 2);
-        k_m2l_all<double><<<n2, 128, 0, st>>>(d, (const C2<double> *)d.h_m2l2, d.m2l_cf, d2);
-        k_l2l<double><<<n3, 32, 0, st>>>(d, d.L2, d.L3, d.op_l2l23, d.b3rep, 3);
-        k_m2l_win<double><<<n2, M2L_THREADS, m2l_smem<double>(), st>>>(
-            d, d.O3, d.L3, (const C2<double> *)d.h_m2l3, d.m2l_cf, d.b2rep, 3);
-        k_l2l<double><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, d.op_l2l34, d.crep, 4);
-        k_m2l_win<double><<<n3, M2L_THREADS, m2l_smem<double>(), st>>>(
-            d, d.O4, d.L4, (const C2<double> *)d.h_m2l4, d.m2l_cf, d.b3rep, 4);
-    }
+    if (mixed)
+        fma_build<float>(d, ncell, n3, n2, d2, d.op32_m2m43, d.op32_m2m32, d.op32_l2l23, d.op32_l2l34,
+                         (const C2<float> *)d.h32_m2l2, d.m2l_cf32, st);
+    else
+        fma_build<double>(d, ncell, n3, n2, d2, d.op_m2m43, d.op_m2m32, d.op_l2l23, d.op_l2l34,
+                          (const C2<double> *)d.h_m2l2, d.m2l_cf, st);
 }
 
 // ------------------------------------------------------------------ per-site terms

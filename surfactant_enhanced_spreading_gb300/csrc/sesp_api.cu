@@ -257,6 +257,44 @@ void m2l_coef(double *cf) {
                     cf[oidx(j, k) * LP + cidx(n, m)] =
                         iIkm2(k, m) * rAnm(j, k) * rAnm(n, m) / (sgn(n) * rAnm(j + n, m - k));
 }
+// Real form of the M2L operator at one offset (h: its 45 H_l^q).  With
+// O_n^-m = conj(O_n^m) the complex 15 x 25 operator T acts on the 25 real
+// components of a multipole and gives the 25 real components of the local
+// expansion (Im L_j^0 vanishes and is dropped): for m > 0, with
+// T = T[(j,k),(n,m)] and T' = T[(j,k),(n,-m)],
+//   Re L += (Re T + Re T') Re O + (Im T' - Im T) Im O,
+//   Im L += (Im T + Im T') Re O + (Re T - Re T') Im O.
+// rop is [input 25][output, padded to M2C_LD].
+void m2l_real(const double *cf, const double2 *h, double *rop) {
+    for (int i = 0; i < LP * M2C_LD; i++) rop[i] = 0.0;
+    auto op = [&](int j, int k, int n, int m) {
+        const int l = j + n, q = m - k;
+        const double c = cf[oidx(j, k) * LP + cidx(n, m)];
+        const double2 hv = h[l * (l + 1) / 2 + abs(q)];
+        return make_double2(c * hv.x, (q < 0 ? -c : c) * hv.y);
+    };
+    for (int j = 0; j <= P; j++)
+        for (int k = 0; k <= j; k++) {
+            const int ore = oidx(j, k), oim = k > 0 ? LPH + ore - (j + 1) : -1;
+            for (int n = 0; n <= P; n++)
+                for (int m = 0; m <= n; m++) {
+                    const int ire = oidx(n, m), iim = m > 0 ? LPH + ire - (n + 1) : -1;
+                    const double2 t = op(j, k, n, m);
+                    if (m == 0) {
+                        rop[ire * M2C_LD + ore] += t.x;
+                        if (oim >= 0) rop[ire * M2C_LD + oim] += t.y;
+                        continue;
+                    }
+                    const double2 u = op(j, k, n, -m);
+                    rop[ire * M2C_LD + ore] += t.x + u.x;
+                    rop[iim * M2C_LD + ore] += u.y - t.y;
+                    if (oim >= 0) {
+                        rop[ire * M2C_LD + oim] += t.y + u.y;
+                        rop[iim * M2C_LD + oim] += t.x - u.x;
+                    }
+                }
+        }
+}
 // M2M operator at child - parent vector d, src/computeOnm3.f90:51-81
 void op_m2m(double x, double y, double z, double2 *op) {
     double rho, al, be;
@@ -560,6 +598,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     const int R = (int)in.size();
     c->reps.assign(R, Rep());
     int nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, naxis = 0, ncol = 0, nwm = 0, nsm = 0, d2 = 1;
+    size_t npk4 = 0, npk3 = 0;
     for (int q = 0; q < R; q++) {
         const RepIn &ri = in[q];
         Rep &r = c->reps[q];
@@ -584,6 +623,10 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         r.pnh1 = DT / df / c->p.tr / (rlx * rlx);
         r.pnh2 = -2.0 * df * c->p.tr;
         r.site0 = nsite; r.mol0 = nmol; r.cell0 = ncell; r.l3_0 = n3; r.l2_0 = n2; r.axis0 = naxis; r.gcol0 = ncol;
+        r.pk4 = (int)npk4; r.pk3 = (int)npk3;
+        npk4 += (size_t)8 * LP * (r.nc[0] / 2 + 4) * (r.nc[1] / 2 + 4) * (r.nc[2] / 2 + 4);
+        npk3 += (size_t)8 * LP * (r.nc[0] / 4 + 4) * (r.nc[1] / 4 + 4) * (r.nc[2] / 4 + 4);
+        if (npk4 >= (1u << 31)) return fail(SESP_EINVAL, "too many cells");
         int cc = r.nc[0] * r.nc[1] * r.nc[2];
         nsite += r.nsite; nmol += r.nmol; ncell += cc; n3 += cc / 8; n2 += cc / 64;
         naxis += r.nc[0] + r.nc[1] + r.nc[2]; ncol += r.nc[0] * r.nc[1];
@@ -626,9 +669,54 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         return e;
     int w2 = 2 * d2 + 1;
     const size_t nh2 = (size_t)w2 * w2 * w2 * NHARM;
-    if ((e = dalloc(c, &d.h_m2l4, (size_t)343 * NHARM)) || (e = dalloc(c, &d.h_m2l3, (size_t)343 * NHARM)) ||
-        (e = dalloc(c, &d.h_m2l2, nh2)) || (e = dalloc(c, &d.h32_m2l4, (size_t)343 * NHARM)) ||
-        (e = dalloc(c, &d.h32_m2l3, (size_t)343 * NHARM)) || (e = dalloc(c, &d.h32_m2l2, nh2)) ||
+    // real-form M2L at L4 and L3: work items of M2C_TILE targets of one parity
+    // class, each split into m2c_groups offset groups (about 8 CTAs per SM)
+    const int mixed = c->p.precision != SESP_PLAIN_FP64;
+    const size_t rsz = mixed ? sizeof(float) : sizeof(double);
+    std::vector<int4> m2c_items;
+    for (int lev = 4; lev >= 3; lev--)
+        for (int q = 0; q < R; q++) {
+            const Rep &r = c->reps[q];
+            const int div = lev == 4 ? 2 : 4;
+            const int ncls = (r.nc[0] / div) * (r.nc[1] / div) * (r.nc[2] / div);
+            for (int cls = 0; cls < 8; cls++)
+                for (int t0 = 0; t0 < ncls; t0 += M2C_TILE)
+                    m2c_items.push_back(make_int4(lev << 28 | q, cls, t0, std::min(M2C_TILE, ncls - t0)));
+        }
+    d.m2c_nitems = (int)m2c_items.size();
+    d.m2c_groups = std::max(1, std::min(24, (8 * c->n_sm + d.m2c_nitems - 1) / d.m2c_nitems));
+    {
+        char *p4 = nullptr, *p3 = nullptr, *q4 = nullptr, *q3 = nullptr, *o4 = nullptr, *o3 = nullptr;
+        if ((e = dalloc(c, &o4, (size_t)343 * LP * M2C_LD * rsz)) || (e = dalloc(c, &o3, (size_t)343 * LP * M2C_LD * rsz)) ||
+            (e = dalloc(c, &p4, npk4 * rsz)) || (e = dalloc(c, &p3, npk3 * rsz)) ||
+            (e = dalloc(c, &q4, (size_t)d.m2c_groups * LP * C * rsz)) ||
+            (e = dalloc(c, &q3, (size_t)d.m2c_groups * LP * n3 * rsz)) ||
+            (e = dalloc(c, &d.m2c_items, m2c_items.size())) || (e = dalloc(c, &d.m2c_off, (size_t)8 * M2C_NOFF)))
+            return e;
+        d.rop4 = o4; d.rop3 = o3; d.pk4 = p4; d.pk3 = p3; d.part4 = q4; d.part3 = q3;
+    }
+    CK(cudaMemcpyAsync(d.m2c_items, m2c_items.data(), m2c_items.size() * sizeof(int4), cudaMemcpyHostToDevice, c->st));
+    {
+        // per parity class (bit a: odd cell index on axis a) the offsets of
+        // the children of the parent's neighbours that are not adjacent
+        std::vector<int> off;
+        for (int cls = 0; cls < 8; cls++)
+            for (int dz = -3; dz <= 3; dz++)
+                for (int dy = -3; dy <= 3; dy++)
+                    for (int dx = -3; dx <= 3; dx++) {
+                        const int dd[3] = {dx, dy, dz};
+                        bool ok = !(abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1);
+                        for (int a = 0; a < 3; a++) {
+                            const int par = (cls >> a) & 1;
+                            ok = ok && dd[a] >= -2 - par && dd[a] <= 3 - par;
+                        }
+                        if (ok) off.push_back((dx + 3) + 7 * (dy + 3) + 49 * (dz + 3));
+                    }
+        if (off.size() != (size_t)8 * M2C_NOFF) return fail(SESP_EINVAL, "M2L offset lists");
+        CK(cudaMemcpyAsync(d.m2c_off, off.data(), off.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+    }
+    if ((e = dalloc(c, &d.h_m2l2, nh2)) || (e = dalloc(c, &d.h32_m2l2, nh2)) ||
         (e = dalloc(c, &d.m2l_cf, (size_t)LPH * LP)) || (e = dalloc(c, &d.m2l_cf32, (size_t)LPH * LP)) ||
         (e = dalloc(c, &d.op_m2m43, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_m2m32, (size_t)8 * LPH * LP)) ||
         (e = dalloc(c, &d.op_l2l23, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op_l2l34, (size_t)8 * LPH * LP)) ||
@@ -738,18 +826,31 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         CK(cudaStreamSynchronize(c->st));
         return 0;
     };
-    auto fill_win = [&](double scale, double2 *dst, float2 *dst32) -> int {
-        std::vector<double2> h((size_t)343 * NHARM, make_double2(0.0, 0.0));
+    std::vector<double> cf(LPH * LP);
+    m2l_coef(cf.data());
+    // real-form operators of the 7^3 offsets at L4 (cell edge rs) and L3 (2 rs)
+    auto fill_win = [&](double scale, void *dst) -> int {
+        std::vector<double> rop((size_t)343 * LP * M2C_LD, 0.0);
+        double2 h[NHARM];
         for (int dz = -3; dz <= 3; dz++)
             for (int dy = -3; dy <= 3; dy++)
                 for (int dx = -3; dx <= 3; dx++) {
                     if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
                     const int oi = (dx + 3) + 7 * (dy + 3) + 49 * (dz + 3);
-                    harm_m2l(dx * scale, dy * scale, dz * scale, &h[(size_t)oi * NHARM]);
+                    harm_m2l(dx * scale, dy * scale, dz * scale, h);
+                    m2l_real(cf.data(), h, &rop[(size_t)oi * LP * M2C_LD]);
                 }
-        return put(h, dst, dst32);
+        if (mixed) {
+            std::vector<float> r32(rop.begin(), rop.end());
+            CK(cudaMemcpyAsync(dst, r32.data(), r32.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));
+            CK(cudaStreamSynchronize(c->st));
+        } else {
+            CK(cudaMemcpyAsync(dst, rop.data(), rop.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+            CK(cudaStreamSynchronize(c->st));
+        }
+        return 0;
     };
-    if ((e = fill_win(RS, d.h_m2l4, d.h32_m2l4)) || (e = fill_win(2 * RS, d.h_m2l3, d.h32_m2l3))) return e;
+    if ((e = fill_win(RS, d.rop4)) || (e = fill_win(2 * RS, d.rop3))) return e;
     {
         std::vector<double2> h(nh2, make_double2(0.0, 0.0));
         for (int dz = -d2; dz <= d2; dz++)
@@ -760,9 +861,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
                     harm_m2l(dx * 4 * RS, dy * 4 * RS, dz * 4 * RS, &h[(size_t)oi * NHARM]);
                 }
         if ((e = put(h, d.h_m2l2, d.h32_m2l2))) return e;
-        std::vector<double> cf(LPH * LP);
         std::vector<float> cf32(LPH * LP);
-        m2l_coef(cf.data());
         for (int i = 0; i < LPH * LP; i++) cf32[i] = (float)cf[i];
         CK(cudaMemcpyAsync(d.m2l_cf, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
         CK(cudaMemcpyAsync(d.m2l_cf32, cf32.data(), cf32.size() * sizeof(float), cudaMemcpyHostToDevice, c->st));

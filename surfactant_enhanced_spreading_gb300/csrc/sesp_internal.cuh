@@ -41,6 +41,10 @@ constexpr double XPI = (double)675.05f;
 constexpr double DT = 0.00127362;
 constexpr double DTSQ2 = 0.00127362 * 0.00127362 / 2.0;
 
+constexpr int M2C_NOFF = 189; // M2L offsets of a cell (6^3 - 3^3 for its parity class)
+constexpr int M2C_LD = 28;    // padded output stride of a real M2L operator row
+constexpr int M2C_W = 2;      // warps of an M2L CTA, 64 targets each (2 per lane)
+constexpr int M2C_TILE = 64 * M2C_W;
 constexpr int GGRP = 8;       // carbon groups per graphite column
 constexpr int GBIN = 32;      // y bins per group
 // y extent of a column's carbons about its centre: rc + half the L4 cell diagonal
@@ -57,7 +61,7 @@ struct Rep {
     int axis0;        // offset of this replica's cell-centre tables (x, then y, then z)
     int gcol0;        // first bottom-layer column of the carbon lists
     int graphite_on;
-    int pad0, pad;
+    int pk4, pk3;     // first element of this replica's class-packed L4 / L3 multipoles
     double rhs[3], rsd[3];
     double pnh1, pnh2;
 };
@@ -133,12 +137,26 @@ struct Dev {
     double2 *O4, *L4, *O3, *L3, *O2, *L2;
     double2 *op_m2m43, *op_m2m32, *op_l2l23, *op_l2l34;
     float2 *op32_m2m43, *op32_m2m32, *op32_l2l23, *op32_l2l34;   // FP32 copies for the mixed path
-    // M2L factors: H_l^q of every offset (45 per offset; L4 and L3 7^3 offsets,
-    // L2 (2 d2 + 1)^3) and the offset-independent coefficients (15 x 25)
-    double2 *h_m2l4, *h_m2l3, *h_m2l2;
-    float2 *h32_m2l4, *h32_m2l3, *h32_m2l2;   // FP32 copies for the mixed path
+    // L2 M2L factors: H_l^q of every offset (45 per offset, (2 d2 + 1)^3
+    // offsets) and the offset-independent coefficients (15 x 25)
+    double2 *h_m2l2;
+    float2 *h32_m2l2;    // FP32 copy for the mixed path
     double *m2l_cf;
     float *m2l_cf32;
+    // L4 and L3 M2L in real form.  A multipole or local expansion is carried
+    // as 25 reals: Re X_n^m for m >= 0 (index n(n+1)/2 + m), then Im X_n^m for
+    // m > 0 (index 15 + n(n-1)/2 + m - 1); X_n^-m = conj(X_n^m) supplies the
+    // rest.  Per offset (dx + 3) + 7 (dy + 3) + 49 (dz + 3) a real operator
+    // [input 25][output, padded to M2C_LD] (FP64 or FP32 by precision).
+    void *rop4, *rop3;
+    // multipoles of each replica repacked per parity class of its cells:
+    // [class 8][component 25][class grid with a zero margin of 2 per side]
+    void *pk4, *pk3;
+    // partial sums per offset group: [group][component 25][cells of the level]
+    void *part4, *part3;
+    int4 *m2c_items;     // work items: (level << 28 | replica, class, first target, targets)
+    int *m2c_off;        // per class its 189 offsets, (dx + 3) + 7 (dy + 3) + 49 (dz + 3)
+    int m2c_nitems, m2c_groups;
     // LJ pair table (eps, sg6), NTYPE^2
     double2 *ljt;
     float2 *ljt32;       // FP32 copy of ljt
