@@ -13,30 +13,43 @@ void upload_tables_exact(const Tables &t, cudaStream_t st) {
     cudaMemcpyToSymbolAsync(cT, &t, sizeof(Tables), 0, cudaMemcpyHostToDevice, st);
 }
 
+constexpr double IRS = 1.0 / RS;
+
+// (int)(q / s) rounded as the reference divides, from q * (1 / s): with
+// |q / s| below 1e6 the product and the rounded quotient differ by less
+// than 1e-9, so they truncate alike unless the product lies within 1e-9 of
+// an integer, where the division itself decides
+__device__ inline int trunc_div(double q, double s, double inv_s) {
+    const double t = q * inv_s;
+    if (fabs(t - rint(t)) > 1e-9) return (int)t;
+    return (int)(q / s);
+}
 // ibox2 - 1 along one axis, src/ibox.f90:127-139
 __device__ inline int rank_axis(const Rep &r, int a, double v) {
-    int k = (int)((v + r.rhs[a]) * r.nr[a] / r.rsd[a]);
+    int k = trunc_div((v + r.rhs[a]) * r.nr[a], r.rsd[a], r.irsd[a]);
     return k < 0 ? 0 : (k >= r.nr[a] ? r.nr[a] - 1 : k);
 }
-// rcen2xtmp, src/init_box_dimensions.f90:40-42
-__device__ inline double rcen2_axis(const Rep &r, int a, int rk) {
-    double b = (double)r.nr[a];
-    return r.rsd[a] * (rk + 1) / b - r.rhs[a] - r.rsd[a] / b / 2.0;
+// rcen2xtmp, src/init_box_dimensions.f90:40-42, tabulated at upload per
+// replica, axis and rank (rsd (rk + 1) / nr - rhs - rsd / nr / 2)
+__device__ inline double rcen2_axis(const Dev &d, const Rep &r, int a, int rk) {
+    const double *t = d.rcen2 + r.axis0 / 4;
+    return t[(a > 0 ? r.nr[0] : 0) + (a > 1 ? r.nr[1] : 0) + rk];
 }
 // ibox64 along one axis relative to a rank centre, src/ibox.f90:172-186
 __device__ inline int local_axis(double v, double c2) {
-    int k = (int)((v - c2 + 2.0 * RS) / RS);
+    int k = trunc_div(v - c2 + 2.0 * RS, RS, IRS);
     return k < 0 ? 0 : (k > 3 ? 3 : k);
 }
 // global key-cell coordinate along one axis (rank by ibox2, cell by ibox64)
-__device__ inline int key_axis(const Rep &r, int a, double v, int *rk) {
+__device__ inline int key_axis(const Dev &d, const Rep &r, int a, double v, int *rk) {
     *rk = rank_axis(r, a, v);
-    return 4 * (*rk) + local_axis(v, rcen2_axis(r, a, *rk));
+    return 4 * (*rk) + local_axis(v, rcen2_axis(d, r, a, *rk));
 }
 // isCentral along one axis (src/ibox.f90:101-124): the cell whose
-// [centre - rs/2, centre + rs/2) holds v, -1 if none
+// [centre - rs/2, centre + rs/2) holds v, -1 if none (the product only
+// picks the three candidates; the comparisons decide)
 __device__ inline int central_axis(const double *cen, int n, double v, double rhs) {
-    int k0 = (int)floor((v + rhs) / RS);
+    int k0 = (int)floor((v + rhs) * IRS);
     const double rs2 = RS / 2.0;
     for (int k = k0 - 1; k <= k0 + 1; k++) {
         if (k < 0 || k >= n) continue;
@@ -46,50 +59,61 @@ __device__ inline int central_axis(const double *cen, int n, double v, double rh
     return -1;
 }
 
+// the cell a site is Central in, or -1
+__device__ inline int central_cell(const Dev &d, const Rep &r, int g) {
+    const double *cx = d.axis + r.axis0;
+    const double *cy = cx + r.nc[0];
+    const double *cz = cy + r.nc[1];
+    int ix = central_axis(cx, r.nc[0], d.x[g], r.rhs[0]);
+    int iy = central_axis(cy, r.nc[1], d.y[g], r.rhs[1]);
+    int iz = central_axis(cz, r.nc[2], d.z[g], r.rhs[2]);
+    return (ix < 0 || iy < 0 || iz < 0) ? -1 : cell_index(r, ix, iy, iz);
+}
+
 // Re-key molecules (src/read_config.f90:44-175 and the delete/add pairs
 // src/delete_w1.f90:54-195, src/delete_s.f90:33-43; key site O for water,
 // 14 for surfactants) and locate every site in the cell it is Central in.
 // A w1 water (all three sites in one rank and one ibox64 cell) has its
 // sites located in its key cell, as the reference stores it there.
-__global__ void k_locate(Dev d, int nmol) {
-    int m = blockIdx.x * blockDim.x + threadIdx.x;
-    if (m >= nmol) return;
+// Threads [0, nmol) take one molecule each (a water with its sites);
+// threads [nmol, nmol + nss) one surfactant site each.
+__global__ void k_locate(Dev d, int nmol, const int *smols, int nss) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nmol) {
+        if (t - nmol >= nss) return;
+        const int m = smols[(t - nmol) / NSURF], g = d.mfirst[m] + (t - nmol) % NSURF;
+        const int loc = central_cell(d, d.rep[d.mrep[m]], g);
+        d.sloc[g] = loc;
+        if (loc >= 0) atomicAdd(&d.ccount[loc], 1);
+        else atomicAdd(&d.counters[2], 1ull);
+        return;
+    }
+    const int m = t;
     const Rep r = d.rep[d.mrep[m]];
     int g0 = d.mfirst[m];
     int kind = d.mkind[m];
     int ks = kind == 0 ? g0 : g0 + 13;
     double p[3] = {d.x[ks], d.y[ks], d.z[ks]};
     int rk[3], kc[3];
-    for (int a = 0; a < 3; a++) kc[a] = key_axis(r, a, p[a], &rk[a]);
+    for (int a = 0; a < 3; a++) kc[a] = key_axis(d, r, a, p[a], &rk[a]);
     int key = cell_index(r, kc[0], kc[1], kc[2]);
     d.mkey[m] = key;
-    int w1 = 0;
-    if (kind == 0) {
-        w1 = 1;
-        for (int t = 1; t < 3; t++) {
-            double q[3] = {d.x[g0 + t], d.y[g0 + t], d.z[g0 + t]};
-            for (int a = 0; a < 3; a++) {
-                if (rank_axis(r, a, q[a]) != rk[a]) w1 = 0;
-                else if (4 * rk[a] + local_axis(q[a], rcen2_axis(r, a, rk[a])) != kc[a]) w1 = 0;
-            }
+    if (kind != 0) {
+        d.mw1[m] = 0;
+        return;
+    }
+    int w1 = 1;
+    for (int s = 1; s < 3; s++) {
+        double q[3] = {d.x[g0 + s], d.y[g0 + s], d.z[g0 + s]};
+        for (int a = 0; a < 3; a++) {
+            if (rank_axis(r, a, q[a]) != rk[a]) w1 = 0;
+            else if (4 * rk[a] + local_axis(q[a], rcen2_axis(d, r, a, rk[a])) != kc[a]) w1 = 0;
         }
     }
     d.mw1[m] = w1;
-    int ns = kind == 0 ? 3 : NSURF;
-    const double *cx = d.axis + r.axis0;
-    const double *cy = cx + r.nc[0];
-    const double *cz = cy + r.nc[1];
-    for (int t = 0; t < ns; t++) {
-        int g = g0 + t;
-        int loc;
-        if (w1) {
-            loc = key;
-        } else {
-            int ix = central_axis(cx, r.nc[0], d.x[g], r.rhs[0]);
-            int iy = central_axis(cy, r.nc[1], d.y[g], r.rhs[1]);
-            int iz = central_axis(cz, r.nc[2], d.z[g], r.rhs[2]);
-            loc = (ix < 0 || iy < 0 || iz < 0) ? -1 : cell_index(r, ix, iy, iz);
-        }
+    for (int s = 0; s < 3; s++) {
+        const int g = g0 + s;
+        const int loc = w1 ? key : central_cell(d, r, g);
         d.sloc[g] = loc;
         if (loc >= 0) atomicAdd(&d.ccount[loc], 1);
         else atomicAdd(&d.counters[2], 1ull);
@@ -112,8 +136,8 @@ __global__ void k_isub(Dev d, int nsurf_sites, const int *surf_mol_of) {
     double pm[3] = {d.x[g0 + j], d.y[g0 + j], d.z[g0 + j]};
     double cen[3];
     for (int a = 0; a < 3; a++) {
-        double c2 = rcen2_axis(r, a, kc[a] / 4);
-        int li = (int)((pm[a] - c2 + 5.0 * RS) / RS) + 1;
+        double c2 = rcen2_axis(d, r, a, kc[a] / 4);
+        int li = trunc_div(pm[a] - c2 + 5.0 * RS, RS, IRS) + 1;
         cen[a] = 10.0 * RS * li / 10.0 - 10.0 * RS / 2.0 - 10.0 * RS / 20.0 + c2;
     }
     const double r15 = 1.5 * RS;
@@ -453,11 +477,11 @@ __global__ void k_init_accel(Dev d, int nsite) {
 
 // ---------------------------------------------------------------- launchers
 
-void launch_locate(const Dev &d, int nmol, cudaStream_t st) {
-    k_locate<<<(nmol + 127) / 128, 128, 0, st>>>(d, nmol);
+void launch_locate(const Dev &d, int nmol, const int *smols, int nsurf_sites, cudaStream_t st) {
+    k_locate<<<(nmol + nsurf_sites + 127) / 128, 128, 0, st>>>(d, nmol, smols, nsurf_sites);
 }
 void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st) {
-    if (nsurf_sites) k_isub<<<(nsurf_sites + 127) / 128, 128, 0, st>>>(d, nsurf_sites, surf_mols);
+    if (nsurf_sites) k_isub<<<(nsurf_sites + 31) / 32, 32, 0, st>>>(d, nsurf_sites, surf_mols);
 }
 // fast = 0 (plain path): the FP64 sweeps above, dividing exactly as the
 // reference does; fast = 1 / 2 (mixed paths): the FP64 / FP32 sweeps of

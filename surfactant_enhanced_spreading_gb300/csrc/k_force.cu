@@ -33,21 +33,41 @@ __device__ inline void cell_xyz(const Rep &r, int c, int &ix, int &iy, int &iz) 
 
 // ------------------------------------------------------------------ sort
 
+// exclusive prefix sum over one block (blockDim.x a multiple of 32, at most
+// 1024): warp shuffles, then the warps' totals; *total gets the block's sum
+__device__ inline int block_exscan(int v, int *total) {
+    __shared__ int ws[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int t = lane < nw ? ws[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        ws[lane] = t;
+    }
+    __syncthreads();
+    const int res = (w ? ws[w - 1] : 0) + x - v;
+    *total = ws[nw - 1];
+    __syncthreads();
+    return res;
+}
+
 __global__ void k_scan(Dev d, int ncell) {
-    __shared__ int part[1024];
     int per = (ncell + blockDim.x - 1) / blockDim.x;
     int b = threadIdx.x * per, e = min(ncell, b + per);
     int s = 0;
     for (int c = b; c < e; c++) s += d.ccount[c];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int acc = 0;
-        for (int t = 0; t < blockDim.x; t++) { int v = part[t]; part[t] = acc; acc += v; }
-        d.cstart[ncell] = acc;
-    }
-    __syncthreads();
-    int acc = part[threadIdx.x];
+    int total;
+    int acc = block_exscan(s, &total);
+    if (threadIdx.x == 0) d.cstart[ncell] = total;
     for (int c = b; c < e; c++) { d.cstart[c] = acc; acc += d.ccount[c]; d.cfill[c] = 0; }
 }
 
@@ -266,20 +286,13 @@ __global__ void k_near_items_count(Dev d, int ncell, int tile) {
 
 // exclusive scan of the item counts in place (one block), total to near_ctl[1]
 __global__ void k_near_items_scan(Dev d, int ncell) {
-    __shared__ int part[1024];
     const int per = (ncell + blockDim.x - 1) / blockDim.x;
     const int b = threadIdx.x * per, e = min(ncell, b + per);
     int s = 0;
     for (int c = b; c < e; c++) s += d.near_icount[c];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int acc = 0;
-        for (int t = 0; t < blockDim.x; t++) { int v = part[t]; part[t] = acc; acc += v; }
-        d.near_ctl[1] = acc;
-    }
-    __syncthreads();
-    int acc = part[threadIdx.x];
+    int total;
+    int acc = block_exscan(s, &total);
+    if (threadIdx.x == 0) d.near_ctl[1] = total;
     for (int c = b; c < e; c++) { int v = d.near_icount[c]; d.near_icount[c] = acc; acc += v; }
 }
 
@@ -771,11 +784,11 @@ __global__ void __launch_bounds__(128) k_m2m(Dev d, const double2 *Oc, double2 *
 
 // L2L, src/shiftLjk2.f90:16-60 and src/shiftLjk3.f90:27-91: child box
 // from its parent (level 2 -> 3 or 3 -> 4), plus the child's M2L partial
-// sums of its G offset groups (real form, [group][25][boxes of the level]),
-// added in group order
+// sums of its G offset groups (real form, [box][group][25]), added in
+// group order
 template <typename R, typename OP>
 __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, const int *brep, int level,
-                      const R *part, int G, int nlev) {
+                      const R *part, int G) {
     const int b = blockIdx.x;
     const Rep r = d.rep[brep[b]];
     const int div = level == 3 ? 2 : 1;  // child grid = nc / div
@@ -794,9 +807,10 @@ __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, cons
     int j, k;
     out_jk(o, j, k);
     R pre = 0, pim = 0;
+    const R *pb = part + (size_t)b * G * LP;
     for (int g = 0; g < G; g++) {
-        pre += part[((size_t)g * LP + o) * nlev + b];
-        if (k > 0) pim += part[((size_t)g * LP + LPH + o - (j + 1)) * nlev + b];
+        pre += pb[g * LP + o];
+        if (k > 0) pim += pb[g * LP + LPH + o - (j + 1)];
     }
     store_jk(Lc + (size_t)b * LP, o, (double)re + (double)pre, (double)im + (double)pim, false);
 }
@@ -913,7 +927,7 @@ __device__ __forceinline__ void m2c_row(const double *op, double va, double vb, 
 }
 
 template <typename R>
-__global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d, int ncell, int n3) {
+__global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d) {
     extern __shared__ __align__(16) unsigned char smraw[];
     R *sop = (R *)smraw;   // [M2C_CH][LP][M2C_LD]
     const int4 it = d.m2c_items[blockIdx.x];
@@ -937,6 +951,13 @@ __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d, int ncell, int n3
         return ((z + 2) * p1 + (y + 2)) * p0 + x + 2;
     };
     const int ia = pidx(ta), ib = pidx(tb);
+    // the class-packed sources of offset k (shifted so that a target's own padded index addresses them)
+    auto src_of = [&](int k) {
+        const int oi = offs[k];
+        const int ex = px + oi % 7 - 3, ey = py + (oi / 7) % 7 - 3, ez = pz + oi / 49 - 3;
+        const int q = (ex & 1) + 2 * (ey & 1) + 4 * (ez & 1);
+        return pk + (size_t)q * LP * vol + ((ez >> 1) * p1 + (ey >> 1)) * p0 + (ex >> 1);
+    };
     R aa[LP], ab[LP];
 #pragma unroll
     for (int i = 0; i < LP; i++) aa[i] = ab[i] = R(0);
@@ -949,17 +970,13 @@ __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d, int ncell, int n3
         }
         __syncthreads();
         for (int kk = 0; kk < nch; kk++) {
-            const int oi = offs[c0 + kk];
-            const int ex = px + oi % 7 - 3, ey = py + (oi / 7) % 7 - 3, ez = pz + oi / 49 - 3;
-            const int q = (ex & 1) + 2 * (ey & 1) + 4 * (ez & 1);
-            const R *src = pk + (size_t)q * LP * vol + ((ez >> 1) * p1 + (ey >> 1)) * p0 + (ex >> 1);
+            const R *src = src_of(c0 + kk);
             const R *op = sop + kk * LP * M2C_LD;
 #pragma unroll
             for (int i = 0; i < LP; i++) m2c_row(op + i * M2C_LD, src[(size_t)i * vol + ia], src[(size_t)i * vol + ib], aa, ab);
         }
     }
     R *part = (R *)(level == 4 ? d.part4 : d.part3);
-    const int ncl = level == 4 ? ncell : n3;
     const int base = level == 4 ? r.cell0 : r.l3_0, n0 = 2 * h0, n1 = 2 * h1;
     auto cell = [&](int t) {
         const int x = t % h0, y = (t / h0) % h1, z = t / (h0 * h1);
@@ -968,12 +985,12 @@ __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d, int ncell, int n3
     if (ta <= last) {
         const int cg = cell(ta);
 #pragma unroll
-        for (int i = 0; i < LP; i++) part[((size_t)g * LP + i) * ncl + cg] = aa[i];
+        for (int i = 0; i < LP; i++) part[((size_t)cg * G + g) * LP + i] = aa[i];
     }
     if (tb <= last) {
         const int cg = cell(tb);
 #pragma unroll
-        for (int i = 0; i < LP; i++) part[((size_t)g * LP + i) * ncl + cg] = ab[i];
+        for (int i = 0; i < LP; i++) part[((size_t)cg * G + g) * LP + i] = ab[i];
     }
 }
 
@@ -1028,10 +1045,10 @@ void fma_build(const Dev &d, int ncell, int n3, int n2, int d2, const OP *m43, c
     k_m2m<R><<<n3, 128, 0, st>>>(d, d.O4, d.O3, m43, d.b3rep, 3);
     k_m2m<R><<<n2, 128, 0, st>>>(d, d.O3, d.O2, m32, d.b2rep, 2);
     k_m2l_pack<R><<<((ncell + n3) * LP + 255) / 256, 256, 0, st>>>(d, ncell, n3);
-    k_m2l_cls<R><<<dim3(d.m2c_nitems, d.m2c_groups), 32 * M2C_W, m2c_smem<R>(), st>>>(d, ncell, n3);
+    k_m2l_cls<R><<<dim3(d.m2c_nitems, d.m2c_groups), 32 * M2C_W, m2c_smem<R>(), st>>>(d);
     k_m2l_all<R><<<n2, 256, 0, st>>>(d, h2, cf, d2);
-    k_l2l<R><<<n3, 32, 0, st>>>(d, d.L2, d.L3, l23, d.b3rep, 3, (const R *)d.part3, d.m2c_groups, n3);
-    k_l2l<R><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, l34, d.crep, 4, (const R *)d.part4, d.m2c_groups, ncell);
+    k_l2l<R><<<n3, 32, 0, st>>>(d, d.L2, d.L3, l23, d.b3rep, 3, (const R *)d.part3, d.m2c_groups);
+    k_l2l<R><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, l34, d.crep, 4, (const R *)d.part4, d.m2c_groups);
 }
 
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {

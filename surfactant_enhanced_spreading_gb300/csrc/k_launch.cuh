@@ -8,7 +8,7 @@ namespace sesp {
 
 // k_exact.cu
 void upload_tables_exact(const Tables &t, cudaStream_t st);
-void launch_locate(const Dev &d, int nmol, cudaStream_t st);
+void launch_locate(const Dev &d, int nmol, const int *smols, int nsurf_sites, cudaStream_t st);
 void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st);
 // launch shape of the mixed paths' constraint halves (results do not depend on it)
 struct ConstraintShape {

@@ -445,7 +445,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
     if (rebuild) {
         tstart(c, 5);
         cudaMemsetAsync(d.ccount, 0, sizeof(int) * c->ncell, c->st);
-        launch_locate(d, c->nmol, c->st);
+        launch_locate(d, c->nmol, c->smols, c->nsm * NSURF, c->st);
         family(c, "locate");
         launch_sort(d, c->nsite, c->ncell, c->st);
         family(c, "cell sort");
@@ -609,6 +609,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
             r.nr[a] = r.nc[a] / 4;
             r.rsd[a] = r.nc[a] * RS;
             r.rhs[a] = r.rsd[a] / 2.0;
+            r.irsd[a] = 1.0 / r.rsd[a];
             d2 = std::max(d2, r.nr[a] - 1);
         }
         if (ri.nw < 0 || ri.ns < 0 || ri.nw + ri.ns == 0) return fail(SESP_EINVAL, "replica %d: empty system", q);
@@ -670,7 +671,8 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     int w2 = 2 * d2 + 1;
     const size_t nh2 = (size_t)w2 * w2 * w2 * NHARM;
     // real-form M2L at L4 and L3: work items of M2C_TILE targets of one parity
-    // class, each split into m2c_groups offset groups (about 8 CTAs per SM)
+    // class, each split into M2C_GROUPS offset groups (a constant, so a
+    // replica's sums do not depend on what else is batched with it)
     const int mixed = c->p.precision != SESP_PLAIN_FP64;
     const size_t rsz = mixed ? sizeof(float) : sizeof(double);
     std::vector<int4> m2c_items;
@@ -684,7 +686,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
                     m2c_items.push_back(make_int4(lev << 28 | q, cls, t0, std::min(M2C_TILE, ncls - t0)));
         }
     d.m2c_nitems = (int)m2c_items.size();
-    d.m2c_groups = std::max(1, std::min(24, (8 * c->n_sm + d.m2c_nitems - 1) / d.m2c_nitems));
+    d.m2c_groups = M2C_GROUPS;
     {
         char *p4 = nullptr, *p3 = nullptr, *q4 = nullptr, *q3 = nullptr, *o4 = nullptr, *o3 = nullptr;
         if ((e = dalloc(c, &o4, (size_t)343 * LP * M2C_LD * rsz)) || (e = dalloc(c, &o3, (size_t)343 * LP * M2C_LD * rsz)) ||
@@ -726,7 +728,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     // static per-site / per-molecule / per-box data
     std::vector<uint8_t> ptype(N);
     std::vector<int> smol(N), mrep(M), mfirst(M), mkind(M), wm, sm, crep(C), b3(n3), b2(n2);
-    std::vector<double> axis, sx(N), sy(N), sz(N), vxa(N, 0.0), vya(N, 0.0), vza(N, 0.0), eta0(R, 0.0);
+    std::vector<double> axis, rcen2, sx(N), sy(N), sz(N), vxa(N, 0.0), vya(N, 0.0), vza(N, 0.0), eta0(R, 0.0);
     std::vector<int> gstart(1, 0);
     std::vector<double4> gpos;
     std::vector<float4> gpos32;   // relative to the column's (x, y) centre and the bottom cell layer's z centre
@@ -757,6 +759,10 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         for (int k = 0; k < cc / 64; k++) b2[r.l2_0 + k] = q;
         size_t a0 = axis.size();
         for (int a = 0; a < 3; a++) axis_centres(r, a, axis);
+        for (int a = 0; a < 3; a++) {   // the reference's operation order (rcen2xtmp)
+            const double b = (double)r.nr[a];
+            for (int rk = 0; rk < r.nr[a]; rk++) rcen2.push_back(r.rsd[a] * (rk + 1) / b - r.rhs[a] - r.rsd[a] / b / 2.0);
+        }
         // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:9-35
         for (int iy = 0; iy < r.nc[1]; iy++)
             for (int ix = 0; ix < r.nc[0]; ix++) {
@@ -811,7 +817,8 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
                 gstart.push_back((int)gpos.size());
             }
     }
-    if ((e = dalloc(c, &d.axis, axis.size())) || (e = dalloc(c, &d.gcol_start, gstart.size())) ||
+    if ((e = dalloc(c, &d.axis, axis.size())) || (e = dalloc(c, &d.rcen2, rcen2.size())) ||
+        (e = dalloc(c, &d.gcol_start, gstart.size())) ||
         (e = dalloc(c, &d.gpos, gpos.size())) || (e = dalloc(c, &d.gpos32, gpos32.size())) ||
         (e = dalloc(c, &d.gbin, gbin.size())) || (e = dalloc(c, &d.ggrp_z, ggrp_z.size())) ||
         (e = dalloc(c, &d.gsite, N)) || (e = dalloc(c, &d.gcount, 1)))
@@ -907,6 +914,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     CK(cudaMemcpyAsync(d.rep, c->reps.data(), R * sizeof(Rep), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.eta, eta0.data(), R * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.axis, axis.data(), axis.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(d.rcen2, rcen2.data(), rcen2.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.crep, crep.data(), C * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.b3rep, b3.data(), n3 * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.b2rep, b2.data(), n2 * sizeof(int), cudaMemcpyHostToDevice, c->st));

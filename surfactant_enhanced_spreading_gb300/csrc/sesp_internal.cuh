@@ -45,6 +45,7 @@ constexpr int M2C_NOFF = 189; // M2L offsets of a cell (6^3 - 3^3 for its parity
 constexpr int M2C_LD = 28;    // padded output stride of a real M2L operator row
 constexpr int M2C_W = 2;      // warps of an M2L CTA, 64 targets each (2 per lane)
 constexpr int M2C_TILE = 64 * M2C_W;
+constexpr int M2C_GROUPS = 21; // offset groups of an M2L work item, 9 offsets each (partial sums added in group order)
 constexpr int GGRP = 8;       // carbon groups per graphite column
 constexpr int GBIN = 32;      // y bins per group
 // y extent of a column's carbons about its centre: rc + half the L4 cell diagonal
@@ -64,6 +65,7 @@ struct Rep {
     int pk4, pk3;     // first element of this replica's class-packed L4 / L3 multipoles
     double rhs[3], rsd[3];
     double pnh1, pnh2;
+    double irsd[3];   // 1 / rsd
 };
 
 // constant topology and force-field tables (reference values, src/init_arrays.f90)
@@ -105,6 +107,7 @@ struct Dev {
     double *eta_part;    // [nrep][32][2] partial kinetic sums of the eta update
     unsigned *eta_ctl;   // [nrep] blocks of the eta update finished
     double *axis;        // cell centre tables
+    double *rcen2;       // rank centres per replica (at axis0 / 4) and axis (src/init_box_dimensions.f90:40-42)
     // cells
     int *crep, *b3rep, *b2rep;
     int *cstart, *ccount, *cfill;
@@ -152,7 +155,7 @@ struct Dev {
     // multipoles of each replica repacked per parity class of its cells:
     // [class 8][component 25][class grid with a zero margin of 2 per side]
     void *pk4, *pk3;
-    // partial sums per offset group: [group][component 25][cells of the level]
+    // partial sums per offset group: [cell of the level][group][component 25]
     void *part4, *part3;
     int4 *m2c_items;     // work items: (level << 28 | replica, class, first target, targets)
     int *m2c_off;        // per class its 189 offsets, (dx + 3) + 7 (dy + 3) + 49 (dz + 3)

@@ -98,10 +98,10 @@ def estimate_bytes(system: S.System) -> int:
     cells = ncell * (5 * 4 + 2 * cz + 4 + 9 * 20) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
     ops = (w2 ** 3 + 4 * 8) * 15 * 25 * 16 + w2 ** 3 * 45 * 24
     # real-form M2L at L4 and L3: operators, class-packed multipoles, partial
-    # sums of up to 24 offset groups (FP64 sizes: an upper bound)
+    # sums of 21 offset groups (FP64 sizes: an upper bound)
     pad4 = int(np.prod(nc // 2 + 4)) * 200
     pad3 = int(np.prod(nc // 4 + 4)) * 200
-    ops += 8 * (2 * 343 * 25 * 28 + pad4 + pad3 + 24 * 25 * (ncell + n3)) + 16 * 16 * (ncell // 1024 + 1) + 8 * 189 * 4
+    ops += 8 * (2 * 343 * 25 * 28 + pad4 + pad3 + 21 * 25 * (ncell + n3)) + 16 * 16 * (ncell // 1024 + 1) + 8 * 189 * 4
     ncarb = system.carbons.reshape(-1, 3).shape[0]
     ncol = int(nc[0] * nc[1])
     graphite = 12 * ncarb * 48 + (ncol + 1) * 4 + ncol * 8 * (33 * 4 + 8) + int(nc.sum()) * 8 + n * 4
