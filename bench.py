@@ -102,8 +102,8 @@ def make_system(small):
 def make_batch(n, seed, small=False):
     """Batched workload: n replicas, waters ~ logU[1k, 30k] (logU[300, 1k]
     for --small), surfactants per water ~ U[0, 2%], each droplet on its own
-    2-layer sheet 2.5x its diameter in the smallest closed box (multiples of
-    4 cells) that holds it."""
+    2-layer sheet over the whole floor of the smallest closed box (multiples
+    of 4 cells) that holds it."""
     from surfactant_enhanced_spreading_gb300 import serve
     rng = np.random.default_rng(seed)
     lo, hi = (300, 1000) if small else (1000, 30000)
@@ -120,7 +120,7 @@ def run_batched(args, local, E):
     n_sites = sum(s.n_sites for s in systems)
     res = {"replicas": len(systems), "sites": n_sites,
            "workload": f"{len(systems)} replicas, waters ~ logU[{'300, 1k' if args.small else '1k, 30k'}], "
-                       "surfactants ~ U[0, 2%] of waters, 2-layer graphite 2.5x the droplet diameter, seed 4242"}
+                       "surfactants ~ U[0, 2%] of waters, 2-layer graphite over the box floor, seed 4242"}
     for name, prec, steps in (("mixed", E.MIXED, 20), ("plain_fp64", E.PLAIN_FP64, 3)):
         eng = E.Engine(systems, prec, device=local)
         eng.force(True)

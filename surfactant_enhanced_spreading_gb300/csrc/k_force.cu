@@ -1098,6 +1098,12 @@ __device__ inline int graphite_column(const Dev &d, const Rep &r, int g, double 
     return r.gcol0 + ix + r.nc[0] * iy;
 }
 
+// walls, src/eval_wall.f90:17-23: 48 / (v - h)^13 + 48 / (h + v)^13 per
+// axis.  The mixed path forms the distances in FP64 (they cancel near a
+// wall) and the rest in FP32 (at most 91 sigma across: no overflow).
+__device__ inline float pow13f(float v) { float v2 = v * v, v4 = v2 * v2, v8 = v4 * v4; return v8 * v4 * v; }
+
+template <bool MIXED>
 __global__ void k_site_forces(Dev d, int nsite, int terms) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nsite) return;
@@ -1108,10 +1114,16 @@ __global__ void k_site_forces(Dev d, int nsite, int terms) {
         fx = d.nf[3 * (size_t)slot]; fy = d.nf[3 * (size_t)slot + 1]; fz = d.nf[3 * (size_t)slot + 2];
     }
     double x = d.x[g], y = d.y[g], z = d.z[g];
-    if (terms & SESP_T_WALL) {  // src/eval_wall.f90:17-23
-        fx += 48.0 / pow13(x - r.rhs[0]); fx += 48.0 / pow13(r.rhs[0] + x);
-        fy += 48.0 / pow13(y - r.rhs[1]); fy += 48.0 / pow13(r.rhs[1] + y);
-        fz += 48.0 / pow13(z - r.rhs[2]); fz += 48.0 / pow13(r.rhs[2] + z);
+    if (terms & SESP_T_WALL) {
+        if constexpr (MIXED) {
+            fx += (double)(48.f / pow13f((float)(x - r.rhs[0])) + 48.f / pow13f((float)(r.rhs[0] + x)));
+            fy += (double)(48.f / pow13f((float)(y - r.rhs[1])) + 48.f / pow13f((float)(r.rhs[1] + y)));
+            fz += (double)(48.f / pow13f((float)(z - r.rhs[2])) + 48.f / pow13f((float)(r.rhs[2] + z)));
+        } else {
+            fx += 48.0 / pow13(x - r.rhs[0]); fx += 48.0 / pow13(r.rhs[0] + x);
+            fy += 48.0 / pow13(y - r.rhs[1]); fy += 48.0 / pow13(r.rhs[1] + y);
+            fz += 48.0 / pow13(z - r.rhs[2]); fz += 48.0 / pow13(r.rhs[2] + z);
+        }
     }
     d.fx[g] = fx; d.fy[g] = fy; d.fz[g] = fz;
 }
@@ -1220,7 +1232,8 @@ void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st) {
 }
 
 void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st) {
-    k_site_forces<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
+    if (mixed) k_site_forces<true><<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
+    else k_site_forces<false><<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
     if (terms & SESP_T_GRAPHITE) {
         if (mixed) k_graphite<float><<<152 * 4, 256, 0, st>>>(d);
         else k_graphite<double><<<152 * 4, 256, 0, st>>>(d);

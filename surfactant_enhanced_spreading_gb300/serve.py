@@ -47,6 +47,7 @@ class Result:
     eta: float = 0.0
     device_bytes: int = 0
     estimate_bytes: int = 0
+    shake_failures: int = 0     # SHAKE/RATTLE molecule failures over the run (engine counter 0)
 
     @property
     def latency(self) -> float:
@@ -168,7 +169,7 @@ class Server:
                 fin = clock() - t0
                 res = Result(rid=req.rid, n_sites=req.system.n_sites, steps=req.steps, arrival=req.arrival,
                              admitted=a["admitted"], finished=fin, device_bytes=a["actual"],
-                             estimate_bytes=a["est"])
+                             estimate_bytes=a["est"], shake_failures=int(eng.counters()[0]))
                 if self.keep_state:
                     pos, vel, _ = eng.state()
                     res.pos, res.vel, res.eta = pos, vel, eng.eta
@@ -194,7 +195,8 @@ def summarize(results: list[Result], wall: float | None = None) -> dict:
     span = wall if wall is not None else (max(r.finished for r in results) - min(r.arrival for r in results))
     return {"requests": len(results), "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
-            "atom_steps_per_s": atom_steps / span if span > 0 else None, "span_s": span}
+            "atom_steps_per_s": atom_steps / span if span > 0 else None, "span_s": span,
+            "shake_failures": int(sum(r.shake_failures for r in results))}
 
 
 def poisson_requests(n: int, rate_per_s: float, seed: int, water=(1000, 50000), surf=(0, 500), steps=(500, 5000),
@@ -233,7 +235,8 @@ def run_one_at_a_time(requests: list[Request], precision: int, device: int = 0, 
         eng.sync()
         pos, vel, _ = eng.state()
         out.append(Result(rid=req.rid, n_sites=req.system.n_sites, steps=req.steps, arrival=req.arrival,
-                          admitted=start, finished=time.perf_counter() - t0, pos=pos, vel=vel, eta=eng.eta))
+                          admitted=start, finished=time.perf_counter() - t0, pos=pos, vel=vel, eta=eng.eta,
+                          shake_failures=int(eng.counters()[0])))
         eng.close()
     return out
 

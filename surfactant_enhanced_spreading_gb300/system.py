@@ -218,7 +218,10 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
 
     The top carbon layer sits 4 A above the lower wall, inside the bottom
     layer of cells, so the graphite term (bottom cells only,
-    src/eval_graphite.f90:13-15) acts on the first water layer.
+    src/eval_graphite.f90:13-15) acts on the first water layer.  The sheet
+    covers the whole floor unless ``graphite_extent`` (half-width, A) limits
+    it: a molecule that leaves a smaller sheet sinks beside its edge, under
+    the top carbon plane, and meets the carbons side-on.
     """
     rng = np.random.default_rng(seed)
     cells = tuple(int(c) for c in cells)
@@ -309,8 +312,9 @@ def droplet(n_water: int, n_surf: int = 0, cells=(8, 8, 8), seed: int = 0, graph
     pos[:, 2] += z_base
     if np.any(np.abs(pos[:, :2]) > half[:2] - 1.0) or np.any(pos[:, 2] > half[2] - 1.0):
         raise RuntimeError("droplet does not fit the box; use more cells")
-    ext = graphite_extent if graphite_extent is not None else min(half[0], 2.5 * radius)
-    carb = graphite(graphite_layers, min(ext, half[0]), min(ext, half[1]), z_graph) if graphite_layers else np.zeros((0, 3))
+    ex = min(graphite_extent, half[0]) if graphite_extent is not None else half[0]
+    ey = min(graphite_extent, half[1]) if graphite_extent is not None else half[1]
+    carb = graphite(graphite_layers, ex, ey, z_graph) if graphite_layers else np.zeros((0, 3))
     masses = np.concatenate([np.tile(WATER_MASS, n_water), np.tile(SURF_MASS, n_surf)])
     vel = maxwell(masses, rng, temperature)
     return System(n_water=n_water, n_surf=n_surf, cells=cells, pos=pos / SIGMA, vel=vel,

@@ -86,3 +86,16 @@ def test_crowded_request_starts_without_failures():
     orc.run(99101, 2)
     assert orc.fail_count() == 0
     assert np.isfinite(orc.get(0)).all()
+
+
+def test_graphite_covers_the_floor():
+    """A droplet far smaller than its box still sits on a sheet that reaches
+    every wall (within one lattice step), so no molecule can leave the sheet
+    and sink beside its edge."""
+    s = S.droplet(1500, 10, cells=(20, 20, 12), seed=3)
+    half = np.array(s.cells, dtype=np.float64) * S.RS / 2.0
+    c = s.carbons.reshape(-1, 3)
+    step = 2.5 / S.SIGMA
+    for a in (0, 1):
+        assert c[:, a].min() < -half[a] + step and c[:, a].max() > half[a] - step
+    assert np.all(np.abs(c[:, :2]) < half[:2])
