@@ -465,7 +465,7 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
 #pragma unroll 2
         for (int sl = th; sl < t1; sl++) pairk_coul32<K>(u, pos32[sl], keys[sl] >> 5, f);
     }
-    double *part = d.near_part + (size_t)pr * 3 * nslot;
+    float *part = (float *)d.near_part + (size_t)pr * 3 * nslot;   // FP32 row partials on the mixed path
 #pragma unroll
     for (int j = 0; j < K; j++)
         if (act[j]) {
@@ -604,33 +604,37 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     const Rep r = d.rep[d.crep[c]];
     int ix, iy, iz;
     cell_xyz(r, c, ix, iy, iz);
-    double fx = 0.0, fy = 0.0, fz = 0.0;
+    // the 9 row partials in row order: FP32 rows summed in FP32 on the mixed
+    // path (one conversion to FP64 per component), FP64 on the plain path
+    R fx = 0, fy = 0, fz = 0;
     if (terms & SESP_T_NEAR) {
         const int mask = near_row_mask(r, iy, iz);
+        const R *part = (const R *)d.near_part;
         for (int pr = 0; pr < 9; pr++) {
             if (!(mask >> pr & 1)) continue;
-            const double *p = d.near_part + (size_t)pr * 3 * nslot + 3 * (size_t)s;
+            const R *p = part + (size_t)pr * 3 * nslot + 3 * (size_t)s;
             fx += p[0]; fy += p[1]; fz += p[2];
         }
     }
     if (terms & SESP_T_FAR) {
-        R Lre[LP], Lim[LP];
-        const double2 *L = d.L4 + (size_t)c * LP;
-        for (int k = 0; k < LP; k++) { double2 v = L[k]; Lre[k] = (R)v.x; Lim[k] = (R)v.y; }
-        R x, y, z;
-        double4 pd = d.srt_pos[s];
-        if (MIXED) {
-            float4 p = d.srt_pos32[s];
-            x = p.x; y = p.y; z = p.z;
+        R Lre[LP], Lim[LP], x, y, z, q;
+        if constexpr (MIXED) {   // the FP32 copy of L4 and the cell-relative FP32 position: no FP64 work
+            const float2 *L = d.L4f + (size_t)c * LP;
+            for (int k = 0; k < LP; k++) { const float2 v = L[k]; Lre[k] = v.x; Lim[k] = v.y; }
+            const float4 p = d.srt_pos32[s];
+            x = p.x; y = p.y; z = p.z; q = p.w * (float)XPI;
         } else {
-            x = (R)(pd.x - cell_centre(d, r, 0, ix)); y = (R)(pd.y - cell_centre(d, r, 1, iy)); z = (R)(pd.z - cell_centre(d, r, 2, iz));
+            const double2 *L = d.L4 + (size_t)c * LP;
+            for (int k = 0; k < LP; k++) { const double2 v = L[k]; Lre[k] = v.x; Lim[k] = v.y; }
+            const double4 pd = d.srt_pos[s];
+            x = pd.x - cell_centre(d, r, 0, ix); y = pd.y - cell_centre(d, r, 1, iy); z = pd.z - cell_centre(d, r, 2, iz);
+            q = pd.w * XPI;
         }
         R gx, gy, gz;
         local_grad<R>(Lre, Lim, x, y, z, gx, gy, gz, nullptr);
-        R q = (R)(pd.w * XPI);
-        fx -= (double)(q * gx); fy -= (double)(q * gy); fz -= (double)(q * gz);
+        fx -= q * gx; fy -= q * gy; fz -= q * gz;
     }
-    d.nf[3 * (size_t)s] = fx; d.nf[3 * (size_t)s + 1] = fy; d.nf[3 * (size_t)s + 2] = fz;
+    d.nf[3 * (size_t)s] = (double)fx; d.nf[3 * (size_t)s + 1] = (double)fy; d.nf[3 * (size_t)s + 2] = (double)fz;
 }
 
 int near_max_ctas_per_sm(int mixed, int tile) {
@@ -788,7 +792,7 @@ __global__ void __launch_bounds__(128) k_m2m(Dev d, const double2 *Oc, double2 *
 // group order
 template <typename R, typename OP>
 __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, const int *brep, int level,
-                      const R *part, int G) {
+                      const R *part, int G, float2 *Lf) {
     const int b = blockIdx.x;
     const Rep r = d.rep[brep[b]];
     const int div = level == 3 ? 2 : 1;  // child grid = nc / div
@@ -812,7 +816,12 @@ __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, cons
         pre += pb[g * LP + o];
         if (k > 0) pim += pb[g * LP + LPH + o - (j + 1)];
     }
-    store_jk(Lc + (size_t)b * LP, o, (double)re + (double)pre, (double)im + (double)pim, false);
+    const double vre = (double)re + (double)pre, vim = (double)im + (double)pim;
+    store_jk(Lc + (size_t)b * LP, o, vre, vim, false);
+    if (Lf) {   // FP32 copy of the finished L4 for the mixed path's L2P
+        Lf[(size_t)b * LP + j * (j + 1) + k] = make_float2((float)vre, (float)vim);
+        if (k > 0) Lf[(size_t)b * LP + j * (j + 1) - k] = make_float2((float)vre, (float)-vim);
+    }
 }
 
 // M2L with the operator of src/computeLjk4.f90:134-158 factored as
@@ -1047,8 +1056,9 @@ void fma_build(const Dev &d, int ncell, int n3, int n2, int d2, const OP *m43, c
     k_m2l_pack<R><<<((ncell + n3) * LP + 255) / 256, 256, 0, st>>>(d, ncell, n3);
     k_m2l_cls<R><<<dim3(d.m2c_nitems, d.m2c_groups), 32 * M2C_W, m2c_smem<R>(), st>>>(d);
     k_m2l_all<R><<<n2, 256, 0, st>>>(d, h2, cf, d2);
-    k_l2l<R><<<n3, 32, 0, st>>>(d, d.L2, d.L3, l23, d.b3rep, 3, (const R *)d.part3, d.m2c_groups);
-    k_l2l<R><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, l34, d.crep, 4, (const R *)d.part4, d.m2c_groups);
+    k_l2l<R><<<n3, 32, 0, st>>>(d, d.L2, d.L3, l23, d.b3rep, 3, (const R *)d.part3, d.m2c_groups, nullptr);
+    k_l2l<R><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, l34, d.crep, 4, (const R *)d.part4, d.m2c_groups,
+                                   sizeof(R) == 4 ? d.L4f : nullptr);
 }
 
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {
@@ -1125,6 +1135,10 @@ __global__ void k_site_forces(Dev d, int nsite, int terms) {
             fz += 48.0 / pow13(z - r.rhs[2]); fz += 48.0 / pow13(r.rhs[2] + z);
         }
     }
+    // the step's graphite and intramolecular forces, cleared for the next step
+    const size_t n = d.nsite;
+    fx += d.fside[g]; fy += d.fside[n + g]; fz += d.fside[2 * n + g];
+    d.fside[g] = 0.0; d.fside[n + g] = 0.0; d.fside[2 * n + g] = 0.0;
     d.fx[g] = fx; d.fy[g] = fy; d.fz[g] = fz;
 }
 
@@ -1222,7 +1236,10 @@ __global__ void k_graphite(Dev d) {
             fy += __shfl_down_sync(0xffffffffu, fy, off);
             fz += __shfl_down_sync(0xffffffffu, fz, off);
         }
-        if (lane == 0) { d.fx[g] += (double)fx; d.fy[g] += (double)fy; d.fz[g] += (double)fz; }
+        if (lane == 0) {
+            const size_t n = d.nsite;
+            d.fside[g] += (double)fx; d.fside[n + g] += (double)fy; d.fside[2 * n + g] += (double)fz;
+        }
     }
 }
 
@@ -1234,6 +1251,9 @@ void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st) {
 void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st) {
     if (mixed) k_site_forces<true><<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
     else k_site_forces<false><<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
+}
+
+void launch_graphite(const Dev &d, int terms, int mixed, cudaStream_t st) {
     if (terms & SESP_T_GRAPHITE) {
         if (mixed) k_graphite<float><<<152 * 4, 256, 0, st>>>(d);
         else k_graphite<double><<<152 * 4, 256, 0, st>>>(d);
@@ -1402,13 +1422,16 @@ __device__ inline R subtract_site(const Pos29<R> &m, int j, uint32_t bits, R f[3
 }
 
 // One block per surfactant: the 36 angles, 30 dihedrals and 312
-// intramolecular pairs are spread over the threads, each writing its site
-// forces to its own slots in shared memory; then thread s sums the slots of
-// site s in the fixed order of the contribution table (deterministic, no
-// atomics) and adds its far-field correction.
+// intramolecular pairs take one thread each (INTRA_THREADS >= their count,
+// so a block is one term deep), each writing its site forces to its own
+// slots in shared memory; then thread s sums the slots of site s in the
+// fixed order of the contribution table (deterministic, no atomics) and adds
+// its far-field correction.
 constexpr int NIPAIR = 270 + NSELF;                 // k >= j+4 pairs of sites 1..15, then the 42 listed
 constexpr int NSLOT = NANGLE * 3 + NDIH * 4 + NIPAIR * 2;
 constexpr int NTERM = NANGLE + NDIH + NIPAIR;
+constexpr int INTRA_THREADS = 384;
+static_assert(INTRA_THREADS >= NTERM, "one term per thread");
 
 struct IntraMap {
     short off[NSURF + 1];  // slots of site s: list[off[s] .. off[s+1])
@@ -1423,7 +1446,7 @@ void upload_intra_map(const void *host_map, cudaStream_t st) {
 size_t intra_map_size() { return sizeof(IntraMap); }
 
 template <typename R>
-__global__ void __launch_bounds__(128) k_intra_block(Dev d, const int *smols, int terms) {
+__global__ void __launch_bounds__(INTRA_THREADS) k_intra_block(Dev d, const int *smols, int terms) {
     __shared__ Pos29<R> m;
     __shared__ R sf[NSLOT][3];
     const int t = blockIdx.x;
@@ -1471,14 +1494,15 @@ __global__ void __launch_bounds__(128) k_intra_block(Dev d, const int *smols, in
             subtract_site<R>(m, s, d.isub[(size_t)t * NSURF + s], f);
             fx += f[0]; fy += f[1]; fz += f[2];
         }
-        d.fx[g0 + s] += (double)fx; d.fy[g0 + s] += (double)fy; d.fz[g0 + s] += (double)fz;
+        const size_t n = d.nsite;
+        d.fside[g0 + s] += (double)fx; d.fside[n + g0 + s] += (double)fy; d.fside[2 * n + g0 + s] += (double)fz;
     }
 }
 
 void launch_intra(const Dev &d, const int *smols, int ns, int terms, int mixed, cudaStream_t st) {
     if (ns && (terms & (SESP_T_VALENCE | SESP_T_DIHEDRAL | SESP_T_BERENDSEN | SESP_T_INTERNAL | SESP_T_SUBTRACT))) {
-        if (mixed) k_intra_block<float><<<ns, 128, 0, st>>>(d, smols, terms);
-        else k_intra_block<double><<<ns, 128, 0, st>>>(d, smols, terms);
+        if (mixed) k_intra_block<float><<<ns, INTRA_THREADS, 0, st>>>(d, smols, terms);
+        else k_intra_block<double><<<ns, INTRA_THREADS, 0, st>>>(d, smols, terms);
     }
 }
 

@@ -50,6 +50,7 @@ int near_max_ctas_per_sm(int mixed, int tile);
 void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st);
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st);
 void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st);
+void launch_graphite(const Dev &d, int terms, int mixed, cudaStream_t st);
 void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st);
 void init_force_kernels();
 void upload_intra_map(const void *host_map, cudaStream_t st);

@@ -345,6 +345,11 @@ struct sesp_ctx {
     int64_t steps = 0;
     // graphs of one step with / without a rebuild
     cudaGraphExec_t g_step[2] = {nullptr, nullptr};
+    // side stream of a step: the graphite and intramolecular terms run there,
+    // beside the far-field build and the pair field (fork after the gather,
+    // join before the site forces)
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     NearShape near = {64, 0};   // pair-field launch shape (autotuned or set; results do not depend on it)
     ConstraintShape cshape = {0, 4, 1};   // constraint halves of the mixed paths (likewise)
     int n_sm = 0;               // streaming multiprocessors of the device
@@ -461,6 +466,17 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
     }
     launch_gather(d, c->nsite, c->ncell, mixed, c->st);
     family(c, "gather");
+    // graphite and intramolecular terms into the side forces (fside), on the
+    // side stream beside the far-field build and the pair field; in order on
+    // the main stream when kernels are timed or checked one by one
+    const bool fork = !c->timing && !c->sync_check;
+    if (fork) {
+        cudaEventRecord(c->ev_fork, c->st);
+        cudaStreamWaitEvent(c->st2, c->ev_fork, 0);
+        launch_graphite(d, terms, mixed, c->st2);
+        launch_intra(d, c->smols, c->nsm, terms, mixed, c->st2);
+        cudaEventRecord(c->ev_join, c->st2);
+    }
     if (rebuild) {
         tstart(c, 6);
         launch_fma_build(d, c->ncell, c->n3, c->n2, mixed, c->d2, c->st);
@@ -472,10 +488,16 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
     family(c, "near field");
     tstop(c, 0);
     tstart(c, 4);
+    if (fork) {
+        cudaStreamWaitEvent(c->st, c->ev_join, 0);
+    } else {
+        launch_graphite(d, terms, mixed, c->st);
+        family(c, "graphite");
+        launch_intra(d, c->smols, c->nsm, terms, mixed, c->st);
+        family(c, "intramolecular");
+    }
     launch_site_forces(d, c->nsite, terms, mixed, c->st);
     family(c, "site forces");
-    launch_intra(d, c->smols, c->nsm, terms, mixed, c->st);
-    family(c, "intramolecular");
     tstop(c, 4);
 }
 
@@ -543,7 +565,13 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     sesp_ctx *c = new sesp_ctx();
     c->p = *p;
     if (set_device(c)) { delete c; return SESP_ECUDA; }
-    if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "stream"); }
+    if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        delete c;
+        return fail(SESP_ECUDA, "stream");
+    }
     for (int k = 0; k < 16; k++) cudaEventCreate(&c->ev[k]);
     init_force_kernels();
     init_constraint_kernels();
@@ -576,6 +604,9 @@ int sesp_destroy(sesp_ctx *c) {
     cudaStreamSynchronize(c->st);
     free_state(c);
     for (int k = 0; k < 16; k++) cudaEventDestroy(c->ev[k]);
+    cudaEventDestroy(c->ev_fork);
+    cudaEventDestroy(c->ev_join);
+    cudaStreamDestroy(c->st2);
     cudaStreamDestroy(c->st);
     delete c;
     return 0;
@@ -644,6 +675,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     Dev &d = c->d;
     memset(&d, 0, sizeof d);
     int N = nsite, M = nmol, C = ncell;
+    d.nsite = N;
     int e = 0;
     double **a12[12] = {&d.x, &d.y, &d.z, &d.vx, &d.vy, &d.vz, &d.ax, &d.ay, &d.az, &d.fx, &d.fy, &d.fz};
     for (auto q : a12) if ((e = dalloc(c, q, N))) return e;
@@ -659,7 +691,9 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.near_items_tmp, near_items_max(N, C))) || (e = dalloc(c, &d.near_cls, near_items_max(N, C))) ||
         (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 66)) ||
         (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
-        (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
+        (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.L4f, (size_t)LP * C)) ||
+        (e = dalloc(c, &d.fside, 3 * (size_t)N)) ||
+        (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
         (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
         (e = dalloc(c, &d.L2, (size_t)LP * n2)) || (e = dalloc(c, &d.counters, 8)) ||
         (e = dalloc(c, &d.ljt, NTYPE * NTYPE)) || (e = dalloc(c, &d.ljt32, NTYPE * NTYPE)) || (e = dalloc(c, &c->wmols, nwm)) || (e = dalloc(c, &c->smols, nsm)) ||

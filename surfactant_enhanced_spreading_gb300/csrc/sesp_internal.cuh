@@ -119,7 +119,7 @@ struct Dev {
     int2 *srt_meta;      // molecule, type
     int *srt_key;        // molecule << 5 | type
     double *nf;          // near + far force by slot [3 * nslot]
-    double *near_part;   // per partner row partial near force [9][3 * nslot]
+    double *near_part;   // per partner row partial near force [9][3 * nslot] (float on the mixed path)
     int2 *near_items;    // near-field work items (cell, row << 24 | chunk), most expensive first
     int2 *near_items_tmp;   // the same in cell order
     int *near_cls;       // cost class of each item in cell order
@@ -138,6 +138,8 @@ struct Dev {
     uint32_t *isub;
     // multipoles / local expansions (double2 = complex)
     double2 *O4, *L4, *O3, *L3, *O2, *L2;
+    float2 *L4f;         // FP32 copy of L4 (mixed path)
+    double *fside;       // graphite + intramolecular forces of the step, [3][nsite]; the site forces add and clear them
     double2 *op_m2m43, *op_m2m32, *op_l2l23, *op_l2l34;
     float2 *op32_m2m43, *op32_m2m32, *op32_l2l23, *op32_l2l34;   // FP32 copies for the mixed path
     // L2 M2L factors: H_l^q of every offset (45 per offset, (2 d2 + 1)^3
@@ -166,6 +168,7 @@ struct Dev {
     // counters: [0] fails, [1] overflow, [2] unlocated, [3] max cell, [5] pairs, [6] LJ pairs
     unsigned long long *counters;
     int max_cell;
+    int nsite;           // sites of all replicas (the stride of fside)
 };
 
 

@@ -93,10 +93,10 @@ def estimate_bytes(system: S.System) -> int:
     n3, n2 = ncell // 8, ncell // 64
     d2 = max(1, int((nc // 4).max()) - 1)
     w2 = 2 * d2 + 1
-    per_site = 12 * 8 + 1 + 4 * 4 + 32 + 16 + 8 + 4 + 3 * 8 + 27 * 8 + 6
+    per_site = 12 * 8 + 1 + 4 * 4 + 32 + 16 + 8 + 4 + 3 * 8 + 27 * 8 + 6 + 3 * 8
     per_mol = 5 * 4 + 2 * 8 + 4 + 4 + 2 * 4 + 2   # incl. the constraint halves' water lists and sweep counts
     cz = 25 * 16
-    cells = ncell * (5 * 4 + 2 * cz + 4 + 9 * 20) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
+    cells = ncell * (5 * 4 + 2 * cz + 4 + 9 * 20 + 25 * 8) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
     ops = (w2 ** 3 + 4 * 8) * 15 * 25 * 16 + w2 ** 3 * 45 * 24
     # real-form M2L at L4 and L3: operators, class-packed multipoles, partial
     # sums of 21 offset groups (FP64 sizes: an upper bound)
