@@ -233,12 +233,13 @@ def run_ours(args, ws, rank, local):
     ms_per_step = t_ms / args.steps
 
     # kernel launches in the timed region for this workload (waters, surfactants
-    # and graphite present): 9 per step (gather, pair field + finish, site
-    # forces, graphite, intramolecular, constraint half + eta for move_a, the
-    # constraint half for move_b) and 20 more per rebuild step (locate, sort 3,
-    # work items 3, isub, graphite list, water order 3, P2M, 2 M2M, 3 M2L, 2 L2L)
+    # and graphite present): 9 per step (gather, graphite and intramolecular on
+    # the side stream, pair field + finish, site forces, constraint half + eta
+    # for move_a, the constraint half for move_b) and 22 more per rebuild step
+    # (locate, sort 3, work items 5, isub, graphite list, water order 3, P2M,
+    # 2 M2M, multipole packing, 2 M2L, 2 L2L)
     n_rebuild = sum(1 for k in range(kb - args.steps, kb) if k % 10 == 0)
-    launches = 9 * args.steps + 20 * n_rebuild
+    launches = 9 * args.steps + 22 * n_rebuild
 
     # --- per-kernel durations over a second pass (events around kernel families)
     eng.enable_timing(True)

@@ -171,8 +171,8 @@ int sesp_set_eta(sesp_ctx *ctx, double eta);
 int sesp_energies(sesp_ctx *ctx, double out[8]);
 /* Launch shape of the pair field: target sites per work item (32 or 64, or
  * 128 on the mixed paths, up to 4 per lane) and CTAs per SM of its
- * persistent kernel.  The shape changes no result,
- * only the time.  sesp_autotune times every candidate on the current state
+ * persistent kernel (default: 64 at the largest CTAs per SM).  The shape
+ * changes no result, only the time.  sesp_autotune times every candidate on the current state
  * (a force call must have built the cell lists) and keeps the fastest:
  * out = {tile, ctas_per_sm, largest ctas_per_sm}.  New for the GPU build (the
  * reference has no launch shapes). */

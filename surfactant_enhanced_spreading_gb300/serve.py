@@ -13,6 +13,11 @@ their memory is released and the next requests are admitted.
 Every run is independent of the others (its own context; all kernels are
 deterministic), so its result is bit-identical whether it runs alone or in
 the mix - which tests/test_gpu_serve.py checks.
+
+A run whose SHAKE/RATTLE failure count passes `max_failures` between chunks
+has blown up (a state that has, collapses into a few cells and slows every
+later step by orders of magnitude): it is stopped, reported as failed with
+the steps it completed, and its memory goes to the next request.
 """
 from __future__ import annotations
 
@@ -48,6 +53,8 @@ class Result:
     device_bytes: int = 0
     estimate_bytes: int = 0
     shake_failures: int = 0     # SHAKE/RATTLE molecule failures over the run (engine counter 0)
+    steps_done: int = -1        # steps completed (-1: all of them)
+    failed: bool = False        # stopped after its failures passed the server's limit
 
     @property
     def latency(self) -> float:
@@ -113,11 +120,12 @@ def estimate_bytes(system: S.System) -> int:
 
 class Server:
     def __init__(self, budget_bytes: int, precision: int = E.MIXED, chunk: int = 100, max_active: int = 64,
-                 device: int = 0, keep_state: bool = True):
+                 device: int = 0, keep_state: bool = True, max_failures: int = 1000):
         self.budget = int(budget_bytes)
         self.precision = precision
         self.chunk = int(chunk)
         self.max_active = int(max_active)
+        self.max_failures = int(max_failures)
         self.device = device
         self.keep_state = keep_state
         self.peak_used = 0          # largest admitted estimate total seen by the last run()
@@ -157,7 +165,9 @@ class Server:
                     continue
                 a["running"] = False
                 req = a["req"]
-                if a["done"] < req.steps:
+                failures = int(eng.counters()[0])
+                failed = failures > self.max_failures
+                if a["done"] < req.steps and not failed:
                     n = min(self.chunk, req.steps - a["done"])
                     eng.run_async(a["kb"], n)
                     a["kb"] += n
@@ -169,7 +179,8 @@ class Server:
                 fin = clock() - t0
                 res = Result(rid=req.rid, n_sites=req.system.n_sites, steps=req.steps, arrival=req.arrival,
                              admitted=a["admitted"], finished=fin, device_bytes=a["actual"],
-                             estimate_bytes=a["est"], shake_failures=int(eng.counters()[0]))
+                             estimate_bytes=a["est"], shake_failures=failures,
+                             steps_done=a["done"] if failed else -1, failed=failed)
                 if self.keep_state:
                     pos, vel, _ = eng.state()
                     res.pos, res.vel, res.eta = pos, vel, eng.eta
@@ -191,12 +202,13 @@ class Server:
 
 def summarize(results: list[Result], wall: float | None = None) -> dict:
     lat = np.array([r.latency for r in results])
-    atom_steps = float(sum(r.n_sites * r.steps for r in results))
+    atom_steps = float(sum(r.n_sites * (r.steps if r.steps_done < 0 else r.steps_done) for r in results))
     span = wall if wall is not None else (max(r.finished for r in results) - min(r.arrival for r in results))
     return {"requests": len(results), "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)), "mean_latency_s": float(lat.mean()),
             "atom_steps_per_s": atom_steps / span if span > 0 else None, "span_s": span,
-            "shake_failures": int(sum(r.shake_failures for r in results))}
+            "shake_failures": int(sum(r.shake_failures for r in results)),
+            "failed_requests": [r.rid for r in results if r.failed]}
 
 
 def poisson_requests(n: int, rate_per_s: float, seed: int, water=(1000, 50000), surf=(0, 500), steps=(500, 5000),

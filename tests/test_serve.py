@@ -99,3 +99,60 @@ def test_graphite_covers_the_floor():
     for a in (0, 1):
         assert c[:, a].min() < -half[a] + step and c[:, a].max() > half[a] - step
     assert np.all(np.abs(c[:, :2]) < half[:2])
+
+
+def test_summary_counts_steps_done_of_failed_runs():
+    res = [serve.Result(rid=0, n_sites=10, steps=100, arrival=0.0, admitted=0.0, finished=1.0),
+           serve.Result(rid=1, n_sites=10, steps=100, arrival=0.0, admitted=0.0, finished=1.0, steps_done=30,
+                        failed=True, shake_failures=5000)]
+    s = serve.summarize(res)
+    assert s["failed_requests"] == [1] and s["shake_failures"] == 5000
+    assert abs(s["atom_steps_per_s"] - (10 * 100 + 10 * 30) / 1.0) < 1e-9
+
+
+class _FakeEngine:
+    """Host stand-in for an engine: its failure counter jumps after the
+    first chunk when the system has an odd number of waters."""
+    def __init__(self, system, precision, device=0):
+        self.system, self.chunks, self.eta = system, 0, 0.0
+
+    def force(self, rebuild=True):
+        pass
+
+    def init_accel(self):
+        pass
+
+    def device_bytes(self):
+        return 1 << 20
+
+    def run_async(self, kb, n):
+        self.chunks += 1
+
+    def busy(self):
+        return False
+
+    def sync(self):
+        pass
+
+    def counters(self):
+        bad = self.system.n_water % 2 == 1 and self.chunks >= 1
+        return [10 ** 6 if bad else 0] + [0] * 7
+
+    def state(self):
+        return None, None, None
+
+    def close(self):
+        pass
+
+
+def test_server_stops_a_blown_up_run(monkeypatch):
+    """A run whose failure count passes the limit between chunks is stopped
+    after the chunk that failed; the others run all their steps."""
+    monkeypatch.setattr(serve.E, "Engine", _FakeEngine)
+    reqs = [serve.Request(rid=k, system=S.System(n_water=300 + k, n_surf=0, cells=(4, 4, 4),
+                                                  pos=np.zeros((3 * (300 + k), 3)), vel=np.zeros((3 * (300 + k), 3)),
+                                                  carbons=np.zeros((0, 3)), graphite_on=False),
+                          steps=500, arrival=0.0) for k in range(2)]
+    res = serve.Server(1 << 40, chunk=100, keep_state=False).run(reqs)
+    assert [r.failed for r in res] == [False, True]
+    assert res[0].steps_done == -1 and res[1].steps_done == 100
