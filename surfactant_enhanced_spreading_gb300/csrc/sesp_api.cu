@@ -467,9 +467,11 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
     launch_gather(d, c->nsite, c->ncell, mixed, c->st);
     family(c, "gather");
     // graphite and intramolecular terms into the side forces (fside), on the
-    // side stream beside the far-field build and the pair field; in order on
-    // the main stream when kernels are timed or checked one by one
-    const bool fork = !c->timing && !c->sync_check;
+    // side stream beside the far-field build and the pair field on the mixed
+    // paths; in order on the main stream on the plain path (its FP64 pair
+    // field beside them ran a batched step at 581 ms against 259 ms in order)
+    // and when kernels are timed or checked one by one
+    const bool fork = mixed && !c->timing && !c->sync_check;
     if (fork) {
         cudaEventRecord(c->ev_fork, c->st);
         cudaStreamWaitEvent(c->st2, c->ev_fork, 0);
