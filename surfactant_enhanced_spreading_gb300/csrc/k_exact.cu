@@ -494,8 +494,8 @@ void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int
         if (ns) k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
     }
-    k_eta<<<nrep * ETA_BLOCKS, ETA_THREADS, 0, st>>>(d);
 }
+void launch_eta(const Dev &d, int nrep, cudaStream_t st) { k_eta<<<nrep * ETA_BLOCKS, ETA_THREADS, 0, st>>>(d); }
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nmol, int nsite, double tol,
                    int maxit, int fast, const ConstraintShape &sh, cudaStream_t st) {
     if (fast) {

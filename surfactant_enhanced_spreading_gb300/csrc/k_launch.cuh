@@ -22,6 +22,9 @@ void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nmol, int nsite, double tol,
                    int maxit, int fast, const ConstraintShape &sh, cudaStream_t st);
 void launch_init_accel(const Dev &d, int nsite, cudaStream_t st);
+// the eta update after the SHAKE half (reads the halves' kinetic sums; the
+// RATTLE half reads eta)
+void launch_eta(const Dev &d, int nrep, cudaStream_t st);
 
 // k_constraint.cu (mixed paths: FP64 or FP32 sweeps); false if the uploaded
 // bond graph is not the one the kernels are specialised for

@@ -349,7 +349,7 @@ struct sesp_ctx {
     // beside the far-field build and the pair field (fork after the gather,
     // join before the site forces)
     cudaStream_t st2 = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_eta = nullptr;
     NearShape near = {64, 0};   // pair-field launch shape (autotuned or set; results do not depend on it)
     ConstraintShape cshape = {0, 4, 1};   // constraint halves of the mixed paths (likewise)
     int n_sm = 0;               // streaming multiprocessors of the device
@@ -503,10 +503,20 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
     tstop(c, 4);
 }
 
-void seq_move_a(sesp_ctx *c) {
+// fork_eta: the eta update goes to the side stream, beside the next force
+// call, which joins it before the site forces (a step's sequence on the
+// mixed paths); otherwise it follows the SHAKE half on the main stream
+void seq_move_a(sesp_ctx *c, bool fork_eta = false) {
     tstart(c, 2);
     launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit,
                   c->p.precision, c->cshape, c->st);
+    if (fork_eta) {
+        cudaEventRecord(c->ev_eta, c->st);
+        cudaStreamWaitEvent(c->st2, c->ev_eta, 0);
+        launch_eta(c->d, c->nrep, c->st2);
+    } else {
+        launch_eta(c->d, c->nrep, c->st);
+    }
     family(c, "move_a");
     tstop(c, 2);
 }
@@ -570,7 +580,8 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_eta, cudaEventDisableTiming) != cudaSuccess) {
         delete c;
         return fail(SESP_ECUDA, "stream");
     }
@@ -608,6 +619,7 @@ int sesp_destroy(sesp_ctx *c) {
     for (int k = 0; k < 16; k++) cudaEventDestroy(c->ev[k]);
     cudaEventDestroy(c->ev_fork);
     cudaEventDestroy(c->ev_join);
+    cudaEventDestroy(c->ev_eta);
     cudaStreamDestroy(c->st2);
     cudaStreamDestroy(c->st);
     delete c;
@@ -1132,7 +1144,9 @@ static int launch_steps(sesp_ctx *c, int kb0, int nsteps) {
             if (!ge) {
                 cudaGraph_t g;
                 CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-                seq_move_a(c);
+                // on the mixed paths the force call forks its side stream and
+                // joins it before the site forces, which also joins the eta update
+                seq_move_a(c, c->p.precision != SESP_PLAIN_FP64);
                 seq_force(c, rb, SESP_T_ALL);
                 seq_move_b(c);
                 CK(cudaStreamEndCapture(c->st, &g));

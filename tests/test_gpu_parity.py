@@ -50,6 +50,18 @@ def test_force_terms_plain(pair, term):
     assert rel(fg, fo) < TOL_PLAIN, (term, rel(fg, fo))
 
 
+@pytest.mark.parametrize("precision,tol", [(E.PLAIN_FP64, TOL_PLAIN), (E.MIXED, TOL_MIXED)])
+def test_far_field_odd_class_grids(precision, tol):
+    """The M2L by parity class on a box whose class grids are odd and unequal
+    (12 x 20 x 8 cells: L4 classes 6 x 10 x 4, L3 classes 3 x 5 x 2, L2 3 x 5 x
+    2 boxes) and whose L2 offsets reach 4: far-field forces against the
+    oracle's direct window and all-pairs translation."""
+    s = S.droplet(300, 2, cells=(12, 20, 8), seed=5)
+    fo = O.Oracle(s).force(True, E.T_FAR)
+    fg = E.Engine(s, precision).force(True, E.T_FAR)
+    assert rel(fg, fo) < tol, rel(fg, fo)
+
+
 def test_force_frozen_lists(sys_small):
     """rebuild = 0 reuses the lists and local expansions of the last rebuild."""
     eng, orc = E.Engine(sys_small), O.Oracle(sys_small)
