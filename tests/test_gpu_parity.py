@@ -72,6 +72,42 @@ def test_force_frozen_lists(sys_small):
     assert rel(eng.force(False), orc.force(False)) < TOL_PLAIN
 
 
+def test_sites_on_cell_and_rank_faces():
+    """Water O sites moved (by under 0.05 sigma, whole molecules) onto cell
+    faces, rank faces and the faces of the rank-local ibox64 grid, each formed
+    in FP64 as the reference forms them: the cell location then takes its
+    exact-division branch, and every force term must still match the
+    oracle."""
+    s = S.droplet(600, 6, cells=(8, 8, 8), seed=24)
+    pos = s.pos.copy()
+    rs = S.RS
+    rhs = np.array(s.cells, dtype=np.float64) * rs / 2.0
+    nr = np.array(s.cells) // 4
+    rsd = np.array(s.cells, dtype=np.float64) * rs
+    faces = []
+    for a in range(3):
+        f = [-rhs[a] + k * rs for k in range(1, s.cells[a])]                         # cell faces
+        for rk in range(nr[a]):                                                       # ibox64 faces in each rank
+            c2 = rsd[a] * (rk + 1) / nr[a] - rhs[a] - rsd[a] / nr[a] / 2.0
+            f += [c2 - 2.0 * rs + k * rs for k in range(1, 4)]
+        faces.append(np.array(f))
+    moved = 0
+    for m in range(s.n_water):
+        o = pos[3 * m]
+        a = m % 3
+        d = faces[a] - o[a]
+        k = int(np.argmin(np.abs(d)))
+        if abs(d[k]) < 0.05:
+            pos[3 * m:3 * m + 3, a] += d[k]
+            pos[3 * m, a] = faces[a][k]   # exactly on the face
+            moved += 1
+    assert moved >= 20
+    t = S.System(n_water=s.n_water, n_surf=s.n_surf, cells=s.cells, pos=pos, vel=s.vel, carbons=s.carbons,
+                 graphite_on=s.graphite_on)
+    eng, orc = E.Engine(t), O.Oracle(t)
+    assert rel(eng.force(True), orc.force(True)) < TOL_PLAIN
+
+
 def test_reference_box_geometry():
     """The reference's 12 x 12 x 12-cell walled cube (3 x 3 x 3 ranks)."""
     s = S.droplet(1500, 20, cells=(12, 12, 12), seed=22)
