@@ -296,20 +296,14 @@ __global__ void k_near_items_scan(Dev d, int ncell) {
     for (int c = b; c < e; c++) { int v = d.near_icount[c]; d.near_icount[c] = acc; acc += v; }
 }
 
-// Items in cell order into near_items_tmp, each with a cost class:
-// floor(log2(targets x partners in its row)).
-__global__ void k_near_items_fill(Dev d, int ncell, int tile) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    const int ni = d.cstart[c + 1] - d.cstart[c];
-    if (ni == 0) return;
+// the work items of one cell, counted per cost class in the block's histogram
+__device__ inline void near_items_fill_cell(const Dev &d, int c, int ni, int tile, int *hist) {
     const Rep r = d.rep[d.crep[c]];
     int ix, iy, iz;
     cell_xyz(r, c, ix, iy, iz);
     const int mask = near_row_mask(r, iy, iz);
     const int nch = (ni + tile - 1) / tile;
     const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
-    int *bcount = d.near_ctl + 2;
     int k = d.near_icount[c];
     for (int pr = 0; pr < 9; pr++) {
         if (!(mask >> pr & 1)) continue;
@@ -320,10 +314,23 @@ __global__ void k_near_items_fill(Dev d, int ncell, int tile) {
             const int cls = 31 - __clz(nt * npart + 1);
             d.near_items_tmp[k] = make_int2(c, pr << 24 | ch);
             d.near_cls[k] = cls;
-            atomicAdd(&bcount[cls], 1);
+            atomicAdd(&hist[cls], 1);
             k++;
         }
     }
+}
+
+// Items in cell order into near_items_tmp, each with a cost class:
+// floor(log2(targets x partners in its row)).
+__global__ void k_near_items_fill(Dev d, int ncell, int tile) {
+    __shared__ int hist[32];   // the block's items per class, added to the global counts once
+    if (threadIdx.x < 32) hist[threadIdx.x] = 0;
+    __syncthreads();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ni = c < ncell ? d.cstart[c + 1] - d.cstart[c] : 0;
+    if (ni > 0) near_items_fill_cell(d, c, ni, tile, hist);
+    __syncthreads();
+    if (threadIdx.x < 32 && hist[threadIdx.x]) atomicAdd(&d.near_ctl[2 + threadIdx.x], hist[threadIdx.x]);
 }
 
 // start of each cost class in the final order, most expensive class first
@@ -338,10 +345,19 @@ __global__ void k_near_items_classes(Dev d) {
 // thread timing; it only decides which warp takes which item first, and every
 // item's arithmetic is the same whatever its position.
 __global__ void k_near_items_place(Dev d) {
+    __shared__ int cnt[32], base[32];   // the block's items per class and their reserved range
+    if (threadIdx.x < 32) cnt[threadIdx.x] = 0;
+    __syncthreads();
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= d.near_ctl[1]) return;
-    const int pos = atomicAdd(&d.near_ctl[34 + d.near_cls[k]], 1);
-    d.near_items[pos] = d.near_items_tmp[k];
+    int cls = -1, rank = 0;
+    if (k < d.near_ctl[1]) {
+        cls = d.near_cls[k];
+        rank = atomicAdd(&cnt[cls], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x < 32 && cnt[threadIdx.x]) base[threadIdx.x] = atomicAdd(&d.near_ctl[34 + threadIdx.x], cnt[threadIdx.x]);
+    __syncthreads();
+    if (cls >= 0) d.near_items[base[cls] + rank] = d.near_items_tmp[k];
 }
 
 void launch_near_items(const Dev &d, int ncell, int nitems_max, int tile, cudaStream_t st) {
@@ -792,8 +808,9 @@ __global__ void __launch_bounds__(128) k_m2m(Dev d, const double2 *Oc, double2 *
 // group order
 template <typename R, typename OP>
 __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, const int *brep, int level,
-                      const R *part, int G, float2 *Lf) {
-    const int b = blockIdx.x;
+                      const R *part, int G, float2 *Lf, int nbox) {
+    const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);   // one warp per child box
+    if (b >= nbox) return;
     const Rep r = d.rep[brep[b]];
     const int div = level == 3 ? 2 : 1;  // child grid = nc / div
     const int base_c = level == 3 ? r.l3_0 : r.cell0;
@@ -804,7 +821,7 @@ __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, cons
     int cx = l % nc[0], cy = (l / nc[0]) % nc[1], cz = l / (nc[0] * nc[1]);
     int ch = (cx & 1) + 2 * (cy & 1) + 4 * (cz & 1);
     int pi = base_p + cx / 2 + np[0] * (cy / 2 + np[1] * (cz / 2));
-    int o = threadIdx.x;
+    int o = threadIdx.x & 31;
     if (o >= LPH) return;
     R re = 0, im = 0;
     apply_op_r<R>(ops + ((size_t)ch * LPH + o) * LP, Lp + (size_t)pi * LP, re, im);
@@ -1056,9 +1073,10 @@ void fma_build(const Dev &d, int ncell, int n3, int n2, int d2, const OP *m43, c
     k_m2l_pack<R><<<((ncell + n3) * LP + 255) / 256, 256, 0, st>>>(d, ncell, n3);
     k_m2l_cls<R><<<dim3(d.m2c_nitems, d.m2c_groups), 32 * M2C_W, m2c_smem<R>(), st>>>(d);
     k_m2l_all<R><<<n2, 256, 0, st>>>(d, h2, cf, d2);
-    k_l2l<R><<<n3, 32, 0, st>>>(d, d.L2, d.L3, l23, d.b3rep, 3, (const R *)d.part3, d.m2c_groups, nullptr);
-    k_l2l<R><<<ncell, 32, 0, st>>>(d, d.L3, d.L4, l34, d.crep, 4, (const R *)d.part4, d.m2c_groups,
-                                   sizeof(R) == 4 ? d.L4f : nullptr);
+    k_l2l<R><<<(n3 + 3) / 4, 128, 0, st>>>(d, d.L2, d.L3, l23, d.b3rep, 3, (const R *)d.part3, d.m2c_groups, nullptr,
+                                          n3);
+    k_l2l<R><<<(ncell + 3) / 4, 128, 0, st>>>(d, d.L3, d.L4, l34, d.crep, 4, (const R *)d.part4, d.m2c_groups,
+                                             sizeof(R) == 4 ? d.L4f : nullptr, ncell);
 }
 
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {
