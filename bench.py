@@ -303,8 +303,7 @@ def run_ours(args, ws, rank, local):
         eng.set_state(hp, hv, ha, eta)
         eng.run(kb, 10)
         kb += 10
-        p2, v2, a2 = eng.state()
-        hp[...] = p2; hv[...] = v2; ha[...] = a2
+        eng.state(out=(hp, hv, ha))
         eta = eng.eta
     t_e2e = D.max(time.perf_counter() - t0)
     e2e_value = ws * n_sites * 10 * chunks / t_e2e

@@ -706,7 +706,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 66)) ||
         (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.L4f, (size_t)LP * C)) ||
-        (e = dalloc(c, &d.fside, 3 * (size_t)N)) ||
+        (e = dalloc(c, &d.fside, 3 * (size_t)N)) || (e = dalloc(c, &d.stage, 9 * (size_t)N)) ||
         (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
         (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
         (e = dalloc(c, &d.L2, (size_t)LP * n2)) || (e = dalloc(c, &d.counters, 8)) ||
@@ -1029,38 +1029,53 @@ int sesp_get_eta_batch(sesp_ctx *c, double *eta) {
     return 0;
 }
 
+// (3, n) site-major host arrays <-> the device's x / y / z arrays: one
+// contiguous copy per array through a device staging buffer, transposed by
+// a kernel (array k of the staging buffer at k * 3n)
+__global__ void k_state_io(Dev d, double *stage, int n, int mask, int unpack) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    double *soa[3][3] = {{d.x, d.y, d.z}, {d.vx, d.vy, d.vz}, {d.ax, d.ay, d.az}};
+    for (int k = 0; k < 3; k++) {
+        if (!(mask >> k & 1)) continue;
+        double *aos = stage + (size_t)k * 3 * n + 3 * (size_t)g;
+        for (int a = 0; a < 3; a++) {
+            if (unpack) soa[k][a][g] = aos[a];
+            else aos[a] = soa[k][a][g];
+        }
+    }
+}
+
 int sesp_download_state(sesp_ctx *c, double *pos, double *vel, double *acc) {
     if (int e = check_ctx(c, true)) return e;
     if (set_device(c)) return SESP_ECUDA;
-    int N = c->nsite;
-    std::vector<double> a(N), b(N), cc(N);
-    double *arrs[3][3] = {{c->d.x, c->d.y, c->d.z}, {c->d.vx, c->d.vy, c->d.vz}, {c->d.ax, c->d.ay, c->d.az}};
+    const int N = c->nsite;
     double *outs[3] = {pos, vel, acc};
-    for (int k = 0; k < 3; k++) {
-        if (!outs[k]) continue;
-        CK(cudaMemcpyAsync(a.data(), arrs[k][0], N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-        CK(cudaMemcpyAsync(b.data(), arrs[k][1], N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-        CK(cudaMemcpyAsync(cc.data(), arrs[k][2], N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-        CK(cudaStreamSynchronize(c->st));
-        for (int g = 0; g < N; g++) { outs[k][3 * g] = a[g]; outs[k][3 * g + 1] = b[g]; outs[k][3 * g + 2] = cc[g]; }
-    }
+    const int mask = (pos ? 1 : 0) | (vel ? 2 : 0) | (acc ? 4 : 0);
+    if (!mask) return 0;
+    k_state_io<<<(N + 255) / 256, 256, 0, c->st>>>(c->d, c->d.stage, N, mask, 0);
+    CK(cudaGetLastError());
+    for (int k = 0; k < 3; k++)
+        if (outs[k])
+            CK(cudaMemcpyAsync(outs[k], c->d.stage + (size_t)k * 3 * N, 3 * (size_t)N * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
     return 0;
 }
 
 int sesp_set_state(sesp_ctx *c, const double *pos, const double *vel, const double *acc, double eta) {
     if (int e = check_ctx(c, true)) return e;
     if (set_device(c)) return SESP_ECUDA;
-    int N = c->nsite;
-    std::vector<double> a(N), b(N), cc(N);
-    double *arrs[3][3] = {{c->d.x, c->d.y, c->d.z}, {c->d.vx, c->d.vy, c->d.vz}, {c->d.ax, c->d.ay, c->d.az}};
+    const int N = c->nsite;
     const double *ins[3] = {pos, vel, acc};
-    for (int k = 0; k < 3; k++) {
-        if (!ins[k]) continue;
-        for (int g = 0; g < N; g++) { a[g] = ins[k][3 * g]; b[g] = ins[k][3 * g + 1]; cc[g] = ins[k][3 * g + 2]; }
-        CK(cudaMemcpyAsync(arrs[k][0], a.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
-        CK(cudaMemcpyAsync(arrs[k][1], b.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
-        CK(cudaMemcpyAsync(arrs[k][2], cc.data(), N * sizeof(double), cudaMemcpyHostToDevice, c->st));
-        CK(cudaStreamSynchronize(c->st));
+    const int mask = (pos ? 1 : 0) | (vel ? 2 : 0) | (acc ? 4 : 0);
+    for (int k = 0; k < 3; k++)
+        if (ins[k])
+            CK(cudaMemcpyAsync(c->d.stage + (size_t)k * 3 * N, ins[k], 3 * (size_t)N * sizeof(double),
+                               cudaMemcpyHostToDevice, c->st));
+    if (mask) {
+        k_state_io<<<(N + 255) / 256, 256, 0, c->st>>>(c->d, c->d.stage, N, mask, 1);
+        CK(cudaGetLastError());
     }
     CK(cudaMemcpyAsync(c->d.eta, &eta, sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));

@@ -246,8 +246,16 @@ class Engine:
         _check(_lib.sesp_device_bytes(self._h, ctypes.byref(v)))
         return v.value
 
-    def state(self):
-        pos, vel, acc = (np.empty((self.n, 3)) for _ in range(3))
+    def state(self, out=None):
+        """(pos, vel, acc) as (n, 3) float64 arrays; ``out``: three such
+        C-contiguous arrays to fill instead (e.g. pinned host buffers)."""
+        if out is None:
+            pos, vel, acc = (np.empty((self.n, 3)) for _ in range(3))
+        else:
+            pos, vel, acc = out
+            for a in out:
+                if a.shape != (self.n, 3) or a.dtype != np.float64 or not a.flags.c_contiguous:
+                    raise ValueError("state(out=...) needs three C-contiguous (n, 3) float64 arrays")
         _check(_lib.sesp_download_state(self._h, _dp(pos), _dp(vel), _dp(acc)))
         return pos, vel, acc
 

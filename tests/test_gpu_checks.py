@@ -1,6 +1,7 @@
 """Diagnostics on the GPU: the reference's consistency checks (molecule
 count, total charge, O and H counts) and its temperature-rescaling variant,
-through the C ABI, against counts and sums taken on the host."""
+through the C ABI, against counts and sums taken on the host; and the state
+transfers of the C ABI."""
 import numpy as np
 import pytest
 
@@ -65,3 +66,22 @@ def test_rescale_temperature_with_reference_velocities():
     with pytest.raises(E.SespError):
         eng.rescale_temperature(0.0)
     eng.close()
+
+
+def test_state_round_trip_through_the_staging_buffer():
+    """sesp_set_state / sesp_download_state move (n, 3) arrays through one
+    copy each and a transposing kernel: exact round trip, partial uploads
+    leave the other arrays alone, and state(out=...) fills caller buffers."""
+    s = S.droplet(300, 3, cells=(8, 8, 8), seed=9)
+    eng = E.Engine(s, E.MIXED)
+    rng = np.random.default_rng(1)
+    p, v, a = (s.pos + 1e-3 * rng.normal(size=s.pos.shape) for _ in range(3))
+    eng.set_state(p, v, a, eta=0.25)
+    p2, v2, a2 = eng.state()
+    assert np.array_equal(p2, p) and np.array_equal(v2, v) and np.array_equal(a2, a)
+    assert eng.eta == 0.25
+    v3 = v * 2.0
+    eng.set_state(vel=v3, eta=0.5)
+    out = tuple(np.empty_like(p) for _ in range(3))
+    eng.state(out=out)
+    assert np.array_equal(out[0], p) and np.array_equal(out[1], v3) and np.array_equal(out[2], a)
