@@ -706,7 +706,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 66)) ||
         (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.L4f, (size_t)LP * C)) ||
-        (e = dalloc(c, &d.fside, 3 * (size_t)N)) || (e = dalloc(c, &d.stage, 9 * (size_t)N)) ||
+        (e = dalloc(c, &d.fside, 3 * (size_t)N)) || (e = dalloc(c, &d.stage, 12 * (size_t)N)) ||
         (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
         (e = dalloc(c, &d.L3, (size_t)LP * n3)) || (e = dalloc(c, &d.O2, (size_t)LP * n2)) ||
         (e = dalloc(c, &d.L2, (size_t)LP * n2)) || (e = dalloc(c, &d.counters, 8)) ||
@@ -1031,12 +1031,13 @@ int sesp_get_eta_batch(sesp_ctx *c, double *eta) {
 
 // (3, n) site-major host arrays <-> the device's x / y / z arrays: one
 // contiguous copy per array through a device staging buffer, transposed by
-// a kernel (array k of the staging buffer at k * 3n)
+// a kernel (array k of the staging buffer at k * 3n: positions, velocities,
+// accelerations, forces)
 __global__ void k_state_io(Dev d, double *stage, int n, int mask, int unpack) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= n) return;
-    double *soa[3][3] = {{d.x, d.y, d.z}, {d.vx, d.vy, d.vz}, {d.ax, d.ay, d.az}};
-    for (int k = 0; k < 3; k++) {
+    double *soa[4][3] = {{d.x, d.y, d.z}, {d.vx, d.vy, d.vz}, {d.ax, d.ay, d.az}, {d.fx, d.fy, d.fz}};
+    for (int k = 0; k < 4; k++) {
         if (!(mask >> k & 1)) continue;
         double *aos = stage + (size_t)k * 3 * n + 3 * (size_t)g;
         for (int a = 0; a < 3; a++) {
@@ -1101,13 +1102,11 @@ int sesp_download_forces(sesp_ctx *c, double *f) {
     if (int e = check_ctx(c, true)) return e;
     if (!f) return fail(SESP_EINVAL, "null output");
     if (set_device(c)) return SESP_ECUDA;
-    int N = c->nsite;
-    std::vector<double> a(N), b(N), cc(N);
-    CK(cudaMemcpyAsync(a.data(), c->d.fx, N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-    CK(cudaMemcpyAsync(b.data(), c->d.fy, N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-    CK(cudaMemcpyAsync(cc.data(), c->d.fz, N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    const int N = c->nsite;
+    k_state_io<<<(N + 255) / 256, 256, 0, c->st>>>(c->d, c->d.stage, N, 8, 0);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(f, c->d.stage + (size_t)9 * N, 3 * (size_t)N * sizeof(double), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
-    for (int g = 0; g < N; g++) { f[3 * g] = a[g]; f[3 * g + 1] = b[g]; f[3 * g + 2] = cc[g]; }
     return 0;
 }
 

@@ -140,7 +140,7 @@ struct Dev {
     double2 *O4, *L4, *O3, *L3, *O2, *L2;
     float2 *L4f;         // FP32 copy of L4 (mixed path)
     double *fside;       // graphite + intramolecular forces of the step, [3][nsite]; the site forces add and clear them
-    double *stage;       // state transfers: positions, velocities, accelerations as (3, nsite) site-major arrays
+    double *stage;       // transfers: positions, velocities, accelerations, forces as (3, nsite) site-major arrays
     double2 *op_m2m43, *op_m2m32, *op_l2l23, *op_l2l34;
     float2 *op32_m2m43, *op32_m2m32, *op32_l2l23, *op32_l2l34;   // FP32 copies for the mixed path
     // L2 M2L factors: H_l^q of every offset (45 per offset, (2 d2 + 1)^3

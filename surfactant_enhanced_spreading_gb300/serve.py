@@ -100,7 +100,7 @@ def estimate_bytes(system: S.System) -> int:
     n3, n2 = ncell // 8, ncell // 64
     d2 = max(1, int((nc // 4).max()) - 1)
     w2 = 2 * d2 + 1
-    per_site = 12 * 8 + 1 + 4 * 4 + 32 + 16 + 8 + 4 + 3 * 8 + 27 * 8 + 6 + 3 * 8 + 9 * 8
+    per_site = 12 * 8 + 1 + 4 * 4 + 32 + 16 + 8 + 4 + 3 * 8 + 27 * 8 + 6 + 3 * 8 + 12 * 8
     per_mol = 5 * 4 + 2 * 8 + 4 + 4 + 2 * 4 + 2   # incl. the constraint halves' water lists and sweep counts
     cz = 25 * 16
     cells = ncell * (5 * 4 + 2 * cz + 4 + 9 * 20 + 25 * 8) + n3 * (4 + 2 * cz) + n2 * (4 + 2 * cz)
