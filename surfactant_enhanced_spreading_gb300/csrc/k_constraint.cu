@@ -727,6 +727,7 @@ __device__ __forceinline__ bool mol_ok(const Dev &d, const CPlan &p, int m, int 
 
 template <typename C, bool SHAKE>
 __global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double tol, int maxit) {
+    griddep_wait();
     constexpr int NF = SHAKE ? 16 : 11;
     extern __shared__ __align__(16) unsigned char cs_smem[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -889,7 +890,7 @@ void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, int nmol
     const int need = (groups + p.s_warps - 1) / p.s_warps;
     p.n_scta = ns ? (need < sh.grid ? need : sh.grid) : 0;
     const size_t smem = p.n_scta ? surf_smem<C, SHAKE>(p.s_warps, p.mpw) : 0;
-    k_constrain<C, SHAKE><<<sh.grid, CW_THREADS, smem, st>>>(d, p, tol, maxit);
+    launch_pdl(k_constrain<C, SHAKE>, dim3(sh.grid), dim3(CW_THREADS), smem, st, d, p, tol, maxit);
 }
 }  // namespace
 

@@ -141,7 +141,9 @@ __device__ inline double cell_centre(const Dev &d, const Rep &r, int a, int i) {
 }
 
 __global__ void k_gather(Dev d, int nslot, int ncell, int mixed) {
+    griddep_wait();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0) d.near_ctl[0] = 0;   // the pair field's work counter
     if (s >= nslot || s >= d.cstart[ncell]) return;
     int g = d.srt_site[s];
     double x = d.x[g], y = d.y[g], z = d.z[g];
@@ -158,7 +160,8 @@ __global__ void k_gather(Dev d, int nslot, int ncell, int mixed) {
 }
 
 void launch_gather(const Dev &d, int nslot, int ncell, int mixed, cudaStream_t st) {
-    if (nslot) k_gather<<<(nslot + 255) / 256, 256, 0, st>>>(d, nslot, ncell, mixed);
+    launch_pdl(k_gather, dim3((nslot + 255) / 256 > 0 ? (nslot + 255) / 256 : 1), dim3(256), 0, st, d, nslot, ncell,
+               mixed);
 }
 
 // ------------------------------------------------------------------ solid harmonics
@@ -540,6 +543,7 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 // in FP32 over one row (at most 3 cells).
 template <bool MIXED, int KMAX>
 __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int tile) {
+    griddep_wait();
     __shared__ float2 s_lj32[MIXED ? NTYPE * NTYPE : 1];
     __shared__ double2 s_lj64[MIXED ? 1 : NTYPE * NTYPE];
     if constexpr (MIXED) {
@@ -612,6 +616,7 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
 // src/evalLjk4.f90:31-282 for every slot; writes nf.
 template <bool MIXED>
 __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
+    griddep_wait();
     typedef typename std::conditional<MIXED, float, double>::type R;
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= nslot || s >= d.cstart[ncell]) return;
@@ -661,15 +666,20 @@ int near_max_ctas_per_sm(int mixed, int tile) {
     return nb > 0 ? nb : 1;
 }
 
-void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st) {
+// reset_counter: the work counter is cleared here (otherwise the step's
+// gather kernel has cleared it)
+void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st,
+                 bool reset_counter) {
     if (terms & SESP_T_NEAR) {
-        cudaMemsetAsync(d.near_ctl, 0, sizeof(int), st);
-        if (mixed && shape.tile > 64) k_near<true, 4><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
-        else if (mixed) k_near<true, 2><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
-        else k_near<false, 2><<<shape.grid, NEAR_THREADS, 0, st>>>(d, nslot, shape.tile);
+        if (reset_counter) cudaMemsetAsync(d.near_ctl, 0, sizeof(int), st);
+        const dim3 g(shape.grid), b(NEAR_THREADS);
+        if (mixed && shape.tile > 64) launch_pdl(k_near<true, 4>, g, b, 0, st, d, nslot, shape.tile);
+        else if (mixed) launch_pdl(k_near<true, 2>, g, b, 0, st, d, nslot, shape.tile);
+        else launch_pdl(k_near<false, 2>, g, b, 0, st, d, nslot, shape.tile);
     }
-    if (mixed) k_near_finish<true><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
-    else k_near_finish<false><<<(nslot + 127) / 128, 128, 0, st>>>(d, nslot, ncell, terms);
+    const dim3 g((nslot + 127) / 128 > 0 ? (nslot + 127) / 128 : 1), b(128);
+    if (mixed) launch_pdl(k_near_finish<true>, g, b, 0, st, d, nslot, ncell, terms);
+    else launch_pdl(k_near_finish<false>, g, b, 0, st, d, nslot, ncell, terms);
 }
 
 // ------------------------------------------------------------------ multipoles
@@ -1133,6 +1143,7 @@ __device__ inline float pow13f(float v) { float v2 = v * v, v4 = v2 * v2, v8 = v
 
 template <bool MIXED>
 __global__ void k_site_forces(Dev d, int nsite, int terms) {
+    griddep_wait();
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nsite) return;
     const Rep r = d.rep[d.mrep[d.smol[g]]];
@@ -1267,8 +1278,9 @@ void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st) {
 }
 
 void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st) {
-    if (mixed) k_site_forces<true><<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
-    else k_site_forces<false><<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, terms);
+    const dim3 g((nsite + 255) / 256), b(256);
+    if (mixed) launch_pdl(k_site_forces<true>, g, b, 0, st, d, nsite, terms);
+    else launch_pdl(k_site_forces<false>, g, b, 0, st, d, nsite, terms);
 }
 
 void launch_graphite(const Dev &d, int terms, int mixed, cudaStream_t st) {

@@ -50,7 +50,8 @@ struct NearShape {
 };
 void launch_near_items(const Dev &d, int ncell, int nitems_max, int tile, cudaStream_t st);
 int near_max_ctas_per_sm(int mixed, int tile);
-void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st);
+void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st,
+                 bool reset_counter);
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st);
 void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st);
 void launch_graphite(const Dev &d, int terms, int mixed, cudaStream_t st);

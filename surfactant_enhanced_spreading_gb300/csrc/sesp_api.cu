@@ -486,7 +486,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         tstop(c, 6);
     }
     tstart(c, 0);
-    launch_near(d, c->ncell, c->nsite, mixed, terms, c->near, c->st);
+    launch_near(d, c->ncell, c->nsite, mixed, terms, c->near, c->st, false);
     family(c, "near field");
     tstop(c, 0);
     tstart(c, 4);
@@ -1346,11 +1346,11 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
             const int cps = cands[k];
             if (cps < 1 || (k > 0 && cps == cands[k - 1])) continue;
             const NearShape sh = {tile, c->n_sm * cps};
-            launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st);   // warm
+            launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st, true);   // warm
             float t[5];
             for (int r = 0; r < 5; r++) {
                 cudaEventRecord(e0, c->st);
-                launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st);
+                launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st, true);
                 cudaEventRecord(e1, c->st);
                 cudaEventSynchronize(e1);
                 cudaEventElapsedTime(&t[r], e0, e1);

@@ -13,11 +13,32 @@
 
 #include <cstdint>
 #include <type_traits>
+#include <utility>
 #include <cuda_runtime.h>
 
 #include "../../include/sesp.h"
 
 namespace sesp {
+
+// Programmatic dependent launch: a kernel launched by launch_pdl may be
+// scheduled while its stream predecessor finishes, and calls griddep_wait()
+// first, which returns once that predecessor has completed and its writes
+// are visible (and at once after an ordinary launch).
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+template <typename... K, typename... A>
+inline cudaError_t launch_pdl(void (*k)(K...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<A>(args)...);
+}
 
 constexpr int P = 4;
 constexpr int LP = 25;        // (P+1)^2 coefficients
