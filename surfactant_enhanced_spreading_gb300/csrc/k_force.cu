@@ -688,6 +688,7 @@ void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const
 //                                          = sum q rfctr(n,m) conj(T_n^m)
 template <typename R>
 __global__ void k_p2m(Dev d) {
+    griddep_wait();
     const int c = blockIdx.x;
     const int s0 = d.cstart[c], n = d.cstart[c + 1] - s0;
     const Rep r = d.rep[d.crep[c]];
@@ -785,6 +786,7 @@ __device__ inline void apply_op_r(const OP *op, const double2 *in, R &re, R &im)
 template <typename R, typename OP>
 __global__ void __launch_bounds__(128) k_m2m(Dev d, const double2 *Oc, double2 *Op, const OP *ops, const int *brep,
                                              int level) {
+    griddep_wait();
     __shared__ R sre[8][LPH], sim[8][LPH];
     const int b = blockIdx.x;
     const Rep r = d.rep[brep[b]];
@@ -819,6 +821,7 @@ __global__ void __launch_bounds__(128) k_m2m(Dev d, const double2 *Oc, double2 *
 template <typename R, typename OP>
 __global__ void k_l2l(Dev d, const double2 *Lp, double2 *Lc, const OP *ops, const int *brep, int level,
                       const R *part, int G, float2 *Lf, int nbox) {
+    griddep_wait();
     const int b = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);   // one warp per child box
     if (b >= nbox) return;
     const Rep r = d.rep[brep[b]];
@@ -910,6 +913,7 @@ __device__ __forceinline__ void m2l_acc(const C2<R> *__restrict__ H, const S *sr
 // multipoles of L4 and L3 to the class-packed real layout (margins stay zero)
 template <typename R>
 __global__ void k_m2l_pack(Dev d, int ncell, int n3) {
+    griddep_wait();
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (ncell + n3) * LP) return;
     const int i = idx % LP, c = idx / LP;
@@ -964,6 +968,7 @@ __device__ __forceinline__ void m2c_row(const double *op, double va, double vb, 
 
 template <typename R>
 __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d) {
+    griddep_wait();
     extern __shared__ __align__(16) unsigned char smraw[];
     R *sop = (R *)smraw;   // [M2C_CH][LP][M2C_LD]
     const int4 it = d.m2c_items[blockIdx.x];
@@ -1036,6 +1041,7 @@ __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d) {
 // output o; the 16 half-warps' sums are added in a fixed order
 template <typename R>
 __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const R *cf, int d2) {
+    griddep_wait();
     __shared__ R scf[LPH * LP];
     __shared__ R sre[16][LPH], sim[16][LPH];
     const int b = blockIdx.x;
@@ -1077,16 +1083,18 @@ size_t m2c_smem() { return sizeof(R) * M2C_CH * LP * M2C_LD; }
 template <typename R, typename OP>
 void fma_build(const Dev &d, int ncell, int n3, int n2, int d2, const OP *m43, const OP *m32, const OP *l23,
                const OP *l34, const C2<R> *h2, const R *cf, cudaStream_t st) {
-    k_p2m<R><<<ncell, 64, 0, st>>>(d);
-    k_m2m<R><<<n3, 128, 0, st>>>(d, d.O4, d.O3, m43, d.b3rep, 3);
-    k_m2m<R><<<n2, 128, 0, st>>>(d, d.O3, d.O2, m32, d.b2rep, 2);
-    k_m2l_pack<R><<<((ncell + n3) * LP + 255) / 256, 256, 0, st>>>(d, ncell, n3);
-    k_m2l_cls<R><<<dim3(d.m2c_nitems, d.m2c_groups), 32 * M2C_W, m2c_smem<R>(), st>>>(d);
-    k_m2l_all<R><<<n2, 256, 0, st>>>(d, h2, cf, d2);
-    k_l2l<R><<<(n3 + 3) / 4, 128, 0, st>>>(d, d.L2, d.L3, l23, d.b3rep, 3, (const R *)d.part3, d.m2c_groups, nullptr,
-                                          n3);
-    k_l2l<R><<<(ncell + 3) / 4, 128, 0, st>>>(d, d.L3, d.L4, l34, d.crep, 4, (const R *)d.part4, d.m2c_groups,
-                                             sizeof(R) == 4 ? d.L4f : nullptr, ncell);
+    // one chain of dependent launches (programmatic: each waits for its predecessor first)
+    launch_pdl(k_p2m<R>, dim3(ncell), dim3(64), 0, st, d);
+    launch_pdl(k_m2m<R, OP>, dim3(n3), dim3(128), 0, st, d, d.O4, d.O3, m43, d.b3rep, 3);
+    launch_pdl(k_m2m<R, OP>, dim3(n2), dim3(128), 0, st, d, d.O3, d.O2, m32, d.b2rep, 2);
+    launch_pdl(k_m2l_pack<R>, dim3(((ncell + n3) * LP + 255) / 256), dim3(256), 0, st, d, ncell, n3);
+    launch_pdl(k_m2l_cls<R>, dim3(d.m2c_nitems, d.m2c_groups), dim3(32 * M2C_W), m2c_smem<R>(), st, d);
+    launch_pdl(k_m2l_all<R>, dim3(n2), dim3(256), 0, st, d, h2, cf, d2);
+    launch_pdl(k_l2l<R, OP>, dim3((n3 + 3) / 4), dim3(128), 0, st, d, (const double2 *)d.L2, d.L3, l23,
+               (const int *)d.b3rep, 3, (const R *)d.part3, d.m2c_groups, (float2 *)nullptr, n3);
+    launch_pdl(k_l2l<R, OP>, dim3((ncell + 3) / 4), dim3(128), 0, st, d, (const double2 *)d.L3, d.L4, l34,
+               (const int *)d.crep, 4, (const R *)d.part4, d.m2c_groups, sizeof(R) == 4 ? d.L4f : (float2 *)nullptr,
+               ncell);
 }
 
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {
