@@ -13,7 +13,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["orc_setup.c", "orc_pair.c", "orc_fma.c", "orc_intra.c", "orc_move.c", "orc_api.c"]
+SOURCES = ["orc_setup.c", "orc_pair.c", "orc_fma.c", "orc_intra.c", "orc_move.c", "orc_api.c", "orc_cfg.c"]
 LIB = os.path.join(HERE, "liborc.so")
 
 

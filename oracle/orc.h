@@ -130,6 +130,14 @@ void orc_eval_pairs_neighbour(orc_sys *s);   /* src/mybox.f90:185-217 */
 void orc_fma_build(orc_sys *s);
 void orc_evalLjk4(orc_sys *s);
 double orc_fma_energy(const orc_sys *s);
+/* single expansion operations of the same formulas (used by orc_cfg.c) */
+void orc_p2m_add(double complex *O, double q, double dx, double dy, double dz);
+void orc_m2m_apply(const double complex *O, double dx, double dy, double dz, double complex *Op);
+void orc_m2l_apply(const double complex *O, double dx, double dy, double dz, double complex *L);
+void orc_l2l_apply(const double complex *L, double dx, double dy, double dz, double complex *Lc);
+void orc_l2p_apply(const double complex *L, double rx, double ry, double rz, double rqq, double *fx, double *fy,
+                   double *fz, double *phi);
+double orc_legendre(int l, int m, double x);
 
 /* intramolecular, external (src/eval_valence.f90 ... src/eval_graphite.f90) */
 void orc_eval_valence(orc_sys *s);

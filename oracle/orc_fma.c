@@ -20,27 +20,35 @@ static inline int gidx(int n, int m) { return n * (n + 1) + m; }
 static inline double fact(int n) { return T.rifact[n + 1]; }
 static inline double neg1pow(int n) { return (n % 2 == 0) ? 1.0 : -1.0; }
 
-/* Associated Legendre function with the Condon-Shortley phase, restated from
- * its standard three-term recurrence in l (P_m^m, P_{m+1}^m, then upward).
- * Conventions of src/rLegendreP.f90:11-19: P(-1,0) = 1 and P(l,m) = 0 for m > l. */
+/* binomial coefficient C(n, k) from the factorial table */
+static inline double binom(int n, int k) { return fact(n) / (fact(k) * fact(n - k)); }
+
+/* Associated Legendre function P_l^m(x) with the Condon-Shortley phase, from
+ * the explicit polynomial that Rodrigues' formula gives when the m-th
+ * derivative of P_l(x) = 2^-l sum_k (-1)^k C(l,k) C(2l-2k,l) x^(l-2k) is taken
+ * term by term (Abramowitz & Stegun 8.6.6 with 22.3.8):
+ *   P_l^m(x) = (-1)^m (1-x^2)^(m/2) 2^-l
+ *              sum_{k=0}^{(l-m)/2} (-1)^k C(l,k) C(2l-2k,l) (l-2k)! / (l-2k-m)! x^(l-2k-m).
+ * The reference's edge conventions are kept (src/rLegendreP.f90:11-19):
+ * P(-1,0) = 1 and P(l,m) = 0 for m > l.  Orders here stay at l <= 2p = 8,
+ * where the sum has at most 5 terms. */
 static double legendre(int l, int m, double x) {
     if (l == -1 && m == 0) return 1.0;
     if (m > l) return 0.0;
-    double pmm = 1.0;
-    if (m > 0) {
-        double s = sqrt((1.0 - x) * (1.0 + x));
-        double oddf = 1.0;
-        for (int i = 1; i <= m; i++) { pmm = -pmm * oddf * s; oddf += 2.0; }
+    double sum = 0.0;
+    for (int k = 0; 2 * k <= l - m; k++) {
+        const int p = l - 2 * k - m;
+        double xp = 1.0;
+        for (int i = 0; i < p; i++) xp *= x;
+        const double c = binom(l, k) * binom(2 * l - 2 * k, l) * fact(l - 2 * k) / fact(p);
+        sum += (k % 2 ? -c : c) * xp;
     }
-    if (l == m) return pmm;
-    double p1 = x * (2 * m + 1) * pmm;
-    if (l == m + 1) return p1;
-    double p0 = pmm, pl = 0.0;
-    for (int ll = m + 2; ll <= l; ll++) {
-        pl = (x * (2 * ll - 1) * p1 - (ll + m - 1) * p0) / (ll - m);
-        p0 = p1; p1 = pl;
-    }
-    return pl;
+    double w = 1.0;   /* (1 - x^2)^(m/2) */
+    const double s = sqrt((1.0 - x) * (1.0 + x));
+    for (int i = 0; i < m; i++) w *= s;
+    double two_l = 1.0;
+    for (int i = 0; i < l; i++) two_l *= 2.0;
+    return (m % 2 ? -w : w) * sum / two_l;
 }
 
 /* Ylm, src/ifma.f90:12-26 */
@@ -419,4 +427,33 @@ double orc_fma_energy(const orc_sys *s) {
     }
     free(site); free(q);
     return e;
+}
+
+/* ---- single-operation entry points for the configuration-preset oracle
+ * (orc_cfg.c), which builds its own periodic interaction lists on top of
+ * the same expansion formulas. */
+
+/* P2M of one charge at (dx, dy, dz) from the cell centre,
+ * src/computeOnm4.f90:142-162: O_n^m += q rho^n Y(n, -m) */
+void orc_p2m_add(double complex *O, double q, double dx, double dy, double dz) {
+    double rho, al, be;
+    sph(dx, dy, dz, &rho, &al, &be);
+    for (int nn = 0; nn <= ORC_P; nn++)
+        for (int m = 0; m <= nn; m++) {
+            double complex v = q * ipow(rho, nn) * Ylm(nn, -m, al, be);
+            O[gidx(nn, m)] += v;
+            if (m > 0) O[gidx(nn, -m)] += conj(v);
+        }
+}
+void orc_m2m_apply(const double complex *O, double dx, double dy, double dz, double complex *Op) { m2m(O, dx, dy, dz, Op); }
+void orc_m2l_apply(const double complex *O, double dx, double dy, double dz, double complex *L) { m2l(O, dx, dy, dz, L); }
+void orc_l2l_apply(const double complex *L, double dx, double dy, double dz, double complex *Lc) { l2l(L, dx, dy, dz, Lc); }
+void orc_l2p_apply(const double complex *L, double rx, double ry, double rz, double rqq, double *fx, double *fy,
+                   double *fz, double *phi) {
+    l2p(L, rx, ry, rz, rqq, fx, fy, fz, phi);
+}
+/* the associated Legendre function above (exported for its test) */
+double orc_legendre(int l, int m, double x) {
+    if (T.rifact[1] == 0.0) orc_init_tables();
+    return legendre(l, m, x);
 }

@@ -66,16 +66,24 @@ class System:
     vel: np.ndarray
     carbons: np.ndarray   # (n_c, 3) float64
     graphite_on: bool = True
+    preset: int = 0       # 0: the reference's force field; 1: the configuration preset (config_preset.py)
+
+    @property
+    def sites_per_surf(self) -> int:
+        return N_SURF_SITE if self.preset == 0 else 12
 
     @property
     def n_sites(self) -> int:
-        return 3 * self.n_water + N_SURF_SITE * self.n_surf
+        return 3 * self.n_water + self.sites_per_surf * self.n_surf
 
     @property
     def half_box(self) -> np.ndarray:
         return np.array(self.cells, dtype=np.float64) * RS / 2.0
 
     def masses(self) -> np.ndarray:
+        if self.preset:
+            from .config_preset import CHAIN_MASS
+            return np.concatenate([np.tile(WATER_MASS, self.n_water), np.tile(CHAIN_MASS, self.n_surf)])
         return np.concatenate([np.tile(WATER_MASS, self.n_water), np.tile(SURF_MASS, self.n_surf)])
 
     def copy(self) -> "System":
