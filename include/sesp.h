@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define SESP_ABI_VERSION 1
+#define SESP_ABI_VERSION 2
 
 /* error codes */
 #define SESP_OK 0
@@ -64,7 +64,27 @@ extern "C" {
 #define SESP_T_SUBTRACT 64   /* src/eval_subtract_fma.f90                     */
 #define SESP_T_WALL 128      /* src/eval_wall.f90                             */
 #define SESP_T_GRAPHITE 256  /* src/eval_graphite.f90                         */
-#define SESP_T_ALL 511
+#define SESP_T_BOND 512      /* harmonic chain bonds (configuration preset)   */
+#define SESP_T_ALL 1023
+
+/* force field and boundaries (sesp_params.preset) */
+#define SESP_PRESET_REFERENCE 0  /* the reference's: SPC/E water, 29-site
+                                    trisiloxane surfactants with rigid bonds,
+                                    closed box with walls (src/init_arrays.f90,
+                                    src/eval_wall.f90)                       */
+#define SESP_PRESET_CONFIG 1     /* the benchmark configurations': SPC water
+                                    (O -0.82 / H +0.41), 12-bead united-atom
+                                    chains with harmonic bonds (1.53 A), 112
+                                    degree angles and triple-cosine dihedrals,
+                                    graphite with Lorentz-Berthelot carbon
+                                    parameters (sigma 3.4 A, eps 0.23 kJ/mol)
+                                    on every LJ site of the bottom cell
+                                    layers, box periodic in x and y (far field
+                                    over the 3 x 3 supercell of images), walls
+                                    at the z faces only.  Cells: multiples of
+                                    4, at least 8 in x and y.  Surfactants are
+                                    the 12-bead chains; the constraint count
+                                    per chain is 0.                          */
 
 typedef struct sesp_ctx sesp_ctx;
 
@@ -84,12 +104,19 @@ typedef struct {
     int shake_maxit;       /* 100 (src/move_w1_a.f90:20)                      */
     int device;            /* CUDA device ordinal                             */
     int max_cell_sites;    /* capacity of one cell, 0 = default (1024)        */
+    int preset;            /* SESP_PRESET_REFERENCE (default) or
+                              SESP_PRESET_CONFIG; sesp_default_config_params
+                              fills the configuration preset's settings       */
 } sesp_params;
 
 /* library and error handling */
 int sesp_abi_version(void);
 int sesp_last_error(char *buf, size_t len);
 int sesp_default_params(sesp_params *p);
+/* the configuration preset's defaults: n_cells 8 x 8 x 8, target 300 K
+ * (3.8363 reduced), Nose-Hoover relaxation 0.1 ps (50 steps), SHAKE / RATTLE
+ * tolerance 1e-8, 100 iterations */
+int sesp_default_config_params(sesp_params *p);
 
 /* lifecycle.  sesp_create allocates nothing that depends on the system size;
  * sesp_upload_state sizes the device state for the system.
@@ -161,7 +188,12 @@ int sesp_run_timed(sesp_ctx *ctx, int kb0, int nsteps, int flush_l2, double *ste
 /* ordered near-field site pairs and LJ-active pairs within rc of the current
  * state and lists (sizes the pair kernel's algorithmic flop count) */
 int sesp_pair_counts(sesp_ctx *ctx, int64_t out[2]);
-int sesp_temperature(sesp_ctx *ctx, double *t);   /* src/compute_temperature.f90:240-242 */
+/* src/compute_temperature.f90:240-242: sum m v^2 / dt^2 / dof over every
+ * replica, dof = 3 sites - constraints; an FP64 reduction on the device in
+ * a fixed order (one block per replica), then one double per replica to the
+ * host (the reference reduces per rank and adds with an allreduce,
+ * src/compute_temperature.f90:239-242) */
+int sesp_temperature(sesp_ctx *ctx, double *t);
 int sesp_get_eta(sesp_ctx *ctx, double *eta);
 int sesp_set_eta(sesp_ctx *ctx, double eta);
 /* energies (the reference computes none; these integrate its force laws):

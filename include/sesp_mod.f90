@@ -9,7 +9,8 @@ module sesp_mod
   implicit none
 
   integer(c_int), parameter :: SESP_PLAIN_FP64 = 0, SESP_MIXED = 1, SESP_MIXED_FP32C = 2
-  integer(c_int), parameter :: SESP_T_ALL = 511
+  integer(c_int), parameter :: SESP_T_ALL = 1023
+  integer(c_int), parameter :: SESP_PRESET_REFERENCE = 0, SESP_PRESET_CONFIG = 1
 
   type, bind(C) :: sesp_params
     integer(c_int) :: n_cells(3)
@@ -22,6 +23,7 @@ module sesp_mod
     integer(c_int) :: shake_maxit
     integer(c_int) :: device
     integer(c_int) :: max_cell_sites
+    integer(c_int) :: preset           ! SESP_PRESET_REFERENCE (0) or SESP_PRESET_CONFIG (1)
   end type sesp_params
 
   interface
@@ -34,6 +36,10 @@ module sesp_mod
       integer(c_size_t), value :: len
     end function
     integer(c_int) function sesp_default_params(p) bind(C, name="sesp_default_params")
+      import :: c_int, sesp_params
+      type(sesp_params), intent(out) :: p
+    end function
+    integer(c_int) function sesp_default_config_params(p) bind(C, name="sesp_default_config_params")
       import :: c_int, sesp_params
       type(sesp_params), intent(out) :: p
     end function

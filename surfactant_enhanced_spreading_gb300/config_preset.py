@@ -88,8 +88,9 @@ def graphite_periodic(layers: int, half_x: float, half_y: float, z_top: float) -
 
 def chain_conformation(rng, tries: int = 200) -> np.ndarray:
     """12 beads in Angstrom from bead 1 at the origin along +z on average:
-    bonds 1.53 A, angles 112 deg, dihedrals trans (60 %) or gauche +-65 deg,
-    beads four or more bonds apart kept 3.2 A apart."""
+    bonds 1.53 A, angles 112 deg, dihedrals trans (60 %) or gauche +-65 deg
+    with +-15 deg of jitter, beads four or more bonds apart kept 3.2 A
+    apart."""
     th = math.radians(ANGLE)
     for _ in range(tries):
         b1 = np.array([0.0, 0.0, 1.0])
@@ -103,6 +104,7 @@ def chain_conformation(rng, tries: int = 200) -> np.ndarray:
         for k in range(3, N_BEAD):
             r = rng.uniform()
             phi = math.pi if r < 0.6 else (math.radians(65.0) if r < 0.8 else -math.radians(65.0))
+            phi += math.radians(rng.uniform(-15.0, 15.0))
             a, b, c = p[k - 3], p[k - 2], p[k - 1]
             bc = (c - b) / np.linalg.norm(c - b)
             n = np.cross(b - a, bc)
@@ -169,16 +171,30 @@ def config_droplet(n_water: int, n_chain: int = 0, cells=(8, 8, 8), seed: int = 
     from scipy.spatial import cKDTree
     chains = []
     if n_chain:
-        placed = None
+        library = [chain_conformation(rng) for _ in range(min(n_chain, 64))]
+        zax = np.array([0.0, 0.0, 1.0])
+        cell = 3.5
+        grid = {}   # spatial hash of placed beads (3.5 A cells) for the clash test
+
+        def clashes(cand):
+            for p in cand:
+                k = np.floor(p / cell).astype(int)
+                for dx in (-1, 0, 1):
+                    for dy in (-1, 0, 1):
+                        for dz in (-1, 0, 1):
+                            for q in grid.get((k[0] + dx, k[1] + dy, k[2] + dz), ()):
+                                if (p[0] - q[0]) ** 2 + (p[1] - q[1]) ** 2 + (p[2] - q[2]) ** 2 < cell * cell:
+                                    return True
+            return False
+
         for k in range(n_chain):
             for t in range(600):
-                conf = chain_conformation(rng)
+                conf = library[int(rng.integers(len(library)))]
                 u = rng.normal(size=3)
                 u[2] = abs(u[2]) + 0.1
                 u /= np.linalg.norm(u)
                 shell = radius + 2.5 + rng.uniform(0.0, 2.0 + 0.002 * k + 0.02 * max(0, t - 100))
                 # rotate the chain's +z axis onto u, then spin it about u
-                zax = np.array([0.0, 0.0, 1.0])
                 v = np.cross(zax, u)
                 s_, c_ = np.linalg.norm(v), zax.dot(u)
                 if s_ < 1e-12:
@@ -189,17 +205,17 @@ def config_droplet(n_water: int, n_chain: int = 0, cells=(8, 8, 8), seed: int = 
                 spin = rng.uniform(0, 2 * math.pi)
                 K = np.array([[0, -u[2], u[1]], [u[2], 0, -u[0]], [-u[1], u[0], 0]])
                 rspin = np.eye(3) + math.sin(spin) * K + (1 - math.cos(spin)) * (K @ K)
-                cand = (rspin @ (rot @ conf.T)).T + u * shell
+                cand = conf @ (rspin @ rot).T + u * shell
                 if cand[:, 2].min() < 2.5:
                     continue
                 if np.min(np.linalg.norm(cand, axis=1)) < radius + 1.5:
                     continue
-                if placed is not None and len(placed):
-                    dmin, _ = cKDTree(placed).query(cand, k=1)
-                    if dmin.min() < 3.5:
-                        continue
+                if clashes(cand):
+                    continue
                 chains.append(cand)
-                placed = cand if placed is None else np.concatenate([placed, cand])
+                for p in cand:
+                    kk = np.floor(p / cell).astype(int)
+                    grid.setdefault((kk[0], kk[1], kk[2]), []).append(p)
                 break
             else:
                 raise RuntimeError("could not place chain %d" % k)
@@ -212,17 +228,29 @@ def config_droplet(n_water: int, n_chain: int = 0, cells=(8, 8, 8), seed: int = 
     wt = water_template()
     wat = np.einsum("ij,mkj->mik", wt, _rand_rots(rng, n_water)) + pts[:, None, :]
     chain_flat = np.concatenate(chains) if chains else np.zeros((0, 3))
+    # re-draw the orientation of waters with a site closer than CLOSE to a
+    # site of another molecule.  A water's sites stay within 1 A of its
+    # (fixed) oxygen, so only waters whose oxygens are within CLOSE + 2 A can
+    # clash: those pairs are found once and re-checked every pass.
+    wp = cKDTree(pts).query_pairs(CLOSE + 2.0 + 1e-6, output_type="ndarray")
+    ctree = cKDTree(chain_flat) if len(chain_flat) else None
+    near_chain = np.zeros(n_water, dtype=bool)
+    if ctree is not None:
+        d, _ = ctree.query(pts, k=1)
+        near_chain = d < CLOSE + 1.0 + 1e-6
     for _pass in range(400):
-        flat = np.concatenate([wat.reshape(-1, 3), chain_flat])
-        pairs = cKDTree(flat).query_pairs(CLOSE, output_type="ndarray")
-        mol = np.concatenate([np.arange(3 * n_water) // 3, n_water + np.arange(len(chain_flat)) // N_BEAD])
-        if len(pairs):
-            pairs = pairs[mol[pairs[:, 0]] != mol[pairs[:, 1]]]
-        if not len(pairs):
+        a, b = wp[:, 0], wp[:, 1]
+        d2 = ((wat[a][:, :, None, :] - wat[b][:, None, :, :]) ** 2).sum(-1).reshape(len(a), -1).min(axis=1)
+        bad_pairs = wp[d2 < CLOSE * CLOSE]
+        # one water of each clashing pair (the later one on even passes, the earlier on odd ones)
+        bad = bad_pairs[:, 0] if _pass % 2 else bad_pairs[:, 1]
+        if near_chain.any():
+            idx = np.nonzero(near_chain)[0]
+            dc, _ = ctree.query(wat[idx].reshape(-1, 3), k=1)
+            bad = np.concatenate([bad, idx[(dc.reshape(-1, 3) < CLOSE).any(axis=1)]])
+        bad = np.unique(bad)
+        if not len(bad):
             break
-        first = pairs[:, 0] if _pass % 2 else pairs[:, 1]
-        other = pairs[:, 1] if _pass % 2 else pairs[:, 0]
-        bad = np.unique(np.where(mol[first] < n_water, first, other) // 3)
         wat[bad] = np.einsum("ij,mkj->mik", wt, _rand_rots(rng, len(bad))) + pts[bad][:, None, :]
     else:
         raise RuntimeError("could not orient the waters without close contacts")
@@ -243,10 +271,13 @@ def config_droplet(n_water: int, n_chain: int = 0, cells=(8, 8, 8), seed: int = 
 
 
 # the benchmark configurations' shapes in this preset (boxes rounded to
-# whole 12 A cells, multiples of 4 per axis)
+# whole 12 A cells, multiples of 4 per axis).  The large one gets 192 A in z
+# instead of 150 A: its hemisphere of 100,000 waters at 1 g/cm^3 has a radius
+# of 112.6 A, which with the chains on its surface and the 4-layer sheet
+# under it does not fit 150 A.
 C1 = dict(n_water=1000, n_chain=0, cells=(8, 8, 8), graphite_layers=2)        # 96 x 96 x 96 A
 C2 = dict(n_water=20000, n_chain=200, cells=(20, 20, 12), graphite_layers=4)  # 240 x 240 x 144 A
-C3 = dict(n_water=100000, n_chain=1000, cells=(40, 40, 12), graphite_layers=4)  # 480 x 480 x 144 A
+C3 = dict(n_water=100000, n_chain=1000, cells=(40, 40, 16), graphite_layers=4)  # 480 x 480 x 192 A
 
 
 def sheet_cells(n_water: int) -> int:

@@ -469,25 +469,131 @@ __global__ void k_move_b(Dev d, const int *mols, int nm, double tol, int maxit) 
 __global__ void k_init_accel(Dev d, int nsite) {
     int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nsite) return;
-    double m = cT.mass[d.ptype[g]];
+    double m = d.tmass[d.ptype[g]];
     d.ax[g] = d.fx[g] * DTSQ2 / m;
     d.ay[g] = d.fy[g] * DTSQ2 / m;
     d.az[g] = d.fz[g] * DTSQ2 / m;
 }
 
+// ---------------------------------------------------------------- configuration preset
+
+// floor division (b > 0)
+__device__ inline int floor_div(int a, int b) { const int q = a / b; return (a % b != 0 && a < 0) ? q - 1 : q; }
+
+// Periodic cell location (configuration preset), one thread per site: the
+// cell index along each axis is floor((r + rhs) / rs); x and y are wrapped
+// into the box and the integer image is kept (positions stay unwrapped, so
+// molecules stay whole); a site outside the z range is in no cell.  The
+// molecule's key is the cell of its first site.
+__global__ void k_locate_cfg(Dev d, int nsite) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nsite) return;
+    const int m = d.smol[g];
+    const Rep r = d.rep[d.mrep[m]];
+    const double x = d.x[g], y = d.y[g], z = d.z[g];
+    int loc = -1, kx = 0, ky = 0;
+    const double lim = 1e9;   // far outside any box: treated as lost (no cell)
+    if (fabs(x) < lim && fabs(y) < lim && fabs(z) < lim) {
+        const int ex = (int)floor((x + r.rhs[0]) * IRS), ey = (int)floor((y + r.rhs[1]) * IRS);
+        const int ez = (int)floor((z + r.rhs[2]) * IRS);
+        kx = floor_div(ex, r.nc[0]);
+        ky = floor_div(ey, r.nc[1]);
+        if (ez >= 0 && ez < r.nc[2] && abs(kx) < 30000 && abs(ky) < 30000)
+            loc = cell_index(r, ex - kx * r.nc[0], ey - ky * r.nc[1], ez);
+    }
+    d.sloc[g] = loc;
+    d.simg[g] = make_short2((short)(loc >= 0 ? kx : 0), (short)(loc >= 0 ? ky : 0));
+    if (loc >= 0) atomicAdd(&d.ccount[loc], 1);
+    else atomicAdd(&d.counters[2], 1ull);
+    if (g == d.mfirst[m]) { d.mkey[m] = loc; d.mw1[m] = 0; }
+}
+
+// Same-molecule sites of each chain bead whose (unwrapped) cells are not
+// adjacent to the bead's own: the pairs the far field counts and the
+// correction removes.  One thread per bead.
+__global__ void k_isub_cfg(Dev d, int nbeads, const int *chain_mols) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nbeads) return;
+    const int m = chain_mols[t / NCH], j = t % NCH;
+    const Rep r = d.rep[d.mrep[m]];
+    const int g0 = d.mfirst[m];
+    auto ext = [&](int g, int a) {
+        const double v = a == 0 ? d.x[g] : (a == 1 ? d.y[g] : d.z[g]);
+        const double c = fabs(v) < 1e9 ? floor((v + r.rhs[a]) * IRS) : 0.0;
+        return (int)c;
+    };
+    const int ej[3] = {ext(g0 + j, 0), ext(g0 + j, 1), ext(g0 + j, 2)};
+    uint32_t mask = 0;
+    for (int k = 0; k < NCH; k++) {
+        if (k == j) continue;
+        const int g = g0 + k;
+        if (abs(ext(g, 0) - ej[0]) > 1 || abs(ext(g, 1) - ej[1]) > 1 || abs(ext(g, 2) - ej[2]) > 1) mask |= 1u << k;
+    }
+    d.isub[t] = mask;
+}
+
+// move_a of flexible chains: the Nose-Hoover scaled predictor of
+// src/move_surfactant_a.f90:36-60 with no constraint, and the kinetic sums
+// before and after (one thread per chain)
+__global__ void k_move_free_a(Dev d, const int *mols, int nm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nm) return;
+    const int m = mols[t], g0 = d.mfirst[m];
+    const double escale = 1.0 - d.eta[d.mrep[m]] * DT / 2.0;
+    double ke0 = 0.0, ke1 = 0.0;
+    for (int i = 0; i < NCH; i++) {
+        const int g = g0 + i;
+        const double mi = d.tmass[d.ptype[g]];
+        double vx = d.vx[g], vy = d.vy[g], vz = d.vz[g];
+        ke0 += mi * (vx * vx + vy * vy + vz * vz);
+        d.x[g] = d.x[g] + vx * escale + d.ax[g];
+        d.y[g] = d.y[g] + vy * escale + d.ay[g];
+        d.z[g] = d.z[g] + vz * escale + d.az[g];
+        vx = vx * escale + d.ax[g]; vy = vy * escale + d.ay[g]; vz = vz * escale + d.az[g];
+        d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
+        ke1 += mi * (vx * vx + vy * vy + vz * vz);
+    }
+    d.ke[2 * m] = ke0;
+    d.ke[2 * m + 1] = ke1;
+}
+
+// move_b of flexible chains: acceleration from force and friction
+// (src/move_surfactant_b.f90:30-55) with no constraint
+__global__ void k_move_free_b(Dev d, const int *mols, int nm) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nm * NCH) return;
+    const int m = mols[t / NCH], g = d.mfirst[m] + t % NCH;
+    const double escale = 2.0 / (2.0 + d.eta[d.mrep[m]] * DT);
+    const double mi = d.tmass[d.ptype[g]];
+    const double axg = d.fx[g] * DTSQ2 / mi, ayg = d.fy[g] * DTSQ2 / mi, azg = d.fz[g] * DTSQ2 / mi;
+    d.ax[g] = axg; d.ay[g] = ayg; d.az[g] = azg;
+    d.vx[g] = escale * (d.vx[g] + axg);
+    d.vy[g] = escale * (d.vy[g] + ayg);
+    d.vz[g] = escale * (d.vz[g] + azg);
+}
+
 // ---------------------------------------------------------------- launchers
 
-void launch_locate(const Dev &d, int nmol, const int *smols, int nsurf_sites, cudaStream_t st) {
-    k_locate<<<(nmol + nsurf_sites + 127) / 128, 128, 0, st>>>(d, nmol, smols, nsurf_sites);
+void launch_locate(const Dev &d, int nmol, const int *smols, int nsurf_sites, int per, int nsite, cudaStream_t st) {
+    if (per) k_locate_cfg<<<(nsite + 127) / 128, 128, 0, st>>>(d, nsite);
+    else k_locate<<<(nmol + nsurf_sites + 127) / 128, 128, 0, st>>>(d, nmol, smols, nsurf_sites);
 }
-void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, cudaStream_t st) {
-    if (nsurf_sites) k_isub<<<(nsurf_sites + 31) / 32, 32, 0, st>>>(d, nsurf_sites, surf_mols);
+void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, int per, cudaStream_t st) {
+    if (!nsurf_sites) return;
+    if (per) k_isub_cfg<<<(nsurf_sites + 127) / 128, 128, 0, st>>>(d, nsurf_sites, surf_mols);
+    else k_isub<<<(nsurf_sites + 31) / 32, 32, 0, st>>>(d, nsurf_sites, surf_mols);
 }
 // fast = 0 (plain path): the FP64 sweeps above, dividing exactly as the
 // reference does; fast = 1 / 2 (mixed paths): the FP64 / FP32 sweeps of
 // k_constraint.cu.
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, int nmol, int nsite,
-                   double tol, int maxit, int fast, const ConstraintShape &sh, cudaStream_t st) {
+                   double tol, int maxit, int fast, const ConstraintShape &sh, int chains, cudaStream_t st) {
+    if (chains) {   // flexible chains: constraints on the waters only
+        if (fast) launch_move_a32(d, nw, smols, 0, nmol, nsite, sh, st, tol, maxit, fast == 2);
+        else if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+        if (ns) k_move_free_a<<<(ns + 127) / 128, 128, 0, st>>>(d, smols, ns);
+        return;
+    }
     if (fast) {
         launch_move_a32(d, nw, smols, ns, nmol, nsite, sh, st, tol, maxit, fast == 2);
     } else {
@@ -497,7 +603,13 @@ void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int
 }
 void launch_eta(const Dev &d, int nrep, cudaStream_t st) { k_eta<<<nrep * ETA_BLOCKS, ETA_THREADS, 0, st>>>(d); }
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nmol, int nsite, double tol,
-                   int maxit, int fast, const ConstraintShape &sh, cudaStream_t st) {
+                   int maxit, int fast, const ConstraintShape &sh, int chains, cudaStream_t st) {
+    if (chains) {
+        if (fast) launch_move_b32(d, nw, smols, 0, nmol, nsite, sh, st, tol, maxit, fast == 2);
+        else if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
+        if (ns) k_move_free_b<<<(ns * NCH + 255) / 256, 256, 0, st>>>(d, smols, ns);
+        return;
+    }
     if (fast) {
         launch_move_b32(d, nw, smols, ns, nmol, nsite, sh, st, tol, maxit, fast == 2);
     } else {

@@ -140,6 +140,10 @@ __device__ inline double cell_centre(const Dev &d, const Rep &r, int a, int i) {
     return t[i];
 }
 
+// Slot positions of the step: the site's position (on the periodic preset
+// wrapped by the image it had at the last rebuild, so it stays beside its
+// frozen cell) and charge, FP64; on the mixed path also FP32 relative to the
+// cell centre.
 __global__ void k_gather(Dev d, int nslot, int ncell, int mixed) {
     griddep_wait();
     int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -147,11 +151,17 @@ __global__ void k_gather(Dev d, int nslot, int ncell, int mixed) {
     if (s >= nslot || s >= d.cstart[ncell]) return;
     int g = d.srt_site[s];
     double x = d.x[g], y = d.y[g], z = d.z[g];
-    double q = cT.q[d.ptype[g]];
+    double q = d.tq[d.ptype[g]];
+    const int c = d.sloc[g];
+    const Rep &rr = d.rep[d.crep[c]];
+    if (rr.per) {
+        const short2 im = d.simg[g];
+        x -= (double)im.x * rr.rsd[0];
+        y -= (double)im.y * rr.rsd[1];
+    }
     d.srt_pos[s] = make_double4(x, y, z, q);
     if (mixed) {
-        int c = d.sloc[g];
-        const Rep r = d.rep[d.crep[c]];
+        const Rep r = rr;
         int ix, iy, iz;
         cell_xyz(r, c, ix, iy, iz);
         d.srt_pos32[s] = make_float4((float)(x - cell_centre(d, r, 0, ix)), (float)(y - cell_centre(d, r, 1, iy)),
@@ -259,6 +269,7 @@ __device__ inline double rsqrt_fp64(double r2) {
 // target sites per lane of a warp) or 32 (one); the autotuner picks it.
 // item.x = cell, item.y = (plane * 3 + row) << 8 | chunk.
 
+// rows of the 27-cell shell inside the box (periodic preset: every row in y)
 __device__ inline int near_row_mask(const Rep &r, int iy, int iz) {
     int mask = 0;
     for (int pl = 0; pl < 3; pl++) {
@@ -266,11 +277,25 @@ __device__ inline int near_row_mask(const Rep &r, int iy, int iz) {
         if (jz < 0 || jz >= r.nc[2]) continue;
         for (int rw = 0; rw < 3; rw++) {
             const int jy = iy + rw - 1;
-            if (jy < 0 || jy >= r.nc[1]) continue;
+            if (!r.per && (jy < 0 || jy >= r.nc[1])) continue;
             mask |= 1 << (pl * 3 + rw);
         }
     }
     return mask;
+}
+
+// index along a periodic axis of n cells (j within one box of [0, n))
+__device__ __forceinline__ int wrap1(int j, int n) { return j < 0 ? j + n : (j >= n ? j - n : j); }
+
+// the cell (x, y wrapped on the periodic preset) of unwrapped coordinates
+__device__ __forceinline__ int shell_cell(const Rep &r, int jx, int jy, int jz) {
+    return r.per ? cell_index(r, wrap1(jx, r.nc[0]), wrap1(jy, r.nc[1]), jz) : cell_index(r, jx, jy, jz);
+}
+
+// first and last cell along x of a partner row (clipped to a closed box)
+__device__ __forceinline__ void row_x(const Rep &r, int ix, int &jx0, int &jx1) {
+    if (r.per) { jx0 = ix - 1; jx1 = ix + 1; }
+    else { jx0 = ix > 0 ? ix - 1 : 0; jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1; }
 }
 
 __global__ void k_near_items_count(Dev d, int ncell, int tile) {
@@ -306,12 +331,21 @@ __device__ inline void near_items_fill_cell(const Dev &d, int c, int ni, int til
     cell_xyz(r, c, ix, iy, iz);
     const int mask = near_row_mask(r, iy, iz);
     const int nch = (ni + tile - 1) / tile;
-    const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+    int jx0, jx1;
+    row_x(r, ix, jx0, jx1);
     int k = d.near_icount[c];
     for (int pr = 0; pr < 9; pr++) {
         if (!(mask >> pr & 1)) continue;
-        const int c0 = cell_index(r, jx0, iy + pr % 3 - 1, iz + pr / 3 - 1);
-        const int npart = d.cstart[c0 + (jx1 - jx0) + 1] - d.cstart[c0];
+        int npart = 0;
+        if (r.per) {
+            for (int jx = jx0; jx <= jx1; jx++) {
+                const int cn = shell_cell(r, jx, iy + pr % 3 - 1, iz + pr / 3 - 1);
+                npart += d.cstart[cn + 1] - d.cstart[cn];
+            }
+        } else {
+            const int c0 = cell_index(r, jx0, iy + pr % 3 - 1, iz + pr / 3 - 1);
+            npart = d.cstart[c0 + (jx1 - jx0) + 1] - d.cstart[c0];
+        }
         for (int ch = 0; ch < nch; ch++) {
             const int nt = min(tile, ni - ch * tile);
             const int cls = 31 - __clz(nt * npart + 1);
@@ -440,7 +474,7 @@ __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int
 
 // One FP32 work item with K target sites per lane (lane + 32 j of the chunk):
 // the force of partner row pr on them, written to that row's partial.
-template <int K>
+template <int K, bool PER>
 __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int nslot, int c, int pr, int first,
                                             int ni, int lane) {
     const float4 *__restrict__ pos32 = d.srt_pos32;
@@ -451,7 +485,10 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
     int ix, iy, iz;
     cell_xyz(r, c, ix, iy, iz);
     const int jy = iy + dyc, jz = iz + dzc;
-    const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+    int jx0, jx1;
+    if constexpr (PER) { jx0 = ix - 1; jx1 = ix + 1; }
+    else row_x(r, ix, jx0, jx1);
+    const int wy = PER ? wrap1(jy, r.nc[1]) : jy;
     Tgt32 t[K];
     bool act[K];
 #pragma unroll
@@ -471,7 +508,8 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
 #pragma unroll
     for (int j = 0; j < K; j++) f[j][0] = f[j][1] = f[j][2] = 0.f;
     for (int jx = jx0; jx <= jx1; jx++) {
-        const int cn = cell_index(r, jx, jy, jz);
+        // positions are cell-relative: the shift is the unwrapped offset
+        const int cn = cell_index(r, PER ? wrap1(jx, r.nc[0]) : jx, wy, jz);
         const int t0 = d.cstart[cn], t1 = d.cstart[cn + 1];
         const float sx = (float)((ix - jx) * RS);
         Tgt32 u[K];   // targets in the partner cell's frame
@@ -541,7 +579,8 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 // change any arithmetic, so results are bit-reproducible.
 // MIXED: FP32 positions relative to the cell centres, FP32 pair terms summed
 // in FP32 over one row (at most 3 cells).
-template <bool MIXED, int KMAX>
+// PER: the periodic preset's instantiation (rows wrap around x and y)
+template <bool MIXED, int KMAX, bool PER>
 __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int tile) {
     griddep_wait();
     __shared__ float2 s_lj32[MIXED ? NTYPE * NTYPE : 1];
@@ -573,15 +612,16 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
         int ix, iy, iz;
         cell_xyz(r, c, ix, iy, iz);
         const int jy = iy + dyc, jz = iz + dzc;
-        const int jx0 = ix > 0 ? ix - 1 : 0, jx1 = ix + 1 < r.nc[0] ? ix + 1 : r.nc[0] - 1;
+        int jx0, jx1;
+        row_x(r, ix, jx0, jx1);
         double *part = d.near_part + (size_t)pr * 3 * nslot;
         if constexpr (MIXED) {
             // K = targets per lane: ceil(targets of the chunk / 32), at most KMAX
             const int nt = min(tile, ni - chunk * tile), kk = (nt + 31) >> 5;
-            if (kk <= 1) near_item32<1>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else if (kk == 2 || KMAX == 2) near_item32<2>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else if (kk == 3) near_item32<(KMAX > 2 ? 3 : 2)>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else near_item32<KMAX>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            if (kk <= 1) near_item32<1, PER>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else if (kk == 2 || KMAX == 2) near_item32<2, PER>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else if (kk == 3) near_item32<(KMAX > 2 ? 3 : 2), PER>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else near_item32<KMAX, PER>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
         } else {
             Tgt64 ta = {0.0, 0.0, 0.0, 0.0, -1, 0}, tb = ta;
             if (a0) {
@@ -596,10 +636,28 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
             }
             const double rc2 = RC * RC;
             double fa[3] = {0.0, 0.0, 0.0}, fb[3] = {0.0, 0.0, 0.0};
-            const int ca = cell_index(r, jx0, jy, jz);
-            const int t0 = d.cstart[ca], t1 = d.cstart[ca + (jx1 - jx0) + 1];
+            if constexpr (PER) {
+                // one cell at a time: a partner cell across a periodic face
+                // holds positions one box length away, so the targets move
+                // by that length into its frame
+                const int wy = wrap1(jy, r.nc[1]);
+                const double sy = (double)(jy - wy) * RS;
+                for (int jx = jx0; jx <= jx1; jx++) {
+                    const int wx = wrap1(jx, r.nc[0]);
+                    const double sx = (double)(jx - wx) * RS;
+                    Tgt64 ua = ta, ub = tb;
+                    ua.x -= sx; ua.y -= sy; ub.x -= sx; ub.y -= sy;
+                    const int cn = cell_index(r, wx, wy, jz);
+                    const int t0 = d.cstart[cn], t1 = d.cstart[cn + 1];
 #pragma unroll 2
-            for (int sl = t0; sl < t1; sl++) pair2_acc64(ta, tb, two, pos64[sl], keys[sl], s_lj64, rc2, fa, fb);
+                    for (int sl = t0; sl < t1; sl++) pair2_acc64(ua, ub, two, pos64[sl], keys[sl], s_lj64, rc2, fa, fb);
+                }
+            } else {
+                const int ca = cell_index(r, jx0, jy, jz);
+                const int t0 = d.cstart[ca], t1 = d.cstart[ca + (jx1 - jx0) + 1];
+#pragma unroll 2
+                for (int sl = t0; sl < t1; sl++) pair2_acc64(ta, tb, two, pos64[sl], keys[sl], s_lj64, rc2, fa, fb);
+            }
             if (a0) {
                 const size_t o = 3 * (size_t)(s0 + i0);
                 part[o] = fa[0]; part[o + 1] = fa[1]; part[o + 2] = fa[2];
@@ -658,24 +716,34 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     d.nf[3 * (size_t)s] = (double)fx; d.nf[3 * (size_t)s + 1] = (double)fy; d.nf[3 * (size_t)s + 2] = (double)fz;
 }
 
-int near_max_ctas_per_sm(int mixed, int tile) {
+template <bool PER>
+int near_max_ctas_t(int mixed, int tile) {
     int nb = 0;
-    if (mixed && tile > 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 4>, NEAR_THREADS, 0);
-    else if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 2>, NEAR_THREADS, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<false, 2>, NEAR_THREADS, 0);
+    if (mixed && tile > 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 4, PER>, NEAR_THREADS, 0);
+    else if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 2, PER>, NEAR_THREADS, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<false, 2, PER>, NEAR_THREADS, 0);
     return nb > 0 ? nb : 1;
+}
+int near_max_ctas_per_sm(int mixed, int tile, int per) {
+    return per ? near_max_ctas_t<true>(mixed, tile) : near_max_ctas_t<false>(mixed, tile);
 }
 
 // reset_counter: the work counter is cleared here (otherwise the step's
 // gather kernel has cleared it)
+template <bool PER>
+void launch_near_t(const Dev &d, int nslot, int mixed, const NearShape &shape, cudaStream_t st) {
+    const dim3 g(shape.grid), b(NEAR_THREADS);
+    if (mixed && shape.tile > 64) launch_pdl(k_near<true, 4, PER>, g, b, 0, st, d, nslot, shape.tile);
+    else if (mixed) launch_pdl(k_near<true, 2, PER>, g, b, 0, st, d, nslot, shape.tile);
+    else launch_pdl(k_near<false, 2, PER>, g, b, 0, st, d, nslot, shape.tile);
+}
+
 void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const NearShape &shape, cudaStream_t st,
-                 bool reset_counter) {
+                 bool reset_counter, int per) {
     if (terms & SESP_T_NEAR) {
         if (reset_counter) cudaMemsetAsync(d.near_ctl, 0, sizeof(int), st);
-        const dim3 g(shape.grid), b(NEAR_THREADS);
-        if (mixed && shape.tile > 64) launch_pdl(k_near<true, 4>, g, b, 0, st, d, nslot, shape.tile);
-        else if (mixed) launch_pdl(k_near<true, 2>, g, b, 0, st, d, nslot, shape.tile);
-        else launch_pdl(k_near<false, 2>, g, b, 0, st, d, nslot, shape.tile);
+        if (per) launch_near_t<true>(d, nslot, mixed, shape, st);
+        else launch_near_t<false>(d, nslot, mixed, shape, st);
     }
     const dim3 g((nslot + 127) / 128 > 0 ? (nslot + 127) / 128 : 1), b(128);
     if (mixed) launch_pdl(k_near_finish<true>, g, b, 0, st, d, nslot, ncell, terms);
@@ -938,7 +1006,24 @@ __global__ void k_m2l_pack(Dev d, int ncell, int n3) {
     }
     const double2 v = (l4 ? d.O4 : d.O3)[(size_t)cc * LP + n * (n + 1) + m];
     R *pk = (R *)(l4 ? d.pk4 : d.pk3) + (l4 ? r.pk4 : r.pk3);
-    pk[((size_t)q * LP + i) * vol + ((z / 2 + 2) * p1 + (y / 2 + 2)) * p0 + x / 2 + 2] = (R)(im ? v.y : v.x);
+    const R val = (R)(im ? v.y : v.x);
+    const int xc = x / 2, yc = y / 2, zc = z / 2;
+    R *base = pk + ((size_t)q * LP + i) * vol + (size_t)(zc + 2) * p1 * p0;
+    if (!r.per) {
+        base[(yc + 2) * p0 + xc + 2] = val;
+        return;
+    }
+    // periodic in x and y: the margins hold the class cells of the opposite
+    // side (one box length away; an even cell count keeps the parity class),
+    // so the interaction lists wrap around the box
+    const int hx = n0 / 2, hy = n1 / 2;
+    int xs[3] = {xc, 0, 0}, ys[3] = {yc, 0, 0}, nx = 1, ny = 1;
+    if (xc < 2) xs[nx++] = xc + hx;
+    if (xc >= hx - 2) xs[nx++] = xc - hx;
+    if (yc < 2) ys[ny++] = yc + hy;
+    if (yc >= hy - 2) ys[ny++] = yc - hy;
+    for (int a = 0; a < ny; a++)
+        for (int b = 0; b < nx; b++) base[(ys[a] + 2) * p0 + xs[b] + 2] = val;
 }
 
 constexpr int M2C_CH = 4;   // operators staged per chunk
@@ -1039,8 +1124,12 @@ __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d) {
 // one CTA per target box; each half-warp takes every 16th of the replica's
 // boxes as sources (one at a time, the same for its lanes), lane o < 15 the
 // output o; the 16 half-warps' sums are added in a fixed order
+// Periodic preset: every (source box, image) pair of the 3 x 3 supercell of
+// images in x and y that is not adjacent to the target (the reach of the far
+// field; nearer images come through the wrapped lists of L3, L4 and the
+// near field).  d2: the largest offset per axis of the H table.
 template <typename R>
-__global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const R *cf, int d2) {
+__global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const R *cf, int3 d2) {
     griddep_wait();
     __shared__ R scf[LPH * LP];
     __shared__ R sre[16][LPH], sim[16][LPH];
@@ -1055,14 +1144,17 @@ __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const
     int h[LP];
     R cr[LP], ci[LP];
     m2l_terms<R>(o < LPH ? o : LPH - 1, scf, h, cr, ci);
-    const int w = 2 * d2 + 1, nb = n[0] * n[1] * n[2];
+    const int wx = 2 * d2.x + 1, wy = 2 * d2.y + 1, nb = n[0] * n[1] * n[2];
+    const int nimg = r.per ? 9 : 1;
     R re = 0, im = 0;
-    for (int s = hw; s < nb; s += 16) {
-        const int sx = s % n[0], sy = (s / n[0]) % n[1], sz = s / (n[0] * n[1]);
+    for (int s = hw; s < nb * nimg; s += 16) {
+        const int img = s / nb, sb = s - img * nb;
+        const int ix = r.per ? img % 3 - 1 : 0, iy = r.per ? img / 3 - 1 : 0;
+        const int sx = sb % n[0] + ix * n[0], sy = (sb / n[0]) % n[1] + iy * n[1], sz = sb / (n[0] * n[1]);
         const int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
         if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-        const int oi = (dx + d2) + w * ((dy + d2) + w * (dz + d2));
-        m2l_acc<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, h, cr, ci, re, im);
+        const int oi = (dx + d2.x) + wx * ((dy + d2.y) + wy * (dz + d2.z));
+        m2l_acc<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + sb) * LP, h, cr, ci, re, im);
     }
     if (o < LPH) { sre[hw][o] = re; sim[hw][o] = im; }
     __syncthreads();
@@ -1081,7 +1173,7 @@ template <typename R>
 size_t m2c_smem() { return sizeof(R) * M2C_CH * LP * M2C_LD; }
 
 template <typename R, typename OP>
-void fma_build(const Dev &d, int ncell, int n3, int n2, int d2, const OP *m43, const OP *m32, const OP *l23,
+void fma_build(const Dev &d, int ncell, int n3, int n2, int3 d2, const OP *m43, const OP *m32, const OP *l23,
                const OP *l34, const C2<R> *h2, const R *cf, cudaStream_t st) {
     // one chain of dependent launches (programmatic: each waits for its predecessor first)
     launch_pdl(k_p2m<R>, dim3(ncell), dim3(64), 0, st, d);
@@ -1097,7 +1189,7 @@ void fma_build(const Dev &d, int ncell, int n3, int n2, int d2, const OP *m43, c
                ncell);
 }
 
-void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int d2, cudaStream_t st) {
+void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int3 d2, cudaStream_t st) {
     if (mixed)
         fma_build<float>(d, ncell, n3, n2, d2, d.op32_m2m43, d.op32_m2m32, d.op32_l2l23, d.op32_l2l34,
                          (const C2<float> *)d.h32_m2l2, d.m2l_cf32, st);
@@ -1131,17 +1223,32 @@ __device__ inline void graphite_site(const Dev &d, int col, double x, double y, 
 // graphite acts on LJ sites that sit in their molecule's key cell in the
 // bottom layer of cells: water O (w1 and split) and surfactant sites in
 // SCentral (src/eval_graphite.f90:13-132)
+// Configuration preset: every LJ site whose cell lies in the bottom cell
+// layers up to r.igz (those within rc plus the 2 A list skin of the top
+// carbon plane), in the column of its cell.
 __device__ inline int graphite_column(const Dev &d, const Rep &r, int g, double &eps, double &sg6) {
     if (!r.graphite_on) return -1;
     int pt = d.ptype[g];
-    if (pt == 1) return -1;
     int loc = d.sloc[g];
-    if (loc < 0 || loc != d.mkey[d.smol[g]]) return -1;
+    const double2 lj = d.tgr[pt];   // (eps, sg^6) with carbon; zero for water H
+    if (lj.x == 0.0 || loc < 0) return -1;
+    if (!r.per && loc != d.mkey[d.smol[g]]) return -1;
     int ix, iy, iz;
     cell_xyz(r, loc, ix, iy, iz);
-    if (iz != 0) return -1;
-    if (pt == 0) { eps = cT.epcw; sg6 = cT.sgcw6; } else { eps = cT.epcs[pt - 2]; sg6 = cT.sgcs6[pt - 2]; }
+    if (iz > (r.per ? r.igz : 0)) return -1;
+    eps = lj.x;
+    sg6 = lj.y;
     return r.gcol0 + ix + r.nc[0] * iy;
+}
+
+// a site's position wrapped by the image of the last rebuild (periodic preset)
+__device__ inline void site_pos(const Dev &d, const Rep &r, int g, double &x, double &y, double &z) {
+    x = d.x[g]; y = d.y[g]; z = d.z[g];
+    if (r.per) {
+        const short2 im = d.simg[g];
+        x -= (double)im.x * r.rsd[0];
+        y -= (double)im.y * r.rsd[1];
+    }
 }
 
 // walls, src/eval_wall.f90:17-23: 48 / (v - h)^13 + 48 / (h + v)^13 per
@@ -1161,14 +1268,18 @@ __global__ void k_site_forces(Dev d, int nsite, int terms) {
         fx = d.nf[3 * (size_t)slot]; fy = d.nf[3 * (size_t)slot + 1]; fz = d.nf[3 * (size_t)slot + 2];
     }
     double x = d.x[g], y = d.y[g], z = d.z[g];
-    if (terms & SESP_T_WALL) {
+    if (terms & SESP_T_WALL) {   // the periodic preset has walls at the z faces only
         if constexpr (MIXED) {
-            fx += (double)(48.f / pow13f((float)(x - r.rhs[0])) + 48.f / pow13f((float)(r.rhs[0] + x)));
-            fy += (double)(48.f / pow13f((float)(y - r.rhs[1])) + 48.f / pow13f((float)(r.rhs[1] + y)));
+            if (!r.per) {
+                fx += (double)(48.f / pow13f((float)(x - r.rhs[0])) + 48.f / pow13f((float)(r.rhs[0] + x)));
+                fy += (double)(48.f / pow13f((float)(y - r.rhs[1])) + 48.f / pow13f((float)(r.rhs[1] + y)));
+            }
             fz += (double)(48.f / pow13f((float)(z - r.rhs[2])) + 48.f / pow13f((float)(r.rhs[2] + z)));
         } else {
-            fx += 48.0 / pow13(x - r.rhs[0]); fx += 48.0 / pow13(r.rhs[0] + x);
-            fy += 48.0 / pow13(y - r.rhs[1]); fy += 48.0 / pow13(r.rhs[1] + y);
+            if (!r.per) {
+                fx += 48.0 / pow13(x - r.rhs[0]); fx += 48.0 / pow13(r.rhs[0] + x);
+                fy += 48.0 / pow13(y - r.rhs[1]); fy += 48.0 / pow13(r.rhs[1] + y);
+            }
             fz += 48.0 / pow13(z - r.rhs[2]); fz += 48.0 / pow13(r.rhs[2] + z);
         }
     }
@@ -1205,13 +1316,15 @@ __global__ void k_graphite(Dev d) {
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int n = *d.gcount;
     const R rc2 = (R)(RC * RC);
-    const float reach = (float)RC + 1e-3f, bin_scale = GBIN / (2.f * GYMAX);
+    const float reach = (float)RC + 1e-3f;
     for (int k = warp; k < n; k += nwarp) {
         int g = d.gsite[k];
         const Rep r = d.rep[d.mrep[d.smol[g]]];
+        const float gymax = r.gymax, bin_scale = GBIN / (2.f * gymax);
         double eps, sg6;
         const int col = graphite_column(d, r, g, eps, sg6);
-        const double xd = d.x[g], yd = d.y[g], zd = d.z[g];
+        double xd, yd, zd;
+        site_pos(d, r, g, xd, yd, zd);
         const int lc = col - r.gcol0, ix = lc % r.nc[0], iy = lc / r.nc[0];
         const float xs = (float)(xd - cell_centre(d, r, 0, ix)), ys = (float)(yd - cell_centre(d, r, 1, iy)),
                     zs = (float)(zd - cell_centre(d, r, 2, 0));
@@ -1222,8 +1335,8 @@ __global__ void k_graphite(Dev d) {
             const float dz = fmaxf(fmaxf(zr.x - zs, zs - zr.y), 0.f);
             if (zr.x <= zr.y && dz < reach) {
                 const float w = sqrtf(fmaxf(reach * reach - dz * dz, 0.f)) + 1e-3f;
-                const int b0 = min(max((int)floorf((ys - w + GYMAX) * bin_scale), 0), GBIN);
-                const int b1 = min(max((int)floorf((ys + w + GYMAX) * bin_scale) + 1, 0), GBIN);
+                const int b0 = min(max((int)floorf((ys - w + gymax) * bin_scale), 0), GBIN);
+                const int b1 = min(max((int)floorf((ys + w + gymax) * bin_scale) + 1, 0), GBIN);
                 const int *bins = d.gbin + gi * (GBIN + 1);
                 s0 = bins[b0];
                 len = bins[b1] - s0;
@@ -1302,15 +1415,17 @@ void launch_graphite(const Dev &d, int terms, int mixed, cudaStream_t st) {
 
 // positions of one surfactant (shared memory in the force kernel); the FP32
 // form holds them relative to the molecule's first site
-template <typename R = double>
-struct Pos29 {
-    R x[NSURF], y[NSURF], z[NSURF];
+template <typename R, int N>
+struct PosN {
+    R x[N], y[N], z[N];
 };
+template <typename R = double>
+using Pos29 = PosN<R, NSURF>;
 
-// one harmonic angle (src/eval_valence.f90:104-145): forces on its 3 sites
-template <typename R>
-__device__ R angle_term(const Pos29<R> &m, int i, R f[3][3]) {
-    int a = cT.ai[i], b = cT.aj[i], c = cT.ak[i];
+// one harmonic angle (src/eval_valence.f90:104-145) at vertex b with
+// equilibrium th0 and constant kth: forces on a, b, c
+template <typename R, int N>
+__device__ R angle_core(const PosN<R, N> &m, int a, int b, int c, double th0, double kth, R f[3][3]) {
     R rxji = m.x[a] - m.x[b], ryji = m.y[a] - m.y[b], rzji = m.z[a] - m.z[b];
     R rxki = m.x[c] - m.x[b], ryki = m.y[c] - m.y[b], rzki = m.z[c] - m.z[b];
     R dp = rxji * rxki + ryji * ryki + rzji * rzki;
@@ -1318,8 +1433,8 @@ __device__ R angle_term(const Pos29<R> &m, int i, R f[3][3]) {
     R rkin = sqrt(rxki * rxki + ryki * ryki + rzki * rzki);
     R th = acos(dp / rjin / rkin);
     R costh = cos(th);
-    R dth = th - (R)cT.th[i];
-    R r1 = (R)cT.rkth[i] * dth / sin(th);
+    R dth = th - (R)th0;
+    R r1 = (R)kth * dth / sin(th);
     R fjx = rxki / rjin / rkin - costh * rxji / (rjin * rjin);
     R fjy = ryki / rjin / rkin - costh * ryji / (rjin * rjin);
     R fjz = rzki / rjin / rkin - costh * rzji / (rjin * rjin);
@@ -1329,7 +1444,11 @@ __device__ R angle_term(const Pos29<R> &m, int i, R f[3][3]) {
     f[0][0] = r1 * fjx; f[0][1] = r1 * fjy; f[0][2] = r1 * fjz;
     f[1][0] = -r1 * (fjx + fkx); f[1][1] = -r1 * (fjy + fky); f[1][2] = -r1 * (fjz + fkz);
     f[2][0] = r1 * fkx; f[2][1] = r1 * fky; f[2][2] = r1 * fkz;
-    return R(0.5) * (R)cT.rkth[i] * dth * dth;
+    return R(0.5) * (R)kth * dth * dth;
+}
+template <typename R>
+__device__ R angle_term(const Pos29<R> &m, int i, R f[3][3]) {
+    return angle_core<R, NSURF>(m, cT.ai[i], cT.aj[i], cT.ak[i], cT.th[i], cT.rkth[i], f);
 }
 
 // one dihedral: r1 = -dU/dcos(phi) applied with the cross-product algebra of
@@ -1338,10 +1457,9 @@ __device__ R angle_term(const Pos29<R> &m, int i, R f[3][3]) {
 // FP32: with c = cos(phi) the ratios are the exact identities
 // sin(2 phi) / sin(phi) = 2c and sin(3 phi) / sin(phi) = 4c^2 - 1, which need
 // neither acos nor a division by sin(phi) (the FP64 form follows the reference).
-template <typename R>
-__device__ R dihedral_term(const Pos29<R> &m, int i, R f[4][3]) {
-    const bool berendsen = i >= 18;
-    int iv = cT.di[i], jv = cT.dj[i], kv = cT.dk[i], lv = cT.dl[i];
+template <typename R, int N>
+__device__ R dihedral_core(const PosN<R, N> &m, int iv, int jv, int kv, int lv, bool berendsen, R dva, R dvb, R dvc,
+                          R f[4][3]) {
     R ax = m.x[jv] - m.x[iv], ay = m.y[jv] - m.y[iv], az = m.z[jv] - m.z[iv];   // r_ji
     R bx = m.x[kv] - m.x[jv], by = m.y[kv] - m.y[jv], bz = m.z[kv] - m.z[jv];   // r_kj
     R cx = m.x[lv] - m.x[kv], cy = m.y[lv] - m.y[kv], cz = m.z[lv] - m.z[kv];   // r_nk
@@ -1350,7 +1468,6 @@ __device__ R dihedral_term(const Pos29<R> &m, int i, R f[4][3]) {
     R nu = sqrt(u1 * u1 + u2 * u2 + u3 * u3), nv = sqrt(v1 * v1 + v2 * v2 + v3 * v3);
     R arg = (u1 * v1 + u2 * v2 + u3 * v3) / nu / nv;
     R r1, e, costh;
-    const R dva = (R)cT.dva[i], dvb = (R)cT.dvb[i], dvc = (R)cT.dvc[i];
     if constexpr (std::is_same<R, double>::value) {
         const double clampv = berendsen ? 0.999999 : 0.99999999999;
         if (arg <= -1.0) arg = -clampv;
@@ -1422,6 +1539,11 @@ __device__ R dihedral_term(const Pos29<R> &m, int i, R f[4][3]) {
     f[2][0] = r1 * (fkx - h * gkx); f[2][1] = r1 * (fky - h * gky); f[2][2] = r1 * (fkz - h * gkz);
     f[3][0] = r1 * (fnx - h * gnx); f[3][1] = r1 * (fny - h * gny); f[3][2] = r1 * (fnz - h * gnz);
     return e;
+}
+template <typename R>
+__device__ R dihedral_term(const Pos29<R> &m, int i, R f[4][3]) {
+    return dihedral_core<R, NSURF>(m, cT.di[i], cT.dj[i], cT.dk[i], cT.dl[i], i >= 18, (R)cT.dva[i], (R)cT.dvb[i],
+                                   (R)cT.dvc[i], f);
 }
 
 // one intramolecular nonbonded pair, Coulomb + LJ without cutoff
@@ -1537,8 +1659,177 @@ __global__ void __launch_bounds__(INTRA_THREADS) k_intra_block(Dev d, const int 
     }
 }
 
-void launch_intra(const Dev &d, const int *smols, int ns, int terms, int mixed, cudaStream_t st) {
-    if (ns && (terms & (SESP_T_VALENCE | SESP_T_DIHEDRAL | SESP_T_BERENDSEN | SESP_T_INTERNAL | SESP_T_SUBTRACT))) {
+
+// ------------------------------------------------------------------ chains (configuration preset)
+
+static __constant__ ChainTables cCh;
+
+void upload_chain_tables(const ChainTables &t, cudaStream_t st) {
+    cudaMemcpyToSymbolAsync(cCh, &t, sizeof(ChainTables), 0, cudaMemcpyHostToDevice, st);
+}
+
+// term slots of one chain: bond b -> 2b + {b, b+1}; angle a -> CH_A0 + 3a +
+// {a, vertex a+1, a+2}; dihedral q -> CH_D0 + 4q + {q .. q+3}; pair p ->
+// CH_P0 + 2p + {a, b} (pairs four or more bonds apart, a ascending, then b)
+constexpr int CH_A0 = 2 * NCH_BOND, CH_D0 = CH_A0 + 3 * NCH_ANGLE, CH_P0 = CH_D0 + 4 * NCH_DIH;
+constexpr int CH_SLOTS = CH_P0 + 2 * NCH_PAIR;
+constexpr int CH_TERMS = NCH_BOND + NCH_ANGLE + NCH_DIH + NCH_PAIR;
+constexpr int CH_THREADS = 96;
+static_assert(CH_THREADS >= CH_TERMS, "one term per thread");
+
+// the p-th pair four or more bonds apart
+__device__ __forceinline__ void chain_pair(int p, int &a, int &b) {
+    a = 0;
+    while (p >= NCH - 4 - a) { p -= NCH - 4 - a; a++; }
+    b = a + 4 + p;
+}
+
+template <typename R>
+__device__ inline R chain_bond(const PosN<R, NCH> &m, int i, R f[2][3]) {
+    const R x = m.x[i] - m.x[i + 1], y = m.y[i] - m.y[i + 1], z = m.z[i] - m.z[i + 1];
+    const R r = sqrt(x * x + y * y + z * z), dr = r - (R)cCh.r0, fm = -(R)cCh.kb * dr / r;
+    f[0][0] = fm * x; f[0][1] = fm * y; f[0][2] = fm * z;
+    f[1][0] = -fm * x; f[1][1] = -fm * y; f[1][2] = -fm * z;
+    return R(0.5) * (R)cCh.kb * dr * dr;
+}
+
+// LJ + Coulomb without cutoff between beads a and b of one chain
+template <typename R>
+__device__ inline R chain_ipair(const Dev &d, const PosN<R, NCH> &m, int a, int b, R f[2][3]) {
+    const R x = m.x[a] - m.x[b], y = m.y[a] - m.y[b], z = m.z[a] - m.z[b];
+    const R rsq = x * x + y * y + z * z;
+    const R rsi = R(1) / rsq, ir = sqrt(rsi), r6 = rsi * rsi * rsi;
+    const R qq = (R)(d.tq[2 + a] * d.tq[2 + b] * XPI);
+    const double2 lj = d.ljt[(2 + a) * NTYPE + 2 + b];   // (48 eps sg6, sg6)
+    const R e48 = (R)lj.x, s6 = (R)lj.y;
+    const R ft = qq * ir * rsi + e48 * r6 * (s6 * r6 - R(0.5)) * rsi;
+    f[0][0] = x * ft; f[0][1] = y * ft; f[0][2] = z * ft;
+    f[1][0] = -x * ft; f[1][1] = -y * ft; f[1][2] = -z * ft;
+    return qq * ir + (e48 / R(12)) * (s6 * r6 * r6 - r6);
+}
+
+// far-field correction of one bead: minus the Coulomb of its own chain's
+// beads in cells not adjacent to its own
+template <typename R>
+__device__ inline R chain_subtract(const Dev &d, const PosN<R, NCH> &m, int j, uint32_t bits, R f[3]) {
+    R e = 0;
+    f[0] = f[1] = f[2] = 0;
+    while (bits) {
+        const int k = __ffs(bits) - 1;
+        bits &= bits - 1;
+        const R x = m.x[j] - m.x[k], y = m.y[j] - m.y[k], z = m.z[j] - m.z[k];
+        const R rmn = sqrt(x * x + y * y + z * z);
+        const R qq = (R)(d.tq[2 + j] * d.tq[2 + k] * XPI);
+        const R fel = qq / (rmn * rmn * rmn);
+        f[0] -= x * fel; f[1] -= y * fel; f[2] -= z * fel;
+        e -= R(0.5) * qq / rmn;
+    }
+    return e;
+}
+
+// One block per chain: the 11 bonds, 10 angles, 9 dihedrals and 36 pairs
+// take one thread each and write their site forces to their own slots in
+// shared memory; thread s then sums site s's slots in slot order (no
+// atomics: deterministic) and adds its far-field correction.  FP32: positions
+// relative to the chain's first bead.
+template <typename R>
+__global__ void __launch_bounds__(CH_THREADS) k_chain_block(Dev d, const int *smols, int terms) {
+    __shared__ PosN<R, NCH> m;
+    __shared__ R sf[CH_SLOTS][3];
+    const int t = blockIdx.x;
+    const int g0 = d.mfirst[smols[t]];
+    if (threadIdx.x < NCH) {
+        if constexpr (std::is_same<R, double>::value) {
+            m.x[threadIdx.x] = d.x[g0 + threadIdx.x];
+            m.y[threadIdx.x] = d.y[g0 + threadIdx.x];
+            m.z[threadIdx.x] = d.z[g0 + threadIdx.x];
+        } else {
+            m.x[threadIdx.x] = (R)(d.x[g0 + threadIdx.x] - d.x[g0]);
+            m.y[threadIdx.x] = (R)(d.y[g0 + threadIdx.x] - d.y[g0]);
+            m.z[threadIdx.x] = (R)(d.z[g0 + threadIdx.x] - d.z[g0]);
+        }
+    }
+    __syncthreads();
+    const int w = threadIdx.x;
+    if (w < NCH_BOND) {
+        R f[2][3] = {{0}};
+        if (terms & SESP_T_BOND) chain_bond<R>(m, w, f);
+        for (int k = 0; k < 2; k++) for (int c = 0; c < 3; c++) sf[2 * w + k][c] = f[k][c];
+    } else if (w < NCH_BOND + NCH_ANGLE) {
+        const int a = w - NCH_BOND;
+        R f[3][3] = {{0}};
+        if (terms & SESP_T_VALENCE) angle_core<R, NCH>(m, a, a + 1, a + 2, cCh.th0, cCh.kth, f);
+        for (int k = 0; k < 3; k++) for (int c = 0; c < 3; c++) sf[CH_A0 + 3 * a + k][c] = f[k][c];
+    } else if (w < NCH_BOND + NCH_ANGLE + NCH_DIH) {
+        const int q = w - NCH_BOND - NCH_ANGLE;
+        R f[4][3] = {{0}};
+        if (terms & SESP_T_DIHEDRAL)
+            dihedral_core<R, NCH>(m, q, q + 1, q + 2, q + 3, false, (R)cCh.dva, (R)cCh.dvb, (R)cCh.dvc, f);
+        for (int k = 0; k < 4; k++) for (int c = 0; c < 3; c++) sf[CH_D0 + 4 * q + k][c] = f[k][c];
+    } else if (w < CH_TERMS) {
+        const int p = w - NCH_BOND - NCH_ANGLE - NCH_DIH;
+        int a, b;
+        chain_pair(p, a, b);
+        R f[2][3] = {{0}};
+        if (terms & SESP_T_INTERNAL) chain_ipair<R>(d, m, a, b, f);
+        for (int k = 0; k < 2; k++) for (int c = 0; c < 3; c++) sf[CH_P0 + 2 * p + k][c] = f[k][c];
+    }
+    __syncthreads();
+    if (threadIdx.x < NCH) {
+        const int s = threadIdx.x;
+        R fx = 0, fy = 0, fz = 0;
+        auto add = [&](int sl) { fx += sf[sl][0]; fy += sf[sl][1]; fz += sf[sl][2]; };
+        if (s >= 1) add(2 * (s - 1) + 1);
+        if (s < NCH_BOND) add(2 * s);
+        if (s < NCH_ANGLE) add(CH_A0 + 3 * s);
+        if (s >= 1 && s - 1 < NCH_ANGLE) add(CH_A0 + 3 * (s - 1) + 1);
+        if (s >= 2) add(CH_A0 + 3 * (s - 2) + 2);
+        for (int k = 0; k < 4; k++)
+            if (s - k >= 0 && s - k < NCH_DIH) add(CH_D0 + 4 * (s - k) + k);
+        for (int p = 0; p < NCH_PAIR; p++) {
+            int a, b;
+            chain_pair(p, a, b);
+            if (a == s) add(CH_P0 + 2 * p);
+            else if (b == s) add(CH_P0 + 2 * p + 1);
+        }
+        if (terms & SESP_T_SUBTRACT) {
+            R f[3];
+            chain_subtract<R>(d, m, s, d.isub[(size_t)t * NCH + s], f);
+            fx += f[0]; fy += f[1]; fz += f[2];
+        }
+        const size_t n = d.nsite;
+        d.fside[g0 + s] += (double)fx; d.fside[n + g0 + s] += (double)fy; d.fside[2 * n + g0 + s] += (double)fz;
+    }
+}
+
+// energies of one chain's terms (diagnostic path): bonded, pairs, far-field correction
+__global__ void k_chain_energy(Dev d, const int *smols, int ns, double *e_mol) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ns) return;
+    const int g0 = d.mfirst[smols[t]];
+    PosN<double, NCH> m;
+    for (int i = 0; i < NCH; i++) { m.x[i] = d.x[g0 + i]; m.y[i] = d.y[g0 + i]; m.z[i] = d.z[g0 + i]; }
+    double eb = 0.0, ei = 0.0, es = 0.0, f2[2][3], f3[3][3], f4[4][3], f1[3];
+    for (int b = 0; b < NCH_BOND; b++) eb += chain_bond<double>(m, b, f2);
+    for (int a = 0; a < NCH_ANGLE; a++) eb += angle_core<double, NCH>(m, a, a + 1, a + 2, cCh.th0, cCh.kth, f3);
+    for (int q = 0; q < NCH_DIH; q++) eb += dihedral_core<double, NCH>(m, q, q + 1, q + 2, q + 3, false, cCh.dva, cCh.dvb, cCh.dvc, f4);
+    for (int p = 0; p < NCH_PAIR; p++) {
+        int a, b;
+        chain_pair(p, a, b);
+        ei += chain_ipair<double>(d, m, a, b, f2);
+    }
+    for (int j = 0; j < NCH; j++) es += chain_subtract<double>(d, m, j, d.isub[(size_t)t * NCH + j], f1);
+    e_mol[3 * t] = eb; e_mol[3 * t + 1] = ei; e_mol[3 * t + 2] = es;
+}
+
+void launch_intra(const Dev &d, const int *smols, int ns, int terms, int mixed, int chains, cudaStream_t st) {
+    const int bits = SESP_T_VALENCE | SESP_T_DIHEDRAL | SESP_T_BERENDSEN | SESP_T_INTERNAL | SESP_T_SUBTRACT | SESP_T_BOND;
+    if (ns && chains && (terms & bits)) {
+        if (mixed) k_chain_block<float><<<ns, CH_THREADS, 0, st>>>(d, smols, terms);
+        else k_chain_block<double><<<ns, CH_THREADS, 0, st>>>(d, smols, terms);
+        return;
+    }
+    if (ns && (terms & bits)) {
         if (mixed) k_intra_block<float><<<ns, INTRA_THREADS, 0, st>>>(d, smols, terms);
         else k_intra_block<double><<<ns, INTRA_THREADS, 0, st>>>(d, smols, terms);
     }
@@ -1583,13 +1874,16 @@ __global__ void k_energy_slot(Dev d, double *e_slot) {
             for (int dyc = -1; dyc <= 1; dyc++)
                 for (int dxc = -1; dxc <= 1; dxc++) {
                     int jx = ix + dxc, jy = iy + dyc, jz = iz + dzc;
-                    if (jx < 0 || jy < 0 || jz < 0 || jx >= r.nc[0] || jy >= r.nc[1] || jz >= r.nc[2]) continue;
-                    int cn = cell_index(r, jx, jy, jz);
+                    if (jz < 0 || jz >= r.nc[2]) continue;
+                    if (!r.per && (jx < 0 || jy < 0 || jx >= r.nc[0] || jy >= r.nc[1])) continue;
+                    const int cn = shell_cell(r, jx, jy, jz);
+                    const double sx = r.per ? (double)(jx - wrap1(jx, r.nc[0])) * RS : 0.0;
+                    const double sy = r.per ? (double)(jy - wrap1(jy, r.nc[1])) * RS : 0.0;
                     for (int s = d.cstart[cn]; s < d.cstart[cn + 1]; s++) {
                         int2 mj = d.srt_meta[s];
                         if (mj.x == mi.x) continue;
                         double4 pj = d.srt_pos[s];
-                        double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                        double dx = pi.x - (pj.x + sx), dy = pi.y - (pj.y + sy), dz = pi.z - pj.z;
                         double r2 = dx * dx + dy * dy + dz * dz;
                         double ir = rsqrt(r2);
                         ec += 0.5 * pi.w * pj.w * XPI * ir;
@@ -1614,12 +1908,18 @@ __global__ void k_energy_site(Dev d, int nsite, double *e_site) {
     if (g >= nsite) return;
     const Rep r = d.rep[d.mrep[d.smol[g]]];
     double x = d.x[g], y = d.y[g], z = d.z[g];
-    double ew = 4.0 / pow12(x - r.rhs[0]) + 4.0 / pow12(r.rhs[0] + x) + 4.0 / pow12(y - r.rhs[1]) +
-                4.0 / pow12(r.rhs[1] + y) + 4.0 / pow12(z - r.rhs[2]) + 4.0 / pow12(r.rhs[2] + z);
+    double ew = 4.0 / pow12(z - r.rhs[2]) + 4.0 / pow12(r.rhs[2] + z);
+    if (!r.per)
+        ew = 4.0 / pow12(x - r.rhs[0]) + 4.0 / pow12(r.rhs[0] + x) + 4.0 / pow12(y - r.rhs[1]) +
+             4.0 / pow12(r.rhs[1] + y) + 4.0 / pow12(z - r.rhs[2]) + 4.0 / pow12(r.rhs[2] + z);
     double eg = 0.0, fx = 0, fy = 0, fz = 0, eps, sg6;
     int col = graphite_column(d, r, g, eps, sg6);
-    if (col >= 0) graphite_site(d, col, x, y, z, eps, sg6, fx, fy, fz, &eg);
-    double m = cT.mass[d.ptype[g]];
+    if (col >= 0) {
+        double xw, yw, zw;
+        site_pos(d, r, g, xw, yw, zw);
+        graphite_site(d, col, xw, yw, zw, eps, sg6, fx, fy, fz, &eg);
+    }
+    double m = d.tmass[d.ptype[g]];
     double ek = 0.5 * m * (d.vx[g] * d.vx[g] + d.vy[g] * d.vy[g] + d.vz[g] * d.vz[g]) / (DT * DT);
     e_site[3 * (size_t)g] = ew; e_site[3 * (size_t)g + 1] = eg; e_site[3 * (size_t)g + 2] = ek;
 }
@@ -1641,14 +1941,17 @@ __global__ void k_count_pairs(Dev d, unsigned long long *out) {
             for (int dyc = -1; dyc <= 1; dyc++)
                 for (int dxc = -1; dxc <= 1; dxc++) {
                     int jx = ix + dxc, jy = iy + dyc, jz = iz + dzc;
-                    if (jx < 0 || jy < 0 || jz < 0 || jx >= r.nc[0] || jy >= r.nc[1] || jz >= r.nc[2]) continue;
-                    int cn = cell_index(r, jx, jy, jz);
+                    if (jz < 0 || jz >= r.nc[2]) continue;
+                    if (!r.per && (jx < 0 || jy < 0 || jx >= r.nc[0] || jy >= r.nc[1])) continue;
+                    const int cn = shell_cell(r, jx, jy, jz);
+                    const double sx = r.per ? (double)(jx - wrap1(jx, r.nc[0])) * RS : 0.0;
+                    const double sy = r.per ? (double)(jy - wrap1(jy, r.nc[1])) * RS : 0.0;
                     for (int s = d.cstart[cn]; s < d.cstart[cn + 1]; s++) {
                         int2 mj = d.srt_meta[s];
                         if (mj.x == mi.x) continue;
                         nc++;
                         double4 pj = d.srt_pos[s];
-                        double dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+                        double dx = pi.x - (pj.x + sx), dy = pi.y - (pj.y + sy), dz = pi.z - pj.z;
                         if (dx * dx + dy * dy + dz * dz <= rc2 && d.ljt[mi.y * NTYPE + mj.y].x != 0.0) nl++;
                     }
                 }
@@ -1661,6 +1964,27 @@ void launch_count_pairs(const Dev &d, int ncell, unsigned long long *out, cudaSt
     k_count_pairs<<<ncell, 128, 0, st>>>(d, out);
 }
 
+// sum m v^2 of each replica (src/compute_temperature.f90:240-242): one block
+// per replica, thread-strided partial sums and a fixed tree, so the result
+// does not depend on timing
+constexpr int TEMP_THREADS = 256;
+__global__ void __launch_bounds__(TEMP_THREADS) k_temperature(Dev d) {
+    __shared__ double sh[TEMP_THREADS];
+    const Rep r = d.rep[blockIdx.x];
+    double a = 0.0;
+    for (int g = r.site0 + threadIdx.x; g < r.site0 + r.nsite; g += TEMP_THREADS)
+        a += d.tmass[d.ptype[g]] * (d.vx[g] * d.vx[g] + d.vy[g] * d.vy[g] + d.vz[g] * d.vz[g]);
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = TEMP_THREADS / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) d.tbuf[blockIdx.x] = sh[0];
+}
+
+void launch_temperature(const Dev &d, int nrep, cudaStream_t st) { k_temperature<<<nrep, TEMP_THREADS, 0, st>>>(d); }
+
 // writes a buffer larger than the L2 cache so the next launch starts cold
 __global__ void k_flush(float4 *buf, size_t n) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -1671,11 +1995,12 @@ void launch_flush(void *buf, size_t bytes, cudaStream_t st) {
     k_flush<<<152 * 8, 256, 0, st>>>((float4 *)buf, bytes / sizeof(float4));
 }
 
-void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int ns, double *e_slot, double *e_site,
-                     double *e_mol, cudaStream_t st) {
+void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int ns, int chains, double *e_slot,
+                     double *e_site, double *e_mol, cudaStream_t st) {
     k_energy_slot<<<ncell, 128, 0, st>>>(d, e_slot);
     k_energy_site<<<(nsite + 255) / 256, 256, 0, st>>>(d, nsite, e_site);
-    if (ns) k_intra_energy<<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, e_mol);
+    if (ns && chains) k_chain_energy<<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, e_mol);
+    else if (ns) k_intra_energy<<<(ns + 63) / 64, 64, 0, st>>>(d, smols, ns, e_mol);
 }
 
 }  // namespace sesp

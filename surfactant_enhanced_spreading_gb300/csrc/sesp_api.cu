@@ -140,6 +140,45 @@ Tables make_tables() {
     return T;
 }
 
+// The configuration preset's force field (the benchmark configurations'
+// water and chains, see SESP_PRESET_CONFIG in sesp.h), in reduced units:
+// per-kind charges, masses, LJ sigma / epsilon and the chains' bonded
+// constants.  Kinds: 0 water O, 1 water H, 2 + b bead b of a chain.
+struct CfgField {
+    double q[NTYPE], mass[NTYPE], sg[NTYPE], ep[NTYPE];
+    ChainTables ch;
+};
+CfgField make_cfg_field() {
+    CfgField F;
+    memset(&F, 0, sizeof F);
+    const double sig = SIGMA, eps = EPSILON, kj = 1000.0 / eps;
+    const double mO = 15.9994, mH = 1.00794;
+    const double pi180 = 4.0 * atan(1.0) / 180.0;
+    F.mass[0] = 1.0; F.mass[1] = mH / mO;
+    F.q[0] = -0.82; F.q[1] = 0.41;
+    // head beads 1-4 (charges summing to zero), then the CH2 tail
+    const double hm[4] = {15.035, 15.9994, 14.027, 15.9994}, hq[4] = {0.40, -0.60, 0.60, -0.40};
+    const double hs[4] = {3.75, 2.80, 3.95, 2.80}, he[4] = {0.815, 0.457, 0.382, 0.457};
+    F.sg[0] = 3.166 / sig; F.ep[0] = 0.650 * kj;
+    for (int b = 0; b < NCH; b++) {
+        const int t = 2 + b;
+        F.mass[t] = (b < 4 ? hm[b] : 14.027) / mO;
+        F.q[t] = b < 4 ? hq[b] : 0.0;
+        F.sg[t] = (b < 4 ? hs[b] : 3.9) / sig;
+        F.ep[t] = (b < 4 ? he[b] : 0.38) * kj;
+    }
+    F.ch.kb = 2000.0 * kj * sig * sig;   // 2000 kJ/mol/A^2
+    F.ch.r0 = 1.53 / sig;
+    F.ch.kth = 519.7 * kj;               // per rad^2
+    F.ch.th0 = 112.0 * pi180;
+    F.ch.dva = 2951.7 / eps;
+    F.ch.dvb = -566.9 / eps;
+    F.ch.dvc = 6579.0 / eps;
+    return F;
+}
+// carbon LJ of the configuration preset: sigma 3.4 A, epsilon 0.23 kJ/mol
+constexpr double CFG_SG_C = 3.4 / SIGMA, CFG_EP_C = 0.23 * (1000.0 / EPSILON);
+
 }  // namespace
 
 
@@ -199,6 +238,38 @@ std::vector<double2> make_lj_table() {
             t[a * NTYPE + b] = make_double2(48.0 * e * s6, s6);
         }
     return t;
+}
+
+// the configuration preset's LJ pair table, Lorentz-Berthelot over its kinds
+std::vector<double2> make_lj_table_cfg(const CfgField &F) {
+    std::vector<double2> t(NTYPE * NTYPE, make_double2(0.0, 0.0));
+    for (int a = 0; a < 2 + NCH; a++)
+        for (int b = 0; b < 2 + NCH; b++) {
+            if (a == 1 || b == 1) continue;
+            const double s = (F.sg[a] + F.sg[b]) / 2.0, s2 = s * s, s6 = s2 * s2 * s2;
+            t[a * NTYPE + b] = make_double2(48.0 * sqrt(F.ep[a] * F.ep[b]) * s6, s6);
+        }
+    return t;
+}
+
+// per-kind charge, mass and graphite (eps, sg^6) of either force field
+void kind_tables(int preset, std::vector<double> &q, std::vector<double> &mass, std::vector<double2> &gr) {
+    q.assign(NTYPE, 0.0); mass.assign(NTYPE, 1.0); gr.assign(NTYPE, make_double2(0.0, 0.0));
+    if (preset == SESP_PRESET_CONFIG) {
+        const CfgField F = make_cfg_field();
+        for (int k = 0; k < 2 + NCH; k++) {
+            q[k] = F.q[k];
+            mass[k] = F.mass[k];
+            if (k == 1) continue;
+            const double s = (F.sg[k] + CFG_SG_C) / 2.0, s2 = s * s, s6 = s2 * s2 * s2;
+            gr[k] = make_double2(sqrt(F.ep[k] * CFG_EP_C), s6);
+        }
+        return;
+    }
+    const Tables T = make_tables();
+    for (int k = 0; k < NTYPE; k++) { q[k] = T.q[k]; mass[k] = T.mass[k]; }
+    gr[0] = make_double2(T.epcw, T.sgcw6);
+    for (int i = 0; i < NSURF; i++) gr[2 + i] = make_double2(T.epcs[i], T.sgcs6[i]);
 }
 
 // ------------------------------------------------------------------ translation operators (src/ifma.f90)
@@ -336,7 +407,10 @@ struct sesp_ctx {
     sesp_params p;
     cudaStream_t st = nullptr;
     bool uploaded = false, have_force = false;
-    int nrep = 0, nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, nwm = 0, nsm = 0, d2 = 1;
+    int nrep = 0, nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, nwm = 0, nsm = 0;
+    int3 d2 = {1, 1, 1};   // largest L2 offset per axis of the far field's H table
+    int chains = 0;        // configuration preset: surfactants are 12-bead flexible chains
+    int ssite = NSURF;     // sites per surfactant
     std::vector<Rep> reps;
     Dev d;
     int *wmols = nullptr, *smols = nullptr;
@@ -450,13 +524,13 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
     if (rebuild) {
         tstart(c, 5);
         cudaMemsetAsync(d.ccount, 0, sizeof(int) * c->ncell, c->st);
-        launch_locate(d, c->nmol, c->smols, c->nsm * NSURF, c->st);
+        launch_locate(d, c->nmol, c->smols, c->nsm * c->ssite, c->chains, c->nsite, c->st);
         family(c, "locate");
         launch_sort(d, c->nsite, c->ncell, c->st);
         family(c, "cell sort");
         launch_near_items(d, c->ncell, (int)near_items_max(c->nsite, c->ncell), c->near.tile, c->st);
         family(c, "near-field items");
-        launch_isub(d, c->nsm * NSURF, c->smols, c->st);
+        launch_isub(d, c->nsm * c->ssite, c->smols, c->chains, c->st);
         family(c, "isub");
         launch_graphite_list(d, c->nsite, c->st);
         family(c, "graphite list");
@@ -476,7 +550,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         cudaEventRecord(c->ev_fork, c->st);
         cudaStreamWaitEvent(c->st2, c->ev_fork, 0);
         launch_graphite(d, terms, mixed, c->st2);
-        launch_intra(d, c->smols, c->nsm, terms, mixed, c->st2);
+        launch_intra(d, c->smols, c->nsm, terms, mixed, c->chains, c->st2);
         cudaEventRecord(c->ev_join, c->st2);
     }
     if (rebuild) {
@@ -486,7 +560,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         tstop(c, 6);
     }
     tstart(c, 0);
-    launch_near(d, c->ncell, c->nsite, mixed, terms, c->near, c->st, false);
+    launch_near(d, c->ncell, c->nsite, mixed, terms, c->near, c->st, false, c->chains);
     family(c, "near field");
     tstop(c, 0);
     tstart(c, 4);
@@ -495,7 +569,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
     } else {
         launch_graphite(d, terms, mixed, c->st);
         family(c, "graphite");
-        launch_intra(d, c->smols, c->nsm, terms, mixed, c->st);
+        launch_intra(d, c->smols, c->nsm, terms, mixed, c->chains, c->st);
         family(c, "intramolecular");
     }
     launch_site_forces(d, c->nsite, terms, mixed, c->st);
@@ -509,7 +583,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
 void seq_move_a(sesp_ctx *c, bool fork_eta = false) {
     tstart(c, 2);
     launch_move_a(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit,
-                  c->p.precision, c->cshape, c->st);
+                  c->p.precision, c->cshape, c->chains, c->st);
     if (fork_eta) {
         cudaEventRecord(c->ev_eta, c->st);
         cudaStreamWaitEvent(c->st2, c->ev_eta, 0);
@@ -523,7 +597,7 @@ void seq_move_a(sesp_ctx *c, bool fork_eta = false) {
 void seq_move_b(sesp_ctx *c) {
     tstart(c, 3);
     launch_move_b(c->d, c->wmols, c->nwm, c->smols, c->nsm, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit,
-                  c->p.precision, c->cshape, c->st);
+                  c->p.precision, c->cshape, c->chains, c->st);
     family(c, "move_b");
     tstop(c, 3);
 }
@@ -561,6 +635,18 @@ int sesp_default_params(sesp_params *p) {
     p->shake_maxit = 100;
     p->device = 0;
     p->max_cell_sites = 0;
+    p->preset = SESP_PRESET_REFERENCE;
+    return 0;
+}
+
+int sesp_default_config_params(sesp_params *p) {
+    if (int e = sesp_default_params(p)) return e;
+    p->n_cells[0] = p->n_cells[1] = p->n_cells[2] = 8;
+    p->preset = SESP_PRESET_CONFIG;
+    p->tr = 8.314462618 * 300.0 / EPSILON;   // 300 K
+    p->tau_steps = 0.1e-12 / 2.0e-15;         // 0.1 ps of 2 fs steps
+    p->shake_tol = 1e-8;
+    p->shake_maxit = 100;
     return 0;
 }
 
@@ -571,11 +657,16 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (p->precision != SESP_PLAIN_FP64 && p->precision != SESP_MIXED && p->precision != SESP_MIXED_FP32C)
         return fail(SESP_EINVAL, "unknown precision");
     if (p->rebuild_interval <= 0) return fail(SESP_EINVAL, "rebuild_interval must be positive");
+    if (p->preset != SESP_PRESET_REFERENCE && p->preset != SESP_PRESET_CONFIG) return fail(SESP_EINVAL, "unknown preset %d", p->preset);
+    if (p->preset == SESP_PRESET_CONFIG && (p->n_cells[0] < 8 || p->n_cells[1] < 8))
+        return fail(SESP_EINVAL, "the periodic preset needs at least 8 cells in x and y");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SESP_ECUDA, "no CUDA device");
     if (p->device < 0 || p->device >= ndev) return fail(SESP_EINVAL, "device %d out of range", p->device);
     sesp_ctx *c = new sesp_ctx();
     c->p = *p;
+    c->chains = p->preset == SESP_PRESET_CONFIG;
+    c->ssite = c->chains ? NCH : NSURF;
     if (set_device(c)) { delete c; return SESP_ECUDA; }
     if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) != cudaSuccess ||
@@ -594,7 +685,7 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
         cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, dev);
         const int mixed = c->p.precision != SESP_PLAIN_FP64;
         c->near.tile = 64;   // 128 (mixed paths) only where the autotuner measures it faster
-        c->near.grid = c->n_sm * near_max_ctas_per_sm(mixed, c->near.tile);
+        c->near.grid = c->n_sm * near_max_ctas_per_sm(mixed, c->near.tile, c->chains);
         c->cshape.grid = c->n_sm;
     }
     c->sync_check = getenv("SESP_SYNC_CHECK") != nullptr;
@@ -605,6 +696,7 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     }
     upload_tables_exact(T, c->st);
     upload_tables_force(T, c->st);
+    upload_chain_tables(make_cfg_field().ch, c->st);
     if (!upload_tables_fast(T, c->st)) { delete c; return fail(SESP_ECUDA, "constraint table upload"); }
     if (cudaStreamSynchronize(c->st) != cudaSuccess) { delete c; return fail(SESP_ECUDA, "table upload"); }
     *out = c;
@@ -642,7 +734,9 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     free_state(c);
     const int R = (int)in.size();
     c->reps.assign(R, Rep());
-    int nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, naxis = 0, ncol = 0, nwm = 0, nsm = 0, d2 = 1;
+    int nsite = 0, nmol = 0, ncell = 0, n3 = 0, n2 = 0, naxis = 0, ncol = 0, nwm = 0, nsm = 0;
+    int3 d2 = {1, 1, 1};
+    const int per = c->chains;   // the configuration preset: periodic in x and y
     size_t npk4 = 0, npk3 = 0;
     for (int q = 0; q < R; q++) {
         const RepIn &ri = in[q];
@@ -650,21 +744,30 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         memset(&r, 0, sizeof r);
         for (int a = 0; a < 3; a++) {
             if (ri.nc[a] <= 0 || ri.nc[a] % 4) return fail(SESP_EINVAL, "replica %d: cells must be positive multiples of 4", q);
+            if (per && a < 2 && ri.nc[a] < 8) return fail(SESP_EINVAL, "replica %d: the periodic preset needs at least 8 cells in x and y", q);
             r.nc[a] = ri.nc[a];
             r.nr[a] = r.nc[a] / 4;
             r.rsd[a] = r.nc[a] * RS;
             r.rhs[a] = r.rsd[a] / 2.0;
             r.irsd[a] = 1.0 / r.rsd[a];
-            d2 = std::max(d2, r.nr[a] - 1);
+            // L2 offsets reach one box further along a periodic axis (images -1, 0, 1)
+            const int reach = (per && a < 2) ? 2 * r.nr[a] - 1 : r.nr[a] - 1;
+            int &dd = a == 0 ? d2.x : (a == 1 ? d2.y : d2.z);
+            dd = std::max(dd, reach);
         }
+        r.per = per;
+        r.ssite = c->ssite;
+        r.igz = -1;
+        r.gymax = GYMAX;
         if (ri.nw < 0 || ri.ns < 0 || ri.nw + ri.ns == 0) return fail(SESP_EINVAL, "replica %d: empty system", q);
         if (!ri.pos) return fail(SESP_EINVAL, "replica %d: null positions", q);
         if (ri.ncarb < 0 || (ri.ncarb > 0 && !ri.carb)) return fail(SESP_EINVAL, "replica %d: bad carbons", q);
         r.nw = ri.nw; r.ns = ri.ns;
-        r.nsite = 3 * ri.nw + NSURF * ri.ns;
+        r.nsite = 3 * ri.nw + c->ssite * ri.ns;
         r.nmol = ri.nw + ri.ns;
         r.graphite_on = c->p.graphite_on;
-        int np = r.nsite, ncon = 3 * ri.nw + NBOND * ri.ns, df = 3 * np - ncon;
+        int np = r.nsite, ncon = 3 * ri.nw + (c->chains ? 0 : NBOND) * ri.ns, df = 3 * np - ncon;
+        r.ncon = ncon;
         double rlx = c->p.tau_steps * DT;
         r.pnh1 = DT / df / c->p.tr / (rlx * rlx);
         r.pnh2 = -2.0 * df * c->p.tr;
@@ -680,8 +783,11 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         for (int g = 0; g < r.nsite; g++)
             for (int a = 0; a < 3; a++) {
                 double v = ri.pos[3 * g + a];
-                if (!(v > -r.rhs[a] && v < r.rhs[a]))
+                if (per && a < 2) {   // periodic axes: any position a rebuild can wrap
+                    if (!(fabs(v) < 1e8)) return fail(SESP_EINVAL, "replica %d: site %d position %g (axis %d)", q, g, v, a);
+                } else if (!(v > -r.rhs[a] && v < r.rhs[a])) {
                     return fail(SESP_EINVAL, "replica %d: site %d outside the box (axis %d: %g)", q, g, a, v);
+                }
             }
     }
     c->nrep = R; c->nsite = nsite; c->nmol = nmol; c->ncell = ncell; c->n3 = n3; c->n2 = n2;
@@ -704,7 +810,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.near_part, 27 * (size_t)N)) || (e = dalloc(c, &d.near_items, near_items_max(N, C))) ||
         (e = dalloc(c, &d.near_items_tmp, near_items_max(N, C))) || (e = dalloc(c, &d.near_cls, near_items_max(N, C))) ||
         (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 66)) ||
-        (e = dalloc(c, &d.isub, (size_t)NSURF * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
+        (e = dalloc(c, &d.isub, (size_t)c->ssite * nsm)) || (e = dalloc(c, &d.O4, (size_t)LP * C)) ||
         (e = dalloc(c, &d.L4, (size_t)LP * C)) || (e = dalloc(c, &d.L4f, (size_t)LP * C)) ||
         (e = dalloc(c, &d.fside, 3 * (size_t)N)) || (e = dalloc(c, &d.stage, 12 * (size_t)N)) ||
         (e = dalloc(c, &d.O3, (size_t)LP * n3)) ||
@@ -714,10 +820,11 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.wlist_a, nwm)) || (e = dalloc(c, &d.wlist_b, nwm)) || (e = dalloc(c, &d.wsw_a, M)) ||
         (e = dalloc(c, &d.wsw_b, M)) || (e = dalloc(c, &d.cctl, 8)) || (e = dalloc(c, &d.wsort_off, 256)) ||
         (e = dalloc(c, &d.eta_part, 64 * (size_t)R)) || (e = dalloc(c, &d.eta_ctl, R)) ||
-        (e = dalloc(c, &d.cnh, C)))
+        (e = dalloc(c, &d.cnh, C)) || (e = dalloc(c, &d.tq, NTYPE)) || (e = dalloc(c, &d.tmass, NTYPE)) ||
+        (e = dalloc(c, &d.tgr, NTYPE)) || (e = dalloc(c, &d.simg, N)) || (e = dalloc(c, &d.tbuf, R)))
         return e;
-    int w2 = 2 * d2 + 1;
-    const size_t nh2 = (size_t)w2 * w2 * w2 * NHARM;
+    const int w2x = 2 * d2.x + 1, w2y = 2 * d2.y + 1, w2z = 2 * d2.z + 1;
+    const size_t nh2 = (size_t)w2x * w2y * w2z * NHARM;
     // real-form M2L at L4 and L3: work items of M2C_TILE targets of one parity
     // class, each split into M2C_GROUPS offset groups (a constant, so a
     // replica's sums do not depend on what else is batched with it)
@@ -785,7 +892,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     double rcut = RC + sqrt(2.0) * RS / 2.0;
     rcut *= rcut;
     for (int q = 0; q < R; q++) {
-        const Rep &r = c->reps[q];
+        Rep &r = c->reps[q];
         const RepIn &ri = in[q];
         for (int m = 0; m < ri.nw; m++) {
             int gm = r.mol0 + m, g0 = r.site0 + 3 * m;
@@ -793,9 +900,9 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
             for (int t = 0; t < 3; t++) { ptype[g0 + t] = t == 0 ? 0 : 1; smol[g0 + t] = gm; }
         }
         for (int k = 0; k < ri.ns; k++) {
-            int gm = r.mol0 + ri.nw + k, g0 = r.site0 + 3 * ri.nw + NSURF * k;
+            int gm = r.mol0 + ri.nw + k, g0 = r.site0 + 3 * ri.nw + c->ssite * k;
             mfirst[gm] = g0; mkind[gm] = 1; mrep[gm] = q; sm.push_back(gm);
-            for (int t = 0; t < NSURF; t++) { ptype[g0 + t] = (uint8_t)(2 + t); smol[g0 + t] = gm; }
+            for (int t = 0; t < c->ssite; t++) { ptype[g0 + t] = (uint8_t)(2 + t); smol[g0 + t] = gm; }
         }
         for (int g = 0; g < r.nsite; g++) {
             sx[r.site0 + g] = ri.pos[3 * g]; sy[r.site0 + g] = ri.pos[3 * g + 1]; sz[r.site0 + g] = ri.pos[3 * g + 2];
@@ -806,36 +913,94 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         for (int k = 0; k < cc / 8; k++) b3[r.l3_0 + k] = q;
         for (int k = 0; k < cc / 64; k++) b2[r.l2_0 + k] = q;
         size_t a0 = axis.size();
-        for (int a = 0; a < 3; a++) axis_centres(r, a, axis);
+        for (int a = 0; a < 3; a++) {
+            if (per)   // uniform cells from the lower face
+                for (int k = 0; k < r.nc[a]; k++) axis.push_back(-r.rhs[a] + (k + 0.5) * RS);
+            else
+                axis_centres(r, a, axis);
+        }
         for (int a = 0; a < 3; a++) {   // the reference's operation order (rcen2xtmp)
             const double b = (double)r.nr[a];
             for (int rk = 0; rk < r.nr[a]; rk++) rcen2.push_back(r.rsd[a] * (rk + 1) / b - r.rhs[a] - r.rsd[a] / b / 2.0);
         }
+        // periodic preset: carbons binned by column; a column's list takes
+        // its neighbours' carbons (and their images across the periodic
+        // faces) within rc + half a cell diagonal + the 2 A list skin
+        std::vector<int> cbin_start, cbin;
+        double rcut_per = RC + sqrt(2.0) * RS / 2.0 + (RS - RC);
+        if (per) {
+            r.gymax = (float)rcut_per + 1e-3f;
+            const int ncc = r.nc[0] * r.nc[1];
+            cbin_start.assign(ncc + 1, 0);
+            std::vector<int> bof(ri.ncarb);
+            double ztop = -1e300;
+            for (int k = 0; k < ri.ncarb; k++) {
+                int bx = (int)floor((ri.carb[3 * k] + r.rhs[0]) / RS), by = (int)floor((ri.carb[3 * k + 1] + r.rhs[1]) / RS);
+                bx = ((bx % r.nc[0]) + r.nc[0]) % r.nc[0];
+                by = ((by % r.nc[1]) + r.nc[1]) % r.nc[1];
+                bof[k] = bx + r.nc[0] * by;
+                cbin_start[bof[k] + 1]++;
+                ztop = std::max(ztop, ri.carb[3 * k + 2]);
+            }
+            for (int b = 0; b < ncc; b++) cbin_start[b + 1] += cbin_start[b];
+            cbin.resize(ri.ncarb);
+            std::vector<int> fill(ncc, 0);
+            for (int k = 0; k < ri.ncarb; k++) cbin[cbin_start[bof[k]] + fill[bof[k]]++] = k;
+            // the layers of cells the graphite acts on: up to the one holding
+            // the top carbon plane + rs (rc plus the list skin)
+            if (ri.ncarb && c->p.graphite_on) {
+                const int iz = (int)floor((ztop + RS + r.rhs[2]) * (1.0 / RS));
+                r.igz = iz < 0 ? 0 : (iz >= r.nc[2] ? r.nc[2] - 1 : iz);
+            }
+        }
         // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:9-35
+        // (lp: the listed carbons' coordinates as the column sees them)
+        std::vector<double> lp;
         for (int iy = 0; iy < r.nc[1]; iy++)
             for (int ix = 0; ix < r.nc[0]; ix++) {
                 double cx = axis[a0 + ix], cy = axis[a0 + r.nc[0] + iy], cz = axis[a0 + r.nc[0] + r.nc[1]];
-                std::vector<int> ks;
-                for (int k = 0; k < ri.ncarb; k++) {
-                    double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
-                    if (dx * dx + dy * dy <= rcut) ks.push_back(k);
+                lp.clear();
+                if (per) {
+                    const double rc2 = rcut_per * rcut_per;
+                    for (int by = iy - 2; by <= iy + 2; by++)      // 5 x 5 columns cover rcut_per (< 2.5 cells);
+                        for (int bx = ix - 2; bx <= ix + 2; bx++) { // at least 8 per axis: no column twice
+                            const int wx = ((bx % r.nc[0]) + r.nc[0]) % r.nc[0], wy = ((by % r.nc[1]) + r.nc[1]) % r.nc[1];
+                            const int b = wx + r.nc[0] * wy;
+                            for (int t = cbin_start[b]; t < cbin_start[b + 1]; t++) {
+                                const int k = cbin[t];
+                                // the image of the carbon nearest the column centre
+                                double gx = ri.carb[3 * k], gy = ri.carb[3 * k + 1];
+                                gx -= r.rsd[0] * floor((gx - cx) / r.rsd[0] + 0.5);
+                                gy -= r.rsd[1] * floor((gy - cy) / r.rsd[1] + 0.5);
+                                const double dx = gx - cx, dy = gy - cy;
+                                if (dx * dx + dy * dy <= rc2) { lp.push_back(gx); lp.push_back(gy); lp.push_back(ri.carb[3 * k + 2]); }
+                            }
+                        }
+                } else {
+                    for (int k = 0; k < ri.ncarb; k++) {
+                        double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
+                        if (dx * dx + dy * dy <= rcut)
+                            for (int a = 0; a < 3; a++) lp.push_back(ri.carb[3 * k + a]);
+                    }
                 }
+                std::vector<int> ks(lp.size() / 3);
+                for (size_t i = 0; i < ks.size(); i++) ks[i] = (int)i;
                 // groups: the column's carbons by z (a graphite layer each, at
                 // most GGRP groups of neighbouring z), each group in order of
                 // its FP32 y with GBIN uniform y bins over [-ymax, ymax], so a
                 // site visits only the groups and the y window within rc
                 std::sort(ks.begin(), ks.end(), [&](int a, int b) {
-                    return ri.carb[3 * a + 2] != ri.carb[3 * b + 2] ? ri.carb[3 * a + 2] < ri.carb[3 * b + 2] : a < b;
+                    return lp[3 * a + 2] != lp[3 * b + 2] ? lp[3 * a + 2] < lp[3 * b + 2] : a < b;
                 });
                 std::vector<int> bounds(1, 0);
                 for (size_t t = 1; t < ks.size(); t++)
-                    if (ri.carb[3 * ks[t] + 2] != ri.carb[3 * ks[t - 1] + 2]) bounds.push_back((int)t);
+                    if (lp[3 * ks[t] + 2] != lp[3 * ks[t - 1] + 2]) bounds.push_back((int)t);
                 bounds.push_back((int)ks.size());
                 const int nz = (int)bounds.size() - 1;
                 std::vector<int> gb(1, 0);   // group bounds: every z level, or GGRP equal runs of them
                 for (int l = 1; l <= GGRP; l++)
                     gb.push_back(bounds[nz <= GGRP ? (l <= nz ? l : nz) : (int)((long long)nz * l / GGRP)]);
-                auto y32 = [&](int k) { return (float)(ri.carb[3 * k + 1] - cy); };
+                auto y32 = [&](int k) { return (float)(lp[3 * k + 1] - cy); };
                 const int base = (int)gpos.size();
                 for (int l = 0; l < GGRP; l++) {
                     const int b0 = gb[l], b1 = gb[l + 1];
@@ -843,7 +1008,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
                               [&](int a, int b) { return y32(a) != y32(b) ? y32(a) < y32(b) : a < b; });
                     float zlo = 0.f, zhi = -1.f;   // empty group
                     for (int t = b0; t < b1; t++) {
-                        const float z = (float)(ri.carb[3 * ks[t] + 2] - cz);
+                        const float z = (float)(lp[3 * ks[t] + 2] - cz);
                         zlo = t == b0 ? z : std::min(zlo, z);
                         zhi = t == b0 ? z : std::max(zhi, z);
                     }
@@ -851,16 +1016,16 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
                     // bin edge j at -ymax + j * bw: the first carbon at or above it
                     int t = b0;
                     for (int j = 0; j < GBIN; j++) {
-                        const double edge = -(double)GYMAX + j * ((double)GYMAX * 2.0 / GBIN);
+                        const double edge = -(double)r.gymax + j * ((double)r.gymax * 2.0 / GBIN);
                         while (t < b1 && (double)y32(ks[t]) < edge) t++;
                         gbin.push_back(base + (j ? t : b0));
                     }
                     gbin.push_back(base + b1);
                 }
                 for (int k : ks) {
-                    double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
-                    gpos.push_back(make_double4(ri.carb[3 * k], ri.carb[3 * k + 1], ri.carb[3 * k + 2], 0.0));
-                    gpos32.push_back(make_float4((float)dx, (float)dy, (float)(ri.carb[3 * k + 2] - cz), 0.f));
+                    double dx = lp[3 * k] - cx, dy = lp[3 * k + 1] - cy;
+                    gpos.push_back(make_double4(lp[3 * k], lp[3 * k + 1], lp[3 * k + 2], 0.0));
+                    gpos32.push_back(make_float4((float)dx, (float)dy, (float)(lp[3 * k + 2] - cz), 0.f));
                 }
                 gstart.push_back((int)gpos.size());
             }
@@ -908,11 +1073,11 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     if ((e = fill_win(RS, d.rop4)) || (e = fill_win(2 * RS, d.rop3))) return e;
     {
         std::vector<double2> h(nh2, make_double2(0.0, 0.0));
-        for (int dz = -d2; dz <= d2; dz++)
-            for (int dy = -d2; dy <= d2; dy++)
-                for (int dx = -d2; dx <= d2; dx++) {
+        for (int dz = -d2.z; dz <= d2.z; dz++)
+            for (int dy = -d2.y; dy <= d2.y; dy++)
+                for (int dx = -d2.x; dx <= d2.x; dx++) {
                     if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-                    const int oi = (dx + d2) + w2 * ((dy + d2) + w2 * (dz + d2));
+                    const int oi = (dx + d2.x) + w2x * ((dy + d2.y) + w2y * (dz + d2.z));
                     harm_m2l(dx * 4 * RS, dy * 4 * RS, dz * 4 * RS, &h[(size_t)oi * NHARM]);
                 }
         if ((e = put(h, d.h_m2l2, d.h32_m2l2))) return e;
@@ -938,7 +1103,16 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
             CK(cudaStreamSynchronize(c->st));
         }
     }
-    std::vector<double2> ljt = make_lj_table();
+    std::vector<double2> ljt = c->chains ? make_lj_table_cfg(make_cfg_field()) : make_lj_table();
+    {
+        std::vector<double> kq, km;
+        std::vector<double2> kg;
+        kind_tables(c->p.preset, kq, km, kg);
+        CK(cudaMemcpyAsync(d.tq, kq.data(), NTYPE * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(d.tmass, km.data(), NTYPE * sizeof(double), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(d.tgr, kg.data(), NTYPE * sizeof(double2), cudaMemcpyHostToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+    }
     std::vector<float2> ljt32(ljt.size());
     for (size_t k = 0; k < ljt.size(); k++) ljt32[k] = make_float2((float)ljt[k].x, (float)ljt[k].y);
     CK(cudaMemcpyAsync(d.ljt32, ljt32.data(), ljt32.size() * sizeof(float2), cudaMemcpyHostToDevice, c->st));
@@ -1010,7 +1184,7 @@ int sesp_upload_batch(sesp_ctx *c, int n_rep, const int *n_water, const int *n_s
         r.pos = pos + 3 * so;
         r.vel = vel ? vel + 3 * so : nullptr;
         r.carb = carbons ? carbons + 3 * co : nullptr;
-        so += (size_t)3 * r.nw + (size_t)NSURF * r.ns;
+        so += (size_t)3 * r.nw + (size_t)c->ssite * r.ns;
         co += r.ncarb;
     }
     return upload_impl(c, in);
@@ -1218,8 +1392,8 @@ int sesp_set_tuning(sesp_ctx *c, int tile, int ctas_per_sm) {
     const int mixed = c->p.precision != SESP_PLAIN_FP64;
     if (tile != 32 && tile != 64 && !(mixed && tile == 128))
         return fail(SESP_EINVAL, "tile must be 32 or 64 (or 128 on the mixed paths)");
-    if (ctas_per_sm < 1 || ctas_per_sm > near_max_ctas_per_sm(mixed, tile))
-        return fail(SESP_EINVAL, "ctas_per_sm must be 1..%d", near_max_ctas_per_sm(mixed, tile));
+    if (ctas_per_sm < 1 || ctas_per_sm > near_max_ctas_per_sm(mixed, tile, c->chains))
+        return fail(SESP_EINVAL, "ctas_per_sm must be 1..%d", near_max_ctas_per_sm(mixed, tile, c->chains));
     if (set_device(c)) return SESP_ECUDA;
     const bool retile = tile != c->near.tile;
     c->near = {tile, c->n_sm * ctas_per_sm};
@@ -1235,7 +1409,7 @@ int sesp_tuning(sesp_ctx *c, int out[3]) {
     if (!out) return fail(SESP_EINVAL, "null output");
     out[0] = c->near.tile;
     out[1] = c->n_sm ? c->near.grid / c->n_sm : 0;
-    out[2] = near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64, c->near.tile);
+    out[2] = near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64, c->near.tile, c->chains);
     return 0;
 }
 
@@ -1299,9 +1473,9 @@ int tune_constraints(sesp_ctx *c) {
             copy(false);
             cudaEventRecord(e0, c->st);
             launch_move_a(d, c->wmols, c->nwm, c->smols, c->nsm, c->nrep, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit,
-                          c->p.precision, sh, c->st);
+                          c->p.precision, sh, c->chains, c->st);
             launch_move_b(d, c->wmols, c->nwm, c->smols, c->nsm, c->nmol, c->nsite, c->p.shake_tol, c->p.shake_maxit, c->p.precision, sh,
-                          c->st);
+                          c->chains, c->st);
             cudaEventRecord(e1, c->st);
             cudaEventSynchronize(e1);
             cudaEventElapsedTime(&t[r], e0, e1);
@@ -1339,18 +1513,18 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     NearShape pick = c->near;
     for (int tile : {128, 64, 32}) {
         if (tile == 128 && !mixed) continue;
-        const int mx = near_max_ctas_per_sm(mixed, tile);
+        const int mx = near_max_ctas_per_sm(mixed, tile, c->chains);
         const int cands[4] = {mx, (3 * mx) / 4, mx / 2, mx / 4};
         launch_near_items(c->d, c->ncell, (int)near_items_max(c->nsite, c->ncell), tile, c->st);
         for (int k = 0; k < 4; k++) {
             const int cps = cands[k];
             if (cps < 1 || (k > 0 && cps == cands[k - 1])) continue;
             const NearShape sh = {tile, c->n_sm * cps};
-            launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st, true);   // warm
+            launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st, true, c->chains);   // warm
             float t[5];
             for (int r = 0; r < 5; r++) {
                 cudaEventRecord(e0, c->st);
-                launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st, true);
+                launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st, true, c->chains);
                 cudaEventRecord(e1, c->st);
                 cudaEventSynchronize(e1);
                 cudaEventElapsedTime(&t[r], e0, e1);
@@ -1363,14 +1537,14 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     cudaEventDestroy(e1);
     c->near = pick;
     launch_near_items(c->d, c->ncell, (int)near_items_max(c->nsite, c->ncell), pick.tile, c->st);
-    if (mixed && c->nsm > 0)
+    if (mixed && c->nsm > 0 && !c->chains)   // flexible chains have no constraint sweeps to shape
         if (int e = tune_constraints(c)) return e;
     drop_graphs(c);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->st));
     out[0] = pick.tile;
     out[1] = pick.grid / c->n_sm;
-    out[2] = near_max_ctas_per_sm(mixed, pick.tile);
+    out[2] = near_max_ctas_per_sm(mixed, pick.tile, c->chains);
     return 0;
 }
 
@@ -1435,19 +1609,17 @@ int sesp_sync(sesp_ctx *c) {
 int sesp_temperature(sesp_ctx *c, double *t) {
     if (int e = check_ctx(c, true)) return e;
     if (!t) return fail(SESP_EINVAL, "null output");
-    int N = c->nsite;
-    std::vector<double> v(3 * (size_t)N);
-    if (int e = sesp_download_state(c, nullptr, v.data(), nullptr)) return e;
-    Tables T = make_tables();
+    if (set_device(c)) return SESP_ECUDA;
+    launch_temperature(c->d, c->nrep, c->st);
+    CK(cudaGetLastError());
+    std::vector<double> sums(c->nrep);
+    CK(cudaMemcpyAsync(sums.data(), c->d.tbuf, c->nrep * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
     double s = 0.0;
     long dof = 0;
-    for (const Rep &r : c->reps) {
-        for (int g = 0; g < r.nsite; g++) {
-            int pt = g < 3 * r.nw ? (g % 3 == 0 ? 0 : 1) : 2 + (g - 3 * r.nw) % NSURF;
-            size_t k = 3 * (size_t)(r.site0 + g);
-            s += T.mass[pt] * (v[k] * v[k] + v[k + 1] * v[k + 1] + v[k + 2] * v[k + 2]);
-        }
-        dof += 3L * r.nsite - (3L * r.nw + (long)NBOND * r.ns);
+    for (int q = 0; q < c->nrep; q++) {
+        s += sums[q];
+        dof += 3L * c->reps[q].nsite - c->reps[q].ncon;
     }
     *t = s / (DT * DT) / (double)dof;   // src/compute_temperature.f90:240-242
     return 0;
@@ -1481,7 +1653,7 @@ int sesp_energies(sesp_ctx *c, double out[8]) {
     CK(cudaMalloc(&em, 3 * sizeof(double) * (c->nsm + 1)));
     cudaMemsetAsync(es, 0, 3 * sizeof(double) * N, c->st);
     launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
-    launch_energies(c->d, c->ncell, N, c->smols, c->nsm, es, ei, em, c->st);
+    launch_energies(c->d, c->ncell, N, c->smols, c->nsm, c->chains, es, ei, em, c->st);
     std::vector<double> hs(3 * (size_t)N), hi(3 * (size_t)N), hm(3 * (size_t)(c->nsm + 1));
     cudaMemcpyAsync(hs.data(), es, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
     cudaMemcpyAsync(hi.data(), ei, hi.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
@@ -1578,7 +1750,7 @@ int sesp_energies_static(sesp_ctx *c, double out[8]) {
     double *tot = em + 3 * ((size_t)SESP_NOALLOC_MAX_SURF + 1);
     CK(cudaMemsetAsync(es, 0, 3 * sizeof(double) * N, c->st));
     launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
-    launch_energies(c->d, c->ncell, N, c->smols, c->nsm, es, ei, em, c->st);
+    launch_energies(c->d, c->ncell, N, c->smols, c->nsm, c->chains, es, ei, em, c->st);
     k_energy_totals<<<1, 32, 0, c->st>>>(es, ei, em, N, c->nsm, tot);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, tot, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
@@ -1617,7 +1789,7 @@ __global__ void k_checks(Dev d, double *out) {
     double q = 0.0;
     for (int m = t; m < r.nmol; m += CHECK_THREADS) {
         const int g0 = d.mfirst[r.mol0 + m];
-        const int ns = d.mkind[r.mol0 + m] == 0 ? 3 : NSURF;
+        const int ns = d.mkind[r.mol0 + m] == 0 ? 3 : r.ssite;
         int ok = 1;
         for (int k = 0; k < ns; k++) ok &= d.sloc[g0 + k] >= 0;
         mol_ok += ok;

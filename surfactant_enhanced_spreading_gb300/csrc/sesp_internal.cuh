@@ -9,6 +9,10 @@
 //    slots, which the pair kernel reads cell by cell;
 //  * multipole and local expansions (25 complex coefficients, order 4) per
 //    L4, L3 and L2 box.
+// Two force fields share the layout (Rep::per tells them apart): the
+// reference's (29-site surfactants, closed box) and the configuration
+// preset (12-bead chains, periodic in x and y; every site keeps the integer
+// image of its last rebuild, and the slot arrays hold positions wrapped by it).
 #pragma once
 
 #include <cstdint>
@@ -51,6 +55,11 @@ constexpr int NDIH = 30;
 constexpr int NSELF = 42;
 constexpr int NHARM = 45;    // M2L factors H_l^q, l = 0..2P, q = 0..l
 constexpr int NM2L = 316;     // 7^3 - 3^3 source offsets at L4 and L3
+// configuration preset: 12-bead chains (types 2..13), 11 bonds, 10 angles,
+// 9 dihedrals, 36 pairs four or more bonds apart
+constexpr int NCH = 12;
+constexpr int NCH_BOND = NCH - 1, NCH_ANGLE = NCH - 2, NCH_DIH = NCH - 3;
+constexpr int NCH_PAIR = (NCH - 4) * (NCH - 3) / 2;
 
 // reduced-unit constants of src/mybox.cmns:36-44 (xpi is a single-precision
 // literal in the reference, hence the float)
@@ -87,6 +96,11 @@ struct Rep {
     double rhs[3], rsd[3];
     double pnh1, pnh2;
     double irsd[3];   // 1 / rsd
+    int per;          // periodic in x and y (configuration preset)
+    int ssite;        // sites per surfactant (29, or 12 for the chains)
+    int igz;          // configuration preset: last cell layer the graphite acts on (-1: none)
+    int ncon;         // constraints (degrees of freedom removed)
+    float gymax;      // half-extent in y of a graphite column's carbons (bins)
 };
 
 // constant topology and force-field tables (reference values, src/init_arrays.f90)
@@ -104,6 +118,14 @@ struct Tables {
     double sgcs6[NSURF], epcs[NSURF];   // carbon - surfactant site LJ
     double sgcw6, epcw;                 // carbon - water O LJ
     double rfctr[LP];                   // sqrt((n-|m|)!/(n+|m|)!) by coefficient
+};
+
+// bonded terms of the configuration preset's chains (one table for every
+// chain; beads are types 2 + b)
+struct ChainTables {
+    double kb, r0;          // bonds: U = kb / 2 (r - r0)^2
+    double kth, th0;        // angles: U = kth / 2 (th - th0)^2
+    double dva, dvb, dvc;   // dihedrals: a (1 + cos) + b (1 - cos 2) + c (1 + cos 3)
 };
 
 struct Dev {
@@ -187,6 +209,13 @@ struct Dev {
     // LJ pair table (eps, sg6), NTYPE^2
     double2 *ljt;
     float2 *ljt32;       // FP32 copy of ljt
+    // per site kind (NTYPE): charge, mass, graphite LJ (48 eps sg6, sg6; zero
+    // without); the force field's values, so kernels shared by both presets
+    // read them here
+    double *tq, *tmass;
+    double2 *tgr;
+    short2 *simg;        // per site: x / y image of the last rebuild (periodic preset)
+    double *tbuf;        // [nrep] temperature sums
     // counters: [0] fails, [1] overflow, [2] unlocated, [3] max cell, [5] pairs, [6] LJ pairs
     unsigned long long *counters;
     int max_cell;

@@ -25,7 +25,10 @@ CHECK_MOLECULES_LOST, CHECK_CHARGE, CHECK_OH_RATIO, CHECK_MISSING_OXYGEN = 1, 2,
 RESCALE_TARGET = 3.9   # target of the reference's temperature-rescaling variant
 
 T_NEAR, T_FAR, T_VALENCE, T_DIHEDRAL, T_BERENDSEN = 1, 2, 4, 8, 16
-T_INTERNAL, T_SUBTRACT, T_WALL, T_GRAPHITE, T_ALL = 32, 64, 128, 256, 511
+T_INTERNAL, T_SUBTRACT, T_WALL, T_GRAPHITE = 32, 64, 128, 256
+T_BOND = 512       # harmonic chain bonds (configuration preset)
+T_ALL = 1023
+PRESET_REFERENCE, PRESET_CONFIG = 0, 1
 
 ERRORS = {1: "EINVAL", 2: "ECUDA", 3: "ENOMEM", 4: "ESTATE", 5: "ECAPACITY", 6: "ESHAKE", 7: "EBUDGET"}
 
@@ -37,7 +40,8 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts",
            "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes",
            "sesp_energies_static", "sesp_autotune", "sesp_tuning", "sesp_set_tuning", "sesp_checks",
-           "sesp_check_flags", "sesp_rescale_temperature", "sesp_set_constraint_tuning", "sesp_constraint_tuning"]
+           "sesp_check_flags", "sesp_rescale_temperature", "sesp_set_constraint_tuning", "sesp_constraint_tuning",
+           "sesp_default_config_params"]
 
 
 class SespError(RuntimeError):
@@ -48,7 +52,7 @@ class Params(ctypes.Structure):
     _fields_ = [("n_cells", ctypes.c_int * 3), ("precision", ctypes.c_int), ("rebuild_interval", ctypes.c_int),
                 ("graphite_on", ctypes.c_int), ("tr", ctypes.c_double), ("tau_steps", ctypes.c_double),
                 ("shake_tol", ctypes.c_double), ("shake_maxit", ctypes.c_int), ("device", ctypes.c_int),
-                ("max_cell_sites", ctypes.c_int)]
+                ("max_cell_sites", ctypes.c_int), ("preset", ctypes.c_int)]
 
 
 _lib = None
@@ -67,6 +71,7 @@ def load(path: str = LIB_PATH):
     L.sesp_abi_version.restype = ctypes.c_int
     L.sesp_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.sesp_default_params.argtypes = [ctypes.POINTER(Params)]
+    L.sesp_default_config_params.argtypes = [ctypes.POINTER(Params)]
     L.sesp_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(P)]
     L.sesp_destroy.argtypes = [P]
     L.sesp_upload_state.argtypes = [P, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int, dp]
@@ -128,10 +133,16 @@ def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def default_params(cells=(12, 12, 12), precision=PLAIN_FP64, **kw) -> Params:
+def default_params(cells=(12, 12, 12), precision=PLAIN_FP64, preset=PRESET_REFERENCE, **kw) -> Params:
+    """The engine's parameters for a force field (``preset``): the reference's
+    settings, or the configuration preset's (300 K, 0.1 ps thermostat, SHAKE
+    tolerance 1e-8); keywords override single fields."""
     L = load()
     p = Params()
-    _check(L.sesp_default_params(ctypes.byref(p)))
+    if preset == PRESET_CONFIG:
+        _check(L.sesp_default_config_params(ctypes.byref(p)))
+    else:
+        _check(L.sesp_default_params(ctypes.byref(p)))
     for a in range(3):
         p.n_cells[a] = int(cells[a])
     p.precision = int(precision)
@@ -149,7 +160,8 @@ class Engine:
             self._init_batch(list(system), precision, device, **kw)
             return
         self.system = system
-        p = default_params(system.cells, precision, device=device, graphite_on=int(system.graphite_on), **kw)
+        p = default_params(system.cells, precision, preset=getattr(system, "preset", 0), device=device,
+                           graphite_on=int(system.graphite_on), **kw)
         h = ctypes.c_void_p()
         _check(L.sesp_create(ctypes.byref(p), ctypes.byref(h)))
         self._h = h
@@ -168,7 +180,10 @@ class Engine:
         self.systems = systems
         self.system = systems[0]
         graphite = int(any(s.graphite_on for s in systems))
-        p = default_params(systems[0].cells, precision, device=device, graphite_on=graphite, **kw)
+        presets = {getattr(s, "preset", 0) for s in systems}
+        if len(presets) != 1:
+            raise ValueError("replicas of one context share one force field (preset)")
+        p = default_params(systems[0].cells, precision, preset=presets.pop(), device=device, graphite_on=graphite, **kw)
         h = ctypes.c_void_p()
         _check(L.sesp_create(ctypes.byref(p), ctypes.byref(h)))
         self._h = h

@@ -22,7 +22,7 @@ def test_library_exports_header_symbols():
     assert len(names) >= 20
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
-    assert lib.sesp_abi_version() == 1
+    assert lib.sesp_abi_version() == 2
 
 
 def test_python_binding_covers_header():
@@ -38,6 +38,18 @@ def test_params_layout_matches_header():
     assert list(p.n_cells) == [12, 12, 12]
     assert p.rebuild_interval == 10 and abs(p.tr - 3.81087) < 1e-15 and p.shake_maxit == 100
     assert abs(p.tau_steps - 7.5) < 1e-15 and abs(p.shake_tol - 1e-4) < 1e-18
+    assert p.preset == engine.PRESET_REFERENCE
+
+
+def test_config_params_defaults():
+    """The configuration preset's settings: 300 K, 0.1 ps thermostat (50 steps
+    of 2 fs), SHAKE tolerance 1e-8 (host code, no GPU)."""
+    from surfactant_enhanced_spreading_gb300 import config_preset as C
+    from surfactant_enhanced_spreading_gb300 import engine
+    p = engine.default_params((8, 8, 8), preset=engine.PRESET_CONFIG)
+    assert p.preset == engine.PRESET_CONFIG and list(p.n_cells) == [8, 8, 8]
+    assert abs(p.tr - C.TR) < 1e-12 and abs(p.tau_steps - 50.0) < 1e-9
+    assert p.shake_tol == 1e-8 and p.shake_maxit == 100
 
 
 def test_fortran_interface_module_lists_every_entry_point():
