@@ -1,27 +1,32 @@
 """Benchmark of the per-timestep force-and-integrate path.
 
-One step = move_a (Nose-Hoover predictor + SHAKE), the force section (near
-field, local-expansion force, intramolecular, walls, graphite; every 10th step
-also the cell sort, lists and far-field build) and move_b (RATTLE), exactly the
-body of the reference's step loop (src/mybox.f90:136-227).
+One step = move_a (Nose-Hoover predictor + SHAKE on the waters), the force
+section (near field, local-expansion force, chain bonded and intramolecular
+terms, walls, graphite; every 10th step also the cell sort, lists and
+far-field build) and move_b (RATTLE), the body of the reference's step loop
+(src/mybox.f90:136-227).
 
-Workload (default): the single-system mixed-precision configuration with the
-reference's force field: 20,000 SPC/E waters and 200 29-site trisiloxane
-surfactants on 4-layer AB graphite, closed box of 24 x 24 x 12 cells of 12 A
-(288 x 288 x 144 A), seeded synthetic droplet.  Metric: atom-steps/s (mobile
-sites x steps / s), with ns/day at 2 fs; the plain FP64 GPU path is measured on
-the same workload and reported beside it with the mixed path's force error.
+Workload (default): the large mixed-precision configuration in the
+configuration preset - 100,000 SPC waters + 1,000 12-bead surfactant chains
+(312,000 mobile sites) on 4-layer graphite, periodic in x and y, 40 x 40 x 16
+cells of 12 A (480 x 480 x 192 A), FMA order 4, SHAKE tolerance 1e-8,
+Nose-Hoover 0.1 ps, a seeded synthetic droplet.  Metric: atom-steps/s
+(mobile sites x steps / s), with ns/day at 2 fs; the plain FP64 GPU path is
+measured on the same workload beside it, with the mixed path's force error
+against it and against the FP64 oracle.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-Under torchrun each rank runs its own replica on its GPU (no collective in the
-data path; replicas only), timing is the max over ranks.
+With --gpus N > 1 outside torchrun the script starts N ranks itself (one per
+GPU); each rank runs its own replica of the workload (no collective in the
+data path: replicas only), the timing is the max over ranks.
 """
 from __future__ import annotations
 
 import argparse
-import math
 import json
+import math
 import os
+import socket
 import statistics
 import subprocess
 import sys
@@ -32,14 +37,20 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-WORKLOAD = dict(n_water=20000, n_surf=200, cells=(24, 24, 12), graphite_layers=4, seed=2024)
 DT_FS = 2.0
 FLOPS_COUL = 18       # per ordered site pair, Coulomb only (sqrt and divide as 1 each)
 FLOPS_LJ_EXTRA = 11   # added when the pair is LJ-active within rc
 FLOPS_L2P = 25 * 40   # local-expansion force per site
+# kernels launched per step on the configuration preset's mixed path (gather;
+# graphite and chain terms on the side stream; pair field + finish; site
+# forces; waters' constraint half, chains' half and the eta update for
+# move_a; the two constraint halves for move_b) and per rebuild step (cell
+# location, sort 3, work items 5, correction masks, graphite list, water
+# order 3, P2M, 2 M2M, multipole packing, 2 M2L, 2 L2L)
+LAUNCHES_STEP, LAUNCHES_REBUILD = 11, 22
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
@@ -52,7 +63,7 @@ def parse():
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
     ap.add_argument("--replicas", type=int, default=64)
     ap.add_argument("--requests", type=int, default=12)
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_info():
@@ -63,7 +74,8 @@ def dist_info():
 
 
 class Dist:
-    """torch.distributed only for the barrier and the max over ranks."""
+    """torch.distributed (gloo) only for the barrier and the max over ranks;
+    the data path has no collective."""
 
     def __init__(self, ws):
         self.ws = ws
@@ -91,27 +103,38 @@ class Dist:
             self.dist.destroy_process_group()
 
 
-def make_system(small):
-    from surfactant_enhanced_spreading_gb300 import system as S
+def workload(small):
+    from surfactant_enhanced_spreading_gb300 import config_preset as C
     if small:
-        return S.droplet(6000, 60, cells=(16, 16, 8), seed=7, graphite_layers=2)
-    w = WORKLOAD
-    return S.droplet(w["n_water"], w["n_surf"], cells=w["cells"], seed=w["seed"], graphite_layers=w["graphite_layers"])
+        return dict(n_water=6000, n_chain=60, cells=(16, 16, 8), graphite_layers=2, seed=7)
+    return dict(**C.C3, seed=2024)
+
+
+def workload_name(small):
+    if small:
+        return "small droplet 6,000 SPC waters + 60 12-bead chains, 16x16x8 cells, periodic x/y, configuration preset"
+    return ("large mixed-precision configuration: 100,000 SPC waters + 1,000 12-bead surfactant chains on 4-layer "
+            "graphite, periodic x/y, 40x40x16 cells of 12 A (480x480x192 A), FMA order 4, SHAKE tol 1e-8, "
+            "Nose-Hoover 0.1 ps, 300 K, configuration preset")
+
+
+def make_system(small):
+    from surfactant_enhanced_spreading_gb300 import config_preset as C
+    return C.config_droplet(**workload(small))
 
 
 def make_batch(n, seed, small=False):
     """Batched workload: n replicas, waters ~ logU[1k, 30k] (logU[300, 1k]
-    for --small), surfactants per water ~ U[0, 2%], each droplet on its own
-    2-layer sheet over the whole floor of the smallest closed box (multiples
-    of 4 cells) that holds it."""
-    from surfactant_enhanced_spreading_gb300 import serve
+    for --small), chains per water ~ U[0, 2%], each droplet on its own
+    periodic 2-layer sheet 2.5 droplet diameters across."""
+    from surfactant_enhanced_spreading_gb300 import serve, config_preset as C
     rng = np.random.default_rng(seed)
     lo, hi = (300, 1000) if small else (1000, 30000)
     out = []
     for k in range(n):
         nw = int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
         ns = int(round(nw * rng.uniform(0.0, 0.02)))
-        out.append(serve.make_request(k, nw, ns, 1, seed=int(rng.integers(1 << 30))).system)
+        out.append(serve.make_request(k, nw, ns, 1, seed=int(rng.integers(1 << 30)), preset=C.PRESET_CONFIG).system)
     return out
 
 
@@ -120,7 +143,8 @@ def run_batched(args, local, E):
     n_sites = sum(s.n_sites for s in systems)
     res = {"replicas": len(systems), "sites": n_sites,
            "workload": f"{len(systems)} replicas, waters ~ logU[{'300, 1k' if args.small else '1k, 30k'}], "
-                       "surfactants ~ U[0, 2%] of waters, 2-layer graphite over the box floor, seed 4242"}
+                       "12-bead chains ~ U[0, 2%] of waters, each on its own periodic 2-layer sheet 2.5 droplet "
+                       "diameters across, configuration preset, seed 4242"}
     for name, prec, steps in (("mixed", E.MIXED, 20), ("plain_fp64", E.PLAIN_FP64, 3)):
         eng = E.Engine(systems, prec, device=local)
         eng.force(True)
@@ -137,21 +161,50 @@ def run_batched(args, local, E):
 
 
 def run_served(args, local):
+    """Poisson requests in the configuration preset served with continuous
+    batching (mixed precision), and the same requests one at a time on the
+    plain FP64 path.  The plain one-at-a-time run is timed on a bounded
+    sample (the first 100-step chunk of each request, after its start-up
+    force call) and its latencies are those of the sequential queue with each
+    request taking its measured time per step x its steps."""
+    from surfactant_enhanced_spreading_gb300 import config_preset as C
     from surfactant_enhanced_spreading_gb300 import engine as E
     from surfactant_enhanced_spreading_gb300 import serve
     dist = (dict(water=(300, 1000), surf=(0, 10), steps=(100, 300)) if args.small else
             dict(water=(1000, 50000), surf=(0, 500), steps=(500, 5000)))
-    reqs = serve.poisson_requests(args.requests, 2.0, 777, **dist)
+    reqs = serve.poisson_requests(args.requests, 2.0, 777, preset=C.PRESET_CONFIG, **dist)
     srv = serve.Server(64 << 30, precision=E.MIXED, chunk=100, device=local, keep_state=False)
-    srv.run([serve.make_request(-1, 300, 3, 100, seed=1)])   # first use of the library
+    srv.run([serve.make_request(-1, 300, 3, 100, seed=1, preset=C.PRESET_CONFIG)])   # first use of the library
     t0 = time.perf_counter()
     results = srv.run(reqs)
     wall = time.perf_counter() - t0
     out = serve.summarize(results)
-    out.update({"requests": len(results), "arrivals_per_s": 2.0, "wall_s": wall,
-                "sample": f"{args.requests} seeded Poisson requests: waters ~ U{list(dist['water'])}, "
-                          f"surfactants ~ U{list(dist['surf'])}, steps ~ U{list(dist['steps'])} in 100-step chunks, "
-                          "mixed precision, HBM budget 64 GiB",
+    # one at a time, plain FP64: per request its rate over one 100-step chunk
+    per_step = {}
+    for req in reqs:
+        eng = E.Engine(req.system, E.PLAIN_FP64, device=local)
+        E.mybox_start(eng)
+        eng.run(99101, 1)
+        ms = eng.run_timed(99102, 100, flush_l2=False)
+        per_step[req.rid] = float(ms.mean()) / 1e3
+        eng.close()
+    t, lat, atom_steps = 0.0, [], 0.0
+    for req in sorted(reqs, key=lambda r: (r.arrival, r.rid)):
+        t = max(t, req.arrival) + per_step[req.rid] * req.steps
+        lat.append(t - req.arrival)
+        atom_steps += req.system.n_sites * req.steps
+    span = t - min(r.arrival for r in reqs)
+    out["one_at_a_time_plain_fp64"] = {
+        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+        "atom_steps_per_s": atom_steps / span, "span_s": span,
+        "how": "each request alone on the plain FP64 path, in arrival order with no overlap; its time per step "
+               "measured over one 100-step chunk (CUDA events) and multiplied by its step count"}
+    out["served_vs_one_at_a_time_plain"] = (out["atom_steps_per_s"] / out["one_at_a_time_plain_fp64"]["atom_steps_per_s"]
+                                            if out["atom_steps_per_s"] else None)
+    out.update({"arrivals_per_s": 2.0, "wall_s": wall,
+                "sample": f"{args.requests} seeded Poisson requests in the configuration preset: waters ~ "
+                          f"U{list(dist['water'])}, 12-bead chains ~ U{list(dist['surf'])}, steps ~ U{list(dist['steps'])} "
+                          "in 100-step chunks, mixed precision, HBM budget 64 GiB",
                 "peak_admitted_bytes": srv.peak_used})
     return out
 
@@ -202,12 +255,64 @@ class Clocks:
         return out
 
 
+def run_e2e(eng, s, kb, steps, D, ws):
+    """End to end through the C ABI with host buffers: every 10-step chunk
+    uploads the state from pinned host memory, runs, downloads the state."""
+    pos, vel, acc = eng.state()
+    try:
+        import torch
+        hp = torch.from_numpy(pos).pin_memory().numpy()
+        hv = torch.from_numpy(vel).pin_memory().numpy()
+        ha = torch.from_numpy(acc).pin_memory().numpy()
+    except Exception:
+        hp, hv, ha = pos, vel, acc
+    eta = eng.eta
+    chunks = max(1, steps // 10)
+    D.barrier()
+    t0 = time.perf_counter()
+    for c in range(chunks):
+        eng.set_state(hp, hv, ha, eta)
+        eng.run(kb, 10)
+        kb += 10
+        eng.state(out=(hp, hv, ha))
+        eta = eng.eta
+    t_e2e = D.max(time.perf_counter() - t0)
+    state_bytes = 3 * 3 * 8 * s.n_sites
+    return kb, {"value": ws * s.n_sites * 10 * chunks / t_e2e, "unit": "atom-steps/s",
+                "h2d_bytes_per_step": state_bytes / 10 + 8 / 10, "d2h_bytes_per_step": state_bytes / 10 + 8 / 10,
+                "how": "per 10-step chunk: sesp_set_state from pinned host pos/vel/acc + eta, sesp_run(10), "
+                       "sesp_download_state and the eta"}
+
+
+def run_dropin(eng, s, kb, steps):
+    """The drop-in call sequence a Fortran host makes (sesp_step and
+    sesp_temperature every step, the state downloaded every 100 steps)."""
+    steps = max(100, steps)
+    pos = np.empty((s.n_sites, 3))
+    vel = np.empty((s.n_sites, 3))
+    acc = np.empty((s.n_sites, 3))
+    t0 = time.perf_counter()
+    for k in range(steps):
+        eng.step(kb)
+        kb += 1
+        eng.temperature()
+        if (k + 1) % 100 == 0:
+            eng.state(out=(pos, vel, acc))
+    dt = time.perf_counter() - t0
+    return kb, {"value": s.n_sites * steps / dt, "unit": "atom-steps/s", "steps": steps,
+                "d2h_bytes_per_step": 8 + 3 * 3 * 8 * s.n_sites / 100, "h2d_bytes_per_step": 0,
+                "how": "sesp_step + sesp_temperature (one double per replica to the host) every step, "
+                       "sesp_download_state every 100 steps"}
+
+
 def run_ours(args, ws, rank, local):
-    import oracle as O  # the CPU-baseline leg only
+    import oracle as O  # the CPU-baseline leg and the error reference only
     from surfactant_enhanced_spreading_gb300 import engine as E
 
     D = Dist(ws)
+    t_gen = time.perf_counter()
     s = make_system(args.small)
+    t_gen = time.perf_counter() - t_gen
     n_sites = s.n_sites
 
     # --- mixed path: warm-up, then K steps with per-step CUDA events, cold L2
@@ -218,7 +323,6 @@ def run_ours(args, ws, rank, local):
     eng.run(kb, args.warmup)
     kb += args.warmup
     tile, ctas, ctas_max = eng.autotune()   # launch shapes (no effect on results)
-    surf_warps, mols_per_warp = eng.constraint_tuning()[:2]
     eng.run(kb, 1)
     kb += 1
     D.barrier()
@@ -226,20 +330,13 @@ def run_ours(args, ws, rank, local):
     clocks.start()
     step_ms = eng.run_timed(kb, args.steps, flush_l2=True)
     clk = clocks.stop()
+    n_rebuild = sum(1 for k in range(kb, kb + args.steps) if k % 10 == 0)
     kb += args.steps
     D.barrier()
     t_ms = D.max(float(step_ms.sum()))
     value = ws * n_sites * args.steps / (t_ms / 1e3)
     ms_per_step = t_ms / args.steps
-
-    # kernel launches in the timed region for this workload (waters, surfactants
-    # and graphite present): 9 per step (gather, graphite and intramolecular on
-    # the side stream, pair field + finish, site forces, constraint half + eta
-    # for move_a, the constraint half for move_b) and 22 more per rebuild step
-    # (locate, sort 3, work items 5, isub, graphite list, water order 3, P2M,
-    # 2 M2M, multipole packing, 2 M2L, 2 L2L)
-    n_rebuild = sum(1 for k in range(kb - args.steps, kb) if k % 10 == 0)
-    launches = 9 * args.steps + 22 * n_rebuild
+    launches = LAUNCHES_STEP * args.steps + LAUNCHES_REBUILD * n_rebuild
 
     # --- per-kernel durations over a second pass (events around kernel families)
     eng.enable_timing(True)
@@ -252,25 +349,26 @@ def run_ours(args, ws, rank, local):
     near_ms = kt[0]
     flops = ncoul * FLOPS_COUL + nlj * FLOPS_LJ_EXTRA + n_sites * FLOPS_L2P
     achieved = flops / (near_ms / 1e3) / 1e12 if near_ms > 0 else None
-    peak = fp32_nominal_tflops(local)
+    peak, peak_source = fp32_peak(local)
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "near_field_traffic.json")
     if os.path.exists(tpath):
         try:
-            traffic = json.load(open(tpath)).get("bytes_per_launch")
+            tj = json.load(open(tpath))
+            if tj.get("workload") == "C3":
+                traffic = tj.get("bytes_per_launch")
         except Exception:
             traffic = None
 
-    # --- the same mixed path with the constraint iterations in FP32 (a
-    # separate precision mode, reported beside the headline)
-    e32 = E.Engine(s, E.MIXED_FP32C, device=local)
-    e32.force(True)
-    e32.init_accel()
-    e32.run(99101, args.warmup)
-    c_ms = e32.run_timed(99101 + args.warmup, args.steps, flush_l2=True)
-    fp32c = {"value": n_sites * args.steps / (c_ms.sum() / 1e3), "unit": "atom-steps/s",
-             "ms_per_step": float(c_ms.mean()), "shake_failures": e32.counters()[0]}
-    del e32
+    # --- end to end through the C ABI with host buffers, and the drop-in loop
+    kb, e2e = run_e2e(eng, s, kb, args.steps, D, ws)
+    kb, dropin = run_dropin(eng, s, kb, 100) if ws == 1 else (kb, None)
+
+    # the mixed path with FP32 constraint corrections is a mode for the
+    # reference's tolerance (1e-4): FP32 corrections cannot resolve this
+    # preset's 1e-8 (the FP32 epsilon is 6e-8), so it is not timed here
+    fp32c = {"skipped": "FP32 constraint corrections cannot reach the SHAKE tolerance 1e-8 of this workload "
+                        "(FP32 epsilon 6e-8); SESP_MIXED_FP32C is for the reference's tolerance 1e-4"}
 
     # --- plain FP64 GPU path on the same workload, and the mixed force error
     plain = E.Engine(s, E.PLAIN_FP64, device=local)
@@ -285,63 +383,34 @@ def run_ours(args, ws, rank, local):
     plain_value = n_sites * args.plain_steps / (p_ms.sum() / 1e3)
     del plain
 
-    # --- end to end through the C ABI with host buffers: each 10-step chunk
-    # uploads the state from pinned host memory, runs, downloads the state
-    pos, vel, acc = eng.state()
-    try:
-        import torch
-        hp = torch.from_numpy(pos).pin_memory().numpy()
-        hv = torch.from_numpy(vel).pin_memory().numpy()
-        ha = torch.from_numpy(acc).pin_memory().numpy()
-    except Exception:
-        hp, hv, ha = pos, vel, acc
-    eta = eng.eta
-    chunks = max(1, args.steps // 10)
-    D.barrier()
-    t0 = time.perf_counter()
-    for c in range(chunks):
-        eng.set_state(hp, hv, ha, eta)
-        eng.run(kb, 10)
-        kb += 10
-        eng.state(out=(hp, hv, ha))
-        eta = eng.eta
-    t_e2e = D.max(time.perf_counter() - t0)
-    e2e_value = ws * n_sites * 10 * chunks / t_e2e
-    state_bytes = 3 * 3 * 8 * n_sites
-    e2e = {"value": e2e_value, "unit": "atom-steps/s", "h2d_bytes_per_step": state_bytes / 10,
-           "d2h_bytes_per_step": state_bytes / 10,
-           "how": "per 10-step chunk: sesp_set_state from pinned host pos/vel/acc, sesp_run(10), sesp_download_state"}
-
     # --- batched replicas and the served stream (single-GPU runs only)
     batched = run_batched(args, local, E) if (ws == 1 and not args.no_batched) else None
     served = run_served(args, local) if (ws == 1 and not args.no_served) else None
 
-    # --- CPU baseline: the oracle on the same workload, bounded sample
-    cpu = None
+    # --- CPU baseline and error reference: the FP64 oracle on the same workload
+    cpu, ferr_oracle = None, None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(s, O)
+        cpu, fo = cpu_baseline(s, O)
+        ferr_oracle = {"mixed": float(np.linalg.norm(f32 - fo) / np.linalg.norm(fo)),
+                       "plain_fp64": float(np.linalg.norm(f64 - fo) / np.linalg.norm(fo))}
 
     T = eng.temperature()
     cnt = eng.counters()
     D.close()
     if rank != 0:
         return
-    ns_day = value / n_sites * 86400 * DT_FS * 1e-6 if ws == 1 else value / ws / n_sites * 86400 * DT_FS * 1e-6
+    ns_day = value / ws / n_sites * 86400 * DT_FS * 1e-6
     line = {
         "metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 pair/multipole/bonded terms; f64 constraint iterations, thermostat, kinetic sums, positions",
         "data": "synthetic (seeded droplet; no dataset)",
-        "config": {"workload": ("small droplet 6,000 waters + 60 surfactants, 16x16x8 cells" if args.small else
-                                "single system, 20,000 SPC/E waters + 200 29-site trisiloxane surfactants on 4-layer "
-                                "graphite, 24x24x12 cells (288x288x144 A), reference force field"),
-                   "n_sites": n_sites, "precision": "mixed", "rebuild_interval": 10,
+        "config": {"workload": workload_name(args.small), "n_sites": n_sites, "precision": "mixed",
+                   "rebuild_interval": 10, "generation_s": t_gen,
                    "l2": "flushed between timed steps (256 MB write outside the timed intervals)",
                    "pair_field_shape": {"tile": tile, "ctas_per_sm": ctas, "ctas_per_sm_max": ctas_max,
                                         "how": "sesp_autotune before the timed steps"},
-                   "constraint_shape": {"surf_warps_per_cta": surf_warps, "surfactants_per_warp": mols_per_warp,
-                                        "how": "sesp_autotune"},
                    "parallelism": f"replicas x{ws}"},
         "ns_per_day": ns_day,
         "plain_fp64": {"value": plain_value, "unit": "atom-steps/s", "steps": args.plain_steps,
@@ -349,19 +418,20 @@ def run_ours(args, ws, rank, local):
         "mixed_vs_plain_speedup": value / ws / plain_value,
         "mixed_fp32_constraints": fp32c,
         "mixed_force_rms_rel_error": ferr,
+        "force_rms_rel_error_vs_oracle": ferr_oracle,
         "batched": batched,
         "served": served,
         "roofline": {"bound": "fp32", "kernel": "k_near<mixed> (pair + fused local-expansion force)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": (achieved / peak) if (achieved and peak) else None, "traffic": traffic,
-                     "peak_source": "nominal FP32 FMA rate: SMs x 128 lanes x 2 x max SM clock (no FP32 figure "
-                                    "in MEASURED_PEAKS.json)",
+                     "peak_source": peak_source,
                      "algorithmic_flops_per_launch": flops, "pairs_coulomb": ncoul, "pairs_lj": nlj,
                      "near_ms_per_launch": near_ms},
         "kernel_ms": {"near": kt[0], "site_and_intra": kt[4], "move_a": kt[2], "move_b": kt[3],
                       "rebuild_sort": kt[5], "far_build": kt[6]},
         "cpu_baseline": cpu,
         "e2e": e2e,
+        "e2e_dropin_loop": dropin,
         "gpu_launches": launches,
         "clocks": clk,
         "temperature": T,
@@ -370,30 +440,33 @@ def run_ours(args, ws, rank, local):
     print(json.dumps(line))
 
 
-def fp32_nominal_tflops(device):
+def fp32_peak(device):
+    """The FP32 FMA rate the pair field is measured against: measured live on
+    this GPU by the library's own FMA loop (sesp_fp32_peak, CUDA events), the
+    nominal SMs x 128 lanes x 2 x max SM clock beside it."""
+    from surfactant_enhanced_spreading_gb300 import engine as E
     try:
-        out = subprocess.run(["nvidia-smi", f"--id={device}", "--query-gpu=clocks.max.sm", "--format=csv,noheader,nounits"],
-                             capture_output=True, text=True, timeout=20).stdout.strip()
-        mhz = float(out.splitlines()[0])
+        mhz = float(subprocess.run(["nvidia-smi", f"--id={device}", "--query-gpu=clocks.max.sm",
+                                    "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                   timeout=20).stdout.strip().splitlines()[0])
     except Exception:
         mhz = 2070.0
-    sms = 152
+    nominal = 152 * 128 * 2 * mhz * 1e6 / 1e12
     try:
-        import torch
-        sms = torch.cuda.get_device_properties(device).multi_processor_count
+        return E.fp32_peak(device), (f"measured: FP32 FMA loop of this library (sesp_fp32_peak, best of 5, CUDA "
+                                     f"events) on this GPU; nominal {nominal:.1f} TFLOP/s")
     except Exception:
-        pass
-    return sms * 128 * 2 * mhz * 1e6 / 1e12
+        return nominal, "nominal FP32 FMA rate: SMs x 128 lanes x 2 x max SM clock (measurement failed)"
 
 
 def oracle_step_rate(s, O):
-    """The oracle (the FP64 C restatement of the reference, OpenMP over cells)
-    on the same system: after the start-up force call, one rebuild step
-    (kb = 99110) and one ordinary step (kb = 99111) are timed and combined on
-    the reference's schedule of one rebuild every 10 steps
-    (src/mybox.f90:24,140)."""
+    """The oracle (the FP64 C restatement, OpenMP over sites and cells) on the
+    same system: the start-up force call (its forces are the error
+    reference), then one rebuild step (kb = 99110) and one ordinary step
+    (kb = 99111) timed and combined on the schedule of one rebuild every 10
+    steps (src/mybox.f90:24,140)."""
     o = O.Oracle(s)
-    o.force(True)
+    fo = o.force(True)
     o.init_accel()
     t0 = time.perf_counter()
     o.step(99110)
@@ -402,32 +475,30 @@ def oracle_step_rate(s, O):
     o.step(99111)
     t_p = time.perf_counter() - t0
     per_step = (t_r + 9.0 * t_p) / 10.0
-    return s.n_sites / per_step, per_step, t_r, t_p, o
+    return s.n_sites / per_step, per_step, t_r, t_p, o, fo
 
 
 def cpu_baseline(s, O):
-    value, per_step, t_r, t_p, _ = oracle_step_rate(s, O)
-    return {"value": value, "unit": "atom-steps/s", "cores": O.threads(), "kind": "port",
-            "sample": f"1 rebuild step ({t_r:.2f} s) + 1 ordinary step ({t_p:.2f} s) of the full workload on "
-                      f"{O.threads()} OpenMP threads, combined as (rebuild + 9 ordinary) / 10"}
+    value, per_step, t_r, t_p, _, fo = oracle_step_rate(s, O)
+    return ({"value": value, "unit": "atom-steps/s", "cores": O.threads(), "kind": "port",
+             "sample": f"1 rebuild step ({t_r:.2f} s) + 1 ordinary step ({t_p:.2f} s) of the full workload on "
+                       f"{O.threads()} OpenMP threads, combined as (rebuild + 9 ordinary) / 10"}, fo)
 
 
 def run_reference(args, ws, rank, local, budget_s=90.0):
-    """The reference's own algorithm on the host cores: the oracle port on all
+    """The path's CPU implementation on the host cores: the oracle port on all
     OpenMP threads (the Fortran + MPI reference cannot be built here: no
-    Fortran compiler or MPI).  K steps are timed when they fit the time
-    budget, else the rebuild-weighted two-step sample stands for them."""
+    Fortran compiler or MPI; its own force field does not describe this
+    workload either).  K steps are timed when they fit the time budget, else
+    the rebuild-weighted two-step sample stands for them."""
     if rank != 0:
         return
     import oracle as O
     s = make_system(args.small)
-    value, per_step, t_r, t_p, o = oracle_step_rate(s, O)
+    value, per_step, t_r, t_p, o, _ = oracle_step_rate(s, O)
     steps = max(1, args.steps)
     if steps * per_step <= budget_s:
         kb0 = 99112
-        for k in range(min(args.warmup, 1)):
-            o.step(kb0)
-            kb0 += 1
         t0 = time.perf_counter()
         o.run(kb0, steps)
         elapsed = time.perf_counter() - t0
@@ -441,17 +512,31 @@ def run_reference(args, ws, rank, local, budget_s=90.0):
     line = {"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": 0, "steps": done,
             "warmup": 1, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded droplet)", "impl": "reference",
-            "config": {"workload": "same system as the GPU arm" + (" (small)" if args.small else ""),
-                       "n_sites": s.n_sites},
+            "config": {"workload": workload_name(args.small), "n_sites": s.n_sites},
             "cpu_baseline": {"value": value, "unit": "atom-steps/s", "cores": O.threads(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-def main():
-    args = parse()
+def spawn_ranks(args, argv):
+    """--gpus N outside torchrun: run this script as N ranks on this node."""
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={args.gpus}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + list(argv)
+    return subprocess.call(cmd)
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    args = parse(argv)
     ws, rank, local = dist_info()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(spawn_ranks(args, argv))
+    if args.gpus != ws:
+        raise SystemExit(f"--gpus {args.gpus} but WORLD_SIZE={ws}: launch with torchrun --nproc-per-node {args.gpus}")
     if args.impl == "reference":
         run_reference(args, ws, rank, local)
     else:

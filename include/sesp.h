@@ -273,6 +273,11 @@ int sesp_rescale_temperature(sesp_ctx *ctx, double target, double *t_before);
  * [0] near field, [1] local-expansion force, [2] move_a, [3] move_b,
  * [4] intramolecular + external, [5] rebuild (sort + lists), [6] far-field build */
 int sesp_kernel_times(sesp_ctx *ctx, double out[8], int reset);
+/* The FP32 fused multiply-add throughput of a device in TFLOP/s: a loop of
+ * independent FMA chains over (SMs x 8) CTAs, best of 5 launches timed with
+ * CUDA events.  The ceiling the FP32 pair field is measured against (the
+ * reference has no counterpart; a diagnostic of the GPU build). */
+int sesp_fp32_peak(int device, double *tflops);
 int sesp_enable_timing(sesp_ctx *ctx, int on);
 
 #ifdef __cplusplus

@@ -238,5 +238,10 @@ module sesp_mod
       type(c_ptr), value :: ctx
       integer(c_int64_t), intent(out) :: bytes
     end function
+    integer(c_int) function sesp_fp32_peak(device, tflops) bind(C, name="sesp_fp32_peak")
+      import :: c_int, c_double
+      integer(c_int), value :: device
+      real(c_double), intent(out) :: tflops
+    end function
   end interface
 end module sesp_mod

@@ -1985,6 +1985,48 @@ __global__ void __launch_bounds__(TEMP_THREADS) k_temperature(Dev d) {
 
 void launch_temperature(const Dev &d, int nrep, cudaStream_t st) { k_temperature<<<nrep, TEMP_THREADS, 0, st>>>(d); }
 
+// FP32 FMA throughput: every thread runs 8 independent chains of `iters`
+// fused multiply-adds (enough to cover the pipe's latency), and writes one
+// value so nothing is optimised away.  2 flops per FMA.
+__global__ void __launch_bounds__(256) k_fma_peak(float *out, int iters, float a, float b) {
+    float x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = (float)(threadIdx.x + k);
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = fmaf(x[k], a, b);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += x[k];
+    if (s == 1234.5f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+// best of 5 launches of k_fma_peak over (SMs x 8) CTAs of 256 threads, in TFLOP/s
+double measure_fp32_peak(int n_sm, cudaStream_t st) {
+    float *out = nullptr;
+    if (cudaMalloc(&out, (size_t)n_sm * 8 * 256 * sizeof(float)) != cudaSuccess) return 0.0;
+    const int iters = 8192;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int r = 0; r < 6; r++) {
+        cudaEventRecord(e0, st);
+        k_fma_peak<<<n_sm * 8, 256, 0, st>>>(out, iters, 0.999f, 0.001f);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (r > 0 && ms < best) best = ms;   // the first launch warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(out);
+    const double flops = 2.0 * 8.0 * iters * (double)n_sm * 8 * 256;
+    return best < 1e29f ? flops / (best * 1e-3) / 1e12 : 0.0;
+}
+
 // writes a buffer larger than the L2 cache so the next launch starts cold
 __global__ void k_flush(float4 *buf, size_t n) {
     size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;

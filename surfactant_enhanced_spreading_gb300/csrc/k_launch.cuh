@@ -73,6 +73,8 @@ void launch_intra(const Dev &d, const int *smols, int ns, int terms, int mixed, 
 void upload_chain_tables(const ChainTables &t, cudaStream_t st);
 void launch_count_pairs(const Dev &d, int ncell, unsigned long long *out, cudaStream_t st);
 void launch_flush(void *buf, size_t bytes, cudaStream_t st);
+// FP32 FMA throughput of the device in TFLOP/s (an FMA loop timed with CUDA events)
+double measure_fp32_peak(int n_sm, cudaStream_t st);
 void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int ns, int chains, double *e_slot,
                      double *e_site, double *e_mol, cudaStream_t st);
 // per-replica sums of m v^2 in a fixed order (one block per replica) into d.tbuf

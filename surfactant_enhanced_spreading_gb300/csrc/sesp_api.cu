@@ -1875,6 +1875,24 @@ int sesp_rescale_temperature(sesp_ctx *c, double target, double *t_before) {
     return 0;
 }
 
+int sesp_fp32_peak(int device, double *tflops) {
+    if (!tflops) return fail(SESP_EINVAL, "null output");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev)
+        return fail(SESP_EINVAL, "device %d not available", device);
+    CK(cudaSetDevice(device));
+    int n_sm = 0;
+    CK(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device));
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const double v = measure_fp32_peak(n_sm, st);
+    cudaStreamDestroy(st);
+    CK(cudaGetLastError());
+    if (!(v > 0.0)) return fail(SESP_ECUDA, "FP32 peak measurement failed");
+    *tflops = v;
+    return 0;
+}
+
 int sesp_kernel_times(sesp_ctx *c, double out[8], int reset) {
     if (int e = check_ctx(c, false)) return e;
     if (!out) return fail(SESP_EINVAL, "null output");

@@ -41,7 +41,7 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes",
            "sesp_energies_static", "sesp_autotune", "sesp_tuning", "sesp_set_tuning", "sesp_checks",
            "sesp_check_flags", "sesp_rescale_temperature", "sesp_set_constraint_tuning", "sesp_constraint_tuning",
-           "sesp_default_config_params"]
+           "sesp_default_config_params", "sesp_fp32_peak"]
 
 
 class SespError(RuntimeError):
@@ -72,6 +72,7 @@ def load(path: str = LIB_PATH):
     L.sesp_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
     L.sesp_default_params.argtypes = [ctypes.POINTER(Params)]
     L.sesp_default_config_params.argtypes = [ctypes.POINTER(Params)]
+    L.sesp_fp32_peak.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
     L.sesp_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(P)]
     L.sesp_destroy.argtypes = [P]
     L.sesp_upload_state.argtypes = [P, ctypes.c_int, ctypes.c_int, dp, dp, ctypes.c_int, dp]
@@ -111,6 +112,13 @@ def load(path: str = LIB_PATH):
     L.sesp_rescale_temperature.argtypes = [P, ctypes.c_double, dp]
     _lib = L
     return L
+
+
+def fp32_peak(device: int = 0) -> float:
+    """Measured FP32 FMA throughput of the device (TFLOP/s)."""
+    v = ctypes.c_double()
+    _check(load().sesp_fp32_peak(int(device), ctypes.byref(v)))
+    return v.value
 
 
 def check_flags(counts) -> int:

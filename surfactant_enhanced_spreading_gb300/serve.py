@@ -27,6 +27,7 @@ import time
 
 import numpy as np
 
+from . import config_preset as CP
 from . import engine as E
 from . import system as S
 
@@ -73,7 +74,16 @@ def cells_for(n_water: int, n_surf: int) -> tuple:
     return (max(cx, 4), max(cx, 4), max(cz, 4))
 
 
-def make_request(rid: int, n_water: int, n_surf: int, steps: int, seed: int, arrival: float = 0.0) -> Request:
+def make_request(rid: int, n_water: int, n_surf: int, steps: int, seed: int, arrival: float = 0.0,
+                 preset: int = 0) -> Request:
+    """One droplet run.  preset 0: the reference's force field in a closed
+    box; preset 1: the configuration preset, 12-bead chains, on a periodic
+    2-layer sheet 2.5 droplet diameters across."""
+    if preset == CP.PRESET_CONFIG:
+        n = CP.sheet_cells(n_water)
+        cells = (n, n, CP.box_height_cells(n_water, n_surf))
+        s = CP.config_droplet(n_water, n_surf, cells=cells, seed=seed, graphite_layers=2)
+        return Request(rid=rid, system=s, steps=steps, arrival=arrival)
     cells = list(cells_for(n_water, n_surf))
     for _ in range(4):
         try:
@@ -98,8 +108,10 @@ def estimate_bytes(system: S.System) -> int:
     nc = np.array(system.cells, dtype=np.int64)
     ncell = int(np.prod(nc))
     n3, n2 = ncell // 8, ncell // 64
-    d2 = max(1, int((nc // 4).max()) - 1)
-    w2 = 2 * d2 + 1
+    per = getattr(system, "preset", 0) == CP.PRESET_CONFIG
+    # the L2 far-field table: offsets reach one more box length along periodic axes
+    reach = [2 * int(nc[a] // 4) - 1 if (per and a < 2) else int(nc[a] // 4) - 1 for a in range(3)]
+    w2 = int(np.prod([2 * max(1, r) + 1 for r in reach])) ** (1.0 / 3.0)
     per_site = 12 * 8 + 1 + 4 * 4 + 32 + 16 + 8 + 4 + 3 * 8 + 27 * 8 + 6 + 3 * 8 + 12 * 8
     per_mol = 5 * 4 + 2 * 8 + 4 + 4 + 2 * 4 + 2   # incl. the constraint halves' water lists and sweep counts
     cz = 25 * 16
@@ -112,8 +124,11 @@ def estimate_bytes(system: S.System) -> int:
     ops += 8 * (2 * 343 * 25 * 28 + pad4 + pad3 + 21 * 25 * (ncell + n3)) + 16 * 16 * (ncell // 1024 + 1) + 8 * 189 * 4
     ncarb = system.carbons.reshape(-1, 3).shape[0]
     ncol = int(nc[0] * nc[1])
-    graphite = 12 * ncarb * 48 + (ncol + 1) * 4 + ncol * 8 * (33 * 4 + 8) + int(nc.sum()) * 8 + n * 4
-    surf = 29 * system.n_surf * 4
+    # each carbon lies within reach of about 8 bottom-layer columns (12 with
+    # the periodic preset's wider reach)
+    reach_cols = 12 if per else 8
+    graphite = reach_cols * ncarb * 48 + (ncol + 1) * 4 + ncol * 8 * (33 * 4 + 8) + int(nc.sum()) * 8 + n * 4
+    surf = system.sites_per_surf * system.n_surf * 4 + n * 4
     total = n * per_site + nmol * per_mol + cells + ops + graphite + surf + 4096
     return int(1.1 * total) + (1 << 20)
 
@@ -212,7 +227,7 @@ def summarize(results: list[Result], wall: float | None = None) -> dict:
 
 
 def poisson_requests(n: int, rate_per_s: float, seed: int, water=(1000, 50000), surf=(0, 500), steps=(500, 5000),
-                     step_quantum: int = 100) -> list[Request]:
+                     step_quantum: int = 100, preset: int = 0) -> list[Request]:
     """Seeded Poisson arrivals of seeded droplet runs."""
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -222,7 +237,7 @@ def poisson_requests(n: int, rate_per_s: float, seed: int, water=(1000, 50000), 
         nw = int(rng.integers(water[0], water[1] + 1))
         ns = int(rng.integers(surf[0], surf[1] + 1))
         st = int(rng.integers(steps[0] // step_quantum, steps[1] // step_quantum + 1)) * step_quantum
-        out.append(make_request(k, nw, ns, st, seed=int(rng.integers(1 << 30)), arrival=t))
+        out.append(make_request(k, nw, ns, st, seed=int(rng.integers(1 << 30)), arrival=t, preset=preset))
     return out
 
 
