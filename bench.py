@@ -63,6 +63,8 @@ def parse(argv=None):
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
     ap.add_argument("--replicas", type=int, default=64)
     ap.add_argument("--requests", type=int, default=12)
+    ap.add_argument("--headline-only", action="store_true",
+                    help="only the mixed path's timed steps and kernel pass (profiling)")
     return ap.parse_args(argv)
 
 
@@ -359,6 +361,19 @@ def run_ours(args, ws, rank, local):
                 traffic = tj.get("bytes_per_launch")
         except Exception:
             traffic = None
+
+    if args.headline_only:
+        D.close()
+        if rank == 0:
+            print(json.dumps({"metric": "atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": ws,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+                              "config": {"workload": workload_name(args.small), "n_sites": n_sites},
+                              "kernel_ms": {"near": kt[0], "site_and_intra": kt[4], "move_a": kt[2], "move_b": kt[3],
+                                            "rebuild_sort": kt[5], "far_build": kt[6]},
+                              "roofline": {"achieved": achieved, "peak": peak, "frac": achieved / peak if achieved else None},
+                              "gpu_launches": launches, "clocks": clk, "shake_failures": eng.counters()[0],
+                              "headline_only": True}))
+        return
 
     # --- end to end through the C ABI with host buffers, and the drop-in loop
     kb, e2e = run_e2e(eng, s, kb, args.steps, D, ws)

@@ -335,6 +335,200 @@ __device__ __forceinline__ int water_b(const Dev &d, int m, double tol, int maxi
     return it;
 }
 
+// ---------------------------------------------------------------- waters in matrix form
+
+// Configuration preset, mixed path: the SHAKE / RATTLE of a water as the 3 x 3
+// system of its three constraints (matrix SHAKE: Kraeutler, van Gunsteren and
+// Huenenberger, J. Comput. Chem. 22, 501 (2001)).  The corrections keep
+// SHAKE's form - bond b moves its sites along its old bond vector R_b,
+// site k by g_b s_kb R_b / m_k (s = +1 for the bond's first site, -1 for its
+// second) - and the same stopping test, |d^2 - |P_b|^2| <= 2 tol d^2 for
+// every bond; only the update differs: instead of Gauss-Seidel sweeps over
+// the bonds (about 31 of them at this preset's tolerance 1e-8, where the
+// water triangle's coupling slows them), Newton steps with the Jacobian of
+// the predictor, J_bc = -2 P_b . K_bc R_c (K_bc = dP_b / d(g_c R_c)), about 4
+// at 1e-8.  RATTLE's constraints R_b . V_b = 0 are linear in the corrections:
+// one solve of A h = -R.V (A_bc = R_b . K_bc R_c) meets them, checked with
+// RATTLE's own test.  Both converge to the constrained state the sweeps
+// approach, so the result differs from the sweeps' by less than the
+// tolerance.
+
+// K_bc of the water triangle (bond b joins sites b and b + 1 mod 3): the
+// sum of the inverse masses on the diagonal, minus the inverse mass of the
+// shared site off it
+__device__ __forceinline__ double wk(int b, int c) {
+    if (b == c) return cF.rm64[wkind(wbi(b))] + cF.rm64[wkind(wbj(b))];
+    const int shared = (wbi(b) == wbi(c) || wbi(b) == wbj(c)) ? wbi(b) : wbj(b);
+    return -cF.rm64[wkind(shared)];
+}
+// s_kb: +1 if site k is bond b's first site, -1 if its second, else 0
+__device__ __forceinline__ double wsgn(int k, int b) { return k == wbi(b) ? 1.0 : (k == wbj(b) ? -1.0 : 0.0); }
+
+__device__ __forceinline__ void inv3(const double (&A)[3][3], double (&B)[3][3]) {
+    B[0][0] = A[1][1] * A[2][2] - A[1][2] * A[2][1];
+    B[0][1] = A[0][2] * A[2][1] - A[0][1] * A[2][2];
+    B[0][2] = A[0][1] * A[1][2] - A[0][2] * A[1][1];
+    B[1][0] = A[1][2] * A[2][0] - A[1][0] * A[2][2];
+    B[1][1] = A[0][0] * A[2][2] - A[0][2] * A[2][0];
+    B[1][2] = A[0][2] * A[1][0] - A[0][0] * A[1][2];
+    B[2][0] = A[1][0] * A[2][1] - A[1][1] * A[2][0];
+    B[2][1] = A[0][1] * A[2][0] - A[0][0] * A[2][1];
+    B[2][2] = A[0][0] * A[1][1] - A[0][1] * A[1][0];
+    const double id = 1.0 / (A[0][0] * B[0][0] + A[0][1] * B[1][0] + A[0][2] * B[2][0]);
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int j = 0; j < 3; j++) B[i][j] *= id;
+}
+
+// SHAKE half of one water in matrix form; returns the Newton steps it ran
+__device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int maxit) {
+    const int g0 = d.mfirst[m];
+    const double escale = __dsub_rn(1.0, __dmul_rn(d.eta[d.mrep[m]], DT) * 0.5);
+    double r[3][3], p[3][3], v[3][3];
+    double ke0 = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int g = g0 + i;
+        const double vx = d.vx[g], vy = d.vy[g], vz = d.vz[g], ax = d.ax[g], ay = d.ay[g], az = d.az[g];
+        r[i][0] = d.x[g]; r[i][1] = d.y[g]; r[i][2] = d.z[g];
+        ke0 = __dadd_rn(ke0, __dmul_rn(cF.mass64[wkind(i)],
+                                       __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
+        p[i][0] = pred_a(r[i][0], vx, ax, escale);
+        p[i][1] = pred_a(r[i][1], vy, ay, escale);
+        p[i][2] = pred_a(r[i][2], vz, az, escale);
+        v[i][0] = vel_a(vx, ax, escale);
+        v[i][1] = vel_a(vy, ay, escale);
+        v[i][2] = vel_a(vz, az, escale);
+    }
+    double R[3][3], P[3][3], D0[3], thr[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+        const int i = wbi(b), j = wbj(b);
+#pragma unroll
+        for (int a = 0; a < 3; a++) { R[b][a] = r[i][a] - r[j][a]; P[b][a] = p[i][a] - p[j][a]; }
+        D0[b] = cF.dsq64_w[b] - (P[b][0] * P[b][0] + P[b][1] * P[b][1] + P[b][2] * P[b][2]);
+        thr[b] = cF.dsq64_w[b] * (2.0 * tol);
+    }
+    double J[3][3], Ji[3][3];
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            J[b][c] = -2.0 * wk(b, c) * (P[b][0] * R[c][0] + P[b][1] * R[c][1] + P[b][2] * R[c][2]);
+    inv3(J, Ji);
+    double cc[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};   // per-site corrections
+    int it = 0;
+    bool done = false;
+    while (it <= maxit) {
+        double f[3];
+        done = true;
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const int i = wbi(b), j = wbj(b);
+            double q = 0.0;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const double cd = cc[i][a] - cc[j][a];
+                q += cd * (cd + 2.0 * P[b][a]);
+            }
+            f[b] = D0[b] - q;   // d^2 - |P_b + c_i - c_j|^2
+            done = done && !(fabs(f[b]) > thr[b]);
+        }
+        if (done) break;
+        double dg[3];
+#pragma unroll
+        for (int b = 0; b < 3; b++) dg[b] = -(Ji[b][0] * f[0] + Ji[b][1] * f[1] + Ji[b][2] * f[2]);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const double rm = cF.rm64[wkind(k)];
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                const double w = wsgn(k, b) * rm * dg[b];
+                if (w != 0.0) { cc[k][0] += w * R[b][0]; cc[k][1] += w * R[b][1]; cc[k][2] += w * R[b][2]; }
+            }
+        }
+        it++;
+    }
+    double ke1 = 0.0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int g = g0 + i;
+        d.x[g] = p[i][0] + cc[i][0]; d.y[g] = p[i][1] + cc[i][1]; d.z[g] = p[i][2] + cc[i][2];
+        const double vx = v[i][0] + cc[i][0], vy = v[i][1] + cc[i][1], vz = v[i][2] + cc[i][2];
+        d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
+        ke1 = __dadd_rn(ke1, __dmul_rn(cF.mass64[wkind(i)],
+                                       __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
+    }
+    d.ke[2 * m] = ke0;
+    d.ke[2 * m + 1] = ke1;
+    if (!done) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    return it + 1;
+}
+
+// RATTLE half of one water in matrix form; returns the solves it ran
+__device__ __forceinline__ int water_b_mat(const Dev &d, int m, double tol, int maxit) {
+    const int g0 = d.mfirst[m];
+    const double escale = 2.0 * recip64(__dadd_rn(2.0, __dmul_rn(d.eta[d.mrep[m]], DT)));
+    double r[3][3], v[3][3];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int g = g0 + i;
+        const double h = cF.dt2m64[wkind(i)];
+        const double ax = d.fx[g] * h, ay = d.fy[g] * h, az = d.fz[g] * h;
+        d.ax[g] = ax; d.ay[g] = ay; d.az[g] = az;
+        v[i][0] = __dmul_rn(escale, __dadd_rn(d.vx[g], ax));
+        v[i][1] = __dmul_rn(escale, __dadd_rn(d.vy[g], ay));
+        v[i][2] = __dmul_rn(escale, __dadd_rn(d.vz[g], az));
+        r[i][0] = d.x[g]; r[i][1] = d.y[g]; r[i][2] = d.z[g];
+    }
+    double R[3][3];
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int a = 0; a < 3; a++) R[b][a] = r[wbi(b)][a] - r[wbj(b)][a];
+    double A[3][3], Ai[3][3];
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) A[b][c] = wk(b, c) * (R[b][0] * R[c][0] + R[b][1] * R[c][1] + R[b][2] * R[c][2]);
+    inv3(A, Ai);
+    int it = 0;
+    bool done = false;
+    while (it <= maxit) {
+        double rv[3];
+        done = true;
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const int i = wbi(b), j = wbj(b);
+            rv[b] = R[b][0] * (v[i][0] - v[j][0]) + R[b][1] * (v[i][1] - v[j][1]) + R[b][2] * (v[i][2] - v[j][2]);
+            // RATTLE's test: -(R.V / dt) / ((1/m_i + 1/m_j) d^2)
+            done = done && !(fabs(cF.fb64_w[b] * rv[b]) > tol);
+        }
+        if (done) break;
+        double h[3];
+#pragma unroll
+        for (int b = 0; b < 3; b++) h[b] = -(Ai[b][0] * rv[0] + Ai[b][1] * rv[1] + Ai[b][2] * rv[2]);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const double rm = cF.rm64[wkind(k)];
+#pragma unroll
+            for (int b = 0; b < 3; b++) {
+                const double w = wsgn(k, b) * rm * h[b];
+                if (w != 0.0) { v[k][0] += w * R[b][0]; v[k][1] += w * R[b][1]; v[k][2] += w * R[b][2]; }
+            }
+        }
+        it++;
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int g = g0 + i;
+        d.vx[g] = v[i][0]; d.vy[g] = v[i][1]; d.vz[g] = v[i][2];
+    }
+    if (!done) { d.mfail[m] += 1; atomicAdd(&d.counters[0], 1ull); }
+    return it + 1;
+}
+
 // ---------------------------------------------------------------- surfactants
 
 // Gauss-Seidel sweeps as a wavefront: sweep k starts WF_LAG bonds after
@@ -715,6 +909,7 @@ struct CPlan {
     int s_warps;        // surfactant warps in each of them
     int mpw;            // surfactants per warp (groups of 4 lanes), 1..MPW
     int nmol, nsite;    // bounds every listed molecule is checked against
+    int mat;            // waters in matrix form (configuration preset, FP64 corrections)
 };
 
 // a listed molecule with its nsites sites inside the state arrays; a list
@@ -765,7 +960,11 @@ __global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double
                     atomicAdd(&d.counters[7], 1ull);
                     continue;
                 }
-                const int sweeps = SHAKE ? water_a<C>(d, m, tol, maxit) : water_b<C>(d, m, tol, maxit);
+                int sweeps;
+                if (std::is_same<C, double>::value && p.mat)
+                    sweeps = SHAKE ? water_a_mat(d, m, tol, maxit) : water_b_mat(d, m, tol, maxit);
+                else
+                    sweeps = SHAKE ? water_a<C>(d, m, tol, maxit) : water_b<C>(d, m, tol, maxit);
                 p.wsw[m] = (uint8_t)(sweeps < 255 ? sweeps : 255);
             }
         }
@@ -874,8 +1073,9 @@ constexpr size_t surf_smem(int s_warps, int mpw) {
 
 template <typename C, bool SHAKE>
 void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, int nmol, int nsite, const ConstraintShape &sh,
-                        double tol, int maxit, cudaStream_t st) {
+                        double tol, int maxit, cudaStream_t st, int mat) {
     CPlan p;
+    p.mat = mat;
     p.smols = smols;
     p.wlist = SHAKE ? d.wlist_a : d.wlist_b;
     p.wsw = SHAKE ? d.wsw_a : d.wsw_b;
@@ -907,17 +1107,17 @@ void init_constraint_kernels() {
 
 // fp32: 1 for FP32 sweeps, 0 for FP64 sweeps
 void launch_move_a32(const Dev &d, int nw, const int *smols, int ns, int nmol, int nsite, const ConstraintShape &sh,
-                     cudaStream_t st, double tol, int maxit, int fp32) {
+                     cudaStream_t st, double tol, int maxit, int fp32, int mat) {
     if (!nw && !ns) return;
-    if (fp32) launch_constrain_t<float, true>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st);
-    else launch_constrain_t<double, true>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st);
+    if (fp32) launch_constrain_t<float, true>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st, 0);
+    else launch_constrain_t<double, true>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st, mat);
 }
 
 void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, int nmol, int nsite, const ConstraintShape &sh,
-                     cudaStream_t st, double tol, int maxit, int fp32) {
+                     cudaStream_t st, double tol, int maxit, int fp32, int mat) {
     if (!nw && !ns) return;
-    if (fp32) launch_constrain_t<float, false>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st);
-    else launch_constrain_t<double, false>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st);
+    if (fp32) launch_constrain_t<float, false>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st, 0);
+    else launch_constrain_t<double, false>(d, smols, ns, nw, nmol, nsite, sh, tol, maxit, st, mat);
 }
 
 void launch_water_order(const Dev &d, const int *wmols, int nw, cudaStream_t st) {

@@ -589,13 +589,13 @@ void launch_isub(const Dev &d, int nsurf_sites, const int *surf_mols, int per, c
 void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nrep, int nmol, int nsite,
                    double tol, int maxit, int fast, const ConstraintShape &sh, int chains, cudaStream_t st) {
     if (chains) {   // flexible chains: constraints on the waters only
-        if (fast) launch_move_a32(d, nw, smols, 0, nmol, nsite, sh, st, tol, maxit, fast == 2);
+        if (fast) launch_move_a32(d, nw, smols, 0, nmol, nsite, sh, st, tol, maxit, fast == 2, 1);
         else if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
         if (ns) k_move_free_a<<<(ns + 127) / 128, 128, 0, st>>>(d, smols, ns);
         return;
     }
     if (fast) {
-        launch_move_a32(d, nw, smols, ns, nmol, nsite, sh, st, tol, maxit, fast == 2);
+        launch_move_a32(d, nw, smols, ns, nmol, nsite, sh, st, tol, maxit, fast == 2, 0);
     } else {
         if (ns) k_move_a_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
@@ -605,13 +605,13 @@ void launch_eta(const Dev &d, int nrep, cudaStream_t st) { k_eta<<<nrep * ETA_BL
 void launch_move_b(const Dev &d, const int *wmols, int nw, const int *smols, int ns, int nmol, int nsite, double tol,
                    int maxit, int fast, const ConstraintShape &sh, int chains, cudaStream_t st) {
     if (chains) {
-        if (fast) launch_move_b32(d, nw, smols, 0, nmol, nsite, sh, st, tol, maxit, fast == 2);
+        if (fast) launch_move_b32(d, nw, smols, 0, nmol, nsite, sh, st, tol, maxit, fast == 2, 1);
         else if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
         if (ns) k_move_free_b<<<(ns * NCH + 255) / 256, 256, 0, st>>>(d, smols, ns);
         return;
     }
     if (fast) {
-        launch_move_b32(d, nw, smols, ns, nmol, nsite, sh, st, tol, maxit, fast == 2);
+        launch_move_b32(d, nw, smols, ns, nmol, nsite, sh, st, tol, maxit, fast == 2, 0);
     } else {
         if (ns) k_move_b_surf<<<(ns + SURF_BLOCK - 1) / SURF_BLOCK, SURF_BLOCK, 0, st>>>(d, smols, ns, tol, maxit);
         if (nw) k_move_b<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);

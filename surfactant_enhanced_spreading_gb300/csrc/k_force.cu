@@ -1129,7 +1129,7 @@ __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d) {
 // field; nearer images come through the wrapped lists of L3, L4 and the
 // near field).  d2: the largest offset per axis of the H table.
 template <typename R>
-__global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const R *cf, int3 d2) {
+__global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const C2<R> *Hper, const R *cf, int3 d2) {
     griddep_wait();
     __shared__ R scf[LPH * LP];
     __shared__ R sre[16][LPH], sim[16][LPH];
@@ -1144,17 +1144,26 @@ __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const
     int h[LP];
     R cr[LP], ci[LP];
     m2l_terms<R>(o < LPH ? o : LPH - 1, scf, h, cr, ci);
-    const int wx = 2 * d2.x + 1, wy = 2 * d2.y + 1, nb = n[0] * n[1] * n[2];
-    const int nimg = r.per ? 9 : 1;
+    const int nb = n[0] * n[1] * n[2];
     R re = 0, im = 0;
-    for (int s = hw; s < nb * nimg; s += 16) {
-        const int img = s / nb, sb = s - img * nb;
-        const int ix = r.per ? img % 3 - 1 : 0, iy = r.per ? img / 3 - 1 : 0;
-        const int sx = sb % n[0] + ix * n[0], sy = (sb / n[0]) % n[1] + iy * n[1], sz = sb / (n[0] * n[1]);
-        const int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
-        if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
-        const int oi = (dx + d2.x) + wx * ((dy + d2.y) + wy * (dz + d2.z));
-        m2l_acc<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + sb) * LP, h, cr, ci, re, im);
+    if (r.per) {
+        // the image-summed factors of the replica: one pass over the box's sources
+        const int wx = 2 * n[0] - 1, wy = 2 * n[1] - 1;
+        const C2<R> *Hr = Hper + (size_t)r.h2off * NH;
+        for (int s = hw; s < nb; s += 16) {
+            const int sx = s % n[0], sy = (s / n[0]) % n[1], sz = s / (n[0] * n[1]);
+            const int oi = (sx - t[0] + n[0] - 1) + wx * ((sy - t[1] + n[1] - 1) + wy * (sz - t[2] + n[2] - 1));
+            m2l_acc<R>(Hr + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, h, cr, ci, re, im);
+        }
+    } else {
+        const int wx = 2 * d2.x + 1, wy = 2 * d2.y + 1;
+        for (int s = hw; s < nb; s += 16) {
+            const int sx = s % n[0], sy = (s / n[0]) % n[1], sz = s / (n[0] * n[1]);
+            const int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
+            if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
+            const int oi = (dx + d2.x) + wx * ((dy + d2.y) + wy * (dz + d2.z));
+            m2l_acc<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, h, cr, ci, re, im);
+        }
     }
     if (o < LPH) { sre[hw][o] = re; sim[hw][o] = im; }
     __syncthreads();
@@ -1174,14 +1183,14 @@ size_t m2c_smem() { return sizeof(R) * M2C_CH * LP * M2C_LD; }
 
 template <typename R, typename OP>
 void fma_build(const Dev &d, int ncell, int n3, int n2, int3 d2, const OP *m43, const OP *m32, const OP *l23,
-               const OP *l34, const C2<R> *h2, const R *cf, cudaStream_t st) {
+               const OP *l34, const C2<R> *h2, const C2<R> *hper, const R *cf, cudaStream_t st) {
     // one chain of dependent launches (programmatic: each waits for its predecessor first)
     launch_pdl(k_p2m<R>, dim3(ncell), dim3(64), 0, st, d);
     launch_pdl(k_m2m<R, OP>, dim3(n3), dim3(128), 0, st, d, d.O4, d.O3, m43, d.b3rep, 3);
     launch_pdl(k_m2m<R, OP>, dim3(n2), dim3(128), 0, st, d, d.O3, d.O2, m32, d.b2rep, 2);
     launch_pdl(k_m2l_pack<R>, dim3(((ncell + n3) * LP + 255) / 256), dim3(256), 0, st, d, ncell, n3);
     launch_pdl(k_m2l_cls<R>, dim3(d.m2c_nitems, d.m2c_groups), dim3(32 * M2C_W), m2c_smem<R>(), st, d);
-    launch_pdl(k_m2l_all<R>, dim3(n2), dim3(256), 0, st, d, h2, cf, d2);
+    launch_pdl(k_m2l_all<R>, dim3(n2), dim3(256), 0, st, d, h2, hper, cf, d2);
     launch_pdl(k_l2l<R, OP>, dim3((n3 + 3) / 4), dim3(128), 0, st, d, (const double2 *)d.L2, d.L3, l23,
                (const int *)d.b3rep, 3, (const R *)d.part3, d.m2c_groups, (float2 *)nullptr, n3);
     launch_pdl(k_l2l<R, OP>, dim3((ncell + 3) / 4), dim3(128), 0, st, d, (const double2 *)d.L3, d.L4, l34,
@@ -1192,10 +1201,10 @@ void fma_build(const Dev &d, int ncell, int n3, int n2, int3 d2, const OP *m43, 
 void launch_fma_build(const Dev &d, int ncell, int n3, int n2, int mixed, int3 d2, cudaStream_t st) {
     if (mixed)
         fma_build<float>(d, ncell, n3, n2, d2, d.op32_m2m43, d.op32_m2m32, d.op32_l2l23, d.op32_l2l34,
-                         (const C2<float> *)d.h32_m2l2, d.m2l_cf32, st);
+                         (const C2<float> *)d.h32_m2l2, (const C2<float> *)d.h32_per, d.m2l_cf32, st);
     else
         fma_build<double>(d, ncell, n3, n2, d2, d.op_m2m43, d.op_m2m32, d.op_l2l23, d.op_l2l34,
-                          (const C2<double> *)d.h_m2l2, d.m2l_cf, st);
+                          (const C2<double> *)d.h_m2l2, (const C2<double> *)d.h_per, d.m2l_cf, st);
 }
 
 // ------------------------------------------------------------------ per-site terms

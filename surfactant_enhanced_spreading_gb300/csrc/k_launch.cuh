@@ -32,10 +32,12 @@ void launch_eta(const Dev &d, int nrep, cudaStream_t st);
 // k_constraint.cu (mixed paths: FP64 or FP32 sweeps); false if the uploaded
 // bond graph is not the one the kernels are specialised for
 bool upload_tables_fast(const Tables &t, cudaStream_t st);
+// mat: waters as the 3 x 3 system of their constraints (matrix SHAKE /
+// RATTLE; the configuration preset's FP64 corrections)
 void launch_move_a32(const Dev &d, int nw, const int *smols, int ns, int nmol, int nsite, const ConstraintShape &sh,
-                     cudaStream_t st, double tol, int maxit, int fp32);
+                     cudaStream_t st, double tol, int maxit, int fp32, int mat);
 void launch_move_b32(const Dev &d, int nw, const int *smols, int ns, int nmol, int nsite, const ConstraintShape &sh,
-                     cudaStream_t st, double tol, int maxit, int fp32);
+                     cudaStream_t st, double tol, int maxit, int fp32, int mat);
 // reorders the halves' water lists by the sweeps of their last call (at list rebuilds)
 void launch_water_order(const Dev &d, const int *wmols, int nw, cudaStream_t st);
 int constraint_max_surf_warps();

@@ -8,7 +8,9 @@
 #include <cstdio>
 #include <cstring>
 #include <cstdlib>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -750,10 +752,10 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
             r.rsd[a] = r.nc[a] * RS;
             r.rhs[a] = r.rsd[a] / 2.0;
             r.irsd[a] = 1.0 / r.rsd[a];
-            // L2 offsets reach one box further along a periodic axis (images -1, 0, 1)
-            const int reach = (per && a < 2) ? 2 * r.nr[a] - 1 : r.nr[a] - 1;
+            // offsets of the shared L2 table (closed boxes; the periodic
+            // preset has per-replica image-summed tables instead)
             int &dd = a == 0 ? d2.x : (a == 1 ? d2.y : d2.z);
-            dd = std::max(dd, reach);
+            dd = std::max(dd, r.nr[a] - 1);
         }
         r.per = per;
         r.ssite = c->ssite;
@@ -1081,6 +1083,41 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
                     harm_m2l(dx * 4 * RS, dy * 4 * RS, dz * 4 * RS, &h[(size_t)oi * NHARM]);
                 }
         if ((e = put(h, d.h_m2l2, d.h32_m2l2))) return e;
+        // periodic preset: per replica, for each offset within the box, the
+        // H of its images not adjacent to the target summed (M2L is linear
+        // in H, so one pass over the box's sources takes every image)
+        std::vector<double2> hp(NHARM, make_double2(0.0, 0.0));
+        if (per) {
+            std::map<std::tuple<int, int, int>, std::vector<double2>> cache;
+            hp.clear();
+            for (int q = 0; q < R; q++) {
+                Rep &r = c->reps[q];
+                r.h2off = (int)(hp.size() / NHARM);
+                const int n0 = r.nr[0], n1 = r.nr[1], n2z = r.nr[2];
+                for (int dz = -(n2z - 1); dz <= n2z - 1; dz++)
+                    for (int dy = -(n1 - 1); dy <= n1 - 1; dy++)
+                        for (int dx = -(n0 - 1); dx <= n0 - 1; dx++) {
+                            double2 acc[NHARM];
+                            for (int k = 0; k < NHARM; k++) acc[k] = make_double2(0.0, 0.0);
+                            for (int iy = -1; iy <= 1; iy++)
+                                for (int ix = -1; ix <= 1; ix++) {
+                                    const int ux = dx + ix * n0, uy = dy + iy * n1;
+                                    if (abs(ux) <= 1 && abs(uy) <= 1 && abs(dz) <= 1) continue;
+                                    auto key = std::make_tuple(ux, uy, dz);
+                                    auto it = cache.find(key);
+                                    if (it == cache.end()) {
+                                        std::vector<double2> hv(NHARM);
+                                        harm_m2l(ux * 4 * RS, uy * 4 * RS, dz * 4 * RS, hv.data());
+                                        it = cache.emplace(key, std::move(hv)).first;
+                                    }
+                                    for (int k = 0; k < NHARM; k++) { acc[k].x += it->second[k].x; acc[k].y += it->second[k].y; }
+                                }
+                            hp.insert(hp.end(), acc, acc + NHARM);
+                        }
+            }
+        }
+        if ((e = dalloc(c, &d.h_per, hp.size())) || (e = dalloc(c, &d.h32_per, hp.size()))) return e;
+        if ((e = put(hp, d.h_per, d.h32_per))) return e;
         std::vector<float> cf32(LPH * LP);
         for (int i = 0; i < LPH * LP; i++) cf32[i] = (float)cf[i];
         CK(cudaMemcpyAsync(d.m2l_cf, cf.data(), cf.size() * sizeof(double), cudaMemcpyHostToDevice, c->st));

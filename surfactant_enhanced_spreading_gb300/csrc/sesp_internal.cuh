@@ -101,6 +101,7 @@ struct Rep {
     int igz;          // configuration preset: last cell layer the graphite acts on (-1: none)
     int ncon;         // constraints (degrees of freedom removed)
     float gymax;      // half-extent in y of a graphite column's carbons (bins)
+    int h2off;        // periodic preset: first record of this replica's image-summed L2 M2L factors
 };
 
 // constant topology and force-field tables (reference values, src/init_arrays.f90)
@@ -190,6 +191,11 @@ struct Dev {
     // offsets) and the offset-independent coefficients (15 x 25)
     double2 *h_m2l2;
     float2 *h32_m2l2;    // FP32 copy for the mixed path
+    // periodic preset: per replica, for every L2 offset (dx, dy, dz) within
+    // the box, the sum of H over the offset's non-adjacent periodic images
+    // (image shifts -1, 0, 1 in x and y), 45 per offset
+    double2 *h_per;
+    float2 *h32_per;
     double *m2l_cf;
     float *m2l_cf32;
     // L4 and L3 M2L in real form.  A multipole or local expansion is carried

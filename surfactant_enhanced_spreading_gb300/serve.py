@@ -109,9 +109,8 @@ def estimate_bytes(system: S.System) -> int:
     ncell = int(np.prod(nc))
     n3, n2 = ncell // 8, ncell // 64
     per = getattr(system, "preset", 0) == CP.PRESET_CONFIG
-    # the L2 far-field table: offsets reach one more box length along periodic axes
-    reach = [2 * int(nc[a] // 4) - 1 if (per and a < 2) else int(nc[a] // 4) - 1 for a in range(3)]
-    w2 = int(np.prod([2 * max(1, r) + 1 for r in reach])) ** (1.0 / 3.0)
+    d2 = max(1, int((nc // 4).max()) - 1)
+    w2 = 2 * d2 + 1
     per_site = 12 * 8 + 1 + 4 * 4 + 32 + 16 + 8 + 4 + 3 * 8 + 27 * 8 + 6 + 3 * 8 + 12 * 8
     per_mol = 5 * 4 + 2 * 8 + 4 + 4 + 2 * 4 + 2   # incl. the constraint halves' water lists and sweep counts
     cz = 25 * 16
@@ -129,6 +128,8 @@ def estimate_bytes(system: S.System) -> int:
     reach_cols = 12 if per else 8
     graphite = reach_cols * ncarb * 48 + (ncol + 1) * 4 + ncol * 8 * (33 * 4 + 8) + int(nc.sum()) * 8 + n * 4
     surf = system.sites_per_surf * system.n_surf * 4 + n * 4
+    if per:   # the image-summed L2 M2L factors of the replica (FP64 and FP32)
+        surf += int(np.prod(2 * (nc // 4) - 1)) * 45 * 24
     total = n * per_site + nmol * per_mol + cells + ops + graphite + surf + 4096
     return int(1.1 * total) + (1 << 20)
 

@@ -146,3 +146,40 @@ def test_periodic_shift_changes_nothing(c1):
     f0 = E.Engine(c1, E.PLAIN_FP64).force(True)
     f1 = E.Engine(s, E.PLAIN_FP64).force(True)
     assert rel(f1, f0) < 1e-10   # the shifted coordinates round differently
+
+
+def test_mixed_water_constraints_matrix_form(c1):
+    """The mixed path's matrix SHAKE / RATTLE of the waters against the plain
+    path's Gauss-Seidel sweeps from identical inputs: both stop inside the
+    1e-8 tolerance of the same constrained state, so positions agree to
+    well below 1e-7 sigma, and every water bond meets the tolerance."""
+    plain = E.Engine(c1, E.PLAIN_FP64)
+    mixed = E.Engine(c1, E.MIXED)
+    f = plain.force(True)
+    mixed.force(True)
+    plain.init_accel()
+    p0, v0, a0 = plain.state()
+    mixed.set_state(p0, v0, a0, 0.0)
+    for e in (plain, mixed):
+        e.move_a()
+    pp, vp, _ = plain.state()
+    pm, vm, _ = mixed.state()
+    assert np.abs(pm - pp).max() < 1e-7
+    assert np.abs(vm - vp).max() < 1e-7
+    w = pm[:3 * c1.n_water].reshape(-1, 3, 3) * 3.166
+    hh = 2 * np.sin(np.radians(109.47 / 2))
+    for (i, j), dd in (((0, 1), 1.0), ((1, 2), hh), ((2, 0), 1.0)):
+        d2 = ((w[:, i] - w[:, j]) ** 2).sum(1)
+        assert np.abs(d2 - dd * dd).max() <= 2.0001e-8 * dd * dd
+    # RATTLE: the mixed path's velocities meet RATTLE's own test, |R.V / dt| /
+    # ((1/m_i + 1/m_j) d^2) <= tol, for every water bond
+    mixed.force(True)
+    mixed.move_b()
+    pm2, vm2, _ = mixed.state()
+    m = np.array([1.0, 1.00794 / 15.9994, 1.00794 / 15.9994])
+    r = pm2[:3 * c1.n_water].reshape(-1, 3, 3)
+    v = vm2[:3 * c1.n_water].reshape(-1, 3, 3)
+    for (i, j), dd in (((0, 1), 1.0), ((1, 2), hh), ((2, 0), 1.0)):
+        g = np.einsum("ij,ij->i", r[:, i] - r[:, j], v[:, i] - v[:, j]) / 0.00127362 / ((1 / m[i] + 1 / m[j]) * dd * dd / 3.166 ** 2)
+        assert np.abs(g).max() <= 1.0001e-8
+    assert mixed.counters()[0] == 0
