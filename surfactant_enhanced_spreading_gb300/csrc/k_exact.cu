@@ -534,27 +534,34 @@ __global__ void k_isub_cfg(Dev d, int nbeads, const int *chain_mols) {
 
 // move_a of flexible chains: the Nose-Hoover scaled predictor of
 // src/move_surfactant_a.f90:36-60 with no constraint, and the kinetic sums
-// before and after (one thread per chain)
+// before and after.  16 lanes per chain, one bead each; the sums are added
+// by a fixed shuffle tree within the 16 lanes.
 __global__ void k_move_free_a(Dev d, const int *mols, int nm) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nm) return;
-    const int m = mols[t], g0 = d.mfirst[m];
-    const double escale = 1.0 - d.eta[d.mrep[m]] * DT / 2.0;
+    const int q = t >> 4, i = t & 15;
     double ke0 = 0.0, ke1 = 0.0;
-    for (int i = 0; i < NCH; i++) {
-        const int g = g0 + i;
+    if (q < nm && i < NCH) {
+        const int m = mols[q], g = d.mfirst[m] + i;
+        const double escale = 1.0 - d.eta[d.mrep[m]] * DT / 2.0;
         const double mi = d.tmass[d.ptype[g]];
         double vx = d.vx[g], vy = d.vy[g], vz = d.vz[g];
-        ke0 += mi * (vx * vx + vy * vy + vz * vz);
+        ke0 = mi * (vx * vx + vy * vy + vz * vz);
         d.x[g] = d.x[g] + vx * escale + d.ax[g];
         d.y[g] = d.y[g] + vy * escale + d.ay[g];
         d.z[g] = d.z[g] + vz * escale + d.az[g];
         vx = vx * escale + d.ax[g]; vy = vy * escale + d.ay[g]; vz = vz * escale + d.az[g];
         d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
-        ke1 += mi * (vx * vx + vy * vy + vz * vz);
+        ke1 = mi * (vx * vx + vy * vy + vz * vz);
     }
-    d.ke[2 * m] = ke0;
-    d.ke[2 * m + 1] = ke1;
+    for (int o = 8; o > 0; o >>= 1) {
+        ke0 += __shfl_xor_sync(0xffffffffu, ke0, o);
+        ke1 += __shfl_xor_sync(0xffffffffu, ke1, o);
+    }
+    if (q < nm && i == 0) {
+        const int m = mols[q];
+        d.ke[2 * m] = ke0;
+        d.ke[2 * m + 1] = ke1;
+    }
 }
 
 // move_b of flexible chains: acceleration from force and friction
@@ -591,7 +598,7 @@ void launch_move_a(const Dev &d, const int *wmols, int nw, const int *smols, int
     if (chains) {   // flexible chains: constraints on the waters only
         if (fast) launch_move_a32(d, nw, smols, 0, nmol, nsite, sh, st, tol, maxit, fast == 2, 1);
         else if (nw) k_move_a<3><<<(nw + 127) / 128, 128, 0, st>>>(d, wmols, nw, tol, maxit);
-        if (ns) k_move_free_a<<<(ns + 127) / 128, 128, 0, st>>>(d, smols, ns);
+        if (ns) k_move_free_a<<<(ns * 16 + 127) / 128, 128, 0, st>>>(d, smols, ns);
         return;
     }
     if (fast) {

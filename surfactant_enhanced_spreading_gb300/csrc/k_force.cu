@@ -424,35 +424,43 @@ struct Tgt64 {
     int m, trow;        // molecule, type * NTYPE
 };
 
+// 1/sqrt(x) of the special-function unit (the approximation rsqrtf uses)
+// without the handling of denormal inputs: pair distances are never
+// denormal, so the result is rsqrtf's and the fix-up instructions go
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // FP32 path, K target sites per lane: one partner against targets t[0..K),
 // Coulomb plus, for a partner with LJ, the LJ term of each target within rc
 // (run when some lane of the warp has one); pairk_coul32 for a water-H
-// partner (no LJ), whose exclusion is a select on the reciprocal distance
-// (it also discards the site itself, at r = 0).
+// partner (no LJ).  A partner of the target's own molecule (and the target
+// itself, at r = 0) is excluded by one select that zeroes the reciprocal
+// distance: its Coulomb and LJ terms are then exactly zero.
 template <int K>
 __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int key, const float2 *ljt, float rc2,
                                             float (&f)[K][3]) {
     const int mj = key >> 5, tj = key & 31;
     float dx[K], dy[K], dz[K], r2[K], ir2[K], ft[K];
-    bool same[K];
 #pragma unroll
     for (int j = 0; j < K; j++) {
         dx[j] = t[j].x - pj.x; dy[j] = t[j].y - pj.y; dz[j] = t[j].z - pj.z;
-        same[j] = mj == t[j].m;
-        r2[j] = same[j] ? 1.f : dx[j] * dx[j] + dy[j] * dy[j] + dz[j] * dz[j];
-        const float ira = rsqrtf(r2[j]);
+        r2[j] = dx[j] * dx[j] + dy[j] * dy[j] + dz[j] * dz[j];
+        const float ira = mj == t[j].m ? 0.f : rsqrt_ftz(r2[j]);
         ir2[j] = ira * ira;
-        ft[j] = (same[j] ? 0.f : t[j].q * pj.w) * ira * ir2[j];
+        ft[j] = (t[j].q * pj.w) * ira * ir2[j];
     }
     if (tj != 1) {   // water H carries no LJ
         bool n[K], any = false;
 #pragma unroll
-        for (int j = 0; j < K; j++) { n[j] = r2[j] <= rc2 && !same[j]; any = any || n[j]; }
+        for (int j = 0; j < K; j++) { n[j] = r2[j] <= rc2; any = any || n[j]; }
         if (__any_sync(0xffffffffu, any)) {
 #pragma unroll
             for (int j = 0; j < K; j++) {
                 const float2 v = ljt[t[j].trow + tj];
-                const float r6 = ir2[j] * ir2[j] * ir2[j];
+                const float r6 = ir2[j] * ir2[j] * ir2[j];   // zero for an excluded partner
                 ft[j] += (n[j] ? v.x : 0.f) * r6 * (v.y * r6 - 0.5f) * ir2[j];
             }
         }
@@ -466,7 +474,7 @@ __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int
     for (int j = 0; j < K; j++) {
         const float dx = t[j].x - pj.x, dy = t[j].y - pj.y, dz = t[j].z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        const float ira = mj == t[j].m ? 0.f : rsqrtf(r2);
+        const float ira = mj == t[j].m ? 0.f : rsqrt_ftz(r2);
         const float ft = (t[j].q * pj.w) * ira * (ira * ira);
         f[j][0] += dx * ft; f[j][1] += dy * ft; f[j][2] += dz * ft;
     }
