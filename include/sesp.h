@@ -230,8 +230,11 @@ int sesp_constraint_tuning(sesp_ctx *ctx, int out[4]);
  * scratch is one fixed array in the library (6.1 MiB on every GPU that loads
  * it); contexts above SESP_NOALLOC_MAX_SITES sites or SESP_NOALLOC_MAX_SURF
  * surfactants get SESP_EINVAL.  The first call on a device looks up the
- * array's device address, so make it before any stream capture.  Calls on one
- * device share the array and take turns under a lock.  No counterpart in the
+ * array's device address, so make it before any stream capture; the address is
+ * kept for the life of the process, so do not call it after a reset of the
+ * device's primary context (cudaDeviceReset).  A call first waits for the work
+ * already queued on its context; calls on one device then share the array and
+ * take turns under a lock.  No counterpart in the
  * reference, which computes no energies. */
 #define SESP_NOALLOC_MAX_SITES 131072
 #define SESP_NOALLOC_MAX_SURF 4096

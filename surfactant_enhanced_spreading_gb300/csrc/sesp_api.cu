@@ -1685,18 +1685,28 @@ int sesp_energies(sesp_ctx *c, double out[8]) {
     if (set_device(c)) return SESP_ECUDA;
     int N = c->nsite;
     double *es = nullptr, *ei = nullptr, *em = nullptr;
-    CK(cudaMalloc(&es, 3 * sizeof(double) * N));
-    CK(cudaMalloc(&ei, 3 * sizeof(double) * N));
-    CK(cudaMalloc(&em, 3 * sizeof(double) * (c->nsm + 1)));
-    cudaMemsetAsync(es, 0, 3 * sizeof(double) * N, c->st);
-    launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
-    launch_energies(c->d, c->ncell, N, c->smols, c->nsm, c->chains, es, ei, em, c->st);
+    // the scratch is freed on every path (a failed allocation frees the earlier ones)
+    struct Scratch {
+        double **p[3];
+        ~Scratch() { for (double **q : p) if (*q) cudaFree(*q); }
+    } guard = {{&es, &ei, &em}};
+    cudaError_t err = cudaMalloc(&es, 3 * sizeof(double) * N);
+    if (err == cudaSuccess) err = cudaMalloc(&ei, 3 * sizeof(double) * N);
+    if (err == cudaSuccess) err = cudaMalloc(&em, 3 * sizeof(double) * (c->nsm + 1));
+    if (err != cudaSuccess) return fail(SESP_ENOMEM, "energies: scratch allocation: %s", cudaGetErrorString(err));
     std::vector<double> hs(3 * (size_t)N), hi(3 * (size_t)N), hm(3 * (size_t)(c->nsm + 1));
-    cudaMemcpyAsync(hs.data(), es, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
-    cudaMemcpyAsync(hi.data(), ei, hi.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
-    cudaMemcpyAsync(hm.data(), em, 3 * sizeof(double) * c->nsm, cudaMemcpyDeviceToHost, c->st);
-    cudaError_t err = cudaStreamSynchronize(c->st);
-    cudaFree(es); cudaFree(ei); cudaFree(em);
+    err = cudaMemsetAsync(es, 0, 3 * sizeof(double) * N, c->st);
+    if (err == cudaSuccess) {
+        launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
+        launch_energies(c->d, c->ncell, N, c->smols, c->nsm, c->chains, es, ei, em, c->st);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(hs.data(), es, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(hi.data(), ei, hi.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    if (err == cudaSuccess) err = cudaMemcpyAsync(hm.data(), em, 3 * sizeof(double) * c->nsm, cudaMemcpyDeviceToHost, c->st);
+    // wait for the queued work before the guard frees the scratch it uses
+    const cudaError_t e2 = cudaStreamSynchronize(c->st);
+    if (err == cudaSuccess) err = e2;
     if (err != cudaSuccess) return fail(SESP_ECUDA, "energies: %s", cudaGetErrorString(err));
     for (int k = 0; k < 8; k++) out[k] = 0.0;
     for (int s = 0; s < N; s++) { out[0] += hs[3 * s]; out[1] += hs[3 * s + 1]; out[2] += hs[3 * s + 2]; }
@@ -1721,7 +1731,10 @@ int sesp_energies(sesp_ctx *c, double out[8]) {
 // process exits.  In host code its name is only a stand-in: its device
 // address is looked up with cudaGetSymbolAddress, once per device, by the
 // first call on that device, with that device current.  That first call
-// should therefore come before any stream capture.  All calls on one device
+// should therefore come before any stream capture, and the address is kept
+// for the life of the process: the function must not be used after
+// something in the process resets the device's primary context
+// (cudaDeviceReset), whose new context has the array elsewhere.  All calls on one device
 // share the array and it keeps the last call's contents: each call clears the
 // per-slot part (slots that no site occupies are summed as zeros), and calls
 // hold a per-device lock until their result has reached the host, because two
@@ -1772,6 +1785,9 @@ int sesp_energies_static(sesp_ctx *c, double out[8]) {
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES)
         return fail(SESP_EINVAL, "sesp_energies_static: device %d is beyond the %d it serves", dev, NOALLOC_MAX_DEVICES);
     if (set_device(c)) return SESP_ECUDA;
+    // the context's earlier work first, outside the lock: the lock then
+    // covers only this call's kernels and copy, not other runs' queues
+    CK(cudaStreamSynchronize(c->st));
     std::lock_guard<std::mutex> hold(g_noalloc_lock[dev]);
     if (!g_noalloc_scratch[dev]) {
         double *p = nullptr;
@@ -1785,13 +1801,18 @@ int sesp_energies_static(sesp_ctx *c, double out[8]) {
     double *ei = es + 3 * (size_t)SESP_NOALLOC_MAX_SITES;
     double *em = ei + 3 * (size_t)SESP_NOALLOC_MAX_SITES;
     double *tot = em + 3 * ((size_t)SESP_NOALLOC_MAX_SURF + 1);
-    CK(cudaMemsetAsync(es, 0, 3 * sizeof(double) * N, c->st));
-    launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
-    launch_energies(c->d, c->ncell, N, c->smols, c->nsm, c->chains, es, ei, em, c->st);
-    k_energy_totals<<<1, 32, 0, c->st>>>(es, ei, em, N, c->nsm, tot);
-    CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(out, tot, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
+    cudaError_t err = cudaMemsetAsync(es, 0, 3 * sizeof(double) * N, c->st);
+    if (err == cudaSuccess) {
+        launch_gather(c->d, c->nsite, c->ncell, 0, c->st);
+        launch_energies(c->d, c->ncell, N, c->smols, c->nsm, c->chains, es, ei, em, c->st);
+        k_energy_totals<<<1, 32, 0, c->st>>>(es, ei, em, N, c->nsm, tot);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpyAsync(out, tot, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->st);
+    // whatever failed, the lock is released only once the GPU is done with the array
+    const cudaError_t e2 = cudaStreamSynchronize(c->st);
+    if (err == cudaSuccess) err = e2;
+    if (err != cudaSuccess) return fail(SESP_ECUDA, "sesp_energies_static: %s", cudaGetErrorString(err));
     return 0;
 }
 

@@ -44,6 +44,8 @@ def test_static_matches_allocating_on_two_calls(precision):
     assert _close(first, ref), (first, ref)
     assert _close(second, ref), (second, ref)
     assert np.array_equal(first, second)
+    # both entry points add the same per-site energies in the same order
+    assert np.array_equal(first, ref)
 
     E.mybox_start(eng)
     eng.run(99101, 15)
@@ -54,6 +56,7 @@ def test_static_matches_allocating_on_two_calls(precision):
     assert not np.array_equal(ref2, ref)
     assert _close(third, ref2), (third, ref2)
     assert _close(fourth, ref2), (fourth, ref2)
+    assert np.array_equal(third, ref2)
 
 
 def test_static_rejects_contexts_beyond_its_scratch():
