@@ -1,6 +1,6 @@
 """Build recipe of the engine library ``libsesp.so`` (sm_103a only).
 
-Four translation units are compiled in parallel with nvcc and linked into a
+Five translation units are compiled in parallel with nvcc and linked into a
 shared library next to this file's package:
 
 * ``k_exact.cu`` with ``-fmad=false``: cell assignment and the FP64
@@ -9,7 +9,8 @@ shared library next to this file's package:
 * ``k_constraint.cu``: the mixed paths' constraint sweeps (FP64, or FP32);
 * ``k_force.cu``: pair, multipole and intramolecular kernels;
 * ``sesp_api.cu``: the C ABI (host code compiled without contraction so the
-  force-field tables and translation operators are reproducible).
+  force-field tables and translation operators are reproducible);
+* ``sesp_common.cpp``: the COMMON-block layer over that ABI (host code).
 """
 import concurrent.futures as cf
 import os
@@ -23,8 +24,10 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
           "--expt-relaxed-constexpr", "-diag-suppress", "1444"]
-UNITS = [("k_exact.cu", ["-fmad=false"]), ("k_constraint.cu", []), ("k_force.cu", []), ("sesp_api.cu", [])]
-HEADERS = ["sesp_internal.cuh", "k_launch.cuh", os.path.join("..", "..", "include", "sesp.h")]
+UNITS = [("k_exact.cu", ["-fmad=false"]), ("k_constraint.cu", []), ("k_force.cu", []), ("sesp_api.cu", []),
+         ("sesp_common.cpp", [])]
+HEADERS = ["sesp_internal.cuh", "k_launch.cuh", os.path.join("..", "..", "include", "sesp.h"),
+           os.path.join("..", "..", "include", "sesp_common.h")]
 
 
 def _nvcc():
@@ -49,7 +52,7 @@ def build(force=False, verbose=False, extra=()):
     objs = []
     for src, flags in UNITS:
         s = os.path.join(HERE, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + hdrs + [__file__]):
             jobs.append([nvcc, "-c", s, "-o", o] + ARCH + COMMON + list(flags) + list(extra))

@@ -81,6 +81,33 @@ __global__ void k_scatter(Dev d, int nsite) {
     d.srt_site[slot] = g;
 }
 
+// The cells around c (offsets -1..1 per axis, wrapped in x and y on the
+// periodic preset) that hold a site of site v's molecule, v itself included:
+// bit (dx + 1) + 3 (dy + 1) + 9 (dz + 1).
+__device__ int molecule_cells(const Dev &d, int c, int v) {
+    const Rep r = d.rep[d.crep[c]];
+    const int m = d.smol[v], g0 = d.mfirst[m], ns = d.mkind[m] == 0 ? 3 : r.ssite;
+    int ix, iy, iz;
+    cell_xyz(r, c, ix, iy, iz);
+    int mask = 0;
+    for (int k = 0; k < ns; k++) {
+        const int ck = d.sloc[g0 + k];
+        if (ck < 0) continue;
+        int jx, jy, jz;
+        cell_xyz(r, ck, jx, jy, jz);
+        int dx = jx - ix, dy = jy - iy;
+        const int dz = jz - iz;
+        if (r.per) {
+            if (2 * dx > r.nc[0]) dx -= r.nc[0];
+            else if (2 * dx < -r.nc[0]) dx += r.nc[0];
+            if (2 * dy > r.nc[1]) dy -= r.nc[1];
+            else if (2 * dy < -r.nc[1]) dy += r.nc[1];
+        }
+        if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) mask |= 1 << ((dx + 1) + 3 * (dy + 1) + 9 * (dz + 1));
+    }
+    return mask;
+}
+
 // order the sites of each cell by site index, so the slot order (and with it
 // every floating-point sum) is independent of the scatter's atomics
 // (order within a cell: sites with LJ first - every kind but water H - then
@@ -104,6 +131,7 @@ __global__ void k_sort_cells(Dev d) {
             d.sslot[v] = s0 + t;
             d.srt_meta[s0 + t] = make_int2(d.smol[v], (int)d.ptype[v]);
             d.srt_key[s0 + t] = d.smol[v] << 5 | (int)d.ptype[v];
+            d.srt_xmask[s0 + t] = molecule_cells(d, c, v);
         }
         if (threadIdx.x == 0) d.cnh[c] = n;   // the pair loop then tests every slot for LJ
         return;
@@ -124,6 +152,7 @@ __global__ void k_sort_cells(Dev d) {
         d.sslot[v] = s0 + rank;
         d.srt_meta[s0 + rank] = make_int2(d.smol[v], (int)d.ptype[v]);
         d.srt_key[s0 + rank] = d.smol[v] << 5 | (int)d.ptype[v];
+        d.srt_xmask[s0 + rank] = molecule_cells(d, c, v);
     }
 }
 
@@ -439,7 +468,7 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
 // partner (no LJ).  A partner of the target's own molecule (and the target
 // itself, at r = 0) is excluded by one select that zeroes the reciprocal
 // distance: its Coulomb and LJ terms are then exactly zero.
-template <int K>
+template <int K, bool EXCL>
 __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int key, const float2 *ljt, float rc2,
                                             float (&f)[K][3]) {
     const int mj = key >> 5, tj = key & 31;
@@ -448,7 +477,7 @@ __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int 
     for (int j = 0; j < K; j++) {
         dx[j] = t[j].x - pj.x; dy[j] = t[j].y - pj.y; dz[j] = t[j].z - pj.z;
         r2[j] = dx[j] * dx[j] + dy[j] * dy[j] + dz[j] * dz[j];
-        const float ira = mj == t[j].m ? 0.f : rsqrt_ftz(r2[j]);
+        const float ira = EXCL && mj == t[j].m ? 0.f : rsqrt_ftz(r2[j]);
         ir2[j] = ira * ira;
         ft[j] = (t[j].q * pj.w) * ira * ir2[j];
     }
@@ -468,16 +497,35 @@ __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int 
 #pragma unroll
     for (int j = 0; j < K; j++) { f[j][0] += dx[j] * ft[j]; f[j][1] += dy[j] * ft[j]; f[j][2] += dz[j] * ft[j]; }
 }
-template <int K>
+// (t[j].q already holds q_target xpi q_H: every water H carries the same charge)
+template <int K, bool EXCL>
 __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int mj, float (&f)[K][3]) {
 #pragma unroll
     for (int j = 0; j < K; j++) {
         const float dx = t[j].x - pj.x, dy = t[j].y - pj.y, dz = t[j].z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        const float ira = mj == t[j].m ? 0.f : rsqrt_ftz(r2);
-        const float ft = (t[j].q * pj.w) * ira * (ira * ira);
+        const float ira = EXCL && mj == t[j].m ? 0.f : rsqrt_ftz(r2);
+        const float ft = t[j].q * ira * (ira * ira);
         f[j][0] += dx * ft; f[j][1] += dy * ft; f[j][2] += dz * ft;
     }
+}
+
+// One partner cell's sites (slots t0..t1, LJ-carrying ones before th) on
+// the targets u, in the partner cell's frame.  EXCL: some target's molecule
+// has a site in this cell, so partners of the same molecule are skipped.
+template <int K, bool EXCL>
+__device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, const int *__restrict__ keys,
+                                            Tgt32 (&u)[K], int t0, int th, int t1, const float2 *ljt, float rc2,
+                                            float (&f)[K][3]) {
+#pragma unroll 2
+    for (int sl = t0; sl < th; sl++) pairk_acc32<K, EXCL>(u, pos32[sl], keys[sl], ljt, rc2, f);
+    if (th < t1) {
+        const float qh = pos32[th].w;
+#pragma unroll
+        for (int j = 0; j < K; j++) u[j].q *= qh;
+    }
+#pragma unroll 2
+    for (int sl = th; sl < t1; sl++) pairk_coul32<K, EXCL>(u, pos32[sl], EXCL ? keys[sl] >> 5 : 0, f);
 }
 
 // One FP32 work item with K target sites per lane (lane + 32 j of the chunk):
@@ -510,6 +558,14 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
             t[j] = {p.x, p.y, p.z, p.w * (float)XPI, kk >> 5, (kk & 31) * NTYPE};
         }
     }
+    // the row's partner cells holding a site of some target's molecule:
+    // bit jx - ix + 1 (from the targets' molecule-cell masks)
+    unsigned xm = 0;
+    const int rowsh = 3 * (dyc + 1) + 9 * (dzc + 1);
+#pragma unroll
+    for (int j = 0; j < K; j++)
+        if (act[j]) xm |= ((unsigned)d.srt_xmask[s0 + first + lane + 32 * j] >> rowsh) & 7u;
+    const unsigned excl = __reduce_or_sync(0xffffffffu, xm);
     const float rc2 = (float)(RC * RC);
     const float sy = (float)(-dyc * RS), sz = (float)(-dzc * RS);
     float f[K][3];
@@ -525,10 +581,8 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
         for (int j = 0; j < K; j++) { u[j] = t[j]; u[j].x += sx; u[j].y += sy; u[j].z += sz; }
         // partners with LJ first (the cell sort puts water H last)
         const int th = t0 + d.cnh[cn];
-#pragma unroll 2
-        for (int sl = t0; sl < th; sl++) pairk_acc32<K>(u, pos32[sl], keys[sl], ljt, rc2, f);
-#pragma unroll 2
-        for (int sl = th; sl < t1; sl++) pairk_coul32<K>(u, pos32[sl], keys[sl] >> 5, f);
+        if ((excl >> (jx - ix + 1)) & 1u) near_cell32<K, true>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
+        else near_cell32<K, false>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
     }
     float *part = (float *)d.near_part + (size_t)pr * 3 * nslot;   // FP32 row partials on the mixed path
 #pragma unroll

@@ -808,7 +808,8 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.b3rep, n3)) || (e = dalloc(c, &d.b2rep, n2)) || (e = dalloc(c, &d.cstart, C + 1)) ||
         (e = dalloc(c, &d.ccount, C)) || (e = dalloc(c, &d.cfill, C)) || (e = dalloc(c, &d.sloc, N)) ||
         (e = dalloc(c, &d.sslot, N)) || (e = dalloc(c, &d.srt_site, N)) || (e = dalloc(c, &d.srt_pos, N)) ||
-        (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.srt_key, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) ||
+        (e = dalloc(c, &d.srt_pos32, N)) || (e = dalloc(c, &d.srt_meta, N)) || (e = dalloc(c, &d.srt_key, N)) ||
+        (e = dalloc(c, &d.srt_xmask, N)) || (e = dalloc(c, &d.nf, 3 * (size_t)N)) ||
         (e = dalloc(c, &d.near_part, 27 * (size_t)N)) || (e = dalloc(c, &d.near_items, near_items_max(N, C))) ||
         (e = dalloc(c, &d.near_items_tmp, near_items_max(N, C))) || (e = dalloc(c, &d.near_cls, near_items_max(N, C))) ||
         (e = dalloc(c, &d.near_icount, C + 1)) || (e = dalloc(c, &d.near_ctl, 66)) ||

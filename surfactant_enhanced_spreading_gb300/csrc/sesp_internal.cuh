@@ -162,6 +162,9 @@ struct Dev {
     float4 *srt_pos32;   // x, y, z relative to the slot's own cell centre, q (mixed)
     int2 *srt_meta;      // molecule, type
     int *srt_key;        // molecule << 5 | type
+    int *srt_xmask;      // per slot: bit dx + 3 dy + 9 dz (each offset + 1) set when the cell at that
+                         // offset from the slot's own holds a site of the slot's molecule (itself
+                         // included), so the pair loop tests same-molecule partners there only
     double *nf;          // near + far force by slot [3 * nslot]
     double *near_part;   // per partner row partial near force [9][3 * nslot] (float on the mixed path)
     int2 *near_items;    // near-field work items (cell, row << 24 | chunk), most expensive first

@@ -52,6 +52,24 @@ def test_config_params_defaults():
     assert p.shake_tol == 1e-8 and p.shake_maxit == 100
 
 
+def test_library_exports_common_layer():
+    """include/sesp_common.h: the layout functions and the gfortran-named
+    subroutines of the step loop are exported by the same library."""
+    from surfactant_enhanced_spreading_gb300.csrc import build
+    lib = ctypes.CDLL(build.build())
+    src = open(os.path.join(ROOT, "include", "sesp_common.h")).read()
+    names = set(re.findall(r"^\s*(?:int|void|sesp_ctx\s*\*|const\s+sesp_cmn_map\s*\*)\s*(\w+)\s*\(", src, flags=re.M))
+    assert {"sesp_cmn_attach", "evalforces_", "move_w2_a_", "move_surfactant_b_"} <= names
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    fmod = open(os.path.join(ROOT, "include", "sesp_common_mod.f90")).read().lower()
+    for n in names:
+        if n.startswith("sesp_cmn_") and not n.endswith("_") and n not in ("sesp_cmn_map_from_domains", "sesp_cmn_map_destroy",
+                                                     "sesp_cmn_assign", "sesp_cmn_scatter", "sesp_cmn_gather",
+                                                     "sesp_cmn_slot", "sesp_cmn_current_map"):
+            assert f'name="{n}"' in fmod, n
+
+
 def test_fortran_interface_module_lists_every_entry_point():
     src = open(os.path.join(ROOT, "include", "sesp_mod.f90")).read().lower()
     for n in _declared():
