@@ -162,7 +162,7 @@ def run_batched(args, local, E):
     return res
 
 
-def run_served(args, local):
+def run_served(args, local, peak_rate=None):
     """Poisson requests in the configuration preset served with continuous
     batching (mixed precision), and the same requests one at a time on the
     plain FP64 path.  The plain one-at-a-time run is timed on a bounded
@@ -181,6 +181,28 @@ def run_served(args, local):
     results = srv.run(reqs)
     wall = time.perf_counter() - t0
     out = serve.summarize(results)
+    # the same requests as the replicas of one batched context (formed again
+    # at chunk boundaries whenever a run joins or leaves)
+    slots = serve.SlotServer(64 << 30, precision=E.MIXED, chunk=100, device=local, keep_state=False)
+    t1 = time.perf_counter()
+    sres = slots.run(reqs)
+    swall = time.perf_counter() - t1
+    out["slots_of_one_context"] = serve.summarize(sres) | {
+        "wall_s": swall, "contexts_formed": slots.reforms, "forming_s": slots.reform_s,
+        "how": "running requests as the replicas of one batched context; at 100-step chunk boundaries (after a "
+               "rebuild step) finished runs leave, arrivals join and the context is formed again from the runs' "
+               "states (bit-identical to each run alone)"}
+    if peak_rate:
+        # the arrival-limited bound: no schedule ends before a_k + (work
+        # arriving at or after a_k) / (the batched rate), for every arrival a_k
+        arr = np.array(sorted(r.arrival for r in reqs))
+        work = np.array([r.system.n_sites * r.steps for r in sorted(reqs, key=lambda r: (r.arrival, r.rid))], float)
+        end = float(np.max(arr + np.cumsum(work[::-1])[::-1] / peak_rate))
+        span = end - float(arr[0])
+        out["arrival_limited"] = {
+            "span_s": span, "atom_steps_per_s": float(work.sum()) / span, "at_rate": peak_rate,
+            "how": "shortest span any schedule can reach if every atom-step runs at the batched leg's mixed rate: "
+                   "max over arrivals a_k of a_k + (atom-steps arriving at or after a_k) / rate"}
     # one at a time, plain FP64: per request its rate over one 100-step chunk
     per_step = {}
     for req in reqs:
@@ -398,15 +420,37 @@ def run_ours(args, ws, rank, local):
     plain_value = n_sites * args.plain_steps / (p_ms.sum() / 1e3)
     del plain
 
+    # --- SESP_MIXED_COMP (compensated FP32 sums in the pair field): its cost
+    # in step and pair-field time, and its force error
+    ceng = E.Engine(s, E.MIXED_COMP, device=local)
+    fcomp = ceng.force(True)
+    ceng.init_accel()
+    ceng.run(99101, 5)
+    ceng.autotune()
+    ceng.run(99106, 1)
+    c_ms = ceng.run_timed(99107, 20, flush_l2=True)
+    ceng.enable_timing(True)
+    ceng.kernel_times(reset=True)
+    ceng.run(99127, 20)
+    ckt = ceng.kernel_times(reset=True)
+    ceng.enable_timing(False)
+    compensated = {"value": n_sites * 20 / (c_ms.sum() / 1e3), "unit": "atom-steps/s", "steps": 20,
+                   "ms_per_step": float(c_ms.mean()), "near_ms_per_launch": ckt[0],
+                   "force_rms_rel_error_vs_plain": float(np.linalg.norm(fcomp - f64) / np.linalg.norm(f64)),
+                   "how": "SESP_MIXED_COMP: Kahan sums per target site in the pair field and over its 9 row partials"}
+    del ceng
+
     # --- batched replicas and the served stream (single-GPU runs only)
     batched = run_batched(args, local, E) if (ws == 1 and not args.no_batched) else None
-    served = run_served(args, local) if (ws == 1 and not args.no_served) else None
+    served = (run_served(args, local, batched["mixed"]["value"] if batched else None)
+              if (ws == 1 and not args.no_served) else None)
 
     # --- CPU baseline and error reference: the FP64 oracle on the same workload
     cpu, ferr_oracle = None, None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         cpu, fo = cpu_baseline(s, O)
         ferr_oracle = {"mixed": float(np.linalg.norm(f32 - fo) / np.linalg.norm(fo)),
+                       "mixed_compensated": float(np.linalg.norm(fcomp - fo) / np.linalg.norm(fo)),
                        "plain_fp64": float(np.linalg.norm(f64 - fo) / np.linalg.norm(fo))}
 
     T = eng.temperature()
@@ -433,6 +477,7 @@ def run_ours(args, ws, rank, local):
         "mixed_vs_plain_speedup": value / ws / plain_value,
         "mixed_fp32_constraints": fp32c,
         "mixed_force_rms_rel_error": ferr,
+        "mixed_compensated": compensated,
         "force_rms_rel_error_vs_oracle": ferr_oracle,
         "batched": batched,
         "served": served,

@@ -53,6 +53,9 @@ extern "C" {
 #define SESP_MIXED_FP32C 2 /* SESP_MIXED with the constraint iterations in
                               FP32 (FP64 state and predictors, FP64 decisions
                               near the tolerance threshold)                   */
+#define SESP_MIXED_COMP 3  /* SESP_MIXED with compensated (Kahan) FP32 sums of
+                              the pair terms per site, in the pair field and
+                              over its nine row partials                      */
 
 /* force terms (bit mask for sesp_force_terms) */
 #define SESP_T_NEAR 1        /* short-range LJ + Coulomb, src/eval[wS]*.f90   */
@@ -128,7 +131,8 @@ int sesp_upload_state(sesp_ctx *ctx, int n_water, int n_surf, const double *pos,
                       int n_carbon, const double *carbons);
 /* any of pos / vel / acc may be NULL */
 int sesp_download_state(sesp_ctx *ctx, double *pos, double *vel, double *acc);
-/* velocities and accelerations in, e.g. to resume a saved state */
+/* velocities and accelerations in, e.g. to resume a saved state; eta is
+ * given to every replica (sesp_set_eta_batch sets them one by one) */
 int sesp_set_state(sesp_ctx *ctx, const double *pos, const double *vel, const double *acc, double eta);
 
 /* several independent systems ("replicas") in one context, laid out back to
@@ -143,6 +147,12 @@ int sesp_upload_batch(sesp_ctx *ctx, int n_rep, const int *n_water, const int *n
 int sesp_replica_count(sesp_ctx *ctx);
 /* the thermostat variable of every replica */
 int sesp_get_eta_batch(sesp_ctx *ctx, double *eta);
+/* set it per replica (sesp_replica_count values), e.g. when a run moves
+ * into another batched context at a rebuild boundary */
+int sesp_set_eta_batch(sesp_ctx *ctx, const double *eta);
+/* SHAKE / RATTLE non-convergences since upload, per replica (the split of
+ * sesp_counters' [0]) */
+int sesp_failures_batch(sesp_ctx *ctx, int64_t *out);
 
 /* the force section.  rebuild = 1 replaces src/mybox.f90:142-152 (molecule
  * re-keying), :163-175 (list builders, multipoles and translations) and

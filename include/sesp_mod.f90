@@ -8,7 +8,7 @@ module sesp_mod
   use iso_c_binding
   implicit none
 
-  integer(c_int), parameter :: SESP_PLAIN_FP64 = 0, SESP_MIXED = 1, SESP_MIXED_FP32C = 2
+  integer(c_int), parameter :: SESP_PLAIN_FP64 = 0, SESP_MIXED = 1, SESP_MIXED_FP32C = 2, SESP_MIXED_COMP = 3
   integer(c_int), parameter :: SESP_T_ALL = 1023
   integer(c_int), parameter :: SESP_PRESET_REFERENCE = 0, SESP_PRESET_CONFIG = 1
 
@@ -228,6 +228,16 @@ module sesp_mod
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: eta(*)
+    end function
+    integer(c_int) function sesp_set_eta_batch(ctx, eta) bind(C, name="sesp_set_eta_batch")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: ctx
+      real(c_double), intent(in) :: eta(*)
+    end function
+    integer(c_int) function sesp_failures_batch(ctx, fails) bind(C, name="sesp_failures_batch")
+      import :: c_int, c_ptr, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int64_t), intent(out) :: fails(*)
     end function
     integer(c_int) function sesp_query(ctx) bind(C, name="sesp_query")
       import :: c_int, c_ptr

@@ -462,15 +462,54 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
     return y;
 }
 
+// Per-target force sums of an FP32 work item.  COMP: compensated (Kahan)
+// summation, each term's rounding error carried in a second register and
+// folded back when the sum is read.
+template <int K, bool COMP>
+struct Acc32 {
+    float f[K][3];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int j = 0; j < K; j++) f[j][0] = f[j][1] = f[j][2] = 0.f;
+    }
+    __device__ __forceinline__ void add(int j, float dx, float dy, float dz, float ft) {
+        f[j][0] += dx * ft; f[j][1] += dy * ft; f[j][2] += dz * ft;
+    }
+    __device__ __forceinline__ float get(int j, int a) const { return f[j][a]; }
+};
+template <int K>
+struct Acc32<K, true> {
+    float f[K][3], e[K][3];
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int j = 0; j < K; j++)
+#pragma unroll
+            for (int a = 0; a < 3; a++) f[j][a] = e[j][a] = 0.f;
+    }
+    __device__ __forceinline__ void add1(float &s, float &c, float v) {
+        const float y = __fsub_rn(v, c);
+        const float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ void add(int j, float dx, float dy, float dz, float ft) {
+        add1(f[j][0], e[j][0], __fmul_rn(dx, ft));
+        add1(f[j][1], e[j][1], __fmul_rn(dy, ft));
+        add1(f[j][2], e[j][2], __fmul_rn(dz, ft));
+    }
+    __device__ __forceinline__ float get(int j, int a) const { return __fsub_rn(f[j][a], e[j][a]); }
+};
+
 // FP32 path, K target sites per lane: one partner against targets t[0..K),
 // Coulomb plus, for a partner with LJ, the LJ term of each target within rc
 // (run when some lane of the warp has one); pairk_coul32 for a water-H
 // partner (no LJ).  A partner of the target's own molecule (and the target
 // itself, at r = 0) is excluded by one select that zeroes the reciprocal
-// distance: its Coulomb and LJ terms are then exactly zero.
-template <int K, bool EXCL>
+// distance: its Coulomb and LJ terms are then exactly zero (EXCL: only
+// in partner cells that hold a site of some target's molecule).
+template <int K, bool EXCL, bool COMP>
 __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int key, const float2 *ljt, float rc2,
-                                            float (&f)[K][3]) {
+                                            Acc32<K, COMP> &f) {
     const int mj = key >> 5, tj = key & 31;
     float dx[K], dy[K], dz[K], r2[K], ir2[K], ft[K];
 #pragma unroll
@@ -495,42 +534,42 @@ __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int 
         }
     }
 #pragma unroll
-    for (int j = 0; j < K; j++) { f[j][0] += dx[j] * ft[j]; f[j][1] += dy[j] * ft[j]; f[j][2] += dz[j] * ft[j]; }
+    for (int j = 0; j < K; j++) f.add(j, dx[j], dy[j], dz[j], ft[j]);
 }
 // (t[j].q already holds q_target xpi q_H: every water H carries the same charge)
-template <int K, bool EXCL>
-__device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int mj, float (&f)[K][3]) {
+template <int K, bool EXCL, bool COMP>
+__device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int mj, Acc32<K, COMP> &f) {
 #pragma unroll
     for (int j = 0; j < K; j++) {
         const float dx = t[j].x - pj.x, dy = t[j].y - pj.y, dz = t[j].z - pj.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
         const float ira = EXCL && mj == t[j].m ? 0.f : rsqrt_ftz(r2);
         const float ft = t[j].q * ira * (ira * ira);
-        f[j][0] += dx * ft; f[j][1] += dy * ft; f[j][2] += dz * ft;
+        f.add(j, dx, dy, dz, ft);
     }
 }
 
 // One partner cell's sites (slots t0..t1, LJ-carrying ones before th) on
 // the targets u, in the partner cell's frame.  EXCL: some target's molecule
 // has a site in this cell, so partners of the same molecule are skipped.
-template <int K, bool EXCL>
+template <int K, bool EXCL, bool COMP>
 __device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, const int *__restrict__ keys,
                                             Tgt32 (&u)[K], int t0, int th, int t1, const float2 *ljt, float rc2,
-                                            float (&f)[K][3]) {
+                                            Acc32<K, COMP> &f) {
 #pragma unroll 2
-    for (int sl = t0; sl < th; sl++) pairk_acc32<K, EXCL>(u, pos32[sl], keys[sl], ljt, rc2, f);
+    for (int sl = t0; sl < th; sl++) pairk_acc32<K, EXCL, COMP>(u, pos32[sl], keys[sl], ljt, rc2, f);
     if (th < t1) {
         const float qh = pos32[th].w;
 #pragma unroll
         for (int j = 0; j < K; j++) u[j].q *= qh;
     }
 #pragma unroll 2
-    for (int sl = th; sl < t1; sl++) pairk_coul32<K, EXCL>(u, pos32[sl], EXCL ? keys[sl] >> 5 : 0, f);
+    for (int sl = th; sl < t1; sl++) pairk_coul32<K, EXCL, COMP>(u, pos32[sl], EXCL ? keys[sl] >> 5 : 0, f);
 }
 
 // One FP32 work item with K target sites per lane (lane + 32 j of the chunk):
 // the force of partner row pr on them, written to that row's partial.
-template <int K, bool PER>
+template <int K, bool PER, bool COMP>
 __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int nslot, int c, int pr, int first,
                                             int ni, int lane) {
     const float4 *__restrict__ pos32 = d.srt_pos32;
@@ -568,9 +607,8 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
     const unsigned excl = __reduce_or_sync(0xffffffffu, xm);
     const float rc2 = (float)(RC * RC);
     const float sy = (float)(-dyc * RS), sz = (float)(-dzc * RS);
-    float f[K][3];
-#pragma unroll
-    for (int j = 0; j < K; j++) f[j][0] = f[j][1] = f[j][2] = 0.f;
+    Acc32<K, COMP> f;
+    f.zero();
     for (int jx = jx0; jx <= jx1; jx++) {
         // positions are cell-relative: the shift is the unwrapped offset
         const int cn = cell_index(r, PER ? wrap1(jx, r.nc[0]) : jx, wy, jz);
@@ -581,15 +619,15 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
         for (int j = 0; j < K; j++) { u[j] = t[j]; u[j].x += sx; u[j].y += sy; u[j].z += sz; }
         // partners with LJ first (the cell sort puts water H last)
         const int th = t0 + d.cnh[cn];
-        if ((excl >> (jx - ix + 1)) & 1u) near_cell32<K, true>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
-        else near_cell32<K, false>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
+        if ((excl >> (jx - ix + 1)) & 1u) near_cell32<K, true, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
+        else near_cell32<K, false, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
     }
     float *part = (float *)d.near_part + (size_t)pr * 3 * nslot;   // FP32 row partials on the mixed path
 #pragma unroll
     for (int j = 0; j < K; j++)
         if (act[j]) {
             const size_t o = 3 * (size_t)(s0 + first + lane + 32 * j);
-            part[o] = f[j][0]; part[o + 1] = f[j][1]; part[o + 2] = f[j][2];
+            part[o] = f.get(j, 0); part[o + 1] = f.get(j, 1); part[o + 2] = f.get(j, 2);
         }
 }
 
@@ -642,7 +680,8 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 // MIXED: FP32 positions relative to the cell centres, FP32 pair terms summed
 // in FP32 over one row (at most 3 cells).
 // PER: the periodic preset's instantiation (rows wrap around x and y)
-template <bool MIXED, int KMAX, bool PER>
+// COMP: compensated (Kahan) FP32 sums per target (SESP_MIXED_COMP)
+template <bool MIXED, int KMAX, bool PER, bool COMP = false>
 __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int tile) {
     griddep_wait();
     __shared__ float2 s_lj32[MIXED ? NTYPE * NTYPE : 1];
@@ -680,10 +719,10 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
         if constexpr (MIXED) {
             // K = targets per lane: ceil(targets of the chunk / 32), at most KMAX
             const int nt = min(tile, ni - chunk * tile), kk = (nt + 31) >> 5;
-            if (kk <= 1) near_item32<1, PER>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else if (kk == 2 || KMAX == 2) near_item32<2, PER>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else if (kk == 3) near_item32<(KMAX > 2 ? 3 : 2), PER>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else near_item32<KMAX, PER>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            if (kk <= 1) near_item32<1, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else if (kk == 2 || KMAX == 2) near_item32<2, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else if (kk == 3) near_item32<(KMAX > 2 ? 3 : 2), PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            else near_item32<KMAX, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
         } else {
             Tgt64 ta = {0.0, 0.0, 0.0, 0.0, -1, 0}, tb = ta;
             if (a0) {
@@ -734,7 +773,7 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
 
 // Sum of the 9 row partials (fixed order) plus the local-expansion force of
 // src/evalLjk4.f90:31-282 for every slot; writes nf.
-template <bool MIXED>
+template <bool MIXED, bool COMP = false>
 __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     griddep_wait();
     typedef typename std::conditional<MIXED, float, double>::type R;
@@ -747,15 +786,28 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     cell_xyz(r, c, ix, iy, iz);
     // the 9 row partials in row order: FP32 rows summed in FP32 on the mixed
     // path (one conversion to FP64 per component), FP64 on the plain path
+    // (COMP: compensated FP32 sums of the rows, as in the pair field)
     R fx = 0, fy = 0, fz = 0;
     if (terms & SESP_T_NEAR) {
         const int mask = near_row_mask(r, iy, iz);
         const R *part = (const R *)d.near_part;
+        R ex = 0, ey = 0, ez = 0;
         for (int pr = 0; pr < 9; pr++) {
             if (!(mask >> pr & 1)) continue;
             const R *p = part + (size_t)pr * 3 * nslot + 3 * (size_t)s;
-            fx += p[0]; fy += p[1]; fz += p[2];
+            if constexpr (COMP) {
+                R v[3] = {p[0], p[1], p[2]}, *sm[3] = {&fx, &fy, &fz}, *em[3] = {&ex, &ey, &ez};
+                for (int a = 0; a < 3; a++) {
+                    const float y = __fsub_rn(v[a], *em[a]);
+                    const float t = __fadd_rn(*sm[a], y);
+                    *em[a] = __fsub_rn(__fsub_rn(t, *sm[a]), y);
+                    *sm[a] = t;
+                }
+            } else {
+                fx += p[0]; fy += p[1]; fz += p[2];
+            }
         }
+        if constexpr (COMP) { fx = __fsub_rn(fx, ex); fy = __fsub_rn(fy, ey); fz = __fsub_rn(fz, ez); }
     }
     if (terms & SESP_T_FAR) {
         R Lre[LP], Lim[LP], x, y, z, q;
@@ -778,10 +830,13 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
     d.nf[3 * (size_t)s] = (double)fx; d.nf[3 * (size_t)s + 1] = (double)fy; d.nf[3 * (size_t)s + 2] = (double)fz;
 }
 
+// mixed: 0 plain FP64, 1 FP32, 2 FP32 with compensated sums
 template <bool PER>
 int near_max_ctas_t(int mixed, int tile) {
     int nb = 0;
-    if (mixed && tile > 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 4, PER>, NEAR_THREADS, 0);
+    if (mixed == 2 && tile > 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 4, PER, true>, NEAR_THREADS, 0);
+    else if (mixed == 2) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 2, PER, true>, NEAR_THREADS, 0);
+    else if (mixed && tile > 64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 4, PER>, NEAR_THREADS, 0);
     else if (mixed) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<true, 2, PER>, NEAR_THREADS, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_near<false, 2, PER>, NEAR_THREADS, 0);
     return nb > 0 ? nb : 1;
@@ -795,7 +850,9 @@ int near_max_ctas_per_sm(int mixed, int tile, int per) {
 template <bool PER>
 void launch_near_t(const Dev &d, int nslot, int mixed, const NearShape &shape, cudaStream_t st) {
     const dim3 g(shape.grid), b(NEAR_THREADS);
-    if (mixed && shape.tile > 64) launch_pdl(k_near<true, 4, PER>, g, b, 0, st, d, nslot, shape.tile);
+    if (mixed == 2 && shape.tile > 64) launch_pdl(k_near<true, 4, PER, true>, g, b, 0, st, d, nslot, shape.tile);
+    else if (mixed == 2) launch_pdl(k_near<true, 2, PER, true>, g, b, 0, st, d, nslot, shape.tile);
+    else if (mixed && shape.tile > 64) launch_pdl(k_near<true, 4, PER>, g, b, 0, st, d, nslot, shape.tile);
     else if (mixed) launch_pdl(k_near<true, 2, PER>, g, b, 0, st, d, nslot, shape.tile);
     else launch_pdl(k_near<false, 2, PER>, g, b, 0, st, d, nslot, shape.tile);
 }
@@ -808,7 +865,8 @@ void launch_near(const Dev &d, int ncell, int nslot, int mixed, int terms, const
         else launch_near_t<false>(d, nslot, mixed, shape, st);
     }
     const dim3 g((nslot + 127) / 128 > 0 ? (nslot + 127) / 128 : 1), b(128);
-    if (mixed) launch_pdl(k_near_finish<true>, g, b, 0, st, d, nslot, ncell, terms);
+    if (mixed == 2) launch_pdl(k_near_finish<true, true>, g, b, 0, st, d, nslot, ncell, terms);
+    else if (mixed) launch_pdl(k_near_finish<true>, g, b, 0, st, d, nslot, ncell, terms);
     else launch_pdl(k_near_finish<false>, g, b, 0, st, d, nslot, ncell, terms);
 }
 

@@ -482,6 +482,11 @@ void axis_centres(const Rep &r, int a, std::vector<double> &out) {
     }
 }
 
+// pair-field arithmetic: 0 FP64, 1 FP32, 2 FP32 with compensated sums
+int near_mode(const sesp_ctx *c) {
+    return c->p.precision == SESP_PLAIN_FP64 ? 0 : (c->p.precision == SESP_MIXED_COMP ? 2 : 1);
+}
+
 int check_ctx(sesp_ctx *c, bool need_state) {
     if (!c) return fail(SESP_EINVAL, "null context");
     if (need_state && !c->uploaded) return fail(SESP_ESTATE, "no state uploaded");
@@ -562,7 +567,7 @@ void seq_force(sesp_ctx *c, int rebuild, int terms) {
         tstop(c, 6);
     }
     tstart(c, 0);
-    launch_near(d, c->ncell, c->nsite, mixed, terms, c->near, c->st, false, c->chains);
+    launch_near(d, c->ncell, c->nsite, near_mode(c), terms, c->near, c->st, false, c->chains);
     family(c, "near field");
     tstop(c, 0);
     tstart(c, 4);
@@ -656,7 +661,8 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
     if (!p || !out) return fail(SESP_EINVAL, "null argument");
     for (int a = 0; a < 3; a++)
         if (p->n_cells[a] <= 0 || p->n_cells[a] % 4) return fail(SESP_EINVAL, "n_cells must be positive multiples of 4");
-    if (p->precision != SESP_PLAIN_FP64 && p->precision != SESP_MIXED && p->precision != SESP_MIXED_FP32C)
+    if (p->precision != SESP_PLAIN_FP64 && p->precision != SESP_MIXED && p->precision != SESP_MIXED_FP32C &&
+        p->precision != SESP_MIXED_COMP)
         return fail(SESP_EINVAL, "unknown precision");
     if (p->rebuild_interval <= 0) return fail(SESP_EINVAL, "rebuild_interval must be positive");
     if (p->preset != SESP_PRESET_REFERENCE && p->preset != SESP_PRESET_CONFIG) return fail(SESP_EINVAL, "unknown preset %d", p->preset);
@@ -687,7 +693,7 @@ int sesp_create(const sesp_params *p, sesp_ctx **out) {
         cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, dev);
         const int mixed = c->p.precision != SESP_PLAIN_FP64;
         c->near.tile = 64;   // 128 (mixed paths) only where the autotuner measures it faster
-        c->near.grid = c->n_sm * near_max_ctas_per_sm(mixed, c->near.tile, c->chains);
+        c->near.grid = c->n_sm * near_max_ctas_per_sm(near_mode(c), c->near.tile, c->chains);
         c->cshape.grid = c->n_sm;
     }
     c->sync_check = getenv("SESP_SYNC_CHECK") != nullptr;
@@ -1241,6 +1247,16 @@ int sesp_get_eta_batch(sesp_ctx *c, double *eta) {
     return 0;
 }
 
+int sesp_set_eta_batch(sesp_ctx *c, const double *eta) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!eta) return fail(SESP_EINVAL, "null input");
+    for (int q = 0; q < c->nrep; q++)
+        if (!std::isfinite(eta[q])) return fail(SESP_EINVAL, "eta of a replica is not finite");
+    CK(cudaMemcpyAsync(c->d.eta, eta, c->nrep * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return 0;
+}
+
 // (3, n) site-major host arrays <-> the device's x / y / z arrays: one
 // contiguous copy per array through a device staging buffer, transposed by
 // a kernel (array k of the staging buffer at k * 3n: positions, velocities,
@@ -1290,7 +1306,8 @@ int sesp_set_state(sesp_ctx *c, const double *pos, const double *vel, const doub
         k_state_io<<<(N + 255) / 256, 256, 0, c->st>>>(c->d, c->d.stage, N, mask, 1);
         CK(cudaGetLastError());
     }
-    CK(cudaMemcpyAsync(c->d.eta, &eta, sizeof(double), cudaMemcpyHostToDevice, c->st));
+    const std::vector<double> etas(c->nrep, eta);   // every replica
+    CK(cudaMemcpyAsync(c->d.eta, etas.data(), c->nrep * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
     return 0;
 }
@@ -1430,8 +1447,8 @@ int sesp_set_tuning(sesp_ctx *c, int tile, int ctas_per_sm) {
     const int mixed = c->p.precision != SESP_PLAIN_FP64;
     if (tile != 32 && tile != 64 && !(mixed && tile == 128))
         return fail(SESP_EINVAL, "tile must be 32 or 64 (or 128 on the mixed paths)");
-    if (ctas_per_sm < 1 || ctas_per_sm > near_max_ctas_per_sm(mixed, tile, c->chains))
-        return fail(SESP_EINVAL, "ctas_per_sm must be 1..%d", near_max_ctas_per_sm(mixed, tile, c->chains));
+    if (ctas_per_sm < 1 || ctas_per_sm > near_max_ctas_per_sm(near_mode(c), tile, c->chains))
+        return fail(SESP_EINVAL, "ctas_per_sm must be 1..%d", near_max_ctas_per_sm(near_mode(c), tile, c->chains));
     if (set_device(c)) return SESP_ECUDA;
     const bool retile = tile != c->near.tile;
     c->near = {tile, c->n_sm * ctas_per_sm};
@@ -1447,7 +1464,7 @@ int sesp_tuning(sesp_ctx *c, int out[3]) {
     if (!out) return fail(SESP_EINVAL, "null output");
     out[0] = c->near.tile;
     out[1] = c->n_sm ? c->near.grid / c->n_sm : 0;
-    out[2] = near_max_ctas_per_sm(c->p.precision != SESP_PLAIN_FP64, c->near.tile, c->chains);
+    out[2] = near_max_ctas_per_sm(near_mode(c), c->near.tile, c->chains);
     return 0;
 }
 
@@ -1551,18 +1568,18 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     NearShape pick = c->near;
     for (int tile : {128, 64, 32}) {
         if (tile == 128 && !mixed) continue;
-        const int mx = near_max_ctas_per_sm(mixed, tile, c->chains);
+        const int mx = near_max_ctas_per_sm(near_mode(c), tile, c->chains);
         const int cands[4] = {mx, (3 * mx) / 4, mx / 2, mx / 4};
         launch_near_items(c->d, c->ncell, (int)near_items_max(c->nsite, c->ncell), tile, c->st);
         for (int k = 0; k < 4; k++) {
             const int cps = cands[k];
             if (cps < 1 || (k > 0 && cps == cands[k - 1])) continue;
             const NearShape sh = {tile, c->n_sm * cps};
-            launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st, true, c->chains);   // warm
+            launch_near(c->d, c->ncell, c->nsite, near_mode(c), SESP_T_NEAR, sh, c->st, true, c->chains);   // warm
             float t[5];
             for (int r = 0; r < 5; r++) {
                 cudaEventRecord(e0, c->st);
-                launch_near(c->d, c->ncell, c->nsite, mixed, SESP_T_NEAR, sh, c->st, true, c->chains);
+                launch_near(c->d, c->ncell, c->nsite, near_mode(c), SESP_T_NEAR, sh, c->st, true, c->chains);
                 cudaEventRecord(e1, c->st);
                 cudaEventSynchronize(e1);
                 cudaEventElapsedTime(&t[r], e0, e1);
@@ -1582,7 +1599,7 @@ int sesp_autotune(sesp_ctx *c, int out[3]) {
     CK(cudaStreamSynchronize(c->st));
     out[0] = pick.tile;
     out[1] = pick.grid / c->n_sm;
-    out[2] = near_max_ctas_per_sm(mixed, pick.tile, c->chains);
+    out[2] = near_max_ctas_per_sm(near_mode(c), pick.tile, c->chains);
     return 0;
 }
 
@@ -1814,6 +1831,22 @@ int sesp_energies_static(sesp_ctx *c, double out[8]) {
     const cudaError_t e2 = cudaStreamSynchronize(c->st);
     if (err == cudaSuccess) err = e2;
     if (err != cudaSuccess) return fail(SESP_ECUDA, "sesp_energies_static: %s", cudaGetErrorString(err));
+    return 0;
+}
+
+int sesp_failures_batch(sesp_ctx *c, int64_t *out) {
+    if (int e = check_ctx(c, true)) return e;
+    if (!out) return fail(SESP_EINVAL, "null output");
+    const int M = c->reps.empty() ? 0 : c->reps.back().mol0 + c->reps.back().nmol;
+    std::vector<int> h(M > 0 ? M : 1);
+    if (M > 0) CK(cudaMemcpyAsync(h.data(), c->d.mfail, M * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int q = 0; q < c->nrep; q++) {
+        const Rep &r = c->reps[q];
+        int64_t n = 0;
+        for (int m = r.mol0; m < r.mol0 + r.nmol; m++) n += h[m];
+        out[q] = n;
+    }
     return 0;
 }
 

@@ -20,6 +20,7 @@ LIB_PATH = os.path.join(_HERE, "libsesp.so")
 PLAIN_FP64 = 0
 MIXED = 1          # FP32 force arithmetic, FP64 constraint iterations
 MIXED_FP32C = 2    # MIXED with FP32 constraint iterations
+MIXED_COMP = 3     # MIXED with compensated FP32 sums in the pair field
 # warning bits of Engine.checks (sesp_check_flags)
 CHECK_MOLECULES_LOST, CHECK_CHARGE, CHECK_OH_RATIO, CHECK_MISSING_OXYGEN = 1, 2, 4, 8
 RESCALE_TARGET = 3.9   # target of the reference's temperature-rescaling variant
@@ -38,7 +39,7 @@ SYMBOLS = ["sesp_abi_version", "sesp_last_error", "sesp_default_params", "sesp_c
            "sesp_download_forces", "sesp_init_accel", "sesp_move_a", "sesp_move_b", "sesp_step", "sesp_run",
            "sesp_run_async", "sesp_sync", "sesp_temperature", "sesp_get_eta", "sesp_set_eta", "sesp_energies",
            "sesp_counters", "sesp_kernel_times", "sesp_enable_timing", "sesp_run_timed", "sesp_pair_counts",
-           "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_query", "sesp_device_bytes",
+           "sesp_upload_batch", "sesp_replica_count", "sesp_get_eta_batch", "sesp_set_eta_batch", "sesp_failures_batch", "sesp_query", "sesp_device_bytes",
            "sesp_energies_static", "sesp_autotune", "sesp_tuning", "sesp_set_tuning", "sesp_checks",
            "sesp_check_flags", "sesp_rescale_temperature", "sesp_set_constraint_tuning", "sesp_constraint_tuning",
            "sesp_default_config_params", "sesp_fp32_peak"]
@@ -99,6 +100,8 @@ def load(path: str = LIB_PATH):
     L.sesp_upload_batch.argtypes = [P, ctypes.c_int, ip, ip, ip, dp, dp, ip, dp]
     L.sesp_replica_count.argtypes = [P]
     L.sesp_get_eta_batch.argtypes = [P, dp]
+    L.sesp_set_eta_batch.argtypes = [P, dp]
+    L.sesp_failures_batch.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.sesp_query.argtypes = [P]
     L.sesp_device_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_int64)]
     L.sesp_energies_static.argtypes = [P, dp]
@@ -214,6 +217,18 @@ class Engine:
         out = np.empty(self.replica_count())
         _check(_lib.sesp_get_eta_batch(self._h, _dp(out)))
         return out
+
+    def failures(self):
+        """SHAKE / RATTLE non-convergences per replica since upload."""
+        out = (ctypes.c_int64 * self.replica_count())()
+        _check(_lib.sesp_failures_batch(self._h, out))
+        return np.array(out[:], dtype=np.int64)
+
+    def set_etas(self, etas):
+        v = np.ascontiguousarray(etas, dtype=np.float64)
+        if v.shape != (self.replica_count(),):
+            raise ValueError("one eta per replica")
+        _check(_lib.sesp_set_eta_batch(self._h, _dp(v)))
 
     def close(self):
         if getattr(self, "_h", None):

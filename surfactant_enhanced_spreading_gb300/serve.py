@@ -216,6 +216,143 @@ class Server:
         return sorted(results, key=lambda r: r.rid)
 
 
+class SlotServer:
+    """The same request loop with the running requests as the replicas
+    ("slots") of one batched context, so that every launch advances all of
+    them.
+
+    Requests join and leave at chunk boundaries.  A chunk is `chunk` steps, a
+    multiple of the rebuild interval, so at a boundary every run has just
+    done a rebuild step.  When the set of runs changes, the context is formed
+    again from the runs' current states.  The old context's state is
+    downloaded: positions, velocities, accelerations, eta and failure counts.
+    The new context uploads it and calls force(rebuild).  The rebuild starts
+    from the same positions the runs' last rebuild step used, so it builds
+    the same lists and local expansions.  Each continuing run then gets back
+    its accelerations and eta; a new run gets init_accel's.  A run's
+    trajectory is therefore bit-identical to the same run alone;
+    tests/test_gpu_serve.py checks it.  Request step counts must be multiples
+    of the rebuild interval (10)."""
+
+    def __init__(self, budget_bytes: int, precision: int = E.MIXED, chunk: int = 100, max_active: int = 64,
+                 device: int = 0, keep_state: bool = True, max_failures: int = 1000, interval: int = 10):
+        if chunk % interval:
+            raise ValueError("the chunk must be a multiple of the rebuild interval")
+        self.budget = int(budget_bytes)
+        self.precision = precision
+        self.chunk = int(chunk)
+        self.interval = int(interval)
+        self.max_active = int(max_active)
+        self.max_failures = int(max_failures)
+        self.device = device
+        self.keep_state = keep_state
+        self.peak_used = 0
+        self.reforms = 0            # contexts formed by the last run()
+        self.reform_s = 0.0         # host time spent forming them
+
+    def _form(self, runs):
+        """A batched context over the runs, each at its current state."""
+        t = time.perf_counter()
+        systems = []
+        for a in runs:
+            s = a["req"].system.copy() if a["pos"] is not None else a["req"].system
+            if a["pos"] is not None:
+                s.pos, s.vel = a["pos"], a["vel"]
+            systems.append(s)
+        eng = E.Engine(systems, self.precision, device=self.device)
+        eng.force(True)
+        eng.init_accel()
+        if any(a["pos"] is not None for a in runs):
+            _, _, acc = eng.state()
+            for k, a in enumerate(runs):
+                if a["acc"] is not None:
+                    acc[eng.offsets[k]:eng.offsets[k + 1]] = a["acc"]
+            eng.set_state(None, None, acc, 0.0)
+        eng.set_etas([a["eta"] for a in runs])
+        self.reforms += 1
+        self.reform_s += time.perf_counter() - t
+        return eng
+
+    def run(self, requests: list[Request], clock=time.perf_counter) -> list[Result]:
+        pending = sorted(requests, key=lambda r: (r.arrival, r.rid))
+        presets = {getattr(r.system, "preset", 0) for r in pending}
+        if len(presets) > 1:
+            raise ValueError("the requests of one batched context share one force field (preset)")
+        for r in pending:
+            if estimate_bytes(r.system) > self.budget:
+                raise E.SespError(f"EBUDGET: request {r.rid} needs more than the whole budget")
+            if r.steps % self.interval:
+                raise ValueError(f"request {r.rid}: steps must be a multiple of {self.interval}")
+        runs, results = [], []
+        eng = None
+        kb = 99101
+        used = 0
+        self.peak_used = 0
+        self.reforms, self.reform_s = 0, 0.0
+        t0 = clock()
+        while pending or runs:
+            if eng is not None:
+                eng.sync()
+                fails = eng.failures()
+                for k, a in enumerate(runs):
+                    a["fails"] = a["fails0"] + int(fails[k])
+            now = clock() - t0
+            leaving = [a for a in runs if a["done"] >= a["req"].steps or a["fails"] > self.max_failures]
+            free = used - sum(a["est"] for a in leaving)
+            joining = []
+            for req in pending:
+                if req.arrival > now or len(runs) - len(leaving) + len(joining) >= self.max_active:
+                    break
+                est = estimate_bytes(req.system)
+                if free + est > self.budget:
+                    break
+                free += est
+                joining.append(req)
+            if eng is not None and (leaving or joining):
+                # chunk boundary with a change: take the runs' states out of the context
+                pos, vel, acc = eng.state()
+                etas = eng.etas()
+                for k, a in enumerate(runs):
+                    sl = slice(eng.offsets[k], eng.offsets[k + 1])
+                    a["pos"], a["vel"], a["acc"], a["eta"] = pos[sl], vel[sl], acc[sl], float(etas[k])
+                eng.close()
+                eng = None
+            for a in leaving:
+                req = a["req"]
+                failed = a["done"] < req.steps
+                res = Result(rid=req.rid, n_sites=req.system.n_sites, steps=req.steps, arrival=req.arrival,
+                             admitted=a["admitted"], finished=now, device_bytes=a["est"], estimate_bytes=a["est"],
+                             shake_failures=a["fails"], steps_done=a["done"] if failed else -1, failed=failed)
+                if self.keep_state:
+                    res.pos, res.vel, res.eta = a["pos"], a["vel"], a["eta"]
+                results.append(res)
+                runs.remove(a)
+            used = free
+            self.peak_used = max(self.peak_used, used)
+            for req in joining:
+                pending.remove(req)
+                runs.append({"req": req, "done": 0, "est": estimate_bytes(req.system), "admitted": clock() - t0,
+                             "pos": None, "vel": None, "acc": None, "eta": 0.0, "fails": 0, "fails0": 0})
+            if not runs:
+                if pending:
+                    wait = pending[0].arrival - (clock() - t0)
+                    if wait > 0:
+                        time.sleep(min(wait, 0.01))
+                continue
+            if eng is None:
+                eng = self._form(runs)
+                for a in runs:
+                    a["fails0"] = a["fails"]
+            n = min(self.chunk, min(a["req"].steps - a["done"] for a in runs))
+            eng.run_async(kb, n)
+            kb += n
+            for a in runs:
+                a["done"] += n
+        if eng is not None:
+            eng.close()
+        return sorted(results, key=lambda r: r.rid)
+
+
 def summarize(results: list[Result], wall: float | None = None) -> dict:
     lat = np.array([r.latency for r in results])
     atom_steps = float(sum(r.n_sites * (r.steps if r.steps_done < 0 else r.steps_done) for r in results))

@@ -27,6 +27,9 @@ def test_bench_small_json():
     sv = line["served"]
     assert sv["requests"] == 3 and 0 < sv["p50_latency_s"] <= sv["p99_latency_s"]
     assert sv["failed_requests"] == [] and sv["one_at_a_time_plain_fp64"]["atom_steps_per_s"] > 0
+    sl = sv["slots_of_one_context"]
+    assert sl["requests"] == 3 and sl["failed_requests"] == [] and sl["contexts_formed"] >= 1
+    assert sv["arrival_limited"]["atom_steps_per_s"] > 0
     assert line["e2e_dropin_loop"]["value"] > 0
     assert line["cpu_baseline"]["value"] > 0 and line["force_rms_rel_error_vs_oracle"]["mixed"] < 1e-5
     assert line["force_rms_rel_error_vs_oracle"]["plain_fp64"] < 1e-10

@@ -4,7 +4,8 @@ SPC water, 12-bead flexible chains, graphite, periodic in x and y.
 Bars: plain FP64 forces and energies within 1e-10 (relative) of the oracle,
 per force term and in total; 100-step plain trajectories within 1e-8 sigma;
 mixed-precision force RMS relative error within 1e-5 of the oracle on the
-20,000-water / 200-chain shape; replicas bit-identical alone and batched."""
+20,000-water / 200-chain shape (also with compensated FP32 sums);
+replicas bit-identical alone and batched."""
 import numpy as np
 import pytest
 
@@ -115,22 +116,23 @@ def test_mixed_force_error_c2_shape():
     s = C.config_droplet(**C.C2, seed=2024)
     orc = O.Oracle(s)
     fo = orc.force(True)
-    for prec in (E.MIXED, E.MIXED_FP32C):
+    for prec in (E.MIXED, E.MIXED_FP32C, E.MIXED_COMP):
         fm = E.Engine(s, prec).force(True)
         assert rel(fm, fo) < 1e-5, (prec, rel(fm, fo))
     fp = E.Engine(s, E.PLAIN_FP64).force(True)
     assert rel(fp, fo) < 1e-10
 
 
-def test_replicas_bit_identical_alone_and_batched():
+@pytest.mark.parametrize("prec", [E.MIXED, E.MIXED_COMP])
+def test_replicas_bit_identical_alone_and_batched(prec):
     systems = [C.config_droplet(400, 4, cells=(8, 8, 8), seed=31), C.config_droplet(900, 10, cells=(12, 8, 8), seed=32)]
-    batch = E.Engine(systems, E.MIXED)
+    batch = E.Engine(systems, prec)
     batch.force(True)
     batch.init_accel()
     batch.run(1, 25)
     pb, vb, _ = batch.state()
     for k, s in enumerate(systems):
-        e = E.Engine(s, E.MIXED)
+        e = E.Engine(s, prec)
         e.force(True)
         e.init_accel()
         e.run(1, 25)
