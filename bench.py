@@ -189,6 +189,7 @@ def run_served(args, local, peak_rate=None):
     swall = time.perf_counter() - t1
     out["slots_of_one_context"] = serve.summarize(sres) | {
         "wall_s": swall, "contexts_formed": slots.reforms, "forming_s": slots.reform_s,
+        "forming_parts_s": slots.form_parts,
         "how": "running requests as the replicas of one batched context; at 100-step chunk boundaries (after a "
                "rebuild step) finished runs leave, arrivals join and the context is formed again from the runs' "
                "states (bit-identical to each run alone)"}

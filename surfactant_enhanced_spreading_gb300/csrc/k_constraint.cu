@@ -351,7 +351,11 @@ __device__ __forceinline__ int water_b(const Dev &d, int m, double tol, int maxi
 // one solve of A h = -R.V (A_bc = R_b . K_bc R_c) meets them, checked with
 // RATTLE's own test.  Both converge to the constrained state the sweeps
 // approach, so the result differs from the sweeps' by less than the
-// tolerance.
+// tolerance.  The 3 x 3 matrices, their inverses and the steps are FP32
+// (GB300 issues FP32 at 64 times its FP64 rate): they only steer.  The
+// residuals, the tolerance tests, the state and the sums of the corrections
+// stay FP64.  A FP32 residual resolves only about the tolerance band, so the
+// last step or two start from the FP64 residual.
 
 // K_bc of the water triangle (bond b joins sites b and b + 1 mod 3): the
 // sum of the inverse masses on the diagonal, minus the inverse mass of the
@@ -364,7 +368,7 @@ __device__ __forceinline__ double wk(int b, int c) {
 // s_kb: +1 if site k is bond b's first site, -1 if its second, else 0
 __device__ __forceinline__ double wsgn(int k, int b) { return k == wbi(b) ? 1.0 : (k == wbj(b) ? -1.0 : 0.0); }
 
-__device__ __forceinline__ void inv3(const double (&A)[3][3], double (&B)[3][3]) {
+__device__ __forceinline__ void inv3f(const float (&A)[3][3], float (&B)[3][3]) {
     B[0][0] = A[1][1] * A[2][2] - A[1][2] * A[2][1];
     B[0][1] = A[0][2] * A[2][1] - A[0][1] * A[2][2];
     B[0][2] = A[0][1] * A[1][2] - A[0][2] * A[1][1];
@@ -374,12 +378,38 @@ __device__ __forceinline__ void inv3(const double (&A)[3][3], double (&B)[3][3])
     B[2][0] = A[1][0] * A[2][1] - A[1][1] * A[2][0];
     B[2][1] = A[0][1] * A[2][0] - A[0][0] * A[2][1];
     B[2][2] = A[0][0] * A[1][1] - A[0][1] * A[1][0];
-    const double id = 1.0 / (A[0][0] * B[0][0] + A[0][1] * B[1][0] + A[0][2] * B[2][0]);
+    const float id = 1.f / (A[0][0] * B[0][0] + A[0][1] * B[1][0] + A[0][2] * B[2][0]);
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
         for (int j = 0; j < 3; j++) B[i][j] *= id;
 }
+
+// site corrections of bond multipliers h: site k moves by s_kb h_b R_b / m_k
+__device__ __forceinline__ void water_move32(const float (&R)[3][3], const float (&h)[3], float (&c)[3][3]) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const float rm = (float)cF.rm64[wkind(k)];
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const float w = (float)wsgn(k, b) * rm * h[b];
+            if (w != 0.f) { c[k][0] += w * R[b][0]; c[k][1] += w * R[b][1]; c[k][2] += w * R[b][2]; }
+        }
+    }
+}
+
+// one Newton step on the corrections from residuals f: g = -J^-1 f
+__device__ __forceinline__ void water_step32(const float (&Ji)[3][3], const float (&R)[3][3], const float (&f)[3],
+                                             float (&c)[3][3]) {
+    float g[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) g[b] = -(Ji[b][0] * f[0] + Ji[b][1] * f[1] + Ji[b][2] * f[2]);
+    water_move32(R, g, c);
+}
+
+// FP32 Newton steps of a water's SHAKE before its FP64 tests (about 4 meet
+// the FP32 residual's resolution)
+constexpr int WMAT_FP32_STEPS = 8;
 
 // SHAKE half of one water in matrix form; returns the Newton steps it ran
 __device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int maxit) {
@@ -410,15 +440,49 @@ __device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int 
         D0[b] = cF.dsq64_w[b] - (P[b][0] * P[b][0] + P[b][1] * P[b][1] + P[b][2] * P[b][2]);
         thr[b] = cF.dsq64_w[b] * (2.0 * tol);
     }
-    double J[3][3], Ji[3][3];
+    // the Jacobian and its inverse in FP32: they only steer the steps
+    float R32[3][3], P32[3][3], J[3][3], Ji[3][3];
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int a = 0; a < 3; a++) { R32[b][a] = (float)R[b][a]; P32[b][a] = (float)P[b][a]; }
 #pragma unroll
     for (int b = 0; b < 3; b++)
 #pragma unroll
         for (int c = 0; c < 3; c++)
-            J[b][c] = -2.0 * wk(b, c) * (P[b][0] * R[c][0] + P[b][1] * R[c][1] + P[b][2] * R[c][2]);
-    inv3(J, Ji);
-    double cc[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};   // per-site corrections
+            J[b][c] = -2.f * (float)wk(b, c) * (P32[b][0] * R32[c][0] + P32[b][1] * R32[c][1] + P32[b][2] * R32[c][2]);
+    inv3f(J, Ji);
+    // FP32 steps on the corrections until the FP32 residual is inside the
+    // tolerance (its rounding, ~1e-9 of d^2 ~ 0.1, is about the tolerance
+    // band itself, so these only bring the corrections near the answer)
+    float c32[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
     int it = 0;
+    for (int k32 = 0; k32 < WMAT_FP32_STEPS && it <= maxit; k32++) {
+        float f[3];
+        bool in = true;
+#pragma unroll
+        for (int b = 0; b < 3; b++) {
+            const int i = wbi(b), j = wbj(b);
+            float q = 0.f;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                const float cd = c32[i][a] - c32[j][a];
+                q += cd * (cd + 2.f * P32[b][a]);
+            }
+            f[b] = (float)D0[b] - q;
+            in = in && !(fabsf(f[b]) > (float)thr[b]);
+        }
+        if (in) break;
+        water_step32(Ji, R32, f, c32);
+        it++;
+    }
+    double cc[3][3];
+#pragma unroll
+    for (int k = 0; k < 3; k++)
+#pragma unroll
+        for (int a = 0; a < 3; a++) cc[k][a] = (double)c32[k][a];
+    // the tolerance test in FP64, as the reference's; a failed test takes
+    // one more step from the FP64 residual (solved in FP32: it is small)
     bool done = false;
     while (it <= maxit) {
         double f[3];
@@ -436,18 +500,12 @@ __device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int 
             done = done && !(fabs(f[b]) > thr[b]);
         }
         if (done) break;
-        double dg[3];
+        float f32[3] = {(float)f[0], (float)f[1], (float)f[2]}, d32[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+        water_step32(Ji, R32, f32, d32);
 #pragma unroll
-        for (int b = 0; b < 3; b++) dg[b] = -(Ji[b][0] * f[0] + Ji[b][1] * f[1] + Ji[b][2] * f[2]);
+        for (int k = 0; k < 3; k++)
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const double rm = cF.rm64[wkind(k)];
-#pragma unroll
-            for (int b = 0; b < 3; b++) {
-                const double w = wsgn(k, b) * rm * dg[b];
-                if (w != 0.0) { cc[k][0] += w * R[b][0]; cc[k][1] += w * R[b][1]; cc[k][2] += w * R[b][2]; }
-            }
-        }
+            for (int a = 0; a < 3; a++) cc[k][a] += (double)d32[k][a];
         it++;
     }
     double ke1 = 0.0;
@@ -487,12 +545,18 @@ __device__ __forceinline__ int water_b_mat(const Dev &d, int m, double tol, int 
     for (int b = 0; b < 3; b++)
 #pragma unroll
         for (int a = 0; a < 3; a++) R[b][a] = r[wbi(b)][a] - r[wbj(b)][a];
-    double A[3][3], Ai[3][3];
+    // the matrix and its inverse in FP32 (they steer the solve; the test is FP64)
+    float R32[3][3], A[3][3], Ai[3][3];
 #pragma unroll
     for (int b = 0; b < 3; b++)
 #pragma unroll
-        for (int c = 0; c < 3; c++) A[b][c] = wk(b, c) * (R[b][0] * R[c][0] + R[b][1] * R[c][1] + R[b][2] * R[c][2]);
-    inv3(A, Ai);
+        for (int c = 0; c < 3; c++) R32[b][c] = (float)R[b][c];
+#pragma unroll
+    for (int b = 0; b < 3; b++)
+#pragma unroll
+        for (int c = 0; c < 3; c++)
+            A[b][c] = (float)wk(b, c) * (R32[b][0] * R32[c][0] + R32[b][1] * R32[c][1] + R32[b][2] * R32[c][2]);
+    inv3f(A, Ai);
     int it = 0;
     bool done = false;
     while (it <= maxit) {
@@ -506,18 +570,16 @@ __device__ __forceinline__ int water_b_mat(const Dev &d, int m, double tol, int 
             done = done && !(fabs(cF.fb64_w[b] * rv[b]) > tol);
         }
         if (done) break;
-        double h[3];
+        // A h = -R.V in FP32 (R.V is small: the rounding of h is far below the tolerance)
+        float rv32[3] = {(float)rv[0], (float)rv[1], (float)rv[2]}, d32[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+        float h[3];
 #pragma unroll
-        for (int b = 0; b < 3; b++) h[b] = -(Ai[b][0] * rv[0] + Ai[b][1] * rv[1] + Ai[b][2] * rv[2]);
+        for (int b = 0; b < 3; b++) h[b] = -(Ai[b][0] * rv32[0] + Ai[b][1] * rv32[1] + Ai[b][2] * rv32[2]);
+        water_move32(R32, h, d32);
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            const double rm = cF.rm64[wkind(k)];
+        for (int k = 0; k < 3; k++)
 #pragma unroll
-            for (int b = 0; b < 3; b++) {
-                const double w = wsgn(k, b) * rm * h[b];
-                if (w != 0.0) { v[k][0] += w * R[b][0]; v[k][1] += w * R[b][1]; v[k][2] += w * R[b][2]; }
-            }
-        }
+            for (int a = 0; a < 3; a++) v[k][a] += (double)d32[k][a];
         it++;
     }
 #pragma unroll

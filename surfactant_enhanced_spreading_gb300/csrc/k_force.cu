@@ -550,21 +550,30 @@ __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int
 }
 
 // One partner cell's sites (slots t0..t1, LJ-carrying ones before th) on
-// the targets u, in the partner cell's frame.  EXCL: some target's molecule
-// has a site in this cell, so partners of the same molecule are skipped.
+// the targets u, in the partner cell's frame.  The LJ-carrying prefix always
+// tests for partners of a target's own molecule; the water-H suffix (about
+// two thirds of the pairs) does so only when EXCL says some target's molecule
+// has a site in this cell.  Only that loop comes in two versions, and the
+// testing one is not unrolled: a second LJ loop and more unrolling cost more
+// in instruction-cache stalls than they saved in instructions.
 template <int K, bool EXCL, bool COMP>
 __device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, const int *__restrict__ keys,
                                             Tgt32 (&u)[K], int t0, int th, int t1, const float2 *ljt, float rc2,
                                             Acc32<K, COMP> &f) {
 #pragma unroll 2
-    for (int sl = t0; sl < th; sl++) pairk_acc32<K, EXCL, COMP>(u, pos32[sl], keys[sl], ljt, rc2, f);
+    for (int sl = t0; sl < th; sl++) pairk_acc32<K, true, COMP>(u, pos32[sl], keys[sl], ljt, rc2, f);
     if (th < t1) {
         const float qh = pos32[th].w;
 #pragma unroll
         for (int j = 0; j < K; j++) u[j].q *= qh;
     }
+    if constexpr (EXCL) {
+#pragma unroll 1
+        for (int sl = th; sl < t1; sl++) pairk_coul32<K, true, COMP>(u, pos32[sl], keys[sl] >> 5, f);
+    } else {
 #pragma unroll 2
-    for (int sl = th; sl < t1; sl++) pairk_coul32<K, EXCL, COMP>(u, pos32[sl], EXCL ? keys[sl] >> 5 : 0, f);
+        for (int sl = th; sl < t1; sl++) pairk_coul32<K, false, COMP>(u, pos32[sl], 0, f);
+    }
 }
 
 // One FP32 work item with K target sites per lane (lane + 32 j of the chunk):
@@ -619,7 +628,8 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
         for (int j = 0; j < K; j++) { u[j] = t[j]; u[j].x += sx; u[j].y += sy; u[j].z += sz; }
         // partners with LJ first (the cell sort puts water H last)
         const int th = t0 + d.cnh[cn];
-        if ((excl >> (jx - ix + 1)) & 1u) near_cell32<K, true, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
+        // (items of one target per lane keep one loop body: less code)
+        if (K == 1 || ((excl >> (jx - ix + 1)) & 1u)) near_cell32<K, true, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
         else near_cell32<K, false, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
     }
     float *part = (float *)d.near_part + (size_t)pr * 3 * nslot;   // FP32 row partials on the mixed path
@@ -1072,15 +1082,19 @@ __device__ inline void m2l_terms(int o, const R *cf, int (&h)[LP], R (&cr)[LP], 
     }
 }
 
+// one term table entry of an L2 M2L output: H index and coefficient (the
+// conjugate's sign folded into ci)
+template <typename R>
+struct M2LTerm { int h; R cr, ci; };
 template <typename R, typename S>
-__device__ __forceinline__ void m2l_acc(const C2<R> *__restrict__ H, const S *src, const int (&h)[LP],
-                                        const R (&cr)[LP], const R (&ci)[LP], R &re, R &im) {
-#pragma unroll
+__device__ __forceinline__ void m2l_acc_s(const C2<R> *__restrict__ H, const S *src, const M2LTerm<R> *tm, R &re, R &im) {
+#pragma unroll 5
     for (int nm = 0; nm < LP; nm++) {
-        const C2<R> hv = H[h[nm]];
+        const M2LTerm<R> t = tm[nm];
+        const C2<R> hv = H[t.h];
         const S mv = src[nm];
         const R mx = (R)mv.x, my = (R)mv.y;
-        const R t1 = cr[nm] * hv.x, t2 = ci[nm] * hv.y;
+        const R t1 = t.cr * hv.x, t2 = t.ci * hv.y;
         re += t1 * mx - t2 * my;
         im += t1 * my + t2 * mx;
     }
@@ -1261,9 +1275,17 @@ __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const
     for (int idx = threadIdx.x; idx < LPH * LP; idx += blockDim.x) scf[idx] = cf[idx];
     __syncthreads();
     const int hw = threadIdx.x >> 4, o = threadIdx.x & 15;
-    int h[LP];
-    R cr[LP], ci[LP];
-    m2l_terms<R>(o < LPH ? o : LPH - 1, scf, h, cr, ci);
+    // the term tables of the 15 outputs in shared memory, not registers (128
+    // -> 48 registers: more CTAs per SM to hide the H and O loads)
+    __shared__ M2LTerm<R> sterm[LPH][LP];
+    if (threadIdx.x < LPH) {
+        int h[LP];
+        R cr[LP], ci[LP];
+        m2l_terms<R>(threadIdx.x, scf, h, cr, ci);
+        for (int nm = 0; nm < LP; nm++) sterm[threadIdx.x][nm] = {h[nm], cr[nm], ci[nm]};
+    }
+    __syncthreads();
+    const M2LTerm<R> *tm = sterm[o < LPH ? o : LPH - 1];
     const int nb = n[0] * n[1] * n[2];
     R re = 0, im = 0;
     if (r.per) {
@@ -1273,7 +1295,7 @@ __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const
         for (int s = hw; s < nb; s += 16) {
             const int sx = s % n[0], sy = (s / n[0]) % n[1], sz = s / (n[0] * n[1]);
             const int oi = (sx - t[0] + n[0] - 1) + wx * ((sy - t[1] + n[1] - 1) + wy * (sz - t[2] + n[2] - 1));
-            m2l_acc<R>(Hr + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, h, cr, ci, re, im);
+            m2l_acc_s<R>(Hr + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, tm, re, im);
         }
     } else {
         const int wx = 2 * d2.x + 1, wy = 2 * d2.y + 1;
@@ -1282,7 +1304,7 @@ __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const
             const int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
             if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
             const int oi = (dx + d2.x) + wx * ((dy + d2.y) + wy * (dz + d2.z));
-            m2l_acc<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, h, cr, ci, re, im);
+            m2l_acc_s<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, tm, re, im);
         }
     }
     if (o < LPH) { sre[hw][o] = re; sim[hw][o] = im; }

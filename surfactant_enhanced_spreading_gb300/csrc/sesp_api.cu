@@ -2,6 +2,7 @@
 // state, host-side force-field tables and multipole translation operators,
 // and the per-step launch sequence (captured into CUDA graphs by sesp_run).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -737,6 +738,16 @@ struct RepIn {
 
 // Lay out one or more replica systems back to back and upload them.
 int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
+    // SESP_TRACE_UPLOAD set: host time of each phase to stderr
+    const bool trace = getenv("SESP_TRACE_UPLOAD") != nullptr;
+    auto t_last = std::chrono::steady_clock::now();
+    auto lap = [&](const char *what) {
+        if (!trace) return;
+        cudaStreamSynchronize(c->st);
+        const auto now = std::chrono::steady_clock::now();
+        fprintf(stderr, "sesp upload: %-22s %8.2f ms\n", what, std::chrono::duration<double, std::milli>(now - t_last).count());
+        t_last = now;
+    };
     if (set_device(c)) return SESP_ECUDA;
     cudaStreamSynchronize(c->st);
     free_state(c);
@@ -807,6 +818,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     int e = 0;
     double **a12[12] = {&d.x, &d.y, &d.z, &d.vx, &d.vy, &d.vz, &d.ax, &d.ay, &d.az, &d.fx, &d.fy, &d.fz};
     for (auto q : a12) if ((e = dalloc(c, q, N))) return e;
+    lap("replica checks");
     if ((e = dalloc(c, &d.ptype, N)) || (e = dalloc(c, &d.smol, N)) || (e = dalloc(c, &d.mrep, M)) ||
         (e = dalloc(c, &d.mfirst, M)) || (e = dalloc(c, &d.mkind, M)) || (e = dalloc(c, &d.mkey, M)) ||
         (e = dalloc(c, &d.mw1, M)) || (e = dalloc(c, &d.ke, 2 * M)) || (e = dalloc(c, &d.mfail, M)) ||
@@ -834,6 +846,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         return e;
     const int w2x = 2 * d2.x + 1, w2y = 2 * d2.y + 1, w2z = 2 * d2.z + 1;
     const size_t nh2 = (size_t)w2x * w2y * w2z * NHARM;
+    lap("allocation");
     // real-form M2L at L4 and L3: work items of M2C_TILE targets of one parity
     // class, each split into M2C_GROUPS offset groups (a constant, so a
     // replica's sums do not depend on what else is batched with it)
@@ -889,6 +902,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.op32_m2m43, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op32_m2m32, (size_t)8 * LPH * LP)) ||
         (e = dalloc(c, &d.op32_l2l23, (size_t)8 * LPH * LP)) || (e = dalloc(c, &d.op32_l2l34, (size_t)8 * LPH * LP)))
         return e;
+    lap("M2L work items");
     // static per-site / per-molecule / per-box data
     std::vector<uint8_t> ptype(N);
     std::vector<int> smol(N), mrep(M), mfirst(M), mkind(M), wm, sm, crep(C), b3(n3), b2(n2);
@@ -1045,6 +1059,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.gbin, gbin.size())) || (e = dalloc(c, &d.ggrp_z, ggrp_z.size())) ||
         (e = dalloc(c, &d.gsite, N)) || (e = dalloc(c, &d.gcount, 1)))
         return e;
+    lap("per-site data, carbons");
     // translation operators
     // M2L factors: H per offset at L4 (cell edge rs), L3 (2 rs) and L2 (4 rs), and the coefficients
     auto put = [&](const std::vector<double2> &h, double2 *dst, float2 *dst32) -> int {
@@ -1079,6 +1094,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         }
         return 0;
     };
+    lap("operators, M2L factors");
     if ((e = fill_win(RS, d.rop4)) || (e = fill_win(2 * RS, d.rop3))) return e;
     {
         std::vector<double2> h(nh2, make_double2(0.0, 0.0));
@@ -1171,6 +1187,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     CK(cudaMemcpyAsync(d.mrep, mrep.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.mfirst, mfirst.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(d.mkind, mkind.data(), M * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    lap("window operators, H tables");
     if (nwm) {
         CK(cudaMemcpyAsync(c->wmols, wm.data(), nwm * sizeof(int), cudaMemcpyHostToDevice, c->st));
         CK(cudaMemcpyAsync(d.wlist_a, wm.data(), nwm * sizeof(int), cudaMemcpyHostToDevice, c->st));
@@ -1198,6 +1215,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
     c->uploaded = true;
     c->have_force = false;
     c->steps = 0;
+    lap("water lists, graphite");
     return 0;
 }
 

@@ -249,10 +249,17 @@ class SlotServer:
         self.peak_used = 0
         self.reforms = 0            # contexts formed by the last run()
         self.reform_s = 0.0         # host time spent forming them
+        self.form_parts = {}        # ... split into upload, force and state
 
     def _form(self, runs):
         """A batched context over the runs, each at its current state."""
         t = time.perf_counter()
+        mark = [t]
+
+        def lap(name):
+            now = time.perf_counter()
+            self.form_parts[name] = self.form_parts.get(name, 0.0) + now - mark[0]
+            mark[0] = now
         systems = []
         for a in runs:
             s = a["req"].system.copy() if a["pos"] is not None else a["req"].system
@@ -260,7 +267,9 @@ class SlotServer:
                 s.pos, s.vel = a["pos"], a["vel"]
             systems.append(s)
         eng = E.Engine(systems, self.precision, device=self.device)
+        lap("upload")
         eng.force(True)
+        lap("force")
         eng.init_accel()
         if any(a["pos"] is not None for a in runs):
             _, _, acc = eng.state()
@@ -269,6 +278,7 @@ class SlotServer:
                     acc[eng.offsets[k]:eng.offsets[k + 1]] = a["acc"]
             eng.set_state(None, None, acc, 0.0)
         eng.set_etas([a["eta"] for a in runs])
+        lap("state")
         self.reforms += 1
         self.reform_s += time.perf_counter() - t
         return eng
@@ -288,7 +298,7 @@ class SlotServer:
         kb = 99101
         used = 0
         self.peak_used = 0
-        self.reforms, self.reform_s = 0, 0.0
+        self.reforms, self.reform_s, self.form_parts = 0, 0.0, {}
         t0 = clock()
         while pending or runs:
             if eng is not None:
