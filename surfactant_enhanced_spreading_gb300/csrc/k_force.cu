@@ -555,24 +555,45 @@ __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int
 // two thirds of the pairs) does so only when EXCL says some target's molecule
 // has a site in this cell.  Only that loop comes in two versions, and the
 // testing one is not unrolled: a second LJ loop and more unrolling cost more
-// in instruction-cache stalls than they saved in instructions.
+// in instruction-cache stalls than they saved in instructions.  The warp
+// stages 32 partners at a time in its shared-memory slot (one coalesced
+// load per lane) and reads them back as broadcasts: shorter load latency
+// than a broadcast L1 load per partner.
 template <int K, bool EXCL, bool COMP>
 __device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, const int *__restrict__ keys,
                                             Tgt32 (&u)[K], int t0, int th, int t1, const float2 *ljt, float rc2,
-                                            Acc32<K, COMP> &f) {
+                                            Acc32<K, COMP> &f, float4 *wpos, int *wkey, int lane) {
+    for (int b0 = t0; b0 < th; b0 += 32) {
+        const int n = min(32, th - b0);
+        __syncwarp();
+        if (lane < n) { wpos[lane] = pos32[b0 + lane]; wkey[lane] = keys[b0 + lane]; }
+        __syncwarp();
 #pragma unroll 2
-    for (int sl = t0; sl < th; sl++) pairk_acc32<K, true, COMP>(u, pos32[sl], keys[sl], ljt, rc2, f);
+        for (int k = 0; k < n; k++) pairk_acc32<K, true, COMP>(u, wpos[k], wkey[k], ljt, rc2, f);
+    }
     if (th < t1) {
         const float qh = pos32[th].w;
 #pragma unroll
         for (int j = 0; j < K; j++) u[j].q *= qh;
     }
     if constexpr (EXCL) {
+        for (int b0 = th; b0 < t1; b0 += 32) {
+            const int n = min(32, t1 - b0);
+            __syncwarp();
+            if (lane < n) { wpos[lane] = pos32[b0 + lane]; wkey[lane] = keys[b0 + lane]; }
+            __syncwarp();
 #pragma unroll 1
-        for (int sl = th; sl < t1; sl++) pairk_coul32<K, true, COMP>(u, pos32[sl], keys[sl] >> 5, f);
+            for (int k = 0; k < n; k++) pairk_coul32<K, true, COMP>(u, wpos[k], wkey[k] >> 5, f);
+        }
     } else {
+        for (int b0 = th; b0 < t1; b0 += 32) {
+            const int n = min(32, t1 - b0);
+            __syncwarp();
+            if (lane < n) wpos[lane] = pos32[b0 + lane];
+            __syncwarp();
 #pragma unroll 2
-        for (int sl = th; sl < t1; sl++) pairk_coul32<K, false, COMP>(u, pos32[sl], 0, f);
+            for (int k = 0; k < n; k++) pairk_coul32<K, false, COMP>(u, wpos[k], 0, f);
+        }
     }
 }
 
@@ -580,7 +601,7 @@ __device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, co
 // the force of partner row pr on them, written to that row's partial.
 template <int K, bool PER, bool COMP>
 __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int nslot, int c, int pr, int first,
-                                            int ni, int lane) {
+                                            int ni, int lane, float4 *wpos, int *wkey) {
     const float4 *__restrict__ pos32 = d.srt_pos32;
     const int *__restrict__ keys = d.srt_key;
     const int dzc = pr / 3 - 1, dyc = pr % 3 - 1;
@@ -629,8 +650,8 @@ __device__ __forceinline__ void near_item32(const Dev &d, const float2 *ljt, int
         // partners with LJ first (the cell sort puts water H last)
         const int th = t0 + d.cnh[cn];
         // (items of one target per lane keep one loop body: less code)
-        if (K == 1 || ((excl >> (jx - ix + 1)) & 1u)) near_cell32<K, true, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
-        else near_cell32<K, false, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f);
+        if (K == 1 || ((excl >> (jx - ix + 1)) & 1u)) near_cell32<K, true, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f, wpos, wkey, lane);
+        else near_cell32<K, false, COMP>(pos32, keys, u, t0, th, t1, ljt, rc2, f, wpos, wkey, lane);
     }
     float *part = (float *)d.near_part + (size_t)pr * 3 * nslot;   // FP32 row partials on the mixed path
 #pragma unroll
@@ -682,8 +703,9 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 
 // Near field as a persistent kernel: each warp takes items from a global
 // counter until none are left, and for its item sums the force of one
-// partner row on 64 target sites (2 per lane), reading the partners straight
-// from L1 (one broadcast load per partner for the whole warp).  Each item
+// partner row on 64 target sites (2 per lane), reading the partners as
+// broadcasts (FP32: staged 32 at a time in the warp's shared-memory slot;
+// FP64: one broadcast L1 load per partner).  Each item
 // writes its own partial per slot (near_part[plane * 3 + row]); k_near_finish
 // adds the 9 partials in a fixed order.  Which warp takes which item does not
 // change any arithmetic, so results are bit-reproducible.
@@ -695,6 +717,8 @@ template <bool MIXED, int KMAX, bool PER, bool COMP = false>
 __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int tile) {
     griddep_wait();
     __shared__ float2 s_lj32[MIXED ? NTYPE * NTYPE : 1];
+    __shared__ float4 s_stage[MIXED ? NEAR_THREADS / 32 : 1][32];
+    __shared__ int s_key[MIXED ? NEAR_THREADS / 32 : 1][32];
     __shared__ double2 s_lj64[MIXED ? 1 : NTYPE * NTYPE];
     if constexpr (MIXED) {
         for (int t = threadIdx.x; t < NTYPE * NTYPE; t += blockDim.x) s_lj32[t] = d.ljt32[t];
@@ -729,10 +753,10 @@ __global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int til
         if constexpr (MIXED) {
             // K = targets per lane: ceil(targets of the chunk / 32), at most KMAX
             const int nt = min(tile, ni - chunk * tile), kk = (nt + 31) >> 5;
-            if (kk <= 1) near_item32<1, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else if (kk == 2 || KMAX == 2) near_item32<2, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else if (kk == 3) near_item32<(KMAX > 2 ? 3 : 2), PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
-            else near_item32<KMAX, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane);
+            if (kk <= 1) near_item32<1, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane, s_stage[threadIdx.x >> 5], s_key[threadIdx.x >> 5]);
+            else if (kk == 2 || KMAX == 2) near_item32<2, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane, s_stage[threadIdx.x >> 5], s_key[threadIdx.x >> 5]);
+            else if (kk == 3) near_item32<(KMAX > 2 ? 3 : 2), PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane, s_stage[threadIdx.x >> 5], s_key[threadIdx.x >> 5]);
+            else near_item32<KMAX, PER, COMP>(d, s_lj32, nslot, c, pr, chunk * tile, ni, lane, s_stage[threadIdx.x >> 5], s_key[threadIdx.x >> 5]);
         } else {
             Tgt64 ta = {0.0, 0.0, 0.0, 0.0, -1, 0}, tb = ta;
             if (a0) {

@@ -3,6 +3,8 @@
 // and the per-step launch sequence (captured into CUDA graphs by sesp_run).
 #include <algorithm>
 #include <chrono>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <complex>
 #include <cstdarg>
@@ -977,81 +979,109 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
             }
         }
         // carbons per bottom-layer column, pre-filtered as src/read_graphite.f90:9-35
-        // (lp: the listed carbons' coordinates as the column sees them)
-        std::vector<double> lp;
-        for (int iy = 0; iy < r.nc[1]; iy++)
-            for (int ix = 0; ix < r.nc[0]; ix++) {
-                double cx = axis[a0 + ix], cy = axis[a0 + r.nc[0] + iy], cz = axis[a0 + r.nc[0] + r.nc[1]];
-                lp.clear();
-                if (per) {
-                    const double rc2 = rcut_per * rcut_per;
-                    for (int by = iy - 2; by <= iy + 2; by++)      // 5 x 5 columns cover rcut_per (< 2.5 cells);
-                        for (int bx = ix - 2; bx <= ix + 2; bx++) { // at least 8 per axis: no column twice
-                            const int wx = ((bx % r.nc[0]) + r.nc[0]) % r.nc[0], wy = ((by % r.nc[1]) + r.nc[1]) % r.nc[1];
-                            const int b = wx + r.nc[0] * wy;
-                            for (int t = cbin_start[b]; t < cbin_start[b + 1]; t++) {
-                                const int k = cbin[t];
-                                // the image of the carbon nearest the column centre
-                                double gx = ri.carb[3 * k], gy = ri.carb[3 * k + 1];
-                                gx -= r.rsd[0] * floor((gx - cx) / r.rsd[0] + 0.5);
-                                gy -= r.rsd[1] * floor((gy - cy) / r.rsd[1] + 0.5);
-                                const double dx = gx - cx, dy = gy - cy;
-                                if (dx * dx + dy * dy <= rc2) { lp.push_back(gx); lp.push_back(gy); lp.push_back(ri.carb[3 * k + 2]); }
-                            }
+        // (lp: the listed carbons' coordinates as the column sees them).
+        // Columns are independent: built on host threads, then appended in
+        // column order (the same arrays as a serial loop).
+        struct ColOut {
+            std::vector<double4> gpos;
+            std::vector<float4> gpos32;
+            std::vector<int> gbin;        // relative to the column's first carbon
+            std::vector<float2> ggrp_z;
+        };
+        const int ncol_r = r.nc[0] * r.nc[1];
+        std::vector<ColOut> cols(ncol_r);
+        auto build_col = [&](int col) {
+            const int ix = col % r.nc[0], iy = col / r.nc[0];
+            ColOut &co = cols[col];
+            std::vector<double> lp;
+            double cx = axis[a0 + ix], cy = axis[a0 + r.nc[0] + iy], cz = axis[a0 + r.nc[0] + r.nc[1]];
+            if (per) {
+                const double rc2 = rcut_per * rcut_per;
+                for (int by = iy - 2; by <= iy + 2; by++)      // 5 x 5 columns cover rcut_per (< 2.5 cells);
+                    for (int bx = ix - 2; bx <= ix + 2; bx++) { // at least 8 per axis: no column twice
+                        const int wx = ((bx % r.nc[0]) + r.nc[0]) % r.nc[0], wy = ((by % r.nc[1]) + r.nc[1]) % r.nc[1];
+                        const int b = wx + r.nc[0] * wy;
+                        for (int t = cbin_start[b]; t < cbin_start[b + 1]; t++) {
+                            const int k = cbin[t];
+                            // the image of the carbon nearest the column centre
+                            double gx = ri.carb[3 * k], gy = ri.carb[3 * k + 1];
+                            gx -= r.rsd[0] * floor((gx - cx) / r.rsd[0] + 0.5);
+                            gy -= r.rsd[1] * floor((gy - cy) / r.rsd[1] + 0.5);
+                            const double dx = gx - cx, dy = gy - cy;
+                            if (dx * dx + dy * dy <= rc2) { lp.push_back(gx); lp.push_back(gy); lp.push_back(ri.carb[3 * k + 2]); }
                         }
-                } else {
-                    for (int k = 0; k < ri.ncarb; k++) {
-                        double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
-                        if (dx * dx + dy * dy <= rcut)
-                            for (int a = 0; a < 3; a++) lp.push_back(ri.carb[3 * k + a]);
                     }
+            } else {
+                for (int k = 0; k < ri.ncarb; k++) {
+                    double dx = ri.carb[3 * k] - cx, dy = ri.carb[3 * k + 1] - cy;
+                    if (dx * dx + dy * dy <= rcut)
+                        for (int a = 0; a < 3; a++) lp.push_back(ri.carb[3 * k + a]);
                 }
-                std::vector<int> ks(lp.size() / 3);
-                for (size_t i = 0; i < ks.size(); i++) ks[i] = (int)i;
-                // groups: the column's carbons by z (a graphite layer each, at
-                // most GGRP groups of neighbouring z), each group in order of
-                // its FP32 y with GBIN uniform y bins over [-ymax, ymax], so a
-                // site visits only the groups and the y window within rc
-                std::sort(ks.begin(), ks.end(), [&](int a, int b) {
-                    return lp[3 * a + 2] != lp[3 * b + 2] ? lp[3 * a + 2] < lp[3 * b + 2] : a < b;
-                });
-                std::vector<int> bounds(1, 0);
-                for (size_t t = 1; t < ks.size(); t++)
-                    if (lp[3 * ks[t] + 2] != lp[3 * ks[t - 1] + 2]) bounds.push_back((int)t);
-                bounds.push_back((int)ks.size());
-                const int nz = (int)bounds.size() - 1;
-                std::vector<int> gb(1, 0);   // group bounds: every z level, or GGRP equal runs of them
-                for (int l = 1; l <= GGRP; l++)
-                    gb.push_back(bounds[nz <= GGRP ? (l <= nz ? l : nz) : (int)((long long)nz * l / GGRP)]);
-                auto y32 = [&](int k) { return (float)(lp[3 * k + 1] - cy); };
-                const int base = (int)gpos.size();
-                for (int l = 0; l < GGRP; l++) {
-                    const int b0 = gb[l], b1 = gb[l + 1];
-                    std::sort(ks.begin() + b0, ks.begin() + b1,
-                              [&](int a, int b) { return y32(a) != y32(b) ? y32(a) < y32(b) : a < b; });
-                    float zlo = 0.f, zhi = -1.f;   // empty group
-                    for (int t = b0; t < b1; t++) {
-                        const float z = (float)(lp[3 * ks[t] + 2] - cz);
-                        zlo = t == b0 ? z : std::min(zlo, z);
-                        zhi = t == b0 ? z : std::max(zhi, z);
-                    }
-                    ggrp_z.push_back(make_float2(zlo, zhi));
-                    // bin edge j at -ymax + j * bw: the first carbon at or above it
-                    int t = b0;
-                    for (int j = 0; j < GBIN; j++) {
-                        const double edge = -(double)r.gymax + j * ((double)r.gymax * 2.0 / GBIN);
-                        while (t < b1 && (double)y32(ks[t]) < edge) t++;
-                        gbin.push_back(base + (j ? t : b0));
-                    }
-                    gbin.push_back(base + b1);
-                }
-                for (int k : ks) {
-                    double dx = lp[3 * k] - cx, dy = lp[3 * k + 1] - cy;
-                    gpos.push_back(make_double4(lp[3 * k], lp[3 * k + 1], lp[3 * k + 2], 0.0));
-                    gpos32.push_back(make_float4((float)dx, (float)dy, (float)(lp[3 * k + 2] - cz), 0.f));
-                }
-                gstart.push_back((int)gpos.size());
             }
+            std::vector<int> ks(lp.size() / 3);
+            for (size_t i = 0; i < ks.size(); i++) ks[i] = (int)i;
+            // groups: the column's carbons by z (a graphite layer each, at
+            // most GGRP groups of neighbouring z), each group in order of
+            // its FP32 y with GBIN uniform y bins over [-ymax, ymax], so a
+            // site visits only the groups and the y window within rc
+            std::sort(ks.begin(), ks.end(), [&](int a, int b) {
+                return lp[3 * a + 2] != lp[3 * b + 2] ? lp[3 * a + 2] < lp[3 * b + 2] : a < b;
+            });
+            std::vector<int> bounds(1, 0);
+            for (size_t t = 1; t < ks.size(); t++)
+                if (lp[3 * ks[t] + 2] != lp[3 * ks[t - 1] + 2]) bounds.push_back((int)t);
+            bounds.push_back((int)ks.size());
+            const int nz = (int)bounds.size() - 1;
+            std::vector<int> gb(1, 0);   // group bounds: every z level, or GGRP equal runs of them
+            for (int l = 1; l <= GGRP; l++)
+                gb.push_back(bounds[nz <= GGRP ? (l <= nz ? l : nz) : (int)((long long)nz * l / GGRP)]);
+            auto y32 = [&](int k) { return (float)(lp[3 * k + 1] - cy); };
+            for (int l = 0; l < GGRP; l++) {
+                const int b0 = gb[l], b1 = gb[l + 1];
+                std::sort(ks.begin() + b0, ks.begin() + b1,
+                          [&](int a, int b) { return y32(a) != y32(b) ? y32(a) < y32(b) : a < b; });
+                float zlo = 0.f, zhi = -1.f;   // empty group
+                for (int t = b0; t < b1; t++) {
+                    const float z = (float)(lp[3 * ks[t] + 2] - cz);
+                    zlo = t == b0 ? z : std::min(zlo, z);
+                    zhi = t == b0 ? z : std::max(zhi, z);
+                }
+                co.ggrp_z.push_back(make_float2(zlo, zhi));
+                // bin edge j at -ymax + j * bw: the first carbon at or above it
+                int t = b0;
+                for (int j = 0; j < GBIN; j++) {
+                    const double edge = -(double)r.gymax + j * ((double)r.gymax * 2.0 / GBIN);
+                    while (t < b1 && (double)y32(ks[t]) < edge) t++;
+                    co.gbin.push_back(j ? t : b0);
+                }
+                co.gbin.push_back(b1);
+            }
+            for (int k : ks) {
+                double dx = lp[3 * k] - cx, dy = lp[3 * k + 1] - cy;
+                co.gpos.push_back(make_double4(lp[3 * k], lp[3 * k + 1], lp[3 * k + 2], 0.0));
+                co.gpos32.push_back(make_float4((float)dx, (float)dy, (float)(lp[3 * k + 2] - cz), 0.f));
+            }
+        };
+        {
+            const int nth = std::max(1, std::min({(int)std::thread::hardware_concurrency(), 32, ncol_r / 16}));
+            std::atomic<int> next{0};
+            auto worker = [&]() {
+                for (int col; (col = next.fetch_add(1)) < ncol_r;) build_col(col);
+            };
+            std::vector<std::thread> pool;
+            for (int t = 1; t < nth; t++) pool.emplace_back(worker);
+            worker();
+            for (auto &th : pool) th.join();
+        }
+        for (int col = 0; col < ncol_r; col++) {
+            const ColOut &co = cols[col];
+            const int base = (int)gpos.size();
+            for (int v : co.gbin) gbin.push_back(base + v);
+            ggrp_z.insert(ggrp_z.end(), co.ggrp_z.begin(), co.ggrp_z.end());
+            gpos.insert(gpos.end(), co.gpos.begin(), co.gpos.end());
+            gpos32.insert(gpos32.end(), co.gpos32.begin(), co.gpos32.end());
+            gstart.push_back((int)gpos.size());
+        }
     }
     if ((e = dalloc(c, &d.axis, axis.size())) || (e = dalloc(c, &d.rcen2, rcen2.size())) ||
         (e = dalloc(c, &d.gcol_start, gstart.size())) ||
@@ -1111,7 +1141,12 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         // in H, so one pass over the box's sources takes every image)
         std::vector<double2> hp(NHARM, make_double2(0.0, 0.0));
         if (per) {
-            std::map<std::tuple<int, int, int>, std::vector<double2>> cache;
+            // H of an L2 offset depends only on its integers: kept for the
+            // life of the process (contexts formed again and again, as the
+            // request server does, compute each offset once)
+            static std::map<std::tuple<int, int, int>, std::vector<double2>> cache;
+            static std::mutex cache_mu;
+            std::lock_guard<std::mutex> cache_lock(cache_mu);
             hp.clear();
             for (int q = 0; q < R; q++) {
                 Rep &r = c->reps[q];
