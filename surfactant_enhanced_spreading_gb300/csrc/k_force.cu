@@ -520,7 +520,7 @@ __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int 
         ir2[j] = ira * ira;
         ft[j] = (t[j].q * pj.w) * ira * ir2[j];
     }
-    if (tj != 1) {   // water H carries no LJ
+    {   // (a water H in the prefix, only in an overflowing cell, has zero LJ table entries)
         bool n[K], any = false;
 #pragma unroll
         for (int j = 0; j < K; j++) { n[j] = r2[j] <= rc2; any = any || n[j]; }
@@ -549,6 +549,80 @@ __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int
     }
 }
 
+// Two targets per lane in Blackwell's paired FP32 arithmetic (fma / add /
+// mul .rn.f32x2: one instruction for both targets; the reciprocal square
+// root stays one MUFU each).  The pair field is issue-bound, so half the
+// FP32 instructions of the two-target items is most of its gain; each
+// element rounds as the scalar form, only the contraction pattern differs.
+// Water-H partners, no exclusion test, plain sums:
+__device__ __forceinline__ void coul_h_x2(const Tgt32 (&u)[2], const float4 *wpos, int n, float (&f)[2][3]) {
+    const float2 tx = make_float2(u[0].x, u[1].x), ty = make_float2(u[0].y, u[1].y), tz = make_float2(u[0].z, u[1].z);
+    const float2 tq = make_float2(u[0].q, u[1].q);
+    float2 fx = make_float2(f[0][0], f[1][0]), fy = make_float2(f[0][1], f[1][1]), fz = make_float2(f[0][2], f[1][2]);
+#pragma unroll 2
+    for (int k = 0; k < n; k++) {
+        const float4 p = wpos[k];
+        const float2 dx = __fadd2_rn(tx, make_float2(-p.x, -p.x));
+        const float2 dy = __fadd2_rn(ty, make_float2(-p.y, -p.y));
+        const float2 dz = __fadd2_rn(tz, make_float2(-p.z, -p.z));
+        const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+        const float2 ira = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+        const float2 ft = __fmul2_rn(__fmul2_rn(tq, ira), __fmul2_rn(ira, ira));
+        fx = __ffma2_rn(dx, ft, fx); fy = __ffma2_rn(dy, ft, fy); fz = __ffma2_rn(dz, ft, fz);
+    }
+    f[0][0] = fx.x; f[1][0] = fx.y; f[0][1] = fy.x; f[1][1] = fy.y; f[0][2] = fz.x; f[1][2] = fz.y;
+}
+// the LJ-carrying prefix with both targets of a lane in f32x2 arithmetic
+// (same-molecule test per target; LJ only when some lane has a target within rc)
+__device__ __forceinline__ void lj_x2(const Tgt32 (&u)[2], const float4 *wpos, const int *wkey, int n, const float2 *ljt,
+                                      float rc2, float (&f)[2][3]) {
+    const float2 tx = make_float2(u[0].x, u[1].x), ty = make_float2(u[0].y, u[1].y), tz = make_float2(u[0].z, u[1].z);
+    const float2 tq = make_float2(u[0].q, u[1].q);
+    float2 fx = make_float2(f[0][0], f[1][0]), fy = make_float2(f[0][1], f[1][1]), fz = make_float2(f[0][2], f[1][2]);
+#pragma unroll 2
+    for (int k = 0; k < n; k++) {
+        const float4 p = wpos[k];
+        const int key = wkey[k], mj = key >> 5, tj = key & 31;
+        const float2 dx = __fadd2_rn(tx, make_float2(-p.x, -p.x));
+        const float2 dy = __fadd2_rn(ty, make_float2(-p.y, -p.y));
+        const float2 dz = __fadd2_rn(tz, make_float2(-p.z, -p.z));
+        const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+        const float2 ira = make_float2(mj == u[0].m ? 0.f : rsqrt_ftz(r2.x), mj == u[1].m ? 0.f : rsqrt_ftz(r2.y));
+        const float2 ir2 = __fmul2_rn(ira, ira);
+        float2 ft = __fmul2_rn(__fmul2_rn(__fmul2_rn(tq, make_float2(p.w, p.w)), ira), ir2);
+        const bool n0 = r2.x <= rc2, n1 = r2.y <= rc2;
+        if (__any_sync(0xffffffffu, n0 || n1)) {
+            const float2 v0 = ljt[u[0].trow + tj], v1 = ljt[u[1].trow + tj];
+            const float2 r6 = __fmul2_rn(__fmul2_rn(ir2, ir2), ir2);
+            const float2 on = make_float2(n0 ? v0.x : 0.f, n1 ? v1.x : 0.f);
+            const float2 w = __ffma2_rn(make_float2(v0.y, v1.y), r6, make_float2(-0.5f, -0.5f));
+            ft = __ffma2_rn(__fmul2_rn(__fmul2_rn(on, r6), w), ir2, ft);
+        }
+        fx = __ffma2_rn(dx, ft, fx); fy = __ffma2_rn(dy, ft, fy); fz = __ffma2_rn(dz, ft, fz);
+    }
+    f[0][0] = fx.x; f[1][0] = fx.y; f[0][1] = fy.x; f[1][1] = fy.y; f[0][2] = fz.x; f[1][2] = fz.y;
+}
+// water-H partners with the same-molecule test, f32x2
+__device__ __forceinline__ void coul_h_x2_excl(const Tgt32 (&u)[2], const float4 *wpos, const int *wkey, int n,
+                                               float (&f)[2][3]) {
+    const float2 tx = make_float2(u[0].x, u[1].x), ty = make_float2(u[0].y, u[1].y), tz = make_float2(u[0].z, u[1].z);
+    const float2 tq = make_float2(u[0].q, u[1].q);
+    float2 fx = make_float2(f[0][0], f[1][0]), fy = make_float2(f[0][1], f[1][1]), fz = make_float2(f[0][2], f[1][2]);
+#pragma unroll 1
+    for (int k = 0; k < n; k++) {
+        const float4 p = wpos[k];
+        const int mj = wkey[k] >> 5;
+        const float2 dx = __fadd2_rn(tx, make_float2(-p.x, -p.x));
+        const float2 dy = __fadd2_rn(ty, make_float2(-p.y, -p.y));
+        const float2 dz = __fadd2_rn(tz, make_float2(-p.z, -p.z));
+        const float2 r2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+        const float2 ira = make_float2(mj == u[0].m ? 0.f : rsqrt_ftz(r2.x), mj == u[1].m ? 0.f : rsqrt_ftz(r2.y));
+        const float2 ft = __fmul2_rn(__fmul2_rn(tq, ira), __fmul2_rn(ira, ira));
+        fx = __ffma2_rn(dx, ft, fx); fy = __ffma2_rn(dy, ft, fy); fz = __ffma2_rn(dz, ft, fz);
+    }
+    f[0][0] = fx.x; f[1][0] = fx.y; f[0][1] = fy.x; f[1][1] = fy.y; f[0][2] = fz.x; f[1][2] = fz.y;
+}
+
 // One partner cell's sites (slots t0..t1, LJ-carrying ones before th) on
 // the targets u, in the partner cell's frame.  The LJ-carrying prefix always
 // tests for partners of a target's own molecule; the water-H suffix (about
@@ -559,6 +633,7 @@ __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int
 // stages 32 partners at a time in its shared-memory slot (one coalesced
 // load per lane) and reads them back as broadcasts: shorter load latency
 // than a broadcast L1 load per partner.
+// Two-target items of the plain mixed path take the paired forms above.
 template <int K, bool EXCL, bool COMP>
 __device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, const int *__restrict__ keys,
                                             Tgt32 (&u)[K], int t0, int th, int t1, const float2 *ljt, float rc2,
@@ -568,8 +643,12 @@ __device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, co
         __syncwarp();
         if (lane < n) { wpos[lane] = pos32[b0 + lane]; wkey[lane] = keys[b0 + lane]; }
         __syncwarp();
+        if constexpr (K == 2 && !COMP) {
+            lj_x2(u, wpos, wkey, n, ljt, rc2, f.f);
+        } else {
 #pragma unroll 2
-        for (int k = 0; k < n; k++) pairk_acc32<K, true, COMP>(u, wpos[k], wkey[k], ljt, rc2, f);
+            for (int k = 0; k < n; k++) pairk_acc32<K, true, COMP>(u, wpos[k], wkey[k], ljt, rc2, f);
+        }
     }
     if (th < t1) {
         const float qh = pos32[th].w;
@@ -582,8 +661,12 @@ __device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, co
             __syncwarp();
             if (lane < n) { wpos[lane] = pos32[b0 + lane]; wkey[lane] = keys[b0 + lane]; }
             __syncwarp();
+            if constexpr (K == 2 && !COMP) {
+                coul_h_x2_excl(u, wpos, wkey, n, f.f);
+            } else {
 #pragma unroll 1
-            for (int k = 0; k < n; k++) pairk_coul32<K, true, COMP>(u, wpos[k], wkey[k] >> 5, f);
+                for (int k = 0; k < n; k++) pairk_coul32<K, true, COMP>(u, wpos[k], wkey[k] >> 5, f);
+            }
         }
     } else {
         for (int b0 = th; b0 < t1; b0 += 32) {
@@ -591,8 +674,12 @@ __device__ __forceinline__ void near_cell32(const float4 *__restrict__ pos32, co
             __syncwarp();
             if (lane < n) wpos[lane] = pos32[b0 + lane];
             __syncwarp();
+            if constexpr (K == 2 && !COMP) {
+                coul_h_x2(u, wpos, n, f.f);
+            } else {
 #pragma unroll 2
-            for (int k = 0; k < n; k++) pairk_coul32<K, false, COMP>(u, wpos[k], 0, f);
+                for (int k = 0; k < n; k++) pairk_coul32<K, false, COMP>(u, wpos[k], 0, f);
+            }
         }
     }
 }
@@ -713,8 +800,10 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 // in FP32 over one row (at most 3 cells).
 // PER: the periodic preset's instantiation (rows wrap around x and y)
 // COMP: compensated (Kahan) FP32 sums per target (SESP_MIXED_COMP)
+// (the FP32 two-target instantiation is held to 8 CTAs per SM, 64 registers:
+// the paired loops want 67, and 7 CTAs per SM ran slower)
 template <bool MIXED, int KMAX, bool PER, bool COMP = false>
-__global__ void __launch_bounds__(NEAR_THREADS) k_near(Dev d, int nslot, int tile) {
+__global__ void __launch_bounds__(NEAR_THREADS, (MIXED && !COMP && KMAX == 2) ? 8 : 1) k_near(Dev d, int nslot, int tile) {
     griddep_wait();
     __shared__ float2 s_lj32[MIXED ? NTYPE * NTYPE : 1];
     __shared__ float4 s_stage[MIXED ? NEAR_THREADS / 32 : 1][32];
