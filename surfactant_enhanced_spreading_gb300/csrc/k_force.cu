@@ -473,7 +473,7 @@ struct Acc32 {
         for (int j = 0; j < K; j++) f[j][0] = f[j][1] = f[j][2] = 0.f;
     }
     __device__ __forceinline__ void add(int j, float dx, float dy, float dz, float ft) {
-        f[j][0] += dx * ft; f[j][1] += dy * ft; f[j][2] += dz * ft;
+        f[j][0] = __fmaf_rn(dx, ft, f[j][0]); f[j][1] = __fmaf_rn(dy, ft, f[j][1]); f[j][2] = __fmaf_rn(dz, ft, f[j][2]);
     }
     __device__ __forceinline__ float get(int j, int a) const { return f[j][a]; }
 };
@@ -514,11 +514,11 @@ __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int 
     float dx[K], dy[K], dz[K], r2[K], ir2[K], ft[K];
 #pragma unroll
     for (int j = 0; j < K; j++) {
-        dx[j] = t[j].x - pj.x; dy[j] = t[j].y - pj.y; dz[j] = t[j].z - pj.z;
-        r2[j] = dx[j] * dx[j] + dy[j] * dy[j] + dz[j] * dz[j];
+        dx[j] = __fsub_rn(t[j].x, pj.x); dy[j] = __fsub_rn(t[j].y, pj.y); dz[j] = __fsub_rn(t[j].z, pj.z);
+        r2[j] = __fmaf_rn(dz[j], dz[j], __fmaf_rn(dy[j], dy[j], __fmul_rn(dx[j], dx[j])));
         const float ira = EXCL && mj == t[j].m ? 0.f : rsqrt_ftz(r2[j]);
-        ir2[j] = ira * ira;
-        ft[j] = (t[j].q * pj.w) * ira * ir2[j];
+        ir2[j] = __fmul_rn(ira, ira);
+        ft[j] = __fmul_rn(__fmul_rn(__fmul_rn(t[j].q, pj.w), ira), ir2[j]);
     }
     {   // (a water H in the prefix, only in an overflowing cell, has zero LJ table entries)
         bool n[K], any = false;
@@ -528,8 +528,9 @@ __device__ __forceinline__ void pairk_acc32(const Tgt32 (&t)[K], float4 pj, int 
 #pragma unroll
             for (int j = 0; j < K; j++) {
                 const float2 v = ljt[t[j].trow + tj];
-                const float r6 = ir2[j] * ir2[j] * ir2[j];   // zero for an excluded partner
-                ft[j] += (n[j] ? v.x : 0.f) * r6 * (v.y * r6 - 0.5f) * ir2[j];
+                const float r6 = __fmul_rn(__fmul_rn(ir2[j], ir2[j]), ir2[j]);   // zero for an excluded partner
+                const float w = __fmaf_rn(v.y, r6, -0.5f);
+                ft[j] = __fmaf_rn(__fmul_rn(__fmul_rn(n[j] ? v.x : 0.f, r6), w), ir2[j], ft[j]);
             }
         }
     }
@@ -541,10 +542,10 @@ template <int K, bool EXCL, bool COMP>
 __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int mj, Acc32<K, COMP> &f) {
 #pragma unroll
     for (int j = 0; j < K; j++) {
-        const float dx = t[j].x - pj.x, dy = t[j].y - pj.y, dz = t[j].z - pj.z;
-        const float r2 = dx * dx + dy * dy + dz * dz;
+        const float dx = __fsub_rn(t[j].x, pj.x), dy = __fsub_rn(t[j].y, pj.y), dz = __fsub_rn(t[j].z, pj.z);
+        const float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
         const float ira = EXCL && mj == t[j].m ? 0.f : rsqrt_ftz(r2);
-        const float ft = t[j].q * ira * (ira * ira);
+        const float ft = __fmul_rn(__fmul_rn(t[j].q, ira), __fmul_rn(ira, ira));
         f.add(j, dx, dy, dz, ft);
     }
 }
@@ -552,8 +553,11 @@ __device__ __forceinline__ void pairk_coul32(const Tgt32 (&t)[K], float4 pj, int
 // Two targets per lane in Blackwell's paired FP32 arithmetic (fma / add /
 // mul .rn.f32x2: one instruction for both targets; the reciprocal square
 // root stays one MUFU each).  The pair field is issue-bound, so half the
-// FP32 instructions of the two-target items is most of its gain; each
-// element rounds as the scalar form, only the contraction pattern differs.
+// FP32 instructions of the two-target items is most of its gain.  The
+// scalar forms above spell out the same roundings in the same order
+// (explicit __fmaf_rn / __fmul_rn / __fsub_rn, so the compiler contracts
+// nothing of its own): a target's force does not depend on whether its item
+// took one, two or four targets per lane, i.e. on the launch shape.
 // Water-H partners, no exclusion test, plain sums:
 __device__ __forceinline__ void coul_h_x2(const Tgt32 (&u)[2], const float4 *wpos, int n, float (&f)[2][3]) {
     const float2 tx = make_float2(u[0].x, u[1].x), ty = make_float2(u[0].y, u[1].y), tz = make_float2(u[0].z, u[1].z);
@@ -800,10 +804,11 @@ __device__ __forceinline__ void pair2_acc64(const Tgt64 &a, const Tgt64 &b, bool
 // in FP32 over one row (at most 3 cells).
 // PER: the periodic preset's instantiation (rows wrap around x and y)
 // COMP: compensated (Kahan) FP32 sums per target (SESP_MIXED_COMP)
-// (the FP32 two-target instantiation is held to 8 CTAs per SM, 64 registers:
-// the paired loops want 67, and 7 CTAs per SM ran slower)
+// (the FP32 two-target instantiations are held to 8 CTAs per SM, 64
+// registers: the paired loops want 67 and the compensated ones 80, and
+// fewer CTAs per SM ran slower)
 template <bool MIXED, int KMAX, bool PER, bool COMP = false>
-__global__ void __launch_bounds__(NEAR_THREADS, (MIXED && !COMP && KMAX == 2) ? 8 : 1) k_near(Dev d, int nslot, int tile) {
+__global__ void __launch_bounds__(NEAR_THREADS, (MIXED && KMAX == 2) ? 8 : 1) k_near(Dev d, int nslot, int tile) {
     griddep_wait();
     __shared__ float2 s_lj32[MIXED ? NTYPE * NTYPE : 1];
     __shared__ float4 s_stage[MIXED ? NEAR_THREADS / 32 : 1][32];
