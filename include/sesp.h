@@ -200,8 +200,8 @@ int sesp_run_timed(sesp_ctx *ctx, int kb0, int nsteps, int flush_l2, double *ste
 int sesp_pair_counts(sesp_ctx *ctx, int64_t out[2]);
 /* src/compute_temperature.f90:240-242: sum m v^2 / dt^2 / dof over every
  * replica, dof = 3 sites - constraints; an FP64 reduction on the device in
- * a fixed order (one block per replica), then one double per replica to the
- * host (the reference reduces per rank and adds with an allreduce,
+ * a fixed order (64 slices per replica, then their sum), then one double per
+ * replica to the host (the reference reduces per rank and adds with an allreduce,
  * src/compute_temperature.f90:239-242) */
 int sesp_temperature(sesp_ctx *ctx, double *t);
 int sesp_get_eta(sesp_ctx *ctx, double *eta);

@@ -2237,11 +2237,18 @@ void launch_count_pairs(const Dev &d, int ncell, unsigned long long *out, cudaSt
 // per replica, thread-strided partial sums and a fixed tree, so the result
 // does not depend on timing
 constexpr int TEMP_THREADS = 256;
-__global__ void __launch_bounds__(TEMP_THREADS) k_temperature(Dev d) {
+// sum of m v^2 per replica in a fixed order: TEMP_SLICES blocks per replica
+// each sum one fixed slice of its sites (a tree in shared memory), then one
+// block per replica adds the slices as a tree; the slices depend only on the
+// replica's site count
+__global__ void __launch_bounds__(TEMP_THREADS) k_temperature(Dev d, int nrep) {
     __shared__ double sh[TEMP_THREADS];
-    const Rep r = d.rep[blockIdx.x];
+    const int q = blockIdx.x / TEMP_SLICES, b = blockIdx.x % TEMP_SLICES;
+    const Rep r = d.rep[q];
+    const int per = (r.nsite + TEMP_SLICES - 1) / TEMP_SLICES;
+    const int g0 = r.site0 + b * per, g1 = min(r.site0 + r.nsite, g0 + per);
     double a = 0.0;
-    for (int g = r.site0 + threadIdx.x; g < r.site0 + r.nsite; g += TEMP_THREADS)
+    for (int g = g0 + threadIdx.x; g < g1; g += TEMP_THREADS)
         a += d.tmass[d.ptype[g]] * (d.vx[g] * d.vx[g] + d.vy[g] * d.vy[g] + d.vz[g] * d.vz[g]);
     sh[threadIdx.x] = a;
     __syncthreads();
@@ -2249,10 +2256,23 @@ __global__ void __launch_bounds__(TEMP_THREADS) k_temperature(Dev d) {
         if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
         __syncthreads();
     }
+    if (threadIdx.x == 0) d.tbuf[nrep + blockIdx.x] = sh[0];
+}
+__global__ void __launch_bounds__(TEMP_SLICES) k_temperature_sum(Dev d, int nrep) {
+    __shared__ double sh[TEMP_SLICES];
+    sh[threadIdx.x] = d.tbuf[nrep + blockIdx.x * TEMP_SLICES + threadIdx.x];
+    __syncthreads();
+    for (int w = TEMP_SLICES / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
     if (threadIdx.x == 0) d.tbuf[blockIdx.x] = sh[0];
 }
 
-void launch_temperature(const Dev &d, int nrep, cudaStream_t st) { k_temperature<<<nrep, TEMP_THREADS, 0, st>>>(d); }
+void launch_temperature(const Dev &d, int nrep, cudaStream_t st) {
+    k_temperature<<<nrep * TEMP_SLICES, TEMP_THREADS, 0, st>>>(d, nrep);
+    k_temperature_sum<<<nrep, TEMP_SLICES, 0, st>>>(d, nrep);
+}
 
 // FP32 FMA throughput: every thread runs 8 independent chains of `iters`
 // fused multiply-adds (enough to cover the pipe's latency), and writes one

@@ -79,7 +79,9 @@ void launch_flush(void *buf, size_t bytes, cudaStream_t st);
 double measure_fp32_peak(int n_sm, cudaStream_t st);
 void launch_energies(const Dev &d, int ncell, int nsite, const int *smols, int ns, int chains, double *e_slot,
                      double *e_site, double *e_mol, cudaStream_t st);
-// per-replica sums of m v^2 in a fixed order (one block per replica) into d.tbuf
+// per-replica sums of m v^2 in a fixed order (TEMP_SLICES slices per replica,
+// then their tree sum) into d.tbuf[0..nrep); the slices go to d.tbuf[nrep..)
+constexpr int TEMP_SLICES = 64;
 void launch_temperature(const Dev &d, int nrep, cudaStream_t st);
 
 }  // namespace sesp

@@ -844,7 +844,7 @@ int upload_impl(sesp_ctx *c, const std::vector<RepIn> &in) {
         (e = dalloc(c, &d.wsw_b, M)) || (e = dalloc(c, &d.cctl, 8)) || (e = dalloc(c, &d.wsort_off, 256)) ||
         (e = dalloc(c, &d.eta_part, 64 * (size_t)R)) || (e = dalloc(c, &d.eta_ctl, R)) ||
         (e = dalloc(c, &d.cnh, C)) || (e = dalloc(c, &d.tq, NTYPE)) || (e = dalloc(c, &d.tmass, NTYPE)) ||
-        (e = dalloc(c, &d.tgr, NTYPE)) || (e = dalloc(c, &d.simg, N)) || (e = dalloc(c, &d.tbuf, R)))
+        (e = dalloc(c, &d.tgr, NTYPE)) || (e = dalloc(c, &d.simg, N)) || (e = dalloc(c, &d.tbuf, (size_t)R * (1 + TEMP_SLICES))))
         return e;
     const int w2x = 2 * d2.x + 1, w2y = 2 * d2.y + 1, w2z = 2 * d2.z + 1;
     const size_t nh2 = (size_t)w2x * w2y * w2z * NHARM;

@@ -224,7 +224,7 @@ struct Dev {
     double *tq, *tmass;
     double2 *tgr;
     short2 *simg;        // per site: x / y image of the last rebuild (periodic preset)
-    double *tbuf;        // [nrep] temperature sums
+    double *tbuf;        // [nrep] temperature sums, then [nrep][TEMP_SLICES] slice sums
     // counters: [0] fails, [1] overflow, [2] unlocated, [3] max cell, [5] pairs, [6] LJ pairs
     unsigned long long *counters;
     int max_cell;
