@@ -415,7 +415,9 @@ constexpr int WMAT_FP32_STEPS = 8;
 __device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int maxit) {
     const int g0 = d.mfirst[m];
     const double escale = __dsub_rn(1.0, __dmul_rn(d.eta[d.mrep[m]], DT) * 0.5);
-    double r[3][3], p[3][3], v[3][3];
+    // (the velocity predictor is formed again at the end from the state, so
+    // it holds no registers through the iterations)
+    double r[3][3], p[3][3];
     double ke0 = 0.0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
@@ -427,9 +429,6 @@ __device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int 
         p[i][0] = pred_a(r[i][0], vx, ax, escale);
         p[i][1] = pred_a(r[i][1], vy, ay, escale);
         p[i][2] = pred_a(r[i][2], vz, az, escale);
-        v[i][0] = vel_a(vx, ax, escale);
-        v[i][1] = vel_a(vy, ay, escale);
-        v[i][2] = vel_a(vz, az, escale);
     }
     double R[3][3], P[3][3], D0[3], thr[3];
 #pragma unroll
@@ -512,8 +511,10 @@ __device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int 
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const int g = g0 + i;
+        const double v0 = vel_a(d.vx[g], d.ax[g], escale), v1 = vel_a(d.vy[g], d.ay[g], escale),
+                     v2 = vel_a(d.vz[g], d.az[g], escale);
         d.x[g] = p[i][0] + cc[i][0]; d.y[g] = p[i][1] + cc[i][1]; d.z[g] = p[i][2] + cc[i][2];
-        const double vx = v[i][0] + cc[i][0], vy = v[i][1] + cc[i][1], vz = v[i][2] + cc[i][2];
+        const double vx = v0 + cc[i][0], vy = v1 + cc[i][1], vz = v2 + cc[i][2];
         d.vx[g] = vx; d.vy[g] = vy; d.vz[g] = vz;
         ke1 = __dadd_rn(ke1, __dmul_rn(cF.mass64[wkind(i)],
                                        __dadd_rn(__dadd_rn(__dmul_rn(vx, vx), __dmul_rn(vy, vy)), __dmul_rn(vz, vz))));
@@ -1040,6 +1041,39 @@ __global__ void __launch_bounds__(CW_THREADS) k_constrain(Dev d, CPlan p, double
     }
 }
 
+// Configuration preset, mixed path: its chains carry no constraints, so the
+// half is the water queue of k_constrain alone (matrix form), in a kernel
+// without the surfactant wavefront's registers and shared memory: several
+// CTAs per SM instead of one, to hide the FP64 latency of the per-water
+// chains.  Same queue, same per-water arithmetic, same counter reset.
+template <bool SHAKE>
+__global__ void __launch_bounds__(CW_THREADS) k_water_mat(Dev d, CPlan p, double tol, int maxit) {
+    griddep_wait();
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned item = 0;
+        if (lane == 0) item = atomicAdd(&p.ctl[1], 1u);
+        item = __shfl_sync(FULL, item, 0);
+        const long long t0 = 32LL * item;
+        if (t0 >= p.nw) break;
+        const int t = (int)t0 + lane;
+        if (t < p.nw) {
+            const int m = p.wlist[t];
+            if (!mol_ok(d, p, m, 3)) {
+                atomicAdd(&d.counters[7], 1ull);
+                continue;
+            }
+            const int sweeps = SHAKE ? water_a_mat(d, m, tol, maxit) : water_b_mat(d, m, tol, maxit);
+            p.wsw[m] = (uint8_t)(sweeps < 255 ? sweeps : 255);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&p.ctl[2], 1u) == gridDim.x - 1) { p.ctl[0] = 0u; p.ctl[1] = 0u; p.ctl[2] = 0u; }
+    }
+}
+
 // ---------------------------------------------------------------- water order
 
 // Counting sort of the water list by the sweeps of the last call, most
@@ -1128,6 +1162,8 @@ int constraint_max_surf_warps() { return MAX_SURF_WARPS; }
 int constraint_max_mols_per_warp(int fp32) { return fp32 ? wavefront_mols<float>() : wavefront_mols<double>(); }
 
 namespace {
+int g_water_mat_ctas[2] = {0, 0};   // CTAs per SM of k_water_mat<RATTLE / SHAKE> (set once)
+
 template <typename C, bool SHAKE>
 constexpr size_t surf_smem(int s_warps, int mpw) {
     return (size_t)s_warps * mpw * sizeof(MolSmem<C, SHAKE ? 16 : 11>);
@@ -1151,12 +1187,20 @@ void launch_constrain_t(const Dev &d, const int *smols, int ns, int nw, int nmol
     const int groups = (ns + p.mpw - 1) / p.mpw;
     const int need = (groups + p.s_warps - 1) / p.s_warps;
     p.n_scta = ns ? (need < sh.grid ? need : sh.grid) : 0;
+    if (std::is_same<C, double>::value && mat && ns == 0) {
+        // waters only, in matrix form: as many CTAs per SM as fit
+        const int occ = g_water_mat_ctas[SHAKE ? 1 : 0] > 0 ? g_water_mat_ctas[SHAKE ? 1 : 0] : 1;
+        launch_pdl(k_water_mat<SHAKE>, dim3(sh.grid * occ), dim3(CW_THREADS), 0, st, d, p, tol, maxit);
+        return;
+    }
     const size_t smem = p.n_scta ? surf_smem<C, SHAKE>(p.s_warps, p.mpw) : 0;
     launch_pdl(k_constrain<C, SHAKE>, dim3(sh.grid), dim3(CW_THREADS), smem, st, d, p, tol, maxit);
 }
 }  // namespace
 
 void init_constraint_kernels() {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_water_mat_ctas[0], k_water_mat<false>, CW_THREADS, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_water_mat_ctas[1], k_water_mat<true>, CW_THREADS, 0);
     cudaFuncSetAttribute(k_constrain<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)surf_smem<double, true>(MAX_SURF_WARPS, MPW));
     cudaFuncSetAttribute(k_constrain<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,

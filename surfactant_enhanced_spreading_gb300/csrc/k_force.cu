@@ -1303,6 +1303,25 @@ __device__ __forceinline__ void m2c_row(const double *op, double va, double vb, 
     }
 }
 
+// FP32 rows in Blackwell's paired arithmetic: the operator row's outputs
+// (o, o + 1) against one target's input, one fma.rn.f32x2 for both outputs
+// (each element rounds as a scalar FMA, so the sums are the scalar ones)
+constexpr int M2C_P = (LP + 1) / 2;   // output pairs (the last one padded)
+__device__ __forceinline__ void m2c_row2(const float *op, float va, float vb, float2 (&aa)[M2C_P], float2 (&ab)[M2C_P]) {
+    const float2 a2 = make_float2(va, va), b2 = make_float2(vb, vb);
+#pragma unroll
+    for (int o4 = 0; o4 < (2 * M2C_P + 3) / 4; o4++) {
+        const float4 w = *(const float4 *)(op + 4 * o4);
+        const float2 w0 = make_float2(w.x, w.y), w1 = make_float2(w.z, w.w);
+        aa[2 * o4] = __ffma2_rn(w0, a2, aa[2 * o4]);
+        ab[2 * o4] = __ffma2_rn(w0, b2, ab[2 * o4]);
+        if (2 * o4 + 1 < M2C_P) {
+            aa[2 * o4 + 1] = __ffma2_rn(w1, a2, aa[2 * o4 + 1]);
+            ab[2 * o4 + 1] = __ffma2_rn(w1, b2, ab[2 * o4 + 1]);
+        }
+    }
+}
+
 template <typename R>
 __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d) {
     griddep_wait();
@@ -1339,6 +1358,9 @@ __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d) {
     R aa[LP], ab[LP];
 #pragma unroll
     for (int i = 0; i < LP; i++) aa[i] = ab[i] = R(0);
+    float2 pa[M2C_P], pb[M2C_P];   // FP32: the sums in output pairs
+#pragma unroll
+    for (int i = 0; i < M2C_P; i++) pa[i] = pb[i] = make_float2(0.f, 0.f);
     for (int c0 = k0; c0 < k1; c0 += M2C_CH) {
         const int nch = min(M2C_CH, k1 - c0);
         __syncthreads();
@@ -1350,8 +1372,21 @@ __global__ void __launch_bounds__(32 * M2C_W) k_m2l_cls(Dev d) {
         for (int kk = 0; kk < nch; kk++) {
             const R *src = src_of(c0 + kk);
             const R *op = sop + kk * LP * M2C_LD;
+            if constexpr (std::is_same<R, float>::value) {
 #pragma unroll
-            for (int i = 0; i < LP; i++) m2c_row(op + i * M2C_LD, src[(size_t)i * vol + ia], src[(size_t)i * vol + ib], aa, ab);
+                for (int i = 0; i < LP; i++)
+                    m2c_row2(op + i * M2C_LD, src[(size_t)i * vol + ia], src[(size_t)i * vol + ib], pa, pb);
+            } else {
+#pragma unroll
+                for (int i = 0; i < LP; i++) m2c_row(op + i * M2C_LD, src[(size_t)i * vol + ia], src[(size_t)i * vol + ib], aa, ab);
+            }
+        }
+    }
+    if constexpr (std::is_same<R, float>::value) {
+#pragma unroll
+        for (int i = 0; i < LP; i++) {
+            aa[i] = (i & 1) ? pa[i >> 1].y : pa[i >> 1].x;
+            ab[i] = (i & 1) ? pb[i >> 1].y : pb[i >> 1].x;
         }
     }
     R *part = (R *)(level == 4 ? d.part4 : d.part3);
