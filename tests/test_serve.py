@@ -156,3 +156,113 @@ def test_server_stops_a_blown_up_run(monkeypatch):
     res = serve.Server(1 << 40, chunk=100, keep_state=False).run(reqs)
     assert [r.failed for r in res] == [False, True]
     assert res[0].steps_done == -1 and res[1].steps_done == 100
+
+
+class _FakeBatch:
+    """Stands in for a batched engine context on the CPU: each chunk of n
+    steps adds n x 1e-3 to positions, n to velocities and accelerations and
+    n x 0.01 to eta, so a run's final state counts the steps it was given;
+    init_accel sets accelerations to 7 (a run carried into a new context
+    must keep its own).  A system with a `fail_per_step` attribute reports
+    that many SHAKE failures per step."""
+    formed = []
+
+    def __init__(self, systems, precision, device=0, **kw):
+        _FakeBatch.formed.append(len(systems))
+        self.systems = systems
+        self.offsets = np.cumsum([0] + [s.n_sites for s in systems])
+        self.pos = np.concatenate([s.pos for s in systems]).copy()
+        self.vel = np.concatenate([s.vel for s in systems]).copy()
+        self.acc = np.zeros_like(self.pos)
+        self.eta = np.zeros(len(systems))
+        self.fail = np.zeros(len(systems), dtype=np.int64)
+
+    def force(self, rebuild=True, terms=None):
+        return np.zeros_like(self.pos)
+
+    def init_accel(self):
+        self.acc[:] = 7.0
+
+    def state(self, out=None):
+        return self.pos.copy(), self.vel.copy(), self.acc.copy()
+
+    def set_state(self, pos=None, vel=None, acc=None, eta=0.0):
+        if acc is not None:
+            self.acc = np.array(acc, dtype=np.float64)
+        self.eta[:] = eta
+
+    def etas(self):
+        return self.eta.copy()
+
+    def set_etas(self, etas):
+        self.eta = np.array(etas, dtype=np.float64)
+
+    def failures(self):
+        return self.fail.copy()
+
+    def run_async(self, kb, n):
+        assert kb % 10 == 1 and n % 10 == 0   # chunks start just after a rebuild step
+        self.pos += n * 1e-3
+        self.vel += n
+        self.acc += n
+        self.eta += 0.01 * n
+        for q, s in enumerate(self.systems):
+            self.fail[q] += n * getattr(s, "fail_per_step", 0)
+
+    def sync(self):
+        pass
+
+    def close(self):
+        pass
+
+
+def _slot_requests():
+    sizes = [(300, 0, 300, 0.0), (400, 2, 200, 0.0), (300, 0, 500, 0.02), (500, 0, 100, 0.04)]
+    return [serve.make_request(k, nw, ns, st, seed=40 + k, arrival=t) for k, (nw, ns, st, t) in enumerate(sizes)]
+
+
+def test_slot_server_carries_each_run_through_reformed_contexts(monkeypatch):
+    monkeypatch.setattr(serve.E, "Engine", _FakeBatch)
+    _FakeBatch.formed = []
+    reqs = _slot_requests()
+    srv = serve.SlotServer(budget_bytes=1 << 40, chunk=100)
+    res = srv.run(reqs)
+    assert [r.rid for r in res] == [0, 1, 2, 3]
+    assert srv.reforms == len(_FakeBatch.formed) >= 3
+    for r, q in zip(res, reqs):
+        assert not r.failed and r.steps_done == -1
+        assert np.allclose(r.pos, q.system.pos + 1e-3 * q.steps)
+        assert np.allclose(r.vel, q.system.vel + q.steps)
+        assert abs(r.eta - 0.01 * q.steps) < 1e-9
+        assert 0 <= r.admitted and r.finished >= r.admitted
+    assert srv.peak_used <= srv.budget
+
+
+def test_slot_server_budget_and_failures(monkeypatch):
+    monkeypatch.setattr(serve.E, "Engine", _FakeBatch)
+    _FakeBatch.formed = []
+    reqs = _slot_requests()
+    reqs[2].system.fail_per_step = 3           # passes max_failures after its first chunk
+    biggest = max(serve.estimate_bytes(r.system) for r in reqs)
+    srv = serve.SlotServer(budget_bytes=int(1.5 * biggest), chunk=100, max_failures=100)
+    res = srv.run(reqs)
+    assert max(_FakeBatch.formed) == 1             # the budget holds one run at a time
+    assert srv.peak_used <= srv.budget
+    bad = res[2]
+    assert bad.failed and bad.steps_done == 100 and bad.shake_failures == 300
+    assert all(not r.failed for k, r in enumerate(res) if k != 2)
+
+
+def test_slot_server_refuses_bad_requests(monkeypatch):
+    monkeypatch.setattr(serve.E, "Engine", _FakeBatch)
+    r = serve.make_request(0, 300, 0, 105, seed=1)
+    with pytest.raises(ValueError, match="multiple"):
+        serve.SlotServer(budget_bytes=1 << 40).run([r])
+    with pytest.raises(ValueError, match="multiple of the rebuild interval"):
+        serve.SlotServer(budget_bytes=1 << 40, chunk=95)
+    a = serve.make_request(0, 300, 0, 100, seed=1)
+    b = serve.make_request(1, 300, 0, 100, seed=2, preset=1)
+    with pytest.raises(ValueError, match="preset"):
+        serve.SlotServer(budget_bytes=1 << 40).run([a, b])
+    with pytest.raises(E.SespError, match="EBUDGET"):
+        serve.SlotServer(budget_bytes=1024).run([a])
