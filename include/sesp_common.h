@@ -42,8 +42,9 @@
  * x (n_cells[2] / 4) domains, numbered d = ix + dx (iy + dy iz) like ibox2
  * (src/ibox.f90:128-139); the reference's 12 x 12 x 12 cells give its 27
  * ranks.  All domains' arrays are passed to this layer at once: one process
- * drives the one GPU.  An MPI driver gathers the ranks' central cells to
- * that process (INTEGRATION.md shows the gather).
+ * drives the one GPU.  An MPI driver keeps its per-rank COMMON and gathers
+ * the ranks' 64 central columns of each array, and the counts, to that
+ * process (one mpi_gatherv per array), scattering them back after each call.
  *
  * Engine molecule order set by sesp_cmn_attach: waters first, by domain,
  * then central cell (ix + 4 iy + 16 iz), then w1 before w2, then slot; then
