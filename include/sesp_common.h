@@ -116,7 +116,8 @@ typedef struct sesp_cmn_map sesp_cmn_map;
 int sesp_cmn_domain_count(const int n_cells[3], int *ndom);
 /* A map whose molecules are the ones in the domains' central cells, in the
  * engine order above; pos and vel (n_sites x 3, engine order) receive their
- * positions and velocities (either may be NULL). */
+ * positions and velocities (either may be NULL; velocities of a domain that
+ * binds no velocity arrays are left as the caller's buffer holds them). */
 int sesp_cmn_map_from_domains(const sesp_cmn_domain *doms, const int n_cells[3], sesp_cmn_map **out,
                               int *n_water, int *n_surf, double *pos, double *vel);
 int sesp_cmn_map_destroy(sesp_cmn_map *m);
@@ -132,7 +133,9 @@ int sesp_cmn_assign(sesp_cmn_map *m, const double *pos);
  * cells 0) */
 int sesp_cmn_scatter(const sesp_cmn_map *m, sesp_cmn_domain *doms, const double *pos, const double *vel,
                      const double *acc, const double *force);
-/* read the arrays asked for (any may be NULL) from the assigned slots */
+/* read the arrays asked for (any may be NULL) from the assigned slots; a
+ * molecule whose domain does not bind an array (NULL pointer) leaves that
+ * output as it was */
 int sesp_cmn_gather(const sesp_cmn_map *m, const sesp_cmn_domain *doms, double *pos, double *vel, double *acc);
 /* where engine molecule `mol` sits: out = {domain, class, central cell, slot} */
 int sesp_cmn_slot(const sesp_cmn_map *m, int mol, int out[4]);
@@ -152,7 +155,8 @@ sesp_ctx *sesp_cmn_context(void);
 /* the attached job's map (NULL when none) */
 const sesp_cmn_map *sesp_cmn_current_map(void);
 /* positions, velocities and accelerations read back from the COMMON
- * arrays into the engine (after the driver changed them) */
+ * arrays into the engine (after the driver changed them); arrays the
+ * domains do not bind keep the engine's values */
 int sesp_cmn_reload(void);
 /* first failure of a gfortran-named subroutine since attach (0 = none) */
 int sesp_cmn_status(void);

@@ -127,16 +127,13 @@ void copy_out(const sesp_cmn_map &m, sesp_cmn_domain *doms, const double *src, i
     }
 }
 
+// (a molecule whose domain does not bind this array keeps what dst holds)
 void copy_in(const sesp_cmn_map &m, const sesp_cmn_domain *doms, double *dst, int kind) {
     for (int mol = 0; mol < m.nw + m.ns; mol++) {
         double *const *arr;
         int col, ld;
         int n = sites_in(m, mol), s0 = site_of(m, mol);
-        if (!locate(doms[m.dom[mol]], m.cls[mol], m.cell[mol], kind, &arr, &col, &ld)) {
-            for (int t = 0; t < n; t++)
-                for (int a = 0; a < 3; a++) dst[3 * (s0 + t) + a] = 0.0;
-            continue;
-        }
+        if (!locate(doms[m.dom[mol]], m.cls[mol], m.cell[mol], kind, &arr, &col, &ld)) continue;
         size_t base = (size_t)col * ld + (size_t)m.slot[mol] * n;
         for (int t = 0; t < n; t++)
             for (int a = 0; a < 3; a++) dst[3 * (s0 + t) + a] = arr[a][base + t];
@@ -457,6 +454,9 @@ const sesp_cmn_map *sesp_cmn_current_map(void) { return g_job.map; }
 int sesp_cmn_reload(void) {
     int rc = need_job();
     if (rc) return rc;
+    // start from the engine's state, so arrays the domains do not bind keep it
+    if ((rc = sesp_download_state(g_job.ctx, g_job.pos.data(), g_job.vel.data(), g_job.acc.data())))
+        return engine_fail(rc, "download");
     sesp_cmn_gather(g_job.map, g_job.doms, g_job.pos.data(), g_job.vel.data(), g_job.acc.data());
     double eta;
     if ((rc = sesp_get_eta(g_job.ctx, &eta))) return engine_fail(rc, "sesp_get_eta");
