@@ -453,6 +453,24 @@ int main(int argc, char **argv) {
         }
         printf("molecules that changed domain, class or cell: %d\n", moved);
     }
+    /* sesp_cmn_reload: a velocity rescale done in the COMMON arrays reaches
+     * the engine; positions and accelerations stay the engine's */
+    {
+        double *vh = alloc_d(3 * (size_t)nsite), *p2 = alloc_d(3 * (size_t)nsite), *v2 = alloc_d(3 * (size_t)nsite),
+               *a2 = alloc_d(3 * (size_t)nsite);
+        for (int i = 0; i < 3 * nsite; i++) vh[i] = 0.5 * vd[i];
+        CHECK(sesp_cmn_scatter(map, doms, NULL, vh, NULL, NULL) == 0, "scatter halved velocities");
+        sesp_cmn_reload_(&my3d);
+        CHECK(sesp_cmn_status() == 0, "reload status %d", sesp_cmn_status());
+        CHECK(sesp_download_state(sesp_cmn_context(), p2, v2, a2) == 0, "download after reload");
+        CHECK(memcmp(v2, vh, 24 * (size_t)nsite) == 0, "reloaded velocities");
+        CHECK(memcmp(p2, pd, 24 * (size_t)nsite) == 0, "positions kept");
+        CHECK(memcmp(a2, ad, 24 * (size_t)nsite) == 0, "accelerations kept");
+        /* put the run's velocities back for the output below */
+        CHECK(sesp_cmn_scatter(map, doms, NULL, vd, NULL, NULL) == 0, "scatter velocities");
+        sesp_cmn_reload_(&my3d);
+        free(vh); free(p2); free(v2); free(a2);
+    }
     if (argc > 3) {
         FILE *fo = fopen(argv[3], "wb");
         fwrite(f0, 8, 3 * (size_t)nsite, fo);
