@@ -44,3 +44,22 @@ def test_batch_trajectory_equal_alone(systems):
         assert np.array_equal(pb[sl], pa)
         assert np.array_equal(vb[sl], va)
         assert etas[q] == alone.eta
+
+
+def test_per_replica_eta_and_failures(systems):
+    """sesp_set_eta_batch sets each replica's thermostat variable (and
+    sesp_set_state gives all replicas the same one); sesp_failures_batch
+    splits the SHAKE / RATTLE failure count by replica."""
+    batch = E.Engine(systems, E.MIXED)
+    batch.force(True)
+    batch.init_accel()
+    batch.set_etas([0.5, -0.25, 0.125])
+    assert list(batch.etas()) == [0.5, -0.25, 0.125]
+    batch.set_state(None, None, None, 0.75)
+    assert list(batch.etas()) == [0.75, 0.75, 0.75]
+    with pytest.raises(ValueError):
+        batch.set_etas([0.0, 0.0])
+    batch.set_etas([0.0, 0.0, 0.0])
+    batch.run(99101, 10)
+    f = batch.failures()
+    assert f.shape == (3,) and f.sum() == batch.counters()[0] == 0
