@@ -52,6 +52,10 @@ struct Fast32 {
     double hfa64_w[3], hfa64_s[NBOND];     // 1 / (2 (1/m_i + 1/m_j))
     double mass64[NTYPE], rm64[NTYPE], rmdt64[NTYPE];
     double dt2m64[NTYPE];                  // dt^2 / (2 m)
+    // the FP32 steering terms of the water matrix kernels, rounded once
+    // here instead of in every water (GB300 converts at its FP64 rate)
+    float rm32_w[2];                       // (float) rm64 of O and H
+    float wk32[3][3];                      // (float) K_bc of the water triangle
 };
 __constant__ Fast32 cF;
 
@@ -217,9 +221,9 @@ __device__ __forceinline__ bool rattle_bond(const Dev &d, int gi, int gj, int ki
 // ---------------------------------------------------------------- waters
 
 // bonds (0,1), (1,2), (2,0); kinds 0 (O), 1 (H)
-__device__ constexpr int wbi(int b) { return b; }
-__device__ constexpr int wbj(int b) { return b == 2 ? 0 : b + 1; }
-__device__ constexpr int wkind(int i) { return i == 0 ? 0 : 1; }
+__host__ __device__ constexpr int wbi(int b) { return b; }
+__host__ __device__ constexpr int wbj(int b) { return b == 2 ? 0 : b + 1; }
+__host__ __device__ constexpr int wkind(int i) { return i == 0 ? 0 : 1; }
 
 // SHAKE half of one water (one thread); returns the sweeps it ran
 template <typename C>
@@ -359,11 +363,11 @@ __device__ __forceinline__ int water_b(const Dev &d, int m, double tol, int maxi
 
 // K_bc of the water triangle (bond b joins sites b and b + 1 mod 3): the
 // sum of the inverse masses on the diagonal, minus the inverse mass of the
-// shared site off it
-__device__ __forceinline__ double wk(int b, int c) {
-    if (b == c) return cF.rm64[wkind(wbi(b))] + cF.rm64[wkind(wbj(b))];
+// shared site off it (FP64; rounded to FP32 once, into cF.wk32)
+inline double wk_host(const double *rm, int b, int c) {
+    if (b == c) return rm[wkind(wbi(b))] + rm[wkind(wbj(b))];
     const int shared = (wbi(b) == wbi(c) || wbi(b) == wbj(c)) ? wbi(b) : wbj(b);
-    return -cF.rm64[wkind(shared)];
+    return -rm[wkind(shared)];
 }
 // s_kb: +1 if site k is bond b's first site, -1 if its second, else 0
 __device__ __forceinline__ double wsgn(int k, int b) { return k == wbi(b) ? 1.0 : (k == wbj(b) ? -1.0 : 0.0); }
@@ -389,7 +393,7 @@ __device__ __forceinline__ void inv3f(const float (&A)[3][3], float (&B)[3][3]) 
 __device__ __forceinline__ void water_move32(const float (&R)[3][3], const float (&h)[3], float (&c)[3][3]) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        const float rm = (float)cF.rm64[wkind(k)];
+        const float rm = cF.rm32_w[wkind(k)];
 #pragma unroll
         for (int b = 0; b < 3; b++) {
             const float w = (float)wsgn(k, b) * rm * h[b];
@@ -449,12 +453,14 @@ __device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int 
     for (int b = 0; b < 3; b++)
 #pragma unroll
         for (int c = 0; c < 3; c++)
-            J[b][c] = -2.f * (float)wk(b, c) * (P32[b][0] * R32[c][0] + P32[b][1] * R32[c][1] + P32[b][2] * R32[c][2]);
+            J[b][c] = -2.f * cF.wk32[b][c] * (P32[b][0] * R32[c][0] + P32[b][1] * R32[c][1] + P32[b][2] * R32[c][2]);
     inv3f(J, Ji);
     // FP32 steps on the corrections until the FP32 residual is inside the
     // tolerance (its rounding, ~1e-9 of d^2 ~ 0.1, is about the tolerance
     // band itself, so these only bring the corrections near the answer)
     float c32[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+    const float D0f[3] = {(float)D0[0], (float)D0[1], (float)D0[2]};
+    const float thrf[3] = {(float)thr[0], (float)thr[1], (float)thr[2]};
     int it = 0;
     for (int k32 = 0; k32 < WMAT_FP32_STEPS && it <= maxit; k32++) {
         float f[3];
@@ -468,8 +474,8 @@ __device__ __forceinline__ int water_a_mat(const Dev &d, int m, double tol, int 
                 const float cd = c32[i][a] - c32[j][a];
                 q += cd * (cd + 2.f * P32[b][a]);
             }
-            f[b] = (float)D0[b] - q;
-            in = in && !(fabsf(f[b]) > (float)thr[b]);
+            f[b] = D0f[b] - q;
+            in = in && !(fabsf(f[b]) > thrf[b]);
         }
         if (in) break;
         water_step32(Ji, R32, f, c32);
@@ -556,7 +562,7 @@ __device__ __forceinline__ int water_b_mat(const Dev &d, int m, double tol, int 
     for (int b = 0; b < 3; b++)
 #pragma unroll
         for (int c = 0; c < 3; c++)
-            A[b][c] = (float)wk(b, c) * (R32[b][0] * R32[c][0] + R32[b][1] * R32[c][1] + R32[b][2] * R32[c][2]);
+            A[b][c] = cF.wk32[b][c] * (R32[b][0] * R32[c][0] + R32[b][1] * R32[c][1] + R32[b][2] * R32[c][2]);
     inv3f(A, Ai);
     int it = 0;
     bool done = false;
@@ -1142,6 +1148,9 @@ bool upload_tables_fast(const Tables &t, cudaStream_t st) {
         f.rmdt64[k] = DT / t.mass[k];
         f.dt2m64[k] = DTSQ2 / t.mass[k];
     }
+    for (int k = 0; k < 2; k++) f.rm32_w[k] = (float)f.rm64[k];
+    for (int b = 0; b < 3; b++)
+        for (int c = 0; c < 3; c++) f.wk32[b][c] = (float)wk_host(f.rm64, b, c);
     for (int b = 0; b < 3; b++) {
         const int ki = b == 0 ? 0 : 1, kj = b == 2 ? 0 : 1;
         const double rs = 1.0 / t.mass[ki] + 1.0 / t.mass[kj];

@@ -1440,6 +1440,18 @@ __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const
     __syncthreads();
     const M2LTerm<R> *tm = sterm[o < LPH ? o : LPH - 1];
     const int nb = n[0] * n[1] * n[2];
+    // a half-warp's current source, rounded to R once by its 16 lanes and
+    // read back as broadcasts (the 15 outputs each converting all 25 FP64
+    // components kept GB300's FP64 pipe, which converts, busy 97% of cycles)
+    __shared__ C2<R> ssrc[16][LP];
+    const unsigned hmask = 0xFFFFu << (16 * (hw & 1));   // the half-warp's lanes (its trip count is its own)
+    auto source = [&](int s) -> const C2<R> * {
+        const double2 *src = d.O2 + (size_t)(r.l2_0 + s) * LP;
+        __syncwarp(hmask);   // the previous source's reads are done
+        for (int q = o; q < LP; q += 16) ssrc[hw][q] = {(R)src[q].x, (R)src[q].y};
+        __syncwarp(hmask);
+        return ssrc[hw];
+    };
     R re = 0, im = 0;
     if (r.per) {
         // the image-summed factors of the replica: one pass over the box's sources
@@ -1448,7 +1460,7 @@ __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const
         for (int s = hw; s < nb; s += 16) {
             const int sx = s % n[0], sy = (s / n[0]) % n[1], sz = s / (n[0] * n[1]);
             const int oi = (sx - t[0] + n[0] - 1) + wx * ((sy - t[1] + n[1] - 1) + wy * (sz - t[2] + n[2] - 1));
-            m2l_acc_s<R>(Hr + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, tm, re, im);
+            m2l_acc_s<R>(Hr + (size_t)oi * NH, source(s), tm, re, im);
         }
     } else {
         const int wx = 2 * d2.x + 1, wy = 2 * d2.y + 1;
@@ -1457,7 +1469,7 @@ __global__ void __launch_bounds__(256) k_m2l_all(Dev d, const C2<R> *Htab, const
             const int dx = sx - t[0], dy = sy - t[1], dz = sz - t[2];
             if (abs(dx) <= 1 && abs(dy) <= 1 && abs(dz) <= 1) continue;
             const int oi = (dx + d2.x) + wx * ((dy + d2.y) + wy * (dz + d2.z));
-            m2l_acc_s<R>(Htab + (size_t)oi * NH, d.O2 + (size_t)(r.l2_0 + s) * LP, tm, re, im);
+            m2l_acc_s<R>(Htab + (size_t)oi * NH, source(s), tm, re, im);
         }
     }
     if (o < LPH) { sre[hw][o] = re; sim[hw][o] = im; }
