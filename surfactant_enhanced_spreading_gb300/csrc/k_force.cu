@@ -1625,6 +1625,13 @@ __global__ void k_graphite_list(Dev d, int nsite) {
 // the visited carbons of all groups and a fixed shuffle tree sums them.
 // FP32 (mixed path): site and carbons relative to the column centre, so each
 // carbon costs FP32 arithmetic only.
+// A warp takes a run of up to 32 consecutive listed sites (the list split
+// evenly over the warps): lane j does the FP64 set-up of the run's site j
+// (column, position, parameters) and, at the end, its FP64 force update, so
+// those run once per run instead of once per site on every lane (GB300
+// issues FP64 and its conversions at 1/64 of the FP32 rate, whatever the
+// active lanes); in between the warp walks the run's sites with their set-up
+// broadcast.
 template <typename R>
 __global__ void k_graphite(Dev d) {
     const int lane = threadIdx.x & 31;
@@ -1633,78 +1640,108 @@ __global__ void k_graphite(Dev d) {
     const int n = *d.gcount;
     const R rc2 = (R)(RC * RC);
     const float reach = (float)RC + 1e-3f;
-    for (int k = warp; k < n; k += nwarp) {
-        int g = d.gsite[k];
-        const Rep r = d.rep[d.mrep[d.smol[g]]];
-        const float gymax = r.gymax, bin_scale = GBIN / (2.f * gymax);
-        double eps, sg6;
-        const int col = graphite_column(d, r, g, eps, sg6);
-        double xd, yd, zd;
-        site_pos(d, r, g, xd, yd, zd);
-        const int lc = col - r.gcol0, ix = lc % r.nc[0], iy = lc / r.nc[0];
-        const float xs = (float)(xd - cell_centre(d, r, 0, ix)), ys = (float)(yd - cell_centre(d, r, 1, iy)),
-                    zs = (float)(zd - cell_centre(d, r, 2, 0));
-        int s0 = 0, len = 0;
-        if (lane < GGRP) {
-            const size_t gi = (size_t)col * GGRP + lane;
-            const float2 zr = d.ggrp_z[gi];
-            const float dz = fmaxf(fmaxf(zr.x - zs, zs - zr.y), 0.f);
-            if (zr.x <= zr.y && dz < reach) {
-                const float w = sqrtf(fmaxf(reach * reach - dz * dz, 0.f)) + 1e-3f;
-                const int b0 = min(max((int)floorf((ys - w + gymax) * bin_scale), 0), GBIN);
-                const int b1 = min(max((int)floorf((ys + w + gymax) * bin_scale) + 1, 0), GBIN);
-                const int *bins = d.gbin + gi * (GBIN + 1);
-                s0 = bins[b0];
-                len = bins[b1] - s0;
+    const int run = min(32, (n + nwarp - 1) / nwarp);
+    for (int k0 = warp * run; k0 < n; k0 += nwarp * run) {
+        // lane set-up of site k0 + lane
+        const bool mine = lane < run && k0 + lane < n;
+        int my_g = 0, my_col = 0;
+        float my_gymax = 1.f, my_xs = 0.f, my_ys = 0.f, my_zs = 0.f;
+        R my_e48 = 0, my_s6 = 0;
+        double my_xd = 0.0, my_yd = 0.0, my_zd = 0.0;
+        if (mine) {
+            my_g = d.gsite[k0 + lane];
+            const Rep r = d.rep[d.mrep[d.smol[my_g]]];
+            my_gymax = r.gymax;
+            double eps, sg6;
+            my_col = graphite_column(d, r, my_g, eps, sg6);
+            site_pos(d, r, my_g, my_xd, my_yd, my_zd);
+            const int lc = my_col - r.gcol0, ix = lc % r.nc[0], iy = lc / r.nc[0];
+            my_xs = (float)(my_xd - cell_centre(d, r, 0, ix));
+            my_ys = (float)(my_yd - cell_centre(d, r, 1, iy));
+            my_zs = (float)(my_zd - cell_centre(d, r, 2, 0));
+            my_e48 = (R)(48.0 * eps * sg6);
+            my_s6 = (R)sg6;
+        }
+        const int cnt = min(run, n - k0);
+        R my_fx = 0, my_fy = 0, my_fz = 0;
+        for (int j = 0; j < cnt; j++) {
+            const int col = __shfl_sync(0xffffffffu, my_col, j);
+            const float gymax = __shfl_sync(0xffffffffu, my_gymax, j), bin_scale = GBIN / (2.f * gymax);
+            const float xs = __shfl_sync(0xffffffffu, my_xs, j), ys = __shfl_sync(0xffffffffu, my_ys, j),
+                        zs = __shfl_sync(0xffffffffu, my_zs, j);
+            const R e48 = __shfl_sync(0xffffffffu, my_e48, j), s6 = __shfl_sync(0xffffffffu, my_s6, j);
+            double xd = 0.0, yd = 0.0, zd = 0.0;
+            if constexpr (!std::is_same<R, float>::value) {
+                xd = __shfl_sync(0xffffffffu, my_xd, j);
+                yd = __shfl_sync(0xffffffffu, my_yd, j);
+                zd = __shfl_sync(0xffffffffu, my_zd, j);
             }
-        }
-        int incl = len;   // inclusive prefix over the group lanes
-        for (int o = 1; o < GGRP; o <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        int st[GGRP], pe[GGRP];
-#pragma unroll
-        for (int q = 0; q < GGRP; q++) {
-            st[q] = __shfl_sync(0xffffffffu, s0, q);
-            pe[q] = __shfl_sync(0xffffffffu, incl, q);
-        }
-        const int total = pe[GGRP - 1];
-        R e48 = (R)(48.0 * eps * sg6), s6 = (R)sg6;
-        R fx = 0, fy = 0, fz = 0;
-        for (int t = lane; t < total; t += 32) {
-            int q = st[0] + t;
-#pragma unroll
-            for (int u = 1; u < GGRP; u++)
-                if (t >= pe[u - 1]) q = st[u] + t - pe[u - 1];
-            if constexpr (std::is_same<R, float>::value) {
-                const float4 c = d.gpos32[q];
-                const float xij = xs - c.x, yij = ys - c.y, zij = zs - c.z;
-                const float r2 = xij * xij + yij * yij + zij * zij;
-                if (r2 <= rc2) {
-                    const float rsi = __fdividef(1.f, r2), r6 = rsi * rsi * rsi;
-                    const float flj = e48 * r6 * (s6 * r6 - 0.5f) * rsi;
-                    fx += xij * flj; fy += yij * flj; fz += zij * flj;
-                }
-            } else {
-                const double4 c = d.gpos[q];
-                R xij = (R)(xd - c.x), yij = (R)(yd - c.y), zij = (R)(zd - c.z);
-                R r2 = xij * xij + yij * yij + zij * zij;
-                if (r2 <= rc2) {
-                    R rsi = R(1) / r2, r6 = rsi * rsi * rsi;
-                    R flj = e48 * r6 * (s6 * r6 - R(0.5)) * rsi;
-                    fx += xij * flj; fy += yij * flj; fz += zij * flj;
+            int s0 = 0, len = 0;
+            if (lane < GGRP) {
+                const size_t gi = (size_t)col * GGRP + lane;
+                const float2 zr = d.ggrp_z[gi];
+                const float dz = fmaxf(fmaxf(zr.x - zs, zs - zr.y), 0.f);
+                if (zr.x <= zr.y && dz < reach) {
+                    const float w = sqrtf(fmaxf(reach * reach - dz * dz, 0.f)) + 1e-3f;
+                    const int b0 = min(max((int)floorf((ys - w + gymax) * bin_scale), 0), GBIN);
+                    const int b1 = min(max((int)floorf((ys + w + gymax) * bin_scale) + 1, 0), GBIN);
+                    const int *bins = d.gbin + gi * (GBIN + 1);
+                    s0 = bins[b0];
+                    len = bins[b1] - s0;
                 }
             }
+            int incl = len;   // inclusive prefix over the group lanes
+            for (int o = 1; o < GGRP; o <<= 1) {
+                const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            int st[GGRP], pe[GGRP];
+#pragma unroll
+            for (int q = 0; q < GGRP; q++) {
+                st[q] = __shfl_sync(0xffffffffu, s0, q);
+                pe[q] = __shfl_sync(0xffffffffu, incl, q);
+            }
+            const int total = pe[GGRP - 1];
+            R fx = 0, fy = 0, fz = 0;
+            for (int t = lane; t < total; t += 32) {
+                int q = st[0] + t;
+#pragma unroll
+                for (int u = 1; u < GGRP; u++)
+                    if (t >= pe[u - 1]) q = st[u] + t - pe[u - 1];
+                if constexpr (std::is_same<R, float>::value) {
+                    const float4 c = d.gpos32[q];
+                    const float xij = xs - c.x, yij = ys - c.y, zij = zs - c.z;
+                    const float r2 = xij * xij + yij * yij + zij * zij;
+                    if (r2 <= rc2) {
+                        const float rsi = __fdividef(1.f, r2), r6 = rsi * rsi * rsi;
+                        const float flj = e48 * r6 * (s6 * r6 - 0.5f) * rsi;
+                        fx += xij * flj; fy += yij * flj; fz += zij * flj;
+                    }
+                } else {
+                    const double4 c = d.gpos[q];
+                    R xij = (R)(xd - c.x), yij = (R)(yd - c.y), zij = (R)(zd - c.z);
+                    R r2 = xij * xij + yij * yij + zij * zij;
+                    if (r2 <= rc2) {
+                        R rsi = R(1) / r2, r6 = rsi * rsi * rsi;
+                        R flj = e48 * r6 * (s6 * r6 - R(0.5)) * rsi;
+                        fx += xij * flj; fy += yij * flj; fz += zij * flj;
+                    }
+                }
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                fx += __shfl_down_sync(0xffffffffu, fx, off);
+                fy += __shfl_down_sync(0xffffffffu, fy, off);
+                fz += __shfl_down_sync(0xffffffffu, fz, off);
+            }
+            // lane 0 holds the sums; lane j keeps them for its update
+            fx = __shfl_sync(0xffffffffu, fx, 0);
+            fy = __shfl_sync(0xffffffffu, fy, 0);
+            fz = __shfl_sync(0xffffffffu, fz, 0);
+            if (lane == j) { my_fx = fx; my_fy = fy; my_fz = fz; }
         }
-        for (int off = 16; off > 0; off >>= 1) {
-            fx += __shfl_down_sync(0xffffffffu, fx, off);
-            fy += __shfl_down_sync(0xffffffffu, fy, off);
-            fz += __shfl_down_sync(0xffffffffu, fz, off);
-        }
-        if (lane == 0) {
-            const size_t n = d.nsite;
-            d.fside[g] += (double)fx; d.fside[n + g] += (double)fy; d.fside[2 * n + g] += (double)fz;
+        if (mine) {
+            const size_t ns = d.nsite;
+            d.fside[my_g] += (double)my_fx; d.fside[ns + my_g] += (double)my_fy; d.fside[2 * ns + my_g] += (double)my_fz;
         }
     }
 }
