@@ -60,47 +60,15 @@ __device__ inline int block_exscan(int v, int *total) {
     return res;
 }
 
-// Single-block exclusive scans: each thread takes a contiguous run of the
-// counts and reads it SCAN_U values at a time with independent loads, all
-// in flight together (one dependent load per value made the scan of 25,600
-// cells latency-bound).
-constexpr int SCAN_U = 16;
-__device__ inline int run_sum(const int *a, int b, int e) {
-    int s = 0;
-    for (int c0 = b; c0 < e; c0 += SCAN_U) {
-        int v[SCAN_U];
-#pragma unroll
-        for (int u = 0; u < SCAN_U; u++) v[u] = c0 + u < e ? a[c0 + u] : 0;
-#pragma unroll
-        for (int u = 0; u < SCAN_U; u++) s += v[u];
-    }
-    return s;
-}
-// out[c] = acc + the counts before c in the run (out may be a itself);
-// zero, if given, is cleared over the run
-__device__ inline void run_write(const int *a, int *out, int *zero, int b, int e, int acc) {
-    for (int c0 = b; c0 < e; c0 += SCAN_U) {
-        int v[SCAN_U];
-#pragma unroll
-        for (int u = 0; u < SCAN_U; u++) v[u] = c0 + u < e ? a[c0 + u] : 0;
-#pragma unroll
-        for (int u = 0; u < SCAN_U; u++)
-            if (c0 + u < e) {
-                out[c0 + u] = acc;
-                acc += v[u];
-                if (zero) zero[c0 + u] = 0;
-            }
-    }
-}
-
 __global__ void k_scan(Dev d, int ncell) {
     int per = (ncell + blockDim.x - 1) / blockDim.x;
-    int b = min(ncell, (int)threadIdx.x * per), e = min(ncell, b + per);
-    const int s = run_sum(d.ccount, b, e);
+    int b = threadIdx.x * per, e = min(ncell, b + per);
+    int s = 0;
+    for (int c = b; c < e; c++) s += d.ccount[c];
     int total;
-    const int acc = block_exscan(s, &total);
+    int acc = block_exscan(s, &total);
     if (threadIdx.x == 0) d.cstart[ncell] = total;
-    run_write(d.ccount, d.cstart, d.cfill, b, e, acc);
+    for (int c = b; c < e; c++) { d.cstart[c] = acc; acc += d.ccount[c]; d.cfill[c] = 0; }
 }
 
 __global__ void k_scatter(Dev d, int nsite) {
@@ -376,12 +344,13 @@ __global__ void k_near_items_count(Dev d, int ncell, int tile) {
 // exclusive scan of the item counts in place (one block), total to near_ctl[1]
 __global__ void k_near_items_scan(Dev d, int ncell) {
     const int per = (ncell + blockDim.x - 1) / blockDim.x;
-    const int b = min(ncell, (int)threadIdx.x * per), e = min(ncell, b + per);
-    const int s = run_sum(d.near_icount, b, e);
+    const int b = threadIdx.x * per, e = min(ncell, b + per);
+    int s = 0;
+    for (int c = b; c < e; c++) s += d.near_icount[c];
     int total;
-    const int acc = block_exscan(s, &total);
+    int acc = block_exscan(s, &total);
     if (threadIdx.x == 0) d.near_ctl[1] = total;
-    run_write(d.near_icount, d.near_icount, nullptr, b, e, acc);
+    for (int c = b; c < e; c++) { int v = d.near_icount[c]; d.near_icount[c] = acc; acc += v; }
 }
 
 // the work items of one cell, counted per cost class in the block's histogram
