@@ -224,15 +224,27 @@ __device__ inline Cx<R> cadd(Cx<R> a, Cx<R> b) { return {a.re + b.re, a.im + b.i
 template <typename R>
 __device__ inline Cx<R> csub(Cx<R> a, Cx<R> b) { return {a.re - b.re, a.im - b.im}; }
 
-// gradient of Phi = sum_n sum_m w_m rfctr(n,m) Re(L_n^m T_n^m) (w_0 = 1, w_m = 2):
-// the potential of the local expansion L (25 coefficients, m >= 0 used)
+// rfctr(n, m) of coefficient ic in the arithmetic's type (the FP32 copy is
+// rounded once on the host: GB300 converts at its FP64 rate)
 template <typename R>
-__device__ inline void local_grad(const R *Lre, const R *Lim, R x, R y, R z, R &gx, R &gy, R &gz, R *phi) {
+__device__ __forceinline__ R rfctr_r(int ic) {
+    if constexpr (std::is_same<R, float>::value) return cT.rfctr32[ic];
+    else return cT.rfctr[ic];
+}
+
+// gradient of Phi = sum_n sum_m w_m rfctr(n,m) Re(L_n^m T_n^m) (w_0 = 1, w_m = 2):
+// the potential of the local expansion L (25 coefficients, m >= 0 used),
+// read as L(ic, re, im).  Both loops unroll, so every coefficient index is a
+// constant: the expansion is read straight from its row (no per-thread copy
+// in local memory).
+template <typename R, typename LF>
+__device__ inline void local_grad(const LF &L, R x, R y, R z, R &gx, R &gy, R &gz, R *phi) {
     R r2 = x * x + y * y + z * z;
     Cx<R> Tmm = {R(1), R(0)};
     Cx<R> dmm[3] = {{R(0), R(0)}, {R(0), R(0)}, {R(0), R(0)}};
     R ax = 0, ay = 0, az = 0, pp = 0;
     Cx<R> xy = {x, y};
+#pragma unroll
     for (int m = 0; m <= P; m++) {
         if (m > 0) {
             R f = -(R)(2 * m - 1);
@@ -245,6 +257,7 @@ __device__ inline void local_grad(const R *Lre, const R *Lim, R x, R y, R z, R &
         Cx<R> T2 = Tmm, T1 = {R(0), R(0)};
         Cx<R> d2[3] = {dmm[0], dmm[1], dmm[2]};
         Cx<R> d1[3] = {{R(0), R(0)}, {R(0), R(0)}, {R(0), R(0)}};
+#pragma unroll
         for (int n = m; n <= P; n++) {
             Cx<R> Tn;
             Cx<R> dn[3];
@@ -264,8 +277,9 @@ __device__ inline void local_grad(const R *Lre, const R *Lim, R x, R y, R z, R &
                 dn[2] = cscale(csub(cadd(cscale(T1, a), cscale(d1[2], a * z)), cadd(cscale(T2, b * 2 * z), cscale(d2[2], b * r2))), inv);
             }
             int ic = n * (n + 1) + m;
-            R w = (m == 0 ? R(1) : R(2)) * (R)cT.rfctr[ic];
-            R lr = Lre[ic], li = Lim[ic];
+            R w = (m == 0 ? R(1) : R(2)) * rfctr_r<R>(ic);
+            R lr, li;
+            L(ic, lr, li);
             ax += w * (lr * dn[0].re - li * dn[0].im);
             ay += w * (lr * dn[1].re - li * dn[1].im);
             az += w * (lr * dn[2].re - li * dn[2].im);
@@ -938,21 +952,21 @@ __global__ void k_near_finish(Dev d, int nslot, int ncell, int terms) {
         if constexpr (COMP) { fx = __fsub_rn(fx, ex); fy = __fsub_rn(fy, ey); fz = __fsub_rn(fz, ez); }
     }
     if (terms & SESP_T_FAR) {
-        R Lre[LP], Lim[LP], x, y, z, q;
-        if constexpr (MIXED) {   // the FP32 copy of L4 and the cell-relative FP32 position: no FP64 work
-            const float2 *L = d.L4f + (size_t)c * LP;
-            for (int k = 0; k < LP; k++) { const float2 v = L[k]; Lre[k] = v.x; Lim[k] = v.y; }
+        R x, y, z, q;
+        // the cell's local expansion: the FP32 copy of L4 on the mixed path
+        typedef typename std::conditional<MIXED, float2, double2>::type R2;
+        const R2 *Lc = (MIXED ? (const R2 *)d.L4f : (const R2 *)d.L4) + (size_t)c * LP;
+        auto L = [&](int k, R &re, R &im) { const R2 v = Lc[k]; re = v.x; im = v.y; };
+        if constexpr (MIXED) {   // the cell-relative FP32 position: no FP64 work
             const float4 p = d.srt_pos32[s];
             x = p.x; y = p.y; z = p.z; q = p.w * (float)XPI;
         } else {
-            const double2 *L = d.L4 + (size_t)c * LP;
-            for (int k = 0; k < LP; k++) { const double2 v = L[k]; Lre[k] = v.x; Lim[k] = v.y; }
             const double4 pd = d.srt_pos[s];
             x = pd.x - cell_centre(d, r, 0, ix); y = pd.y - cell_centre(d, r, 1, iy); z = pd.z - cell_centre(d, r, 2, iz);
             q = pd.w * XPI;
         }
         R gx, gy, gz;
-        local_grad<R>(Lre, Lim, x, y, z, gx, gy, gz, nullptr);
+        local_grad<R>(L, x, y, z, gx, gy, gz, nullptr);
         fx -= q * gx; fy -= q * gy; fz -= q * gz;
     }
     d.nf[3 * (size_t)s] = (double)fx; d.nf[3 * (size_t)s + 1] = (double)fy; d.nf[3 * (size_t)s + 2] = (double)fz;
@@ -1037,7 +1051,7 @@ __global__ void k_p2m(Dev d) {
                 if (nn > m) T2 = T1;
                 T1 = Tn;
                 int ic = nn * (nn + 1) + m;
-                R w = q * (R)cT.rfctr[ic];
+                R w = q * rfctr_r<R>(ic);
                 // ordering index among m >= 0 coefficients: o(n,m) = n(n+1)/2 + m
                 int oi = nn * (nn + 1) / 2 + m;
                 acc[2 * oi] += w * Tn.re;
@@ -2248,7 +2262,8 @@ __global__ void k_energy_slot(Dev d, double *e_slot) {
                     }
                 }
         double gx, gy, gz, phi;
-        local_grad<double>(Lre, Lim, pi.x - cx, pi.y - cy, pi.z - cz, gx, gy, gz, &phi);
+        auto L = [&](int k, double &re, double &im) { re = Lre[k]; im = Lim[k]; };
+        local_grad<double>(L, pi.x - cx, pi.y - cy, pi.z - cz, gx, gy, gz, &phi);
         e_slot[3 * (size_t)(s0 + i)] = ec;
         e_slot[3 * (size_t)(s0 + i) + 1] = el;
         e_slot[3 * (size_t)(s0 + i) + 2] = 0.5 * pi.w * XPI * phi;

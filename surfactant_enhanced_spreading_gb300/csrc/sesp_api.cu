@@ -142,6 +142,7 @@ Tables make_tables() {
     T.epcw = 392.0 / epsilon;
     for (int n = 0; n <= P; n++)
         for (int m = -n; m <= n; m++) T.rfctr[n * (n + 1) + m] = sqrt(fact(n - abs(m)) / fact(n + abs(m)));
+    for (int k = 0; k < LP; k++) T.rfctr32[k] = (float)T.rfctr[k];
     return T;
 }
 

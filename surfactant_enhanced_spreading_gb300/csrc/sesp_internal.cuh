@@ -119,6 +119,7 @@ struct Tables {
     double sgcs6[NSURF], epcs[NSURF];   // carbon - surfactant site LJ
     double sgcw6, epcw;                 // carbon - water O LJ
     double rfctr[LP];                   // sqrt((n-|m|)!/(n+|m|)!) by coefficient
+    float rfctr32[LP];                  // the same rounded to FP32 (the FP32 multipole kernels)
 };
 
 // bonded terms of the configuration preset's chains (one table for every
