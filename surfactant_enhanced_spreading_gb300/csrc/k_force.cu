@@ -1586,38 +1586,78 @@ __device__ inline void site_pos(const Dev &d, const Rep &r, int g, double &x, do
 // wall) and the rest in FP32 (at most 91 sigma across: no overflow).
 __device__ inline float pow13f(float v) { float v2 = v * v, v4 = v2 * v2, v8 = v4 * v4; return v8 * v4 * v; }
 
-template <bool MIXED>
-__global__ void k_site_forces(Dev d, int nsite, int terms) {
-    griddep_wait();
-    int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nsite) return;
-    const Rep r = d.rep[d.mrep[d.smol[g]]];
-    double fx = 0.0, fy = 0.0, fz = 0.0;
-    int slot = d.sslot[g];
+// what one site's force assembly reads
+struct SiteIn {
+    int per;
+    double rhs0, rhs1, rhs2;
+    double nx, ny, nz;   // the pair-field force of its slot (0 without one)
+    double x, y, z;
+    double sx, sy, sz;   // the side forces
+};
+
+__device__ __forceinline__ void site_load(const Dev &d, int g, int terms, SiteIn &in) {
+    const Rep &r = d.rep[d.mrep[d.smol[g]]];
+    in.per = r.per;
+    in.rhs2 = r.rhs[2];
+    in.nx = in.ny = in.nz = 0.0;
+    const int slot = d.sslot[g];
     if ((terms & (SESP_T_NEAR | SESP_T_FAR)) && slot >= 0) {
-        fx = d.nf[3 * (size_t)slot]; fy = d.nf[3 * (size_t)slot + 1]; fz = d.nf[3 * (size_t)slot + 2];
+        in.nx = d.nf[3 * (size_t)slot]; in.ny = d.nf[3 * (size_t)slot + 1]; in.nz = d.nf[3 * (size_t)slot + 2];
     }
-    double x = d.x[g], y = d.y[g], z = d.z[g];
+    in.z = d.z[g];
+    // x and y enter only the side walls of a closed box (fewer registers
+    // held for the periodic preset)
+    in.x = in.y = in.rhs0 = in.rhs1 = 0.0;
+    if ((terms & SESP_T_WALL) && !in.per) { in.x = d.x[g]; in.y = d.y[g]; in.rhs0 = r.rhs[0]; in.rhs1 = r.rhs[1]; }
+    const size_t n = d.nsite;
+    in.sx = d.fside[g]; in.sy = d.fside[n + g]; in.sz = d.fside[2 * n + g];
+}
+
+template <bool MIXED>
+__device__ __forceinline__ void site_store(const Dev &d, int g, int terms, const SiteIn &in) {
+    double fx = in.nx, fy = in.ny, fz = in.nz;
+    const double x = in.x, y = in.y, z = in.z;
     if (terms & SESP_T_WALL) {   // the periodic preset has walls at the z faces only
         if constexpr (MIXED) {
-            if (!r.per) {
-                fx += (double)(48.f / pow13f((float)(x - r.rhs[0])) + 48.f / pow13f((float)(r.rhs[0] + x)));
-                fy += (double)(48.f / pow13f((float)(y - r.rhs[1])) + 48.f / pow13f((float)(r.rhs[1] + y)));
+            if (!in.per) {
+                fx += (double)(48.f / pow13f((float)(x - in.rhs0)) + 48.f / pow13f((float)(in.rhs0 + x)));
+                fy += (double)(48.f / pow13f((float)(y - in.rhs1)) + 48.f / pow13f((float)(in.rhs1 + y)));
             }
-            fz += (double)(48.f / pow13f((float)(z - r.rhs[2])) + 48.f / pow13f((float)(r.rhs[2] + z)));
+            fz += (double)(48.f / pow13f((float)(z - in.rhs2)) + 48.f / pow13f((float)(in.rhs2 + z)));
         } else {
-            if (!r.per) {
-                fx += 48.0 / pow13(x - r.rhs[0]); fx += 48.0 / pow13(r.rhs[0] + x);
-                fy += 48.0 / pow13(y - r.rhs[1]); fy += 48.0 / pow13(r.rhs[1] + y);
+            if (!in.per) {
+                fx += 48.0 / pow13(x - in.rhs0); fx += 48.0 / pow13(in.rhs0 + x);
+                fy += 48.0 / pow13(y - in.rhs1); fy += 48.0 / pow13(in.rhs1 + y);
             }
-            fz += 48.0 / pow13(z - r.rhs[2]); fz += 48.0 / pow13(r.rhs[2] + z);
+            fz += 48.0 / pow13(z - in.rhs2); fz += 48.0 / pow13(in.rhs2 + z);
         }
     }
     // the step's graphite and intramolecular forces, cleared for the next step
     const size_t n = d.nsite;
-    fx += d.fside[g]; fy += d.fside[n + g]; fz += d.fside[2 * n + g];
+    fx += in.sx; fy += in.sy; fz += in.sz;
     d.fside[g] = 0.0; d.fside[n + g] = 0.0; d.fside[2 * n + g] = 0.0;
     d.fx[g] = fx; d.fy[g] = fy; d.fz[g] = fz;
+}
+
+// Total site forces: the slot's pair-field force, walls, side forces.  A
+// thread takes SITE_PER sites (blockDim.x apart) and issues every load of
+// all of them before it sums and stores any.  The kernel is a chain of
+// dependent loads (site -> molecule -> replica, site -> slot -> force).  With
+// one site per thread, 312,000 sites took 1.34 waves of CTAs, and the second
+// wave waited out the whole chain again.  Two sites per thread (64 registers)
+// run the two chains side by side, in 1.003 waves.
+constexpr int SITE_PER = 2;
+template <bool MIXED>
+__global__ void k_site_forces(Dev d, int nsite, int terms) {
+    griddep_wait();
+    const int g0 = blockIdx.x * SITE_PER * blockDim.x + threadIdx.x;
+    SiteIn in[SITE_PER];
+#pragma unroll
+    for (int k = 0; k < SITE_PER; k++)
+        if (g0 + k * (int)blockDim.x < nsite) site_load(d, g0 + k * blockDim.x, terms, in[k]);
+#pragma unroll
+    for (int k = 0; k < SITE_PER; k++)
+        if (g0 + k * (int)blockDim.x < nsite) site_store<MIXED>(d, g0 + k * blockDim.x, terms, in[k]);
 }
 
 // sites the graphite acts on, listed at every rebuild (their cells are frozen
@@ -1766,7 +1806,7 @@ void launch_graphite_list(const Dev &d, int nsite, cudaStream_t st) {
 }
 
 void launch_site_forces(const Dev &d, int nsite, int terms, int mixed, cudaStream_t st) {
-    const dim3 g((nsite + 255) / 256), b(256);
+    const dim3 g((nsite + SITE_PER * 256 - 1) / (SITE_PER * 256)), b(256);
     if (mixed) launch_pdl(k_site_forces<true>, g, b, 0, st, d, nsite, terms);
     else launch_pdl(k_site_forces<false>, g, b, 0, st, d, nsite, terms);
 }
